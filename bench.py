@@ -1,0 +1,276 @@
+#!/usr/bin/env python
+"""Newton iterations per second of the OptCuts geometry step on one GB300.
+
+Workload (default): the lat-long ellipsoid, axes (1, 0.6, 0.4), 316 x 316
+grid with 8 random spherical-harmonic bumps (199,080 triangles, seed 2),
+one-point cut + Tutte embedding, lambda = 0.999, scaffold off (the reference
+runs its first Newton phase of a closed genus-0 mesh without the scaffold).
+A step is one Optimizer::solve(1): gradient, PSD-projected Hessian, block
+assembly, PCG direction, injective bound and line search.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the same
+workload (the Newton solve does not shard); value = iterations of all ranks
+divided by the slowest rank's time.  --impl reference times the CPU
+restatement of the reference path (oracle/port, the reference's own
+sources are not present on the GPU host) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton iter/s @200k tris"
+UNIT = "iter/s"
+PCG_BYTES_PER_TRI = 140.0   # algorithmic bytes per triangle per PCG iteration
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="ellipsoid_199k")
+    p.add_argument("--lam", type=float, default=0.999)
+    p.add_argument("--cpu-sample-iters", type=int, default=1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(n):
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(name):
+    from optcuts_gb300 import init as I
+    from optcuts_gb300 import meshes as M
+    V, F = M.CONFIGS[name]()
+    return I.init_uv(V, F)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_port_time(st, lam, iters, threads):
+    import oracle as O
+    _, tr, _ = O.newton(st.V_rest, st.F, st.fixedVert, st.UV, 1.0 - lam, iters, threads=threads)
+    return float(np.sum(tr["seconds"])), len(tr["seconds"])
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    st = workload(args.workload)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup if args.warmup < 1 else 0):
+        pass
+    secs, n = 0.0, 0
+    per = []
+    for _ in range(args.steps):
+        s, k = cpu_port_time(st, args.lam, args.cpu_sample_iters, threads)
+        secs += s
+        n += k
+        per.append(s / max(k, 1))
+    v = n / secs
+    sample = "%d x %d Newton iteration(s) of %s from the Tutte start" % (args.steps, args.cpu_sample_iters,
+                                                                          args.workload)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * secs / n, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "triangles": len(st.F), "lambda": args.lam, "scaffold": False},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args, rank, world):
+    import optcuts_gb300 as oc
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(device)
+    st = workload(args.workload)
+    nF, nV = len(st.F), len(st.UV)
+    ctx = oc.Context(device)
+    mesh = oc.TriMesh(st.V_rest, st.UV, st.F, st.fixedVert, ctx=ctx)
+    opt = oc.Optimizer(mesh, [1.0 - args.lam], timing=1)
+    opt.precompute()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
+
+    def flush_l2():
+        ctx.synchronize()
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        opt.solve(1)
+    opt.phase_ms()
+    launches0 = opt.launch_count()
+    flush_l2()
+    barrier(world)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(device) if rank == 0 else None
+    step_ms, pcg_ms, pcg_iters = [], [], []
+    for _ in range(args.steps):
+        opt.solve(1)
+        ctx.synchronize()
+        ph = opt.phase_ms()
+        step_ms.append(sum(ph.values()))
+        pcg_ms.append(ph["pcg"])
+        pcg_iters.append(opt.last_step()["pcgIters"])
+        flush_l2()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop() if sampler else None
+    launches = opt.launch_count() - launches0
+    total_s = sum(step_ms) / 1000.0
+    total_s_max = allreduce_max(total_s, world)
+    value = world * args.steps / total_s_max
+
+    # end to end through the C ABI with host buffers: UV in, solve(1), UV out
+    e2e = None
+    if not args.no_e2e:
+        uv_host = mesh.V
+        e2e_steps = max(3, args.steps)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            mesh.V = uv_host
+            opt.solve(1)
+            uv_host = mesh.V
+        t1 = time.perf_counter()
+        e2e_max = allreduce_max(t1 - t0, world)
+        e2e = {"value": world * e2e_steps / e2e_max, "unit": UNIT, "h2d_bytes_per_step": 16 * nV,
+               "d2h_bytes_per_step": 16 * nV}
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    avg_pcg_ms = statistics.mean(pcg_ms)
+    avg_iters = statistics.mean(pcg_iters)
+    achieved = PCG_BYTES_PER_TRI * nF * avg_iters / (avg_pcg_ms / 1000.0) / 1e9
+    roofline = {"kernel": "k_pcg", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                "bytes_per_tri_per_iter": PCG_BYTES_PER_TRI, "pcg_iters_per_step": avg_iters,
+                "pcg_ms_per_step": avg_pcg_ms}
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        secs, n = cpu_port_time(st, args.lam, args.cpu_sample_iters, threads)
+        cpu = {"value": n / secs, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d Newton iteration(s) of %s from the Tutte start" % (n, args.workload)}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "triangles": nF, "vertices": nV, "lambda": args.lam,
+                   "scaffold": False, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between timed steps (256 MB write)", "pcg_tol": 1e-8,
+                   "precision": "fp64 energy/gradient/Krylov, fp32 Hessian projection + matrix storage"},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        "energy": opt.getLastEnergyVal(),
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

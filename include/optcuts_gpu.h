@@ -1,0 +1,150 @@
+/* optcuts_gpu.h -- C ABI of the GB300 (sm_103a) OptCuts geometry step.
+ *
+ * One GPU, one process.  Every entry point takes plain pointers and sizes,
+ * returns an int status (oc_status), and never throws.  Host pointers are
+ * caller-owned; device state lives behind opaque handles.
+ *
+ * Layouts follow the reference's own conventions:
+ *   V_rest   nV x 3 row-major float64  (TriMesh::V_rest, src/TriMesh.hpp:30)
+ *   UV       nV x 2 row-major float64  (TriMesh::V, src/TriMesh.hpp:31)
+ *   F        nF x 3 row-major int32    (TriMesh::F, src/TriMesh.hpp:32)
+ *   gradient / search direction: 2*nV interleaved [u0, v0, u1, v1, ...]
+ *            (src/Energy/SymDirichletEnergy.cpp:262, src/Optimizer.cpp:666-669)
+ *   fixed vertices: list of vertex ids (TriMesh::fixedVert, src/TriMesh.hpp:56)
+ *
+ * Precision: energies, gradients, injective-step roots, line-search
+ * acceptance and Krylov dot products / vector updates are float64; the
+ * per-triangle Hessian's PSD projection and the stored sparse matrix values
+ * are float32 (SpMV accumulates in float64).
+ */
+#ifndef OPTCUTS_GPU_H
+#define OPTCUTS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    OC_OK = 0,
+    OC_ERR_INVALID = 1,          /* bad argument / size / index */
+    OC_ERR_INVERTED = 2,         /* inverted UV triangle (Optimizer.cpp:65-67 exits) */
+    OC_ERR_NOT_CONVERGED = 3,    /* PCG hit its iteration cap */
+    OC_ERR_TIMEOUT = 4,          /* a device loop hit its clock budget */
+    OC_ERR_BOUNDS = 5,           /* index out of range (checked builds) */
+    OC_ERR_CUDA = 6,             /* CUDA runtime error; see oc_last_error() */
+    OC_ERR_DEGENERATE = 7,       /* zero-area rest triangle (TriMesh.cpp:399-402 exits) */
+    OC_ERR_NOT_SPD = 8,          /* non-positive diagonal block in the Newton matrix */
+    OC_ERR_NOMEM = 9
+} oc_status;
+
+typedef struct oc_ctx oc_ctx;
+typedef struct oc_mesh oc_mesh;
+typedef struct oc_linsys oc_linsys;
+typedef struct oc_optimizer oc_optimizer;
+
+/* ---- context ---------------------------------------------------------- */
+/* stream: a cudaStream_t, or NULL for a stream owned by the context. */
+int oc_ctx_create(int device, void* stream, oc_ctx** out);
+int oc_ctx_destroy(oc_ctx* ctx);
+const char* oc_last_error(const oc_ctx* ctx);
+const char* oc_status_string(int status);
+int oc_ctx_synchronize(oc_ctx* ctx);
+
+/* ---- mesh: TriMesh state on the device ---------------------------------
+ * Replaces the TriMesh data the hot path reads (TriMesh.hpp:30-63) and
+ * TriMesh::computeFeatures' rest constants (TriMesh.cpp:343-404).
+ * areaThres: TriMesh::areaThres_AM (0 for surface meshes). */
+int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV,
+                   const int* F, int nF, const int* fixedVert, int nFixed,
+                   double areaThres, oc_mesh** out);
+int oc_mesh_destroy(oc_mesh* mesh);
+int oc_mesh_set_uv(oc_mesh* mesh, const double* UV);        /* host -> device */
+int oc_mesh_get_uv(oc_mesh* mesh, double* UV);              /* device -> host */
+/* rest: nF x 8 (triArea, triAreaSq, e0SqLen, e1SqLen, e0dote1, e0SqLen_div_dbAreaSq,
+ * e1SqLen_div_dbAreaSq, e0dote1_div_dbAreaSq); scalars: surfaceArea, avgEdgeLen,
+ * virtualRadius (TriMesh.cpp:343-404). Either pointer may be NULL. */
+int oc_mesh_rest_constants(oc_mesh* mesh, double* rest, double* scalars);
+/* TriMesh::checkInversion (TriMesh.cpp:1710-1756): *ok = 1 if every UV triangle
+ * has signed double area >= 0. */
+int oc_mesh_check_inversion(oc_mesh* mesh, int* ok);
+
+/* ---- Energy: SymDirichletEnergy (Energy.hpp:27-44) -------------------- */
+/* Energy::computeEnergyVal (Energy.cpp:35-40) */
+int oc_sd_energy(oc_mesh* mesh, int uniformWeight, double* energyVal);
+/* SymDirichletEnergy::getEnergyValPerElem (SymDirichletEnergy.cpp:24-46) */
+int oc_sd_energy_per_elem(oc_mesh* mesh, int uniformWeight, double* energyValPerElem);
+/* SymDirichletEnergy::computeGradient (SymDirichletEnergy.cpp:258-304); 2*nV */
+int oc_sd_gradient(oc_mesh* mesh, int uniformWeight, double* gradient);
+/* SymDirichletEnergy::computeHessian (SymDirichletEnergy.cpp:429-549) per
+ * triangle, PSD-projected (IglUtils::makePD, IglUtils.hpp:71-90): out nF x 36
+ * row-major 6x6 in local order (u1,v1,u2,v2,u3,v3), before fixed-vertex
+ * removal and before energyParams scaling. */
+int oc_sd_hessian_blocks(oc_mesh* mesh, int uniformWeight, double* blocks);
+/* SymDirichletEnergy::initStepSize (SymDirichletEnergy.cpp:551-610): lowers
+ * *stepSize in place to the largest inversion-free step along searchDir. */
+int oc_sd_init_step_size(oc_mesh* mesh, const double* searchDir, double* stepSize);
+
+/* ---- LinSysSolver (LinSysSolver.hpp:22-187, EigenLibSolver.cpp:21-107) --
+ * Full-symmetric 2x2-block CSR on the device, block-Jacobi PCG solve. */
+int oc_linsys_create(oc_ctx* ctx, oc_linsys** out);
+int oc_linsys_destroy(oc_linsys* ls);
+/* set_pattern(vNeighbor, fixedVert) (LinSysSolver.hpp:37-135): the vertex
+ * adjacency is taken from the triangles F; fixed rows keep only the diagonal. */
+int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF,
+                          const int* fixedVert, int nFixed);
+/* update_a(I, J, V) (LinSysSolver.hpp:138-159): triplets with I <= J are summed
+ * into the matrix (mirrored to the lower half), the rest are ignored. */
+int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* V, int nTriplets);
+/* factorize() (EigenLibSolver.cpp:80-93): builds the block-Jacobi preconditioner. */
+int oc_linsys_factorize(oc_linsys* ls);
+/* solve(rhs, result) (EigenLibSolver.cpp:96-107): PCG to relative residual
+ * tol (<= 0: 1e-8) within maxIter (<= 0: 20000).  iters / relres may be NULL. */
+int oc_linsys_solve(oc_linsys* ls, const double* rhs, double* result, double tol, int maxIter,
+                    int* iters, double* relres);
+/* multiply(x, Ax) (LinSysSolver.hpp:172-187) */
+int oc_linsys_multiply(oc_linsys* ls, const double* x, double* Ax);
+
+/* ---- Optimizer (Optimizer.hpp:74-142), scaffold off ---------------------
+ * energyParam = energyParams[0] = 1 - lambda.  The mesh is borrowed (its UV
+ * is the optimizer's `result.V`). */
+typedef struct {
+    double pcgTol;        /* relative residual, default 1e-8 */
+    int pcgMaxIter;       /* default 20000 */
+    double relGL2Tol;     /* Optimizer.cpp:70, default 1e-12 */
+    int lineSearchBatch;  /* trial step sizes per energy launch, 1..8, default 4 */
+    int timing;           /* 1: record per-phase CUDA-event times */
+} oc_optimizer_config;
+
+int oc_optimizer_default_config(oc_optimizer_config* cfg);
+int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_config* cfg,
+                        oc_optimizer** out);
+int oc_optimizer_destroy(oc_optimizer* opt);
+/* Optimizer::precompute (Optimizer.cpp:154-201) */
+int oc_optimizer_precompute(oc_optimizer* opt);
+/* Optimizer::solve (Optimizer.cpp:203-261): *result = 0 (not converged) or
+ * 1 (converged, or the line search stopped). */
+int oc_optimizer_solve(oc_optimizer* opt, int maxIter, int* result);
+/* Optimizer::getLastEnergyVal (Optimizer.cpp:845-850) */
+int oc_optimizer_get_last_energy(oc_optimizer* opt, double* energy);
+int oc_optimizer_get_iter_num(oc_optimizer* opt, int* iterNum);
+/* Optimizer::setRelGL2Tol (Optimizer.cpp:142-147) */
+int oc_optimizer_set_rel_gl2_tol(oc_optimizer* opt, double tol);
+/* energyParams[0] changed by the caller, then updateEnergyData(true, false,
+ * false) (Optimizer.cpp:323-334; main.cpp:764). */
+int oc_optimizer_set_energy_param(oc_optimizer* opt, double energyParam);
+/* Last iteration's diagnostics: accepted step, PCG iterations and relative
+ * residual, line-search energy launches, ||g||^2 at its start. */
+int oc_optimizer_last_step(oc_optimizer* opt, double* stepSize, int* pcgIters, double* pcgRelRes,
+                           int* lineSearchLaunches, double* gradSqNorm);
+/* Per-phase device milliseconds accumulated since the last call (timing=1):
+ * out[0..5] = gradient, hessian+projection, assembly+preconditioner, PCG,
+ * injective step, line search.  Names match the reference's timer_step
+ * buckets (main.cpp:1557-1565). */
+int oc_optimizer_phase_ms(oc_optimizer* opt, double* out6);
+/* Kernel launches this optimizer issued since creation (for accounting). */
+int oc_optimizer_launch_count(oc_optimizer* opt, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,393 @@
+"""optcuts_gb300 -- the OptCuts geometry step on one GB300 (sm_103a).
+
+Python mirror of the reference's interfaces for the path, over the C ABI in
+include/optcuts_gpu.h (library: optcuts_gb300/_lib/liboc_gpu.so):
+
+    TriMesh             -- device-resident mesh state (src/TriMesh.hpp:28-63)
+    SymDirichletEnergy  -- computeEnergyVal / getEnergyValPerElem /
+                           computeGradient / computeHessian / initStepSize
+                           (src/Energy/Energy.hpp:27-44)
+    LinSysSolver        -- set_pattern / update_a / factorize / solve /
+                           multiply (src/LinSysSolver/LinSysSolver.hpp:22-187)
+    Optimizer           -- precompute / solve / getLastEnergyVal / ...
+                           (src/Optimizer.hpp:74-142)
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+visible, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "liboc_gpu.so")
+
+_lib = None
+
+OC_OK = 0
+OC_ERR_NOT_CONVERGED = 3
+
+
+class OCError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+
+
+class OptimizerConfig(ctypes.Structure):
+    _fields_ = [("pcgTol", ctypes.c_double), ("pcgMaxIter", ctypes.c_int), ("relGL2Tol", ctypes.c_double),
+                ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int)]
+
+
+_SIGS = {
+    "oc_ctx_create": [ctypes.c_int, _vp, ctypes.POINTER(_vp)],
+    "oc_ctx_destroy": [_vp],
+    "oc_ctx_synchronize": [_vp],
+    "oc_mesh_create": [_vp, _d, _d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double,
+                       ctypes.POINTER(_vp)],
+    "oc_mesh_destroy": [_vp],
+    "oc_mesh_set_uv": [_vp, _d],
+    "oc_mesh_get_uv": [_vp, _d],
+    "oc_mesh_rest_constants": [_vp, _d, _d],
+    "oc_mesh_check_inversion": [_vp, _i],
+    "oc_sd_energy": [_vp, ctypes.c_int, _d],
+    "oc_sd_energy_per_elem": [_vp, ctypes.c_int, _d],
+    "oc_sd_gradient": [_vp, ctypes.c_int, _d],
+    "oc_sd_hessian_blocks": [_vp, ctypes.c_int, _d],
+    "oc_sd_init_step_size": [_vp, _d, _d],
+    "oc_linsys_create": [_vp, ctypes.POINTER(_vp)],
+    "oc_linsys_destroy": [_vp],
+    "oc_linsys_set_pattern": [_vp, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int],
+    "oc_linsys_update_a": [_vp, _i, _i, _d, ctypes.c_int],
+    "oc_linsys_factorize": [_vp],
+    "oc_linsys_solve": [_vp, _d, _d, ctypes.c_double, ctypes.c_int, _i, _d],
+    "oc_linsys_multiply": [_vp, _d, _d],
+    "oc_optimizer_default_config": [ctypes.POINTER(OptimizerConfig)],
+    "oc_optimizer_create": [_vp, ctypes.c_double, ctypes.POINTER(OptimizerConfig), ctypes.POINTER(_vp)],
+    "oc_optimizer_destroy": [_vp],
+    "oc_optimizer_precompute": [_vp],
+    "oc_optimizer_solve": [_vp, ctypes.c_int, _i],
+    "oc_optimizer_get_last_energy": [_vp, _d],
+    "oc_optimizer_get_iter_num": [_vp, _i],
+    "oc_optimizer_set_rel_gl2_tol": [_vp, ctypes.c_double],
+    "oc_optimizer_set_energy_param": [_vp, ctypes.c_double],
+    "oc_optimizer_last_step": [_vp, _d, _i, _d, _i, _d],
+    "oc_optimizer_phase_ms": [_vp, _d],
+    "oc_optimizer_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+}
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("liboc_gpu.so is not built (run: python -m optcuts_gb300.build); "
+                              "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L.oc_last_error.argtypes = [_vp]
+        L.oc_last_error.restype = ctypes.c_char_p
+        L.oc_status_string.argtypes = [ctypes.c_int]
+        L.oc_status_string.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def _pd(a):
+    return a.ctypes.data_as(_d)
+
+
+def _pi(a):
+    return a.ctypes.data_as(_i)
+
+
+def _f8(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+def _i4(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+class Context:
+    """One GPU and one CUDA stream."""
+
+    def __init__(self, device=0):
+        h = _vp()
+        rc = lib().oc_ctx_create(device, None, ctypes.byref(h))
+        if rc != OC_OK:
+            raise OCError(rc, "oc_ctx_create failed (no usable GPU?)")
+        self.h = h
+
+    def check(self, rc, what, allow=(OC_OK,)):
+        if rc not in allow:
+            msg = lib().oc_last_error(self.h).decode() or lib().oc_status_string(rc).decode()
+            raise OCError(rc, "%s: %s" % (what, msg))
+        return rc
+
+    def synchronize(self):
+        self.check(lib().oc_ctx_synchronize(self.h), "synchronize")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class TriMesh:
+    """Device-resident TriMesh state (V_rest, V = UV, F, fixedVert)."""
+
+    def __init__(self, V_rest, UV, F, fixedVert=(0,), areaThres=0.0, ctx=None):
+        self.ctx = ctx or default_context()
+        self.V_rest = _f8(V_rest)
+        self.F = _i4(F)
+        self.fixedVert = _i4(np.asarray(fixedVert).reshape(-1))
+        uv = _f8(UV)
+        if self.V_rest.ndim != 2 or self.V_rest.shape[1] != 3 or uv.shape != (len(self.V_rest), 2):
+            raise ValueError("V_rest must be (n, 3) and UV (n, 2)")
+        if self.F.ndim != 2 or self.F.shape[1] != 3:
+            raise ValueError("F must be (m, 3)")
+        self.nV, self.nF = len(self.V_rest), len(self.F)
+        h = _vp()
+        self.ctx.check(lib().oc_mesh_create(self.ctx.h, _pd(self.V_rest), _pd(uv), self.nV, _pi(self.F), self.nF,
+                                            _pi(self.fixedVert), len(self.fixedVert), float(areaThres),
+                                            ctypes.byref(h)), "TriMesh")
+        self.h = h
+
+    @property
+    def V(self):
+        out = np.empty((self.nV, 2))
+        self.ctx.check(lib().oc_mesh_get_uv(self.h, _pd(out)), "get UV")
+        return out
+
+    @V.setter
+    def V(self, uv):
+        uv = _f8(uv)
+        if uv.shape != (self.nV, 2):
+            raise ValueError("UV shape")
+        self.ctx.check(lib().oc_mesh_set_uv(self.h, _pd(uv)), "set UV")
+
+    def rest_constants(self):
+        rest = np.empty((self.nF, 8))
+        sc = np.empty(3)
+        self.ctx.check(lib().oc_mesh_rest_constants(self.h, _pd(rest), _pd(sc)), "rest constants")
+        return rest, sc
+
+    @property
+    def surfaceArea(self):
+        return self.rest_constants()[1][0]
+
+    def checkInversion(self):
+        ok = ctypes.c_int()
+        self.ctx.check(lib().oc_mesh_check_inversion(self.h, ctypes.byref(ok)), "checkInversion")
+        return bool(ok.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oc_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SymDirichletEnergy:
+    """src/Energy/SymDirichletEnergy.hpp:15-42, on the device."""
+
+    needRefactorize = True
+
+    def computeEnergyVal(self, data, uniformWeight=False):
+        e = ctypes.c_double()
+        data.ctx.check(lib().oc_sd_energy(data.h, int(uniformWeight), ctypes.byref(e)), "computeEnergyVal")
+        return e.value
+
+    def getEnergyValPerElem(self, data, uniformWeight=False):
+        out = np.empty(data.nF)
+        data.ctx.check(lib().oc_sd_energy_per_elem(data.h, int(uniformWeight), _pd(out)), "getEnergyValPerElem")
+        return out
+
+    def computeGradient(self, data, uniformWeight=False):
+        g = np.empty(2 * data.nV)
+        data.ctx.check(lib().oc_sd_gradient(data.h, int(uniformWeight), _pd(g)), "computeGradient")
+        return g
+
+    def computeHessian(self, data, uniformWeight=False):
+        """Per-triangle PSD-projected 6x6 blocks, shape (nF, 6, 6)."""
+        out = np.empty((data.nF, 6, 6))
+        data.ctx.check(lib().oc_sd_hessian_blocks(data.h, int(uniformWeight), _pd(out)), "computeHessian")
+        return out
+
+    def initStepSize(self, data, searchDir, stepSize=1.0):
+        d = _f8(searchDir)
+        if d.size != 2 * data.nV:
+            raise ValueError("searchDir size")
+        s = ctypes.c_double(stepSize)
+        data.ctx.check(lib().oc_sd_init_step_size(data.h, _pd(d), ctypes.byref(s)), "initStepSize")
+        return s.value
+
+
+class LinSysSolver:
+    """GPU block-CSR matrix + block-Jacobi PCG behind the reference's
+    LinSysSolver interface (LinSysSolver.hpp:22-187)."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx or default_context()
+        h = _vp()
+        self.ctx.check(lib().oc_linsys_create(self.ctx.h, ctypes.byref(h)), "LinSysSolver")
+        self.h = h
+        self.numRows = 0
+        self.last_iters = 0
+        self.last_relres = 0.0
+
+    def set_pattern(self, nV, F, fixedVert):
+        F, fx = _i4(F), _i4(np.asarray(fixedVert).reshape(-1))
+        self.ctx.check(lib().oc_linsys_set_pattern(self.h, nV, _pi(F), len(F), _pi(fx), len(fx)), "set_pattern")
+        self.numRows = 2 * nV
+
+    def update_a(self, I, J, V):
+        I, J, V = _i4(I), _i4(J), _f8(V)
+        self.ctx.check(lib().oc_linsys_update_a(self.h, _pi(I), _pi(J), _pd(V), len(V)), "update_a")
+
+    def analyze_pattern(self):
+        pass
+
+    def factorize(self):
+        return self.ctx.check(lib().oc_linsys_factorize(self.h), "factorize") == OC_OK
+
+    def solve(self, rhs, tol=1e-8, maxIter=20000):
+        rhs = _f8(rhs)
+        x = np.empty(self.numRows)
+        it = ctypes.c_int()
+        rr = ctypes.c_double()
+        rc = self.ctx.check(lib().oc_linsys_solve(self.h, _pd(rhs), _pd(x), tol, maxIter, ctypes.byref(it),
+                                                  ctypes.byref(rr)), "solve", allow=(OC_OK, OC_ERR_NOT_CONVERGED))
+        self.last_iters, self.last_relres, self.last_converged = it.value, rr.value, rc == OC_OK
+        return x
+
+    def multiply(self, x):
+        x = _f8(x)
+        y = np.empty(self.numRows)
+        self.ctx.check(lib().oc_linsys_multiply(self.h, _pd(x), _pd(y)), "multiply")
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oc_linsys_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_config(**kw):
+    c = OptimizerConfig()
+    lib().oc_optimizer_default_config(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Optimizer:
+    """Projected Newton with the injective line search (Optimizer.hpp:74-142),
+    scaffold off.  energyParams = [1 - lambda] as in main.cpp:1569."""
+
+    def __init__(self, data0, energyParams, config=None, **kw):
+        self.data = data0
+        self.ctx = data0.ctx
+        self.energyParams = list(energyParams)
+        cfg = config if config is not None else default_config(**kw)
+        h = _vp()
+        self.ctx.check(lib().oc_optimizer_create(data0.h, float(self.energyParams[0]), ctypes.byref(cfg),
+                                                 ctypes.byref(h)), "Optimizer")
+        self.h = h
+
+    def precompute(self):
+        self.ctx.check(lib().oc_optimizer_precompute(self.h), "precompute")
+
+    def solve(self, maxIter=100):
+        r = ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_solve(self.h, maxIter, ctypes.byref(r)), "solve",
+                       allow=(OC_OK, OC_ERR_NOT_CONVERGED))
+        return r.value
+
+    def getLastEnergyVal(self, excludeScaffold=False):
+        e = ctypes.c_double()
+        self.ctx.check(lib().oc_optimizer_get_last_energy(self.h, ctypes.byref(e)), "getLastEnergyVal")
+        return e.value
+
+    def getIterNum(self):
+        n = ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_get_iter_num(self.h, ctypes.byref(n)), "getIterNum")
+        return n.value
+
+    def setRelGL2Tol(self, tol):
+        self.ctx.check(lib().oc_optimizer_set_rel_gl2_tol(self.h, tol), "setRelGL2Tol")
+
+    def updateEnergyData(self):
+        self.ctx.check(lib().oc_optimizer_set_energy_param(self.h, float(self.energyParams[0])), "updateEnergyData")
+
+    def getResult(self):
+        return self.data
+
+    def last_step(self):
+        s, r, g = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        it, ls = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_last_step(self.h, ctypes.byref(s), ctypes.byref(it), ctypes.byref(r),
+                                                    ctypes.byref(ls), ctypes.byref(g)), "last_step")
+        return {"stepSize": s.value, "pcgIters": it.value, "pcgRelRes": r.value, "lineSearchLaunches": ls.value,
+                "gradSqNorm": g.value}
+
+    def phase_ms(self):
+        out = np.zeros(6)
+        self.ctx.check(lib().oc_optimizer_phase_ms(self.h, _pd(out)), "phase_ms")
+        return dict(zip(["gradient", "hessian", "assembly", "pcg", "injective", "linesearch"], out.tolist()))
+
+    def launch_count(self):
+        n = ctypes.c_longlong()
+        self.ctx.check(lib().oc_optimizer_launch_count(self.h, ctypes.byref(n)), "launch_count")
+        return n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oc_optimizer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,327 @@
+// FP64 per-triangle kernels of the geometry step: energy, gradient,
+// inversion-free step bound, step forward, inversion check and the
+// deterministic reductions behind them.
+//
+// This translation unit is compiled with -fmad=false so that every
+// expression rounds exactly as the reference's scalar x86-64 code does
+// (no fused multiply-add there either); with IEEE division and square root
+// the per-triangle energies, gradients and step bounds are bit-identical to
+// src/Energy/SymDirichletEnergy.cpp.  Sums over triangles use a fixed-order
+// two-pass reduction, so results are deterministic run to run.
+
+#include "oc_internal.h"
+
+#include <cstdint>
+
+namespace oc {
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NT values per thread; thread 0 writes NT partials.
+template <int NT>
+__device__ __forceinline__ void block_sum_store(double (&v)[NT], int nTrials, double* out)
+{
+    __shared__ double sh[NT][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        if (k < nTrials) {
+            double s = warp_sum(v[k]);
+            if (lane == 0) sh[k][warp] = s;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            if (k < nTrials) {
+                double s = lane < nw ? sh[k][lane] : 0.0;
+                s = warp_sum(s);
+                if (lane == 0) out[k] = s;
+            }
+        }
+    }
+}
+
+struct Corners {
+    double2 U1, U2, U3;
+};
+
+__device__ __forceinline__ double2 at(const double2* uv, const double2* dir, double alpha, int v)
+{
+    double2 p = uv[v];
+    if (dir) {
+        const double2 d = dir[v];
+        p.x = p.x + alpha * d.x;   // Optimizer::stepForward, Optimizer.cpp:667-668
+        p.y = p.y + alpha * d.y;
+    }
+    return p;
+}
+
+// SymDirichletEnergy::getEnergyValPerElem body (SymDirichletEnergy.cpp:32-44).
+__device__ __forceinline__ double elem_energy(const DeviceMesh& m, int t, double w, const double2 U1,
+                                              const double2 U2, const double2 U3)
+{
+    const double a0 = U2.x - U1.x, a1 = U2.y - U1.y;   // U2m1
+    const double b0 = U3.x - U1.x, b1 = U3.y - U1.y;   // U3m1
+    const double area_U = 0.5 * (a0 * b1 - a1 * b0);
+    const double A2 = m.A2[t];
+    return w * (1.0 + A2 / area_U / area_U) *
+           (((b0 * b0 + b1 * b1) * m.e0[t] + (a0 * a0 + a1 * a1) * m.e1[t]) / 4 / A2 -
+            (b0 * a0 + b1 * a1) * m.e01[t] / 2 / A2);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(256) k_energy(DeviceMesh m, const double2* __restrict__ uv,
+                                                const double2* __restrict__ dir, Alphas alphas, int nTrials,
+                                                int uniform, double* partials)
+{
+    double acc[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) acc[k] = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.nF; t += gridDim.x * blockDim.x) {
+        const int i0 = m.F0[t], i1 = m.F1[t], i2 = m.F2[t];
+        const double w = uniform ? 1.0 : m.w[t];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            if (k < nTrials) {
+                const double a = alphas.a[k];
+                acc[k] += elem_energy(m, t, w, at(uv, dir, a, i0), at(uv, dir, a, i1), at(uv, dir, a, i2));
+            }
+        }
+    }
+    block_sum_store<NT>(acc, nTrials, partials + (size_t)blockIdx.x * kMaxTrials);
+}
+
+__global__ void k_energy_elem(DeviceMesh m, int uniform, double* out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    const double w = uniform ? 1.0 : m.w[t];
+    out[t] = elem_energy(m, t, w, m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]);
+}
+
+// Fixed-order final reduction of nBlocks x nVals partials (single block).
+__global__ void k_reduce_final(const double* partials, int nBlocks, int nVals, double* out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ double sh[32];
+    for (int k = 0; k < nVals; ++k) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < nBlocks; b += blockDim.x) s += partials[(size_t)b * kMaxTrials + k];
+        s = warp_sum(s);
+        if (lane == 0) sh[warp] = s;
+        __syncthreads();
+        if (warp == 0) {
+            double v = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+            v = warp_sum(v);
+            if (lane == 0) out[k] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// SymDirichletEnergy::computeGradient per-corner terms (SymDirichletEnergy.cpp:267-297),
+// written to cornerBuf[k * nF + t].
+__global__ void __launch_bounds__(256) k_grad_corners(DeviceMesh m, int uniform, double2* __restrict__ cornerBuf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    const double2 U1 = m.uv[m.F0[t]], U2 = m.uv[m.F1[t]], U3 = m.uv[m.F2[t]];
+    const double a0 = U2.x - U1.x, a1 = U2.y - U1.y;   // U2m1
+    const double b0 = U3.x - U1.x, b1 = U3.y - U1.y;   // U3m1
+    const double area_U = 0.5 * (a0 * b1 - a1 * b0);
+    const double A2 = m.A2[t], e0 = m.e0[t], e1 = m.e1[t], e01 = m.e01[t];
+    const double leftTerm = 1.0 + A2 / area_U / area_U;
+    const double rightTerm = ((b0 * b0 + b1 * b1) * e0 + (a0 * a0 + a1 * a1) * e1) / 4 / A2 -
+                             (b0 * a0 + b1 * a1) * e01 / 2 / A2;
+    const double areaRatio = A2 / area_U / area_U / area_U;
+    const double w = uniform ? 1.0 : m.w[t];
+    const int nF = m.nF;
+    {
+        const double eo0 = U3.x - U2.x, eo1 = U3.y - U2.y;
+        const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
+        const double dR0 = ((e01 - e0) * b0 + (e01 - e1) * a0) / 2.0 / A2;
+        const double dR1 = ((e01 - e0) * b1 + (e01 - e1) * a1) / 2.0 / A2;
+        cornerBuf[t] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+    }
+    {
+        const double eo0 = U1.x - U3.x, eo1 = U1.y - U3.y;
+        const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
+        const double dR0 = (e1 * a0 - e01 * b0) / 2.0 / A2;
+        const double dR1 = (e1 * a1 - e01 * b1) / 2.0 / A2;
+        cornerBuf[nF + t] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+    }
+    {
+        const double eo0 = U2.x - U1.x, eo1 = U2.y - U1.y;
+        const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
+        const double dR0 = (e0 * b0 - e01 * a0) / 2.0 / A2;
+        const double dR1 = (e0 * b1 - e01 * a1) / 2.0 / A2;
+        cornerBuf[2 * nF + t] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+    }
+}
+
+// Per-vertex gather in triangle order (the reference's scatter order), fixed
+// rows zeroed (SymDirichletEnergy.cpp:300-303), times energyParams[0]
+// (Optimizer.cpp:786); block partials of ||g||^2.
+__global__ void __launch_bounds__(256) k_grad_gather(DeviceMesh m, const double2* __restrict__ cornerBuf, double scale,
+                                                     double2* __restrict__ g, double* partials)
+{
+    double acc[1] = {0.0};
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m.nV; v += gridDim.x * blockDim.x) {
+        double sx = 0.0, sy = 0.0;
+        for (int p = m.vcPtr[v]; p < m.vcPtr[v + 1]; ++p) {
+            const double2 c = cornerBuf[m.vcIdx[p]];
+            sx = sx + c.x;
+            sy = sy + c.y;
+        }
+        if (m.fixedMask[v]) { sx = 0.0; sy = 0.0; }
+        sx = scale * sx;
+        sy = scale * sy;
+        g[v] = make_double2(sx, sy);
+        acc[0] += sx * sx + sy * sy;
+    }
+    block_sum_store<1>(acc, 1, partials + (size_t)blockIdx.x * kMaxTrials);
+}
+
+// SymDirichletEnergy::initStepSize (SymDirichletEnergy.cpp:555-609); the
+// minimum over triangles is taken with an atomicMin on the bit pattern of
+// positive doubles (order-independent, hence deterministic).
+__global__ void __launch_bounds__(256) k_init_step(DeviceMesh m, const double2* __restrict__ dir, double stepSize,
+                                                   unsigned long long* minBits)
+{
+    double best = stepSize;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.nF; t += gridDim.x * blockDim.x) {
+        const int i0 = m.F0[t], i1 = m.F1[t], i2 = m.F2[t];
+        const double2 U1 = m.uv[i0], U2 = m.uv[i1], U3 = m.uv[i2];
+        const double2 V1 = dir[i0], V2 = dir[i1], V3 = dir[i2];
+        const double U2m1x = U2.x - U1.x, U2m1y = U2.y - U1.y;
+        const double U3m1x = U3.x - U1.x, U3m1y = U3.y - U1.y;
+        const double V2m1x = V2.x - V1.x, V2m1y = V2.y - V1.y;
+        const double V3m1x = V3.x - V1.x, V3m1y = V3.y - V1.y;
+        const double a = V2m1x * V3m1y - V2m1y * V3m1x;
+        const double b = U2m1x * V3m1y - U2m1y * V3m1x + V2m1x * U3m1y - V2m1y * U3m1x;
+        const double c = U2m1x * U3m1y - U2m1y * U3m1x;
+        const double delta = b * b - 4.0 * a * c;
+        double bound = stepSize;
+        if (a > 0.0) {
+            if ((b < 0.0) && (delta >= 0.0)) bound = 2.0 * c / (-b + sqrt(delta));
+        }
+        else if (a < 0.0) {
+            if (b < 0.0) bound = 2.0 * c / (-b + sqrt(delta));
+            else bound = (-b - sqrt(delta)) / 2.0 / a;
+        }
+        else {
+            if (b < 0.0) bound = -c / b;
+        }
+        if (bound < best) best = bound;
+    }
+    // block min via shuffles (exact), then one atomic per block
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = fmin(best, __shfl_down_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0) {
+        // every bound of a valid (non-inverted) triangle is positive; a
+        // non-positive or NaN bound is clamped to 0 so the host sees it
+        const double v = (best > 0.0) ? best : 0.0;
+        atomicMin(minBits, static_cast<unsigned long long>(__double_as_longlong(v)));
+    }
+}
+
+__global__ void k_set_bits(unsigned long long* dst, double v)
+{
+    *dst = static_cast<unsigned long long>(__double_as_longlong(v));
+}
+
+__global__ void k_step_forward(const double2* __restrict__ uv0, const double2* __restrict__ dir, double alpha,
+                               double2* __restrict__ uv, int nV)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nV) return;
+    const double2 p = uv0[v], d = dir[v];
+    uv[v] = make_double2(p.x + alpha * d.x, p.y + alpha * d.y);
+}
+
+// TriMesh::checkInversion (TriMesh.cpp:1710-1756): count of triangles with
+// signed double area < 0, into minBits (as a plain counter).
+__global__ void k_check_inversion(DeviceMesh m, unsigned long long* count)
+{
+    unsigned int bad = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.nF; t += gridDim.x * blockDim.x) {
+        const double2 U1 = m.uv[m.F0[t]], U2 = m.uv[m.F1[t]], U3 = m.uv[m.F2[t]];
+        const double e00 = U2.x - U1.x, e01 = U2.y - U1.y, e10 = U3.x - U1.x, e11 = U3.y - U1.y;
+        const double dbArea = e00 * e11 - e01 * e10;
+        if (dbArea < 0.0) ++bad;
+    }
+    for (int o = 16; o > 0; o >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, o);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(count, static_cast<unsigned long long>(bad));
+}
+
+} // namespace
+
+int reduce_blocks_for(int n)
+{
+    int b = (n + 255) / 256;
+    if (b > 1216) b = 1216;   // 152 SMs x 8 resident 256-thread blocks
+    return b < 1 ? 1 : b;
+}
+
+void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st)
+{
+    k_reduce_final<<<1, 256, 0, st>>>(s.partials, nBlocks, nVals, s.result);
+}
+
+void launch_energy(const DeviceMesh& m, const double2* uv, const double2* dir, const double* alphas, int nTrials,
+                   int uniform, double scale, Scratch& s, cudaStream_t st)
+{
+    (void)scale;
+    Alphas a = {{0, 0, 0, 0, 0, 0, 0, 0}};
+    for (int k = 0; k < nTrials && k < 8; ++k) a.a[k] = alphas ? alphas[k] : 0.0;
+    const int nb = reduce_blocks_for(m.nF);
+    if (nTrials <= 1)
+        k_energy<1><<<nb, 256, 0, st>>>(m, uv, dir, a, 1, uniform, s.partials);
+    else if (nTrials <= 4)
+        k_energy<4><<<nb, 256, 0, st>>>(m, uv, dir, a, nTrials, uniform, s.partials);
+    else
+        k_energy<8><<<nb, 256, 0, st>>>(m, uv, dir, a, nTrials, uniform, s.partials);
+    launch_reduce_final(s, nb, nTrials < 1 ? 1 : nTrials, st);
+}
+
+void launch_energy_elem(const DeviceMesh& m, int uniform, double* out, cudaStream_t st)
+{
+    k_energy_elem<<<(m.nF + 255) / 256, 256, 0, st>>>(m, uniform, out);
+}
+
+void launch_gradient(const DeviceMesh& m, int uniform, double scale, double2* cornerBuf, double2* g, Scratch& s,
+                     cudaStream_t st)
+{
+    k_grad_corners<<<(m.nF + 255) / 256, 256, 0, st>>>(m, uniform, cornerBuf);
+    const int nb = reduce_blocks_for(m.nV);
+    k_grad_gather<<<nb, 256, 0, st>>>(m, cornerBuf, scale, g, s.partials);
+    launch_reduce_final(s, nb, 1, st);
+}
+
+void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, Scratch& s, cudaStream_t st)
+{
+    k_set_bits<<<1, 1, 0, st>>>(s.minBits, stepSize);
+    k_init_step<<<reduce_blocks_for(m.nF), 256, 0, st>>>(m, dir, stepSize, s.minBits);
+}
+
+void launch_step_forward(const double2* uv0, const double2* dir, double alpha, double2* uv, int nV, cudaStream_t st)
+{
+    k_step_forward<<<(nV + 255) / 256, 256, 0, st>>>(uv0, dir, alpha, uv, nV);
+}
+
+void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st)
+{
+    cudaMemsetAsync(s.minBits, 0, sizeof(unsigned long long), st);
+    k_check_inversion<<<reduce_blocks_for(m.nF), 256, 0, st>>>(m, s.minBits);
+}
+
+} // namespace oc

@@ -1,0 +1,103 @@
+// Internal declarations shared by the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "optcuts_gpu.h"
+
+#include <string>
+#include <vector>
+
+namespace oc {
+
+// 2x2 FP64 matrix, row-major (block-Jacobi inverse of one vertex row).
+struct __align__(32) Mat2d {
+    double a00, a01, a10, a11;
+};
+
+// Line-search step sizes passed by value to the energy kernel.
+struct Alphas {
+    double a[8];
+};
+
+constexpr int kMaxTrials = 8;       // line-search step sizes per energy launch
+constexpr int kReduceThreads = 256; // block size of the reduction kernels
+
+// Device-resident triangle mesh (structure of arrays for per-triangle data,
+// vertex-major double2 for UV so a corner gather is one 16-byte load).
+struct DeviceMesh {
+    int nV = 0, nF = 0;
+    int *F0 = nullptr, *F1 = nullptr, *F2 = nullptr;   // corner vertex ids
+    // FP64 rest constants in the reference's own form (TriMesh.cpp:367-393):
+    // triAreaSq, the area weight triArea/surfaceArea, e0SqLen, e1SqLen,
+    // e0dote1 (energy and gradient divide at use, SymDirichletEnergy.cpp:42-44)
+    // and the *_div_dbAreaSq values the Hessian reads.
+    double *A2 = nullptr, *w = nullptr;
+    double *e0 = nullptr, *e1 = nullptr, *e01 = nullptr;
+    double *e0d = nullptr, *e1d = nullptr, *e01d = nullptr;
+    double2* uv = nullptr;                              // nV
+    // vertex -> incident corners (CSR, each list sorted by triangle id);
+    // corner code = k * nF + t
+    int *vcPtr = nullptr, *vcIdx = nullptr;
+    unsigned char* fixedMask = nullptr;                 // nV
+};
+
+// Reduction scratch: per-block partials then a fixed-order final pass.
+struct Scratch {
+    double* partials = nullptr;     // [maxBlocks * kMaxTrials]
+    double* result = nullptr;       // [kMaxTrials + 8]
+    double* hostResult = nullptr;   // pinned mirror
+    unsigned long long* minBits = nullptr;
+    int maxBlocks = 0;
+};
+
+// Full-symmetric 2x2-block CSR pattern + per-slot contribution lists.
+struct DeviceBsr {
+    int nRows = 0, nnzb = 0;
+    int *rowPtr = nullptr, *col = nullptr;
+    float4* val = nullptr;         // nnzb blocks, row-major (a00, a01, a10, a11)
+    int* diagSlot = nullptr;       // nRows
+    unsigned char* rowFixed = nullptr;
+    // contributions: slot -> list of (t * 9 + a * 3 + b)
+    int *cPtr = nullptr, *cIdx = nullptr;
+    Mat2d* dinv = nullptr;         // block-Jacobi inverses (FP64)
+};
+
+struct PcgWork {
+    double2 *x = nullptr, *r = nullptr, *p = nullptr, *z = nullptr, *u = nullptr, *w = nullptr;
+    double* partials = nullptr;    // [grid * 4]
+    int* status = nullptr;         // [4] iterations, flag
+    int grid = 0, block = 0, n = 0;
+};
+
+// ---- launchers (kernels live in oc_fp64.cu / oc_kernels.cu) ----
+// energy at uv + alpha_k * dir for k < nTrials (dir may be null: alphas ignored)
+void launch_energy(const DeviceMesh& m, const double2* uv, const double2* dir, const double* alphasHost,
+                   int nTrials, int uniform, double scale, Scratch& s, cudaStream_t st);
+void launch_energy_elem(const DeviceMesh& m, int uniform, double* out, cudaStream_t st);
+// corner gradients (3 x nF double2) then per-vertex gather; writes ||g||^2 to s.result[0]
+void launch_gradient(const DeviceMesh& m, int uniform, double scale, double2* cornerBuf, double2* g,
+                     Scratch& s, cudaStream_t st);
+// min over triangles of the inversion-free bound, starting from stepSize
+void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, Scratch& s, cudaStream_t st);
+void launch_step_forward(const double2* uv0, const double2* dir, double alpha, double2* uv, int nV,
+                         cudaStream_t st);
+void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st);
+void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st);
+int reduce_blocks_for(int n);
+
+// per-triangle projected Hessian: 21 FP32 values per triangle (SoA, scaled by `scale`)
+void launch_hessian(const DeviceMesh& m, int uniform, float* hb, cudaStream_t st);
+// expand the 21 packed values to full 6x6 FP64 (for the API / tests)
+void launch_hessian_expand(const float* hb, int nF, double* out, cudaStream_t st);
+void launch_assemble(const DeviceBsr& b, const float* hb, int nF, double scale, cudaStream_t st);
+int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag);
+void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag);
+// solves A x = rhsSign * rhs (rhsSign = -1 gives the Newton direction from g)
+int pcg_solve(const DeviceBsr& b, const double2* rhs, double2* x, PcgWork& wk, double tol, int maxIter,
+              double rhsSign, cudaStream_t st, int* itersOut, double* relresOut, std::string* err);
+void pcg_alloc(PcgWork& wk, int nRows, int device);
+void pcg_free(PcgWork& wk);
+void launch_spmv(const DeviceBsr& b, const double2* x, double2* y, cudaStream_t st);
+
+} // namespace oc

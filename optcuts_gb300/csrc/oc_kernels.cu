@@ -1,0 +1,557 @@
+// Newton-matrix kernels of the geometry step: per-triangle Hessian with PSD
+// projection, block-CSR assembly, block-Jacobi preconditioner, SpMV and the
+// persistent PCG solve.
+//
+// Precision: the per-triangle 6x6 Hessian is formed in FP64 with the
+// reference's closed-form second derivatives (SymDirichletEnergy.cpp:
+// 440-522), normalised by its largest entry and projected to PSD in FP32.
+// Matrix values are stored in FP32; SpMV, preconditioner and every Krylov
+// vector and dot product are FP64.  The systems are extremely ill-conditioned
+// (a Tutte start has UV triangles 1e-9 times their rest area), and FP32
+// Krylov arithmetic stalls on them, FP32 storage does not.
+
+#include "oc_internal.h"
+
+#include <cooperative_groups.h>
+
+#include <cmath>
+#include <cstdio>
+
+namespace cg = cooperative_groups;
+
+namespace oc {
+namespace {
+
+// Orthonormal basis of the complement of the two rigid translations in the
+// 6-dimensional corner space (u1, v1, u2, v2, u3, v3):
+// columns q1(x)e_x, q1(x)e_y, q2(x)e_x, q2(x)e_y with q1 = (1,-1,0)/sqrt2,
+// q2 = (1,1,-2)/sqrt6.  The SD Hessian annihilates translations, so its
+// eigen-decomposition reduces to the 4x4 matrix Q^T H Q.
+__constant__ float kQ1[3] = {0.70710678118654752f, -0.70710678118654752f, 0.0f};
+__constant__ float kQ2[3] = {0.40824829046386302f, 0.40824829046386302f, -0.81649658092772603f};
+
+__device__ __forceinline__ float qv(int col, int row)
+{
+    // Q[row][col], row in 0..5 (vertex = row/2, comp = row%2), col in 0..3
+    const int vert = row >> 1, comp = row & 1;
+    const int qi = col >> 1, qc = col & 1;
+    if (comp != qc) return 0.0f;
+    return qi == 0 ? kQ1[vert] : kQ2[vert];
+}
+
+// Cyclic Jacobi on a symmetric 4x4 (FP32).  A -> diag(eigenvalues), V columns = eigenvectors.
+__device__ void jacobi4(float A[4][4], float V[4][4])
+{
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.0f : 0.0f;
+    float fro = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) fro += A[i][j] * A[i][j];
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        float off = 0.0f;
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = p + 1; q < 4; ++q) off += A[p][q] * A[p][q];
+        if (off <= 1e-14f * fro) break;
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+#pragma unroll
+            for (int q = p + 1; q < 4; ++q) {
+                const float apq = A[p][q];
+                if (fabsf(apq) < 1e-30f) continue;
+                const float theta = (A[q][q] - A[p][p]) / (2.0f * apq);
+                const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.0f)));
+                const float c = rsqrtf(fmaf(t, t, 1.0f)), s = t * c;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - s * akq;
+                    A[k][q] = s * akp + c * akq;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - s * aqk;
+                    A[q][k] = s * apk + c * aqk;
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+        }
+    }
+}
+
+// Packed symmetric 6x6: 3 diagonal 2x2 blocks (xx, xy, yy) at 0..8, then
+// off-diagonal blocks (0,1), (0,2), (1,2) row-major at 9..20.
+__device__ __forceinline__ int pair_index(int a, int b) { return a + b - 1; }   // (0,1)->0 (0,2)->1 (1,2)->2
+
+__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, float* __restrict__ hb)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    const int nF = m.nF;
+    const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
+    // ---- FP64 element Hessian (SymDirichletEnergy.cpp:440-522) ----
+    const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
+    const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
+    const double area_U = 0.5 * (U2m1[0] * U3m1[1] - U2m1[1] * U3m1[0]);
+    const double A2 = m.A2[t];
+    const double areaRatio = A2 / area_U / area_U / area_U;
+    const double dAR = 1.5 * areaRatio / area_U;
+    const double w = uniform ? 1.0 : m.w[t];
+    // e0SqLen_div_dbAreaSq etc. (TriMesh.cpp:391-393)
+    const double e0d = m.e0d[t], e1d = m.e1d[t], e01d = m.e01d[t];
+    const double leftTerm = 1.0 + A2 / area_U / area_U;
+    const double rightTerm = ((U3m1[0] * U3m1[0] + U3m1[1] * U3m1[1]) * e0d +
+                              (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) * 0.5 -
+                             (U3m1[0] * U2m1[0] + U3m1[1] * U2m1[1]) * e01d;
+    double ort[3][2], dL[3][2], dR[3][2];
+    ort[0][0] = U[2].y - U[1].y; ort[0][1] = -(U[2].x - U[1].x);
+    ort[1][0] = U[0].y - U[2].y; ort[1][1] = -(U[0].x - U[2].x);
+    ort[2][0] = U[1].y - U[0].y; ort[2][1] = -(U[1].x - U[0].x);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { dL[k][0] = areaRatio * ort[k][0]; dL[k][1] = areaRatio * ort[k][1]; }
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        dR[0][c] = (e01d - e0d) * U3m1[c] + (e01d - e1d) * U2m1[c];
+        dR[1][c] = e1d * U2m1[c] - e01d * U3m1[c];
+        dR[2][c] = e0d * U3m1[c] - e01d * U2m1[c];
+    }
+    const double d2R[3][3] = {{e0d + e1d - 2.0 * e01d, e01d - e1d, e01d - e0d},
+                              {e01d - e1d, e1d, -e01d},
+                              {e01d - e0d, -e01d, e0d}};
+    const double skew[3][3] = {{0, 1, -1}, {-1, 0, 1}, {1, -1, 0}};
+    double H[6][6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = i; j < 3; ++j) {
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    double d2L = dAR * ort[i][a] * ort[j][b];
+                    if (i != j) d2L += areaRatio * skew[i][j] * ((a == 0 && b == 1) ? -1.0 : ((a == 1 && b == 0) ? 1.0 : 0.0));
+                    const double v = w * (d2L * rightTerm + dL[i][a] * dR[j][b] +
+                                          (a == b ? d2R[i][j] * leftTerm : 0.0) + dR[i][a] * dL[j][b]);
+                    H[2 * i + a][2 * j + b] = v;
+                    H[2 * j + b][2 * i + a] = v;
+                }
+            }
+        }
+    }
+    // ---- normalise, project to PSD in FP32 (IglUtils::makePD, IglUtils.hpp:71-90) ----
+    double hmax = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) hmax = fmax(hmax, fabs(H[i][j]));
+    const double inv = (hmax > 0.0 && hmax < 1e300) ? 1.0 / hmax : 1.0;
+    float Hf[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) Hf[i][j] = static_cast<float>(H[i][j] * inv);
+    // M = Q^T Hf Q
+    float HQ[6][4];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s = fmaf(Hf[i][k], qv(c, k), s);
+            HQ[i][c] = s;
+        }
+    float M[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s = fmaf(qv(r, k), HQ[k][c], s);
+            M[r][c] = s;
+        }
+    // PSD test by LDL^T pivots of M
+    bool pd = true;
+    {
+        float L[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) L[i][j] = M[i][j];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float d = L[k][k];
+            if (!(d > 0.0f)) pd = false;
+            const float id = (d > 0.0f) ? 1.0f / d : 0.0f;
+#pragma unroll
+            for (int i = k + 1; i < 4; ++i) {
+                const float f = L[i][k] * id;
+#pragma unroll
+                for (int j = k + 1; j < 4; ++j) L[i][j] -= f * L[k][j];
+            }
+        }
+    }
+    if (!pd) {
+        float V[4][4];
+        jacobi4(M, V);
+        float lam[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) lam[k] = fmaxf(M[k][k], 0.0f);
+        // Mp = V diag(lam) V^T ; Hf = Q Mp Q^T
+        float Mp[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float s = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) s = fmaf(V[r][k] * lam[k], V[c][k], s);
+                Mp[r][c] = s;
+            }
+        float QM[6][4];
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float s = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) s = fmaf(qv(k, i), Mp[k][c], s);
+                QM[i][c] = s;
+            }
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+                float s = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) s = fmaf(QM[i][k], qv(k, j), s);
+                Hf[i][j] = s;
+            }
+    }
+    const float sc = static_cast<float>(hmax > 0.0 && hmax < 1e300 ? hmax : 1.0);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        hb[(3 * a + 0) * (size_t)nF + t] = Hf[2 * a][2 * a] * sc;
+        hb[(3 * a + 1) * (size_t)nF + t] = 0.5f * (Hf[2 * a][2 * a + 1] + Hf[2 * a + 1][2 * a]) * sc;
+        hb[(3 * a + 2) * (size_t)nF + t] = Hf[2 * a + 1][2 * a + 1] * sc;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = a + 1; b < 3; ++b) {
+            const int p = pair_index(a, b);
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                    hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] =
+                        0.5f * (Hf[2 * a + i][2 * b + j] + Hf[2 * b + j][2 * a + i]) * sc;
+        }
+}
+
+__device__ __forceinline__ float4 local_block(const float* __restrict__ hb, int nF, int code)
+{
+    const int t = code / 9, ab = code - 9 * t, a = ab / 3, b = ab - 3 * a;
+    if (a == b) {
+        const float xx = hb[(3 * a) * (size_t)nF + t], xy = hb[(3 * a + 1) * (size_t)nF + t],
+                    yy = hb[(3 * a + 2) * (size_t)nF + t];
+        return make_float4(xx, xy, xy, yy);
+    }
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    const int base = 9 + 4 * pair_index(lo, hi);
+    const float h00 = hb[(base + 0) * (size_t)nF + t], h01 = hb[(base + 1) * (size_t)nF + t],
+                h10 = hb[(base + 2) * (size_t)nF + t], h11 = hb[(base + 3) * (size_t)nF + t];
+    return a < b ? make_float4(h00, h01, h10, h11) : make_float4(h00, h10, h01, h11);
+}
+
+__global__ void k_hessian_expand(const float* __restrict__ hb, int nF, double* __restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nF) return;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            const float4 B = local_block(hb, nF, t * 9 + a * 3 + b);
+            double* o = out + 36 * (size_t)t;
+            o[6 * (2 * a) + 2 * b] = B.x;
+            o[6 * (2 * a) + 2 * b + 1] = B.y;
+            o[6 * (2 * a + 1) + 2 * b] = B.z;
+            o[6 * (2 * a + 1) + 2 * b + 1] = B.w;
+        }
+}
+
+// One thread per block slot: fixed-order sum of its triangle contributions
+// (the device counterpart of LinSysSolver::update_a, LinSysSolver.hpp:138-159,
+// and Optimizer.cpp:825's energyParams scaling).
+__global__ void __launch_bounds__(256) k_assemble(DeviceBsr b, const float* __restrict__ hb, int nF, float scale)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nnzb) return;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int p = b.cPtr[s]; p < b.cPtr[s + 1]; ++p) {
+        const float4 B = local_block(hb, nF, b.cIdx[p]);
+        acc.x += B.x; acc.y += B.y; acc.z += B.z; acc.w += B.w;
+    }
+    b.val[s] = make_float4(acc.x * scale, acc.y * scale, acc.z * scale, acc.w * scale);
+}
+
+// Fixed rows: diagonal = energyParam * I (SymDirichletEnergy.cpp:541-548 scaled
+// at Optimizer.cpp:825); block-Jacobi inverse per row in FP64.
+__global__ void k_precond(DeviceBsr b, float fixedDiag, int* flag)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.nRows) return;
+    const int s = b.diagSlot[r];
+    if (b.rowFixed[r] && fixedDiag > 0.0f) b.val[s] = make_float4(fixedDiag, 0.f, 0.f, fixedDiag);
+    const float4 D = b.val[s];
+    const double a = D.x, bb = 0.5 * ((double)D.y + (double)D.z), d = D.w;
+    const double det = a * d - bb * bb;
+    if (a > 0.0 && det > 0.0) {
+        b.dinv[r] = Mat2d{d / det, -bb / det, -bb / det, a / det};
+    }
+    else {
+        // singular or indefinite diagonal block: fall back to a scaled identity
+        const double m = fmax(fabs(a), fabs(d));
+        const double iv = m > 0.0 ? 1.0 / m : 1.0;
+        b.dinv[r] = Mat2d{iv, 0.0, 0.0, iv};
+        atomicAdd(flag, 1);
+    }
+}
+
+__device__ __forceinline__ double2 row_spmv(const DeviceBsr& b, int r, const double2* __restrict__ x)
+{
+    double sx = 0.0, sy = 0.0;
+    const int e = b.rowPtr[r + 1];
+    for (int p = b.rowPtr[r]; p < e; ++p) {
+        const float4 A = b.val[p];
+        const double2 xv = x[b.col[p]];
+        sx = fma((double)A.x, xv.x, sx);
+        sx = fma((double)A.y, xv.y, sx);
+        sy = fma((double)A.z, xv.x, sy);
+        sy = fma((double)A.w, xv.y, sy);
+    }
+    return make_double2(sx, sy);
+}
+
+__global__ void k_spmv(DeviceBsr b, const double2* __restrict__ x, double2* __restrict__ y)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.nRows) return;
+    y[r] = row_spmv(b, r, x);
+}
+
+__device__ __forceinline__ double2 apply_dinv(const Mat2d M, const double2 v)
+{
+    return make_double2(M.a00 * v.x + M.a01 * v.y, M.a10 * v.x + M.a11 * v.y);
+}
+
+__device__ __forceinline__ double block_reduce_sum(double v, double* sh)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (warp == 0) {
+        s = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    }
+    __syncthreads();
+    return s;   // valid in thread 0
+}
+
+// Persistent block-Jacobi PCG in the Chronopoulos-Gear form: one SpMV and
+// one fused reduction (gamma = r.u, delta = w.u, ||r||^2) per iteration,
+// two grid-wide barriers per iteration.  Every block reduces the per-block
+// partials in the same fixed order, so all blocks take identical decisions
+// and the result is deterministic.  The loop is capped at maxIter.
+__global__ void __launch_bounds__(512) k_pcg(DeviceBsr b, const double2* __restrict__ rhs, double2* __restrict__ x,
+                                             double2* __restrict__ r, double2* __restrict__ p,
+                                             double2* __restrict__ z, double2* __restrict__ u,
+                                             double2* __restrict__ wv, double tol2, int maxIter, double rhsSign,
+                                             double* __restrict__ partials, int* status, double* outScalars)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[32];
+    __shared__ double bc[4];
+    const int n = b.nRows;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    for (int i = gtid; i < n; i += gstride) {
+        const double2 bi = make_double2(rhsSign * rhs[i].x, rhsSign * rhs[i].y);
+        x[i] = make_double2(0.0, 0.0);
+        r[i] = bi;
+        u[i] = apply_dinv(b.dinv[i], bi);
+        p[i] = make_double2(0.0, 0.0);
+        z[i] = make_double2(0.0, 0.0);
+    }
+    grid.sync();
+    double alphaPrev = 1.0, gammaPrev = 1.0;
+    double bb = -1.0, rr = 0.0;
+    int it = 0;
+    for (;; ++it) {
+        double gam = 0.0, del = 0.0, rrl = 0.0;
+        for (int i = gtid; i < n; i += gstride) {
+            const double2 wi = row_spmv(b, i, u);
+            const double2 ri = r[i], ui = u[i];
+            wv[i] = wi;
+            gam += ri.x * ui.x + ri.y * ui.y;
+            del += wi.x * ui.x + wi.y * ui.y;
+            rrl += ri.x * ri.x + ri.y * ri.y;
+        }
+        gam = block_reduce_sum(gam, sh);
+        del = block_reduce_sum(del, sh);
+        rrl = block_reduce_sum(rrl, sh);
+        if (threadIdx.x == 0) {
+            partials[4 * blockIdx.x + 0] = gam;
+            partials[4 * blockIdx.x + 1] = del;
+            partials[4 * blockIdx.x + 2] = rrl;
+        }
+        grid.sync();
+        if (threadIdx.x < 32) {
+            double g3[3] = {0.0, 0.0, 0.0};
+            for (int k = threadIdx.x; k < (int)gridDim.x; k += 32) {
+                g3[0] += partials[4 * k + 0];
+                g3[1] += partials[4 * k + 1];
+                g3[2] += partials[4 * k + 2];
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) g3[q] += __shfl_down_sync(0xffffffffu, g3[q], o);
+            if (threadIdx.x == 0) { bc[0] = g3[0]; bc[1] = g3[1]; bc[2] = g3[2]; }
+        }
+        __syncthreads();
+        gam = bc[0]; del = bc[1]; rr = bc[2];
+        if (bb < 0.0) bb = rr;
+        const bool done = (rr <= tol2 * bb) || !(rr == rr) || it >= maxIter;
+        if (done) break;
+        double beta, alpha;
+        if (it == 0) { beta = 0.0; alpha = gam / del; }
+        else { beta = gam / gammaPrev; alpha = gam / (del - beta * gam / alphaPrev); }
+        for (int i = gtid; i < n; i += gstride) {
+            const double2 ui = u[i], wi = wv[i];
+            double2 pi = p[i], zi = z[i], xi = x[i], ri = r[i];
+            pi.x = ui.x + beta * pi.x; pi.y = ui.y + beta * pi.y;
+            zi.x = wi.x + beta * zi.x; zi.y = wi.y + beta * zi.y;
+            xi.x += alpha * pi.x; xi.y += alpha * pi.y;
+            ri.x -= alpha * zi.x; ri.y -= alpha * zi.y;
+            p[i] = pi; z[i] = zi; x[i] = xi; r[i] = ri;
+            u[i] = apply_dinv(b.dinv[i], ri);
+        }
+        gammaPrev = gam;
+        alphaPrev = alpha;
+        grid.sync();
+    }
+    if (gtid == 0) {
+        status[0] = it;
+        status[1] = (rr <= tol2 * bb) ? 1 : 0;
+        outScalars[0] = rr;
+        outScalars[1] = bb;
+    }
+}
+
+} // namespace
+
+void launch_hessian(const DeviceMesh& m, int uniform, float* hb, cudaStream_t st)
+{
+    k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
+}
+
+void launch_hessian_expand(const float* hb, int nF, double* out, cudaStream_t st)
+{
+    k_hessian_expand<<<(nF + 255) / 256, 256, 0, st>>>(hb, nF, out);
+}
+
+void launch_assemble(const DeviceBsr& b, const float* hb, int nF, double scale, cudaStream_t st)
+{
+    k_assemble<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b, hb, nF, static_cast<float>(scale));
+}
+
+int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag)
+{
+    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, -1.0f, dFlag);
+    return 0;
+}
+
+void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag)
+{
+    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, static_cast<float>(fixedDiag), dFlag);
+}
+
+void launch_spmv(const DeviceBsr& b, const double2* x, double2* y, cudaStream_t st)
+{
+    k_spmv<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, x, y);
+}
+
+void pcg_alloc(PcgWork& wk, int nRows, int device)
+{
+    wk.n = nRows;
+    const size_t bytes = sizeof(double2) * (size_t)(nRows > 0 ? nRows : 1);
+    cudaMalloc(&wk.x, bytes);
+    cudaMalloc(&wk.r, bytes);
+    cudaMalloc(&wk.p, bytes);
+    cudaMalloc(&wk.z, bytes);
+    cudaMalloc(&wk.u, bytes);
+    cudaMalloc(&wk.w, bytes);
+    int nsm = 0, perSm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    wk.block = 512;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_pcg, wk.block, 0);
+    if (perSm > 2) perSm = 2;
+    if (perSm < 1) perSm = 1;
+    wk.grid = nsm * perSm;
+    const int need = (nRows + wk.block - 1) / wk.block;
+    if (wk.grid > need) wk.grid = need > 0 ? need : 1;
+    cudaMalloc(&wk.partials, sizeof(double) * 4 * (size_t)wk.grid + 4 * sizeof(double));
+    cudaMalloc(&wk.status, sizeof(int) * 4);
+}
+
+void pcg_free(PcgWork& wk)
+{
+    cudaFree(wk.x); cudaFree(wk.r); cudaFree(wk.p); cudaFree(wk.z); cudaFree(wk.u); cudaFree(wk.w);
+    cudaFree(wk.partials); cudaFree(wk.status);
+    wk = PcgWork{};
+}
+
+int pcg_solve(const DeviceBsr& b, const double2* rhs, double2* x, PcgWork& wk, double tol, int maxIter,
+              double rhsSign, cudaStream_t st, int* itersOut, double* relresOut, std::string* err)
+{
+    double* scal = wk.partials + 4 * (size_t)wk.grid;
+    double tol2 = tol * tol;
+    DeviceBsr bb = b;
+    double2* xo = x;
+    void* args[] = {&bb, (void*)&rhs, &xo, &wk.r, &wk.p, &wk.z, &wk.u, &wk.w, &tol2, &maxIter, &rhsSign,
+                    &wk.partials, &wk.status, &scal};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(wk.grid), dim3(wk.block), args, 0, st);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("PCG launch: ") + cudaGetErrorString(e);
+        return OC_ERR_CUDA;
+    }
+    int hs[4];
+    double hsc[2];
+    cudaMemcpyAsync(hs, wk.status, sizeof(int) * 2, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hsc, scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("PCG: ") + cudaGetErrorString(e);
+        return OC_ERR_CUDA;
+    }
+    if (itersOut) *itersOut = hs[0];
+    if (relresOut) *relresOut = hsc[1] > 0.0 ? std::sqrt(hsc[0] / hsc[1]) : 0.0;
+    return hs[1] ? 0 : OC_ERR_NOT_CONVERGED;
+}
+
+} // namespace oc

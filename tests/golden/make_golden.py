@@ -1,0 +1,101 @@
+"""Generates the golden vectors in tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_driver -- the reference's own sources compiled by
+oracle/ref/Makefile -- on seeded synthetic meshes (optcuts_gb300.meshes) and
+packs its dumps into one compressed .npz per case:
+
+    V_rest, UV0, F, fixedVert, bnd     initial state after the reference's
+                                       own cut + Tutte initialisation
+    rest, scalars                      TriMesh::computeFeatures constants
+    E_elem0, grad0                     per-triangle energy, gradient at UV0
+    H0_blocks, H0_tris                 per-triangle PSD-projected Hessians
+                                       (rebuilt from the reference's triplets)
+    dir0                               SimplicialLDLT Newton direction at UV0
+    trace_E, trace_gsq, trace_alpha    per-iteration Optimizer::solve(1) trace
+    UV_iters (small cases)             UV after every iteration
+
+Usage (needs the reference source tree; not part of the test run):
+    make -C oracle/ref && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from optcuts_gb300 import meshes  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+# case -> (mesh generator key, lambda, Newton iterations, max Hessian triangles, dump UV per iteration)
+CASES = {
+    "triangle": ("triangle", 0.999, 20, None, True),
+    "plane": ("plane", 0.999, 20, None, True),
+    "cube": ("cube", 0.999, 40, None, True),
+    "icosphere_320": ("icosphere_320", 0.999, 40, None, True),
+    "ellipsoid_2k": ("ellipsoid_2k", 0.999, 300, None, False),
+    "torus_768": ("torus_768", 0.999, 30, None, False),
+    "icosphere_5k": ("icosphere_5k", 0.999, 120, 512, False),
+}
+
+
+def per_tri_blocks(F, fixed, Hv, ntri):
+    """Per-triangle 6x6 blocks from the reference's triplet stream
+    (IglUtils::addBlockToMatrix appends free x free entries tri by tri)."""
+    fixed = set(int(v) for v in fixed)
+    out = np.zeros((ntri, 6, 6))
+    p = 0
+    for t in range(ntri):
+        idx = [a for a in range(3) if int(F[t, a]) not in fixed]
+        for a in idx:
+            for b in idx:
+                for i in range(2):
+                    for j in range(2):
+                        out[t, 2 * a + i, 2 * b + j] = Hv[p]
+                        p += 1
+    return out
+
+
+def run_case(name, key, lam, iters, hmax, states):
+    V, F = meshes.CONFIGS[key]()
+    with tempfile.TemporaryDirectory() as td:
+        obj = os.path.join(td, "mesh.obj")
+        meshes.write_obj(obj, V, F)
+        out = os.path.join(td, "out") + "/"
+        os.makedirs(out)
+        args = [DRIVER, obj, out, repr(lam), str(iters), "hess"] + (["states"] if states else [])
+        subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                       env=dict(os.environ, OC_REF_THREADS="1"))
+        ld = lambda n: np.load(out + n + ".npy")  # noqa: E731
+        Fm, fixed = ld("F"), ld("fixedVert")
+        nt = len(Fm) if hmax is None else min(hmax, len(Fm))
+        blocks = per_tri_blocks(Fm, fixed, ld("H0_V"), nt)
+        pack = dict(V_rest=ld("V_rest"), UV0=ld("UV0"), F=Fm, fixedVert=fixed, bnd=ld("bnd"),
+                    rest=ld("rest"), scalars=ld("scalars"), E_elem0=ld("E_elem0"), grad0=ld("grad0"),
+                    H0_blocks=blocks, dir0=ld("dir0"), trace_E=ld("trace_E"), trace_gsq=ld("trace_gsq"),
+                    trace_alpha=ld("trace_alpha"), trace_status=ld("trace_status"),
+                    mesh_V=V, mesh_F=F)
+        if states:
+            pack["UV_iters"] = ld("UV_iters")
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack)
+    return pack
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit("build the reference driver first: make -C oracle/ref")
+    for name, (key, lam, iters, hmax, states) in CASES.items():
+        p = run_case(name, key, lam, iters, hmax, states)
+        print("%-14s nV=%6d nF=%6d iters=%d E0=%.6g Elast=%.6g" % (
+            name, len(p["UV0"]), len(p["F"]), len(p["trace_E"]) - 1, p["trace_E"][0], p["trace_E"][-1]))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,99 @@
+"""The projected-Newton Optimizer on the GPU against the reference's traces.
+
+The reference solves each Newton system exactly (SimplicialLDLT); the GPU
+path uses block-Jacobi PCG to a relative residual of 1e-8.  At a Tutte start
+the Newton matrix has condition numbers near 1e14, so the search directions
+differ in near-null modes and the per-iteration energies separate by up to
+~10-20% in the first iterations (two exact LDL^T orderings already differ at
+1e-4); both runs converge to the same stationary energy, which is what these
+tests pin (relative 1e-4 .. 5e-3), together with the invariants: monotone
+energy, no inverted triangle, determinism."""
+import numpy as np
+import pytest
+
+import optcuts_gb300 as oc
+from conftest import SCAFFOLD_OFF
+
+pytestmark = pytest.mark.gpu
+
+
+def run(g, iters=400, **cfg):
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    par = 1.0 - g["scalars"][4]
+    opt = oc.Optimizer(m, [par], **cfg)
+    opt.precompute()
+    E = [opt.getLastEnergyVal()]
+    steps = []
+    status = 0
+    for _ in range(iters):
+        status = opt.solve(1)
+        E.append(opt.getLastEnergyVal())
+        steps.append(opt.last_step())
+        if status == 1:
+            break
+    return m, opt, np.array(E), steps, status
+
+
+@pytest.mark.parametrize("case,tol", [("cube", 1e-6), ("icosphere_320", 1e-4), ("ellipsoid_2k", 5e-3),
+                                      ("icosphere_5k", 1e-3)])
+def test_converged_energy_matches_reference(golden, case, tol):
+    g = golden(case)
+    m, opt, E, steps, status = run(g)
+    assert status == 1
+    assert E[0] == pytest.approx(g["trace_E"][0], rel=1e-14)
+    assert abs(E[-1] - g["trace_E"][-1]) / g["trace_E"][-1] < tol
+    assert np.all(np.diff(E) <= 0.0)                 # line search never accepts an increase
+    assert m.checkInversion()                        # zero flipped triangles
+    assert all(s["pcgRelRes"] <= 1e-8 for s in steps if s["pcgIters"] > 0)
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_OFF)
+def test_first_iterations_track_reference(golden, case):
+    g = golden(case)
+    _, _, E, _, _ = run(g, iters=10)
+    m = min(len(E), len(g["trace_E"]))
+    rel = np.abs(E[:m] - g["trace_E"][:m]) / g["trace_E"][:m]
+    assert rel[0] < 1e-14
+    assert rel.max() < 0.25, rel
+
+
+def test_deterministic(golden):
+    g = golden("icosphere_320")
+    m1, _, E1, _, _ = run(g, iters=6)
+    m2, _, E2, _, _ = run(g, iters=6)
+    np.testing.assert_array_equal(E1, E2)
+    np.testing.assert_array_equal(m1.V, m2.V)
+
+
+def test_converged_gradient_below_target(golden):
+    g = golden("icosphere_320")
+    m, opt, E, steps, status = run(g)
+    par = 1.0 - g["scalars"][4]
+    grad = par * oc.SymDirichletEnergy().computeGradient(m)
+    nV = len(g["UV0"])
+    target = par * (nV - 1) / nV * 1e-12
+    # stopped either by ||g||^2 < targetGRes or by the relative-decrease test
+    assert grad @ grad < target or steps[-1]["stepSize"] > 1e-3
+
+
+def test_inverted_start_rejected(golden):
+    g = golden("icosphere_320")
+    uv = g["UV0"].copy()
+    t = g["F"][3]
+    uv[t[0]], uv[t[1]] = g["UV0"][t[1]], g["UV0"][t[0]]
+    m = oc.TriMesh(g["V_rest"], uv, g["F"], g["fixedVert"])
+    opt = oc.Optimizer(m, [0.001])
+    with pytest.raises(oc.OCError) as e:
+        opt.precompute()
+    assert e.value.status == 2
+
+
+def test_energy_param_update(golden):
+    g = golden("icosphere_320")
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    opt = oc.Optimizer(m, [0.001])
+    opt.precompute()
+    e1 = opt.getLastEnergyVal()
+    opt.energyParams[0] = 0.002
+    opt.updateEnergyData()
+    assert opt.getLastEnergyVal() == pytest.approx(2 * e1, rel=1e-15)

@@ -1,0 +1,93 @@
+"""The CPU restatement (oracle/port) against the reference's own golden
+vectors (tests/golden/, generated from the compiled reference)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN_CASES, SCAFFOLD_OFF
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_rest_constants_exact(golden, case):
+    g = golden(case)
+    rest, sc = O.rest_constants(g["V_rest"], g["F"])
+    np.testing.assert_array_equal(rest, g["rest"])
+    np.testing.assert_array_equal(sc, g["scalars"][:3])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_energy_and_gradient_bit_exact(golden, case):
+    g = golden(case)
+    e = O.energy_elem(g["rest"], g["F"], g["UV0"])
+    np.testing.assert_array_equal(e, g["E_elem0"])
+    grad = O.gradient(g["rest"], g["F"], g["UV0"], g["fixedVert"])
+    np.testing.assert_array_equal(grad, g["grad0"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_hessian_blocks(golden, case):
+    g = golden(case)
+    ref = g["H0_blocks"]
+    H = O.hessian_blocks(g["rest"], g["F"], g["UV0"])[: len(ref)]
+    fixed = set(g["fixedVert"].tolist())
+    # the reference stream omits fixed-vertex rows/cols
+    for t in range(len(ref)):
+        keep = np.array([int(g["F"][t, k // 2]) not in fixed for k in range(6)])
+        H[t][~keep, :] = 0.0
+        H[t][:, ~keep] = 0.0
+    scale = np.abs(ref).reshape(len(ref), -1).max(axis=1)[:, None, None] + 1e-300
+    assert np.max(np.abs(H - ref) / scale) < 1e-10
+
+
+def scaffold_on(g):
+    # disks and cut-to-disk meshes start with the bijectivity scaffold on
+    # (main.cpp:1572); closed genus-0 meshes start with it off
+    return bool(g["scalars"][5])
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_OFF)
+def test_init_step_size_on_reference_direction(golden, case):
+    g = golden(case)
+    s = O.init_step_size(g["F"], g["UV0"], g["dir0"], 1.0)
+    assert 0.0 < s <= 1.0
+    if g["trace_alpha"][0] > 0 and abs(g["trace_alpha"][0] - 0.99 * s) > 1e-15 * s:
+        # the first trial was halved by the line search
+        r = g["trace_alpha"][0] / (0.99 * s)
+        assert abs(np.log2(r) - round(np.log2(r))) < 1e-9
+    else:
+        assert g["trace_alpha"][0] == pytest.approx(0.99 * s, rel=1e-15)
+
+
+def test_scaffold_flags(golden):
+    for c in GOLDEN_CASES:
+        assert scaffold_on(golden(c)) == (c not in SCAFFOLD_OFF)
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_OFF)
+def test_ldlt_direction_matches_reference(golden, case):
+    g = golden(case)
+    par = 1.0 - g["scalars"][4]
+    S = O.Solver(len(g["UV0"]), g["F"], g["fixedVert"], g["V_rest"])
+    S.factorize(O.hessian_blocks(g["rest"], g["F"], g["UV0"]), par)
+    d = S.solve(-par * g["grad0"])
+    # two exact factorizations (different orderings) of an ill-conditioned
+    # matrix agree only to ~cond * eps
+    rel = np.linalg.norm(d - g["dir0"]) / np.linalg.norm(g["dir0"])
+    assert rel < 5e-3, rel
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_OFF)
+def test_newton_trace_matches_reference(golden, case):
+    g = golden(case)
+    par = 1.0 - g["scalars"][4]
+    assert g["trace_status"][-1] == 1   # the reference ran to convergence
+    _, tr, st = O.newton(g["V_rest"], g["F"], g["fixedVert"], g["UV0"], par, 400)
+    assert st == 1
+    m = min(len(tr["E"]), len(g["trace_E"]), 11)
+    rel = np.abs(tr["E"][:m] - g["trace_E"][:m]) / g["trace_E"][:m]
+    assert rel[0] < 1e-14
+    # the trace is sensitive to the solver's rounding (cond ~ 1e14 at a Tutte
+    # start: two exact LDL^T orderings disagree at 1e-4 in the direction);
+    # the converged energy is not
+    assert rel.max() < 5e-3, rel
+    assert abs(tr["E"][-1] - g["trace_E"][-1]) / g["trace_E"][-1] < 1e-4
