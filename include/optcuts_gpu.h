@@ -85,9 +85,26 @@ int oc_sd_hessian_blocks(oc_mesh* mesh, int uniformWeight, double* blocks);
 int oc_sd_init_step_size(oc_mesh* mesh, const double* searchDir, double* stepSize);
 
 /* ---- LinSysSolver (LinSysSolver.hpp:22-187, EigenLibSolver.cpp:21-107) --
- * Full-symmetric 2x2-block CSR on the device, block-Jacobi PCG solve. */
+ * Full-symmetric 2x2-block CSR on the device.  Two solvers:
+ *   OC_SOLVER_DIRECT  multifrontal sparse Cholesky (FP64 fronts), the exact
+ *                     solve SimplicialLDLT performs in the reference (default)
+ *   OC_SOLVER_PCG     block-Jacobi preconditioned conjugate gradients */
+enum { OC_SOLVER_DIRECT = 0, OC_SOLVER_PCG = 1 };
 int oc_linsys_create(oc_ctx* ctx, oc_linsys** out);
 int oc_linsys_destroy(oc_linsys* ls);
+/* set_type(threadAmt, mtype) (LinSysSolver.hpp:35): selects the solver;
+ * call before set_pattern. */
+int oc_linsys_set_type(oc_linsys* ls, int solverKind);
+/* analyze_pattern() (EigenLibSolver.cpp:71-77): symbolic factorisation
+ * (nested dissection, front structure); set_pattern runs it implicitly. */
+int oc_linsys_analyze_pattern(oc_linsys* ls);
+/* Symbolic statistics of the direct solver: out[0..7] = fronts, tree levels,
+ * largest front rows, front pool doubles, factor flops, tiled launches,
+ * factor entries (sum of m*k), DOF. */
+int oc_linsys_stats(oc_linsys* ls, double* out8);
+/* The same symbolic analysis without any device call (host only). */
+int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
+                          double* out8);
 /* set_pattern(vNeighbor, fixedVert) (LinSysSolver.hpp:37-135): the vertex
  * adjacency is taken from the triangles F; fixed rows keep only the diagonal. */
 int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF,
@@ -95,10 +112,14 @@ int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF,
 /* update_a(I, J, V) (LinSysSolver.hpp:138-159): triplets with I <= J are summed
  * into the matrix (mirrored to the lower half), the rest are ignored. */
 int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* V, int nTriplets);
-/* factorize() (EigenLibSolver.cpp:80-93): builds the block-Jacobi preconditioner. */
+/* factorize() (EigenLibSolver.cpp:80-93): numeric Cholesky (direct) or the
+ * block-Jacobi preconditioner (PCG).  OC_ERR_NOT_SPD if a pivot or diagonal
+ * block was not positive (the factorisation still completes). */
 int oc_linsys_factorize(oc_linsys* ls);
-/* solve(rhs, result) (EigenLibSolver.cpp:96-107): PCG to relative residual
- * tol (<= 0: 1e-8) within maxIter (<= 0: 20000).  iters / relres may be NULL. */
+/* solve(rhs, result) (EigenLibSolver.cpp:96-107).  Direct: tol / maxIter are
+ * ignored, *iters = 0 and *relres = the computed relative residual.  PCG: to
+ * relative residual tol (<= 0: 1e-8) within maxIter (<= 0: 20000).  iters /
+ * relres may be NULL. */
 int oc_linsys_solve(oc_linsys* ls, const double* rhs, double* result, double tol, int maxIter,
                     int* iters, double* relres);
 /* multiply(x, Ax) (LinSysSolver.hpp:172-187) */
@@ -113,6 +134,7 @@ typedef struct {
     double relGL2Tol;     /* Optimizer.cpp:70, default 1e-12 */
     int lineSearchBatch;  /* trial step sizes per energy launch, 1..8, default 4 */
     int timing;           /* 1: record per-phase CUDA-event times */
+    int linearSolver;     /* OC_SOLVER_DIRECT (default) or OC_SOLVER_PCG */
 } oc_optimizer_config;
 
 int oc_optimizer_default_config(oc_optimizer_config* cfg);
@@ -132,15 +154,17 @@ int oc_optimizer_set_rel_gl2_tol(oc_optimizer* opt, double tol);
 /* energyParams[0] changed by the caller, then updateEnergyData(true, false,
  * false) (Optimizer.cpp:323-334; main.cpp:764). */
 int oc_optimizer_set_energy_param(oc_optimizer* opt, double energyParam);
-/* Last iteration's diagnostics: accepted step, PCG iterations and relative
- * residual, line-search energy launches, ||g||^2 at its start. */
+/* Last iteration's diagnostics: accepted step, PCG iterations (0 for the
+ * direct solver) and relative residual, line-search energy launches, ||g||^2
+ * at its start. */
 int oc_optimizer_last_step(oc_optimizer* opt, double* stepSize, int* pcgIters, double* pcgRelRes,
                            int* lineSearchLaunches, double* gradSqNorm);
 /* Per-phase device milliseconds accumulated since the last call (timing=1):
- * out[0..5] = gradient, hessian+projection, assembly+preconditioner, PCG,
- * injective step, line search.  Names match the reference's timer_step
- * buckets (main.cpp:1557-1565). */
-int oc_optimizer_phase_ms(oc_optimizer* opt, double* out6);
+ * out[0..6] = gradient, hessian+projection (matrixComputation), block
+ * assembly (matrixAssembly), numeric factorisation or PCG preconditioner
+ * (numericalFactorization), solve (backSolve), injective step, line search
+ * (lineSearch) -- the reference's timer_step buckets, main.cpp:1557-1565. */
+int oc_optimizer_phase_ms(oc_optimizer* opt, double* out7);
 /* Kernel launches this optimizer issued since creation (for accounting). */
 int oc_optimizer_launch_count(oc_optimizer* opt, long long* launches);
 

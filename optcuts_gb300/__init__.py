@@ -44,7 +44,11 @@ _vp = ctypes.c_void_p
 
 class OptimizerConfig(ctypes.Structure):
     _fields_ = [("pcgTol", ctypes.c_double), ("pcgMaxIter", ctypes.c_int), ("relGL2Tol", ctypes.c_double),
-                ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int)]
+                ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int), ("linearSolver", ctypes.c_int)]
+
+
+SOLVER_DIRECT = 0
+SOLVER_PCG = 1
 
 
 _SIGS = {
@@ -65,6 +69,10 @@ _SIGS = {
     "oc_sd_init_step_size": [_vp, _d, _d],
     "oc_linsys_create": [_vp, ctypes.POINTER(_vp)],
     "oc_linsys_destroy": [_vp],
+    "oc_linsys_set_type": [_vp, ctypes.c_int],
+    "oc_linsys_analyze_pattern": [_vp],
+    "oc_linsys_stats": [_vp, _d],
+    "oc_chol_analyze_stats": [ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_int, _d],
     "oc_linsys_set_pattern": [_vp, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int],
     "oc_linsys_update_a": [_vp, _i, _i, _d, ctypes.c_int],
     "oc_linsys_factorize": [_vp],
@@ -261,11 +269,12 @@ class LinSysSolver:
     """GPU block-CSR matrix + block-Jacobi PCG behind the reference's
     LinSysSolver interface (LinSysSolver.hpp:22-187)."""
 
-    def __init__(self, ctx=None):
+    def __init__(self, ctx=None, solver=SOLVER_DIRECT):
         self.ctx = ctx or default_context()
         h = _vp()
         self.ctx.check(lib().oc_linsys_create(self.ctx.h, ctypes.byref(h)), "LinSysSolver")
         self.h = h
+        self.ctx.check(lib().oc_linsys_set_type(h, int(solver)), "set_type")
         self.numRows = 0
         self.last_iters = 0
         self.last_relres = 0.0
@@ -280,7 +289,12 @@ class LinSysSolver:
         self.ctx.check(lib().oc_linsys_update_a(self.h, _pi(I), _pi(J), _pd(V), len(V)), "update_a")
 
     def analyze_pattern(self):
-        pass
+        self.ctx.check(lib().oc_linsys_analyze_pattern(self.h), "analyze_pattern")
+
+    def stats(self):
+        out = np.zeros(8)
+        self.ctx.check(lib().oc_linsys_stats(self.h, _pd(out)), "stats")
+        return symbolic_stats_dict(out)
 
     def factorize(self):
         return self.ctx.check(lib().oc_linsys_factorize(self.h), "factorize") == OC_OK
@@ -311,6 +325,22 @@ class LinSysSolver:
             self.close()
         except Exception:
             pass
+
+
+def symbolic_stats_dict(out):
+    keys = ["fronts", "levels", "max_front_rows", "pool_doubles", "flops", "launches", "factor_entries", "dof"]
+    return dict(zip(keys, [float(x) for x in out]))
+
+
+def chol_analyze_stats(nV, F, fixedVert=(0,), leafSize=16):
+    """Symbolic analysis of the direct solver, host only (no GPU needed)."""
+    F = _i4(F)
+    fx = _i4(np.asarray(fixedVert).reshape(-1))
+    out = np.zeros(8)
+    rc = lib().oc_chol_analyze_stats(int(nV), _pi(F), len(F), _pi(fx), len(fx), int(leafSize), _pd(out))
+    if rc != OC_OK:
+        raise OCError(rc, "oc_chol_analyze_stats")
+    return symbolic_stats_dict(out)
 
 
 def default_config(**kw):
@@ -371,10 +401,12 @@ class Optimizer:
         return {"stepSize": s.value, "pcgIters": it.value, "pcgRelRes": r.value, "lineSearchLaunches": ls.value,
                 "gradSqNorm": g.value}
 
+    PHASES = ["gradient", "hessian", "assembly", "factorize", "solve", "injective", "linesearch"]
+
     def phase_ms(self):
-        out = np.zeros(6)
+        out = np.zeros(7)
         self.ctx.check(lib().oc_optimizer_phase_ms(self.h, _pd(out)), "phase_ms")
-        return dict(zip(["gradient", "hessian", "assembly", "pcg", "injective", "linesearch"], out.tolist()))
+        return dict(zip(self.PHASES, out.tolist()))
 
     def launch_count(self):
         n = ctypes.c_longlong()

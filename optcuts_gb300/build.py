@@ -20,14 +20,18 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "liboc_gpu.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no FMA contraction (aarch64 GCC contracts by default), so the
+# host-side rest constants round exactly as the reference's do on x86-64
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+          "-Xcompiler", "-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 UNITS = {
     "oc_fp64.cu": ["-fmad=false"],
     "oc_kernels.cu": [],
+    "oc_chol.cu": [],
     "oc_api.cu": ["-Xcompiler", "-fvisibility=default"],
 }
-HEADERS = ["oc_internal.h"]
+HEADERS = ["oc_internal.h", "oc_chol.h"]
 
 
 def _newest_input():

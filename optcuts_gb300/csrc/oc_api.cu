@@ -4,6 +4,7 @@
 // EigenLibSolver, Optimizer).  No exception crosses the ABI; every entry
 // point returns an oc_status.
 
+#include "oc_chol.h"
 #include "oc_internal.h"
 
 #include <algorithm>
@@ -45,6 +46,8 @@ struct oc_linsys {
     int* dFlag = nullptr;
     double2 *tmpIn = nullptr, *tmpOut = nullptr;
     bool patternSet = false;
+    int kind = OC_SOLVER_DIRECT;
+    oc::CholPlan chol;
 };
 
 struct oc_optimizer {
@@ -60,8 +63,9 @@ struct oc_optimizer {
     double lastStep = 0.0, lastRelRes = 0.0, lastGsq = 0.0;
     int lastPcgIters = 0, lastLsLaunches = 0;
     long long launches = 0;
-    cudaEvent_t ev[8] = {};
-    double phaseMs[6] = {0, 0, 0, 0, 0, 0};
+    int badPivots = 0;
+    cudaEvent_t ev[9] = {};
+    double phaseMs[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -221,6 +225,37 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     ls->nV = nV;
     ls->nF = nF;
     ls->patternSet = true;
+    oc::chol_free(ls->chol);
+    if (ls->kind == OC_SOLVER_DIRECT) {
+        // analyze_pattern (EigenLibSolver.cpp:71-77): symbolic factorisation
+        oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data());
+        std::string err;
+        int rc = oc::chol_upload(ls->chol, &err);
+        if (rc) return fail(ctx, rc, err);
+    }
+    return OC_OK;
+}
+
+// numeric factorisation (direct) or preconditioner (PCG); fixedDiag > 0 sets
+// the fixed rows' diagonal blocks to fixedDiag * I first
+int linsys_factor(oc_linsys* ls, double fixedDiag, int* nBad)
+{
+    oc_ctx* ctx = ls->ctx;
+    cudaStream_t st = ctx->stream;
+    OC_CUDA(ctx, cudaMemsetAsync(ls->dFlag, 0, sizeof(int), st));
+    if (fixedDiag > 0.0) oc::launch_precond_fixed(ls->b, fixedDiag, st, ls->dFlag);
+    else oc::launch_precond(ls->b, st, ls->dFlag);
+    int bad = 0;
+    if (ls->kind == OC_SOLVER_DIRECT) {
+        std::string err;
+        int rc = oc::chol_factorize(ls->chol, ls->b, st, &err, &bad);
+        if (rc) return fail(ctx, rc, err);
+    }
+    else {
+        OC_CUDA(ctx, cudaMemcpyAsync(&bad, ls->dFlag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        OC_CUDA(ctx, cudaStreamSynchronize(st));
+    }
+    if (nBad) *nBad = bad;
     return OC_OK;
 }
 
@@ -545,8 +580,65 @@ int oc_linsys_destroy(oc_linsys* ls)
     if (!ls) return OC_ERR_INVALID;
     free_bsr(ls->b);
     oc::pcg_free(ls->wk);
+    oc::chol_free(ls->chol);
     cudaFree(ls->dFlag); cudaFree(ls->tmpIn); cudaFree(ls->tmpOut);
     delete ls;
+    return OC_OK;
+}
+
+int oc_linsys_set_type(oc_linsys* ls, int kind)
+{
+    if (!ls || (kind != OC_SOLVER_DIRECT && kind != OC_SOLVER_PCG)) return OC_ERR_INVALID;
+    ls->kind = kind;
+    return OC_OK;
+}
+
+int oc_linsys_analyze_pattern(oc_linsys* ls)
+{
+    if (!ls || !ls->patternSet) return OC_ERR_INVALID;
+    if (ls->kind != OC_SOLVER_DIRECT || ls->chol.onDevice) return OC_OK;
+    oc::chol_analyze(ls->chol, ls->nV, ls->rowPtr.data(), ls->col.data());
+    std::string err;
+    int rc = oc::chol_upload(ls->chol, &err);
+    return rc ? fail(ls->ctx, rc, err) : OC_OK;
+}
+
+static void chol_stats(const oc::CholPlan& P, double* out)
+{
+    double entries = 0.0;
+    for (int f = 0; f < P.nFronts; ++f) entries += (double)P.fm[f] * P.fk[f];
+    out[0] = P.nFronts;
+    out[1] = P.nLevels;
+    out[2] = P.maxM;
+    out[3] = (double)P.poolSize;
+    out[4] = P.flops;
+    out[5] = (double)P.launches.size();
+    out[6] = entries;
+    out[7] = P.nDof;
+}
+
+int oc_linsys_stats(oc_linsys* ls, double* out8)
+{
+    if (!ls || !out8 || !ls->patternSet || ls->kind != OC_SOLVER_DIRECT) return OC_ERR_INVALID;
+    chol_stats(ls->chol, out8);
+    return OC_OK;
+}
+
+int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize, double* out8)
+{
+    if (nV <= 0 || nF < 0 || (nF && !F) || nFixed < 0 || (nFixed && !fixedVert) || !out8) return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
+    std::vector<unsigned char> mask(nV, 0);
+    for (int i = 0; i < nFixed; ++i) {
+        if (fixedVert[i] < 0 || fixedVert[i] >= nV) return OC_ERR_INVALID;
+        mask[fixedVert[i]] = 1;
+    }
+    std::vector<int> rowPtr, col, diagSlot, cPtr, cIdx;
+    build_pattern(nV, F, nF, mask, rowPtr, col, diagSlot, cPtr, cIdx);
+    oc::CholPlan P;
+    oc::chol_analyze(P, nV, rowPtr.data(), col.data(), leafSize > 0 ? leafSize : 16);
+    chol_stats(P, out8);
     return OC_OK;
 }
 
@@ -598,12 +690,10 @@ int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* 
 int oc_linsys_factorize(oc_linsys* ls)
 {
     if (!ls || !ls->patternSet) return OC_ERR_INVALID;
-    OC_CUDA(ls->ctx, cudaMemsetAsync(ls->dFlag, 0, sizeof(int), ls->ctx->stream));
-    oc::launch_precond(ls->b, ls->ctx->stream, ls->dFlag);
-    int flag = 0;
-    OC_CUDA(ls->ctx, cudaMemcpyAsync(&flag, ls->dFlag, sizeof(int), cudaMemcpyDeviceToHost, ls->ctx->stream));
-    OC_CUDA(ls->ctx, cudaStreamSynchronize(ls->ctx->stream));
-    return flag ? fail(ls->ctx, OC_ERR_NOT_SPD, "factorize: non-positive diagonal block") : OC_OK;
+    int bad = 0;
+    int rc = linsys_factor(ls, -1.0, &bad);
+    if (rc) return rc;
+    return bad ? fail(ls->ctx, OC_ERR_NOT_SPD, "factorize: non-positive pivot or diagonal block") : OC_OK;
 }
 
 int oc_linsys_solve(oc_linsys* ls, const double* rhs, double* result, double tol, int maxIter, int* iters,
@@ -612,12 +702,34 @@ int oc_linsys_solve(oc_linsys* ls, const double* rhs, double* result, double tol
     if (!ls || !ls->patternSet || !rhs || !result) return OC_ERR_INVALID;
     if (!(tol > 0.0)) tol = 1e-8;
     if (maxIter <= 0) maxIter = 20000;
-    OC_CUDA(ls->ctx, cudaMemcpyAsync(ls->tmpIn, rhs, sizeof(double2) * ls->nV, cudaMemcpyHostToDevice, ls->ctx->stream));
+    cudaStream_t st = ls->ctx->stream;
+    OC_CUDA(ls->ctx, cudaMemcpyAsync(ls->tmpIn, rhs, sizeof(double2) * ls->nV, cudaMemcpyHostToDevice, st));
     std::string err;
-    int rc = oc::pcg_solve(ls->b, ls->tmpIn, ls->tmpOut, ls->wk, tol, maxIter, 1.0, ls->ctx->stream, iters, relres, &err);
-    if (rc == OC_ERR_CUDA) return fail(ls->ctx, rc, err);
-    OC_CUDA(ls->ctx, cudaMemcpyAsync(result, ls->tmpOut, sizeof(double2) * ls->nV, cudaMemcpyDeviceToHost, ls->ctx->stream));
-    OC_CUDA(ls->ctx, cudaStreamSynchronize(ls->ctx->stream));
+    int rc;
+    if (ls->kind == OC_SOLVER_DIRECT) {
+        rc = oc::chol_solve(ls->chol, ls->tmpIn, ls->tmpOut, 1.0, st, &err);
+        if (rc) return fail(ls->ctx, rc, err);
+        if (iters) *iters = 0;
+    }
+    else {
+        rc = oc::pcg_solve(ls->b, ls->tmpIn, ls->tmpOut, ls->wk, tol, maxIter, 1.0, st, iters, relres, &err);
+        if (rc == OC_ERR_CUDA) return fail(ls->ctx, rc, err);
+    }
+    OC_CUDA(ls->ctx, cudaMemcpyAsync(result, ls->tmpOut, sizeof(double2) * ls->nV, cudaMemcpyDeviceToHost, st));
+    OC_CUDA(ls->ctx, cudaStreamSynchronize(st));
+    if (ls->kind == OC_SOLVER_DIRECT && relres) {
+        // relative residual ||rhs - A x|| / ||rhs|| of the computed solution
+        oc::launch_spmv(ls->b, ls->tmpOut, ls->tmpIn, st);
+        std::vector<double> ax(2 * (size_t)ls->nV);
+        OC_CUDA(ls->ctx, cudaMemcpyAsync(ax.data(), ls->tmpIn, sizeof(double2) * ls->nV, cudaMemcpyDeviceToHost, st));
+        OC_CUDA(ls->ctx, cudaStreamSynchronize(st));
+        double rr = 0.0, bb = 0.0;
+        for (size_t i = 0; i < ax.size(); ++i) {
+            rr += (rhs[i] - ax[i]) * (rhs[i] - ax[i]);
+            bb += rhs[i] * rhs[i];
+        }
+        *relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+    }
     return rc;
 }
 
@@ -641,6 +753,7 @@ int oc_optimizer_default_config(oc_optimizer_config* c)
     c->relGL2Tol = 1e-12;
     c->lineSearchBatch = 4;
     c->timing = 0;
+    c->linearSolver = OC_SOLVER_DIRECT;
     return OC_OK;
 }
 
@@ -663,7 +776,9 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
     int rc = OC_OK;
     if (dalloc(&o->g, nV) != cudaSuccess || dalloc(&o->dir, nV) != cudaSuccess || dalloc(&o->uv0, nV) != cudaSuccess)
         rc = fail(ctx, OC_ERR_CUDA, "optimizer alloc");
+    if (o->cfg.linearSolver != OC_SOLVER_PCG) o->cfg.linearSolver = OC_SOLVER_DIRECT;
     if (rc == OC_OK) rc = oc_linsys_create(ctx, &o->ls);
+    if (rc == OC_OK) rc = oc_linsys_set_type(o->ls, o->cfg.linearSolver);
     if (rc == OC_OK && o->cfg.timing)
         for (auto& e : o->ev) cudaEventCreate(&e);
     if (rc != OC_OK) {
@@ -757,32 +872,46 @@ static int solve_one(oc_optimizer* o, int* converged)
         }
         return OC_OK;
     }
-    // Hessian, projection, assembly, preconditioner
+    // Hessian + PSD projection (computeHessian), block assembly (update_a)
     oc::launch_hessian(m->d, 0, m->hb, st);
     record(o, 2);
     oc::launch_assemble(o->ls->b, m->hb, m->d.nF, o->param, st);
-    oc::launch_precond_fixed(o->ls->b, o->param, st, o->ls->dFlag);
-    o->launches += 3;
+    o->launches += 2;
     record(o, 3);
+    // factorize (direct) or block-Jacobi preconditioner (PCG); fixed rows = param * I
+    int bad = 0;
+    rc = linsys_factor(o->ls, o->param, &bad);
+    if (rc) return rc;
+    o->badPivots = bad;
+    o->launches += 1 + (o->ls->kind == OC_SOLVER_DIRECT ? 3 + (long long)o->ls->chol.launches.size() : 0);
+    record(o, 4);
     // search direction: H d = -g
     std::string err;
     int iters = 0;
     double relres = 0.0;
-    rc = oc::pcg_solve(o->ls->b, o->g, o->dir, o->ls->wk, o->cfg.pcgTol, o->cfg.pcgMaxIter, -1.0, st, &iters,
-                       &relres, &err);
-    o->launches += 1;
-    if (rc == OC_ERR_CUDA) return fail(ctx, rc, err);
-    const int pcgStatus = rc;
+    int solveStatus = OC_OK;
+    if (o->ls->kind == OC_SOLVER_DIRECT) {
+        rc = oc::chol_solve(o->ls->chol, o->g, o->dir, -1.0, st, &err);
+        if (rc) return fail(ctx, rc, err);
+        o->launches += 2 + 2LL * o->ls->chol.nLevels;
+    }
+    else {
+        rc = oc::pcg_solve(o->ls->b, o->g, o->dir, o->ls->wk, o->cfg.pcgTol, o->cfg.pcgMaxIter, -1.0, st, &iters,
+                           &relres, &err);
+        o->launches += 1;
+        if (rc == OC_ERR_CUDA) return fail(ctx, rc, err);
+        solveStatus = rc;
+    }
     o->lastPcgIters = iters;
     o->lastRelRes = relres;
-    record(o, 4);
+    record(o, 5);
     // Optimizer::lineSearch: injective bound, then halve until E <= E_last
     oc::launch_init_step(m->d, o->dir, 1.0, m->scratch, st);
     o->launches += 2;
     double step = 1.0;
     rc = read_min(m, &step);
     if (rc) return rc;
-    record(o, 5);
+    record(o, 6);
     step *= 0.99;
     OC_CUDA(ctx, cudaMemcpyAsync(o->uv0, m->d.uv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToDevice, st));
     bool stopped = false;
@@ -818,7 +947,7 @@ static int solve_one(oc_optimizer* o, int* converged)
     oc::launch_step_forward(o->uv0, o->dir, accepted, m->d.uv, m->d.nV, st);
     o->launches += 1;
     OC_CUDA(ctx, cudaGetLastError());
-    record(o, 6);
+    record(o, 7);
     o->lastEDec = o->lastEnergyVal - testE;
     if ((o->lastEDec / o->lastEnergyVal < 1.0e-6 * accepted) && (accepted > 1.0e-3)) stopped = true;   // :635-638
     o->lastEnergyVal = testE;
@@ -826,18 +955,15 @@ static int solve_one(oc_optimizer* o, int* converged)
     o->lastLsLaunches = lsLaunches;
     o->globalIterNum++;
     if (o->cfg.timing) {
-        cudaEventSynchronize(o->ev[6]);
-        float ms[6] = {0, 0, 0, 0, 0, 0};
-        cudaEventElapsedTime(&ms[0], o->ev[0], o->ev[1]);
-        cudaEventElapsedTime(&ms[1], o->ev[1], o->ev[2]);
-        cudaEventElapsedTime(&ms[2], o->ev[2], o->ev[3]);
-        cudaEventElapsedTime(&ms[3], o->ev[3], o->ev[4]);
-        cudaEventElapsedTime(&ms[4], o->ev[4], o->ev[5]);
-        cudaEventElapsedTime(&ms[5], o->ev[5], o->ev[6]);
-        for (int k = 0; k < 6; ++k) o->phaseMs[k] += ms[k];
+        cudaEventSynchronize(o->ev[7]);
+        for (int k = 0; k < 7; ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, o->ev[k], o->ev[k + 1]);
+            o->phaseMs[k] += ms;
+        }
     }
     *converged = stopped ? 1 : 0;
-    return pcgStatus == OC_ERR_NOT_CONVERGED ? OC_ERR_NOT_CONVERGED : OC_OK;
+    return solveStatus == OC_ERR_NOT_CONVERGED ? OC_ERR_NOT_CONVERGED : OC_OK;
 }
 
 int oc_optimizer_solve(oc_optimizer* o, int maxIter, int* result)
@@ -902,11 +1028,11 @@ int oc_optimizer_last_step(oc_optimizer* o, double* stepSize, int* pcgIters, dou
     return OC_OK;
 }
 
-int oc_optimizer_phase_ms(oc_optimizer* o, double* out6)
+int oc_optimizer_phase_ms(oc_optimizer* o, double* out7)
 {
-    if (!o || !out6) return OC_ERR_INVALID;
-    for (int k = 0; k < 6; ++k) {
-        out6[k] = o->phaseMs[k];
+    if (!o || !out7) return OC_ERR_INVALID;
+    for (int k = 0; k < 7; ++k) {
+        out7[k] = o->phaseMs[k];
         o->phaseMs[k] = 0.0;
     }
     return OC_OK;

@@ -1,0 +1,670 @@
+// Multifrontal sparse Cholesky on the device -- the exact Newton solve.
+//
+// The reference factorises the Newton matrix with Eigen's SimplicialLDLT
+// (src/LinSysSolver/EigenLibSolver.cpp:71-107) on one host thread; at
+// 200k triangles that is ~94% of its iteration time.  Block-Jacobi PCG does
+// not converge on these systems (a Tutte start has condition numbers near
+// 1e14), so the default solver here is an exact factorisation too:
+//
+//  * symbolic (host, once per topology): nested dissection of the vertex
+//    graph by BFS level sets; each dissection node is one dense front whose
+//    rows are its own vertices followed by the ancestor vertices its subtree
+//    touches; per-topology maps for assembling the block-CSR values into the
+//    fronts, for the children's extend-add and for the tiled kernels' work;
+//  * numeric (device, every iteration): fronts are processed bottom-up one
+//    tree level at a time; within a level every front is factorised by the
+//    same batched tile kernels (32 x 32 FP64 tiles: diagonal Cholesky,
+//    triangular solve of the panel, trailing update), so one launch serves
+//    all fronts of a level;
+//  * solve: forward and backward substitution front by front, level by
+//    level, with the children's update vectors extend-added in a fixed
+//    order (deterministic, no atomics).
+//
+// All arithmetic is FP64.  A non-positive pivot (the matrix is PSD by
+// construction; a pivot can only vanish in rounding) is replaced by its
+// magnitude (or 1e-300) and counted.
+
+#include "oc_chol.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <functional>
+#include <numeric>
+
+namespace oc {
+
+// ------------------------------------------------------------------ symbolic
+namespace {
+
+struct NdNode {
+    std::vector<int> S;
+    std::vector<int> children;
+};
+
+// Nested dissection of `verts` (all with tag == curTag on entry) by BFS
+// level sets from a pseudo-peripheral vertex.  Returns the node id.
+int nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::vector<int>& tag, int& tagCounter,
+             std::vector<int>& level, std::vector<NdNode>& nodes, int leafSize)
+{
+    const int myTag = ++tagCounter;
+    for (int v : verts) tag[v] = myTag;
+    auto make_leaf = [&]() {
+        nodes.push_back(NdNode{verts, {}});
+        return static_cast<int>(nodes.size()) - 1;
+    };
+    if ((int)verts.size() <= leafSize) return make_leaf();
+    // two BFS passes: the second starts at the last vertex reached by the first
+    std::vector<int> q;
+    q.reserve(verts.size());
+    auto bfs = [&](int s) {
+        q.clear();
+        for (int v : verts) level[v] = -1;
+        level[s] = 0;
+        q.push_back(s);
+        for (size_t h = 0; h < q.size(); ++h) {
+            const int v = q[h];
+            for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p) {
+                const int u = col[p];
+                if (tag[u] == myTag && level[u] < 0) {
+                    level[u] = level[v] + 1;
+                    q.push_back(u);
+                }
+            }
+        }
+    };
+    bfs(verts[0]);
+    bfs(q.back());
+    const int reached = static_cast<int>(q.size());
+    const int maxLevel = level[q.back()];
+    if (maxLevel < 2) return make_leaf();
+    std::vector<int> cnt(maxLevel + 1, 0);
+    for (int i = 0; i < reached; ++i) cnt[level[q[i]]]++;
+    const int total = static_cast<int>(verts.size());
+    int sepLevel = 1, cum = 0;
+    for (int l = 0; l <= maxLevel; ++l) {
+        cum += cnt[l];
+        if (2 * cum >= total) { sepLevel = l; break; }
+    }
+    sepLevel = std::max(1, std::min(sepLevel, maxLevel - 1));
+    std::vector<int> left, right, sep;
+    for (int v : verts) {
+        const int l = level[v];
+        if (l < 0 || l > sepLevel) right.push_back(v);
+        else if (l < sepLevel) left.push_back(v);
+        else sep.push_back(v);
+    }
+    if (sep.empty() || (left.empty() && right.empty())) return make_leaf();
+    std::vector<int> kids;
+    if (!left.empty()) kids.push_back(nd_build(rowPtr, col, left, tag, tagCounter, level, nodes, leafSize));
+    if (!right.empty()) kids.push_back(nd_build(rowPtr, col, right, tag, tagCounter, level, nodes, leafSize));
+    nodes.push_back(NdNode{std::move(sep), std::move(kids)});
+    return static_cast<int>(nodes.size()) - 1;
+}
+
+int tiles_of(int k, int m) { return (k + kTile - 1) / kTile + (m - k + kTile - 1) / kTile; }
+
+} // namespace
+
+void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize)
+{
+    P = CholPlan{};
+    P.nV = nV;
+    P.nDof = 2 * nV;
+    std::vector<NdNode> nodes;
+    std::vector<int> tag(nV, 0), level(nV, -1);
+    int tagCounter = 0;
+    // components: run the dissection on every connected set of vertices
+    std::vector<int> roots;
+    {
+        std::vector<char> seen(nV, 0);
+        for (int s = 0; s < nV; ++s) {
+            if (seen[s]) continue;
+            std::vector<int> comp{s};
+            seen[s] = 1;
+            for (size_t h = 0; h < comp.size(); ++h) {
+                const int v = comp[h];
+                for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p)
+                    if (!seen[col[p]]) { seen[col[p]] = 1; comp.push_back(col[p]); }
+            }
+            roots.push_back(nd_build(rowPtr, col, comp, tag, tagCounter, level, nodes, leafSize));
+        }
+    }
+    // nodes are created children-first: creation order is a postorder
+    const int nF = static_cast<int>(nodes.size());
+    P.nFronts = nF;
+    std::vector<int> parent(nF, -1);
+    for (int f = 0; f < nF; ++f)
+        for (int c : nodes[f].children) parent[c] = f;
+    std::vector<int> pos(nV, -1);
+    P.vertOrder.reserve(nV);
+    std::vector<int> vstart(nF);
+    for (int f = 0; f < nF; ++f) {
+        vstart[f] = static_cast<int>(P.vertOrder.size());
+        for (int v : nodes[f].S) {
+            pos[v] = static_cast<int>(P.vertOrder.size());
+            P.vertOrder.push_back(v);
+        }
+    }
+    P.permDof.resize(P.nDof);
+    for (int k = 0; k < nV; ++k) {
+        P.permDof[2 * k] = 2 * P.vertOrder[k];
+        P.permDof[2 * k + 1] = 2 * P.vertOrder[k] + 1;
+    }
+    // boundary sets (ancestor vertices each subtree touches), bottom-up
+    std::vector<std::vector<int>> B(nF);
+    for (int f = 0; f < nF; ++f) {
+        const int last = vstart[f] + static_cast<int>(nodes[f].S.size()) - 1;
+        std::vector<int> cand;
+        for (int v : nodes[f].S)
+            for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p)
+                if (pos[col[p]] > last) cand.push_back(pos[col[p]]);
+        for (int c : nodes[f].children)
+            for (int u : B[c])
+                if (u > last) cand.push_back(u);
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        B[f] = std::move(cand);   // elimination positions, ascending
+    }
+    // fronts
+    P.fk.resize(nF); P.fm.resize(nF); P.fparent = parent; P.flevel.assign(nF, 0); P.fdofStart.resize(nF);
+    P.foff.resize(nF); P.fupd.resize(nF); P.frowOff.resize(nF); P.relOff.resize(nF);
+    P.childOff.assign(nF + 1, 0);
+    long long pool = 0, upd = 0;
+    for (int f = 0; f < nF; ++f) {
+        const int ns = static_cast<int>(nodes[f].S.size());
+        const int k = 2 * ns, m = 2 * (ns + static_cast<int>(B[f].size()));
+        P.fk[f] = k;
+        P.fm[f] = m;
+        P.fdofStart[f] = 2 * vstart[f];
+        P.foff[f] = pool;
+        pool += (long long)m * m;
+        P.fupd[f] = upd;
+        upd += m - k;
+        P.frowOff[f] = static_cast<int>(P.rowIdx.size());
+        for (int i = 0; i < ns; ++i) { P.rowIdx.push_back(2 * (vstart[f] + i)); P.rowIdx.push_back(2 * (vstart[f] + i) + 1); }
+        for (int u : B[f]) { P.rowIdx.push_back(2 * u); P.rowIdx.push_back(2 * u + 1); }
+        P.maxM = std::max(P.maxM, m);
+        int lv = 0;
+        for (int c : nodes[f].children) lv = std::max(lv, P.flevel[c] + 1);
+        P.flevel[f] = lv;
+        P.childOff[f + 1] = P.childOff[f] + static_cast<int>(nodes[f].children.size());
+        const double kk = k, mm = m, r = mm - kk;
+        P.flops += kk * kk * kk / 3.0 + kk * kk * r + kk * r * r;
+    }
+    P.poolSize = pool;
+    P.updSize = upd;
+    for (int f = 0; f < nF; ++f)
+        for (int c : nodes[f].children) P.childList.push_back(c);
+    // child update row -> parent row (both row lists ascending)
+    for (int f = 0; f < nF; ++f) {
+        P.relOff[f] = static_cast<int>(P.relIdx.size());
+        const int pf = parent[f];
+        if (pf < 0) continue;
+        const int* prow = P.rowIdx.data() + P.frowOff[pf];
+        const int pm = P.fm[pf];
+        for (int i = P.fk[f]; i < P.fm[f]; ++i) {
+            const int dof = P.rowIdx[P.frowOff[f] + i];
+            const int* it = std::lower_bound(prow, prow + pm, dof);
+            P.relIdx.push_back(static_cast<int>(it - prow));
+        }
+    }
+    // levels
+    for (int f = 0; f < nF; ++f) P.nLevels = std::max(P.nLevels, P.flevel[f] + 1);
+    P.levelFrontOff.assign(P.nLevels + 1, 0);
+    for (int f = 0; f < nF; ++f) P.levelFrontOff[P.flevel[f] + 1]++;
+    for (int l = 0; l < P.nLevels; ++l) P.levelFrontOff[l + 1] += P.levelFrontOff[l];
+    P.levelFronts.resize(nF);
+    {
+        std::vector<int> fill(P.levelFrontOff.begin(), P.levelFrontOff.end() - 1);
+        for (int f = 0; f < nF; ++f) P.levelFronts[fill[P.flevel[f]]++] = f;
+    }
+    // launch schedule: per level, extend-add per child slot, then per panel
+    // the diagonal-tile Cholesky, the panel solve and the trailing update
+    for (int l = 0; l < P.nLevels; ++l) {
+        const int* lf = P.levelFronts.data() + P.levelFrontOff[l];
+        const int nl = P.levelFrontOff[l + 1] - P.levelFrontOff[l];
+        int maxKids = 0, maxPanels = 0;
+        for (int i = 0; i < nl; ++i) {
+            const int f = lf[i];
+            maxKids = std::max(maxKids, P.childOff[f + 1] - P.childOff[f]);
+            maxPanels = std::max(maxPanels, (P.fk[f] + kTile - 1) / kTile);
+        }
+        for (int c = 0; c < maxKids; ++c) {
+            const int off = static_cast<int>(P.tasks.size());
+            for (int i = 0; i < nl; ++i) {
+                const int f = lf[i];
+                if (P.childOff[f + 1] - P.childOff[f] <= c) continue;
+                const int ch = P.childList[P.childOff[f] + c];
+                const int u = P.fm[ch] - P.fk[ch];
+                for (int j0 = 0; j0 < u; j0 += 16) P.tasks.push_back(TileTask{ch, f, j0, std::min(j0 + 16, u)});
+            }
+            const int cnt = static_cast<int>(P.tasks.size()) - off;
+            if (cnt) P.launches.push_back({0, l, 0, off, cnt, c});
+        }
+        for (int p = 0; p < maxPanels; ++p) {
+            int off = static_cast<int>(P.tasks.size());
+            for (int i = 0; i < nl; ++i) {
+                const int f = lf[i];
+                if ((P.fk[f] + kTile - 1) / kTile > p) P.tasks.push_back(TileTask{f, p, p, p});
+            }
+            if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
+            off = static_cast<int>(P.tasks.size());
+            for (int i = 0; i < nl; ++i) {
+                const int f = lf[i];
+                if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
+                const int nt = tiles_of(P.fk[f], P.fm[f]);
+                for (int ti = p + 1; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, p, p});
+            }
+            if ((int)P.tasks.size() > off) P.launches.push_back({2, l, p, off, (int)P.tasks.size() - off, 0});
+            off = static_cast<int>(P.tasks.size());
+            for (int i = 0; i < nl; ++i) {
+                const int f = lf[i];
+                if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
+                const int nt = tiles_of(P.fk[f], P.fm[f]);
+                for (int tj = p + 1; tj < nt; ++tj)
+                    for (int ti = tj; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, tj, p});
+            }
+            if ((int)P.tasks.size() > off) P.launches.push_back({3, l, p, off, (int)P.tasks.size() - off, 0});
+        }
+    }
+    // assembly map: block slot (r, c) with pos[r] >= pos[c] goes to the front owning c
+    std::vector<int> owner(nV);
+    for (int f = 0; f < nF; ++f)
+        for (int v : nodes[f].S) owner[v] = f;
+    const int nnzb = rowPtr[nV];
+    P.asmDest.assign(nnzb, -1);
+    P.asmLd.assign(nnzb, 0);
+    P.asmDiag.assign(nnzb, 0);
+    for (int r = 0; r < nV; ++r)
+        for (int s = rowPtr[r]; s < rowPtr[r + 1]; ++s) {
+            const int c = col[s];
+            if (pos[r] < pos[c]) continue;
+            const int f = owner[c];
+            const int m = P.fm[f];
+            const int jc = 2 * (pos[c] - vstart[f]);
+            const int* prow = P.rowIdx.data() + P.frowOff[f];
+            const int ir = static_cast<int>(std::lower_bound(prow, prow + m, 2 * pos[r]) - prow);
+            P.asmDest[s] = P.foff[f] + ir + (long long)jc * m;
+            P.asmLd[s] = m;
+            P.asmDiag[s] = (r == c) ? 1 : 0;
+        }
+}
+
+// ------------------------------------------------------------------ kernels
+namespace {
+
+__device__ __forceinline__ void tile_bounds(int k, int m, int t, int& start, int& len)
+{
+    const int nP = (k + kTile - 1) / kTile;
+    if (t < nP) {
+        start = t * kTile;
+        len = min(kTile, k - start);
+    }
+    else {
+        start = k + (t - nP) * kTile;
+        len = min(kTile, m - start);
+    }
+}
+
+__global__ void k_asm_fronts(const float4* __restrict__ val, const long long* __restrict__ dest,
+                             const int* __restrict__ ld, const unsigned char* __restrict__ diag, int nnzb,
+                             double* __restrict__ pool)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nnzb) return;
+    const long long d = dest[s];
+    if (d < 0) return;
+    const float4 v = val[s];
+    const long long m = ld[s];
+    pool[d] = v.x;
+    pool[d + 1] = v.z;
+    pool[d + 1 + m] = v.w;
+    if (!diag[s]) pool[d + m] = v.y;
+}
+
+// extend-add of a child's update matrix into its parent (columns j0..j1)
+__global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                const int* __restrict__ relOff, const int* __restrict__ relIdx,
+                                                double* __restrict__ pool)
+{
+    const TileTask t = tasks[blockIdx.x];
+    const int ch = t.front, par = t.i;
+    const int kc = fk[ch], mc = fm[ch], mp = fm[par];
+    const int u = mc - kc;
+    const double* C = pool + foff[ch];
+    double* Pm = pool + foff[par];
+    const int* rel = relIdx + relOff[ch];
+    for (int j = t.j; j < t.p; ++j) {
+        const int pj = rel[j];
+        const double* cc = C + (long long)(kc + j) * mc + kc;
+        double* pc = Pm + (long long)pj * mp;
+        for (int i = j + threadIdx.x; i < u; i += blockDim.x) pc[rel[i]] += cc[i];
+    }
+}
+
+// Cholesky of the diagonal tile of panel p (lower triangle, in place).
+__global__ void __launch_bounds__(256) k_potrf(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                               const int* __restrict__ fm, const long long* __restrict__ foff,
+                                               double* __restrict__ pool, int* flag)
+{
+    __shared__ double A[kTile][kTile + 1];
+    const TileTask t = tasks[blockIdx.x];
+    const int k = fk[t.front], m = fm[t.front];
+    int s0, w;
+    tile_bounds(k, m, t.p, s0, w);
+    double* F = pool + foff[t.front];
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int r = e % kTile, c = e / kTile;
+        A[r][c] = (r < w && c < w && r >= c) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
+    }
+    __syncthreads();
+    for (int c = 0; c < w; ++c) {
+        if (threadIdx.x == 0) {
+            double d = A[c][c];
+            if (!(d > 0.0)) {
+                atomicAdd(flag, 1);
+                d = fabs(d) > 0.0 ? fabs(d) : 1e-300;
+            }
+            A[c][c] = sqrt(d);
+        }
+        __syncthreads();
+        const double inv = 1.0 / A[c][c];
+        for (int r = c + 1 + threadIdx.x; r < w; r += blockDim.x) A[r][c] *= inv;
+        __syncthreads();
+        const int n = w - c - 1;
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            const int r = c + 1 + e % n, c2 = c + 1 + e / n;
+            if (r >= c2) A[r][c2] -= A[r][c] * A[c2][c];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+        const int r = e % w, c = e / w;
+        if (r >= c) F[(s0 + r) + (long long)(s0 + c) * m] = A[r][c];
+    }
+}
+
+// X = A(i, p) * L(p, p)^-T for tile row i below the diagonal tile.
+__global__ void __launch_bounds__(256) k_trsm(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                              const int* __restrict__ fm, const long long* __restrict__ foff,
+                                              double* __restrict__ pool)
+{
+    __shared__ double L[kTile][kTile + 1];
+    __shared__ double X[kTile][kTile + 1];
+    const TileTask t = tasks[blockIdx.x];
+    const int k = fk[t.front], m = fm[t.front];
+    int s0, w, r0, h;
+    tile_bounds(k, m, t.p, s0, w);
+    tile_bounds(k, m, t.i, r0, h);
+    double* F = pool + foff[t.front];
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int r = e % kTile, c = e / kTile;
+        L[r][c] = (r < w && c < w && r >= c) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
+        X[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
+    }
+    __syncthreads();
+    for (int c = 0; c < w; ++c) {
+        const double inv = 1.0 / L[c][c];
+        for (int r = threadIdx.x; r < h; r += blockDim.x) X[r][c] *= inv;
+        __syncthreads();
+        const int n = w - c - 1;
+        for (int e = threadIdx.x; e < h * n; e += blockDim.x) {
+            const int r = e % h, c2 = c + 1 + e / h;
+            X[r][c2] -= X[r][c] * L[c2][c];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < h * w; e += blockDim.x) {
+        const int r = e % h, c = e / h;
+        F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c];
+    }
+}
+
+// C(i, j) -= L(i, p) * L(j, p)^T  (trailing update, FP64)
+__global__ void __launch_bounds__(256) k_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                double* __restrict__ pool)
+{
+    __shared__ double Ai[kTile][kTile + 1];
+    __shared__ double Aj[kTile][kTile + 1];
+    const TileTask t = tasks[blockIdx.x];
+    const int k = fk[t.front], m = fm[t.front];
+    int s0, w, r0, h, c0, hc;
+    tile_bounds(k, m, t.p, s0, w);
+    tile_bounds(k, m, t.i, r0, h);
+    tile_bounds(k, m, t.j, c0, hc);
+    double* F = pool + foff[t.front];
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int r = e % kTile, c = e / kTile;
+        Ai[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
+        Aj[r][c] = (r < hc && c < w) ? F[(c0 + r) + (long long)(s0 + c) * m] : 0.0;
+    }
+    __syncthreads();
+    // each thread: 4 elements of the 32 x 32 tile (rows tr + 8q)
+    const int tc = threadIdx.x % kTile, tr = threadIdx.x / kTile;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int c = 0; c < w; ++c) {
+        const double b = Aj[tc][c];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = fma(Ai[tr + 8 * q][c], b, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int r = tr + 8 * q;
+        if (r < h && tc < hc && (t.i != t.j || r >= tc)) F[(r0 + r) + (long long)(c0 + tc) * m] -= acc[q];
+    }
+}
+
+__global__ void k_permute_in(const double* __restrict__ rhs, const int* __restrict__ perm, double sign, int n,
+                             double* __restrict__ out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] = sign * rhs[perm[j]];
+}
+
+__global__ void k_permute_out(const double* __restrict__ xp, const int* __restrict__ perm, int n, double* __restrict__ x)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) x[perm[j]] = xp[j];
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[32] = v;
+    }
+    __syncthreads();
+    const double s = red[32];
+    __syncthreads();
+    return s;
+}
+
+// Forward substitution of one front (one CTA per front of the level).
+// b (in yperm on entry for this front's pivots) -> y; update vector to upd.
+__global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
+                                             const int* __restrict__ fm, const long long* __restrict__ foff,
+                                             const long long* __restrict__ fupd, const int* __restrict__ fdof,
+                                             const int* __restrict__ childOff, const int* __restrict__ childList,
+                                             const int* __restrict__ relOff, const int* __restrict__ relIdx,
+                                             const double* __restrict__ pool, double* __restrict__ upd,
+                                             double* __restrict__ y)
+{
+    extern __shared__ double sh[];
+    const int f = fronts[blockIdx.x];
+    const int k = fk[f], m = fm[f], d0 = fdof[f];
+    for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : 0.0;
+    __syncthreads();
+    for (int c = childOff[f]; c < childOff[f + 1]; ++c) {
+        const int ch = childList[c];
+        const int u = fm[ch] - fk[ch];
+        const int* rel = relIdx + relOff[ch];
+        const double* uc = upd + fupd[ch];
+        for (int i = threadIdx.x; i < u; i += blockDim.x) sh[rel[i]] += uc[i];
+        __syncthreads();
+    }
+    const double* L = pool + foff[f];
+    for (int c = 0; c < k; ++c) {
+        const double yc = sh[c] / L[c + (long long)c * m];
+        __syncthreads();
+        if (threadIdx.x == 0) sh[c] = yc;
+        const double* lc = L + (long long)c * m;
+        for (int r = c + 1 + threadIdx.x; r < m; r += blockDim.x) sh[r] -= lc[r] * yc;
+        __syncthreads();
+    }
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        if (r < k) y[d0 + r] = sh[r];
+        else upd[fupd[f] + (r - k)] = sh[r];
+    }
+}
+
+// Backward substitution of one front: x_S = L11^-T (y_S - L21^T x_B).
+__global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, const int* __restrict__ fk,
+                                             const int* __restrict__ fm, const long long* __restrict__ foff,
+                                             const int* __restrict__ fdof, const int* __restrict__ frowOff,
+                                             const int* __restrict__ rowIdx, const double* __restrict__ pool,
+                                             const double* __restrict__ y, double* __restrict__ x)
+{
+    extern __shared__ double sh[];
+    __shared__ double red[33];
+    const int f = fronts[blockIdx.x];
+    const int k = fk[f], m = fm[f], d0 = fdof[f];
+    const int* rows = rowIdx + frowOff[f];
+    for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : x[rows[r]];
+    __syncthreads();
+    const double* L = pool + foff[f];
+    for (int c = k - 1; c >= 0; --c) {
+        const double* lc = L + (long long)c * m;
+        double s = 0.0;
+        for (int r = c + 1 + threadIdx.x; r < m; r += blockDim.x) s += lc[r] * sh[r];
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) sh[c] = (sh[c] - s) / lc[c];
+        __syncthreads();
+    }
+    for (int r = threadIdx.x; r < k; r += blockDim.x) x[d0 + r] = sh[r];
+}
+
+template <typename T>
+cudaError_t up(T** d, const std::vector<T>& h)
+{
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(d), sizeof(T) * (h.empty() ? 1 : h.size()));
+    if (e != cudaSuccess) return e;
+    if (!h.empty()) e = cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
+    return e;
+}
+
+} // namespace
+
+int chol_upload(CholPlan& P, std::string* err)
+{
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    chk(cudaMalloc(&P.pool, sizeof(double) * (size_t)std::max<long long>(P.poolSize, 1)));
+    chk(cudaMalloc(&P.upd, sizeof(double) * (size_t)std::max<long long>(P.updSize, 1)));
+    chk(cudaMalloc(&P.yperm, sizeof(double) * (size_t)std::max(P.nDof, 1)));
+    chk(cudaMalloc(&P.xperm, sizeof(double) * (size_t)std::max(P.nDof, 1)));
+    chk(up(&P.dPermDof, P.permDof)); chk(up(&P.dFk, P.fk)); chk(up(&P.dFm, P.fm));
+    chk(up(&P.dFdofStart, P.fdofStart)); chk(up(&P.dFrowOff, P.frowOff)); chk(up(&P.dFoff, P.foff));
+    chk(up(&P.dFupd, P.fupd)); chk(up(&P.dRowIdx, P.rowIdx)); chk(up(&P.dChildOff, P.childOff));
+    chk(up(&P.dChildList, P.childList)); chk(up(&P.dRelOff, P.relOff)); chk(up(&P.dRelIdx, P.relIdx));
+    chk(up(&P.dLevelFronts, P.levelFronts)); chk(up(&P.dTasks, P.tasks)); chk(up(&P.dAsmDest, P.asmDest));
+    chk(up(&P.dAsmLd, P.asmLd)); chk(up(&P.dAsmDiag, P.asmDiag));
+    chk(cudaMalloc(&P.dFlag, sizeof(int)));
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("chol upload: ") + cudaGetErrorString(e);
+        chol_free(P);
+        return OC_ERR_CUDA;
+    }
+    P.onDevice = true;
+    return OC_OK;
+}
+
+void chol_free(CholPlan& P)
+{
+    cudaFree(P.pool); cudaFree(P.upd); cudaFree(P.yperm); cudaFree(P.xperm);
+    cudaFree(P.dPermDof); cudaFree(P.dFk); cudaFree(P.dFm); cudaFree(P.dFdofStart); cudaFree(P.dFrowOff);
+    cudaFree(P.dFoff); cudaFree(P.dFupd); cudaFree(P.dRowIdx); cudaFree(P.dChildOff); cudaFree(P.dChildList);
+    cudaFree(P.dRelOff); cudaFree(P.dRelIdx); cudaFree(P.dLevelFronts); cudaFree(P.dTasks);
+    cudaFree(P.dAsmDest); cudaFree(P.dAsmLd); cudaFree(P.dAsmDiag); cudaFree(P.dFlag);
+    P.pool = P.upd = P.yperm = P.xperm = nullptr;
+    P.dPermDof = P.dFk = P.dFm = P.dFdofStart = P.dFrowOff = nullptr;
+    P.dFoff = P.dFupd = nullptr;
+    P.dRowIdx = P.dChildOff = P.dChildList = P.dRelOff = P.dRelIdx = P.dLevelFronts = nullptr;
+    P.dTasks = nullptr;
+    P.dAsmDest = nullptr;
+    P.dAsmLd = nullptr;
+    P.dAsmDiag = nullptr;
+    P.dFlag = nullptr;
+    P.onDevice = false;
+}
+
+int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBad)
+{
+    if (!P.onDevice) return OC_ERR_INVALID;
+    cudaMemsetAsync(P.pool, 0, sizeof(double) * (size_t)P.poolSize, st);
+    cudaMemsetAsync(P.dFlag, 0, sizeof(int), st);
+    k_asm_fronts<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b.val, P.dAsmDest, P.dAsmLd, P.dAsmDiag, b.nnzb, P.pool);
+    for (const auto& L : P.launches) {
+        const TileTask* t = P.dTasks + L.taskOff;
+        switch (L.kind) {
+        case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
+        case 1: k_potrf<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        case 2: k_trsm<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        default: k_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("chol factorize: ") + cudaGetErrorString(e);
+        return OC_ERR_CUDA;
+    }
+    if (nBad) {
+        e = cudaMemcpyAsync(nBad, P.dFlag, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            if (err) *err = std::string("chol factorize: ") + cudaGetErrorString(e);
+            return OC_ERR_CUDA;
+        }
+    }
+    return OC_OK;
+}
+
+int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, std::string* err)
+{
+    if (!P.onDevice) return OC_ERR_INVALID;
+    const int n = P.nDof;
+    k_permute_in<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(rhs), P.dPermDof, sign, n, P.yperm);
+    const size_t shm = sizeof(double) * (size_t)P.maxM;
+    if (shm > 48 * 1024) {
+        cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    }
+    for (int l = 0; l < P.nLevels; ++l) {
+        const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
+        k_fwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart, P.dChildOff,
+                                     P.dChildList, P.dRelOff, P.dRelIdx, P.pool, P.upd, P.yperm);
+    }
+    for (int l = P.nLevels - 1; l >= 0; --l) {
+        const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
+        k_bwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFdofStart, P.dFrowOff, P.dRowIdx,
+                                     P.pool, P.yperm, P.xperm);
+    }
+    k_permute_out<<<(n + 255) / 256, 256, 0, st>>>(P.xperm, P.dPermDof, n, reinterpret_cast<double*>(x));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("chol solve: ") + cudaGetErrorString(e);
+        return OC_ERR_CUDA;
+    }
+    return OC_OK;
+}
+
+} // namespace oc

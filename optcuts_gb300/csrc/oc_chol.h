@@ -1,0 +1,71 @@
+// Multifrontal sparse Cholesky on the device: the exact Newton solve behind
+// LinSysSolver::analyze_pattern / factorize / solve
+// (src/LinSysSolver/EigenLibSolver.cpp:71-107, SimplicialLDLT there).
+#pragma once
+
+#include "oc_internal.h"
+
+#include <string>
+#include <vector>
+
+namespace oc {
+
+constexpr int kTile = 32;   // dense tile edge (FP64) of the front kernels
+
+struct TileTask {           // one CTA's work item in a tiled front kernel
+    int front, i, j, p;
+};
+
+struct CholPlan {
+    // ---- host symbolic data ----
+    int nV = 0, nDof = 0, nFronts = 0, nLevels = 0;
+    std::vector<int> vertOrder;          // elimination order of vertices
+    std::vector<int> permDof;            // permuted DOF -> original DOF
+    std::vector<int> fk, fm, fparent, flevel, fdofStart;
+    std::vector<long long> foff, fupd;   // front pool offset, update-vector offset
+    std::vector<int> frowOff;            // offset into rowIdx (m entries per front)
+    std::vector<int> rowIdx;             // permuted DOF of each front row
+    std::vector<int> childOff, childList;            // children per front (CSR)
+    std::vector<int> relOff;             // per front: offset into relIdx (m - k entries)
+    std::vector<int> relIdx;             // child update row -> parent front row
+    long long poolSize = 0, updSize = 0;
+    double flops = 0.0;
+    int maxM = 0;
+    // per-level front lists and tiled task lists
+    std::vector<int> levelFrontOff, levelFronts;
+    struct Launch { int kind; int level; int p; int taskOff; int taskCount; int child; };
+    std::vector<Launch> launches;        // in execution order
+    std::vector<TileTask> tasks;
+    // assembly map from the block-CSR pattern
+    std::vector<long long> asmDest;      // per slot: pool offset of entry (0,0) or -1
+    std::vector<int> asmLd;              // per slot: leading dimension (front m)
+    std::vector<unsigned char> asmDiag;  // per slot: diagonal block (lower half only)
+
+    // ---- device copies ----
+    double* pool = nullptr;
+    double* upd = nullptr;
+    double* yperm = nullptr;     // nDof
+    double* xperm = nullptr;     // nDof
+    int *dPermDof = nullptr, *dFk = nullptr, *dFm = nullptr, *dFdofStart = nullptr, *dFrowOff = nullptr;
+    long long *dFoff = nullptr, *dFupd = nullptr;
+    int *dRowIdx = nullptr, *dChildOff = nullptr, *dChildList = nullptr, *dRelOff = nullptr, *dRelIdx = nullptr;
+    int* dLevelFronts = nullptr;
+    TileTask* dTasks = nullptr;
+    long long* dAsmDest = nullptr;
+    int* dAsmLd = nullptr;
+    unsigned char* dAsmDiag = nullptr;
+    int* dFlag = nullptr;        // non-positive pivot count
+    bool onDevice = false;
+};
+
+// Symbolic analysis from a full-symmetric vertex block pattern (rowPtr/col
+// over vertices incl. the diagonal).  Nested dissection by BFS level sets.
+void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize = 16);
+int chol_upload(CholPlan& P, std::string* err);
+void chol_free(CholPlan& P);
+// Numeric factorisation of the block-CSR values (FP32 storage, FP64 fronts).
+int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBadPivots);
+// Solves A x = sign * rhs.
+int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, std::string* err);
+
+} // namespace oc

@@ -31,11 +31,14 @@ def build(force=False):
     src = os.path.join(_HERE, "port", "oc_oracle.cpp")
     if (not force and os.path.exists(_SO)
             and os.path.getmtime(_SO) >= os.path.getmtime(src)
-            and os.path.getmtime(_SO) >= os.path.getmtime(os.path.join(_HERE, "port", "oc_oracle.h"))):
+            and os.path.getmtime(_SO) >= os.path.getmtime(os.path.join(_HERE, "port", "oc_oracle.h"))
+            and os.path.getmtime(_SO) >= os.path.getmtime(os.path.abspath(__file__))):
         return _SO
     os.makedirs(_BUILD, exist_ok=True)
     tmp = _SO + ".tmp%d" % os.getpid()
-    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", src, "-o", tmp])
+    # -ffp-contract=off: aarch64 GCC would fuse multiply-adds and change rounding
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", src,
+                           "-o", tmp])
     os.replace(tmp, _SO)
     return _SO
 

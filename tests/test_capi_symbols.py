@@ -5,6 +5,7 @@ import glob
 import os
 import re
 
+import numpy as np
 import pytest
 
 import optcuts_gb300 as oc
@@ -46,3 +47,24 @@ def test_loud_failure_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(oc, "_lib", None)
     with pytest.raises(ImportError):
         oc.lib()
+
+
+def test_symbolic_analysis_host_only():
+    """Nested-dissection front structure of the direct solver (no GPU)."""
+    from optcuts_gb300 import init as I
+    from optcuts_gb300 import meshes as M
+    V, F = M.CONFIGS["icosphere_1k"]()
+    st = I.init_uv(V, F)
+    s = oc.chol_analyze_stats(len(st.UV), st.F, st.fixedVert)
+    n = 2 * len(st.UV)
+    assert s["dof"] == n
+    assert s["fronts"] > 10 and s["levels"] >= 4
+    # the factor is sparse: far fewer entries than the dense lower triangle
+    assert n < s["factor_entries"] < n * n / 8
+    assert s["flops"] > 0 and s["max_front_rows"] <= n
+
+
+def test_symbolic_analysis_rejects_bad_input():
+    F = np.array([[0, 1, 5]], np.int32)
+    with pytest.raises(oc.OCError):
+        oc.chol_analyze_stats(3, F)

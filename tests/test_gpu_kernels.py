@@ -119,13 +119,76 @@ def _assembled_dense(g, par):
     return A
 
 
+def _reference_triplets(g, par):
+    """Triplets in the reference's order (IglUtils::addBlockToMatrix + the
+    fixed-vertex diagonal, SymDirichletEnergy.cpp:536-548), scaled by par."""
+    B = O.hessian_blocks(g["rest"], g["F"], g["UV0"])
+    fixed = set(g["fixedVert"].tolist())
+    I, J, V = [], [], []
+    for t, tri in enumerate(g["F"]):
+        idx = [a for a in range(3) if int(tri[a]) not in fixed]
+        for a in idx:
+            for b in idx:
+                for i in range(2):
+                    for j in range(2):
+                        I.append(2 * tri[a] + i)
+                        J.append(2 * tri[b] + j)
+                        V.append(par * B[t, 2 * a + i, 2 * b + j])
+    for v in sorted(fixed):
+        I += [2 * v, 2 * v + 1]
+        J += [2 * v, 2 * v + 1]
+        V += [par, par]
+    return np.array(I), np.array(J), np.array(V)
+
+
+@pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k"])
+def test_direct_solver_matches_reference_direction(golden, case):
+    """Multifrontal Cholesky vs the reference's SimplicialLDLT direction."""
+    g = golden(case)
+    par = 1.0 - g["scalars"][4]
+    I, J, V = _reference_triplets(g, par)
+    ls = oc.LinSysSolver(solver=oc.SOLVER_DIRECT)
+    ls.set_pattern(len(g["UV0"]), g["F"], g["fixedVert"])
+    ls.update_a(I, J, V)
+    assert ls.factorize()
+    b = -par * g["grad0"]
+    d = ls.solve(b)
+    assert ls.last_relres < 1e-9, ls.last_relres
+    # matrix entries are stored in FP32: the direction agrees with the
+    # reference's FP64 LDL^T to ~cond(A) * 6e-8 in the near-null modes
+    rel = np.linalg.norm(d - g["dir0"]) / np.linalg.norm(g["dir0"])
+    assert rel < 5e-2, rel
+    st = ls.stats()
+    assert st["dof"] == 2 * len(g["UV0"]) and st["fronts"] >= 1
+
+
+@pytest.mark.parametrize("case", ["cube", "icosphere_320"])
+def test_direct_solver_dense_check(golden, case):
+    g = golden(case)
+    par = 1.0 - g["scalars"][4]
+    A = _assembled_dense(g, par)
+    I, J = np.nonzero(A)
+    ls = oc.LinSysSolver(solver=oc.SOLVER_DIRECT)
+    ls.set_pattern(len(g["UV0"]), g["F"], g["fixedVert"])
+    ls.update_a(I, J, A[I, J])
+    ls.factorize()
+    A32 = A.astype(np.float32).astype(np.float64)
+    rng = np.random.default_rng(1)
+    b = rng.standard_normal(A.shape[0])
+    x = ls.solve(b)
+    x_ref = np.linalg.solve(A32, b)
+    cond = np.linalg.cond(A32)
+    assert np.linalg.norm(x - x_ref) <= 1e-13 * cond * np.linalg.norm(x_ref)
+    assert np.linalg.norm(A32 @ x - b) <= 1e-10 * np.linalg.norm(b)
+
+
 @pytest.mark.parametrize("case", ["cube", "icosphere_320"])
 def test_linsys_update_a_multiply_solve(golden, case):
     g = golden(case)
     par = 1.0 - g["scalars"][4]
     A = _assembled_dense(g, par)
     I, J = np.nonzero(A)
-    ls = oc.LinSysSolver()
+    ls = oc.LinSysSolver(solver=oc.SOLVER_PCG)
     ls.set_pattern(len(g["UV0"]), g["F"], g["fixedVert"])
     ls.update_a(I, J, A[I, J])
     assert ls.factorize()
@@ -146,7 +209,7 @@ def test_linsys_iteration_cap_reports_not_converged(golden):
     par = 1.0 - g["scalars"][4]
     A = _assembled_dense(g, par)
     I, J = np.nonzero(A)
-    ls = oc.LinSysSolver()
+    ls = oc.LinSysSolver(solver=oc.SOLVER_PCG)
     ls.set_pattern(len(g["UV0"]), g["F"], g["fixedVert"])
     ls.update_a(I, J, A[I, J])
     ls.factorize()

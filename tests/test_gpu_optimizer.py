@@ -97,3 +97,23 @@ def test_energy_param_update(golden):
     opt.energyParams[0] = 0.002
     opt.updateEnergyData()
     assert opt.getLastEnergyVal() == pytest.approx(2 * e1, rel=1e-15)
+
+
+def test_pcg_solver_option_runs(golden):
+    """The block-Jacobi PCG solver behind the same Optimizer (spec form)."""
+    g = golden("icosphere_320")
+    m, opt, E, steps, status = run(g, iters=5, linearSolver=oc.SOLVER_PCG, pcgMaxIter=50000)
+    assert np.all(np.diff(E) <= 0.0) and m.checkInversion()
+    assert all(s["pcgIters"] > 0 for s in steps)
+
+
+def test_phase_timing_and_launch_count(golden):
+    g = golden("icosphere_320")
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    opt = oc.Optimizer(m, [0.001], timing=1)
+    opt.precompute()
+    opt.solve(2)
+    ph = opt.phase_ms()
+    assert set(ph) == set(oc.Optimizer.PHASES) and all(v >= 0.0 for v in ph.values())
+    assert ph["factorize"] > 0.0 and ph["solve"] > 0.0
+    assert opt.launch_count() > 10
