@@ -167,6 +167,8 @@ int oc_optimizer_last_step(oc_optimizer* opt, double* stepSize, int* pcgIters, d
 int oc_optimizer_phase_ms(oc_optimizer* opt, double* out7);
 /* Kernel launches this optimizer issued since creation (for accounting). */
 int oc_optimizer_launch_count(oc_optimizer* opt, long long* launches);
+/* oc_linsys_stats of the optimizer's own solver (after precompute). */
+int oc_optimizer_solver_stats(oc_optimizer* opt, double* out8);
 
 #ifdef __cplusplus
 }

@@ -90,6 +90,7 @@ _SIGS = {
     "oc_optimizer_last_step": [_vp, _d, _i, _d, _i, _d],
     "oc_optimizer_phase_ms": [_vp, _d],
     "oc_optimizer_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "oc_optimizer_solver_stats": [_vp, _d],
 }
 
 
@@ -407,6 +408,11 @@ class Optimizer:
         out = np.zeros(7)
         self.ctx.check(lib().oc_optimizer_phase_ms(self.h, _pd(out)), "phase_ms")
         return dict(zip(self.PHASES, out.tolist()))
+
+    def solver_stats(self):
+        out = np.zeros(8)
+        self.ctx.check(lib().oc_optimizer_solver_stats(self.h, _pd(out)), "solver_stats")
+        return symbolic_stats_dict(out)
 
     def launch_count(self):
         n = ctypes.c_longlong()

@@ -639,7 +639,7 @@ int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, in
     oc::CholPlan P;
     oc::chol_analyze(P, nV, rowPtr.data(), col.data(), leafSize > 0 ? leafSize : 16);
     chol_stats(P, out8);
-    return OC_OK;
+    return P.valid ? OC_OK : OC_ERR_INVALID;
 }
 
 int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const int* fixedVert, int nFixed)
@@ -1036,6 +1036,12 @@ int oc_optimizer_phase_ms(oc_optimizer* o, double* out7)
         o->phaseMs[k] = 0.0;
     }
     return OC_OK;
+}
+
+int oc_optimizer_solver_stats(oc_optimizer* o, double* out8)
+{
+    if (!o) return OC_ERR_INVALID;
+    return oc_linsys_stats(o->ls, out8);
 }
 
 int oc_optimizer_launch_count(oc_optimizer* o, long long* n)

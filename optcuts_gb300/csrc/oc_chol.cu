@@ -208,7 +208,8 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
         for (int i = P.fk[f]; i < P.fm[f]; ++i) {
             const int dof = P.rowIdx[P.frowOff[f] + i];
             const int* it = std::lower_bound(prow, prow + pm, dof);
-            P.relIdx.push_back(static_cast<int>(it - prow));
+            if (it == prow + pm || *it != dof) P.valid = false;   // structure invariant violated
+            P.relIdx.push_back(it == prow + pm ? 0 : static_cast<int>(it - prow));
         }
     }
     // levels
@@ -286,7 +287,12 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             const int m = P.fm[f];
             const int jc = 2 * (pos[c] - vstart[f]);
             const int* prow = P.rowIdx.data() + P.frowOff[f];
-            const int ir = static_cast<int>(std::lower_bound(prow, prow + m, 2 * pos[r]) - prow);
+            const int* it = std::lower_bound(prow, prow + m, 2 * pos[r]);
+            if (it == prow + m || *it != 2 * pos[r] || jc + 1 >= P.fk[f]) {
+                P.valid = false;
+                continue;
+            }
+            const int ir = static_cast<int>(it - prow);
             P.asmDest[s] = P.foff[f] + ir + (long long)jc * m;
             P.asmLd[s] = m;
             P.asmDiag[s] = (r == c) ? 1 : 0;
@@ -566,6 +572,10 @@ cudaError_t up(T** d, const std::vector<T>& h)
 
 int chol_upload(CholPlan& P, std::string* err)
 {
+    if (!P.valid) {
+        if (err) *err = "chol: inconsistent symbolic structure";
+        return OC_ERR_INVALID;
+    }
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
     chk(cudaMalloc(&P.pool, sizeof(double) * (size_t)std::max<long long>(P.poolSize, 1)));

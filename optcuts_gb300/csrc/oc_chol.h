@@ -19,6 +19,7 @@ struct TileTask {           // one CTA's work item in a tiled front kernel
 struct CholPlan {
     // ---- host symbolic data ----
     int nV = 0, nDof = 0, nFronts = 0, nLevels = 0;
+    bool valid = true;                   // every index map resolved (checked before upload)
     std::vector<int> vertOrder;          // elimination order of vertices
     std::vector<int> permDof;            // permuted DOF -> original DOF
     std::vector<int> fk, fm, fparent, flevel, fdofStart;
