@@ -32,7 +32,7 @@ struct oc_mesh {
     std::vector<int> F, fixed;
     double2* cornerBuf = nullptr;   // 3 x nF corner gradients
     double2* tmpV = nullptr;        // nV scratch
-    float* hb = nullptr;            // 21 x nF packed Hessians
+    double* hb = nullptr;           // 21 x nF packed Hessians
     double* tmpF = nullptr;         // nF x 36 scratch for API outputs (lazy)
 };
 
@@ -215,7 +215,7 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     OC_CUDA(ctx, upload(b.rowFixed, mask.data(), nV, st));
     OC_CUDA(ctx, upload(b.cPtr, cPtr.data(), cPtr.size(), st));
     OC_CUDA(ctx, upload(b.cIdx, cIdx.data(), cIdx.size(), st));
-    OC_CUDA(ctx, cudaMemsetAsync(b.val, 0, sizeof(float4) * (size_t)(b.nnzb ? b.nnzb : 1), st));
+    OC_CUDA(ctx, cudaMemsetAsync(b.val, 0, sizeof(oc::Blk2) * (size_t)(b.nnzb ? b.nnzb : 1), st));
     oc::pcg_alloc(ls->wk, nV, ctx->device);
     OC_CUDA(ctx, cudaGetLastError());
     OC_CUDA(ctx, dalloc(&ls->tmpIn, nV));
@@ -659,7 +659,7 @@ int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* 
 {
     if (!ls || !ls->patternSet || n < 0 || (n && (!I || !J || !V))) return OC_ERR_INVALID;
     const int nV = ls->nV;
-    std::vector<float4> host(ls->b.nnzb, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<oc::Blk2> host(ls->b.nnzb, oc::Blk2{0.0, 0.0, 0.0, 0.0});
     std::vector<double> acc(4 * (size_t)ls->b.nnzb, 0.0);
     auto slot = [&](int r, int c) -> int {
         const int* lo = ls->col.data() + ls->rowPtr[r];
@@ -680,8 +680,7 @@ int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* 
         }
     }
     for (int s = 0; s < ls->b.nnzb; ++s)
-        host[s] = make_float4((float)acc[4 * (size_t)s], (float)acc[4 * (size_t)s + 1], (float)acc[4 * (size_t)s + 2],
-                              (float)acc[4 * (size_t)s + 3]);
+        host[s] = oc::Blk2{acc[4 * (size_t)s], acc[4 * (size_t)s + 1], acc[4 * (size_t)s + 2], acc[4 * (size_t)s + 3]};
     OC_CUDA(ls->ctx, upload(ls->b.val, host.data(), host.size(), ls->ctx->stream));
     OC_CUDA(ls->ctx, cudaStreamSynchronize(ls->ctx->stream));
     return OC_OK;

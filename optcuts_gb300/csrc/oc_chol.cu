@@ -13,16 +13,17 @@
 //    fronts, for the children's extend-add and for the tiled kernels' work;
 //  * numeric (device, every iteration): fronts are processed bottom-up one
 //    tree level at a time; within a level every front is factorised by the
-//    same batched tile kernels (32 x 32 FP64 tiles: diagonal Cholesky,
-//    triangular solve of the panel, trailing update), so one launch serves
-//    all fronts of a level;
+//    same batched tile kernels (32 x 32 FP64 tiles: LDL^T of the diagonal
+//    tile, triangular solve of the panel, trailing update), so one launch
+//    serves all fronts of a level;
 //  * solve: forward and backward substitution front by front, level by
 //    level, with the children's update vectors extend-added in a fixed
 //    order (deterministic, no atomics).
 //
-// All arithmetic is FP64.  A non-positive pivot (the matrix is PSD by
-// construction; a pivot can only vanish in rounding) is replaced by its
-// magnitude (or 1e-300) and counted.
+// All arithmetic is FP64.  The factorisation is LDL^T without pivoting, the
+// reference's own (SimplicialLDLT): a PSD-projected matrix with near-null
+// modes can produce tiny negative pivots in rounding, which LDL^T carries;
+// a zero or non-finite pivot is replaced by 1e-300 and counted.
 
 #include "oc_chol.h"
 
@@ -315,7 +316,7 @@ __device__ __forceinline__ void tile_bounds(int k, int m, int t, int& start, int
     }
 }
 
-__global__ void k_asm_fronts(const float4* __restrict__ val, const long long* __restrict__ dest,
+__global__ void k_asm_fronts(const Blk2* __restrict__ val, const long long* __restrict__ dest,
                              const int* __restrict__ ld, const unsigned char* __restrict__ diag, int nnzb,
                              double* __restrict__ pool)
 {
@@ -323,12 +324,12 @@ __global__ void k_asm_fronts(const float4* __restrict__ val, const long long* __
     if (s >= nnzb) return;
     const long long d = dest[s];
     if (d < 0) return;
-    const float4 v = val[s];
+    const Blk2 v = val[s];
     const long long m = ld[s];
-    pool[d] = v.x;
-    pool[d + 1] = v.z;
-    pool[d + 1 + m] = v.w;
-    if (!diag[s]) pool[d + m] = v.y;
+    pool[d] = v.a00;
+    pool[d + 1] = v.a10;
+    pool[d + 1 + m] = v.a11;
+    if (!diag[s]) pool[d + m] = v.a01;
 }
 
 // extend-add of a child's update matrix into its parent (columns j0..j1)
@@ -352,12 +353,16 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
     }
 }
 
-// Cholesky of the diagonal tile of panel p (lower triangle, in place).
-__global__ void __launch_bounds__(256) k_potrf(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                               const int* __restrict__ fm, const long long* __restrict__ foff,
-                                               double* __restrict__ pool, int* flag)
+// LDL^T of the diagonal tile of panel p, in place: unit-lower L below the
+// diagonal, D on the diagonal (the factorisation SimplicialLDLT computes;
+// negative pivots are allowed, a zero or non-finite one is counted and
+// replaced by 1e-300).
+__global__ void __launch_bounds__(256) k_ldl_diag(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                  const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                  double* __restrict__ pool, int* flag)
 {
     __shared__ double A[kTile][kTile + 1];
+    __shared__ double T[kTile];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w;
@@ -370,21 +375,22 @@ __global__ void __launch_bounds__(256) k_potrf(const TileTask* __restrict__ task
     __syncthreads();
     for (int c = 0; c < w; ++c) {
         if (threadIdx.x == 0) {
-            double d = A[c][c];
-            if (!(d > 0.0)) {
+            const double d = A[c][c];
+            if (!(d != 0.0) || !isfinite(d)) {
                 atomicAdd(flag, 1);
-                d = fabs(d) > 0.0 ? fabs(d) : 1e-300;
+                A[c][c] = 1e-300;
             }
-            A[c][c] = sqrt(d);
         }
         __syncthreads();
-        const double inv = 1.0 / A[c][c];
-        for (int r = c + 1 + threadIdx.x; r < w; r += blockDim.x) A[r][c] *= inv;
+        const double d = A[c][c];
+        for (int r = c + 1 + threadIdx.x; r < w; r += blockDim.x) T[r] = A[r][c];
         __syncthreads();
+        const double inv = 1.0 / d;
         const int n = w - c - 1;
+        for (int r = c + 1 + threadIdx.x; r < w; r += blockDim.x) A[r][c] = T[r] * inv;
         for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
             const int r = c + 1 + e % n, c2 = c + 1 + e / n;
-            if (r >= c2) A[r][c2] -= A[r][c] * A[c2][c];
+            if (r >= c2) A[r][c2] -= T[r] * inv * T[c2];
         }
         __syncthreads();
     }
@@ -394,10 +400,10 @@ __global__ void __launch_bounds__(256) k_potrf(const TileTask* __restrict__ task
     }
 }
 
-// X = A(i, p) * L(p, p)^-T for tile row i below the diagonal tile.
-__global__ void __launch_bounds__(256) k_trsm(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                              const int* __restrict__ fm, const long long* __restrict__ foff,
-                                              double* __restrict__ pool)
+// L(i, p) = A(i, p) * L(p, p)^-T * D_p^-1 for a tile row below the diagonal tile.
+__global__ void __launch_bounds__(256) k_ldl_trsm(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                  const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                  double* __restrict__ pool)
 {
     __shared__ double L[kTile][kTile + 1];
     __shared__ double X[kTile][kTile + 1];
@@ -413,10 +419,7 @@ __global__ void __launch_bounds__(256) k_trsm(const TileTask* __restrict__ tasks
         X[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
     }
     __syncthreads();
-    for (int c = 0; c < w; ++c) {
-        const double inv = 1.0 / L[c][c];
-        for (int r = threadIdx.x; r < h; r += blockDim.x) X[r][c] *= inv;
-        __syncthreads();
+    for (int c = 0; c + 1 < w; ++c) {
         const int n = w - c - 1;
         for (int e = threadIdx.x; e < h * n; e += blockDim.x) {
             const int r = e % h, c2 = c + 1 + e / h;
@@ -426,14 +429,14 @@ __global__ void __launch_bounds__(256) k_trsm(const TileTask* __restrict__ tasks
     }
     for (int e = threadIdx.x; e < h * w; e += blockDim.x) {
         const int r = e % h, c = e / h;
-        F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c];
+        F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c] / L[c][c];
     }
 }
 
-// C(i, j) -= L(i, p) * L(j, p)^T  (trailing update, FP64)
-__global__ void __launch_bounds__(256) k_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                double* __restrict__ pool)
+// C(i, j) -= L(i, p) * D_p * L(j, p)^T  (trailing update, FP64)
+__global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                    const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                    double* __restrict__ pool)
 {
     __shared__ double Ai[kTile][kTile + 1];
     __shared__ double Aj[kTile][kTile + 1];
@@ -443,10 +446,11 @@ __global__ void __launch_bounds__(256) k_update(const TileTask* __restrict__ tas
     tile_bounds(k, m, t.p, s0, w);
     tile_bounds(k, m, t.i, r0, h);
     tile_bounds(k, m, t.j, c0, hc);
-    double* F = pool + foff[t.front];
+    const double* F = pool + foff[t.front];
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
         const int r = e % kTile, c = e / kTile;
-        Ai[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
+        const double dc = c < w ? F[(s0 + c) + (long long)(s0 + c) * m] : 0.0;
+        Ai[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] * dc : 0.0;
         Aj[r][c] = (r < hc && c < w) ? F[(c0 + r) + (long long)(s0 + c) * m] : 0.0;
     }
     __syncthreads();
@@ -458,10 +462,11 @@ __global__ void __launch_bounds__(256) k_update(const TileTask* __restrict__ tas
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q] = fma(Ai[tr + 8 * q][c], b, acc[q]);
     }
+    double* Fw = pool + foff[t.front];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int r = tr + 8 * q;
-        if (r < h && tc < hc && (t.i != t.j || r >= tc)) F[(r0 + r) + (long long)(c0 + tc) * m] -= acc[q];
+        if (r < h && tc < hc && (t.i != t.j || r >= tc)) Fw[(r0 + r) + (long long)(c0 + tc) * m] -= acc[q];
     }
 }
 
@@ -478,25 +483,11 @@ __global__ void k_permute_out(const double* __restrict__ xp, const int* __restri
     if (j < n) x[perm[j]] = xp[j];
 }
 
-__device__ __forceinline__ double block_sum(double v, double* red)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-        v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[32] = v;
-    }
-    __syncthreads();
-    const double s = red[32];
-    __syncthreads();
-    return s;
-}
-
-// Forward substitution of one front (one CTA per front of the level).
-// b (in yperm on entry for this front's pivots) -> y; update vector to upd.
+// Forward substitution of one front (one CTA per front of the level), in
+// 32-column blocks: warp 0 solves the unit-lower diagonal block with
+// shuffles, then every thread updates the rows below (coalesced column
+// reads).  The pivots' values leave divided by D (z = D^-1 y); the update
+// vector for the parent leaves in upd.
 __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
                                              const int* __restrict__ fm, const long long* __restrict__ foff,
                                              const long long* __restrict__ fupd, const int* __restrict__ fdof,
@@ -508,6 +499,7 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
     extern __shared__ double sh[];
     const int f = fronts[blockIdx.x];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : 0.0;
     __syncthreads();
     for (int c = childOff[f]; c < childOff[f + 1]; ++c) {
@@ -519,21 +511,34 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
         __syncthreads();
     }
     const double* L = pool + foff[f];
-    for (int c = 0; c < k; ++c) {
-        const double yc = sh[c] / L[c + (long long)c * m];
+    for (int c0 = 0; c0 < k; c0 += 32) {
+        const int w = min(32, k - c0);
+        if (warp == 0) {
+            double v = lane < w ? sh[c0 + lane] : 0.0;
+            for (int c = 0; c < w; ++c) {
+                const double yc = __shfl_sync(0xffffffffu, v, c);
+                if (lane > c && lane < w) v -= L[(c0 + lane) + (long long)(c0 + c) * m] * yc;
+            }
+            if (lane < w) sh[c0 + lane] = v;
+        }
         __syncthreads();
-        if (threadIdx.x == 0) sh[c] = yc;
-        const double* lc = L + (long long)c * m;
-        for (int r = c + 1 + threadIdx.x; r < m; r += blockDim.x) sh[r] -= lc[r] * yc;
+        for (int r = c0 + w + threadIdx.x; r < m; r += blockDim.x) {
+            double s = 0.0;
+            for (int c = 0; c < w; ++c) s = fma(L[r + (long long)(c0 + c) * m], sh[c0 + c], s);
+            sh[r] -= s;
+        }
         __syncthreads();
     }
     for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        if (r < k) y[d0 + r] = sh[r];
+        if (r < k) y[d0 + r] = sh[r] / L[r + (long long)r * m];
         else upd[fupd[f] + (r - k)] = sh[r];
     }
 }
 
-// Backward substitution of one front: x_S = L11^-T (y_S - L21^T x_B).
+// Backward substitution of one front: x_S = L11^-T (z_S - L21^T x_B), unit
+// diagonal, in 32-column blocks from the last: the block's dot products with
+// the rows below (one warp per column, strided), then warp 0 solves the
+// diagonal block with shuffles.
 __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, const int* __restrict__ fk,
                                              const int* __restrict__ fm, const long long* __restrict__ foff,
                                              const int* __restrict__ fdof, const int* __restrict__ frowOff,
@@ -541,19 +546,33 @@ __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, con
                                              const double* __restrict__ y, double* __restrict__ x)
 {
     extern __shared__ double sh[];
-    __shared__ double red[33];
+    __shared__ double dots[32];
     const int f = fronts[blockIdx.x];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int* rows = rowIdx + frowOff[f];
     for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : x[rows[r]];
     __syncthreads();
     const double* L = pool + foff[f];
-    for (int c = k - 1; c >= 0; --c) {
-        const double* lc = L + (long long)c * m;
-        double s = 0.0;
-        for (int r = c + 1 + threadIdx.x; r < m; r += blockDim.x) s += lc[r] * sh[r];
-        s = block_sum(s, red);
-        if (threadIdx.x == 0) sh[c] = (sh[c] - s) / lc[c];
+    const int nBlocks = (k + 31) / 32;
+    for (int b = nBlocks - 1; b >= 0; --b) {
+        const int c0 = 32 * b, w = min(32, k - c0);
+        for (int c = warp; c < w; c += nw) {
+            const double* lc = L + (long long)(c0 + c) * m;
+            double s = 0.0;
+            for (int r = c0 + w + lane; r < m; r += 32) s = fma(lc[r], sh[r], s);
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0) dots[c] = s;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double v = lane < w ? sh[c0 + lane] - dots[lane] : 0.0;
+            for (int r = w - 1; r >= 0; --r) {
+                const double xr = __shfl_sync(0xffffffffu, v, r);
+                if (lane < r) v -= L[(c0 + r) + (long long)(c0 + lane) * m] * xr;
+            }
+            if (lane < w) sh[c0 + lane] = v;
+        }
         __syncthreads();
     }
     for (int r = threadIdx.x; r < k; r += blockDim.x) x[d0 + r] = sh[r];
@@ -627,9 +646,9 @@ int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string
         const TileTask* t = P.dTasks + L.taskOff;
         switch (L.kind) {
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
-        case 1: k_potrf<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        case 2: k_trsm<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
-        default: k_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        case 1: k_ldl_diag<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        case 2: k_ldl_trsm<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         }
     }
     cudaError_t e = cudaGetLastError();

@@ -15,6 +15,11 @@ struct __align__(32) Mat2d {
     double a00, a01, a10, a11;
 };
 
+// One 2x2 block of the Newton matrix, row-major.
+struct __align__(32) Blk2 {
+    double a00, a01, a10, a11;
+};
+
 // Line-search step sizes passed by value to the energy kernel.
 struct Alphas {
     double a[8];
@@ -55,7 +60,7 @@ struct Scratch {
 struct DeviceBsr {
     int nRows = 0, nnzb = 0;
     int *rowPtr = nullptr, *col = nullptr;
-    float4* val = nullptr;         // nnzb blocks, row-major (a00, a01, a10, a11)
+    Blk2* val = nullptr;           // nnzb blocks (FP64)
     int* diagSlot = nullptr;       // nRows
     unsigned char* rowFixed = nullptr;
     // contributions: slot -> list of (t * 9 + a * 3 + b)
@@ -86,11 +91,11 @@ void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st);
 void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st);
 int reduce_blocks_for(int n);
 
-// per-triangle projected Hessian: 21 FP32 values per triangle (SoA, scaled by `scale`)
-void launch_hessian(const DeviceMesh& m, int uniform, float* hb, cudaStream_t st);
+// per-triangle PSD-projected Hessian: 21 FP64 values per triangle (SoA)
+void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st);
 // expand the 21 packed values to full 6x6 FP64 (for the API / tests)
-void launch_hessian_expand(const float* hb, int nF, double* out, cudaStream_t st);
-void launch_assemble(const DeviceBsr& b, const float* hb, int nF, double scale, cudaStream_t st);
+void launch_hessian_expand(const double* hb, int nF, double* out, cudaStream_t st);
+void launch_assemble(const DeviceBsr& b, const double* hb, int nF, double scale, cudaStream_t st);
 int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag);
 void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag);
 // solves A x = rhsSign * rhs (rhsSign = -1 gives the Newton direction from g)

@@ -2,13 +2,12 @@
 // projection, block-CSR assembly, block-Jacobi preconditioner, SpMV and the
 // persistent PCG solve.
 //
-// Precision: the per-triangle 6x6 Hessian is formed in FP64 with the
-// reference's closed-form second derivatives (SymDirichletEnergy.cpp:
-// 440-522), normalised by its largest entry and projected to PSD in FP32.
-// Matrix values are stored in FP32; SpMV, preconditioner and every Krylov
-// vector and dot product are FP64.  The systems are extremely ill-conditioned
-// (a Tutte start has UV triangles 1e-9 times their rest area), and FP32
-// Krylov arithmetic stalls on them, FP32 storage does not.
+// Precision: FP64 throughout.  The Newton systems are extremely
+// ill-conditioned (a Tutte start has UV triangles 1e-9 times their rest
+// area, condition numbers near 1e14): FP32 Krylov arithmetic stalls on them,
+// and an FP32-rounded matrix (or FP32 eigen-projection) moves the exact
+// Newton direction by up to cond * 6e-8 in its near-null modes, which shows
+// up as energy-trace differences of tens of percent against the reference.
 
 #include "oc_internal.h"
 
@@ -25,63 +24,65 @@ namespace {
 // Orthonormal basis of the complement of the two rigid translations in the
 // 6-dimensional corner space (u1, v1, u2, v2, u3, v3):
 // columns q1(x)e_x, q1(x)e_y, q2(x)e_x, q2(x)e_y with q1 = (1,-1,0)/sqrt2,
-// q2 = (1,1,-2)/sqrt6.  The SD Hessian annihilates translations, so its
-// eigen-decomposition reduces to the 4x4 matrix Q^T H Q.
-__constant__ float kQ1[3] = {0.70710678118654752f, -0.70710678118654752f, 0.0f};
-__constant__ float kQ2[3] = {0.40824829046386302f, 0.40824829046386302f, -0.81649658092772603f};
+// q2 = (1,1,-2)/sqrt6.  The SD Hessian annihilates translations, so the
+// eigen-decomposition behind the PSD projection reduces to the 4x4 matrix
+// Q^T H Q (the two translation eigenvalues are zero up to rounding; the
+// reference's 6x6 eigen-clamp sets them to zero too when they round below).
+__constant__ double kQ1[3] = {0.70710678118654752440, -0.70710678118654752440, 0.0};
+__constant__ double kQ2[3] = {0.40824829046386301637, 0.40824829046386301637, -0.81649658092772603273};
 
-__device__ __forceinline__ float qv(int col, int row)
+__device__ __forceinline__ double qv(int col, int row)
 {
     // Q[row][col], row in 0..5 (vertex = row/2, comp = row%2), col in 0..3
     const int vert = row >> 1, comp = row & 1;
     const int qi = col >> 1, qc = col & 1;
-    if (comp != qc) return 0.0f;
+    if (comp != qc) return 0.0;
     return qi == 0 ? kQ1[vert] : kQ2[vert];
 }
 
-// Cyclic Jacobi on a symmetric 4x4 (FP32).  A -> diag(eigenvalues), V columns = eigenvectors.
-__device__ void jacobi4(float A[4][4], float V[4][4])
+// Cyclic Jacobi on a symmetric 4x4 (FP64).  A -> diag(eigenvalues), V columns = eigenvectors.
+__device__ void jacobi4(double A[4][4], double V[4][4])
 {
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.0f : 0.0f;
-    float fro = 0.0f;
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+    double fro = 0.0;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) fro += A[i][j] * A[i][j];
-    for (int sweep = 0; sweep < 12; ++sweep) {
-        float off = 0.0f;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        double off = 0.0;
 #pragma unroll
         for (int p = 0; p < 4; ++p)
 #pragma unroll
             for (int q = p + 1; q < 4; ++q) off += A[p][q] * A[p][q];
-        if (off <= 1e-14f * fro) break;
+        if (!(off > 1e-32 * fro)) break;
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
 #pragma unroll
             for (int q = p + 1; q < 4; ++q) {
-                const float apq = A[p][q];
-                if (fabsf(apq) < 1e-30f) continue;
-                const float theta = (A[q][q] - A[p][p]) / (2.0f * apq);
-                const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.0f)));
-                const float c = rsqrtf(fmaf(t, t, 1.0f)), s = t * c;
+                const double apq = A[p][q];
+                if (apq == 0.0) continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+                const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+                const double c = 1.0 / sqrt(fma(t, t, 1.0)), s = t * c;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float akp = A[k][p], akq = A[k][q];
+                    const double akp = A[k][p], akq = A[k][q];
                     A[k][p] = c * akp - s * akq;
                     A[k][q] = s * akp + c * akq;
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float apk = A[p][k], aqk = A[q][k];
+                    const double apk = A[p][k], aqk = A[q][k];
                     A[p][k] = c * apk - s * aqk;
                     A[q][k] = s * apk + c * aqk;
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const float vkp = V[k][p], vkq = V[k][q];
+                    const double vkp = V[k][p], vkq = V[k][q];
                     V[k][p] = c * vkp - s * vkq;
                     V[k][q] = s * vkp + c * vkq;
                 }
@@ -94,25 +95,26 @@ __device__ void jacobi4(float A[4][4], float V[4][4])
 // off-diagonal blocks (0,1), (0,2), (1,2) row-major at 9..20.
 __device__ __forceinline__ int pair_index(int a, int b) { return a + b - 1; }   // (0,1)->0 (0,2)->1 (1,2)->2
 
-__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, float* __restrict__ hb)
+// Per-triangle Hessian (SymDirichletEnergy.cpp:440-522) projected to PSD
+// (IglUtils::makePD, IglUtils.hpp:71-90), all FP64.
+__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, double* __restrict__ hb)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m.nF) return;
     const int nF = m.nF;
     const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
-    // ---- FP64 element Hessian (SymDirichletEnergy.cpp:440-522) ----
     const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
     const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
     const double area_U = 0.5 * (U2m1[0] * U3m1[1] - U2m1[1] * U3m1[0]);
     const double A2 = m.A2[t];
     const double areaRatio = A2 / area_U / area_U / area_U;
-    const double dAR = 1.5 * areaRatio / area_U;
+    const double dAR = 3.0 / 2.0 * areaRatio / area_U;
     const double w = uniform ? 1.0 : m.w[t];
     // e0SqLen_div_dbAreaSq etc. (TriMesh.cpp:391-393)
     const double e0d = m.e0d[t], e1d = m.e1d[t], e01d = m.e01d[t];
     const double leftTerm = 1.0 + A2 / area_U / area_U;
     const double rightTerm = ((U3m1[0] * U3m1[0] + U3m1[1] * U3m1[1]) * e0d +
-                              (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) * 0.5 -
+                              (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) / 2. -
                              (U3m1[0] * U2m1[0] + U3m1[1] * U2m1[1]) * e01d;
     double ort[3][2], dL[3][2], dR[3][2];
     ort[0][0] = U[2].y - U[1].y; ort[0][1] = -(U[2].x - U[1].x);
@@ -149,103 +151,89 @@ __global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, floa
             }
         }
     }
-    // ---- normalise, project to PSD in FP32 (IglUtils::makePD, IglUtils.hpp:71-90) ----
-    double hmax = 0.0;
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int j = i; j < 6; ++j) hmax = fmax(hmax, fabs(H[i][j]));
-    const double inv = (hmax > 0.0 && hmax < 1e300) ? 1.0 / hmax : 1.0;
-    float Hf[6][6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int j = 0; j < 6; ++j) Hf[i][j] = static_cast<float>(H[i][j] * inv);
-    // M = Q^T Hf Q
-    float HQ[6][4];
+    // M = Q^T H Q
+    double HQ[6][4];
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            float s = 0.0f;
+            double s = 0.0;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) s = fmaf(Hf[i][k], qv(c, k), s);
+            for (int k = 0; k < 6; ++k) s = fma(H[i][k], qv(c, k), s);
             HQ[i][c] = s;
         }
-    float M[4][4];
+    double M[4][4];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            float s = 0.0f;
+            double s = 0.0;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) s = fmaf(qv(r, k), HQ[k][c], s);
+            for (int k = 0; k < 6; ++k) s = fma(qv(r, k), HQ[k][c], s);
             M[r][c] = s;
         }
-    // PSD test by LDL^T pivots of M
+    // PSD test by the LDL^T pivots of M (positive pivots <=> positive definite)
     bool pd = true;
     {
-        float L[4][4];
+        double L[4][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) L[i][j] = M[i][j];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float d = L[k][k];
-            if (!(d > 0.0f)) pd = false;
-            const float id = (d > 0.0f) ? 1.0f / d : 0.0f;
+            const double d = L[k][k];
+            if (!(d > 0.0)) pd = false;
+            const double id = (d > 0.0) ? 1.0 / d : 0.0;
 #pragma unroll
             for (int i = k + 1; i < 4; ++i) {
-                const float f = L[i][k] * id;
+                const double f = L[i][k] * id;
 #pragma unroll
                 for (int j = k + 1; j < 4; ++j) L[i][j] -= f * L[k][j];
             }
         }
     }
     if (!pd) {
-        float V[4][4];
+        double V[4][4];
         jacobi4(M, V);
-        float lam[4];
+        double lam[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) lam[k] = fmaxf(M[k][k], 0.0f);
-        // Mp = V diag(lam) V^T ; Hf = Q Mp Q^T
-        float Mp[4][4];
+        for (int k = 0; k < 4; ++k) lam[k] = fmax(M[k][k], 0.0);
+        double Mp[4][4];
 #pragma unroll
         for (int r = 0; r < 4; ++r)
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                float s = 0.0f;
+                double s = 0.0;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) s = fmaf(V[r][k] * lam[k], V[c][k], s);
+                for (int k = 0; k < 4; ++k) s = fma(V[r][k] * lam[k], V[c][k], s);
                 Mp[r][c] = s;
             }
-        float QM[6][4];
+        double QM[6][4];
 #pragma unroll
         for (int i = 0; i < 6; ++i)
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                float s = 0.0f;
+                double s = 0.0;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) s = fmaf(qv(k, i), Mp[k][c], s);
+                for (int k = 0; k < 4; ++k) s = fma(qv(k, i), Mp[k][c], s);
                 QM[i][c] = s;
             }
 #pragma unroll
         for (int i = 0; i < 6; ++i)
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
-                float s = 0.0f;
+                double s = 0.0;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) s = fmaf(QM[i][k], qv(k, j), s);
-                Hf[i][j] = s;
+                for (int k = 0; k < 4; ++k) s = fma(QM[i][k], qv(k, j), s);
+                H[i][j] = s;
             }
     }
-    const float sc = static_cast<float>(hmax > 0.0 && hmax < 1e300 ? hmax : 1.0);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        hb[(3 * a + 0) * (size_t)nF + t] = Hf[2 * a][2 * a] * sc;
-        hb[(3 * a + 1) * (size_t)nF + t] = 0.5f * (Hf[2 * a][2 * a + 1] + Hf[2 * a + 1][2 * a]) * sc;
-        hb[(3 * a + 2) * (size_t)nF + t] = Hf[2 * a + 1][2 * a + 1] * sc;
+        hb[(3 * a + 0) * (size_t)nF + t] = H[2 * a][2 * a];
+        hb[(3 * a + 1) * (size_t)nF + t] = 0.5 * (H[2 * a][2 * a + 1] + H[2 * a + 1][2 * a]);
+        hb[(3 * a + 2) * (size_t)nF + t] = H[2 * a + 1][2 * a + 1];
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -256,74 +244,73 @@ __global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, floa
             for (int i = 0; i < 2; ++i)
 #pragma unroll
                 for (int j = 0; j < 2; ++j)
-                    hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] =
-                        0.5f * (Hf[2 * a + i][2 * b + j] + Hf[2 * b + j][2 * a + i]) * sc;
+                    hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] = 0.5 * (H[2 * a + i][2 * b + j] + H[2 * b + j][2 * a + i]);
         }
 }
 
-__device__ __forceinline__ float4 local_block(const float* __restrict__ hb, int nF, int code)
+__device__ __forceinline__ Blk2 local_block(const double* __restrict__ hb, int nF, int code)
 {
     const int t = code / 9, ab = code - 9 * t, a = ab / 3, b = ab - 3 * a;
     if (a == b) {
-        const float xx = hb[(3 * a) * (size_t)nF + t], xy = hb[(3 * a + 1) * (size_t)nF + t],
-                    yy = hb[(3 * a + 2) * (size_t)nF + t];
-        return make_float4(xx, xy, xy, yy);
+        const double xx = hb[(3 * a) * (size_t)nF + t], xy = hb[(3 * a + 1) * (size_t)nF + t],
+                     yy = hb[(3 * a + 2) * (size_t)nF + t];
+        return Blk2{xx, xy, xy, yy};
     }
     const int lo = a < b ? a : b, hi = a < b ? b : a;
     const int base = 9 + 4 * pair_index(lo, hi);
-    const float h00 = hb[(base + 0) * (size_t)nF + t], h01 = hb[(base + 1) * (size_t)nF + t],
-                h10 = hb[(base + 2) * (size_t)nF + t], h11 = hb[(base + 3) * (size_t)nF + t];
-    return a < b ? make_float4(h00, h01, h10, h11) : make_float4(h00, h10, h01, h11);
+    const double h00 = hb[(base + 0) * (size_t)nF + t], h01 = hb[(base + 1) * (size_t)nF + t],
+                 h10 = hb[(base + 2) * (size_t)nF + t], h11 = hb[(base + 3) * (size_t)nF + t];
+    return a < b ? Blk2{h00, h01, h10, h11} : Blk2{h00, h10, h01, h11};
 }
 
-__global__ void k_hessian_expand(const float* __restrict__ hb, int nF, double* __restrict__ out)
+__global__ void k_hessian_expand(const double* __restrict__ hb, int nF, double* __restrict__ out)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nF) return;
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
-            const float4 B = local_block(hb, nF, t * 9 + a * 3 + b);
+            const Blk2 B = local_block(hb, nF, t * 9 + a * 3 + b);
             double* o = out + 36 * (size_t)t;
-            o[6 * (2 * a) + 2 * b] = B.x;
-            o[6 * (2 * a) + 2 * b + 1] = B.y;
-            o[6 * (2 * a + 1) + 2 * b] = B.z;
-            o[6 * (2 * a + 1) + 2 * b + 1] = B.w;
+            o[6 * (2 * a) + 2 * b] = B.a00;
+            o[6 * (2 * a) + 2 * b + 1] = B.a01;
+            o[6 * (2 * a + 1) + 2 * b] = B.a10;
+            o[6 * (2 * a + 1) + 2 * b + 1] = B.a11;
         }
 }
 
 // One thread per block slot: fixed-order sum of its triangle contributions
 // (the device counterpart of LinSysSolver::update_a, LinSysSolver.hpp:138-159,
 // and Optimizer.cpp:825's energyParams scaling).
-__global__ void __launch_bounds__(256) k_assemble(DeviceBsr b, const float* __restrict__ hb, int nF, float scale)
+__global__ void __launch_bounds__(256) k_assemble(DeviceBsr b, const double* __restrict__ hb, int nF, double scale)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= b.nnzb) return;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    Blk2 acc{0.0, 0.0, 0.0, 0.0};
     for (int p = b.cPtr[s]; p < b.cPtr[s + 1]; ++p) {
-        const float4 B = local_block(hb, nF, b.cIdx[p]);
-        acc.x += B.x; acc.y += B.y; acc.z += B.z; acc.w += B.w;
+        const Blk2 B = local_block(hb, nF, b.cIdx[p]);
+        acc.a00 += B.a00; acc.a01 += B.a01; acc.a10 += B.a10; acc.a11 += B.a11;
     }
-    b.val[s] = make_float4(acc.x * scale, acc.y * scale, acc.z * scale, acc.w * scale);
+    b.val[s] = Blk2{acc.a00 * scale, acc.a01 * scale, acc.a10 * scale, acc.a11 * scale};
 }
 
 // Fixed rows: diagonal = energyParam * I (SymDirichletEnergy.cpp:541-548 scaled
-// at Optimizer.cpp:825); block-Jacobi inverse per row in FP64.
-__global__ void k_precond(DeviceBsr b, float fixedDiag, int* flag)
+// at Optimizer.cpp:825); block-Jacobi inverse per row.
+__global__ void k_precond(DeviceBsr b, double fixedDiag, int* flag)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= b.nRows) return;
     const int s = b.diagSlot[r];
-    if (b.rowFixed[r] && fixedDiag > 0.0f) b.val[s] = make_float4(fixedDiag, 0.f, 0.f, fixedDiag);
-    const float4 D = b.val[s];
-    const double a = D.x, bb = 0.5 * ((double)D.y + (double)D.z), d = D.w;
+    if (b.rowFixed[r] && fixedDiag > 0.0) b.val[s] = Blk2{fixedDiag, 0.0, 0.0, fixedDiag};
+    const Blk2 D = b.val[s];
+    const double a = D.a00, bb = 0.5 * (D.a01 + D.a10), d = D.a11;
     const double det = a * d - bb * bb;
     if (a > 0.0 && det > 0.0) {
         b.dinv[r] = Mat2d{d / det, -bb / det, -bb / det, a / det};
     }
     else {
         // singular or indefinite diagonal block: fall back to a scaled identity
-        const double m = fmax(fabs(a), fabs(d));
-        const double iv = m > 0.0 ? 1.0 / m : 1.0;
+        const double mx = fmax(fabs(a), fabs(d));
+        const double iv = mx > 0.0 ? 1.0 / mx : 1.0;
         b.dinv[r] = Mat2d{iv, 0.0, 0.0, iv};
         atomicAdd(flag, 1);
     }
@@ -334,12 +321,12 @@ __device__ __forceinline__ double2 row_spmv(const DeviceBsr& b, int r, const dou
     double sx = 0.0, sy = 0.0;
     const int e = b.rowPtr[r + 1];
     for (int p = b.rowPtr[r]; p < e; ++p) {
-        const float4 A = b.val[p];
+        const Blk2 A = b.val[p];
         const double2 xv = x[b.col[p]];
-        sx = fma((double)A.x, xv.x, sx);
-        sx = fma((double)A.y, xv.y, sx);
-        sy = fma((double)A.z, xv.x, sy);
-        sy = fma((double)A.w, xv.y, sy);
+        sx = fma(A.a00, xv.x, sx);
+        sx = fma(A.a01, xv.y, sx);
+        sy = fma(A.a10, xv.x, sy);
+        sy = fma(A.a11, xv.y, sy);
     }
     return make_double2(sx, sy);
 }
@@ -465,30 +452,30 @@ __global__ void __launch_bounds__(512) k_pcg(DeviceBsr b, const double2* __restr
 
 } // namespace
 
-void launch_hessian(const DeviceMesh& m, int uniform, float* hb, cudaStream_t st)
+void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st)
 {
     k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
 }
 
-void launch_hessian_expand(const float* hb, int nF, double* out, cudaStream_t st)
+void launch_hessian_expand(const double* hb, int nF, double* out, cudaStream_t st)
 {
     k_hessian_expand<<<(nF + 255) / 256, 256, 0, st>>>(hb, nF, out);
 }
 
-void launch_assemble(const DeviceBsr& b, const float* hb, int nF, double scale, cudaStream_t st)
+void launch_assemble(const DeviceBsr& b, const double* hb, int nF, double scale, cudaStream_t st)
 {
-    k_assemble<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b, hb, nF, static_cast<float>(scale));
+    k_assemble<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b, hb, nF, scale);
 }
 
 int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag)
 {
-    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, -1.0f, dFlag);
+    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, -1.0, dFlag);
     return 0;
 }
 
 void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag)
 {
-    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, static_cast<float>(fixedDiag), dFlag);
+    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, fixedDiag, dFlag);
 }
 
 void launch_spmv(const DeviceBsr& b, const double2* x, double2* y, cudaStream_t st)

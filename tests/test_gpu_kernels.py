@@ -57,13 +57,16 @@ def test_uniform_weight_energy_and_gradient(golden, case):
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_hessian_psd_projection(golden, case):
-    """FP32 projection: per block, error relative to the block's largest entry."""
+    """FP64 projection: per block, error relative to the block's largest entry
+    (eigen-solvers differ -- Jacobi on the 4x4 translation-free part here,
+    Eigen's tridiagonal QR on the 6x6 in the reference -- so agreement is to
+    rounding, not bit-exact)."""
     g = golden(case)
     H = oc.SymDirichletEnergy().computeHessian(mesh_of(g))
     ref_all = O.hessian_blocks(g["rest"], g["F"], g["UV0"])
     scale = np.abs(ref_all).reshape(len(ref_all), -1).max(axis=1)[:, None, None]
     err = np.abs(H - ref_all) / scale
-    assert err.max() < 2e-5, err.max()
+    assert err.max() < 1e-10, err.max()
     # against the reference's own blocks (fixed rows/cols removed there)
     ref = g["H0_blocks"]
     fixed = set(g["fixedVert"].tolist())
@@ -72,10 +75,10 @@ def test_hessian_psd_projection(golden, case):
         keep = np.array([int(g["F"][t, k // 2]) not in fixed for k in range(6)])
         Hm[t][~keep, :] = 0.0
         Hm[t][:, ~keep] = 0.0
-    assert (np.abs(Hm - ref) / scale[: len(ref)]).max() < 2e-5
-    # every projected block is PSD to FP32 accuracy
+    assert (np.abs(Hm - ref) / scale[: len(ref)]).max() < 1e-10
+    # every projected block is PSD to rounding
     ev = np.linalg.eigvalsh(H)
-    assert (ev.min(axis=1) / scale[:, 0, 0]).min() > -1e-5
+    assert (ev.min(axis=1) / scale[:, 0, 0]).min() > -1e-12
 
 
 @pytest.mark.parametrize("case", SCAFFOLD_OFF)
@@ -154,10 +157,10 @@ def test_direct_solver_matches_reference_direction(golden, case):
     b = -par * g["grad0"]
     d = ls.solve(b)
     assert ls.last_relres < 1e-9, ls.last_relres
-    # matrix entries are stored in FP32: the direction agrees with the
-    # reference's FP64 LDL^T to ~cond(A) * 6e-8 in the near-null modes
+    # two exact FP64 LDL^T factorisations with different orderings agree to
+    # ~cond(A) * eps in the near-null modes (the CPU oracle sees the same)
     rel = np.linalg.norm(d - g["dir0"]) / np.linalg.norm(g["dir0"])
-    assert rel < 5e-2, rel
+    assert rel < 5e-3, rel
     st = ls.stats()
     assert st["dof"] == 2 * len(g["UV0"]) and st["fronts"] >= 1
 
@@ -172,14 +175,14 @@ def test_direct_solver_dense_check(golden, case):
     ls.set_pattern(len(g["UV0"]), g["F"], g["fixedVert"])
     ls.update_a(I, J, A[I, J])
     ls.factorize()
-    A32 = A.astype(np.float32).astype(np.float64)
     rng = np.random.default_rng(1)
     b = rng.standard_normal(A.shape[0])
     x = ls.solve(b)
-    x_ref = np.linalg.solve(A32, b)
-    cond = np.linalg.cond(A32)
+    x_ref = np.linalg.solve(A, b)
+    cond = np.linalg.cond(A)
     assert np.linalg.norm(x - x_ref) <= 1e-13 * cond * np.linalg.norm(x_ref)
-    assert np.linalg.norm(A32 @ x - b) <= 1e-10 * np.linalg.norm(b)
+    # backward stable: residual at rounding level of ||A|| ||x||
+    assert np.linalg.norm(A @ x - b) <= 1e-12 * np.linalg.norm(A, 2) * np.linalg.norm(x)
 
 
 @pytest.mark.parametrize("case", ["cube", "icosphere_320"])
@@ -195,13 +198,12 @@ def test_linsys_update_a_multiply_solve(golden, case):
     rng = np.random.default_rng(0)
     x = rng.standard_normal(A.shape[0])
     y = ls.multiply(x)
-    # FP32 storage, FP64 accumulation
-    assert np.linalg.norm(y - A @ x) <= 1e-6 * np.linalg.norm(A) * np.linalg.norm(x)
+    assert np.linalg.norm(y - A @ x) <= 1e-14 * np.linalg.norm(A) * np.linalg.norm(x)
     b = -par * g["grad0"]
     d = ls.solve(b, tol=1e-10, maxIter=50000)
     assert ls.last_converged
-    A32 = A.astype(np.float32).astype(np.float64)
-    assert np.linalg.norm(A32 @ d - b) <= 1e-9 * np.linalg.norm(b)
+    # recursive PCG residual 1e-10; the true residual within rounding of it
+    assert np.linalg.norm(A @ d - b) <= 1e-9 * np.linalg.norm(b) + 1e-13 * np.linalg.norm(A, 2) * np.linalg.norm(d)
 
 
 def test_linsys_iteration_cap_reports_not_converged(golden):
