@@ -105,6 +105,9 @@ int oc_linsys_stats(oc_linsys* ls, double* out8);
 /* The same symbolic analysis without any device call (host only). */
 int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
                           double* out8);
+/* Its vertex elimination order (nV entries), host only. */
+int oc_chol_analyze_order(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
+                          int* vertexOrder);
 /* set_pattern(vNeighbor, fixedVert) (LinSysSolver.hpp:37-135): the vertex
  * adjacency is taken from the triangles F; fixed rows keep only the diagonal. */
 int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF,

@@ -642,6 +642,25 @@ int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, in
     return P.valid ? OC_OK : OC_ERR_INVALID;
 }
 
+int oc_chol_analyze_order(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize, int* order)
+{
+    if (!order) return OC_ERR_INVALID;
+    if (nV <= 0 || nF < 0 || (nF && !F) || nFixed < 0 || (nFixed && !fixedVert)) return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
+    std::vector<unsigned char> mask(nV, 0);
+    for (int i = 0; i < nFixed; ++i) {
+        if (fixedVert[i] < 0 || fixedVert[i] >= nV) return OC_ERR_INVALID;
+        mask[fixedVert[i]] = 1;
+    }
+    std::vector<int> rowPtr, col, diagSlot, cPtr, cIdx;
+    build_pattern(nV, F, nF, mask, rowPtr, col, diagSlot, cPtr, cIdx);
+    oc::CholPlan P;
+    oc::chol_analyze(P, nV, rowPtr.data(), col.data(), leafSize > 0 ? leafSize : 16);
+    std::copy(P.vertOrder.begin(), P.vertOrder.end(), order);
+    return P.valid ? OC_OK : OC_ERR_INVALID;
+}
+
 int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const int* fixedVert, int nFixed)
 {
     if (!ls || nV <= 0 || nF < 0 || (nF && !F) || nFixed < 0 || (nFixed && !fixedVert)) return OC_ERR_INVALID;

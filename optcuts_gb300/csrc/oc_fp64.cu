@@ -234,6 +234,135 @@ __global__ void __launch_bounds__(256) k_init_step(DeviceMesh m, const double2* 
     }
 }
 
+// Cyclic Jacobi eigen-decomposition of a symmetric 6x6: A is destroyed (its
+// diagonal holds the eigenvalues), V receives the eigenvectors as columns.
+__device__ void jacobi_eig6(double A[6][6], double V[6][6])
+{
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+    double fro = 0.0;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) fro += A[i][j] * A[i][j];
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 6; ++p)
+            for (int q = p + 1; q < 6; ++q) off += A[p][q] * A[p][q];
+        if (off <= 1e-34 * fro) break;
+        for (int p = 0; p < 6; ++p) {
+            for (int q = p + 1; q < 6; ++q) {
+                const double apq = A[p][q];
+                if (apq == 0.0) continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 6; ++k) {
+                    const double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - s * akq;
+                    A[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - s * aqk;
+                    A[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+        }
+    }
+}
+
+// Per-triangle Hessian (SymDirichletEnergy.cpp:440-522) projected to PSD by
+// the 6x6 eigen-clamp of IglUtils::makePD (IglUtils.hpp:71-90): unchanged
+// when the smallest eigenvalue is >= 0, otherwise V max(Lambda, 0) V^T.
+// The full 6x6 decomposition matters: for stiff elements (entries up to
+// ~1e26 at a Tutte start) the rounding-level translation components it keeps
+// change the Newton direction, and reducing to the 4-dimensional
+// translation-free part first does not reproduce the reference.
+// Output: the upper triangle as 21 values per triangle (SoA).
+__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, double* __restrict__ hb)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    const int nF = m.nF;
+    const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
+    const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
+    const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
+    const double area_U = 0.5 * (U2m1[0] * U3m1[1] - U2m1[1] * U3m1[0]);
+    const double triAreaSq = m.A2[t];
+    const double areaRatio = triAreaSq / area_U / area_U / area_U;
+    const double dAR = 3.0 / 2.0 * areaRatio / area_U;
+    const double e0d = m.e0d[t], e1d = m.e1d[t], e01d = m.e01d[t];
+    const double w = uniform ? 1.0 : m.w[t];
+    const double leftTerm = 1.0 + triAreaSq / area_U / area_U;
+    const double rightTerm = ((U3m1[0] * U3m1[0] + U3m1[1] * U3m1[1]) * e0d +
+                              (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) / 2. -
+                             (U3m1[0] * U2m1[0] + U3m1[1] * U2m1[1]) * e01d;
+    double ort[3][2];
+    ort[0][0] = U[2].y - U[1].y; ort[0][1] = -(U[2].x - U[1].x);
+    ort[1][0] = U[0].y - U[2].y; ort[1][1] = -(U[0].x - U[2].x);
+    ort[2][0] = U[1].y - U[0].y; ort[2][1] = -(U[1].x - U[0].x);
+    double dL[3][2], dR[3][2];
+    for (int k = 0; k < 3; ++k) { dL[k][0] = areaRatio * ort[k][0]; dL[k][1] = areaRatio * ort[k][1]; }
+    for (int c = 0; c < 2; ++c) {
+        dR[0][c] = (e01d - e0d) * U3m1[c] + (e01d - e1d) * U2m1[c];
+        dR[1][c] = e1d * U2m1[c] - e01d * U3m1[c];
+        dR[2][c] = e0d * U3m1[c] - e01d * U2m1[c];
+    }
+    const double d2R[3][3] = {{e0d + e1d - 2.0 * e01d, e01d - e1d, e01d - e0d},
+                              {e01d - e1d, e1d, -e01d},
+                              {e01d - e0d, -e01d, e0d}};
+    const double skew[3][3] = {{0, 1, -1}, {-1, 0, 1}, {1, -1, 0}};
+    double H[6][6];
+    for (int i = 0; i < 3; ++i) {
+        for (int j = i; j < 3; ++j) {
+            for (int a = 0; a < 2; ++a) {
+                for (int b = 0; b < 2; ++b) {
+                    double d2L = dAR * ort[i][a] * ort[j][b];
+                    if (i != j) d2L += areaRatio * skew[i][j] * ((a == 0 && b == 1) ? -1.0 : ((a == 1 && b == 0) ? 1.0 : 0.0));
+                    const double v = w * (d2L * rightTerm + dL[i][a] * dR[j][b] +
+                                          (a == b ? d2R[i][j] * leftTerm : 0.0) + dR[i][a] * dL[j][b]);
+                    H[2 * i + a][2 * j + b] = v;
+                    H[2 * j + b][2 * i + a] = v;
+                }
+            }
+        }
+    }
+    double A[6][6], V[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
+    jacobi_eig6(A, V);
+    double lam[6], lmin = A[0][0];
+    for (int i = 0; i < 6; ++i) {
+        lam[i] = A[i][i];
+        if (lam[i] < lmin) lmin = lam[i];
+    }
+    if (lmin < 0.0) {
+        for (int i = 0; i < 6; ++i)
+            if (lam[i] < 0.0) lam[i] = 0.0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += V[i][k] * lam[k] * V[j][k];
+                H[i][j] = s;
+            }
+    }
+    for (int a = 0; a < 3; ++a) {
+        hb[(3 * a + 0) * (size_t)nF + t] = H[2 * a][2 * a];
+        hb[(3 * a + 1) * (size_t)nF + t] = H[2 * a][2 * a + 1];
+        hb[(3 * a + 2) * (size_t)nF + t] = H[2 * a + 1][2 * a + 1];
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = a + 1; b < 3; ++b) {
+            const int p = a + b - 1;   // (0,1) -> 0, (0,2) -> 1, (1,2) -> 2
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] = H[2 * a + i][2 * b + j];
+        }
+}
+
 __global__ void k_set_bits(unsigned long long* dst, double v)
 {
     *dst = static_cast<unsigned long long>(__double_as_longlong(v));
@@ -270,6 +399,11 @@ int reduce_blocks_for(int n)
     int b = (n + 255) / 256;
     if (b > 1216) b = 1216;   // 152 SMs x 8 resident 256-thread blocks
     return b < 1 ? 1 : b;
+}
+
+void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st)
+{
+    k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
 }
 
 void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st)

@@ -1,6 +1,6 @@
-// Newton-matrix kernels of the geometry step: per-triangle Hessian with PSD
-// projection, block-CSR assembly, block-Jacobi preconditioner, SpMV and the
-// persistent PCG solve.
+// Newton-matrix kernels of the geometry step: block-CSR assembly of the
+// per-triangle Hessians (computed in oc_fp64.cu), block-Jacobi
+// preconditioner, SpMV and the persistent PCG solve.
 //
 // Precision: FP64 throughout.  The Newton systems are extremely
 // ill-conditioned (a Tutte start has UV triangles 1e-9 times their rest
@@ -21,233 +21,12 @@ namespace cg = cooperative_groups;
 namespace oc {
 namespace {
 
-// Orthonormal basis of the complement of the two rigid translations in the
-// 6-dimensional corner space (u1, v1, u2, v2, u3, v3):
-// columns q1(x)e_x, q1(x)e_y, q2(x)e_x, q2(x)e_y with q1 = (1,-1,0)/sqrt2,
-// q2 = (1,1,-2)/sqrt6.  The SD Hessian annihilates translations, so the
-// eigen-decomposition behind the PSD projection reduces to the 4x4 matrix
-// Q^T H Q (the two translation eigenvalues are zero up to rounding; the
-// reference's 6x6 eigen-clamp sets them to zero too when they round below).
-__constant__ double kQ1[3] = {0.70710678118654752440, -0.70710678118654752440, 0.0};
-__constant__ double kQ2[3] = {0.40824829046386301637, 0.40824829046386301637, -0.81649658092772603273};
-
-__device__ __forceinline__ double qv(int col, int row)
-{
-    // Q[row][col], row in 0..5 (vertex = row/2, comp = row%2), col in 0..3
-    const int vert = row >> 1, comp = row & 1;
-    const int qi = col >> 1, qc = col & 1;
-    if (comp != qc) return 0.0;
-    return qi == 0 ? kQ1[vert] : kQ2[vert];
-}
-
-// Cyclic Jacobi on a symmetric 4x4 (FP64).  A -> diag(eigenvalues), V columns = eigenvectors.
-__device__ void jacobi4(double A[4][4], double V[4][4])
-{
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
-    double fro = 0.0;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) fro += A[i][j] * A[i][j];
-    for (int sweep = 0; sweep < 30; ++sweep) {
-        double off = 0.0;
-#pragma unroll
-        for (int p = 0; p < 4; ++p)
-#pragma unroll
-            for (int q = p + 1; q < 4; ++q) off += A[p][q] * A[p][q];
-        if (!(off > 1e-32 * fro)) break;
-#pragma unroll
-        for (int p = 0; p < 3; ++p) {
-#pragma unroll
-            for (int q = p + 1; q < 4; ++q) {
-                const double apq = A[p][q];
-                if (apq == 0.0) continue;
-                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
-                const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
-                const double c = 1.0 / sqrt(fma(t, t, 1.0)), s = t * c;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const double akp = A[k][p], akq = A[k][q];
-                    A[k][p] = c * akp - s * akq;
-                    A[k][q] = s * akp + c * akq;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const double apk = A[p][k], aqk = A[q][k];
-                    A[p][k] = c * apk - s * aqk;
-                    A[q][k] = s * apk + c * aqk;
-                }
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const double vkp = V[k][p], vkq = V[k][q];
-                    V[k][p] = c * vkp - s * vkq;
-                    V[k][q] = s * vkp + c * vkq;
-                }
-            }
-        }
-    }
-}
-
 // Packed symmetric 6x6: 3 diagonal 2x2 blocks (xx, xy, yy) at 0..8, then
 // off-diagonal blocks (0,1), (0,2), (1,2) row-major at 9..20.
 __device__ __forceinline__ int pair_index(int a, int b) { return a + b - 1; }   // (0,1)->0 (0,2)->1 (1,2)->2
 
 // Per-triangle Hessian (SymDirichletEnergy.cpp:440-522) projected to PSD
 // (IglUtils::makePD, IglUtils.hpp:71-90), all FP64.
-__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, double* __restrict__ hb)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m.nF) return;
-    const int nF = m.nF;
-    const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
-    const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
-    const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
-    const double area_U = 0.5 * (U2m1[0] * U3m1[1] - U2m1[1] * U3m1[0]);
-    const double A2 = m.A2[t];
-    const double areaRatio = A2 / area_U / area_U / area_U;
-    const double dAR = 3.0 / 2.0 * areaRatio / area_U;
-    const double w = uniform ? 1.0 : m.w[t];
-    // e0SqLen_div_dbAreaSq etc. (TriMesh.cpp:391-393)
-    const double e0d = m.e0d[t], e1d = m.e1d[t], e01d = m.e01d[t];
-    const double leftTerm = 1.0 + A2 / area_U / area_U;
-    const double rightTerm = ((U3m1[0] * U3m1[0] + U3m1[1] * U3m1[1]) * e0d +
-                              (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) / 2. -
-                             (U3m1[0] * U2m1[0] + U3m1[1] * U2m1[1]) * e01d;
-    double ort[3][2], dL[3][2], dR[3][2];
-    ort[0][0] = U[2].y - U[1].y; ort[0][1] = -(U[2].x - U[1].x);
-    ort[1][0] = U[0].y - U[2].y; ort[1][1] = -(U[0].x - U[2].x);
-    ort[2][0] = U[1].y - U[0].y; ort[2][1] = -(U[1].x - U[0].x);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { dL[k][0] = areaRatio * ort[k][0]; dL[k][1] = areaRatio * ort[k][1]; }
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-        dR[0][c] = (e01d - e0d) * U3m1[c] + (e01d - e1d) * U2m1[c];
-        dR[1][c] = e1d * U2m1[c] - e01d * U3m1[c];
-        dR[2][c] = e0d * U3m1[c] - e01d * U2m1[c];
-    }
-    const double d2R[3][3] = {{e0d + e1d - 2.0 * e01d, e01d - e1d, e01d - e0d},
-                              {e01d - e1d, e1d, -e01d},
-                              {e01d - e0d, -e01d, e0d}};
-    const double skew[3][3] = {{0, 1, -1}, {-1, 0, 1}, {1, -1, 0}};
-    double H[6][6];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-        for (int j = i; j < 3; ++j) {
-#pragma unroll
-            for (int a = 0; a < 2; ++a) {
-#pragma unroll
-                for (int b = 0; b < 2; ++b) {
-                    double d2L = dAR * ort[i][a] * ort[j][b];
-                    if (i != j) d2L += areaRatio * skew[i][j] * ((a == 0 && b == 1) ? -1.0 : ((a == 1 && b == 0) ? 1.0 : 0.0));
-                    const double v = w * (d2L * rightTerm + dL[i][a] * dR[j][b] +
-                                          (a == b ? d2R[i][j] * leftTerm : 0.0) + dR[i][a] * dL[j][b]);
-                    H[2 * i + a][2 * j + b] = v;
-                    H[2 * j + b][2 * i + a] = v;
-                }
-            }
-        }
-    }
-    // M = Q^T H Q
-    double HQ[6][4];
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            double s = 0.0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) s = fma(H[i][k], qv(c, k), s);
-            HQ[i][c] = s;
-        }
-    double M[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            double s = 0.0;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) s = fma(qv(r, k), HQ[k][c], s);
-            M[r][c] = s;
-        }
-    // PSD test by the LDL^T pivots of M (positive pivots <=> positive definite)
-    bool pd = true;
-    {
-        double L[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) L[i][j] = M[i][j];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const double d = L[k][k];
-            if (!(d > 0.0)) pd = false;
-            const double id = (d > 0.0) ? 1.0 / d : 0.0;
-#pragma unroll
-            for (int i = k + 1; i < 4; ++i) {
-                const double f = L[i][k] * id;
-#pragma unroll
-                for (int j = k + 1; j < 4; ++j) L[i][j] -= f * L[k][j];
-            }
-        }
-    }
-    if (!pd) {
-        double V[4][4];
-        jacobi4(M, V);
-        double lam[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) lam[k] = fmax(M[k][k], 0.0);
-        double Mp[4][4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                double s = 0.0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) s = fma(V[r][k] * lam[k], V[c][k], s);
-                Mp[r][c] = s;
-            }
-        double QM[6][4];
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                double s = 0.0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) s = fma(qv(k, i), Mp[k][c], s);
-                QM[i][c] = s;
-            }
-#pragma unroll
-        for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int j = 0; j < 6; ++j) {
-                double s = 0.0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) s = fma(QM[i][k], qv(k, j), s);
-                H[i][j] = s;
-            }
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        hb[(3 * a + 0) * (size_t)nF + t] = H[2 * a][2 * a];
-        hb[(3 * a + 1) * (size_t)nF + t] = 0.5 * (H[2 * a][2 * a + 1] + H[2 * a + 1][2 * a]);
-        hb[(3 * a + 2) * (size_t)nF + t] = H[2 * a + 1][2 * a + 1];
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = a + 1; b < 3; ++b) {
-            const int p = pair_index(a, b);
-#pragma unroll
-            for (int i = 0; i < 2; ++i)
-#pragma unroll
-                for (int j = 0; j < 2; ++j)
-                    hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] = 0.5 * (H[2 * a + i][2 * b + j] + H[2 * b + j][2 * a + i]);
-        }
-}
-
 __device__ __forceinline__ Blk2 local_block(const double* __restrict__ hb, int nF, int code)
 {
     const int t = code / 9, ab = code - 9 * t, a = ab / 3, b = ab - 3 * a;
@@ -451,11 +230,6 @@ __global__ void __launch_bounds__(512) k_pcg(DeviceBsr b, const double2* __restr
 }
 
 } // namespace
-
-void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st)
-{
-    k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
-}
 
 void launch_hessian_expand(const double* hb, int nF, double* out, cudaStream_t st)
 {

@@ -510,7 +510,30 @@ void ocr_init_step_size(const int* F, int nF, const double* UV, const double* di
     *stepSize = step;
 }
 
+static ocr_solver* solver_create(int nV, const int* F, int nF, const int* fixedVert, int nFixed, const double* Vr,
+                                 const int* givenOrder);
+
 ocr_solver* ocr_solver_create(int nV, const int* F, int nF, const int* fixedVert, int nFixed, const double* Vr)
+{
+    return solver_create(nV, F, nF, fixedVert, nFixed, Vr, nullptr);
+}
+
+ocr_solver* ocr_solver_create_ordered(int nV, const int* F, int nF, const int* fixedVert, int nFixed,
+                                      const int* vertexOrder)
+{
+    return solver_create(nV, F, nF, fixedVert, nFixed, nullptr, vertexOrder);
+}
+
+int ocr_solver_negative_pivots(const ocr_solver* s)
+{
+    const Solver& S = *reinterpret_cast<const Solver*>(s);
+    int n = 0;
+    for (double d : S.D) n += d < 0.0;
+    return n;
+}
+
+static ocr_solver* solver_create(int nV, const int* F, int nF, const int* fixedVert, int nFixed, const double* Vr,
+                                 const int* givenOrder)
 {
     Solver* S = new Solver;
     S->nV = nV;
@@ -545,7 +568,8 @@ ocr_solver* ocr_solver_create(int nV, const int* F, int nF, const int* fixedVert
     for (int v = 0; v < nV; ++v) verts[v] = v;
     int tagCounter = 0;
     S->order.clear();
-    nested_dissection(*S, Vr, verts, tag, tagCounter, S->order);
+    if (givenOrder) S->order.assign(givenOrder, givenOrder + nV);
+    else nested_dissection(*S, Vr, verts, tag, tagCounter, S->order);
     S->pinv.assign(nV, 0);
     for (int k = 0; k < nV; ++k) S->pinv[S->order[k]] = k;
     symbolic(*S);

@@ -54,6 +54,11 @@ void ocr_init_step_size(const int* F, int nF, const double* UV, const double* di
 typedef struct ocr_solver ocr_solver;
 ocr_solver* ocr_solver_create(int nV, const int* F, int nF, const int* fixedVert, int nFixed,
                               const double* V_rest);
+/* Same factorisation under a caller-given vertex elimination order. */
+ocr_solver* ocr_solver_create_ordered(int nV, const int* F, int nF, const int* fixedVert, int nFixed,
+                                      const int* vertexOrder);
+/* Number of negative D entries of the last factorisation. */
+int ocr_solver_negative_pivots(const ocr_solver*);
 void ocr_solver_destroy(ocr_solver*);
 /* blocks: nF x 36 (as from ocr_hessian_blocks), scaled by param; returns 0 or -1 on a non-positive pivot */
 int ocr_solver_factorize(ocr_solver*, const double* blocks, double param);
