@@ -84,6 +84,30 @@ int oc_sd_hessian_blocks(oc_mesh* mesh, int uniformWeight, double* blocks);
  * *stepSize in place to the largest inversion-free step along searchDir. */
 int oc_sd_init_step_size(oc_mesh* mesh, const double* searchDir, double* stepSize);
 
+/* Allocation-free energy evaluation (no counterpart in the reference; an
+ * addition for callers that cannot allocate device memory themselves -- e.g.
+ * code running inside a host framework that owns every allocation, or work
+ * recorded into an externally managed CUDA graph).  Computes, on the given
+ * stream, E_k = sum over triangles of the symmetric Dirichlet energy at
+ * UV + alphas[k] * dir for k < nTrials (dir NULL: the energy at UV), the
+ * line-search evaluation of Optimizer::lineSearch (Optimizer.cpp:593-610).
+ * All pointers except `alphas` (host, nTrials values) are DEVICE pointers
+ * owned by the caller:
+ *   F        nF x 3 int32 row-major       UV, dir   nV x 2 float64 row-major
+ *   rest     nF x 8 float64, the layout of oc_mesh_rest_constants
+ *   energies nTrials float64 (output; unweighted by energyParams)
+ * surfaceArea is TriMesh::surfaceArea (the area weights' normaliser).
+ * It calls no cudaMalloc/cudaFree: block partial sums go to a static device
+ * array sized for 1216 blocks x 8 trials (76 KB, held by every GPU that loads
+ * the library until exit).  nTrials must be 1..8 (else OC_ERR_INVALID).
+ * The first call on each device looks the array's address up
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU (different
+ * streams, no ordering) race and must be serialised by the caller. */
+int oc_sd_energy_trials_noalloc(const int* F, const double* UV, const double* dir, const double* rest,
+                                double surfaceArea, int nF, const double* alphas, int nTrials, int uniformWeight,
+                                double* energies, void* stream);
+
 /* ---- LinSysSolver (LinSysSolver.hpp:22-187, EigenLibSolver.cpp:21-107) --
  * Full-symmetric 2x2-block CSR on the device.  Two solvers:
  *   OC_SOLVER_DIRECT  multifrontal sparse Cholesky (FP64 fronts), the exact

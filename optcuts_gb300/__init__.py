@@ -91,6 +91,8 @@ _SIGS = {
     "oc_optimizer_phase_ms": [_vp, _d],
     "oc_optimizer_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_solver_stats": [_vp, _d],
+    "oc_sd_energy_trials_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
+                                    _vp, _vp],
 }
 
 

@@ -12,6 +12,7 @@
 #include "oc_internal.h"
 
 #include <cstdint>
+#include <mutex>
 
 namespace oc {
 namespace {
@@ -401,6 +402,53 @@ int reduce_blocks_for(int n)
     return b < 1 ? 1 : b;
 }
 
+// ------------------------------------------------- allocation-free energy
+// Variant of k_energy for caller-owned, reference-layout device arrays (F
+// nF x 3, rest nF x 8), with its block partials in a file-scope device array
+// instead of an allocation.  Callers that cannot allocate (a host framework
+// owning all device memory, externally captured graphs) use it through
+// oc_sd_energy_trials_noalloc.
+namespace {
+
+constexpr int kNoAllocBlocks = 1216;
+static __device__ __align__(256) double g_noallocPartials[kNoAllocBlocks * kMaxTrials];
+
+template <int NT>
+__global__ void __launch_bounds__(256) k_energy_aos(const int* __restrict__ F, const double2* __restrict__ uv,
+                                                    const double2* __restrict__ dir, const double* __restrict__ rest,
+                                                    double surfaceArea, int nF, Alphas alphas, int nTrials,
+                                                    int uniform, double* partials)
+{
+    double acc[NT];
+#pragma unroll
+    for (int k = 0; k < NT; ++k) acc[k] = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nF; t += gridDim.x * blockDim.x) {
+        const int i0 = F[3 * t], i1 = F[3 * t + 1], i2 = F[3 * t + 2];
+        const double* r = rest + 8 * (size_t)t;
+        const double w = uniform ? 1.0 : r[0] / surfaceArea;
+        const double A2 = r[1], e0 = r[2], e1 = r[3], e01 = r[4];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            if (k < nTrials) {
+                const double a = alphas.a[k];
+                const double2 U1 = at(uv, dir, a, i0), U2 = at(uv, dir, a, i1), U3 = at(uv, dir, a, i2);
+                const double a0 = U2.x - U1.x, a1 = U2.y - U1.y;
+                const double b0 = U3.x - U1.x, b1 = U3.y - U1.y;
+                const double area_U = 0.5 * (a0 * b1 - a1 * b0);
+                acc[k] += w * (1.0 + A2 / area_U / area_U) *
+                          (((b0 * b0 + b1 * b1) * e0 + (a0 * a0 + a1 * a1) * e1) / 4 / A2 -
+                           (b0 * a0 + b1 * a1) * e01 / 2 / A2);
+            }
+        }
+    }
+    block_sum_store<NT>(acc, nTrials, partials + (size_t)blockIdx.x * kMaxTrials);
+}
+
+std::mutex g_noallocMu;
+double* g_noallocPtr[256] = {};
+
+} // namespace
+
 void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st)
 {
     k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
@@ -458,4 +506,49 @@ void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st)
     k_check_inversion<<<reduce_blocks_for(m.nF), 256, 0, st>>>(m, s.minBits);
 }
 
+// Device address of the file-scope partials array for the current device;
+// looked up once per device (host code cannot use the symbol directly: its
+// host-side name is only a stand-in for the device array).
+static int noalloc_scratch(double** out)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return OC_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_noallocMu);
+    if (!g_noallocPtr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noallocPartials) != cudaSuccess || !p) return OC_ERR_CUDA;
+        g_noallocPtr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noallocPtr[dev];
+    return OC_OK;
+}
+
 } // namespace oc
+
+extern "C" __attribute__((visibility("default"))) int
+oc_sd_energy_trials_noalloc(const int* F, const double* UV, const double* dir, const double* rest, double surfaceArea,
+                            int nF, const double* alphas, int nTrials, int uniformWeight, double* energies,
+                            void* stream)
+{
+    using namespace oc;
+    if (!F || !UV || !rest || !energies || nF <= 0 || !(surfaceArea > 0.0)) return OC_ERR_INVALID;
+    if (nTrials < 1 || nTrials > kMaxTrials) return OC_ERR_INVALID;   // scratch holds 8 trials per block
+    if (dir && !alphas) return OC_ERR_INVALID;
+    double* partials = nullptr;
+    int rc = noalloc_scratch(&partials);
+    if (rc) return rc;
+    Alphas a = {{0, 0, 0, 0, 0, 0, 0, 0}};
+    for (int k = 0; k < nTrials; ++k) a.a[k] = alphas ? alphas[k] : 0.0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = reduce_blocks_for(nF);   // <= kNoAllocBlocks
+    const double2* uv = reinterpret_cast<const double2*>(UV);
+    const double2* d = reinterpret_cast<const double2*>(dir);
+    if (nTrials == 1)
+        k_energy_aos<1><<<nb, 256, 0, st>>>(F, uv, d, rest, surfaceArea, nF, a, 1, uniformWeight, partials);
+    else if (nTrials <= 4)
+        k_energy_aos<4><<<nb, 256, 0, st>>>(F, uv, d, rest, surfaceArea, nF, a, nTrials, uniformWeight, partials);
+    else
+        k_energy_aos<8><<<nb, 256, 0, st>>>(F, uv, d, rest, surfaceArea, nF, a, nTrials, uniformWeight, partials);
+    k_reduce_final<<<1, 256, 0, st>>>(partials, nb, nTrials, energies);
+    return cudaGetLastError() == cudaSuccess ? OC_OK : OC_ERR_CUDA;
+}
