@@ -272,6 +272,19 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             if ((int)P.tasks.size() > off) P.launches.push_back({3, l, p, off, (int)P.tasks.size() - off, 0});
         }
     }
+    // substitution chunks of the rectangular part of each front, per level
+    P.rectRowOff.assign(P.nLevels + 1, 0);
+    P.rectColOff.assign(P.nLevels + 1, 0);
+    for (int l = 0; l < P.nLevels; ++l) {
+        for (int i = P.levelFrontOff[l]; i < P.levelFrontOff[l + 1]; ++i) {
+            const int f = P.levelFronts[i];
+            for (int r0 = P.fk[f]; r0 < P.fm[f]; r0 += kRectRows) P.rectRowTasks.push_back(make_int2(f, r0));
+            if (P.fm[f] > P.fk[f])
+                for (int c0 = 0; c0 < P.fk[f]; c0 += kRectCols) P.rectColTasks.push_back(make_int2(f, c0));
+        }
+        P.rectRowOff[l + 1] = static_cast<int>(P.rectRowTasks.size());
+        P.rectColOff[l + 1] = static_cast<int>(P.rectColTasks.size());
+    }
     // assembly map: block slot (r, c) with pos[r] >= pos[c] goes to the front owning c
     std::vector<int> owner(nV);
     for (int f = 0; f < nF; ++f)
@@ -356,81 +369,78 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
 // LDL^T of the diagonal tile of panel p, in place: unit-lower L below the
 // diagonal, D on the diagonal (the factorisation SimplicialLDLT computes;
 // negative pivots are allowed, a zero or non-finite one is counted and
-// replaced by 1e-300).
-__global__ void __launch_bounds__(256) k_ldl_diag(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                  const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                  double* __restrict__ pool, int* flag)
+// replaced by 1e-300).  One warp per tile: lane r keeps row r in registers,
+// the pivot column is broadcast with shuffles -- no shared memory, no
+// block barriers on this serial step of the factorisation.
+__global__ void __launch_bounds__(32) k_ldl_diag(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                 const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                 double* __restrict__ pool, int* flag)
 {
-    __shared__ double A[kTile][kTile + 1];
-    __shared__ double T[kTile];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w;
     tile_bounds(k, m, t.p, s0, w);
     double* F = pool + foff[t.front];
-    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-        const int r = e % kTile, c = e / kTile;
-        A[r][c] = (r < w && c < w && r >= c) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
-    }
-    __syncthreads();
-    for (int c = 0; c < w; ++c) {
-        if (threadIdx.x == 0) {
-            const double d = A[c][c];
+    const int r = threadIdx.x;
+    double a[kTile];
+#pragma unroll
+    for (int c = 0; c < kTile; ++c) a[c] = (r < w && c < w && c <= r) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
+#pragma unroll
+    for (int c = 0; c < kTile; ++c) {
+        if (c < w) {
+            double d = __shfl_sync(0xffffffffu, a[c], c);
             if (!(d != 0.0) || !isfinite(d)) {
-                atomicAdd(flag, 1);
-                A[c][c] = 1e-300;
+                if (r == 0) atomicAdd(flag, 1);
+                d = 1e-300;
+                if (r == c) a[c] = d;
             }
+            const double tr = a[c];   // A[r][c] before scaling (row r > c)
+            const double l = tr / d;
+#pragma unroll
+            for (int c2 = c + 1; c2 < kTile; ++c2) {
+                const double tc2 = __shfl_sync(0xffffffffu, tr, c2);
+                if (c2 < w && r >= c2) a[c2] = fma(-l, tc2, a[c2]);
+            }
+            if (r > c) a[c] = l;
         }
-        __syncthreads();
-        const double d = A[c][c];
-        for (int r = c + 1 + threadIdx.x; r < w; r += blockDim.x) T[r] = A[r][c];
-        __syncthreads();
-        const double inv = 1.0 / d;
-        const int n = w - c - 1;
-        for (int r = c + 1 + threadIdx.x; r < w; r += blockDim.x) A[r][c] = T[r] * inv;
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-            const int r = c + 1 + e % n, c2 = c + 1 + e / n;
-            if (r >= c2) A[r][c2] -= T[r] * inv * T[c2];
-        }
-        __syncthreads();
     }
-    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
-        const int r = e % w, c = e / w;
-        if (r >= c) F[(s0 + r) + (long long)(s0 + c) * m] = A[r][c];
-    }
+#pragma unroll
+    for (int c = 0; c < kTile; ++c)
+        if (r < w && c <= r && c < w) F[(s0 + r) + (long long)(s0 + c) * m] = a[c];
 }
 
-// L(i, p) = A(i, p) * L(p, p)^-T * D_p^-1 for a tile row below the diagonal tile.
-__global__ void __launch_bounds__(256) k_ldl_trsm(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                  const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                  double* __restrict__ pool)
+// L(i, p) = A(i, p) * L(p, p)^-T * D_p^-1 for a tile row below the diagonal
+// tile.  One warp per tile row: lane r solves row r in registers against the
+// diagonal tile, read from shared memory by broadcast.
+__global__ void __launch_bounds__(32) k_ldl_trsm(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                 const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                 double* __restrict__ pool)
 {
     __shared__ double L[kTile][kTile + 1];
-    __shared__ double X[kTile][kTile + 1];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w, r0, h;
     tile_bounds(k, m, t.p, s0, w);
     tile_bounds(k, m, t.i, r0, h);
     double* F = pool + foff[t.front];
-    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-        const int r = e % kTile, c = e / kTile;
-        L[r][c] = (r < w && c < w && r >= c) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
-        X[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
-    }
-    __syncthreads();
-    for (int c = 0; c + 1 < w; ++c) {
-        const int n = w - c - 1;
-        for (int e = threadIdx.x; e < h * n; e += blockDim.x) {
-            const int r = e % h, c2 = c + 1 + e / h;
-            X[r][c2] -= X[r][c] * L[c2][c];
+    const int r = threadIdx.x;
+#pragma unroll 4
+    for (int c = 0; c < kTile; ++c) L[r][c] = (r < w && c < w && c <= r) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
+    double x[kTile];
+#pragma unroll
+    for (int c = 0; c < kTile; ++c) x[c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
+    __syncwarp();
+#pragma unroll
+    for (int c = 0; c < kTile; ++c) {
+        if (c < w) {
+#pragma unroll
+            for (int c2 = c + 1; c2 < kTile; ++c2)
+                if (c2 < w) x[c2] = fma(-x[c], L[c2][c], x[c2]);
         }
-        __syncthreads();
     }
-    for (int e = threadIdx.x; e < h * w; e += blockDim.x) {
-        const int r = e % h, c = e / h;
-        F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c] / L[c][c];
-    }
+#pragma unroll
+    for (int c = 0; c < kTile; ++c)
+        if (r < h && c < w) F[(r0 + r) + (long long)(s0 + c) * m] = x[c] / L[c][c];
 }
 
 // C(i, j) -= L(i, p) * D_p * L(j, p)^T  (trailing update, FP64)
@@ -483,11 +493,12 @@ __global__ void k_permute_out(const double* __restrict__ xp, const int* __restri
     if (j < n) x[perm[j]] = xp[j];
 }
 
-// Forward substitution of one front (one CTA per front of the level), in
-// 32-column blocks: warp 0 solves the unit-lower diagonal block with
-// shuffles, then every thread updates the rows below (coalesced column
-// reads).  The pivots' values leave divided by D (z = D^-1 y); the update
-// vector for the parent leaves in upd.
+// Forward substitution, pivot part of one front (one CTA per front of the
+// level): gather this front's right-hand side plus the children's update
+// vectors (fixed child order), solve the unit-lower L11 y = b in 32-column
+// blocks (warp-shuffle diagonal block, coalesced column updates of the
+// remaining pivot rows), store y (not yet divided by D) and the gathered
+// right-hand side of the non-pivot rows, which k_fwd_rect then updates.
 __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
                                              const int* __restrict__ fm, const long long* __restrict__ foff,
                                              const long long* __restrict__ fupd, const int* __restrict__ fdof,
@@ -522,7 +533,7 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
             if (lane < w) sh[c0 + lane] = v;
         }
         __syncthreads();
-        for (int r = c0 + w + threadIdx.x; r < m; r += blockDim.x) {
+        for (int r = c0 + w + threadIdx.x; r < k; r += blockDim.x) {
             double s = 0.0;
             for (int c = 0; c < w; ++c) s = fma(L[r + (long long)(c0 + c) * m], sh[c0 + c], s);
             sh[r] -= s;
@@ -530,37 +541,84 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
         __syncthreads();
     }
     for (int r = threadIdx.x; r < m; r += blockDim.x) {
-        if (r < k) y[d0 + r] = sh[r] / L[r + (long long)r * m];
+        if (r < k) y[d0 + r] = sh[r];
         else upd[fupd[f] + (r - k)] = sh[r];
     }
 }
 
-// Backward substitution of one front: x_S = L11^-T (z_S - L21^T x_B), unit
-// diagonal, in 32-column blocks from the last: the block's dot products with
-// the rows below (one warp per column, strided), then warp 0 solves the
-// diagonal block with shuffles.
+// Forward substitution, non-pivot rows: upd_r -= sum_c L21[r][c] y_c, one CTA
+// per chunk of kRectRows rows of one front (all fronts of a level per launch).
+__global__ void __launch_bounds__(kRectRows) k_fwd_rect(const int2* __restrict__ tasks, const int* __restrict__ fk,
+                                                        const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                        const long long* __restrict__ fupd, const int* __restrict__ fdof,
+                                                        const double* __restrict__ pool, double* __restrict__ upd,
+                                                        const double* __restrict__ y)
+{
+    extern __shared__ double ys[];
+    const int2 t = tasks[blockIdx.x];
+    const int f = t.x, k = fk[f], m = fm[f], d0 = fdof[f];
+    for (int c = threadIdx.x; c < k; c += blockDim.x) ys[c] = y[d0 + c];
+    __syncthreads();
+    const int r = t.y + threadIdx.x;
+    if (r >= m) return;
+    const double* L = pool + foff[f] + r;
+    double s0 = 0.0, s1 = 0.0;
+    int c = 0;
+    for (; c + 1 < k; c += 2) {
+        s0 = fma(L[(long long)c * m], ys[c], s0);
+        s1 = fma(L[(long long)(c + 1) * m], ys[c + 1], s1);
+    }
+    if (c < k) s0 = fma(L[(long long)c * m], ys[c], s0);
+    upd[fupd[f] + (r - k)] -= s0 + s1;
+}
+
+// Backward substitution, non-pivot part: t_c = sum_{r >= k} L21[r][c] x_r for
+// a chunk of kRectCols pivot columns of one front (a warp per column).
+__global__ void __launch_bounds__(256) k_bwd_rect(const int2* __restrict__ tasks, const int* __restrict__ fk,
+                                                  const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                  const int* __restrict__ fdof, const int* __restrict__ frowOff,
+                                                  const int* __restrict__ rowIdx, const double* __restrict__ pool,
+                                                  const double* __restrict__ x, double* __restrict__ tdot)
+{
+    const int2 t = tasks[blockIdx.x];
+    const int f = t.x, k = fk[f], m = fm[f], d0 = fdof[f];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = t.y + warp;
+    if (c >= k || warp >= kRectCols) return;
+    const int* rows = rowIdx + frowOff[f];
+    const double* lc = pool + foff[f] + (long long)c * m;
+    double s = 0.0;
+    for (int r = k + lane; r < m; r += 32) s = fma(lc[r], x[rows[r]], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) tdot[d0 + c] = s;
+}
+
+// Backward substitution, pivot part of one front: x_S = L11^-T (D^-1 y_S - t)
+// with t = L21^T x_B from k_bwd_rect (zero for fronts without ancestors), in
+// 32-column blocks from the last.
 __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, const int* __restrict__ fk,
                                              const int* __restrict__ fm, const long long* __restrict__ foff,
-                                             const int* __restrict__ fdof, const int* __restrict__ frowOff,
-                                             const int* __restrict__ rowIdx, const double* __restrict__ pool,
-                                             const double* __restrict__ y, double* __restrict__ x)
+                                             const int* __restrict__ fdof, const double* __restrict__ pool,
+                                             const double* __restrict__ y, const double* __restrict__ tdot,
+                                             double* __restrict__ x)
 {
     extern __shared__ double sh[];
     __shared__ double dots[32];
     const int f = fronts[blockIdx.x];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int* rows = rowIdx + frowOff[f];
-    for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : x[rows[r]];
-    __syncthreads();
     const double* L = pool + foff[f];
+    const bool rect = m > k;
+    for (int r = threadIdx.x; r < k; r += blockDim.x)
+        sh[r] = y[d0 + r] / L[r + (long long)r * m] - (rect ? tdot[d0 + r] : 0.0);
+    __syncthreads();
     const int nBlocks = (k + 31) / 32;
     for (int b = nBlocks - 1; b >= 0; --b) {
         const int c0 = 32 * b, w = min(32, k - c0);
         for (int c = warp; c < w; c += nw) {
             const double* lc = L + (long long)(c0 + c) * m;
             double s = 0.0;
-            for (int r = c0 + w + lane; r < m; r += 32) s = fma(lc[r], sh[r], s);
+            for (int r = c0 + w + lane; r < k; r += 32) s = fma(lc[r], sh[r], s);
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (lane == 0) dots[c] = s;
         }
@@ -607,6 +665,8 @@ int chol_upload(CholPlan& P, std::string* err)
     chk(up(&P.dChildList, P.childList)); chk(up(&P.dRelOff, P.relOff)); chk(up(&P.dRelIdx, P.relIdx));
     chk(up(&P.dLevelFronts, P.levelFronts)); chk(up(&P.dTasks, P.tasks)); chk(up(&P.dAsmDest, P.asmDest));
     chk(up(&P.dAsmLd, P.asmLd)); chk(up(&P.dAsmDiag, P.asmDiag));
+    chk(up(&P.dRectRowTasks, P.rectRowTasks)); chk(up(&P.dRectColTasks, P.rectColTasks));
+    chk(cudaMalloc(&P.tmpDot, sizeof(double) * (size_t)std::max(P.nDof, 1)));
     chk(cudaMalloc(&P.dFlag, sizeof(int)));
     if (e != cudaSuccess) {
         if (err) *err = std::string("chol upload: ") + cudaGetErrorString(e);
@@ -624,6 +684,9 @@ void chol_free(CholPlan& P)
     cudaFree(P.dFoff); cudaFree(P.dFupd); cudaFree(P.dRowIdx); cudaFree(P.dChildOff); cudaFree(P.dChildList);
     cudaFree(P.dRelOff); cudaFree(P.dRelIdx); cudaFree(P.dLevelFronts); cudaFree(P.dTasks);
     cudaFree(P.dAsmDest); cudaFree(P.dAsmLd); cudaFree(P.dAsmDiag); cudaFree(P.dFlag);
+    cudaFree(P.dRectRowTasks); cudaFree(P.dRectColTasks); cudaFree(P.tmpDot);
+    P.dRectRowTasks = P.dRectColTasks = nullptr;
+    P.tmpDot = nullptr;
     P.pool = P.upd = P.yperm = P.xperm = nullptr;
     P.dPermDof = P.dFk = P.dFm = P.dFdofStart = P.dFrowOff = nullptr;
     P.dFoff = P.dFupd = nullptr;
@@ -646,8 +709,8 @@ int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string
         const TileTask* t = P.dTasks + L.taskOff;
         switch (L.kind) {
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
-        case 1: k_ldl_diag<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        case 2: k_ldl_trsm<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        case 1: k_ldl_diag<<<L.taskCount, 32, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        case 2: k_ldl_trsm<<<L.taskCount, 32, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         }
     }
@@ -672,20 +735,31 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
     if (!P.onDevice) return OC_ERR_INVALID;
     const int n = P.nDof;
     k_permute_in<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(rhs), P.dPermDof, sign, n, P.yperm);
-    const size_t shm = sizeof(double) * (size_t)P.maxM;
+    int maxK = 0;
+    for (int f = 0; f < P.nFronts; ++f) maxK = std::max(maxK, P.fk[f]);
+    const size_t shm = sizeof(double) * (size_t)P.maxM, shmK = sizeof(double) * (size_t)std::max(maxK, 1);
     if (shm > 48 * 1024) {
         cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         cudaFuncSetAttribute(k_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     }
+    if (shmK > 48 * 1024) cudaFuncSetAttribute(k_fwd_rect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmK);
     for (int l = 0; l < P.nLevels; ++l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
         k_fwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart, P.dChildOff,
                                      P.dChildList, P.dRelOff, P.dRelIdx, P.pool, P.upd, P.yperm);
+        const int ro = P.rectRowOff[l], rc = P.rectRowOff[l + 1] - ro;
+        if (rc)
+            k_fwd_rect<<<rc, kRectRows, shmK, st>>>(P.dRectRowTasks + ro, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart,
+                                                    P.pool, P.upd, P.yperm);
     }
     for (int l = P.nLevels - 1; l >= 0; --l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
-        k_bwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFdofStart, P.dFrowOff, P.dRowIdx,
-                                     P.pool, P.yperm, P.xperm);
+        const int co = P.rectColOff[l], cc = P.rectColOff[l + 1] - co;
+        if (cc)
+            k_bwd_rect<<<cc, 32 * kRectCols, 0, st>>>(P.dRectColTasks + co, P.dFk, P.dFm, P.dFoff, P.dFdofStart,
+                                                      P.dFrowOff, P.dRowIdx, P.pool, P.xperm, P.tmpDot);
+        k_bwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFdofStart, P.pool, P.yperm,
+                                     P.tmpDot, P.xperm);
     }
     k_permute_out<<<(n + 255) / 256, 256, 0, st>>>(P.xperm, P.dPermDof, n, reinterpret_cast<double*>(x));
     cudaError_t e = cudaGetLastError();

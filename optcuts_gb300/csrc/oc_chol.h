@@ -10,7 +10,9 @@
 
 namespace oc {
 
-constexpr int kTile = 32;   // dense tile edge (FP64) of the front kernels
+constexpr int kTile = 32;      // dense tile edge (FP64) of the front kernels
+constexpr int kRectRows = 256; // rows of L21 per CTA in the forward GEMV
+constexpr int kRectCols = 8;   // columns of L21 per CTA in the backward GEMV^T
 
 struct TileTask {           // one CTA's work item in a tiled front kernel
     int front, i, j, p;
@@ -37,6 +39,13 @@ struct CholPlan {
     struct Launch { int kind; int level; int p; int taskOff; int taskCount; int child; };
     std::vector<Launch> launches;        // in execution order
     std::vector<TileTask> tasks;
+    // substitution work split: per level, (front, first row/column) chunks of
+    // the rectangular part L21 (rows k..m) for the multi-CTA GEMV kernels
+    std::vector<int> rectRowOff, rectColOff;   // nLevels + 1
+    std::vector<int2> rectRowTasks, rectColTasks;
+    int2* dRectRowTasks = nullptr;
+    int2* dRectColTasks = nullptr;
+    double* tmpDot = nullptr;                  // nDof: L21^T x_B per pivot
     // assembly map from the block-CSR pattern
     std::vector<long long> asmDest;      // per slot: pool offset of entry (0,0) or -1
     std::vector<int> asmLd;              // per slot: leading dimension (front m)
