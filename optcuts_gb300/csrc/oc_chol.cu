@@ -265,9 +265,12 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
-                const int nt = tiles_of(P.fk[f], P.fm[f]);
-                for (int tj = p + 1; tj < nt; ++tj)
-                    for (int ti = tj; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, tj, p});
+                // trailing region [s, m) x [s, m), s = end of panel p, in
+                // 64 x 64 blocks (lower triangle of blocks)
+                const int s = std::min((p + 1) * kTile, P.fk[f]);
+                const int nb = (P.fm[f] - s + kUpd - 1) / kUpd;
+                for (int bj = 0; bj < nb; ++bj)
+                    for (int bi = bj; bi < nb; ++bi) P.tasks.push_back(TileTask{f, bi, bj, p});
             }
             if ((int)P.tasks.size() > off) P.launches.push_back({3, l, p, off, (int)P.tasks.size() - off, 0});
         }
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(32) k_ldl_trsm(const TileTask* __restrict__ ta
     tile_bounds(k, m, t.i, r0, h);
     double* F = pool + foff[t.front];
     const int r = threadIdx.x;
-#pragma unroll 4
+#pragma unroll
     for (int c = 0; c < kTile; ++c) L[r][c] = (r < w && c < w && c <= r) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
     double x[kTile];
 #pragma unroll
@@ -443,40 +446,64 @@ __global__ void __launch_bounds__(32) k_ldl_trsm(const TileTask* __restrict__ ta
         if (r < h && c < w) F[(r0 + r) + (long long)(s0 + c) * m] = x[c] / L[c][c];
 }
 
-// C(i, j) -= L(i, p) * D_p * L(j, p)^T  (trailing update, FP64)
+// Trailing update C -= L(:, p) * D_p * L(:, p)^T of the region below and right
+// of panel p, in 64 x 64 blocks (task: block row bi, block column bj >= ...,
+// lower triangle only).  256 threads, 4 x 4 accumulators each; the panel
+// columns of both block rows are staged column-major in shared memory so a
+// thread's four rows (or columns) are one 32-byte read.
 __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
                                                     const int* __restrict__ fm, const long long* __restrict__ foff,
                                                     double* __restrict__ pool)
 {
-    __shared__ double Ai[kTile][kTile + 1];
-    __shared__ double Aj[kTile][kTile + 1];
+    __shared__ __align__(16) double Ai[kTile][kUpd];
+    __shared__ __align__(16) double Aj[kTile][kUpd];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
-    int s0, w, r0, h, c0, hc;
+    int s0, w;
     tile_bounds(k, m, t.p, s0, w);
-    tile_bounds(k, m, t.i, r0, h);
-    tile_bounds(k, m, t.j, c0, hc);
-    const double* F = pool + foff[t.front];
-    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-        const int r = e % kTile, c = e / kTile;
-        const double dc = c < w ? F[(s0 + c) + (long long)(s0 + c) * m] : 0.0;
-        Ai[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] * dc : 0.0;
-        Aj[r][c] = (r < hc && c < w) ? F[(c0 + r) + (long long)(s0 + c) * m] : 0.0;
+    const int s = s0 + w;                       // first row/column after the panel
+    const int r0 = s + kUpd * t.i, c0 = s + kUpd * t.j;
+    const int h = min(kUpd, m - r0), hc = min(kUpd, m - c0);
+    double* F = pool + foff[t.front];
+    for (int e = threadIdx.x; e < kTile * kUpd; e += blockDim.x) {
+        const int r = e % kUpd, c = e / kUpd;
+        double ai = 0.0, aj = 0.0;
+        if (c < w) {
+            const double* col = F + (long long)(s0 + c) * m;
+            if (r < h) ai = col[r0 + r] * col[s0 + c];   // L(r, c) * D_c
+            if (r < hc) aj = col[c0 + r];
+        }
+        Ai[c][r] = ai;
+        Aj[c][r] = aj;
     }
     __syncthreads();
-    // each thread: 4 elements of the 32 x 32 tile (rows tr + 8q)
-    const int tc = threadIdx.x % kTile, tr = threadIdx.x / kTile;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 4 x 4 each
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
     for (int c = 0; c < w; ++c) {
-        const double b = Aj[tc][c];
+        const double2 a01 = *reinterpret_cast<const double2*>(&Ai[c][4 * ty]);
+        const double2 a23 = *reinterpret_cast<const double2*>(&Ai[c][4 * ty + 2]);
+        const double2 b01 = *reinterpret_cast<const double2*>(&Aj[c][4 * tx]);
+        const double2 b23 = *reinterpret_cast<const double2*>(&Aj[c][4 * tx + 2]);
+        const double a[4] = {a01.x, a01.y, a23.x, a23.y}, b[4] = {b01.x, b01.y, b23.x, b23.y};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[q] = fma(Ai[tr + 8 * q][c], b, acc[q]);
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
-    double* Fw = pool + foff[t.front];
+    const bool diag = (t.i == t.j);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int r = tr + 8 * q;
-        if (r < h && tc < hc && (t.i != t.j || r >= tc)) Fw[(r0 + r) + (long long)(c0 + tc) * m] -= acc[q];
+    for (int i = 0; i < 4; ++i) {
+        const int r = 4 * ty + i;
+        if (r >= h) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int cc = 4 * tx + j;
+            if (cc < hc && (!diag || r >= cc)) F[(r0 + r) + (long long)(c0 + cc) * m] -= acc[i][j];
+        }
     }
 }
 

@@ -11,6 +11,7 @@
 namespace oc {
 
 constexpr int kTile = 32;      // dense tile edge (FP64) of the front kernels
+constexpr int kUpd = 64;       // edge of the trailing-update blocks (FP64, 4x4 per thread)
 constexpr int kRectRows = 256; // rows of L21 per CTA in the forward GEMV
 constexpr int kRectCols = 8;   // columns of L21 per CTA in the backward GEMV^T
 
