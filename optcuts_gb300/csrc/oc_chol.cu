@@ -247,20 +247,18 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             if (cnt) P.launches.push_back({0, l, 0, off, cnt, c});
         }
         for (int p = 0; p < maxPanels; ++p) {
+            // panel: every CTA factors the diagonal tile (redundantly, it is
+            // small) and solves one tile row below it; the first writes the
+            // factored diagonal tile back (task.j = 1)
             int off = static_cast<int>(P.tasks.size());
-            for (int i = 0; i < nl; ++i) {
-                const int f = lf[i];
-                if ((P.fk[f] + kTile - 1) / kTile > p) P.tasks.push_back(TileTask{f, p, p, p});
-            }
-            if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
-            off = static_cast<int>(P.tasks.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
                 const int nt = tiles_of(P.fk[f], P.fm[f]);
-                for (int ti = p + 1; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, p, p});
+                if (nt == p + 1) P.tasks.push_back(TileTask{f, p, 1, p});
+                for (int ti = p + 1; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, ti == p + 1 ? 1 : 0, p});
             }
-            if ((int)P.tasks.size() > off) P.launches.push_back({2, l, p, off, (int)P.tasks.size() - off, 0});
+            if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
             off = static_cast<int>(P.tasks.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
@@ -369,81 +367,73 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
     }
 }
 
-// LDL^T of the diagonal tile of panel p, in place: unit-lower L below the
-// diagonal, D on the diagonal (the factorisation SimplicialLDLT computes;
-// negative pivots are allowed, a zero or non-finite one is counted and
-// replaced by 1e-300).  One warp per tile: lane r keeps row r in registers,
-// the pivot column is broadcast with shuffles -- no shared memory, no
-// block barriers on this serial step of the factorisation.
-__global__ void __launch_bounds__(32) k_ldl_diag(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                 const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                 double* __restrict__ pool, int* flag)
+// One panel step of the front factorisation, for one tile row below the
+// diagonal tile: LDL^T of the w x w diagonal tile of panel p in shared memory
+// (unit-lower L, D on the diagonal -- the factorisation SimplicialLDLT
+// computes; negative pivots pass, a zero or non-finite one is replaced by
+// 1e-300 and counted), then L(i, p) = A(i, p) L(p, p)^-T D^-1.  Every CTA of
+// the panel factors the (small) diagonal tile itself, so the factorisation
+// and the panel solve are one launch; the CTA flagged in task.j writes the
+// factored diagonal tile back.  A panel without tile rows below gets one
+// diagonal-only task (task.i == task.p).
+__global__ void __launch_bounds__(256) k_ldl_panel(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                   const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                   double* __restrict__ pool, int* flag)
 {
+    __shared__ double A[kTile][kTile + 1];
+    __shared__ double X[kTile][kTile + 1];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
-    int s0, w;
+    int s0, w, r0 = 0, h = 0;
     tile_bounds(k, m, t.p, s0, w);
+    const bool hasRow = t.i > t.p;
+    if (hasRow) tile_bounds(k, m, t.i, r0, h);
     double* F = pool + foff[t.front];
-    const int r = threadIdx.x;
-    double a[kTile];
-#pragma unroll
-    for (int c = 0; c < kTile; ++c) a[c] = (r < w && c < w && c <= r) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
-#pragma unroll
-    for (int c = 0; c < kTile; ++c) {
-        if (c < w) {
-            double d = __shfl_sync(0xffffffffu, a[c], c);
-            if (!(d != 0.0) || !isfinite(d)) {
-                if (r == 0) atomicAdd(flag, 1);
-                d = 1e-300;
-                if (r == c) a[c] = d;
-            }
-            const double tr = a[c];   // A[r][c] before scaling (row r > c)
-            const double l = tr / d;
-#pragma unroll
-            for (int c2 = c + 1; c2 < kTile; ++c2) {
-                const double tc2 = __shfl_sync(0xffffffffu, tr, c2);
-                if (c2 < w && r >= c2) a[c2] = fma(-l, tc2, a[c2]);
-            }
-            if (r > c) a[c] = l;
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int r = e % kTile, c = e / kTile;
+        A[r][c] = (r < w && c < w && r >= c) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
+        X[r][c] = (hasRow && r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
+    }
+    __syncthreads();
+    for (int c = 0; c < w; ++c) {
+        double d = A[c][c];
+        const bool bad = !(d != 0.0) || !isfinite(d);
+        if (bad) d = 1e-300;
+        const double id = 1.0 / d;
+        const int n = w - c - 1;
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            const int rr = c + 1 + e % n, c2 = c + 1 + e / n;
+            if (rr >= c2) A[rr][c2] -= A[rr][c] * id * A[c2][c];
+        }
+        __syncthreads();
+        // scale column c (the next step reads only columns > c)
+        for (int rr = c + 1 + threadIdx.x; rr < w; rr += blockDim.x) A[rr][c] *= id;
+        if (threadIdx.x == 0 && bad) {
+            A[c][c] = d;
+            if (t.j) atomicAdd(flag, 1);
         }
     }
-#pragma unroll
-    for (int c = 0; c < kTile; ++c)
-        if (r < w && c <= r && c < w) F[(s0 + r) + (long long)(s0 + c) * m] = a[c];
-}
-
-// L(i, p) = A(i, p) * L(p, p)^-T * D_p^-1 for a tile row below the diagonal
-// tile.  One warp per tile row: lane r solves row r in registers against the
-// diagonal tile, read from shared memory by broadcast.
-__global__ void __launch_bounds__(32) k_ldl_trsm(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                 const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                 double* __restrict__ pool)
-{
-    __shared__ double L[kTile][kTile + 1];
-    const TileTask t = tasks[blockIdx.x];
-    const int k = fk[t.front], m = fm[t.front];
-    int s0, w, r0, h;
-    tile_bounds(k, m, t.p, s0, w);
-    tile_bounds(k, m, t.i, r0, h);
-    double* F = pool + foff[t.front];
-    const int r = threadIdx.x;
-#pragma unroll
-    for (int c = 0; c < kTile; ++c) L[r][c] = (r < w && c < w && c <= r) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
-    double x[kTile];
-#pragma unroll
-    for (int c = 0; c < kTile; ++c) x[c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
-    __syncwarp();
-#pragma unroll
-    for (int c = 0; c < kTile; ++c) {
-        if (c < w) {
-#pragma unroll
-            for (int c2 = c + 1; c2 < kTile; ++c2)
-                if (c2 < w) x[c2] = fma(-x[c], L[c2][c], x[c2]);
+    __syncthreads();
+    if (hasRow) {
+        for (int c = 0; c + 1 < w; ++c) {
+            const int n = w - c - 1;
+            for (int e = threadIdx.x; e < h * n; e += blockDim.x) {
+                const int r = e % h, c2 = c + 1 + e / h;
+                X[r][c2] -= X[r][c] * A[c2][c];
+            }
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < h * w; e += blockDim.x) {
+            const int r = e % h, c = e / h;
+            F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c] / A[c][c];
         }
     }
-#pragma unroll
-    for (int c = 0; c < kTile; ++c)
-        if (r < h && c < w) F[(r0 + r) + (long long)(s0 + c) * m] = x[c] / L[c][c];
+    if (t.j) {
+        for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+            const int r = e % w, c = e / w;
+            if (r >= c) F[(s0 + r) + (long long)(s0 + c) * m] = A[r][c];
+        }
+    }
 }
 
 // Trailing update C -= L(:, p) * D_p * L(:, p)^T of the region below and right
@@ -736,8 +726,7 @@ int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string
         const TileTask* t = P.dTasks + L.taskOff;
         switch (L.kind) {
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
-        case 1: k_ldl_diag<<<L.taskCount, 32, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        case 2: k_ldl_trsm<<<L.taskCount, 32, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        case 1: k_ldl_panel<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
         default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         }
     }
