@@ -696,6 +696,11 @@ int chol_upload(CholPlan& P, std::string* err)
 
 void chol_free(CholPlan& P)
 {
+    if (P.factGraph) cudaGraphExecDestroy(P.factGraph);
+    if (P.solveGraph) cudaGraphExecDestroy(P.solveGraph);
+    P.factGraph = P.solveGraph = nullptr;
+    P.factKey = nullptr;
+    P.solveKey[0] = P.solveKey[1] = nullptr;
     cudaFree(P.pool); cudaFree(P.upd); cudaFree(P.yperm); cudaFree(P.xperm);
     cudaFree(P.dPermDof); cudaFree(P.dFk); cudaFree(P.dFm); cudaFree(P.dFdofStart); cudaFree(P.dFrowOff);
     cudaFree(P.dFoff); cudaFree(P.dFupd); cudaFree(P.dRowIdx); cudaFree(P.dChildOff); cudaFree(P.dChildList);
@@ -716,9 +721,8 @@ void chol_free(CholPlan& P)
     P.onDevice = false;
 }
 
-int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBad)
+static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)
 {
-    if (!P.onDevice) return OC_ERR_INVALID;
     cudaMemsetAsync(P.pool, 0, sizeof(double) * (size_t)P.poolSize, st);
     cudaMemsetAsync(P.dFlag, 0, sizeof(int), st);
     k_asm_fronts<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b.val, P.dAsmDest, P.dAsmLd, P.dAsmDiag, b.nnzb, P.pool);
@@ -730,6 +734,29 @@ int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string
         default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         }
     }
+}
+
+// The launch sequence is fixed per topology, so it is captured once into a
+// CUDA graph (keyed by the block-CSR value array it reads) and replayed.
+int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBad)
+{
+    if (!P.onDevice) return OC_ERR_INVALID;
+    if (P.useGraphs && (!P.factGraph || P.factKey != b.val)) {
+        if (P.factGraph) cudaGraphExecDestroy(P.factGraph);
+        P.factGraph = nullptr;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            enqueue_factorize(P, b, st);
+            if (cudaStreamEndCapture(st, &g) == cudaSuccess && g) {
+                if (cudaGraphInstantiate(&P.factGraph, g, 0) != cudaSuccess) P.factGraph = nullptr;
+                cudaGraphDestroy(g);
+            }
+        }
+        cudaGetLastError();   // a failed capture falls back to direct launches
+        P.factKey = b.val;
+    }
+    if (P.factGraph) cudaGraphLaunch(P.factGraph, st);
+    else enqueue_factorize(P, b, st);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         if (err) *err = std::string("chol factorize: ") + cudaGetErrorString(e);
@@ -746,19 +773,11 @@ int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string
     return OC_OK;
 }
 
-int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, std::string* err)
+static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, size_t shm,
+                          size_t shmK)
 {
-    if (!P.onDevice) return OC_ERR_INVALID;
     const int n = P.nDof;
     k_permute_in<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(rhs), P.dPermDof, sign, n, P.yperm);
-    int maxK = 0;
-    for (int f = 0; f < P.nFronts; ++f) maxK = std::max(maxK, P.fk[f]);
-    const size_t shm = sizeof(double) * (size_t)P.maxM, shmK = sizeof(double) * (size_t)std::max(maxK, 1);
-    if (shm > 48 * 1024) {
-        cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        cudaFuncSetAttribute(k_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-    }
-    if (shmK > 48 * 1024) cudaFuncSetAttribute(k_fwd_rect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmK);
     for (int l = 0; l < P.nLevels; ++l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
         k_fwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart, P.dChildOff,
@@ -778,6 +797,39 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
                                      P.tmpDot, P.xperm);
     }
     k_permute_out<<<(n + 255) / 256, 256, 0, st>>>(P.xperm, P.dPermDof, n, reinterpret_cast<double*>(x));
+}
+
+// Forward/backward substitution; captured into a CUDA graph per
+// (rhs, x, sign) and replayed.
+int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, std::string* err)
+{
+    if (!P.onDevice) return OC_ERR_INVALID;
+    int maxK = 0;
+    for (int f = 0; f < P.nFronts; ++f) maxK = std::max(maxK, P.fk[f]);
+    const size_t shm = sizeof(double) * (size_t)P.maxM, shmK = sizeof(double) * (size_t)std::max(maxK, 1);
+    if (shm > 48 * 1024) {
+        cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    }
+    if (shmK > 48 * 1024) cudaFuncSetAttribute(k_fwd_rect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmK);
+    if (P.useGraphs && (!P.solveGraph || P.solveKey[0] != rhs || P.solveKey[1] != x || P.solveSign != sign)) {
+        if (P.solveGraph) cudaGraphExecDestroy(P.solveGraph);
+        P.solveGraph = nullptr;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            enqueue_solve(P, rhs, x, sign, st, shm, shmK);
+            if (cudaStreamEndCapture(st, &g) == cudaSuccess && g) {
+                if (cudaGraphInstantiate(&P.solveGraph, g, 0) != cudaSuccess) P.solveGraph = nullptr;
+                cudaGraphDestroy(g);
+            }
+        }
+        cudaGetLastError();
+        P.solveKey[0] = rhs;
+        P.solveKey[1] = x;
+        P.solveSign = sign;
+    }
+    if (P.solveGraph) cudaGraphLaunch(P.solveGraph, st);
+    else enqueue_solve(P, rhs, x, sign, st, shm, shmK);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         if (err) *err = std::string("chol solve: ") + cudaGetErrorString(e);

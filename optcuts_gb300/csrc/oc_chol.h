@@ -67,6 +67,12 @@ struct CholPlan {
     unsigned char* dAsmDiag = nullptr;
     int* dFlag = nullptr;        // non-positive pivot count
     bool onDevice = false;
+    // captured launch sequences (fixed per topology)
+    bool useGraphs = true;
+    cudaGraphExec_t factGraph = nullptr, solveGraph = nullptr;
+    const void* factKey = nullptr;
+    const void* solveKey[2] = {nullptr, nullptr};
+    double solveSign = 0.0;
 };
 
 // Symbolic analysis from a full-symmetric vertex block pattern (rowPtr/col
