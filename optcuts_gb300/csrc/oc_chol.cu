@@ -473,7 +473,10 @@ __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-    for (int c = 0; c < w; ++c) {
+    // threads whose 4 x 4 patch lies outside the block's rows/columns, or
+    // wholly above the diagonal of a diagonal block, have nothing to update
+    const bool idle = (4 * ty >= h) || (4 * tx >= hc) || (t.i == t.j && 4 * ty + 3 < 4 * tx);
+    for (int c = 0; c < (idle ? 0 : w); ++c) {
         const double2 a01 = *reinterpret_cast<const double2*>(&Ai[c][4 * ty]);
         const double2 a23 = *reinterpret_cast<const double2*>(&Ai[c][4 * ty + 2]);
         const double2 b01 = *reinterpret_cast<const double2*>(&Aj[c][4 * tx]);
