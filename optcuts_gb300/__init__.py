@@ -330,6 +330,16 @@ class LinSysSolver:
             pass
 
 
+def energy_w(last_energy, seam_length, virtual_radius, lam):
+    """E_w = (1 - lambda) E_SD + lambda E_se, with E_se = seam length /
+    virtualRadius -- the value Optimizer::writeEnergyValToFile records per
+    iteration in fracture mode (Optimizer.cpp:706-716).  `last_energy` is
+    Optimizer.getLastEnergyVal() = (1 - lambda) E_SD; the seam length comes
+    from optcuts_gb300.init.seam_sparsity and is constant during a Newton
+    phase (it changes only with the topology)."""
+    return last_energy + lam * seam_length / virtual_radius
+
+
 def symbolic_stats_dict(out):
     keys = ["fronts", "levels", "max_front_rows", "pool_doubles", "flops", "launches", "factor_entries", "dof"]
     return dict(zip(keys, [float(x) for x in out]))

@@ -25,13 +25,61 @@ import numpy as np
 
 
 class InitState:
-    def __init__(self, V_rest, UV, F, fixed, cut_path, bnd):
+    def __init__(self, V_rest, UV, F, fixed, cut_path, bnd, cohE):
         self.V_rest = V_rest
         self.UV = UV
         self.F = F
         self.fixedVert = fixed
         self.cut_path = cut_path
         self.bnd = bnd
+        self.cohE = cohE
+
+
+def cohesive_edges(F_mesh, F_uv):
+    """Cohesive-edge pairs of a cut mesh (TriMesh.cpp:128-166): for every
+    UV-boundary half-edge (a, b) of F_uv whose surface half-edge is interior,
+    the row (a, b, c, d) with (c, d) the opposite side's UV vertices; each
+    surface edge is recorded once, in triangle / edge order."""
+    F_mesh = np.asarray(F_mesh)
+    F_uv = np.asarray(F_uv)
+    he_uv = set()
+    he = {}
+    for t in range(len(F_uv)):
+        for e in range(3):
+            he_uv.add((int(F_uv[t, e]), int(F_uv[t, (e + 1) % 3])))
+            he[(int(F_mesh[t, e]), int(F_mesh[t, (e + 1) % 3]))] = (t, e)
+    rows = []
+    for t in range(len(F_uv)):
+        for e in range(3):
+            a, b = int(F_uv[t, e]), int(F_uv[t, (e + 1) % 3])
+            if (b, a) in he_uv:
+                continue
+            key = (int(F_mesh[t, (e + 1) % 3]), int(F_mesh[t, e]))
+            if key in he:
+                t2, e2 = he[key]
+                rows.append([a, b, int(F_uv[t2, (e2 + 1) % 3]), int(F_uv[t2, e2])])
+                he.pop((int(F_mesh[t, e]), int(F_mesh[t, (e + 1) % 3])), None)
+    return np.asarray(rows, np.int32).reshape(-1, 4)
+
+
+def seam_sparsity(V_rest, UV, cohE, avg_edge_len, init_seam_len=0.0, tri_soup=False):
+    """TriMesh::computeSeamSparsity (TriMesh.cpp:1542-1558): total rest length
+    of the interior cohesive edges (in tri-soup mode only those whose UV
+    copies separated by more than 1% of the average edge length), plus the
+    initial seam length.  Divide by virtualRadius for E_se."""
+    V_rest = np.asarray(V_rest)
+    cohE = np.asarray(cohE).reshape(-1, 4)
+    s = 0.0
+    for row in cohE:
+        if row.min() < 0:
+            continue
+        if tri_soup:
+            UVa = np.asarray(UV)
+            if not (np.linalg.norm(UVa[row[0]] - UVa[row[2]]) / avg_edge_len > 1e-2 or
+                    np.linalg.norm(UVa[row[1]] - UVa[row[3]]) / avg_edge_len > 1e-2):
+                continue
+        s += float(np.linalg.norm(V_rest[row[0]] - V_rest[row[1]]))
+    return s + init_seam_len
 
 
 def euler_characteristic(V, F):
@@ -136,7 +184,8 @@ def harmonic(F, n, bnd, bnd_uv):
 def init_uv(V, F):
     """Cut (if closed genus 0) and Tutte-embed; returns an InitState."""
     V = np.asarray(V, np.float64)
-    F = np.asarray(F, np.int32)
+    F_mesh = np.asarray(F, np.int32)
+    F = F_mesh
     ec = euler_characteristic(V, F)
     path = None
     if ec == 2:
@@ -148,4 +197,7 @@ def init_uv(V, F):
         raise ValueError("mesh has no boundary after the cut")
     bnd = np.asarray(bnd, np.int64)
     UV = harmonic(F, len(V), bnd, map_vertices_to_circle(V, bnd))
-    return InitState(V, UV, F, np.array([0], np.int32), path, bnd)
+    # a cut mesh is built from (F_mesh, F_uv) with cohesive edges along the
+    # cut (TriMesh.cpp:122-189); an uncut disk has none (TriMesh.cpp:116-120)
+    cohE = cohesive_edges(F_mesh, F) if path is not None else np.zeros((0, 4), np.int32)
+    return InitState(V, UV, F, np.array([0], np.int32), path, bnd, cohE)

@@ -5,7 +5,7 @@ oracle/ref/Makefile -- on seeded synthetic meshes (optcuts_gb300.meshes) and
 packs its dumps into one compressed .npz per case:
 
     V_rest, UV0, F, fixedVert, bnd     initial state after the reference's
-                                       own cut + Tutte initialisation
+    cohE                               own cut + Tutte initialisation
     rest, scalars                      TriMesh::computeFeatures constants
     E_elem0, grad0                     per-triangle energy, gradient at UV0
     H0_blocks, H0_tris                 per-triangle PSD-projected Hessians
@@ -77,7 +77,7 @@ def run_case(name, key, lam, iters, hmax, states):
         Fm, fixed = ld("F"), ld("fixedVert")
         nt = len(Fm) if hmax is None else min(hmax, len(Fm))
         blocks = per_tri_blocks(Fm, fixed, ld("H0_V"), nt)
-        pack = dict(V_rest=ld("V_rest"), UV0=ld("UV0"), F=Fm, fixedVert=fixed, bnd=ld("bnd"),
+        pack = dict(V_rest=ld("V_rest"), UV0=ld("UV0"), F=Fm, fixedVert=fixed, bnd=ld("bnd"), cohE=ld("cohE"),
                     rest=ld("rest"), scalars=ld("scalars"), E_elem0=ld("E_elem0"), grad0=ld("grad0"),
                     H0_blocks=blocks, dir0=ld("dir0"), trace_E=ld("trace_E"), trace_gsq=ld("trace_gsq"),
                     trace_alpha=ld("trace_alpha"), trace_status=ld("trace_status"),

@@ -117,3 +117,16 @@ def test_phase_timing_and_launch_count(golden):
     assert set(ph) == set(oc.Optimizer.PHASES) and all(v >= 0.0 for v in ph.values())
     assert ph["factorize"] > 0.0 and ph["solve"] > 0.0
     assert opt.launch_count() > 10
+
+
+def test_energy_w_trace_matches_reference(golden):
+    """E_w = (1-lambda) E_SD + lambda E_se per iteration (Optimizer.cpp:706-716)."""
+    from optcuts_gb300 import init as I
+    g = golden("icosphere_320")
+    lam = g["scalars"][4]
+    seam = I.seam_sparsity(g["V_rest"], g["UV0"], g["cohE"], g["scalars"][1])
+    m, opt, E, steps, status = run(g)
+    Ew = [oc.energy_w(e, seam, g["scalars"][2], lam) for e in E]
+    Ew_ref = g["trace_E"][-1] + lam * g["scalars"][3] / g["scalars"][2]
+    assert abs(Ew[-1] - Ew_ref) / Ew_ref < 1e-4
+    assert np.all(np.diff(Ew) <= 0.0)

@@ -56,3 +56,13 @@ def test_obj_roundtrip(tmp_path):
     (tmp_path / "t.obj").write_text("v 0 0 0\n")
     with pytest.raises(ValueError):
         M.read_obj(str(tmp_path / "t.obj"))
+
+
+@pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle"])
+def test_cohesive_edges_and_seam_term_match_reference(golden, case):
+    g = golden(case)
+    st = I.init_uv(g["mesh_V"], g["mesh_F"])
+    np.testing.assert_array_equal(st.cohE.reshape(-1, 4), g["cohE"].reshape(-1, 4))
+    # E_se before division by virtualRadius (TriMesh::computeSeamSparsity)
+    avg = g["scalars"][1]
+    assert I.seam_sparsity(st.V_rest, st.UV, st.cohE, avg) == pytest.approx(g["scalars"][3], rel=1e-15, abs=0)
