@@ -152,9 +152,12 @@ int oc_linsys_solve(oc_linsys* ls, const double* rhs, double* result, double tol
 /* multiply(x, Ax) (LinSysSolver.hpp:172-187) */
 int oc_linsys_multiply(oc_linsys* ls, const double* x, double* Ax);
 
-/* ---- Optimizer (Optimizer.hpp:74-142), scaffold off ---------------------
+/* ---- Optimizer (Optimizer.hpp:74-142) -----------------------------------
  * energyParam = energyParams[0] = 1 - lambda.  The mesh is borrowed (its UV
- * is the optimizer's `result.V`). */
+ * is the optimizer's `result.V`).  With a scaffold set (see
+ * oc_optimizer_set_scaffold) the optimizer runs the reference's
+ * scaffolding branches; w_scaf = 0.01 * energyParam at creation
+ * (Optimizer.cpp:87). */
 typedef struct {
     double pcgTol;        /* relative residual, default 1e-8 */
     int pcgMaxIter;       /* default 20000 */
@@ -196,6 +199,37 @@ int oc_optimizer_phase_ms(oc_optimizer* opt, double* out7);
 int oc_optimizer_launch_count(oc_optimizer* opt, long long* launches);
 /* oc_linsys_stats of the optimizer's own solver (after precompute). */
 int oc_optimizer_solver_stats(oc_optimizer* opt, double* out8);
+
+/* ---- Scaffold (Scaffold.hpp:18-70; Optimizer.cpp scaffolding branches) ---
+ * Replaces `scaffold = Scaffold(result, UV_bnds, E, bnd)` (Optimizer.cpp:
+ * 157-161, 251-257): the caller passes the air mesh Scaffold's constructor
+ * builds (Scaffold.cpp:27-205), i.e. airMesh.V (nAirV x 2, row-major), airMesh.F
+ * (nAirF x 3) and bnd (air vertex i < nBnd is mesh vertex bnd[i]; rows
+ * 0..nBnd-1 of airV are those vertices' current UV, as Triangle returns its
+ * input points first).  Air-only vertex i >= nBnd becomes system vertex
+ * nV + i - nBnd (localVI2Global).  areaThres < 0 selects the whole-mesh
+ * areaThres_AM = sqrt(3)/4 (avgEdgeLen/2)^2 (Scaffold.cpp:34, 189).  The
+ * mesh's fixed vertices on the boundary are fixed in the air mesh too.
+ * The next solve() then includes w_scaf/|F_air| * E_SD(air mesh, uniform
+ * weights) in energy, gradient, Hessian, injective step and line search.
+ * The reference rebuilds the scaffold after every iteration; a caller that
+ * does not call this again keeps the air mesh as the last step moved it.
+ * The Newton-matrix pattern and its analysis are rebuilt on the next solve
+ * when the air connectivity differs from the previous call's. */
+int oc_optimizer_set_scaffold(oc_optimizer* opt, const double* airV, int nAirV, const int* airF, int nAirF,
+                              const int* bnd, int nBnd, double areaThres);
+/* Optimizer::setScaffolding(false) (Optimizer.cpp:307-317) */
+int oc_optimizer_clear_scaffold(oc_optimizer* opt);
+/* current air-mesh UV (nAirV x 2): Scaffold::airMesh.V after the last step */
+int oc_optimizer_get_scaffold_uv(oc_optimizer* opt, double* airV);
+/* energyVal_scaffold of the last evaluation; getLastEnergyVal(true) is
+ * oc_optimizer_get_last_energy minus this (Optimizer.cpp:845-850) */
+int oc_optimizer_get_last_energy_scaffold(oc_optimizer* opt, double* scaffoldEnergy);
+/* vertices of the Newton system (wholeMeshSize with a scaffold, else nV) */
+int oc_optimizer_system_size(oc_optimizer* opt, int* nVerts);
+/* gradient and searchDir of the last iteration (2 x system size each,
+ * interleaved u, v; either may be NULL) */
+int oc_optimizer_last_vectors(oc_optimizer* opt, double* gradient, double* searchDir);
 
 #ifdef __cplusplus
 }

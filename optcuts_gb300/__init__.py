@@ -91,6 +91,12 @@ _SIGS = {
     "oc_optimizer_phase_ms": [_vp, _d],
     "oc_optimizer_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_solver_stats": [_vp, _d],
+    "oc_optimizer_set_scaffold": [_vp, _d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double],
+    "oc_optimizer_clear_scaffold": [_vp],
+    "oc_optimizer_get_scaffold_uv": [_vp, _d],
+    "oc_optimizer_get_last_energy_scaffold": [_vp, _d],
+    "oc_optimizer_system_size": [_vp, _i],
+    "oc_optimizer_last_vectors": [_vp, _d, _d],
     "oc_sd_energy_trials_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
                                     _vp, _vp],
 }
@@ -364,9 +370,25 @@ def default_config(**kw):
     return c
 
 
+class Scaffold:
+    """Air mesh of the bijectivity scaffold as Scaffold's constructor leaves it
+    (Scaffold.hpp:18-24): airMesh.V (nAirV x 2), airMesh.F (nAirF x 3) and bnd
+    (air vertex i < len(bnd) is mesh vertex bnd[i])."""
+
+    def __init__(self, airV, airF, bnd):
+        self.airV = np.ascontiguousarray(airV, np.float64).reshape(-1, 2)
+        self.airF = np.ascontiguousarray(airF, np.int32).reshape(-1, 3)
+        self.bnd = np.ascontiguousarray(bnd, np.int32).ravel()
+
+    def localVI2Global(self, nV):
+        nb = len(self.bnd)
+        return np.concatenate([self.bnd, nV + np.arange(len(self.airV) - nb, dtype=np.int32)])
+
+
 class Optimizer:
     """Projected Newton with the injective line search (Optimizer.hpp:74-142),
-    scaffold off.  energyParams = [1 - lambda] as in main.cpp:1569."""
+    with or without a scaffold.  energyParams = [1 - lambda] as in
+    main.cpp:1569."""
 
     def __init__(self, data0, energyParams, config=None, **kw):
         self.data = data0
@@ -390,7 +412,41 @@ class Optimizer:
     def getLastEnergyVal(self, excludeScaffold=False):
         e = ctypes.c_double()
         self.ctx.check(lib().oc_optimizer_get_last_energy(self.h, ctypes.byref(e)), "getLastEnergyVal")
+        if excludeScaffold:
+            es = ctypes.c_double()
+            self.ctx.check(lib().oc_optimizer_get_last_energy_scaffold(self.h, ctypes.byref(es)), "getLastEnergyVal")
+            return e.value - es.value
         return e.value
+
+    def setScaffold(self, scaffold, areaThres=-1.0):
+        """Installs the air mesh for the next solve() (the reference rebuilds it
+        after every iteration, Optimizer.cpp:251-257)."""
+        self.scaffold = scaffold
+        self.ctx.check(lib().oc_optimizer_set_scaffold(
+            self.h, _pd(scaffold.airV), len(scaffold.airV), _pi(scaffold.airF), len(scaffold.airF),
+            _pi(scaffold.bnd), len(scaffold.bnd), float(areaThres)), "setScaffold")
+
+    def clearScaffold(self):
+        self.scaffold = None
+        self.ctx.check(lib().oc_optimizer_clear_scaffold(self.h), "clearScaffold")
+
+    def scaffoldV(self):
+        """Current air-mesh UV (Scaffold::airMesh.V after the last step)."""
+        out = np.zeros_like(self.scaffold.airV)
+        self.ctx.check(lib().oc_optimizer_get_scaffold_uv(self.h, _pd(out)), "scaffoldV")
+        return out
+
+    def systemSize(self):
+        n = ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_system_size(self.h, ctypes.byref(n)), "systemSize")
+        return n.value
+
+    def lastVectors(self):
+        """(gradient, searchDir) of the last iteration, interleaved u, v."""
+        n = self.systemSize()
+        g, d = np.zeros(2 * n), np.zeros(2 * n)
+        self.ctx.check(lib().oc_optimizer_last_vectors(self.h, _pd(g), _pd(d)), "lastVectors")
+        return g, d
 
     def getIterNum(self):
         n = ctypes.c_int()

@@ -66,6 +66,17 @@ struct oc_optimizer {
     int badPivots = 0;
     cudaEvent_t ev[9] = {};
     double phaseMs[7] = {0, 0, 0, 0, 0, 0, 0};
+    // scaffold (the Optimizer's scaffolding branches): an air mesh over the
+    // augmented vertex numbering [mesh vertices | air-only vertices]
+    // (Scaffold::localVI2Global, Scaffold.cpp:179-184)
+    bool scaf = false, patternStale = true;
+    oc::DeviceMesh air;
+    int nWhole = 0, capWhole = 0, capAirF = 0, nAirV = 0, nBnd = 0;
+    double wScaf = 0.0, airScale = 0.0, eScaf = 0.0;
+    double2* wuv = nullptr;         // augmented UV (capWhole)
+    double2* airCorner = nullptr;   // 3 x capAirF
+    double* airHb = nullptr;        // 21 x capAirF
+    std::vector<int> airFw, bnd;    // air triangles in augmented ids; boundary map
 };
 
 namespace {
@@ -121,6 +132,113 @@ int read_min(oc_mesh* m, double* out)
     std::memcpy(&bits, m->scratch.hostResult, sizeof(bits));
     std::memcpy(out, &bits, sizeof(bits));
     return OC_OK;
+}
+
+// TriMesh::computeFeatures rest constants (TriMesh.cpp:355-393), 8 per
+// triangle: triArea, triAreaSq, e0SqLen, e1SqLen, e0dote1 and the three
+// *_div_dbAreaSq values; triangles below areaThres take the degenerate-air
+// clamp (:373-383).  Returns false on a zero-area triangle (:368-372).
+bool rest_constants(const double* V_rest, const int* F, int nF, double areaThres, std::vector<double>& rest,
+                    double& surfaceArea)
+{
+    rest.resize(8 * (size_t)nF);
+    surfaceArea = 0.0;
+    bool invalid = false;
+    for (int t = 0; t < nF; ++t) {
+        const double* P1 = V_rest + 3 * (size_t)F[3 * t];
+        const double* P2 = V_rest + 3 * (size_t)F[3 * t + 1];
+        const double* P3 = V_rest + 3 * (size_t)F[3 * t + 2];
+        const double a[3] = {P2[0] - P1[0], P2[1] - P1[1], P2[2] - P1[2]};
+        const double b[3] = {P3[0] - P1[0], P3[1] - P1[1], P3[2] - P1[2]};
+        const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+        double* r = &rest[8 * (size_t)t];
+        r[0] = 0.5 * std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (r[0] == 0.0) invalid = true;
+        if (r[0] < areaThres) {
+            r[0] = areaThres;
+            surfaceArea += areaThres;
+            r[1] = areaThres * areaThres;
+            r[2] = r[3] = 4.0 / std::sqrt(3.0) * areaThres;
+            r[4] = r[2] / 2.0;
+            r[5] = r[6] = 2.0 / std::sqrt(3.0) / areaThres;
+            r[7] = r[5] / 2.0;
+        }
+        else {
+            surfaceArea += r[0];
+            r[1] = r[0] * r[0];
+            r[2] = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+            r[3] = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+            r[4] = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+            r[5] = r[2] / 2. / r[1];
+            r[6] = r[3] / 2. / r[1];
+            r[7] = r[4] / 2. / r[1];
+        }
+    }
+    return !invalid;
+}
+
+void device_mesh_free(oc::DeviceMesh& d)
+{
+    cudaFree(d.F0); cudaFree(d.F1); cudaFree(d.F2);
+    cudaFree(d.A2); cudaFree(d.w); cudaFree(d.e0); cudaFree(d.e1); cudaFree(d.e01);
+    cudaFree(d.e0d); cudaFree(d.e1d); cudaFree(d.e01d);
+    cudaFree(d.vcPtr); cudaFree(d.vcIdx); cudaFree(d.fixedMask);
+    double2* uv = d.uv;
+    d = oc::DeviceMesh{};
+    d.uv = uv;   // owned by the caller
+}
+
+// Uploads a triangle set in the device layout (SoA indices and rest
+// constants, vertex -> corner lists in triangle order, fixed mask); d.uv is
+// left to the caller.  Frees what d held before.
+int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int nF, const std::vector<double>& rest,
+                       double surfaceArea, const std::vector<unsigned char>& mask)
+{
+    device_mesh_free(d);
+    d.nV = nV;
+    d.nF = nF;
+    std::vector<int> f0(nF), f1(nF), f2(nF);
+    std::vector<double> col[8];
+    for (auto& c : col) c.resize(nF);
+    for (int t = 0; t < nF; ++t) {
+        f0[t] = F[3 * t]; f1[t] = F[3 * t + 1]; f2[t] = F[3 * t + 2];
+        const double* r = &rest[8 * (size_t)t];
+        col[0][t] = r[1];                    // triAreaSq
+        col[1][t] = r[0] / surfaceArea;      // w (SymDirichletEnergy.cpp:41)
+        col[2][t] = r[2]; col[3][t] = r[3]; col[4][t] = r[4];
+        col[5][t] = r[5]; col[6][t] = r[6]; col[7][t] = r[7];
+    }
+    // vertex -> corners, sorted by triangle id
+    std::vector<int> vcPtr(nV + 1, 0), vcIdx(3 * (size_t)nF);
+    for (int t = 0; t < nF; ++t)
+        for (int k = 0; k < 3; ++k) vcPtr[F[3 * t + k] + 1]++;
+    for (int v = 0; v < nV; ++v) vcPtr[v + 1] += vcPtr[v];
+    {
+        std::vector<int> fill(vcPtr.begin(), vcPtr.end() - 1);
+        for (int t = 0; t < nF; ++t)
+            for (int k = 0; k < 3; ++k) vcIdx[fill[F[3 * t + k]]++] = k * nF + t;
+    }
+    cudaStream_t st = ctx->stream;
+    int rc = OC_OK;
+    auto chk = [&](cudaError_t e, const char* what) {
+        if (rc == OC_OK && e != cudaSuccess) rc = fail(ctx, OC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    };
+    chk(dalloc(&d.F0, nF), "alloc"); chk(dalloc(&d.F1, nF), "alloc"); chk(dalloc(&d.F2, nF), "alloc");
+    double** dcols[8] = {&d.A2, &d.w, &d.e0, &d.e1, &d.e01, &d.e0d, &d.e1d, &d.e01d};
+    for (int k = 0; k < 8; ++k) chk(dalloc(dcols[k], nF), "alloc");
+    chk(dalloc(&d.vcPtr, nV + 1), "alloc");
+    chk(dalloc(&d.vcIdx, 3 * (size_t)nF), "alloc");
+    chk(dalloc(&d.fixedMask, nV), "alloc");
+    if (rc == OC_OK) {
+        chk(upload(d.F0, f0.data(), nF, st), "upload"); chk(upload(d.F1, f1.data(), nF, st), "upload");
+        chk(upload(d.F2, f2.data(), nF, st), "upload");
+        for (int k = 0; k < 8; ++k) chk(upload(*dcols[k], col[k].data(), nF, st), "upload");
+        chk(upload(d.vcPtr, vcPtr.data(), nV + 1, st), "upload");
+        chk(upload(d.vcIdx, vcIdx.data(), 3 * (size_t)nF, st), "upload");
+        chk(upload(d.fixedMask, mask.data(), nV, st), "upload");
+        chk(cudaStreamSynchronize(st), "sync");   // host staging vectors go out of scope
+    }
+    return rc;
 }
 
 // Full-symmetric 2x2-block pattern from the triangles (the vertex adjacency
@@ -238,12 +356,12 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
 
 // numeric factorisation (direct) or preconditioner (PCG); fixedDiag > 0 sets
 // the fixed rows' diagonal blocks to fixedDiag * I first
-int linsys_factor(oc_linsys* ls, double fixedDiag, int* nBad)
+int linsys_factor(oc_linsys* ls, double fixedDiag, int* nBad, double fixedDiag2 = 0.0)
 {
     oc_ctx* ctx = ls->ctx;
     cudaStream_t st = ctx->stream;
     OC_CUDA(ctx, cudaMemsetAsync(ls->dFlag, 0, sizeof(int), st));
-    if (fixedDiag > 0.0) oc::launch_precond_fixed(ls->b, fixedDiag, st, ls->dFlag);
+    if (fixedDiag > 0.0) oc::launch_precond_fixed(ls->b, fixedDiag, st, ls->dFlag, fixedDiag2);
     else oc::launch_precond(ls->b, st, ls->dFlag);
     int bad = 0;
     if (ls->kind == OC_SOLVER_DIRECT) {
@@ -348,38 +466,7 @@ int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV, 
     m->rest.resize(8 * (size_t)nF);
     // TriMesh::computeFeatures rest constants (TriMesh.cpp:343-404)
     double surfaceArea = 0.0;
-    bool invalid = false;
-    for (int t = 0; t < nF; ++t) {
-        const double* P1 = V_rest + 3 * (size_t)F[3 * t];
-        const double* P2 = V_rest + 3 * (size_t)F[3 * t + 1];
-        const double* P3 = V_rest + 3 * (size_t)F[3 * t + 2];
-        const double a[3] = {P2[0] - P1[0], P2[1] - P1[1], P2[2] - P1[2]};
-        const double b[3] = {P3[0] - P1[0], P3[1] - P1[1], P3[2] - P1[2]};
-        const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-        double* r = &m->rest[8 * (size_t)t];
-        r[0] = 0.5 * std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-        if (r[0] == 0.0) invalid = true;
-        if (r[0] < areaThres) {
-            r[0] = areaThres;
-            surfaceArea += areaThres;
-            r[1] = areaThres * areaThres;
-            r[2] = r[3] = 4.0 / std::sqrt(3.0) * areaThres;
-            r[4] = r[2] / 2.0;
-            r[5] = r[6] = 2.0 / std::sqrt(3.0) / areaThres;
-            r[7] = r[5] / 2.0;
-        }
-        else {
-            surfaceArea += r[0];
-            r[1] = r[0] * r[0];
-            r[2] = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
-            r[3] = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
-            r[4] = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-            r[5] = r[2] / 2. / r[1];
-            r[6] = r[3] / 2. / r[1];
-            r[7] = r[4] / 2. / r[1];
-        }
-    }
-    if (invalid) {
+    if (!rest_constants(V_rest, F, nF, areaThres, m->rest, surfaceArea)) {
         delete m;
         return fail(ctx, OC_ERR_DEGENERATE, "oc_mesh_create: zero-area rest triangle");
     }
@@ -393,45 +480,15 @@ int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV, 
     m->scalars[0] = surfaceArea;
     m->scalars[1] = avg / (3.0 * nF);
     m->scalars[2] = std::sqrt(surfaceArea / M_PI);
-    // SoA upload
-    oc::DeviceMesh& d = m->d;
-    d.nV = nV;
-    d.nF = nF;
-    std::vector<int> f0(nF), f1(nF), f2(nF);
-    std::vector<double> col[8];
-    for (auto& c : col) c.resize(nF);
-    for (int t = 0; t < nF; ++t) {
-        f0[t] = F[3 * t]; f1[t] = F[3 * t + 1]; f2[t] = F[3 * t + 2];
-        const double* r = &m->rest[8 * (size_t)t];
-        col[0][t] = r[1];                    // triAreaSq
-        col[1][t] = r[0] / surfaceArea;      // w (SymDirichletEnergy.cpp:41)
-        col[2][t] = r[2]; col[3][t] = r[3]; col[4][t] = r[4];
-        col[5][t] = r[5]; col[6][t] = r[6]; col[7][t] = r[7];
-    }
-    // vertex -> corners, sorted by triangle id
-    std::vector<int> vcPtr(nV + 1, 0), vcIdx(3 * (size_t)nF);
-    for (int t = 0; t < nF; ++t)
-        for (int k = 0; k < 3; ++k) vcPtr[F[3 * t + k] + 1]++;
-    for (int v = 0; v < nV; ++v) vcPtr[v + 1] += vcPtr[v];
-    {
-        std::vector<int> fill(vcPtr.begin(), vcPtr.end() - 1);
-        for (int t = 0; t < nF; ++t)
-            for (int k = 0; k < 3; ++k) vcIdx[fill[F[3 * t + k]]++] = k * nF + t;
-    }
     std::vector<unsigned char> mask(nV, 0);
     for (int i = 0; i < nFixed; ++i) mask[fixedVert[i]] = 1;
+    oc::DeviceMesh& d = m->d;
+    int rc = device_mesh_upload(ctx, d, nV, F, nF, m->rest, surfaceArea, mask);
     cudaStream_t st = ctx->stream;
-    int rc = OC_OK;
     auto chk = [&](cudaError_t e, const char* what) {
         if (rc == OC_OK && e != cudaSuccess) rc = fail(ctx, OC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     };
-    chk(dalloc(&d.F0, nF), "alloc"); chk(dalloc(&d.F1, nF), "alloc"); chk(dalloc(&d.F2, nF), "alloc");
-    double** dcols[8] = {&d.A2, &d.w, &d.e0, &d.e1, &d.e01, &d.e0d, &d.e1d, &d.e01d};
-    for (int k = 0; k < 8; ++k) chk(dalloc(dcols[k], nF), "alloc");
     chk(dalloc(&d.uv, nV), "alloc");
-    chk(dalloc(&d.vcPtr, nV + 1), "alloc");
-    chk(dalloc(&d.vcIdx, 3 * (size_t)nF), "alloc");
-    chk(dalloc(&d.fixedMask, nV), "alloc");
     chk(dalloc(&m->cornerBuf, 3 * (size_t)nF), "alloc");
     chk(dalloc(&m->tmpV, nV), "alloc");
     chk(dalloc(&m->hb, 21 * (size_t)nF), "alloc");
@@ -441,13 +498,7 @@ int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV, 
     chk(dalloc(&m->scratch.minBits, 2), "alloc");
     chk(cudaMallocHost(&m->scratch.hostResult, sizeof(double) * 16), "alloc host");
     if (rc == OC_OK) {
-        chk(upload(d.F0, f0.data(), nF, st), "upload"); chk(upload(d.F1, f1.data(), nF, st), "upload");
-        chk(upload(d.F2, f2.data(), nF, st), "upload");
-        for (int k = 0; k < 8; ++k) chk(upload(*dcols[k], col[k].data(), nF, st), "upload");
         chk(cudaMemcpyAsync(d.uv, UV, sizeof(double2) * nV, cudaMemcpyHostToDevice, st), "upload");
-        chk(upload(d.vcPtr, vcPtr.data(), nV + 1, st), "upload");
-        chk(upload(d.vcIdx, vcIdx.data(), 3 * (size_t)nF, st), "upload");
-        chk(upload(d.fixedMask, mask.data(), nV, st), "upload");
         chk(cudaStreamSynchronize(st), "sync");
     }
     if (rc != OC_OK) {
@@ -461,11 +512,8 @@ int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV, 
 int oc_mesh_destroy(oc_mesh* m)
 {
     if (!m) return OC_ERR_INVALID;
-    oc::DeviceMesh& d = m->d;
-    cudaFree(d.F0); cudaFree(d.F1); cudaFree(d.F2);
-    cudaFree(d.A2); cudaFree(d.w); cudaFree(d.e0); cudaFree(d.e1); cudaFree(d.e01);
-    cudaFree(d.e0d); cudaFree(d.e1d); cudaFree(d.e01d);
-    cudaFree(d.uv); cudaFree(d.vcPtr); cudaFree(d.vcIdx); cudaFree(d.fixedMask);
+    device_mesh_free(m->d);
+    cudaFree(m->d.uv);
     cudaFree(m->cornerBuf); cudaFree(m->tmpV); cudaFree(m->hb); cudaFree(m->tmpF);
     cudaFree(m->scratch.partials); cudaFree(m->scratch.result); cudaFree(m->scratch.minBits);
     if (m->scratch.hostResult) cudaFreeHost(m->scratch.hostResult);
@@ -782,6 +830,8 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
     if (!o) return OC_ERR_NOMEM;
     o->mesh = mesh;
     o->param = energyParam;
+    o->wScaf = energyParam * 0.01;   // w_scaf, fixed at construction (Optimizer.cpp:87)
+    o->nWhole = o->capWhole = mesh->d.nV;
     if (cfg) o->cfg = *cfg;
     else oc_optimizer_default_config(&o->cfg);
     if (!(o->cfg.pcgTol > 0.0)) o->cfg.pcgTol = 1e-8;
@@ -811,6 +861,9 @@ int oc_optimizer_destroy(oc_optimizer* o)
 {
     if (!o) return OC_ERR_INVALID;
     cudaFree(o->g); cudaFree(o->dir); cudaFree(o->uv0);
+    cudaFree(o->wuv); cudaFree(o->airCorner); cudaFree(o->airHb);
+    o->air.uv = nullptr;
+    device_mesh_free(o->air);
     if (o->ls) oc_linsys_destroy(o->ls);
     for (auto& e : o->ev)
         if (e) cudaEventDestroy(e);
@@ -826,16 +879,92 @@ static void update_target_gres(oc_optimizer* o)
                     o->relGL2Tol;
 }
 
+// the mesh as the optimizer's kernels see it: with a scaffold, its UV is the
+// leading part of the augmented UV
+static oc::DeviceMesh mesh_view(const oc_optimizer* o)
+{
+    oc::DeviceMesh md = o->mesh->d;
+    if (o->scaf) md.uv = o->wuv;
+    return md;
+}
+
+static const double2* current_uv(const oc_optimizer* o) { return o->scaf ? o->wuv : o->mesh->d.uv; }
+
+// Optimizer::computeEnergyVal (Optimizer.cpp:764-781) at uv + alphas[k] dir:
+// energyParams[0] E_SD, plus with a scaffold w_scaf / |F_air| times the air
+// mesh's uniform-weight E_SD (scafOut receives that part).
 static int compute_energy(oc_optimizer* o, const double2* uv, const double2* dir, const double* alphas, int n,
-                          double* out)
+                          double* out, double* scafOut = nullptr)
 {
     oc_mesh* m = o->mesh;
-    oc::launch_energy(m->d, uv, dir, alphas, n, 0, 1.0, m->scratch, m->ctx->stream);
+    cudaStream_t st = m->ctx->stream;
+    oc::launch_energy(mesh_view(o), uv, dir, alphas, n, 0, 1.0, m->scratch, st);
     o->launches += 2;
-    double e[oc::kMaxTrials];
-    int rc = read_result(m, n, e);
+    if (o->scaf) {
+        oc::launch_energy(o->air, uv, dir, alphas, n, 1, 1.0, m->scratch, st, m->scratch.result + oc::kMaxTrials);
+        o->launches += 2;
+    }
+    double e[2 * oc::kMaxTrials];
+    int rc = read_result(m, o->scaf ? 2 * oc::kMaxTrials : n, e);
     if (rc) return rc;
-    for (int k = 0; k < n; ++k) out[k] = o->param * e[k];   // Optimizer.cpp:767
+    for (int k = 0; k < n; ++k) {
+        out[k] = o->param * e[k];   // Optimizer.cpp:767
+        double es = 0.0;
+        if (o->scaf) {
+            es = e[oc::kMaxTrials + k] * o->airScale;   // Optimizer.cpp:776
+            out[k] += es;
+        }
+        if (scafOut) scafOut[k] = es;
+    }
+    return OC_OK;
+}
+
+// (Re)builds the Newton-matrix pattern and its symbolic factorisation for
+// the current system: the mesh alone, or mesh + air mesh in the augmented
+// numbering (Scaffold::mergeVNeighbor / mergeFixedV, Scaffold.cpp:295-313,
+// then LinSysSolver::set_pattern + analyze_pattern, Optimizer.cpp:521-527).
+static int ensure_pattern(oc_optimizer* o)
+{
+    if (!o->patternStale) return OC_OK;
+    oc_mesh* m = o->mesh;
+    const int nV = m->d.nV;
+    int rc;
+    if (!o->scaf) {
+        std::vector<unsigned char> mask(nV, 0);
+        for (int v : m->fixed) mask[v] = 1;
+        rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask);
+    }
+    else {
+        // rowFixed: 1 = fixed mesh vertex, 2 = fixed in the air mesh as well
+        // (its diagonal also receives the air mesh's w_scaf / |F_air|)
+        std::vector<unsigned char> mask(o->nWhole, 0);
+        for (int v : m->fixed) mask[v] = 1;
+        for (int v : m->fixed)
+            for (int i = 0; i < o->nBnd; ++i)
+                if (o->bnd[i] == v) mask[v] = 2;
+        std::vector<int> Fw(m->F);
+        Fw.insert(Fw.end(), o->airFw.begin(), o->airFw.end());
+        rc = linsys_set_pattern(o->ls, o->nWhole, Fw.data(), static_cast<int>(Fw.size() / 3), mask);
+    }
+    if (rc) return rc;
+    o->patternStale = false;
+    return OC_OK;
+}
+
+// capacity of the augmented vectors (gradient, direction, UV copies)
+static int ensure_whole(oc_optimizer* o, int n)
+{
+    if (n <= o->capWhole && o->wuv) return OC_OK;
+    const int cap = std::max(n, o->capWhole);
+    double2 *g = nullptr, *d = nullptr, *u0 = nullptr, *w = nullptr;
+    if (dalloc(&g, cap) != cudaSuccess || dalloc(&d, cap) != cudaSuccess || dalloc(&u0, cap) != cudaSuccess ||
+        dalloc(&w, cap) != cudaSuccess) {
+        cudaFree(g); cudaFree(d); cudaFree(u0); cudaFree(w);
+        return fail(o->mesh->ctx, OC_ERR_CUDA, "optimizer: augmented vector alloc");
+    }
+    cudaFree(o->g); cudaFree(o->dir); cudaFree(o->uv0); cudaFree(o->wuv);
+    o->g = g; o->dir = d; o->uv0 = u0; o->wuv = w;
+    o->capWhole = cap;
     return OC_OK;
 }
 
@@ -847,29 +976,40 @@ int oc_optimizer_precompute(oc_optimizer* o)
     int rc = oc_mesh_check_inversion(m, &ok);   // Optimizer.cpp:65-67
     if (rc) return rc;
     if (!ok) return fail(m->ctx, OC_ERR_INVERTED, "precompute: inverted UV triangle");
-    std::vector<unsigned char> mask(m->d.nV, 0);
-    for (int v : m->fixed) mask[v] = 1;
-    rc = linsys_set_pattern(o->ls, m->d.nV, m->F.data(), m->d.nF, mask);
+    o->patternStale = true;
+    rc = ensure_pattern(o);
     if (rc) return rc;
+    if (o->scaf)
+        OC_CUDA(m->ctx, cudaMemcpyAsync(o->wuv, m->d.uv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToDevice,
+                                        m->ctx->stream));
     o->lastEDec = 0.0;
     update_target_gres(o);
-    rc = compute_energy(o, m->d.uv, nullptr, nullptr, 1, &o->lastEnergyVal);
+    rc = compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
     if (rc) return rc;
     o->precomputed = true;
     return OC_OK;
 }
 
 // One Newton iteration: Optimizer::solve's body (Optimizer.cpp:208-230) with
-// solve_oneStep (:505-573) and lineSearch (:575-652), scaffold off.
+// solve_oneStep (:505-573) and lineSearch (:575-652), including the
+// scaffolding branches when an air mesh is set.
 static int solve_one(oc_optimizer* o, int* converged)
 {
     oc_mesh* m = o->mesh;
     oc_ctx* ctx = m->ctx;
     cudaStream_t st = ctx->stream;
+    const oc::DeviceMesh md = mesh_view(o);
+    const int nSys = o->scaf ? o->nWhole : m->d.nV;
     *converged = 0;
     record(o, 0);
-    oc::launch_gradient(m->d, 0, o->param, m->cornerBuf, o->g, m->scratch, st);
-    o->launches += 3;
+    if (o->scaf) {
+        oc::launch_gradient_scaf(md, o->param, m->cornerBuf, o->air, o->airScale, o->airCorner, o->g, m->scratch, st);
+        o->launches += 4;
+    }
+    else {
+        oc::launch_gradient(md, 0, o->param, m->cornerBuf, o->g, m->scratch, st);
+        o->launches += 3;
+    }
     double gsq = 0.0;
     int rc = read_result(m, 1, &gsq);
     if (rc) return rc;
@@ -891,14 +1031,17 @@ static int solve_one(oc_optimizer* o, int* converged)
         return OC_OK;
     }
     // Hessian + PSD projection (computeHessian), block assembly (update_a)
-    oc::launch_hessian(m->d, 0, m->hb, st);
+    oc::launch_hessian(md, 0, m->hb, st);
+    if (o->scaf) oc::launch_hessian(o->air, 1, o->airHb, st);
     record(o, 2);
-    oc::launch_assemble(o->ls->b, m->hb, m->d.nF, o->param, st);
-    o->launches += 2;
+    if (o->scaf) oc::launch_assemble_scaf(o->ls->b, m->hb, m->d.nF, o->param, o->airHb, o->air.nF, o->airScale, st);
+    else oc::launch_assemble(o->ls->b, m->hb, m->d.nF, o->param, st);
+    o->launches += o->scaf ? 3 : 2;
     record(o, 3);
-    // factorize (direct) or block-Jacobi preconditioner (PCG); fixed rows = param * I
+    // factorize (direct) or block-Jacobi preconditioner (PCG); fixed rows =
+    // param * I (+ w_scaf / |F_air| * I when also fixed in the air mesh)
     int bad = 0;
-    rc = linsys_factor(o->ls, o->param, &bad);
+    rc = linsys_factor(o->ls, o->param, &bad, o->param + o->airScale);
     if (rc) return rc;
     o->badPivots = bad;
     o->launches += 1 + (o->ls->kind == OC_SOLVER_DIRECT ? 3 + (long long)o->ls->chol.launches.size() : 0);
@@ -923,52 +1066,80 @@ static int solve_one(oc_optimizer* o, int* converged)
     o->lastPcgIters = iters;
     o->lastRelRes = relres;
     record(o, 5);
-    // Optimizer::lineSearch: injective bound, then halve until E <= E_last
-    oc::launch_init_step(m->d, o->dir, 1.0, m->scratch, st);
+    // Optimizer::lineSearch: injective bound over the mesh and the air mesh
+    // (Optimizer::initStepSize, :692-704), then halve until E <= E_last
+    oc::launch_init_step(md, o->dir, 1.0, m->scratch, st);
     o->launches += 2;
+    if (o->scaf) {
+        oc::launch_init_step(o->air, o->dir, 1.0, m->scratch, st, false);
+        o->launches += 1;
+    }
     double step = 1.0;
     rc = read_min(m, &step);
     if (rc) return rc;
     record(o, 6);
     step *= 0.99;
-    OC_CUDA(ctx, cudaMemcpyAsync(o->uv0, m->d.uv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToDevice, st));
+    OC_CUDA(ctx, cudaMemcpyAsync(o->uv0, current_uv(o), sizeof(double2) * nSys, cudaMemcpyDeviceToDevice, st));
     bool stopped = false;
-    double testE = 0.0, accepted = -1.0, lastTried = step, lastTriedE = 0.0;
+    double testE = 0.0, testScaf = 0.0, accepted = -1.0, lastTried = step, lastTriedE = 0.0, lastTriedScaf = 0.0;
+    double lastScaf0 = 0.0;
     int lsLaunches = 0;
     int batch = 1;
     double alpha = step;
+    bool first = true;
     while (accepted < 0.0) {
-        double alphas[oc::kMaxTrials], E[oc::kMaxTrials];
+        double alphas[oc::kMaxTrials], E[oc::kMaxTrials], Es[oc::kMaxTrials];
         int n = 0;
-        for (double a = alpha; n < batch && a != 0.0; a /= 2.0) alphas[n++] = a;
-        if (n == 0) break;
-        rc = compute_energy(o, o->uv0, o->dir, alphas, n, E);
+        // with a scaffold the first launch also re-evaluates E at the current
+        // point (alpha = 0): lastEnergyVal is recomputed because the air
+        // mesh changed since the last step (Optimizer.cpp:588-592)
+        const int lead = (first && o->scaf) ? 1 : 0;
+        if (lead) alphas[n++] = 0.0;
+        for (double a = alpha; n < batch + lead && a != 0.0; a /= 2.0) alphas[n++] = a;
+        if (n == lead) break;
+        rc = compute_energy(o, o->uv0, o->dir, alphas, n, E, Es);
         if (rc) return rc;
         ++lsLaunches;
-        for (int k = 0; k < n; ++k) {
+        if (lead) {
+            o->lastEnergyVal = E[0];
+            lastScaf0 = Es[0];
+        }
+        for (int k = lead; k < n; ++k) {
             lastTried = alphas[k];
             lastTriedE = E[k];
+            lastTriedScaf = Es[k];
             if (!(E[k] > o->lastEnergyVal)) {   // while(testingE > lastEnergyVal) halves, Optimizer.cpp:597
                 accepted = alphas[k];
                 testE = E[k];
+                testScaf = Es[k];
                 break;
             }
         }
         alpha = alphas[n - 1] / 2.0;
         batch = o->cfg.lineSearchBatch;
+        first = false;
     }
     if (accepted < 0.0) {   // step reached 0 (Optimizer.cpp:600-606): keep the last trial
         stopped = true;
         accepted = lastTried;
         testE = lastTriedE;
+        testScaf = lastTriedScaf;
     }
-    oc::launch_step_forward(o->uv0, o->dir, accepted, m->d.uv, m->d.nV, st);
+    if (o->scaf) {
+        oc::launch_step_forward(o->uv0, o->dir, accepted, o->wuv, nSys, st);
+        OC_CUDA(ctx, cudaMemcpyAsync(m->d.uv, o->wuv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToDevice, st));
+    }
+    else {
+        oc::launch_step_forward(o->uv0, o->dir, accepted, m->d.uv, nSys, st);
+    }
     o->launches += 1;
     OC_CUDA(ctx, cudaGetLastError());
     record(o, 7);
     o->lastEDec = o->lastEnergyVal - testE;
+    if (o->scaf) o->lastEDec += (-lastScaf0 + testScaf);   // Optimizer.cpp:632-634
     if ((o->lastEDec / o->lastEnergyVal < 1.0e-6 * accepted) && (accepted > 1.0e-3)) stopped = true;   // :635-638
     o->lastEnergyVal = testE;
+    o->eScaf = testScaf;
     o->lastStep = accepted;
     o->lastLsLaunches = lsLaunches;
     o->globalIterNum++;
@@ -990,6 +1161,11 @@ int oc_optimizer_solve(oc_optimizer* o, int maxIter, int* result)
     if (!o->precomputed) return fail(o->mesh->ctx, OC_ERR_INVALID, "solve before precompute");
     *result = 0;
     int status = OC_OK;
+    int prc = ensure_pattern(o);
+    if (prc) return prc;
+    if (o->scaf)   // the mesh's UV is authoritative (oc_mesh_set_uv may have moved it)
+        OC_CUDA(o->mesh->ctx, cudaMemcpyAsync(o->wuv, o->mesh->d.uv, sizeof(double2) * o->mesh->d.nV,
+                                              cudaMemcpyDeviceToDevice, o->mesh->ctx->stream));
     for (int it = 0; it < maxIter; ++it) {
         int conv = 0;
         int rc = solve_one(o, &conv);
@@ -1031,7 +1207,10 @@ int oc_optimizer_set_energy_param(oc_optimizer* o, double p)
     o->param = p;
     update_target_gres(o);
     if (!o->precomputed) return OC_OK;
-    return compute_energy(o, o->mesh->d.uv, nullptr, nullptr, 1, &o->lastEnergyVal);
+    if (o->scaf)
+        OC_CUDA(o->mesh->ctx, cudaMemcpyAsync(o->wuv, o->mesh->d.uv, sizeof(double2) * o->mesh->d.nV,
+                                              cudaMemcpyDeviceToDevice, o->mesh->ctx->stream));
+    return compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
 }
 
 int oc_optimizer_last_step(oc_optimizer* o, double* stepSize, int* pcgIters, double* pcgRelRes, int* lsLaunches,
@@ -1060,6 +1239,132 @@ int oc_optimizer_solver_stats(oc_optimizer* o, double* out8)
 {
     if (!o) return OC_ERR_INVALID;
     return oc_linsys_stats(o->ls, out8);
+}
+
+int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, const int* airF, int nAirF,
+                              const int* bnd, int nBnd, double areaThres)
+{
+    if (!o || !airV || !airF || !bnd || nAirF <= 0 || nBnd <= 0 || nAirV < nBnd) return OC_ERR_INVALID;
+    oc_mesh* m = o->mesh;
+    oc_ctx* ctx = m->ctx;
+    const int nV = m->d.nV;
+    if ((long long)nV + nAirV - nBnd >= (1LL << 30) || ((long long)m->d.nF + nAirF) * 9 >= (1LL << 31))
+        return fail(ctx, OC_ERR_INVALID, "set_scaffold: system too large");
+    for (long long i = 0; i < 3LL * nAirF; ++i)
+        if (airF[i] < 0 || airF[i] >= nAirV) return fail(ctx, OC_ERR_INVALID, "set_scaffold: air vertex index out of range");
+    std::vector<int> isBnd(nV, -1);
+    for (int i = 0; i < nBnd; ++i) {
+        if (bnd[i] < 0 || bnd[i] >= nV) return fail(ctx, OC_ERR_INVALID, "set_scaffold: boundary vertex out of range");
+        if (isBnd[bnd[i]] >= 0) return fail(ctx, OC_ERR_INVALID, "set_scaffold: repeated boundary vertex");
+        isBnd[bnd[i]] = i;
+    }
+    // areaThres_AM = sqrt(3)/4 edgeLen_eps^2, edgeLen_eps = avgEdgeLen / 2
+    // for a whole-mesh scaffold (Scaffold.cpp:34, 189)
+    if (!(areaThres >= 0.0)) {
+        const double eps = m->scalars[1] * 0.5;
+        areaThres = std::sqrt(3.0) / 4.0 * eps * eps;
+    }
+    // air mesh rest shape = its own layout, z = 0 (Scaffold.cpp:187-190)
+    std::vector<double> V3(3 * (size_t)nAirV);
+    for (int i = 0; i < nAirV; ++i) {
+        V3[3 * (size_t)i] = airV[2 * (size_t)i];
+        V3[3 * (size_t)i + 1] = airV[2 * (size_t)i + 1];
+        V3[3 * (size_t)i + 2] = 0.0;
+    }
+    std::vector<double> rest;
+    double area = 0.0;
+    if (!rest_constants(V3.data(), airF, nAirF, areaThres, rest, area))
+        return fail(ctx, OC_ERR_DEGENERATE, "set_scaffold: zero-area air triangle");
+    const int nWhole = nV + nAirV - nBnd;
+    auto toWhole = [&](int a) { return a < nBnd ? bnd[a] : nV + a - nBnd; };   // localVI2Global
+    std::vector<int> Fw(3 * (size_t)nAirF);
+    for (size_t i = 0; i < Fw.size(); ++i) Fw[i] = toWhole(airF[i]);
+    // fixed air vertices: the mesh's fixed vertices on the boundary (Scaffold.cpp:193-199)
+    std::vector<unsigned char> airMask(nWhole, 0);
+    for (int v : m->fixed)
+        if (isBnd[v] >= 0) airMask[v] = 1;
+    const bool samePattern = o->scaf && !o->patternStale && Fw == o->airFw && o->nWhole == nWhole &&
+                             std::equal(bnd, bnd + nBnd, o->bnd.begin(), o->bnd.end());
+    int rc = ensure_whole(o, nWhole);
+    if (rc) return rc;
+    if (nAirF > o->capAirF) {
+        cudaFree(o->airCorner); cudaFree(o->airHb);
+        o->airCorner = nullptr; o->airHb = nullptr;
+        o->capAirF = 0;
+        if (dalloc(&o->airCorner, 3 * (size_t)nAirF) != cudaSuccess || dalloc(&o->airHb, 21 * (size_t)nAirF) != cudaSuccess)
+            return fail(ctx, OC_ERR_CUDA, "set_scaffold: alloc");
+        o->capAirF = nAirF;
+    }
+    o->air.uv = nullptr;
+    rc = device_mesh_upload(ctx, o->air, nWhole, Fw.data(), nAirF, rest, area, airMask);
+    if (rc) return rc;
+    o->air.uv = o->wuv;
+    cudaStream_t st = ctx->stream;
+    OC_CUDA(ctx, cudaMemcpyAsync(o->wuv, m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToDevice, st));
+    if (nAirV > nBnd)
+        OC_CUDA(ctx, cudaMemcpyAsync(o->wuv + nV, airV + 2 * (size_t)nBnd, sizeof(double2) * (nAirV - nBnd),
+                                     cudaMemcpyHostToDevice, st));
+    OC_CUDA(ctx, cudaStreamSynchronize(st));
+    o->airFw.swap(Fw);
+    o->bnd.assign(bnd, bnd + nBnd);
+    o->nWhole = nWhole;
+    o->nAirV = nAirV;
+    o->nBnd = nBnd;
+    o->airScale = o->wScaf / nAirF;   // w_scaf / airMesh.F.rows() (Optimizer.cpp:776)
+    o->scaf = true;
+    if (!samePattern) o->patternStale = true;
+    return OC_OK;
+}
+
+int oc_optimizer_clear_scaffold(oc_optimizer* o)
+{
+    if (!o) return OC_ERR_INVALID;
+    if (o->scaf) o->patternStale = true;
+    o->scaf = false;
+    o->eScaf = 0.0;
+    o->nWhole = o->mesh->d.nV;
+    return OC_OK;
+}
+
+int oc_optimizer_get_scaffold_uv(oc_optimizer* o, double* airV)
+{
+    if (!o || !airV || !o->scaf) return OC_ERR_INVALID;
+    oc_mesh* m = o->mesh;
+    std::vector<double> w(2 * (size_t)o->nWhole);
+    OC_CUDA(m->ctx, cudaMemcpyAsync(w.data(), o->wuv, sizeof(double2) * o->nWhole, cudaMemcpyDeviceToHost, m->ctx->stream));
+    OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+    for (int i = 0; i < o->nAirV; ++i) {
+        const int v = i < o->nBnd ? o->bnd[i] : m->d.nV + i - o->nBnd;
+        airV[2 * (size_t)i] = w[2 * (size_t)v];
+        airV[2 * (size_t)i + 1] = w[2 * (size_t)v + 1];
+    }
+    return OC_OK;
+}
+
+int oc_optimizer_get_last_energy_scaffold(oc_optimizer* o, double* eScaf)
+{
+    if (!o || !eScaf) return OC_ERR_INVALID;
+    *eScaf = o->eScaf;
+    return OC_OK;
+}
+
+int oc_optimizer_system_size(oc_optimizer* o, int* nVerts)
+{
+    if (!o || !nVerts) return OC_ERR_INVALID;
+    *nVerts = o->scaf ? o->nWhole : o->mesh->d.nV;
+    return OC_OK;
+}
+
+int oc_optimizer_last_vectors(oc_optimizer* o, double* gradient, double* searchDir)
+{
+    if (!o) return OC_ERR_INVALID;
+    oc_mesh* m = o->mesh;
+    const int n = o->scaf ? o->nWhole : m->d.nV;
+    cudaStream_t st = m->ctx->stream;
+    if (gradient) OC_CUDA(m->ctx, cudaMemcpyAsync(gradient, o->g, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+    if (searchDir) OC_CUDA(m->ctx, cudaMemcpyAsync(searchDir, o->dir, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+    OC_CUDA(m->ctx, cudaStreamSynchronize(st));
+    return OC_OK;
 }
 
 int oc_optimizer_launch_count(oc_optimizer* o, long long* n)

@@ -192,6 +192,57 @@ __global__ void __launch_bounds__(256) k_grad_gather(DeviceMesh m, const double2
     block_sum_store<1>(acc, 1, partials + (size_t)blockIdx.x * kMaxTrials);
 }
 
+// Augmented gradient with a scaffold, over the whole vertex numbering (mesh
+// vertices, then air-only vertices): Optimizer::computeGradient scales the
+// mesh gradient by energyParams[0] (Optimizer.cpp:786), then
+// Scaffold::augmentGradient (Scaffold.cpp:210-230) adds w * g_air on the
+// boundary vertices and sets w * g_air on the air-only ones.  Both gathers
+// follow triangle order; the air mesh's fixed rows are zeroed before the
+// scaling, as SymDirichletEnergy::computeGradient does for any mesh.
+__global__ void __launch_bounds__(256) k_grad_gather_scaf(DeviceMesh m, const double2* __restrict__ cornerBuf,
+                                                          double scale, DeviceMesh a,
+                                                          const double2* __restrict__ airCorner, double airScale,
+                                                          double2* __restrict__ g, double* partials)
+{
+    double acc[1] = {0.0};
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < a.nV; v += gridDim.x * blockDim.x) {
+        double gx = 0.0, gy = 0.0;
+        const bool onMesh = v < m.nV;
+        if (onMesh) {
+            double sx = 0.0, sy = 0.0;
+            for (int p = m.vcPtr[v]; p < m.vcPtr[v + 1]; ++p) {
+                const double2 c = cornerBuf[m.vcIdx[p]];
+                sx = sx + c.x;
+                sy = sy + c.y;
+            }
+            if (m.fixedMask[v]) { sx = 0.0; sy = 0.0; }
+            gx = scale * sx;
+            gy = scale * sy;
+        }
+        const int p0 = a.vcPtr[v], p1 = a.vcPtr[v + 1];
+        if (p1 > p0) {
+            double sx = 0.0, sy = 0.0;
+            for (int p = p0; p < p1; ++p) {
+                const double2 c = airCorner[a.vcIdx[p]];
+                sx = sx + c.x;
+                sy = sy + c.y;
+            }
+            if (a.fixedMask[v]) { sx = 0.0; sy = 0.0; }
+            if (onMesh) {
+                gx = gx + airScale * sx;
+                gy = gy + airScale * sy;
+            }
+            else {
+                gx = airScale * sx;
+                gy = airScale * sy;
+            }
+        }
+        g[v] = make_double2(gx, gy);
+        acc[0] += gx * gx + gy * gy;
+    }
+    block_sum_store<1>(acc, 1, partials + (size_t)blockIdx.x * kMaxTrials);
+}
+
 // SymDirichletEnergy::initStepSize (SymDirichletEnergy.cpp:555-609); the
 // minimum over triangles is taken with an atomicMin on the bit pattern of
 // positive doubles (order-independent, hence deterministic).
@@ -454,13 +505,13 @@ void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t s
     k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
 }
 
-void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st)
+void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st, double* out)
 {
-    k_reduce_final<<<1, 256, 0, st>>>(s.partials, nBlocks, nVals, s.result);
+    k_reduce_final<<<1, 256, 0, st>>>(s.partials, nBlocks, nVals, out ? out : s.result);
 }
 
 void launch_energy(const DeviceMesh& m, const double2* uv, const double2* dir, const double* alphas, int nTrials,
-                   int uniform, double scale, Scratch& s, cudaStream_t st)
+                   int uniform, double scale, Scratch& s, cudaStream_t st, double* out)
 {
     (void)scale;
     Alphas a = {{0, 0, 0, 0, 0, 0, 0, 0}};
@@ -472,7 +523,7 @@ void launch_energy(const DeviceMesh& m, const double2* uv, const double2* dir, c
         k_energy<4><<<nb, 256, 0, st>>>(m, uv, dir, a, nTrials, uniform, s.partials);
     else
         k_energy<8><<<nb, 256, 0, st>>>(m, uv, dir, a, nTrials, uniform, s.partials);
-    launch_reduce_final(s, nb, nTrials < 1 ? 1 : nTrials, st);
+    launch_reduce_final(s, nb, nTrials < 1 ? 1 : nTrials, st, out);
 }
 
 void launch_energy_elem(const DeviceMesh& m, int uniform, double* out, cudaStream_t st)
@@ -489,9 +540,20 @@ void launch_gradient(const DeviceMesh& m, int uniform, double scale, double2* co
     launch_reduce_final(s, nb, 1, st);
 }
 
-void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, Scratch& s, cudaStream_t st)
+void launch_gradient_scaf(const DeviceMesh& m, double scale, double2* cornerBuf, const DeviceMesh& air,
+                          double airScale, double2* airCornerBuf, double2* g, Scratch& s, cudaStream_t st)
 {
-    k_set_bits<<<1, 1, 0, st>>>(s.minBits, stepSize);
+    k_grad_corners<<<(m.nF + 255) / 256, 256, 0, st>>>(m, 0, cornerBuf);
+    k_grad_corners<<<(air.nF + 255) / 256, 256, 0, st>>>(air, 1, airCornerBuf);
+    const int nb = reduce_blocks_for(air.nV);
+    k_grad_gather_scaf<<<nb, 256, 0, st>>>(m, cornerBuf, scale, air, airCornerBuf, airScale, g, s.partials);
+    launch_reduce_final(s, nb, 1, st);
+}
+
+void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, Scratch& s, cudaStream_t st,
+                      bool reset)
+{
+    if (reset) k_set_bits<<<1, 1, 0, st>>>(s.minBits, stepSize);
     k_init_step<<<reduce_blocks_for(m.nF), 256, 0, st>>>(m, dir, stepSize, s.minBits);
 }
 

@@ -77,18 +77,26 @@ struct PcgWork {
 
 // ---- launchers (kernels live in oc_fp64.cu / oc_kernels.cu) ----
 // energy at uv + alpha_k * dir for k < nTrials (dir may be null: alphas ignored)
+// (sums go to s.result, or to out when given)
 void launch_energy(const DeviceMesh& m, const double2* uv, const double2* dir, const double* alphasHost,
-                   int nTrials, int uniform, double scale, Scratch& s, cudaStream_t st);
+                   int nTrials, int uniform, double scale, Scratch& s, cudaStream_t st, double* out = nullptr);
 void launch_energy_elem(const DeviceMesh& m, int uniform, double* out, cudaStream_t st);
 // corner gradients (3 x nF double2) then per-vertex gather; writes ||g||^2 to s.result[0]
 void launch_gradient(const DeviceMesh& m, int uniform, double scale, double2* cornerBuf, double2* g,
                      Scratch& s, cudaStream_t st);
-// min over triangles of the inversion-free bound, starting from stepSize
-void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, Scratch& s, cudaStream_t st);
+// augmented gradient with a scaffold (Optimizer.cpp:783-797): mesh corners
+// times scale, plus the air mesh's (uniform weights) times airScale on the
+// boundary and air-only vertices; g and ||g||^2 over air.nV vertices
+void launch_gradient_scaf(const DeviceMesh& m, double scale, double2* cornerBuf, const DeviceMesh& air,
+                          double airScale, double2* airCornerBuf, double2* g, Scratch& s, cudaStream_t st);
+// min over triangles of the inversion-free bound, starting from stepSize;
+// with reset = false the running minimum of an earlier launch is lowered
+void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, Scratch& s, cudaStream_t st,
+                      bool reset = true);
 void launch_step_forward(const double2* uv0, const double2* dir, double alpha, double2* uv, int nV,
                          cudaStream_t st);
 void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st);
-void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st);
+void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st, double* out = nullptr);
 int reduce_blocks_for(int n);
 
 // per-triangle PSD-projected Hessian: 21 FP64 values per triangle (SoA)
@@ -96,8 +104,14 @@ void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t s
 // expand the 21 packed values to full 6x6 FP64 (for the API / tests)
 void launch_hessian_expand(const double* hb, int nF, double* out, cudaStream_t st);
 void launch_assemble(const DeviceBsr& b, const double* hb, int nF, double scale, cudaStream_t st);
+// contributions t < nF from hb (times scale), the rest from the air mesh's
+// hbAir (triangle t - nF, times airScale)
+void launch_assemble_scaf(const DeviceBsr& b, const double* hb, int nF, double scale, const double* hbAir, int nFa,
+                          double airScale, cudaStream_t st);
 int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag);
-void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag);
+// fixed rows get fixedDiag * I (rowFixed == 1) or fixedDiag2 * I (rowFixed == 2)
+void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag,
+                          double fixedDiag2 = 0.0);
 // solves A x = rhsSign * rhs (rhsSign = -1 gives the Newton direction from g)
 int pcg_solve(const DeviceBsr& b, const double2* rhs, double2* x, PcgWork& wk, double tol, int maxIter,
               double rhsSign, cudaStream_t st, int* itersOut, double* relresOut, std::string* err);

@@ -72,14 +72,44 @@ __global__ void __launch_bounds__(256) k_assemble(DeviceBsr b, const double* __r
     b.val[s] = Blk2{acc.a00 * scale, acc.a01 * scale, acc.a10 * scale, acc.a11 * scale};
 }
 
+// Assembly with a scaffold: the mesh's contributions (scaled by
+// energyParams[0], Optimizer.cpp:825) come first in every slot list, then the
+// air mesh's (scaled by w_scaf / |F_air|, Scaffold::augmentProxyMatrix,
+// Scaffold.cpp:232-250, remapped to the augmented numbering).
+__global__ void __launch_bounds__(256) k_assemble_scaf(DeviceBsr b, const double* __restrict__ hb, int nF, double scale,
+                                                       const double* __restrict__ hbAir, int nFa, double airScale)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= b.nnzb) return;
+    Blk2 acc{0.0, 0.0, 0.0, 0.0}, accA{0.0, 0.0, 0.0, 0.0};
+    const int split = 9 * nF;
+    for (int p = b.cPtr[s]; p < b.cPtr[s + 1]; ++p) {
+        const int code = b.cIdx[p];
+        if (code < split) {
+            const Blk2 B = local_block(hb, nF, code);
+            acc.a00 += B.a00; acc.a01 += B.a01; acc.a10 += B.a10; acc.a11 += B.a11;
+        }
+        else {
+            const Blk2 B = local_block(hbAir, nFa, code - split);
+            accA.a00 += B.a00; accA.a01 += B.a01; accA.a10 += B.a10; accA.a11 += B.a11;
+        }
+    }
+    b.val[s] = Blk2{acc.a00 * scale + accA.a00 * airScale, acc.a01 * scale + accA.a01 * airScale,
+                    acc.a10 * scale + accA.a10 * airScale, acc.a11 * scale + accA.a11 * airScale};
+}
+
 // Fixed rows: diagonal = energyParam * I (SymDirichletEnergy.cpp:541-548 scaled
-// at Optimizer.cpp:825); block-Jacobi inverse per row.
-__global__ void k_precond(DeviceBsr b, double fixedDiag, int* flag)
+// at Optimizer.cpp:825), plus w_scaf / |F_air| * I when the vertex is also a
+// fixed air-mesh vertex (rowFixed == 2); block-Jacobi inverse per row.
+__global__ void k_precond(DeviceBsr b, double fixedDiag, double fixedDiag2, int* flag)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= b.nRows) return;
     const int s = b.diagSlot[r];
-    if (b.rowFixed[r] && fixedDiag > 0.0) b.val[s] = Blk2{fixedDiag, 0.0, 0.0, fixedDiag};
+    if (b.rowFixed[r] && fixedDiag > 0.0) {
+        const double d = b.rowFixed[r] == 2 ? fixedDiag2 : fixedDiag;
+        b.val[s] = Blk2{d, 0.0, 0.0, d};
+    }
     const Blk2 D = b.val[s];
     const double a = D.a00, bb = 0.5 * (D.a01 + D.a10), d = D.a11;
     const double det = a * d - bb * bb;
@@ -241,15 +271,21 @@ void launch_assemble(const DeviceBsr& b, const double* hb, int nF, double scale,
     k_assemble<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b, hb, nF, scale);
 }
 
+void launch_assemble_scaf(const DeviceBsr& b, const double* hb, int nF, double scale, const double* hbAir, int nFa,
+                          double airScale, cudaStream_t st)
+{
+    k_assemble_scaf<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b, hb, nF, scale, hbAir, nFa, airScale);
+}
+
 int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag)
 {
-    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, -1.0, dFlag);
+    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, -1.0, -1.0, dFlag);
     return 0;
 }
 
-void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag)
+void launch_precond_fixed(const DeviceBsr& b, double fixedDiag, cudaStream_t st, int* dFlag, double fixedDiag2)
 {
-    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, fixedDiag, dFlag);
+    k_precond<<<(b.nRows + 255) / 256, 256, 0, st>>>(b, fixedDiag, fixedDiag2, dFlag);
 }
 
 void launch_spmv(const DeviceBsr& b, const double2* x, double2* y, cudaStream_t st)

@@ -208,6 +208,24 @@ def torus_knot_tube(nu=2000, nv=512, p=2, q=3, radius=0.15, noise=0.002, seed=4)
     return P.reshape(-1, 3), _grid_torus_faces(nu, nv)
 
 
+def bumpy_sheet(n=40, amp=0.25, noise=0.01, seed=5):
+    """Open disk: n x n grid over [-1, 1]^2 with height
+    amp * sin(2x) * cos(3y) plus N(0, noise); alternating diagonals."""
+    rng = np.random.default_rng(seed)
+    x, y = np.meshgrid(np.linspace(-1.0, 1.0, n), np.linspace(-1.0, 1.0, n), indexing="ij")
+    z = amp * np.sin(2.0 * x) * np.cos(3.0 * y) + rng.normal(0.0, noise, x.shape)
+    V = np.stack([x.ravel(), y.ravel(), z.ravel()], 1)
+    F = []
+    for i in range(n - 1):
+        for j in range(n - 1):
+            a, b, c, d = i * n + j, (i + 1) * n + j, (i + 1) * n + j + 1, i * n + j + 1
+            if (i + j) % 2 == 0:
+                F += [[a, b, c], [a, c, d]]
+            else:
+                F += [[a, b, d], [b, c, d]]
+    return V, np.asarray(F, np.int32)
+
+
 def plane():
     V = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float64)
     F = np.array([[0, 1, 2], [0, 2, 3]], np.int32)
@@ -240,6 +258,7 @@ CONFIGS = {
     "ellipsoid_2k": lambda: ellipsoid(32, 32, (1.0, 0.6, 0.4), 8, 6, 0.02, 2),
     "ellipsoid_20k": lambda: ellipsoid(100, 100, (1.0, 0.6, 0.4), 8, 6, 0.02, 2),
     "torus_768": lambda: torus(24, 16, 1.0, 0.35, 1),
+    "sheet_3k": lambda: bumpy_sheet(40, 0.25, 0.01, 5),
     "cube": cube,
     "plane": plane,
     "triangle": single_triangle,

@@ -22,6 +22,10 @@
 //        states    dump UV after every iteration
 //        time      print wall-clock seconds per Newton iteration
 //        nodump    write only the trace (for timing runs)
+//        scaf      scaffolding on even after a one-point cut of a closed mesh
+//        scafdump  dump, per iteration, the air mesh the iteration used
+//                  (vertices, triangles, boundary map, fixed air vertices)
+//                  and the augmented gradient / direction of iteration 0
 // Outputs are .npy files in outdir (which must exist).
 
 #include "Optimizer.hpp"
@@ -135,12 +139,14 @@ int main(int argc, char** argv)
     if (out.back() != '/') out += '/';
     const double lambda_init = std::stod(argv[3]);
     const int iters = std::stoi(argv[4]);
-    bool dumpHess = false, dumpStates = false, doTime = false, noDump = false;
+    bool dumpHess = false, dumpStates = false, doTime = false, noDump = false, forceScaf = false, scafDump = false;
     for (int i = 5; i < argc; ++i) {
         if (!std::strcmp(argv[i], "hess")) dumpHess = true;
         else if (!std::strcmp(argv[i], "states")) dumpStates = true;
         else if (!std::strcmp(argv[i], "time")) doTime = true;
         else if (!std::strcmp(argv[i], "nodump")) noDump = true;
+        else if (!std::strcmp(argv[i], "scaf")) forceScaf = true;
+        else if (!std::strcmp(argv[i], "scafdump")) scafDump = true;
     }
     outputFolderPath = out;
     logFile.open(out + "log.txt");
@@ -234,7 +240,7 @@ int main(int argc, char** argv)
     std::vector<double> energyParams;
     energyParams.emplace_back(1.0 - lambda_init);
     energyTerms.emplace_back(new OptCuts::SymDirichletEnergy());
-    const bool scaffolding = bijective && !rand1PInitCut;
+    const bool scaffolding = bijective && (!rand1PInitCut || forceScaf);
 
     // ---- initial-state dumps ---------------------------------------------
     if (!noDump) {
@@ -281,30 +287,46 @@ int main(int argc, char** argv)
     auto t1 = std::chrono::steady_clock::now();
     if (lambda_init > 0.0) fractureMode = true;
 
-    std::vector<double> trE, trESD, trG, trAlpha, trTime, trStatus;
+    std::vector<double> trE, trESD, trG, trAlpha, trTime, trStatus, trEtot;
     trE.push_back(opt.getLastEnergyVal(true));
+    trEtot.push_back(opt.getLastEnergyVal(false));
     std::vector<double> states;
+    // per-iteration scaffolds, concatenated: air V rows, air F rows, bnd, fixed
+    std::vector<double> scV;
+    std::vector<int> scF, scB, scFix, scOff;   // scOff: per iteration nV, nF, nBnd, nFixed
     for (int it = 0; it < iters; ++it) {
         Eigen::MatrixXd Vprev = opt.getResult().V;
+        if (scaffolding && scafDump) {
+            const OptCuts::Scaffold& S = opt.getScaffold();
+            Eigen::Matrix<double, Eigen::Dynamic, Eigen::Dynamic, Eigen::RowMajor> AV = S.airMesh.V;
+            Eigen::Matrix<int, Eigen::Dynamic, Eigen::Dynamic, Eigen::RowMajor> AF = S.airMesh.F;
+            scV.insert(scV.end(), AV.data(), AV.data() + AV.size());
+            scF.insert(scF.end(), AF.data(), AF.data() + AF.size());
+            scB.insert(scB.end(), S.bnd.data(), S.bnd.data() + S.bnd.size());
+            scFix.insert(scFix.end(), S.airMesh.fixedVert.begin(), S.airMesh.fixedVert.end());
+            scOff.insert(scOff.end(), {(int)AV.rows(), (int)AF.rows(), (int)S.bnd.size(), (int)S.airMesh.fixedVert.size()});
+        }
         auto s0 = std::chrono::steady_clock::now();
         int st = opt.solve(1);
         auto s1 = std::chrono::steady_clock::now();
         const Eigen::VectorXd& d = opt.searchDirection();
         const Eigen::MatrixXd& Vn = opt.getResult().V;
         double num = 0.0, den = 0.0;
-        for (int v = 0; v < Vn.rows() && d.size() == 2 * Vn.rows(); ++v) {
+        for (int v = 0; v < Vn.rows() && d.size() >= 2 * Vn.rows(); ++v) {
             for (int k = 0; k < 2; ++k) {
                 num += (Vn(v, k) - Vprev(v, k)) * d[2 * v + k];
                 den += d[2 * v + k] * d[2 * v + k];
             }
         }
         trE.push_back(opt.getLastEnergyVal(true));
+        trEtot.push_back(opt.getLastEnergyVal(false));
         trESD.push_back(opt.getLastEnergyVal(true) / energyParams[0]);
         trG.push_back(opt.grad().squaredNorm());
         trAlpha.push_back(den > 0 ? num / den : 0.0);
         trTime.push_back(std::chrono::duration<double>(s1 - s0).count());
         trStatus.push_back(st);
         if (it == 0 && !noDump) npy_vec(out + "dir0.npy", d);
+        if (it == 0 && !noDump && scaffolding) npy_vec(out + "gradw0.npy", opt.grad());
         if (dumpStates) {
             Eigen::Matrix<double, Eigen::Dynamic, Eigen::Dynamic, Eigen::RowMajor> R = Vn;
             states.insert(states.end(), R.data(), R.data() + R.size());
@@ -318,6 +340,14 @@ int main(int argc, char** argv)
     npy_vecd(out + "trace_alpha.npy", trAlpha);
     npy_vecd(out + "trace_time.npy", trTime);
     npy_vecd(out + "trace_status.npy", trStatus);
+    npy_vecd(out + "trace_Etot.npy", trEtot);
+    if (scaffolding && scafDump) {
+        write_npy(out + "scaf_V.npy", scV.data(), "<f8", 8, {scV.size() / 2, 2});
+        write_npy(out + "scaf_F.npy", scF.data(), "<i4", 4, {scF.size() / 3, 3});
+        npy_veci(out + "scaf_bnd.npy", scB);
+        npy_veci(out + "scaf_fixed.npy", scFix);
+        write_npy(out + "scaf_off.npy", scOff.data(), "<i4", 4, {scOff.size() / 4, 4});
+    }
     npy_vecd(out + "misc.npy", {std::chrono::duration<double>(t1 - t0).count(), opt.targetG()});
     if (dumpStates) {
         const size_t nv = opt.getResult().V.rows();

@@ -19,7 +19,8 @@ def load_golden(name):
         return {k: z[k] for k in z.files}
 
 
-GOLDEN_CASES = ["triangle", "plane", "cube", "icosphere_320", "ellipsoid_2k", "torus_768", "icosphere_5k"]
+GOLDEN_CASES = ["triangle", "plane", "cube", "icosphere_320", "ellipsoid_2k", "torus_768", "icosphere_5k",
+                "sheet_3k", "icosphere_320_scaf"]
 # closed genus-0 inputs: the reference runs its first Newton phase without the scaffold
 SCAFFOLD_OFF = ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k"]
 
@@ -33,3 +34,21 @@ def golden():
             cache[name] = load_golden(name)
         return cache[name]
     return get
+
+
+# cases whose golden holds the air mesh of every iteration
+SCAFFOLD_DUMPS = ["triangle", "plane", "torus_768", "sheet_3k", "icosphere_320_scaf"]
+
+
+def golden_scaffolds(g):
+    """Per-iteration air meshes of a golden: list of (airV, airF, bnd, fixed)."""
+    out = []
+    pv = pf = pb = px = 0
+    for nv, nf, nb, nx in g["scaf_off"]:
+        out.append((g["scaf_V"][pv:pv + nv], g["scaf_F"][pf:pf + nf], g["scaf_bnd"][pb:pb + nb],
+                    g["scaf_fixed"][px:px + nx]))
+        pv += nv
+        pf += nf
+        pb += nb
+        px += nx
+    return out

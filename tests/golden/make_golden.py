@@ -13,6 +13,11 @@ packs its dumps into one compressed .npz per case:
     dir0                               SimplicialLDLT Newton direction at UV0
     trace_E, trace_gsq, trace_alpha    per-iteration Optimizer::solve(1) trace
     UV_iters (small cases)             UV after every iteration
+    trace_Etot                         energy including the scaffold term
+    scaf_V, scaf_F, scaf_bnd,          scaffold cases: the air mesh each
+    scaf_fixed, scaf_off               iteration used (concatenated; scaf_off
+                                       rows = nAirV, nAirF, nBnd, nFixed)
+    gradw0                             augmented gradient of iteration 0
 
 Usage (needs the reference source tree; not part of the test run):
     make -C oracle/ref && python tests/golden/make_golden.py
@@ -34,15 +39,20 @@ from optcuts_gb300 import meshes  # noqa: E402
 
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
-# case -> (mesh generator key, lambda, Newton iterations, max Hessian triangles, dump UV per iteration)
+# case -> (mesh generator key, lambda, Newton iterations, max Hessian triangles, dump UV per iteration,
+#          extra driver flags)
 CASES = {
-    "triangle": ("triangle", 0.999, 20, None, True),
-    "plane": ("plane", 0.999, 20, None, True),
-    "cube": ("cube", 0.999, 40, None, True),
-    "icosphere_320": ("icosphere_320", 0.999, 40, None, True),
-    "ellipsoid_2k": ("ellipsoid_2k", 0.999, 300, None, False),
-    "torus_768": ("torus_768", 0.999, 30, None, False),
-    "icosphere_5k": ("icosphere_5k", 0.999, 120, 512, False),
+    "triangle": ("triangle", 0.999, 20, None, True, ["scafdump"]),
+    "plane": ("plane", 0.999, 20, None, True, ["scafdump"]),
+    "cube": ("cube", 0.999, 40, None, True, []),
+    "icosphere_320": ("icosphere_320", 0.999, 40, None, True, []),
+    "ellipsoid_2k": ("ellipsoid_2k", 0.999, 300, None, False, []),
+    "torus_768": ("torus_768", 0.999, 30, None, False, ["scafdump"]),
+    "icosphere_5k": ("icosphere_5k", 0.999, 120, 512, False, []),
+    # scaffold on: an open bumpy sheet (disk, 156 boundary vertices) and a
+    # closed sphere after its one-point cut with the scaffold forced on
+    "sheet_3k": ("sheet_3k", 0.999, 40, 256, True, ["scafdump"]),
+    "icosphere_320_scaf": ("icosphere_320", 0.999, 40, None, True, ["scaf", "scafdump"]),
 }
 
 
@@ -63,14 +73,14 @@ def per_tri_blocks(F, fixed, Hv, ntri):
     return out
 
 
-def run_case(name, key, lam, iters, hmax, states):
+def run_case(name, key, lam, iters, hmax, states, flags):
     V, F = meshes.CONFIGS[key]()
     with tempfile.TemporaryDirectory() as td:
         obj = os.path.join(td, "mesh.obj")
         meshes.write_obj(obj, V, F)
         out = os.path.join(td, "out") + "/"
         os.makedirs(out)
-        args = [DRIVER, obj, out, repr(lam), str(iters), "hess"] + (["states"] if states else [])
+        args = [DRIVER, obj, out, repr(lam), str(iters), "hess"] + (["states"] if states else []) + flags
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
                        env=dict(os.environ, OC_REF_THREADS="1"))
         ld = lambda n: np.load(out + n + ".npy")  # noqa: E731
@@ -84,6 +94,10 @@ def run_case(name, key, lam, iters, hmax, states):
                     mesh_V=V, mesh_F=F)
         if states:
             pack["UV_iters"] = ld("UV_iters")
+        pack["trace_Etot"] = ld("trace_Etot")
+        if "scafdump" in flags and os.path.exists(out + "scaf_off.npy"):
+            for k in ("scaf_V", "scaf_F", "scaf_bnd", "scaf_fixed", "scaf_off", "gradw0"):
+                pack[k] = ld(k)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack)
     return pack
 
@@ -91,8 +105,11 @@ def run_case(name, key, lam, iters, hmax, states):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle/ref")
-    for name, (key, lam, iters, hmax, states) in CASES.items():
-        p = run_case(name, key, lam, iters, hmax, states)
+    only = set(sys.argv[1:])
+    for name, (key, lam, iters, hmax, states, flags) in CASES.items():
+        if only and name not in only:
+            continue
+        p = run_case(name, key, lam, iters, hmax, states, flags)
         print("%-14s nV=%6d nF=%6d iters=%d E0=%.6g Elast=%.6g" % (
             name, len(p["UV0"]), len(p["F"]), len(p["trace_E"]) - 1, p["trace_E"][0], p["trace_E"][-1]))
 

@@ -1,0 +1,112 @@
+"""The Optimizer's scaffolding branches on the GPU, fed the air meshes the
+reference's own Scaffold built (Triangle, every iteration) and compared with
+the reference's run on the same air meshes (tests/golden)."""
+import numpy as np
+import pytest
+
+import optcuts_gb300 as oc
+from conftest import SCAFFOLD_DUMPS, golden_scaffolds
+
+pytestmark = pytest.mark.gpu
+
+
+def scaffold(g, k):
+    airV, airF, bnd, _ = golden_scaffolds(g)[k]
+    return oc.Scaffold(airV, airF, bnd)
+
+
+def start(g, **cfg):
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    par = 1.0 - g["scalars"][4]
+    opt = oc.Optimizer(m, [par], **cfg)
+    opt.setScaffold(scaffold(g, 0))
+    opt.precompute()
+    return m, opt
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_DUMPS)
+def test_initial_energy_and_gradient(golden, case):
+    g = golden(case)
+    m, opt = start(g)
+    assert opt.getLastEnergyVal() == pytest.approx(g["trace_Etot"][0], rel=1e-14)
+    assert opt.getLastEnergyVal(excludeScaffold=True) == pytest.approx(g["trace_E"][0], rel=1e-13)
+    opt.solve(1)
+    grad, d = opt.lastVectors()
+    assert opt.systemSize() * 2 == len(g["gradw0"])
+    np.testing.assert_array_equal(grad, g["gradw0"])      # same operations, same order
+    rel = np.linalg.norm(d - g["dir0"]) / np.linalg.norm(g["dir0"])
+    assert rel < 5e-3, rel
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_DUMPS)
+def test_trajectory_with_reference_air_meshes(golden, case):
+    g = golden(case)
+    m, opt = start(g)
+    E, Et = [opt.getLastEnergyVal(True)], [opt.getLastEnergyVal()]
+    scafs = golden_scaffolds(g)
+    status = 0
+    for k in range(len(scafs)):
+        if k > 0:
+            opt.setScaffold(scaffold(g, k))
+        status = opt.solve(1)
+        E.append(opt.getLastEnergyVal(True))
+        Et.append(opt.getLastEnergyVal())
+        assert m.checkInversion()
+        if status == 1:
+            break
+    E, Et = np.array(E), np.array(Et)
+    n = min(len(E), len(g["trace_E"]))
+    rel = np.abs(E[:n] - g["trace_E"][:n]) / g["trace_E"][:n]
+    assert rel.max() < 2e-2, rel
+    assert abs(E[-1] - g["trace_E"][-1]) / g["trace_E"][-1] < 1e-4
+    nt = min(len(Et), len(g["trace_Etot"]))
+    assert np.abs(Et[:nt] - g["trace_Etot"][:nt]).max() / g["trace_Etot"][0] < 2e-2
+
+
+def test_scaffold_moves_with_the_step(golden):
+    """Without a new air mesh the old one is stepped along (Scaffold::stepForward)."""
+    g = golden("sheet_3k")
+    m, opt = start(g)
+    sc = scaffold(g, 0)
+    opt.solve(1)
+    Vair = opt.scaffoldV()
+    nb = len(sc.bnd)
+    np.testing.assert_array_equal(Vair[:nb], m.V[sc.bnd])
+    _, d = opt.lastVectors()
+    step = opt.last_step()["stepSize"]
+    nV = len(g["UV0"])
+    want = sc.airV[nb:] + step * d[2 * nV:].reshape(-1, 2)
+    np.testing.assert_array_equal(Vair[nb:], want)
+    # a second solve without setScaffold runs on the moved air mesh
+    e0 = opt.getLastEnergyVal()
+    opt.solve(1)
+    assert opt.getLastEnergyVal() <= e0
+
+
+def test_clear_scaffold_returns_to_mesh_system(golden):
+    g = golden("sheet_3k")
+    m, opt = start(g)
+    nV = len(g["UV0"])
+    assert opt.systemSize() > nV
+    opt.solve(1)
+    opt.clearScaffold()
+    assert opt.systemSize() == nV
+    opt.solve(1)
+    grad, _ = opt.lastVectors()
+    assert len(grad) == 2 * nV
+    assert m.checkInversion()
+
+
+def test_bad_scaffold_rejected(golden):
+    g = golden("sheet_3k")
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    opt = oc.Optimizer(m, [0.001])
+    airV, airF, bnd, _ = golden_scaffolds(g)[0]
+    bad = airF.copy()
+    bad[0, 0] = len(airV)
+    with pytest.raises(oc.OCError):
+        opt.setScaffold(oc.Scaffold(airV, bad, bnd))
+    bnd2 = bnd.copy()
+    bnd2[1] = bnd2[0]
+    with pytest.raises(oc.OCError):
+        opt.setScaffold(oc.Scaffold(airV, airF, bnd2))

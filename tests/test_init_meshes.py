@@ -7,7 +7,8 @@ from optcuts_gb300 import init as I
 from optcuts_gb300 import meshes as M
 
 
-@pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle"])
+@pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle",
+                                  "sheet_3k"])
 def test_init_matches_reference(golden, case):
     g = golden(case)
     st = I.init_uv(g["mesh_V"], g["mesh_F"])
@@ -58,7 +59,8 @@ def test_obj_roundtrip(tmp_path):
         M.read_obj(str(tmp_path / "t.obj"))
 
 
-@pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle"])
+@pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle",
+                                  "sheet_3k"])
 def test_cohesive_edges_and_seam_term_match_reference(golden, case):
     g = golden(case)
     st = I.init_uv(g["mesh_V"], g["mesh_F"])
