@@ -218,10 +218,19 @@ int oc_optimizer_solver_stats(oc_optimizer* opt, double* out8);
  * when the air connectivity differs from the previous call's. */
 int oc_optimizer_set_scaffold(oc_optimizer* opt, const double* airV, int nAirV, const int* airF, int nAirF,
                               const int* bnd, int nBnd, double areaThres);
+/* `scaffold = Scaffold(result)` done here: the air mesh of the mesh's
+ * current UV from the project's own generator (oc_air_mesh_build, 20 degree
+ * refinement), then oc_optimizer_set_scaffold with the whole-mesh
+ * areaThres_AM. */
+int oc_optimizer_rebuild_scaffold(oc_optimizer* opt);
 /* Optimizer::setScaffolding(false) (Optimizer.cpp:307-317) */
 int oc_optimizer_clear_scaffold(oc_optimizer* opt);
-/* current air-mesh UV (nAirV x 2): Scaffold::airMesh.V after the last step */
-int oc_optimizer_get_scaffold_uv(oc_optimizer* opt, double* airV);
+/* The current scaffold (Optimizer::getScaffold, Optimizer.cpp:118-124):
+ * sizes, and into non-NULL arrays airMesh.V as the last step moved it
+ * (nAirV x 2), airMesh.F (nAirF x 3) and bnd (nBnd).  OC_ERR_INVALID
+ * without a scaffold. */
+int oc_optimizer_get_scaffold(oc_optimizer* opt, int* nAirV, int* nAirF, int* nBnd, double* airV, int* airF,
+                              int* bnd);
 /* energyVal_scaffold of the last evaluation; getLastEnergyVal(true) is
  * oc_optimizer_get_last_energy minus this (Optimizer.cpp:845-850) */
 int oc_optimizer_get_last_energy_scaffold(oc_optimizer* opt, double* scaffoldEnergy);
@@ -230,6 +239,24 @@ int oc_optimizer_system_size(oc_optimizer* opt, int* nVerts);
 /* gradient and searchDir of the last iteration (2 x system size each,
  * interleaved u, v; either may be NULL) */
 int oc_optimizer_last_vectors(oc_optimizer* opt, double* gradient, double* searchDir);
+
+/* ---- Air mesh without Triangle (replaces Scaffold.cpp:27-205) -----------
+ * Host-only.  For a UV layout (UV nV x 2, F nF x 3) and the mesh's rest
+ * avgEdgeLen: the boundary loops (each started at its smallest vertex), the
+ * reference's segmented bounding box (margin 4 avgEdgeLen, segments about
+ * 9 avgEdgeLen) and a constrained Delaunay triangulation of the region
+ * between them, every mesh component's interior removed; with
+ * minAngleDeg > 0 the air region is refined towards that minimum angle
+ * (Triangle's "q" uses 20) by interior Steiner points, never on a segment
+ * (as "Y").  Rows of airV: the nBnd boundary vertices (loop by loop), the
+ * box points, then the Steiner points.  OC_ERR_INVALID if the boundary
+ * self-touches or no boundary exists. */
+typedef struct oc_air_mesh oc_air_mesh;
+int oc_air_mesh_build(const double* UV, int nV, const int* F, int nF, double avgEdgeLen, double minAngleDeg,
+                      oc_air_mesh** out);
+int oc_air_mesh_sizes(const oc_air_mesh* am, int* nAirV, int* nAirF, int* nBnd);
+int oc_air_mesh_get(const oc_air_mesh* am, double* airV, int* airF, int* bnd);
+int oc_air_mesh_destroy(oc_air_mesh* am);
 
 #ifdef __cplusplus
 }

@@ -93,7 +93,12 @@ _SIGS = {
     "oc_optimizer_solver_stats": [_vp, _d],
     "oc_optimizer_set_scaffold": [_vp, _d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double],
     "oc_optimizer_clear_scaffold": [_vp],
-    "oc_optimizer_get_scaffold_uv": [_vp, _d],
+    "oc_optimizer_rebuild_scaffold": [_vp],
+    "oc_air_mesh_build": [_d, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_vp)],
+    "oc_air_mesh_sizes": [_vp, _i, _i, _i],
+    "oc_air_mesh_get": [_vp, _d, _i, _i],
+    "oc_air_mesh_destroy": [_vp],
+    "oc_optimizer_get_scaffold": [_vp, _i, _i, _i, _d, _i, _i],
     "oc_optimizer_get_last_energy_scaffold": [_vp, _d],
     "oc_optimizer_system_size": [_vp, _i],
     "oc_optimizer_last_vectors": [_vp, _d, _d],
@@ -380,6 +385,28 @@ class Scaffold:
         self.airF = np.ascontiguousarray(airF, np.int32).reshape(-1, 3)
         self.bnd = np.ascontiguousarray(bnd, np.int32).ravel()
 
+    @classmethod
+    def build(cls, UV, F, avgEdgeLen, minAngle=20.0):
+        """The project's own air mesh for a UV layout (constrained Delaunay
+        between the boundary loops and the reference's segmented box, refined
+        towards minAngle degrees; no Triangle).  Host only."""
+        UV, F = _f8(UV), _i4(F)
+        h = _vp()
+        rc = lib().oc_air_mesh_build(_pd(UV), len(UV), _pi(F), len(F), float(avgEdgeLen), float(minAngle),
+                                     ctypes.byref(h))
+        if rc != OC_OK:
+            raise OCError(rc, "air mesh: " + lib().oc_status_string(rc).decode())
+        try:
+            nv, nf, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            lib().oc_air_mesh_sizes(h, ctypes.byref(nv), ctypes.byref(nf), ctypes.byref(nb))
+            V = np.zeros((nv.value, 2))
+            Fa = np.zeros((nf.value, 3), np.int32)
+            b = np.zeros(nb.value, np.int32)
+            lib().oc_air_mesh_get(h, _pd(V), _pi(Fa), _pi(b))
+        finally:
+            lib().oc_air_mesh_destroy(h)
+        return cls(V, Fa, b)
+
     def localVI2Global(self, nV):
         nb = len(self.bnd)
         return np.concatenate([self.bnd, nV + np.arange(len(self.airV) - nb, dtype=np.int32)])
@@ -421,20 +448,34 @@ class Optimizer:
     def setScaffold(self, scaffold, areaThres=-1.0):
         """Installs the air mesh for the next solve() (the reference rebuilds it
         after every iteration, Optimizer.cpp:251-257)."""
-        self.scaffold = scaffold
         self.ctx.check(lib().oc_optimizer_set_scaffold(
             self.h, _pd(scaffold.airV), len(scaffold.airV), _pi(scaffold.airF), len(scaffold.airF),
             _pi(scaffold.bnd), len(scaffold.bnd), float(areaThres)), "setScaffold")
 
+    def rebuildScaffold(self):
+        """Scaffold(result) for the current UV with the project's air-mesh
+        generator (what the reference does after every iteration)."""
+        self.ctx.check(lib().oc_optimizer_rebuild_scaffold(self.h), "rebuildScaffold")
+        return self.getScaffold()
+
+    def getScaffold(self):
+        """The current air mesh (airMesh.V as the last step moved it)."""
+        nv, nf, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_get_scaffold(self.h, ctypes.byref(nv), ctypes.byref(nf), ctypes.byref(nb),
+                                                       None, None, None), "getScaffold")
+        V = np.zeros((nv.value, 2))
+        F = np.zeros((nf.value, 3), np.int32)
+        b = np.zeros(nb.value, np.int32)
+        self.ctx.check(lib().oc_optimizer_get_scaffold(self.h, None, None, None, _pd(V), _pi(F), _pi(b)),
+                       "getScaffold")
+        return Scaffold(V, F, b)
+
     def clearScaffold(self):
-        self.scaffold = None
         self.ctx.check(lib().oc_optimizer_clear_scaffold(self.h), "clearScaffold")
 
     def scaffoldV(self):
         """Current air-mesh UV (Scaffold::airMesh.V after the last step)."""
-        out = np.zeros_like(self.scaffold.airV)
-        self.ctx.check(lib().oc_optimizer_get_scaffold_uv(self.h, _pd(out)), "scaffoldV")
-        return out
+        return self.getScaffold().airV
 
     def systemSize(self):
         n = ctypes.c_int()

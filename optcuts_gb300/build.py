@@ -30,8 +30,9 @@ UNITS = {
     "oc_kernels.cu": [],
     "oc_chol.cu": [],
     "oc_api.cu": ["-Xcompiler", "-fvisibility=default"],
+    "oc_airmesh.cpp": [],
 }
-HEADERS = ["oc_internal.h", "oc_chol.h"]
+HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h"]
 
 
 def _newest_input():
@@ -42,7 +43,7 @@ def _newest_input():
 
 
 def _compile(unit, extra, verbose):
-    obj = os.path.join(OUT_DIR, unit.replace(".cu", ".o"))
+    obj = os.path.join(OUT_DIR, os.path.splitext(unit)[0] + ".o")
     cmd = [NVCC, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

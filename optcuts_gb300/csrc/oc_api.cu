@@ -4,6 +4,7 @@
 // EigenLibSolver, Optimizer).  No exception crosses the ABI; every entry
 // point returns an oc_status.
 
+#include "oc_airmesh.h"
 #include "oc_chol.h"
 #include "oc_internal.h"
 
@@ -77,6 +78,7 @@ struct oc_optimizer {
     double2* airCorner = nullptr;   // 3 x capAirF
     double* airHb = nullptr;        // 21 x capAirF
     std::vector<int> airFw, bnd;    // air triangles in augmented ids; boundary map
+    std::vector<int> airF;          // air triangles in air-mesh ids
 };
 
 namespace {
@@ -1306,6 +1308,7 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
                                      cudaMemcpyHostToDevice, st));
     OC_CUDA(ctx, cudaStreamSynchronize(st));
     o->airFw.swap(Fw);
+    o->airF.assign(airF, airF + 3 * (size_t)nAirF);
     o->bnd.assign(bnd, bnd + nBnd);
     o->nWhole = nWhole;
     o->nAirV = nAirV;
@@ -1314,6 +1317,22 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     o->scaf = true;
     if (!samePattern) o->patternStale = true;
     return OC_OK;
+}
+
+int oc_optimizer_rebuild_scaffold(oc_optimizer* o)
+{
+    if (!o) return OC_ERR_INVALID;
+    oc_mesh* m = o->mesh;
+    std::vector<double> uv(2 * (size_t)m->d.nV);
+    OC_CUDA(m->ctx, cudaMemcpyAsync(uv.data(), m->d.uv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToHost,
+                                    m->ctx->stream));
+    OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+    oc::AirMesh am;
+    std::string err;
+    const int rc = oc::air_mesh_build(uv.data(), m->d.nV, m->F.data(), m->d.nF, m->scalars[1], am, &err);
+    if (rc) return fail(m->ctx, rc, err);
+    return oc_optimizer_set_scaffold(o, am.V.data(), static_cast<int>(am.V.size() / 2), am.F.data(),
+                                     static_cast<int>(am.F.size() / 3), am.bnd.data(), am.nBnd, -1.0);
 }
 
 int oc_optimizer_clear_scaffold(oc_optimizer* o)
@@ -1326,17 +1345,25 @@ int oc_optimizer_clear_scaffold(oc_optimizer* o)
     return OC_OK;
 }
 
-int oc_optimizer_get_scaffold_uv(oc_optimizer* o, double* airV)
+int oc_optimizer_get_scaffold(oc_optimizer* o, int* nAirV, int* nAirF, int* nBnd, double* airV, int* airF, int* bnd)
 {
-    if (!o || !airV || !o->scaf) return OC_ERR_INVALID;
+    if (!o || !o->scaf) return OC_ERR_INVALID;
     oc_mesh* m = o->mesh;
-    std::vector<double> w(2 * (size_t)o->nWhole);
-    OC_CUDA(m->ctx, cudaMemcpyAsync(w.data(), o->wuv, sizeof(double2) * o->nWhole, cudaMemcpyDeviceToHost, m->ctx->stream));
-    OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
-    for (int i = 0; i < o->nAirV; ++i) {
-        const int v = i < o->nBnd ? o->bnd[i] : m->d.nV + i - o->nBnd;
-        airV[2 * (size_t)i] = w[2 * (size_t)v];
-        airV[2 * (size_t)i + 1] = w[2 * (size_t)v + 1];
+    if (nAirV) *nAirV = o->nAirV;
+    if (nAirF) *nAirF = static_cast<int>(o->airF.size() / 3);
+    if (nBnd) *nBnd = o->nBnd;
+    if (airF) std::copy(o->airF.begin(), o->airF.end(), airF);
+    if (bnd) std::copy(o->bnd.begin(), o->bnd.end(), bnd);
+    if (airV) {
+        std::vector<double> w(2 * (size_t)o->nWhole);
+        OC_CUDA(m->ctx, cudaMemcpyAsync(w.data(), o->wuv, sizeof(double2) * o->nWhole, cudaMemcpyDeviceToHost,
+                                        m->ctx->stream));
+        OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+        for (int i = 0; i < o->nAirV; ++i) {
+            const int v = i < o->nBnd ? o->bnd[i] : m->d.nV + i - o->nBnd;
+            airV[2 * (size_t)i] = w[2 * (size_t)v];
+            airV[2 * (size_t)i + 1] = w[2 * (size_t)v + 1];
+        }
     }
     return OC_OK;
 }

@@ -110,3 +110,29 @@ def test_bad_scaffold_rejected(golden):
     bnd2[1] = bnd2[0]
     with pytest.raises(oc.OCError):
         opt.setScaffold(oc.Scaffold(airV, airF, bnd2))
+
+
+@pytest.mark.parametrize("case,tol", [("sheet_3k", 1e-4), ("torus_768", 1e-3), ("icosphere_320_scaf", 1e-4)])
+def test_own_air_meshes_reach_reference_energy(golden, case, tol):
+    """The reference's loop with the project's air meshes: rebuild the
+    scaffold from the current UV after every iteration (Optimizer.cpp:251-257)."""
+    g = golden(case)
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    par = 1.0 - g["scalars"][4]
+    opt = oc.Optimizer(m, [par])
+    opt.rebuildScaffold()
+    opt.precompute()
+    E = [opt.getLastEnergyVal(True)]
+    status = 0
+    for _ in range(200):
+        status = opt.solve(1)
+        E.append(opt.getLastEnergyVal(True))
+        assert m.checkInversion()
+        if status == 1:
+            break
+        opt.rebuildScaffold()
+    assert status == 1
+    assert abs(E[-1] - g["trace_E"][-1]) / g["trace_E"][-1] < tol
+    # the air mesh the last rebuild made still covers box minus mesh
+    sc = opt.getScaffold()
+    assert set(sc.bnd.tolist()) == set(golden_scaffolds(g)[0][2].tolist())
