@@ -3,10 +3,13 @@
 
 Workload (default): the lat-long ellipsoid, axes (1, 0.6, 0.4), 316 x 316
 grid with 8 random spherical-harmonic bumps (199,080 triangles, seed 2),
-one-point cut + Tutte embedding, lambda = 0.999, scaffold off (the reference
-runs its first Newton phase of a closed genus-0 mesh without the scaffold).
-A step is one Optimizer::solve(1): gradient, PSD-projected Hessian, block
-assembly, PCG direction, injective bound and line search.
+one-point cut + Tutte embedding, lambda = 0.999, bijectivity scaffold on.
+A step is what the reference's Optimizer::solve(1) does with the scaffold
+on: one Newton iteration (gradient, PSD-projected Hessian, block assembly,
+multifrontal LDL^T factorisation and solve, injective bound, line search)
+over mesh + air mesh, then the scaffold rebuilt for the new UV
+(Optimizer.cpp:251-257; here the project's own air-mesh generator).
+--scaffold off times the scaffold-free Newton phase instead.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -48,6 +51,7 @@ def parse():
     p.add_argument("--cpu-sample-iters", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--scaffold", default="on", choices=["on", "off"])
     return p.parse_args()
 
 
@@ -138,9 +142,24 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def cpu_port_time(st, lam, iters, threads):
+def avg_edge_len(st):
+    V, F = st.V_rest, st.F
+    return float(np.mean(np.linalg.norm(V[F[:, [1, 2, 0]]] - V[F], axis=2)))
+
+
+def air_mesh(st):
+    """Input air mesh for the CPU arm: the scaffold of the start UV."""
+    import optcuts_gb300 as oc
+    sc = oc.Scaffold.build(st.UV, st.F, avg_edge_len(st))
+    return sc.airV, sc.airF, sc.bnd
+
+
+def cpu_port_time(st, lam, iters, threads, scaffold):
     import oracle as O
-    _, tr, _ = O.newton(st.V_rest, st.F, st.fixedVert, st.UV, 1.0 - lam, iters, threads=threads)
+    kw = {}
+    if scaffold:
+        kw = dict(scaffold=air_mesh(st), avg_edge_len=avg_edge_len(st))
+    _, tr, _ = O.newton(st.V_rest, st.F, st.fixedVert, st.UV, 1.0 - lam, iters, threads=threads, **kw)
     return float(np.sum(tr["seconds"])), len(tr["seconds"])
 
 
@@ -149,23 +168,23 @@ def run_reference(args, rank, world):
         return
     st = workload(args.workload)
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup if args.warmup < 1 else 0):
-        pass
+    scaf = args.scaffold == "on"
     secs, n = 0.0, 0
     per = []
     for _ in range(args.steps):
-        s, k = cpu_port_time(st, args.lam, args.cpu_sample_iters, threads)
+        s, k = cpu_port_time(st, args.lam, args.cpu_sample_iters, threads, scaf)
         secs += s
         n += k
         per.append(s / max(k, 1))
     v = n / secs
-    sample = "%d x %d Newton iteration(s) of %s from the Tutte start" % (args.steps, args.cpu_sample_iters,
-                                                                          args.workload)
+    sample = "%d x %d Newton iteration(s) of %s from the Tutte start%s" % (
+        args.steps, args.cpu_sample_iters, args.workload,
+        ", scaffold of the start UV moved with each step" if scaf else "")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * secs / n, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "triangles": len(st.F), "lambda": args.lam, "scaffold": False},
+        "config": {"workload": args.workload, "triangles": len(st.F), "lambda": args.lam, "scaffold": scaf},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -178,10 +197,21 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(device)
     st = workload(args.workload)
     nF, nV = len(st.F), len(st.UV)
-    ctx = oc.Context(device)
+    scaf = args.scaffold == "on"
+    # one stream for the library, the L2 flush and the timing events
+    stream = torch.cuda.Stream(device)
+    torch.cuda.set_stream(stream)
+    ctx = oc.Context(device, stream=stream.cuda_stream)
     mesh = oc.TriMesh(st.V_rest, st.UV, st.F, st.fixedVert, ctx=ctx)
     opt = oc.Optimizer(mesh, [1.0 - args.lam], timing=1)
+    if scaf:
+        opt.rebuildScaffold()
     opt.precompute()
+
+    def step():
+        opt.solve(1)
+        if scaf:
+            opt.rebuildScaffold()   # Optimizer.cpp:251-257
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
 
     def flush_l2():
@@ -190,7 +220,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
-        opt.solve(1)
+        step()
     opt.phase_ms()
     launches0 = opt.launch_count()
     flush_l2()
@@ -199,11 +229,13 @@ def run_ours(args, rank, world):
     sampler = ClockSampler(device) if rank == 0 else None
     step_ms, phases = [], []
     for _ in range(args.steps):
-        opt.solve(1)
-        ctx.synchronize()
-        ph = opt.phase_ms()
-        step_ms.append(sum(ph.values()))
-        phases.append(ph)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        phases.append(opt.phase_ms())
         flush_l2()
     torch.cuda.synchronize()
     barrier(world)
@@ -222,7 +254,7 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             mesh.V = uv_host
-            opt.solve(1)
+            step()
             uv_host = mesh.V
         t1 = time.perf_counter()
         e2e_max = allreduce_max(t1 - t0, world)
@@ -245,15 +277,17 @@ def run_ours(args, rank, world):
     cpu = None
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        secs, n = cpu_port_time(st, args.lam, args.cpu_sample_iters, threads)
+        secs, n = cpu_port_time(st, args.lam, args.cpu_sample_iters, threads, scaf)
         cpu = {"value": n / secs, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "%d Newton iteration(s) of %s from the Tutte start" % (n, args.workload)}
+               "sample": "%d Newton iteration(s) of %s from the Tutte start%s" % (
+                   n, args.workload, ", scaffold of the start UV moved with each step" if scaf else "")}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, "triangles": nF, "vertices": nV, "lambda": args.lam,
-                   "scaffold": False, "parallelism": "replicas" if world > 1 else "single",
+                   "scaffold": scaf, "system_vertices": opt.systemSize(),
+                   "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed between timed steps (256 MB write)", "solver": "multifrontal Cholesky (FP64)",
                    "precision": "fp64 throughout (energy, gradient, Hessian eigen-clamp, LDL^T)"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,

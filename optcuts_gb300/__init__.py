@@ -144,11 +144,12 @@ def _i4(a):
 
 
 class Context:
-    """One GPU and one CUDA stream."""
+    """One GPU and one CUDA stream (the caller's cudaStream_t handle as an
+    int, e.g. torch.cuda.current_stream().cuda_stream, or a new stream)."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, stream=None):
         h = _vp()
-        rc = lib().oc_ctx_create(device, None, ctypes.byref(h))
+        rc = lib().oc_ctx_create(device, _vp(stream) if stream else None, ctypes.byref(h))
         if rc != OC_OK:
             raise OCError(rc, "oc_ctx_create failed (no usable GPU?)")
         self.h = h

@@ -47,6 +47,12 @@ _d = ctypes.POINTER(ctypes.c_double)
 _i = ctypes.POINTER(ctypes.c_int)
 
 
+class ScaffoldArgs(ctypes.Structure):
+    _fields_ = [("airV", ctypes.POINTER(ctypes.c_double)), ("nAirV", ctypes.c_int),
+                ("airF", ctypes.POINTER(ctypes.c_int)), ("nAirF", ctypes.c_int),
+                ("bnd", ctypes.POINTER(ctypes.c_int)), ("nBnd", ctypes.c_int), ("areaThres", ctypes.c_double)]
+
+
 class NewtonOpts(ctypes.Structure):
     _fields_ = [("energyParam", ctypes.c_double), ("relGL2Tol", ctypes.c_double),
                 ("maxIter", ctypes.c_int), ("nThreads", ctypes.c_int)]
@@ -72,6 +78,8 @@ def lib():
         L.ocr_solver_nnz_L.restype = ctypes.c_longlong
         L.ocr_newton.argtypes = [_d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, _d,
                                  ctypes.POINTER(NewtonOpts), _d, _d, _d, _d, _i]
+        L.ocr_newton_scaffold.argtypes = [_d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, _d,
+                                          ctypes.POINTER(NewtonOpts), ctypes.POINTER(ScaffoldArgs), _d, _d, _d, _d, _i]
         _lib = L
     return _lib
 
@@ -164,8 +172,11 @@ class Solver:
             self._h = None
 
 
-def newton(V_rest, F, fixed, UV, energy_param, iters, rel_gl2_tol=1e-12, threads=1):
-    """Projected-Newton loop, scaffold off; returns (UV, traces dict, status)."""
+def newton(V_rest, F, fixed, UV, energy_param, iters, rel_gl2_tol=1e-12, threads=1, scaffold=None,
+           area_thres=None, avg_edge_len=None):
+    """Projected-Newton loop; returns (UV, traces dict, status).  scaffold =
+    (airV, airF, bnd) runs the scaffolding branches with that air mesh moved
+    along each step (areaThres_AM from avg_edge_len unless area_thres)."""
     V_rest, F, fixed = _f8(V_rest), _i4(F), _i4(fixed)
     UV = np.array(UV, np.float64, copy=True, order="C")
     o = NewtonOpts(energy_param, rel_gl2_tol, iters, threads)
@@ -174,8 +185,16 @@ def newton(V_rest, F, fixed, UV, energy_param, iters, rel_gl2_tol=1e-12, threads
     tA = np.zeros(iters)
     tS = np.zeros(iters)
     st = np.zeros(1, np.int32)
-    n = lib().ocr_newton(_pd(V_rest), len(V_rest), _pi(F), len(F), _pi(fixed), len(fixed), _pd(UV),
-                         ctypes.byref(o), _pd(tE), _pd(tG), _pd(tA), _pd(tS), _pi(st))
+    if scaffold is not None:
+        aV, aF, bnd = _f8(scaffold[0]), _i4(scaffold[1]), _i4(scaffold[2])
+        if area_thres is None:
+            area_thres = np.sqrt(3.0) / 4.0 * (0.5 * avg_edge_len) ** 2
+        sa = ScaffoldArgs(_pd(aV), len(aV), _pi(aF), len(aF), _pi(bnd), len(bnd), float(area_thres))
+        n = lib().ocr_newton_scaffold(_pd(V_rest), len(V_rest), _pi(F), len(F), _pi(fixed), len(fixed), _pd(UV),
+                                      ctypes.byref(o), ctypes.byref(sa), _pd(tE), _pd(tG), _pd(tA), _pd(tS), _pi(st))
+    else:
+        n = lib().ocr_newton(_pd(V_rest), len(V_rest), _pi(F), len(F), _pi(fixed), len(fixed), _pd(UV),
+                             ctypes.byref(o), _pd(tE), _pd(tG), _pd(tA), _pd(tS), _pi(st))
     if n < 0:
         raise ArithmeticError("factorization failed")
     return UV, {"E": tE[:n + 1], "gsq": tG[:n], "alpha": tA[:n], "seconds": tS[:n]}, int(st[0])

@@ -630,29 +630,124 @@ void ocr_solver_solve(ocr_solver* s, const double* rhs, double* x)
     for (int k = 0; k < n; ++k) x[2 * S.order[k >> 1] + (k & 1)] = z[k];
 }
 
-int ocr_newton(const double* Vr, int nV, const int* F, int nF, const int* fixedVert, int nFixed,
-               double* UV, const ocr_newton_opts* o, double* traceE, double* traceGsq,
-               double* traceAlpha, double* traceSeconds, int* status)
+// solver_factorize for an augmented system: blocks of triangles t < nF
+// scaled by param, the rest (air triangles) by airScale; fixed rows get
+// param (+ airScale when airFixed marks them) times identity.
+static int solver_factorize_scaf(Solver& S, const double* blocks, int nF, int nFa, double param, double airScale,
+                                 const std::vector<char>& airFixed)
+{
+    std::fill(S.blk.begin(), S.blk.end(), 0.0);
+    for (int t = 0; t < nF + nFa; ++t) {
+        const double* H = blocks + 36 * (size_t)t;
+        const double sc = t < nF ? param : airScale;
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const int slot = S.triSlot[9 * (size_t)t + 3 * a + b];
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) S.blk[4 * slot + 2 * i + j] += sc * H[6 * (2 * a + i) + 2 * b + j];
+            }
+    }
+    for (int v = 0; v < S.nV; ++v) {
+        if (!S.isFixed[v]) continue;
+        const double d = airFixed[v] ? param + airScale : param;   // Scaffold.cpp:193-199 + Optimizer.cpp:839
+        for (int p = S.vptr[v]; p < S.vptr[v + 1]; ++p) {
+            double* B = &S.blk[4 * p];
+            if (S.vadj[p] == v) { B[0] = d; B[1] = 0; B[2] = 0; B[3] = d; }
+        }
+    }
+    return numeric(S);
+}
+
+static int newton_impl(const double* Vr, int nV, const int* F, int nF, const int* fixedVert, int nFixed, double* UV,
+                       const ocr_newton_opts* o, const ocr_scaffold* sc, double* traceE, double* traceGsq,
+                       double* traceAlpha, double* traceSeconds, int* status)
 {
     using clk = std::chrono::steady_clock;
     std::vector<double> rest(8 * (size_t)nF);
-    double sc[3];
-    ocr_rest_constants(Vr, nV, F, nF, 0.0, rest.data(), sc);
+    double scal[3];
+    ocr_rest_constants(Vr, nV, F, nF, 0.0, rest.data(), scal);
     const double par = o->energyParam;
-    // Optimizer::precompute (Optimizer.cpp:154-201), scaffold off
-    ocr_solver* solver = ocr_solver_create(nV, F, nF, fixedVert, nFixed, Vr);
+    // scaffold: air mesh in the augmented numbering (Scaffold.cpp:179-199)
+    const int nBnd = sc ? sc->nBnd : 0, nFa = sc ? sc->nAirF : 0;
+    const int nW = sc ? nV + sc->nAirV - nBnd : nV;
+    std::vector<int> Fw(F, F + 3 * (size_t)nF);
+    std::vector<double> restA, Vw(3 * (size_t)nW, 0.0), W(2 * (size_t)nW);
+    std::vector<int> airFixedList;
+    std::vector<char> airFixed(nW, 0);
+    std::copy(Vr, Vr + 3 * (size_t)nV, Vw.begin());
+    std::copy(UV, UV + 2 * (size_t)nV, W.begin());
+    double airScale = 0.0;
+    if (sc) {
+        auto whole = [&](int a) { return a < nBnd ? sc->bnd[a] : nV + a - nBnd; };
+        std::vector<double> V3(3 * (size_t)sc->nAirV, 0.0);
+        for (int i = 0; i < sc->nAirV; ++i) {
+            V3[3 * i] = sc->airV[2 * i];
+            V3[3 * i + 1] = sc->airV[2 * i + 1];
+        }
+        restA.resize(8 * (size_t)nFa);
+        double sa[3];
+        ocr_rest_constants(V3.data(), sc->nAirV, sc->airF, nFa, sc->areaThres, restA.data(), sa);
+        for (int k = 0; k < 3 * nFa; ++k) Fw.push_back(whole(sc->airF[k]));
+        for (int i = nBnd; i < sc->nAirV; ++i) {
+            const int v = whole(i);
+            W[2 * v] = sc->airV[2 * i];
+            W[2 * v + 1] = sc->airV[2 * i + 1];
+            Vw[3 * v] = sc->airV[2 * i];
+            Vw[3 * v + 1] = sc->airV[2 * i + 1];
+        }
+        for (int i = 0; i < nFixed; ++i)
+            for (int k = 0; k < nBnd; ++k)
+                if (sc->bnd[k] == fixedVert[i]) {
+                    airFixed[fixedVert[i]] = 1;
+                    airFixedList.push_back(fixedVert[i]);
+                }
+        airScale = 0.01 * par / nFa;   // w_scaf / |F_air| (Optimizer.cpp:87, 776)
+    }
+    const int* Fa = Fw.data() + 3 * (size_t)nF;
+    auto energy = [&](const double* X, double* eScaf) {
+        double e = par * ocr_energy(rest.data(), F, nF, X, 0);
+        double es = 0.0;
+        if (sc) {
+            es = ocr_energy(restA.data(), Fa, nFa, X, 1) * airScale;
+            e += es;
+        }
+        if (eScaf) *eScaf = es;
+        return e;
+    };
+    // Optimizer::precompute (Optimizer.cpp:154-201)
+    ocr_solver* solver = ocr_solver_create(nW, Fw.data(), nF + nFa, fixedVert, nFixed, Vw.data());
     const double targetGRes = par * static_cast<double>(nV - nFixed) / nV * o->relGL2Tol;   // Optimizer.cpp:677
-    double lastE = par * ocr_energy(rest.data(), F, nF, UV, 0);
+    double lastE = energy(W.data(), nullptr);
     traceE[0] = lastE;
-    std::vector<double> g(2 * (size_t)nV), d(2 * (size_t)nV), blocks(36 * (size_t)nF), UV0(2 * (size_t)nV);
+    std::vector<double> g(2 * (size_t)nW), ga(2 * (size_t)nW), d(2 * (size_t)nW), W0(2 * (size_t)nW);
+    std::vector<double> blocks(36 * (size_t)(nF + nFa));
     int it = 0;
     *status = 0;
     for (; it < o->maxIter; ++it) {
         auto t0 = clk::now();
-        // Optimizer::solve (Optimizer.cpp:209-228)
-        ocr_gradient(rest.data(), F, nF, UV, nV, fixedVert, nFixed, 0, g.data());
+        // Optimizer::solve (Optimizer.cpp:209-228); augmentGradient (Scaffold.cpp:210-230)
+        ocr_gradient(rest.data(), F, nF, W.data(), nV, fixedVert, nFixed, 0, g.data());
+        for (int k = 0; k < 2 * nV; ++k) g[k] *= par;
+        for (int k = 2 * nV; k < 2 * nW; ++k) g[k] = 0.0;
+        if (sc) {
+            ocr_gradient(restA.data(), Fa, nFa, W.data(), nW, airFixedList.data(), (int)airFixedList.size(), 1,
+                         ga.data());
+            std::vector<char> onAir(nW, 0);
+            for (int k = 0; k < 3 * nFa; ++k) onAir[Fa[k]] = 1;
+            for (int v = 0; v < nW; ++v) {
+                if (!onAir[v]) continue;
+                if (v < nV) {
+                    g[2 * v] += airScale * ga[2 * v];
+                    g[2 * v + 1] += airScale * ga[2 * v + 1];
+                }
+                else {
+                    g[2 * v] = airScale * ga[2 * v];
+                    g[2 * v + 1] = airScale * ga[2 * v + 1];
+                }
+            }
+        }
         double gsq = 0.0;
-        for (auto& gi : g) { gi *= par; gsq += gi * gi; }
+        for (double gi : g) gsq += gi * gi;
         traceGsq[it] = gsq;
         if (gsq < targetGRes) {
             *status = 1;
@@ -663,8 +758,10 @@ int ocr_newton(const double* Vr, int nV, const int* F, int nF, const int* fixedV
             break;
         }
         // Optimizer::solve_oneStep (Optimizer.cpp:505-573)
-        hessian_blocks_mt(rest.data(), F, nF, UV, 0, blocks.data(), o->nThreads);
-        if (solver_factorize(*reinterpret_cast<Solver*>(solver), blocks.data(), par, nF) != 0) {
+        hessian_blocks_mt(rest.data(), F, nF, W.data(), 0, blocks.data(), o->nThreads);
+        if (sc) hessian_blocks_mt(restA.data(), Fa, nFa, W.data(), 1, blocks.data() + 36 * (size_t)nF, o->nThreads);
+        Solver& S = *reinterpret_cast<Solver*>(solver);
+        if (solver_factorize_scaf(S, blocks.data(), nF, nFa, par, airScale, airFixed) != 0) {
             ocr_solver_destroy(solver);
             return -1;
         }
@@ -673,21 +770,25 @@ int ocr_newton(const double* Vr, int nV, const int* F, int nF, const int* fixedV
         // Optimizer::lineSearch (Optimizer.cpp:575-652)
         bool stopped = false;
         double step = 1.0;
-        ocr_init_step_size(F, nF, UV, d.data(), &step);
+        ocr_init_step_size(F, nF, W.data(), d.data(), &step);
+        if (sc) ocr_init_step_size(Fa, nFa, W.data(), d.data(), &step);
         step *= 0.99;
-        std::memcpy(UV0.data(), UV, sizeof(double) * 2 * nV);
+        double eScaf0 = 0.0, eScaf = 0.0;
+        if (sc) lastE = energy(W.data(), &eScaf0);   // Optimizer.cpp:588-592
+        std::memcpy(W0.data(), W.data(), sizeof(double) * 2 * nW);
         auto forward = [&](double s) {
-            for (int k = 0; k < 2 * nV; ++k) UV[k] = UV0[k] + s * d[k];
+            for (int k = 0; k < 2 * nW; ++k) W[k] = W0[k] + s * d[k];
         };
         forward(step);
-        double testE = par * ocr_energy(rest.data(), F, nF, UV, 0);
+        double testE = energy(W.data(), &eScaf);
         while (testE > lastE) {
             step /= 2.0;
             if (step == 0.0) { stopped = true; break; }
             forward(step);
-            testE = par * ocr_energy(rest.data(), F, nF, UV, 0);
+            testE = energy(W.data(), &eScaf);
         }
-        const double lastEDec = lastE - testE;
+        double lastEDec = lastE - testE;
+        if (sc) lastEDec += (-eScaf0 + eScaf);   // Optimizer.cpp:632-634
         if ((lastEDec / lastE < 1.0e-6 * step) && (step > 1.0e-3)) stopped = true;
         lastE = testE;
         traceE[it + 1] = lastE;
@@ -695,8 +796,25 @@ int ocr_newton(const double* Vr, int nV, const int* F, int nF, const int* fixedV
         traceSeconds[it] = std::chrono::duration<double>(clk::now() - t0).count();
         if (stopped) { *status = 1; ++it; break; }
     }
+    std::copy(W.begin(), W.begin() + 2 * (size_t)nV, UV);
     ocr_solver_destroy(solver);
     return it;
+}
+
+int ocr_newton(const double* Vr, int nV, const int* F, int nF, const int* fixedVert, int nFixed,
+               double* UV, const ocr_newton_opts* o, double* traceE, double* traceGsq,
+               double* traceAlpha, double* traceSeconds, int* status)
+{
+    return newton_impl(Vr, nV, F, nF, fixedVert, nFixed, UV, o, nullptr, traceE, traceGsq, traceAlpha, traceSeconds,
+                       status);
+}
+
+int ocr_newton_scaffold(const double* Vr, int nV, const int* F, int nF, const int* fixedVert, int nFixed,
+                        double* UV, const ocr_newton_opts* o, const ocr_scaffold* scaffold, double* traceE,
+                        double* traceGsq, double* traceAlpha, double* traceSeconds, int* status)
+{
+    return newton_impl(Vr, nV, F, nF, fixedVert, nFixed, UV, o, scaffold, traceE, traceGsq, traceAlpha, traceSeconds,
+                       status);
 }
 
 } // extern "C"

@@ -82,6 +82,24 @@ int ocr_newton(const double* V_rest, int nV, const int* F, int nF, const int* fi
                double* UV, const ocr_newton_opts* opts,
                double* traceE, double* traceGsq, double* traceAlpha, double* traceSeconds, int* status);
 
+/* The same loop with the bijectivity scaffold (the scaffolding branches of
+ * Optimizer.cpp:764-843 and lineSearch :585-634, Scaffold.cpp:179-293): an
+ * air mesh (airV nAirV x 2, airF, bnd as Scaffold's members) given once and
+ * moved with every step (Scaffold::stepForward), not rebuilt per iteration.
+ * traceE holds energies including the scaffold term. */
+typedef struct {
+    const double* airV;
+    int nAirV;
+    const int* airF;
+    int nAirF;
+    const int* bnd;
+    int nBnd;
+    double areaThres;     /* areaThres_AM (Scaffold.cpp:189) */
+} ocr_scaffold;
+int ocr_newton_scaffold(const double* V_rest, int nV, const int* F, int nF, const int* fixedVert, int nFixed,
+                        double* UV, const ocr_newton_opts* opts, const ocr_scaffold* scaffold,
+                        double* traceE, double* traceGsq, double* traceAlpha, double* traceSeconds, int* status);
+
 #ifdef __cplusplus
 }
 #endif

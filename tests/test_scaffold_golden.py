@@ -67,3 +67,28 @@ def test_augmented_gradient_bit_exact(golden, case):
     whole[2 * nV:] = w * ga[2 * nb:]
     np.testing.assert_array_equal(whole, g["gradw0"])
     assert len(g["dir0"]) == len(whole)
+
+
+@pytest.mark.parametrize("case", ["sheet_3k", "torus_768", "icosphere_320_scaf"])
+def test_port_first_iteration_with_scaffold(golden, case):
+    """The CPU restatement's scaffolding branches, one Newton iteration on the
+    reference's own first air mesh."""
+    g = golden(case)
+    par = 1.0 - g["scalars"][4]
+    airV, airF, bnd, _ = golden_scaffolds(g)[0]
+    _, tr, _ = O.newton(g["V_rest"], g["F"], g["fixedVert"], g["UV0"], par, 1, scaffold=(airV, airF, bnd),
+                        avg_edge_len=g["scalars"][1])
+    assert tr["E"][0] == pytest.approx(g["trace_Etot"][0], rel=1e-14)
+    assert tr["E"][1] == pytest.approx(g["trace_Etot"][1], rel=1e-3)
+    assert tr["gsq"][0] == pytest.approx(float(g["gradw0"] @ g["gradw0"]), rel=1e-12)
+    if g["trace_alpha"][0] > 0:
+        assert tr["alpha"][0] == pytest.approx(g["trace_alpha"][0], rel=1e-3)
+
+
+def test_port_scaffold_run_is_monotone(golden):
+    g = golden("sheet_3k")
+    par = 1.0 - g["scalars"][4]
+    airV, airF, bnd, _ = golden_scaffolds(g)[0]
+    _, tr, st = O.newton(g["V_rest"], g["F"], g["fixedVert"], g["UV0"], par, 40, scaffold=(airV, airF, bnd),
+                         avg_edge_len=g["scalars"][1])
+    assert st == 1 and np.all(np.diff(tr["E"]) <= 0.0)
