@@ -165,6 +165,11 @@ typedef struct {
     int lineSearchBatch;  /* trial step sizes per energy launch, 1..8, default 4 */
     int timing;           /* 1: record per-phase CUDA-event times */
     int linearSolver;     /* OC_SOLVER_DIRECT (default) or OC_SOLVER_PCG */
+    int scaffoldPattern;  /* 0 (default): a small scaffold's boundary and air
+                             vertices form one dense block, so rebuilding the
+                             air mesh keeps the analysis; 1: always the exact
+                             pattern (analysed again when the air mesh's
+                             connectivity changes) */
 } oc_optimizer_config;
 
 int oc_optimizer_default_config(oc_optimizer_config* cfg);

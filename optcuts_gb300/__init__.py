@@ -44,7 +44,8 @@ _vp = ctypes.c_void_p
 
 class OptimizerConfig(ctypes.Structure):
     _fields_ = [("pcgTol", ctypes.c_double), ("pcgMaxIter", ctypes.c_int), ("relGL2Tol", ctypes.c_double),
-                ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int), ("linearSolver", ctypes.c_int)]
+                ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int), ("linearSolver", ctypes.c_int),
+                ("scaffoldPattern", ctypes.c_int)]
 
 
 SOLVER_DIRECT = 0

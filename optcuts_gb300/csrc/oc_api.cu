@@ -70,9 +70,11 @@ struct oc_optimizer {
     // scaffold (the Optimizer's scaffolding branches): an air mesh over the
     // augmented vertex numbering [mesh vertices | air-only vertices]
     // (Scaffold::localVI2Global, Scaffold.cpp:179-184)
-    bool scaf = false, patternStale = true;
+    bool scaf = false, patternStale = true, airContribStale = false, cliqueMode = false;
     oc::DeviceMesh air;
-    int nWhole = 0, capWhole = 0, capAirF = 0, nAirV = 0, nBnd = 0;
+    // nWhole: system vertices incl. unused air slots (nV + capAir);
+    // nWholeReal: nV + air-only vertices
+    int nWhole = 0, nWholeReal = 0, capAir = 0, capWhole = 0, capAirF = 0, nAirV = 0, nBnd = 0;
     double wScaf = 0.0, airScale = 0.0, eScaf = 0.0;
     double2* wuv = nullptr;         // augmented UV (capWhole)
     double2* airCorner = nullptr;   // 3 x capAirF
@@ -247,22 +249,34 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
 // LinSysSolver::set_pattern reads from TriMesh::vNeighbor,
 // LinSysSolver.hpp:37-135).  Fixed rows keep only their diagonal block.
 // Also produces, per block slot, the ordered list of triangle contributions
-// (t * 9 + a * 3 + b), free-free pairs only.
+// (t * 9 + a * 3 + b), free-free pairs only.  extraF adds adjacency only
+// (air triangles, whose contributions are listed separately); clique adds
+// every pair among its vertices.
 void build_pattern(int nV, const int* F, int nF, const std::vector<unsigned char>& fixedMask,
                    std::vector<int>& rowPtr, std::vector<int>& col, std::vector<int>& diagSlot,
-                   std::vector<int>& cPtr, std::vector<int>& cIdx)
+                   std::vector<int>& cPtr, std::vector<int>& cIdx, const int* extraF = nullptr, int nExtraF = 0,
+                   const std::vector<int>* clique = nullptr)
 {
-    std::vector<int> deg(nV, 1);
     std::vector<std::vector<int>> nb(nV);
     for (int v = 0; v < nV; ++v) nb[v].push_back(v);
-    for (int t = 0; t < nF; ++t)
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) {
-                if (a == b) continue;
-                const int va = F[3 * t + a], vb = F[3 * t + b];
-                if (fixedMask[va] || fixedMask[vb]) continue;
-                nb[va].push_back(vb);
-            }
+    auto add_tris = [&](const int* T, int n) {
+        for (int t = 0; t < n; ++t)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    if (a == b) continue;
+                    const int va = T[3 * t + a], vb = T[3 * t + b];
+                    if (fixedMask[va] || fixedMask[vb]) continue;
+                    nb[va].push_back(vb);
+                }
+    };
+    add_tris(F, nF);
+    if (extraF) add_tris(extraF, nExtraF);
+    if (clique)
+        for (int va : *clique) {
+            if (fixedMask[va]) continue;
+            for (int vb : *clique)
+                if (vb != va && !fixedMask[vb]) nb[va].push_back(vb);
+        }
     rowPtr.assign(nV + 1, 0);
     for (int v = 0; v < nV; ++v) {
         std::sort(nb[v].begin(), nb[v].end());
@@ -300,18 +314,54 @@ void build_pattern(int nV, const int* F, int nF, const std::vector<unsigned char
         }
 }
 
+// Per-slot contribution lists of the air triangles (augmented ids) in an
+// existing pattern; false if a free-free pair has no slot.
+bool air_contributions(const std::vector<int>& rowPtr, const std::vector<int>& col,
+                       const std::vector<unsigned char>& fixedMask, const int* Fa, int nFa, std::vector<int>& aPtr,
+                       std::vector<int>& aIdx)
+{
+    const int nV = static_cast<int>(rowPtr.size()) - 1;
+    const int nnzb = rowPtr[nV];
+    std::vector<int> slotOf(9 * (size_t)nFa, -1);
+    aPtr.assign(nnzb + 1, 0);
+    for (int t = 0; t < nFa; ++t)
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const int va = Fa[3 * t + a], vb = Fa[3 * t + b];
+                if (fixedMask[va] || fixedMask[vb]) continue;
+                const int* lo = col.data() + rowPtr[va];
+                const int* hi = col.data() + rowPtr[va + 1];
+                const int* f = std::lower_bound(lo, hi, vb);
+                if (f == hi || *f != vb) return false;
+                const int s = static_cast<int>(f - col.data());
+                slotOf[9 * (size_t)t + 3 * a + b] = s;
+                aPtr[s + 1]++;
+            }
+    for (int s = 0; s < nnzb; ++s) aPtr[s + 1] += aPtr[s];
+    aIdx.resize(aPtr[nnzb] ? aPtr[nnzb] : 1);
+    std::vector<int> fill(aPtr.begin(), aPtr.end() - 1);
+    for (int t = 0; t < nFa; ++t)
+        for (int k = 0; k < 9; ++k) {
+            const int s = slotOf[9 * (size_t)t + k];
+            if (s >= 0) aIdx[fill[s]++] = 9 * t + k;
+        }
+    return true;
+}
+
 void free_bsr(oc::DeviceBsr& b)
 {
     cudaFree(b.rowPtr); cudaFree(b.col); cudaFree(b.val); cudaFree(b.diagSlot); cudaFree(b.rowFixed);
     cudaFree(b.cPtr); cudaFree(b.cIdx); cudaFree(b.dinv);
+    cudaFree(b.aPtr); cudaFree(b.aIdx);
     b = oc::DeviceBsr{};
 }
 
-int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::vector<unsigned char>& mask)
+int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::vector<unsigned char>& mask,
+                       const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr)
 {
     oc_ctx* ctx = ls->ctx;
     std::vector<int> cPtr, cIdx;
-    build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx);
+    build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx, extraF, nExtraF, clique);
     ls->rowFixed = mask;
     free_bsr(ls->b);
     oc::pcg_free(ls->wk);
@@ -347,8 +397,9 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     ls->patternSet = true;
     oc::chol_free(ls->chol);
     if (ls->kind == OC_SOLVER_DIRECT) {
-        // analyze_pattern (EigenLibSolver.cpp:71-77): symbolic factorisation
-        oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data());
+        // analyze_pattern (EigenLibSolver.cpp:71-77): symbolic factorisation;
+        // a clique (scaffold boundary + air vertices) is eliminated last
+        oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique);
         std::string err;
         int rc = oc::chol_upload(ls->chol, &err);
         if (rc) return fail(ctx, rc, err);
@@ -822,6 +873,7 @@ int oc_optimizer_default_config(oc_optimizer_config* c)
     c->lineSearchBatch = 4;
     c->timing = 0;
     c->linearSolver = OC_SOLVER_DIRECT;
+    c->scaffoldPattern = 0;
     return OC_OK;
 }
 
@@ -833,7 +885,7 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
     o->mesh = mesh;
     o->param = energyParam;
     o->wScaf = energyParam * 0.01;   // w_scaf, fixed at construction (Optimizer.cpp:87)
-    o->nWhole = o->capWhole = mesh->d.nV;
+    o->nWhole = o->nWholeReal = o->capWhole = mesh->d.nV;
     if (cfg) o->cfg = *cfg;
     else oc_optimizer_default_config(&o->cfg);
     if (!(o->cfg.pcgTol > 0.0)) o->cfg.pcgTol = 1e-8;
@@ -925,31 +977,69 @@ static int compute_energy(oc_optimizer* o, const double2* uv, const double2* dir
 // the current system: the mesh alone, or mesh + air mesh in the augmented
 // numbering (Scaffold::mergeVNeighbor / mergeFixedV, Scaffold.cpp:295-313,
 // then LinSysSolver::set_pattern + analyze_pattern, Optimizer.cpp:521-527).
+//
+// A small scaffold (boundary + air vertices <= kCliqueMax) is given a
+// pattern that does not depend on the air mesh's connectivity: every pair
+// of boundary and air slots is a block (a clique, eliminated last as one
+// dense front), with capAir >= the air-only vertex count padded by unused,
+// decoupled slots.  Rebuilding the air mesh then changes only the values
+// and the air contribution lists, not the analysis, as long as the
+// boundary and capAir stay the same.  A larger scaffold gets the exact
+// pattern, analysed again whenever its connectivity changes (as the
+// reference re-analyses every iteration).
+static constexpr int kCliqueMax = 512;
+
 static int ensure_pattern(oc_optimizer* o)
 {
-    if (!o->patternStale) return OC_OK;
     oc_mesh* m = o->mesh;
     const int nV = m->d.nV;
-    int rc;
-    if (!o->scaf) {
-        std::vector<unsigned char> mask(nV, 0);
-        for (int v : m->fixed) mask[v] = 1;
-        rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask);
+    if (o->patternStale) {
+        int rc;
+        if (!o->scaf) {
+            std::vector<unsigned char> mask(nV, 0);
+            for (int v : m->fixed) mask[v] = 1;
+            rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask);
+        }
+        else {
+            // rowFixed: 1 = fixed mesh vertex or unused air slot, 2 = fixed in
+            // the air mesh as well (its diagonal also receives w_scaf / |F_air|)
+            std::vector<unsigned char> mask(o->nWhole, 0);
+            for (int v : m->fixed) mask[v] = 1;
+            for (int v : m->fixed)
+                for (int i = 0; i < o->nBnd; ++i)
+                    if (o->bnd[i] == v) mask[v] = 2;
+            for (int v = o->nWholeReal; v < o->nWhole; ++v) mask[v] = 1;
+            if (o->cliqueMode) {
+                std::vector<int> clique(o->bnd);
+                for (int v = nV; v < o->nWhole; ++v) clique.push_back(v);
+                rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, nullptr, 0, &clique);
+            }
+            else {
+                rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, o->airFw.data(),
+                                        static_cast<int>(o->airFw.size() / 3));
+            }
+        }
+        if (rc) return rc;
+        o->patternStale = false;
+        o->airContribStale = o->scaf;
     }
-    else {
-        // rowFixed: 1 = fixed mesh vertex, 2 = fixed in the air mesh as well
-        // (its diagonal also receives the air mesh's w_scaf / |F_air|)
-        std::vector<unsigned char> mask(o->nWhole, 0);
-        for (int v : m->fixed) mask[v] = 1;
-        for (int v : m->fixed)
-            for (int i = 0; i < o->nBnd; ++i)
-                if (o->bnd[i] == v) mask[v] = 2;
-        std::vector<int> Fw(m->F);
-        Fw.insert(Fw.end(), o->airFw.begin(), o->airFw.end());
-        rc = linsys_set_pattern(o->ls, o->nWhole, Fw.data(), static_cast<int>(Fw.size() / 3), mask);
+    if (o->scaf && o->airContribStale) {
+        oc_linsys* ls = o->ls;
+        std::vector<int> aPtr, aIdx;
+        if (!air_contributions(ls->rowPtr, ls->col, ls->rowFixed, o->airFw.data(), static_cast<int>(o->airFw.size() / 3),
+                               aPtr, aIdx))
+            return fail(m->ctx, OC_ERR_INVALID, "scaffold: air triangle outside the pattern");
+        cudaFree(ls->b.aPtr);
+        cudaFree(ls->b.aIdx);
+        ls->b.aPtr = ls->b.aIdx = nullptr;
+        cudaStream_t st = m->ctx->stream;
+        OC_CUDA(m->ctx, dalloc(&ls->b.aPtr, aPtr.size()));
+        OC_CUDA(m->ctx, dalloc(&ls->b.aIdx, aIdx.size()));
+        OC_CUDA(m->ctx, upload(ls->b.aPtr, aPtr.data(), aPtr.size(), st));
+        OC_CUDA(m->ctx, upload(ls->b.aIdx, aIdx.data(), aIdx.size(), st));
+        OC_CUDA(m->ctx, cudaStreamSynchronize(st));
+        o->airContribStale = false;
     }
-    if (rc) return rc;
-    o->patternStale = false;
     return OC_OK;
 }
 
@@ -1277,7 +1367,22 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     double area = 0.0;
     if (!rest_constants(V3.data(), airF, nAirF, areaThres, rest, area))
         return fail(ctx, OC_ERR_DEGENERATE, "set_scaffold: zero-area air triangle");
-    const int nWhole = nV + nAirV - nBnd;
+    const int nAirOnly = nAirV - nBnd;
+    // clique pattern for small scaffolds: air slots padded to a multiple of
+    // 32, reused while the air-only count fits and the boundary is unchanged
+    int capAir = (nAirOnly + 31) / 32 * 32;
+    // the same boundary vertex set (the clique does not depend on their order)
+    bool sameBnd = false;
+    if (o->scaf && (int)o->bnd.size() == nBnd) {
+        std::vector<int> x(bnd, bnd + nBnd), y(o->bnd);
+        std::sort(x.begin(), x.end());
+        std::sort(y.begin(), y.end());
+        sameBnd = x == y;
+    }
+    if (sameBnd && o->cliqueMode && nAirOnly <= o->capAir && o->capAir - nAirOnly <= 64) capAir = o->capAir;
+    const bool cliqueMode = o->cfg.scaffoldPattern == 0 && nBnd + capAir <= kCliqueMax;
+    if (!cliqueMode) capAir = nAirOnly;
+    const int nWhole = nV + capAir;
     auto toWhole = [&](int a) { return a < nBnd ? bnd[a] : nV + a - nBnd; };   // localVI2Global
     std::vector<int> Fw(3 * (size_t)nAirF);
     for (size_t i = 0; i < Fw.size(); ++i) Fw[i] = toWhole(airF[i]);
@@ -1285,8 +1390,9 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     std::vector<unsigned char> airMask(nWhole, 0);
     for (int v : m->fixed)
         if (isBnd[v] >= 0) airMask[v] = 1;
-    const bool samePattern = o->scaf && !o->patternStale && Fw == o->airFw && o->nWhole == nWhole &&
-                             std::equal(bnd, bnd + nBnd, o->bnd.begin(), o->bnd.end());
+    const bool samePattern = o->scaf && !o->patternStale && sameBnd && o->nWhole == nWhole &&
+                             o->cliqueMode == cliqueMode &&
+                             (cliqueMode || (Fw == o->airFw && std::equal(bnd, bnd + nBnd, o->bnd.begin())));
     int rc = ensure_whole(o, nWhole);
     if (rc) return rc;
     if (nAirF > o->capAirF) {
@@ -1306,16 +1412,22 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     if (nAirV > nBnd)
         OC_CUDA(ctx, cudaMemcpyAsync(o->wuv + nV, airV + 2 * (size_t)nBnd, sizeof(double2) * (nAirV - nBnd),
                                      cudaMemcpyHostToDevice, st));
+    if (nWhole > nV + nAirOnly)   // unused air slots: not in any triangle, kept at 0
+        OC_CUDA(ctx, cudaMemsetAsync(o->wuv + nV + nAirOnly, 0, sizeof(double2) * (nWhole - nV - nAirOnly), st));
     OC_CUDA(ctx, cudaStreamSynchronize(st));
     o->airFw.swap(Fw);
     o->airF.assign(airF, airF + 3 * (size_t)nAirF);
     o->bnd.assign(bnd, bnd + nBnd);
     o->nWhole = nWhole;
+    o->nWholeReal = nV + nAirOnly;
+    o->capAir = capAir;
+    o->cliqueMode = cliqueMode;
     o->nAirV = nAirV;
     o->nBnd = nBnd;
     o->airScale = o->wScaf / nAirF;   // w_scaf / airMesh.F.rows() (Optimizer.cpp:776)
     o->scaf = true;
     if (!samePattern) o->patternStale = true;
+    o->airContribStale = true;
     return OC_OK;
 }
 
@@ -1341,7 +1453,7 @@ int oc_optimizer_clear_scaffold(oc_optimizer* o)
     if (o->scaf) o->patternStale = true;
     o->scaf = false;
     o->eScaf = 0.0;
-    o->nWhole = o->mesh->d.nV;
+    o->nWhole = o->nWholeReal = o->mesh->d.nV;
     return OC_OK;
 }
 
@@ -1378,7 +1490,7 @@ int oc_optimizer_get_last_energy_scaffold(oc_optimizer* o, double* eScaf)
 int oc_optimizer_system_size(oc_optimizer* o, int* nVerts)
 {
     if (!o || !nVerts) return OC_ERR_INVALID;
-    *nVerts = o->scaf ? o->nWhole : o->mesh->d.nV;
+    *nVerts = o->scaf ? o->nWholeReal : o->mesh->d.nV;
     return OC_OK;
 }
 
@@ -1386,7 +1498,7 @@ int oc_optimizer_last_vectors(oc_optimizer* o, double* gradient, double* searchD
 {
     if (!o) return OC_ERR_INVALID;
     oc_mesh* m = o->mesh;
-    const int n = o->scaf ? o->nWhole : m->d.nV;
+    const int n = o->scaf ? o->nWholeReal : m->d.nV;
     cudaStream_t st = m->ctx->stream;
     if (gradient) OC_CUDA(m->ctx, cudaMemcpyAsync(gradient, o->g, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
     if (searchDir) OC_CUDA(m->ctx, cudaMemcpyAsync(searchDir, o->dir, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));

@@ -109,7 +109,8 @@ int tiles_of(int k, int m) { return (k + kTile - 1) / kTile + (m - k + kTile - 1
 
 } // namespace
 
-void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize)
+void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize,
+                  const std::vector<int>* rootVerts)
 {
     P = CholPlan{};
     P.nV = nV;
@@ -118,9 +119,12 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     std::vector<int> tag(nV, 0), level(nV, -1);
     int tagCounter = 0;
     // components: run the dissection on every connected set of vertices
+    // (the forced root vertices excluded: tag 0 keeps the BFS out of them)
     std::vector<int> roots;
     {
         std::vector<char> seen(nV, 0);
+        if (rootVerts)
+            for (int v : *rootVerts) seen[v] = 1;
         for (int s = 0; s < nV; ++s) {
             if (seen[s]) continue;
             std::vector<int> comp{s};
@@ -133,6 +137,7 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             roots.push_back(nd_build(rowPtr, col, comp, tag, tagCounter, level, nodes, leafSize));
         }
     }
+    if (rootVerts && !rootVerts->empty()) nodes.push_back(NdNode{*rootVerts, roots});
     // nodes are created children-first: creation order is a postorder
     const int nF = static_cast<int>(nodes.size());
     P.nFronts = nF;

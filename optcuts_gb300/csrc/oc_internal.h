@@ -65,6 +65,9 @@ struct DeviceBsr {
     unsigned char* rowFixed = nullptr;
     // contributions: slot -> list of (t * 9 + a * 3 + b)
     int *cPtr = nullptr, *cIdx = nullptr;
+    // scaffold air-mesh contributions, same coding over the air triangles
+    // (aPtr has nnzb + 1 entries; null without a scaffold)
+    int *aPtr = nullptr, *aIdx = nullptr;
     Mat2d* dinv = nullptr;         // block-Jacobi inverses (FP64)
 };
 
@@ -104,8 +107,8 @@ void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t s
 // expand the 21 packed values to full 6x6 FP64 (for the API / tests)
 void launch_hessian_expand(const double* hb, int nF, double* out, cudaStream_t st);
 void launch_assemble(const DeviceBsr& b, const double* hb, int nF, double scale, cudaStream_t st);
-// contributions t < nF from hb (times scale), the rest from the air mesh's
-// hbAir (triangle t - nF, times airScale)
+// mesh contributions (cPtr/cIdx) from hb times scale plus the air mesh's
+// (aPtr/aIdx) from hbAir times airScale
 void launch_assemble_scaf(const DeviceBsr& b, const double* hb, int nF, double scale, const double* hbAir, int nFa,
                           double airScale, cudaStream_t st);
 int launch_precond(const DeviceBsr& b, cudaStream_t st, int* dFlag);

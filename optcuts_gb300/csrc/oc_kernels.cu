@@ -82,17 +82,13 @@ __global__ void __launch_bounds__(256) k_assemble_scaf(DeviceBsr b, const double
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= b.nnzb) return;
     Blk2 acc{0.0, 0.0, 0.0, 0.0}, accA{0.0, 0.0, 0.0, 0.0};
-    const int split = 9 * nF;
     for (int p = b.cPtr[s]; p < b.cPtr[s + 1]; ++p) {
-        const int code = b.cIdx[p];
-        if (code < split) {
-            const Blk2 B = local_block(hb, nF, code);
-            acc.a00 += B.a00; acc.a01 += B.a01; acc.a10 += B.a10; acc.a11 += B.a11;
-        }
-        else {
-            const Blk2 B = local_block(hbAir, nFa, code - split);
-            accA.a00 += B.a00; accA.a01 += B.a01; accA.a10 += B.a10; accA.a11 += B.a11;
-        }
+        const Blk2 B = local_block(hb, nF, b.cIdx[p]);
+        acc.a00 += B.a00; acc.a01 += B.a01; acc.a10 += B.a10; acc.a11 += B.a11;
+    }
+    for (int p = b.aPtr[s]; p < b.aPtr[s + 1]; ++p) {
+        const Blk2 B = local_block(hbAir, nFa, b.aIdx[p]);
+        accA.a00 += B.a00; accA.a01 += B.a01; accA.a10 += B.a10; accA.a11 += B.a11;
     }
     b.val[s] = Blk2{acc.a00 * scale + accA.a00 * airScale, acc.a01 * scale + accA.a01 * airScale,
                     acc.a10 * scale + accA.a10 * airScale, acc.a11 * scale + accA.a11 * airScale};

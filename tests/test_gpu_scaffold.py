@@ -136,3 +136,37 @@ def test_own_air_meshes_reach_reference_energy(golden, case, tol):
     # the air mesh the last rebuild made still covers box minus mesh
     sc = opt.getScaffold()
     assert set(sc.bnd.tolist()) == set(golden_scaffolds(g)[0][2].tolist())
+
+
+def test_clique_and_exact_patterns_agree(golden):
+    """The connectivity-independent scaffold pattern (boundary + air slots as
+    one dense block) and the exact pattern give the same Newton step (up to
+    the elimination order's rounding on these ill-conditioned systems) and
+    the same converged energy."""
+    g = golden("sheet_3k")
+    dirs, E = [], []
+    for mode in (0, 1):
+        m, opt = start(g, scaffoldPattern=mode)
+        opt.solve(1)
+        dirs.append(opt.lastVectors()[1])
+        for k in range(1, 60):
+            opt.setScaffold(scaffold(g, min(k, len(golden_scaffolds(g)) - 1)))
+            if opt.solve(1) == 1:
+                break
+        E.append(opt.getLastEnergyVal(True))
+    assert len(dirs[0]) == len(dirs[1])
+    assert np.linalg.norm(dirs[0] - dirs[1]) <= 5e-3 * np.linalg.norm(dirs[1])
+    assert E[0] == pytest.approx(E[1], rel=1e-6)
+
+
+def test_rebuilt_scaffold_keeps_analysis(golden):
+    """Rebuilding the air mesh with an unchanged boundary reuses the symbolic
+    factorisation (same fronts) in the dense-block mode."""
+    g = golden("icosphere_320_scaf")
+    m, opt = start(g)
+    opt.solve(1)
+    s0 = opt.solver_stats()
+    opt.rebuildScaffold()
+    opt.solve(1)
+    s1 = opt.solver_stats()
+    assert s0 == s1
