@@ -245,6 +245,37 @@ int oc_optimizer_system_size(oc_optimizer* opt, int* nVerts);
  * interleaved u, v; either may be NULL) */
 int oc_optimizer_last_vectors(oc_optimizer* opt, double* gradient, double* searchDir);
 
+/* ---- Topology queries (TriMesh::querySplit / queryMerge, TriMesh.cpp:548-951)
+ * The candidates of one outer-loop topology step, each scored by its exact
+ * local projected-Newton solve (TriMesh::computeLocalLDec and
+ * computeLocalEdDec_inSplit / _bSplit / _merge, TriMesh.cpp:2105-2862),
+ * all local solves in one batched device launch.  This is the
+ * bijectivity-off form (no local air meshes).  opType: */
+enum { OC_OP_BOUNDARY_SPLIT = 0, OC_OP_INTERIOR_SPLIT = 1, OC_OP_MERGE = 2 };
+typedef struct oc_topo_result oc_topo_result;
+/* TriMesh::cohE (nCohE x 4), needed by merge queries */
+int oc_mesh_set_cohesive_edges(oc_mesh* mesh, const int* cohE, int nCohE);
+/* SymDirichletEnergy::computeDivGradPerVert (SymDirichletEnergy.cpp:108-147)
+ * at the mesh's current UV: the split filter, nV values */
+int oc_mesh_split_filter(oc_mesh* mesh, double* divGrad);
+/* querySplit(lambda_t, false, opType == OC_OP_INTERIOR_SPLIT) or
+ * queryMerge(lambda_t).  lambda_t as the reference passes it
+ * (1 - energyParams[0]); filterExp = filterExp_in (<= 0: 0.6). */
+int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, oc_topo_result** out);
+/* candidate count, index of the largest E_w decrease (-1: none), size of
+ * the filtered pool (inSplitTotalAmt for interior splits), local problems
+ * solved, their largest iteration count, host build and device solve ms */
+int oc_topo_result_info(const oc_topo_result* r, int* nCand, int* best, int* pool, int* nProblems, int* maxIters,
+                        double* buildMs, double* solveMs);
+/* candidate c as the reference records it: EwDec (interior splits halved,
+ * TriMesh.cpp:702-704), energyChanges (2), path (<= 3), newVertPos (<= 4 x 2) */
+int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, double* energyChanges, int* path,
+                             int* pathLen, double* newVertPos, int* posRows);
+int oc_topo_result_destroy(oc_topo_result* r);
+/* host only: the split filter's candidate vertices, in order */
+int oc_topology_split_candidates(int nV, const int* F, int nF, const double* divGrad, int interior, double filterExp,
+                                 int* cands, int* nCands, int* pool);
+
 /* ---- Air mesh without Triangle (replaces Scaffold.cpp:27-205) -----------
  * Host-only.  For a UV layout (UV nV x 2, F nF x 3) and the mesh's rest
  * avgEdgeLen: the boundary loops (each started at its smallest vertex), the

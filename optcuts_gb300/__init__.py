@@ -50,6 +50,7 @@ class OptimizerConfig(ctypes.Structure):
 
 SOLVER_DIRECT = 0
 SOLVER_PCG = 1
+OP_BOUNDARY_SPLIT, OP_INTERIOR_SPLIT, OP_MERGE = 0, 1, 2
 
 
 _SIGS = {
@@ -99,6 +100,13 @@ _SIGS = {
     "oc_air_mesh_sizes": [_vp, _i, _i, _i],
     "oc_air_mesh_get": [_vp, _d, _i, _i],
     "oc_air_mesh_destroy": [_vp],
+    "oc_mesh_set_cohesive_edges": [_vp, _i, ctypes.c_int],
+    "oc_mesh_split_filter": [_vp, _d],
+    "oc_topology_query": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_vp)],
+    "oc_topo_result_info": [_vp, _i, _i, _i, _i, _i, _d, _d],
+    "oc_topo_result_candidate": [_vp, ctypes.c_int, _d, _d, _i, _i, _d, _i],
+    "oc_topo_result_destroy": [_vp],
+    "oc_topology_split_candidates": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_double, _i, _i, _i],
     "oc_optimizer_get_scaffold": [_vp, _i, _i, _i, _d, _i, _i],
     "oc_optimizer_get_last_energy_scaffold": [_vp, _d],
     "oc_optimizer_system_size": [_vp, _i],
@@ -234,6 +242,52 @@ class TriMesh:
         self.ctx.check(lib().oc_mesh_check_inversion(self.h, ctypes.byref(ok)), "checkInversion")
         return bool(ok.value)
 
+    # ---- topology (TriMesh::querySplit / queryMerge) ----
+    def setCohesiveEdges(self, cohE):
+        c = _i4(np.asarray(cohE).reshape(-1, 4))
+        self.ctx.check(lib().oc_mesh_set_cohesive_edges(self.h, _pi(c), len(c)), "setCohesiveEdges")
+
+    def splitFilter(self):
+        """SymDirichletEnergy::computeDivGradPerVert at the current UV."""
+        out = np.zeros(self.nV)
+        self.ctx.check(lib().oc_mesh_split_filter(self.h, _pd(out)), "splitFilter")
+        return out
+
+    def _query(self, op, lambda_t, filterExp):
+        h = _vp()
+        self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), ctypes.byref(h)),
+                       "topology query")
+        try:
+            n, best, pool, nprob, mit = (ctypes.c_int() for _ in range(5))
+            bms, sms = ctypes.c_double(), ctypes.c_double()
+            lib().oc_topo_result_info(h, ctypes.byref(n), ctypes.byref(best), ctypes.byref(pool), ctypes.byref(nprob),
+                                      ctypes.byref(mit), ctypes.byref(bms), ctypes.byref(sms))
+            cands = []
+            for c in range(n.value):
+                ew, ec = ctypes.c_double(), np.zeros(2)
+                path, plen = np.zeros(3, np.int32), ctypes.c_int()
+                pos, rows = np.zeros(8), ctypes.c_int()
+                lib().oc_topo_result_candidate(h, c, ctypes.byref(ew), _pd(ec), _pi(path), ctypes.byref(plen),
+                                               _pd(pos), ctypes.byref(rows))
+                cands.append({"EwDec": ew.value, "energyChanges": (float(ec[0]), float(ec[1])),
+                              "path": path[:plen.value].tolist(), "newVertPos": pos[:2 * rows.value].reshape(-1, 2)})
+        finally:
+            lib().oc_topo_result_destroy(h)
+        b = best.value
+        return {"EwDec_max": cands[b]["EwDec"] if b >= 0 else 0.0, "best": b,
+                "path_max": cands[b]["path"] if b >= 0 else [], "candidates": cands, "pool": pool.value,
+                "local_problems": nprob.value, "max_local_iters": mit.value, "build_ms": bms.value,
+                "solve_ms": sms.value}
+
+    def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6):
+        """TriMesh::querySplit(lambda_t, false, splitInterior) with every local
+        solve batched on the GPU (bijectivity off)."""
+        return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp)
+
+    def queryMerge(self, lambda_t):
+        """TriMesh::queryMerge(lambda_t, false) (bijectivity off)."""
+        return self._query(OP_MERGE, lambda_t, 0.6)
+
     def close(self):
         if getattr(self, "h", None):
             lib().oc_mesh_destroy(self.h)
@@ -351,6 +405,19 @@ def energy_w(last_energy, seam_length, virtual_radius, lam):
     from optcuts_gb300.init.seam_sparsity and is constant during a Newton
     phase (it changes only with the topology)."""
     return last_energy + lam * seam_length / virtual_radius
+
+
+def split_candidates(nV, F, divGrad, interior, filterExp=0.6):
+    """Host-only split filter (TriMesh.cpp:561-629): candidate vertices in
+    the reference's order and the filtered pool size."""
+    F, dg = _i4(F), _f8(divGrad)
+    out = np.zeros(nV, np.int32)
+    n, pool = ctypes.c_int(), ctypes.c_int()
+    rc = lib().oc_topology_split_candidates(nV, _pi(F), len(F), _pd(dg), int(interior), float(filterExp), _pi(out),
+                                            ctypes.byref(n), ctypes.byref(pool))
+    if rc != OC_OK:
+        raise OCError(rc, "split_candidates")
+    return out[:n.value], pool.value
 
 
 def symbolic_stats_dict(out):

@@ -31,8 +31,9 @@ UNITS = {
     "oc_chol.cu": [],
     "oc_api.cu": ["-Xcompiler", "-fvisibility=default"],
     "oc_airmesh.cpp": [],
+    "oc_topo.cpp": [],
 }
-HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h"]
+HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h"]
 
 
 def _newest_input():

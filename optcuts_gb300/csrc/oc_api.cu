@@ -7,6 +7,7 @@
 #include "oc_airmesh.h"
 #include "oc_chol.h"
 #include "oc_internal.h"
+#include "oc_topo.h"
 
 #include <algorithm>
 #include <cmath>
@@ -29,6 +30,9 @@ struct oc_mesh {
     oc::DeviceMesh d;
     oc::Scratch scratch;
     std::vector<double> rest;       // nF x 8, TriMesh feature layout
+    std::vector<double> Vrest;      // nV x 3
+    std::vector<int> cohE;          // nCohE x 4 cohesive edge pairs (TriMesh::cohE)
+    double* divGrad = nullptr;      // nV (lazy)
     double scalars[3] = {0, 0, 0};  // surfaceArea, avgEdgeLen, virtualRadius
     std::vector<int> F, fixed;
     double2* cornerBuf = nullptr;   // 3 x nF corner gradients
@@ -185,7 +189,7 @@ void device_mesh_free(oc::DeviceMesh& d)
 {
     cudaFree(d.F0); cudaFree(d.F1); cudaFree(d.F2);
     cudaFree(d.A2); cudaFree(d.w); cudaFree(d.e0); cudaFree(d.e1); cudaFree(d.e01);
-    cudaFree(d.e0d); cudaFree(d.e1d); cudaFree(d.e01d);
+    cudaFree(d.e0d); cudaFree(d.e1d); cudaFree(d.e01d); cudaFree(d.area);
     cudaFree(d.vcPtr); cudaFree(d.vcIdx); cudaFree(d.fixedMask);
     double2* uv = d.uv;
     d = oc::DeviceMesh{};
@@ -202,7 +206,7 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
     d.nV = nV;
     d.nF = nF;
     std::vector<int> f0(nF), f1(nF), f2(nF);
-    std::vector<double> col[8];
+    std::vector<double> col[9];
     for (auto& c : col) c.resize(nF);
     for (int t = 0; t < nF; ++t) {
         f0[t] = F[3 * t]; f1[t] = F[3 * t + 1]; f2[t] = F[3 * t + 2];
@@ -211,6 +215,7 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
         col[1][t] = r[0] / surfaceArea;      // w (SymDirichletEnergy.cpp:41)
         col[2][t] = r[2]; col[3][t] = r[3]; col[4][t] = r[4];
         col[5][t] = r[5]; col[6][t] = r[6]; col[7][t] = r[7];
+        col[8][t] = r[0];                    // triArea
     }
     // vertex -> corners, sorted by triangle id
     std::vector<int> vcPtr(nV + 1, 0), vcIdx(3 * (size_t)nF);
@@ -228,15 +233,15 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
         if (rc == OC_OK && e != cudaSuccess) rc = fail(ctx, OC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     };
     chk(dalloc(&d.F0, nF), "alloc"); chk(dalloc(&d.F1, nF), "alloc"); chk(dalloc(&d.F2, nF), "alloc");
-    double** dcols[8] = {&d.A2, &d.w, &d.e0, &d.e1, &d.e01, &d.e0d, &d.e1d, &d.e01d};
-    for (int k = 0; k < 8; ++k) chk(dalloc(dcols[k], nF), "alloc");
+    double** dcols[9] = {&d.A2, &d.w, &d.e0, &d.e1, &d.e01, &d.e0d, &d.e1d, &d.e01d, &d.area};
+    for (int k = 0; k < 9; ++k) chk(dalloc(dcols[k], nF), "alloc");
     chk(dalloc(&d.vcPtr, nV + 1), "alloc");
     chk(dalloc(&d.vcIdx, 3 * (size_t)nF), "alloc");
     chk(dalloc(&d.fixedMask, nV), "alloc");
     if (rc == OC_OK) {
         chk(upload(d.F0, f0.data(), nF, st), "upload"); chk(upload(d.F1, f1.data(), nF, st), "upload");
         chk(upload(d.F2, f2.data(), nF, st), "upload");
-        for (int k = 0; k < 8; ++k) chk(upload(*dcols[k], col[k].data(), nF, st), "upload");
+        for (int k = 0; k < 9; ++k) chk(upload(*dcols[k], col[k].data(), nF, st), "upload");
         chk(upload(d.vcPtr, vcPtr.data(), nV + 1, st), "upload");
         chk(upload(d.vcIdx, vcIdx.data(), 3 * (size_t)nF, st), "upload");
         chk(upload(d.fixedMask, mask.data(), nV, st), "upload");
@@ -516,6 +521,7 @@ int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV, 
     m->ctx = ctx;
     m->F.assign(F, F + 3 * (size_t)nF);
     m->fixed.assign(fixedVert, fixedVert + nFixed);
+    m->Vrest.assign(V_rest, V_rest + 3 * (size_t)nV);
     m->rest.resize(8 * (size_t)nF);
     // TriMesh::computeFeatures rest constants (TriMesh.cpp:343-404)
     double surfaceArea = 0.0;
@@ -567,7 +573,7 @@ int oc_mesh_destroy(oc_mesh* m)
     if (!m) return OC_ERR_INVALID;
     device_mesh_free(m->d);
     cudaFree(m->d.uv);
-    cudaFree(m->cornerBuf); cudaFree(m->tmpV); cudaFree(m->hb); cudaFree(m->tmpF);
+    cudaFree(m->cornerBuf); cudaFree(m->tmpV); cudaFree(m->hb); cudaFree(m->tmpF); cudaFree(m->divGrad);
     cudaFree(m->scratch.partials); cudaFree(m->scratch.result); cudaFree(m->scratch.minBits);
     if (m->scratch.hostResult) cudaFreeHost(m->scratch.hostResult);
     delete m;
@@ -662,6 +668,125 @@ int oc_sd_init_step_size(oc_mesh* m, const double* searchDir, double* stepSize)
     int rc = read_min(m, &s);
     if (rc) return rc;
     *stepSize = s;
+    return OC_OK;
+}
+
+// ------------------------------------------------------------------ topology
+int oc_mesh_set_cohesive_edges(oc_mesh* m, const int* cohE, int nCohE)
+{
+    if (!m || nCohE < 0 || (nCohE && !cohE)) return OC_ERR_INVALID;
+    for (long long i = 0; i < 4LL * nCohE; ++i)
+        if (cohE[i] < -1 || cohE[i] >= m->d.nV) return fail(m->ctx, OC_ERR_INVALID, "cohesive edge: vertex out of range");
+    m->cohE.assign(cohE, cohE + 4 * (size_t)nCohE);
+    return OC_OK;
+}
+
+int oc_mesh_split_filter(oc_mesh* m, double* divGrad)
+{
+    if (!m || !divGrad) return OC_ERR_INVALID;
+    if (!m->divGrad) OC_CUDA(m->ctx, dalloc(&m->divGrad, m->d.nV));
+    oc::launch_divgrad(m->d, m->cornerBuf, m->divGrad, m->ctx->stream);
+    OC_CUDA(m->ctx, cudaGetLastError());
+    OC_CUDA(m->ctx, cudaMemcpyAsync(divGrad, m->divGrad, sizeof(double) * m->d.nV, cudaMemcpyDeviceToHost,
+                                    m->ctx->stream));
+    OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+    return OC_OK;
+}
+
+struct oc_topo_result {
+    std::vector<oc::TopoCandidate> cands;
+    int best = -1, pool = 0;
+    oc::TopoStats stats;
+};
+
+int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, oc_topo_result** out)
+{
+    if (!m || !out || opType < 0 || opType > 2) return OC_ERR_INVALID;
+    *out = nullptr;
+    const int nV = m->d.nV;
+    std::vector<double> uv(2 * (size_t)nV), dg;
+    OC_CUDA(m->ctx, cudaMemcpyAsync(uv.data(), m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToHost, m->ctx->stream));
+    OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+    if (opType != oc::kOpMerge) {
+        dg.resize(nV);
+        int rc = oc_mesh_split_filter(m, dg.data());
+        if (rc) return rc;
+    }
+    oc::TopoQueryIn in;
+    in.nV = nV;
+    in.nF = m->d.nF;
+    in.F = m->F.data();
+    in.Vrest = m->Vrest.data();
+    in.rest = m->rest.data();
+    in.UV = uv.data();
+    in.cohE = m->cohE.empty() ? nullptr : m->cohE.data();
+    in.nCohE = static_cast<int>(m->cohE.size() / 4);
+    in.surfaceArea = m->scalars[0];
+    in.avgEdgeLen = m->scalars[1];
+    in.virtualRadius = m->scalars[2];
+    in.divGrad = dg.empty() ? nullptr : dg.data();
+    in.dm = &m->d;
+    in.st = m->ctx->stream;
+    oc_topo_result* r = new (std::nothrow) oc_topo_result;
+    if (!r) return OC_ERR_NOMEM;
+    std::string err;
+    const int rc = oc::topo_query(in, opType, lambda_t, filterExp > 0.0 ? filterExp : 0.6, r->cands, r->best, r->pool,
+                                  r->stats, &err);
+    if (rc) {
+        delete r;
+        return fail(m->ctx, rc, err);
+    }
+    *out = r;
+    return OC_OK;
+}
+
+int oc_topo_result_info(const oc_topo_result* r, int* nCand, int* best, int* pool, int* nProblems, int* maxIters,
+                        double* buildMs, double* solveMs)
+{
+    if (!r) return OC_ERR_INVALID;
+    if (nCand) *nCand = static_cast<int>(r->cands.size());
+    if (best) *best = r->best;
+    if (pool) *pool = r->pool;
+    if (nProblems) *nProblems = r->stats.nProblems;
+    if (maxIters) *maxIters = r->stats.maxIters;
+    if (buildMs) *buildMs = r->stats.buildMs;
+    if (solveMs) *solveMs = r->stats.solveMs;
+    return OC_OK;
+}
+
+int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, double* energyChanges, int* path,
+                             int* pathLen, double* newVertPos, int* posRows)
+{
+    if (!r || c < 0 || c >= (int)r->cands.size()) return OC_ERR_INVALID;
+    const oc::TopoCandidate& C = r->cands[c];
+    if (EwDec) *EwDec = C.EwDec;
+    if (energyChanges) { energyChanges[0] = C.ec0; energyChanges[1] = C.ec1; }
+    if (pathLen) *pathLen = static_cast<int>(C.path.size());
+    if (path) std::copy(C.path.begin(), C.path.end(), path);
+    if (posRows) *posRows = static_cast<int>(C.pos.size() / 2);
+    if (newVertPos) std::copy(C.pos.begin(), C.pos.end(), newVertPos);
+    return OC_OK;
+}
+
+int oc_topology_split_candidates(int nV, const int* F, int nF, const double* divGrad, int interior, double filterExp,
+                                 int* cands, int* nCands, int* pool)
+{
+    if (nV <= 0 || nF <= 0 || !F || !divGrad || !nCands) return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
+    std::vector<int> c;
+    int p = 0;
+    oc::topo_split_candidates(nV, F, nF, divGrad, interior != 0, filterExp > 0.0 ? filterExp : 0.6, c, p);
+    if (cands) std::copy(c.begin(), c.end(), cands);
+    *nCands = static_cast<int>(c.size());
+    if (pool) *pool = p;
+    return OC_OK;
+}
+
+int oc_topo_result_destroy(oc_topo_result* r)
+{
+    if (!r) return OC_ERR_INVALID;
+    delete r;
     return OC_OK;
 }
 

@@ -129,44 +129,52 @@ __global__ void k_reduce_final(const double* partials, int nBlocks, int nVals, d
     }
 }
 
-// SymDirichletEnergy::computeGradient per-corner terms (SymDirichletEnergy.cpp:267-297),
-// written to cornerBuf[k * nF + t].
-__global__ void __launch_bounds__(256) k_grad_corners(DeviceMesh m, int uniform, double2* __restrict__ cornerBuf)
+// SymDirichletEnergy::computeGradient per-corner terms (SymDirichletEnergy.cpp:
+// 267-297; also computeLocalGradient, :215-256) of one triangle.
+__device__ __forceinline__ void tri_corner_grads(const double2 U1, const double2 U2, const double2 U3, double A2,
+                                                 double e0, double e1, double e01, double w, double2 g[3])
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m.nF) return;
-    const double2 U1 = m.uv[m.F0[t]], U2 = m.uv[m.F1[t]], U3 = m.uv[m.F2[t]];
     const double a0 = U2.x - U1.x, a1 = U2.y - U1.y;   // U2m1
     const double b0 = U3.x - U1.x, b1 = U3.y - U1.y;   // U3m1
     const double area_U = 0.5 * (a0 * b1 - a1 * b0);
-    const double A2 = m.A2[t], e0 = m.e0[t], e1 = m.e1[t], e01 = m.e01[t];
     const double leftTerm = 1.0 + A2 / area_U / area_U;
     const double rightTerm = ((b0 * b0 + b1 * b1) * e0 + (a0 * a0 + a1 * a1) * e1) / 4 / A2 -
                              (b0 * a0 + b1 * a1) * e01 / 2 / A2;
     const double areaRatio = A2 / area_U / area_U / area_U;
-    const double w = uniform ? 1.0 : m.w[t];
-    const int nF = m.nF;
     {
         const double eo0 = U3.x - U2.x, eo1 = U3.y - U2.y;
         const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
         const double dR0 = ((e01 - e0) * b0 + (e01 - e1) * a0) / 2.0 / A2;
         const double dR1 = ((e01 - e0) * b1 + (e01 - e1) * a1) / 2.0 / A2;
-        cornerBuf[t] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+        g[0] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
     }
     {
         const double eo0 = U1.x - U3.x, eo1 = U1.y - U3.y;
         const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
         const double dR0 = (e1 * a0 - e01 * b0) / 2.0 / A2;
         const double dR1 = (e1 * a1 - e01 * b1) / 2.0 / A2;
-        cornerBuf[nF + t] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+        g[1] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
     }
     {
         const double eo0 = U2.x - U1.x, eo1 = U2.y - U1.y;
         const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
         const double dR0 = (e0 * b0 - e01 * a0) / 2.0 / A2;
         const double dR1 = (e0 * b1 - e01 * a1) / 2.0 / A2;
-        cornerBuf[2 * nF + t] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+        g[2] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
     }
+}
+
+// Corner gradients of every triangle, written to cornerBuf[k * nF + t].
+__global__ void __launch_bounds__(256) k_grad_corners(DeviceMesh m, int uniform, double2* __restrict__ cornerBuf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    double2 g[3];
+    tri_corner_grads(m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]], m.A2[t], m.e0[t], m.e1[t], m.e01[t],
+                     uniform ? 1.0 : m.w[t], g);
+    cornerBuf[t] = g[0];
+    cornerBuf[m.nF + t] = g[1];
+    cornerBuf[2 * m.nF + t] = g[2];
 }
 
 // Per-vertex gather in triangle order (the reference's scatter order), fixed
@@ -243,6 +251,33 @@ __global__ void __launch_bounds__(256) k_grad_gather_scaf(DeviceMesh m, const do
     block_sum_store<1>(acc, 1, partials + (size_t)blockIdx.x * kMaxTrials);
 }
 
+// SymDirichletEnergy::initStepSize per triangle (SymDirichletEnergy.cpp:
+// 555-609): the bound from det(U + alpha V) > 0, or stepSize when none.
+__device__ __forceinline__ double tri_step_bound(const double2 U1, const double2 U2, const double2 U3, const double2 V1,
+                                                 const double2 V2, const double2 V3, double stepSize)
+{
+    const double U2m1x = U2.x - U1.x, U2m1y = U2.y - U1.y;
+    const double U3m1x = U3.x - U1.x, U3m1y = U3.y - U1.y;
+    const double V2m1x = V2.x - V1.x, V2m1y = V2.y - V1.y;
+    const double V3m1x = V3.x - V1.x, V3m1y = V3.y - V1.y;
+    const double a = V2m1x * V3m1y - V2m1y * V3m1x;
+    const double b = U2m1x * V3m1y - U2m1y * V3m1x + V2m1x * U3m1y - V2m1y * U3m1x;
+    const double c = U2m1x * U3m1y - U2m1y * U3m1x;
+    const double delta = b * b - 4.0 * a * c;
+    double bound = stepSize;
+    if (a > 0.0) {
+        if ((b < 0.0) && (delta >= 0.0)) bound = 2.0 * c / (-b + sqrt(delta));
+    }
+    else if (a < 0.0) {
+        if (b < 0.0) bound = 2.0 * c / (-b + sqrt(delta));
+        else bound = (-b - sqrt(delta)) / 2.0 / a;
+    }
+    else {
+        if (b < 0.0) bound = -c / b;
+    }
+    return bound;
+}
+
 // SymDirichletEnergy::initStepSize (SymDirichletEnergy.cpp:555-609); the
 // minimum over triangles is taken with an atomicMin on the bit pattern of
 // positive doubles (order-independent, hence deterministic).
@@ -252,27 +287,7 @@ __global__ void __launch_bounds__(256) k_init_step(DeviceMesh m, const double2* 
     double best = stepSize;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m.nF; t += gridDim.x * blockDim.x) {
         const int i0 = m.F0[t], i1 = m.F1[t], i2 = m.F2[t];
-        const double2 U1 = m.uv[i0], U2 = m.uv[i1], U3 = m.uv[i2];
-        const double2 V1 = dir[i0], V2 = dir[i1], V3 = dir[i2];
-        const double U2m1x = U2.x - U1.x, U2m1y = U2.y - U1.y;
-        const double U3m1x = U3.x - U1.x, U3m1y = U3.y - U1.y;
-        const double V2m1x = V2.x - V1.x, V2m1y = V2.y - V1.y;
-        const double V3m1x = V3.x - V1.x, V3m1y = V3.y - V1.y;
-        const double a = V2m1x * V3m1y - V2m1y * V3m1x;
-        const double b = U2m1x * V3m1y - U2m1y * V3m1x + V2m1x * U3m1y - V2m1y * U3m1x;
-        const double c = U2m1x * U3m1y - U2m1y * U3m1x;
-        const double delta = b * b - 4.0 * a * c;
-        double bound = stepSize;
-        if (a > 0.0) {
-            if ((b < 0.0) && (delta >= 0.0)) bound = 2.0 * c / (-b + sqrt(delta));
-        }
-        else if (a < 0.0) {
-            if (b < 0.0) bound = 2.0 * c / (-b + sqrt(delta));
-            else bound = (-b - sqrt(delta)) / 2.0 / a;
-        }
-        else {
-            if (b < 0.0) bound = -c / b;
-        }
+        const double bound = tri_step_bound(m.uv[i0], m.uv[i1], m.uv[i2], dir[i0], dir[i1], dir[i2], stepSize);
         if (bound < best) best = bound;
     }
     // block min via shuffles (exact), then one atomic per block
@@ -335,20 +350,14 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
 // change the Newton direction, and reducing to the 4-dimensional
 // translation-free part first does not reproduce the reference.
 // Output: the upper triangle as 21 values per triangle (SoA).
-__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, double* __restrict__ hb)
+__device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, double e1d, double e01d, double w,
+                            double H[6][6])
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m.nF) return;
-    const int nF = m.nF;
-    const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
     const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
     const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
     const double area_U = 0.5 * (U2m1[0] * U3m1[1] - U2m1[1] * U3m1[0]);
-    const double triAreaSq = m.A2[t];
     const double areaRatio = triAreaSq / area_U / area_U / area_U;
     const double dAR = 3.0 / 2.0 * areaRatio / area_U;
-    const double e0d = m.e0d[t], e1d = m.e1d[t], e01d = m.e01d[t];
-    const double w = uniform ? 1.0 : m.w[t];
     const double leftTerm = 1.0 + triAreaSq / area_U / area_U;
     const double rightTerm = ((U3m1[0] * U3m1[0] + U3m1[1] * U3m1[1]) * e0d +
                               (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) / 2. -
@@ -368,7 +377,6 @@ __global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, doub
                               {e01d - e1d, e1d, -e01d},
                               {e01d - e0d, -e01d, e0d}};
     const double skew[3][3] = {{0, 1, -1}, {-1, 0, 1}, {1, -1, 0}};
-    double H[6][6];
     for (int i = 0; i < 3; ++i) {
         for (int j = i; j < 3; ++j) {
             for (int a = 0; a < 2; ++a) {
@@ -402,6 +410,16 @@ __global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, doub
                 H[i][j] = s;
             }
     }
+}
+
+__global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, double* __restrict__ hb)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    const int nF = m.nF;
+    const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
+    double H[6][6];
+    tri_hessian(U, m.A2[t], m.e0d[t], m.e1d[t], m.e01d[t], uniform ? 1.0 : m.w[t], H);
     for (int a = 0; a < 3; ++a) {
         hb[(3 * a + 0) * (size_t)nF + t] = H[2 * a][2 * a];
         hb[(3 * a + 1) * (size_t)nF + t] = H[2 * a][2 * a + 1];
@@ -442,6 +460,316 @@ __global__ void k_check_inversion(DeviceMesh m, unsigned long long* count)
     }
     for (int o = 16; o > 0; o >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, o);
     if ((threadIdx.x & 31) == 0 && bad) atomicAdd(count, static_cast<unsigned long long>(bad));
+}
+
+// SymDirichletEnergy::computeDivGradPerVert with its standard-deviation
+// filter (SymDirichletEnergy.cpp:108-147): per vertex, the standard
+// deviation of its incident corner gradients (mean and deviations summed in
+// triangle order; 0 for a vertex with one incident triangle).
+__global__ void __launch_bounds__(256) k_divgrad(DeviceMesh m, const double2* __restrict__ cornerBuf,
+                                                 double* __restrict__ out)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m.nV) return;
+    const int p0 = m.vcPtr[v], p1 = m.vcPtr[v + 1];
+    const int n = p1 - p0;
+    double mx = 0.0, my = 0.0;
+    for (int p = p0; p < p1; ++p) {
+        const double2 c = cornerBuf[m.vcIdx[p]];
+        mx = mx + c.x;
+        my = my + c.y;
+    }
+    mx = mx / n;
+    my = my / n;
+    double sd = 0.0;
+    for (int p = p0; p < p1; ++p) {
+        const double2 c = cornerBuf[m.vcIdx[p]];
+        const double dx = c.x - mx, dy = c.y - my;
+        sd = sd + (dx * dx + dy * dy);
+    }
+    out[v] = (n == 1) ? 0.0 : sqrt(sd / (n - 1.0));
+}
+
+// ---------------------------------------------------- local topology solves
+// One warp per local problem: the projected-Newton loop the reference runs
+// on a candidate's local mesh (Optimizer with useDense, energyParams {1},
+// relGL2Tol 1e-6, solve(maxIter): Optimizer.cpp:203-261, 505-652; dense
+// Hessian SymDirichletEnergy.cpp:306-427 + LDLT).  Lanes own triangles;
+// sums over triangles are taken in triangle order by single lanes, so the
+// result is deterministic.
+constexpr int kLocalChunk = 32;
+
+struct LocalShared {
+    double2 pos[kLocalMaxFree], pos0[kLocalMaxFree];
+    double dir[2 * kLocalMaxFree], g[2 * kLocalMaxFree];
+    double H[2 * kLocalMaxFree][2 * kLocalMaxFree];
+    double triE[kLocalChunk];
+    double triG[kLocalChunk][6];
+    double triH[kLocalChunk][21];
+    int triSlot[kLocalChunk][3];
+};
+
+__device__ __forceinline__ int sym21(int i, int j)   // packed upper triangle of a 6x6
+{
+    if (i > j) { const int t = i; i = j; j = t; }
+    return i * 6 - i * (i - 1) / 2 + (j - i);
+}
+
+// corner positions and free slots of local triangle t, at pos (+ alpha dir)
+__device__ __forceinline__ void local_corners(const LocalBatch& b, const LocalProblem& P, const LocalShared& S, int t,
+                                              const double2* pos, bool withDir, double alpha, double2 U[3], int slot[3])
+{
+    for (int k = 0; k < 3; ++k) {
+        const int lv = b.ltCorner[3 * (P.triOff + t) + k];
+        const int sl = b.lvSlot[P.vertOff + lv];
+        slot[k] = sl;
+        if (sl >= 0) {
+            double2 p = pos[sl];
+            if (withDir) {
+                p.x = p.x + alpha * S.dir[2 * sl];
+                p.y = p.y + alpha * S.dir[2 * sl + 1];
+            }
+            U[k] = p;
+        }
+        else {
+            U[k] = b.lvPos[P.vertOff + lv];
+        }
+    }
+}
+
+// local energy (weights triArea / localArea) at pos0 + alpha dir or at pos
+__device__ double local_energy(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P, LocalShared& S,
+                               const double2* pos, bool withDir, double alpha, int lane)
+{
+    double acc = 0.0;
+    for (int c0 = 0; c0 < P.nTri; c0 += kLocalChunk) {
+        const int t = c0 + lane;
+        double e = 0.0;
+        if (t < P.nTri) {
+            double2 U[3];
+            int sl[3];
+            local_corners(b, P, S, t, pos, withDir, alpha, U, sl);
+            const int g = b.ltGlobal[P.triOff + t];
+            e = elem_energy(m, g, m.area[g] / P.localArea, U[0], U[1], U[2]);
+        }
+        S.triE[lane] = e;
+        __syncwarp();
+        if (lane == 0) {
+            const int n = min(kLocalChunk, P.nTri - c0);
+            for (int k = 0; k < n; ++k) acc = acc + S.triE[k];
+        }
+        __syncwarp();
+    }
+    return __shfl_sync(0xffffffffu, acc, 0);
+}
+
+__global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m, double surfaceArea, LocalBatch b)
+{
+    __shared__ LocalShared shared[kLocalWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pi = blockIdx.x * kLocalWarps + warp;
+    if (pi >= b.nProb) return;   // uniform per warp
+    LocalShared& S = shared[warp];
+    const LocalProblem P = b.prob[pi];
+    const int nDof = 2 * P.nFree;
+    for (int j = lane; j < P.nVert; j += 32) {
+        const int sl = b.lvSlot[P.vertOff + j];
+        if (sl >= 0) S.pos[sl] = b.lvPos[P.vertOff + j];
+    }
+    __syncwarp();
+    // initial energy: the candidate's global triangles with global weights,
+    // rescaled to the local mesh (TriMesh.cpp:2355-2361)
+    double initE = 0.0;
+    if (lane == 0) {
+        for (int k = 0; k < P.nInit; ++k) {
+            const int g = b.initTri[P.initOff + k];
+            initE = initE + elem_energy(m, g, m.w[g], m.uv[m.F0[g]], m.uv[m.F1[g]], m.uv[m.F2[g]]);
+        }
+        initE = initE * (surfaceArea / P.localArea);
+    }
+    initE = __shfl_sync(0xffffffffu, initE, 0);
+    double lastE = local_energy(m, b, P, S, S.pos, false, 0.0, lane);   // precompute
+    int status = 0, it = 0;
+    bool finite = isfinite(lastE);
+    for (; it < P.maxIter && finite; ++it) {
+        // gradient (fixed vertices have no slot: zero rows)
+        double gj = 0.0;
+        for (int c0 = 0; c0 < P.nTri; c0 += kLocalChunk) {
+            const int t = c0 + lane;
+            if (t < P.nTri) {
+                double2 U[3];
+                int sl[3];
+                local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
+                const int g = b.ltGlobal[P.triOff + t];
+                double2 cg[3];
+                tri_corner_grads(U[0], U[1], U[2], m.A2[g], m.e0[g], m.e1[g], m.e01[g], m.area[g] / P.localArea, cg);
+                for (int k = 0; k < 3; ++k) {
+                    S.triG[lane][2 * k] = cg[k].x;
+                    S.triG[lane][2 * k + 1] = cg[k].y;
+                    S.triSlot[lane][k] = sl[k];
+                }
+            }
+            __syncwarp();
+            if (lane < nDof) {
+                const int n = min(kLocalChunk, P.nTri - c0);
+                for (int q = 0; q < n; ++q)
+                    for (int k = 0; k < 3; ++k)
+                        if (S.triSlot[q][k] == (lane >> 1)) gj = gj + S.triG[q][2 * k + (lane & 1)];
+            }
+            __syncwarp();
+        }
+        if (lane < nDof) S.g[lane] = gj;
+        __syncwarp();
+        double gsq = 0.0;
+        for (int j = 0; j < nDof; ++j) gsq = gsq + S.g[j] * S.g[j];
+        if (gsq < P.targetGRes) {   // Optimizer.cpp:215-221
+            status = 1;
+            break;
+        }
+        // dense Hessian of the free DOFs: projected triangle blocks summed in
+        // triangle order (IglUtils::addBlockToMatrix, IglUtils.cpp:453-489)
+        const int nEnt = nDof * (nDof + 1) / 2;
+        double hacc[2] = {0.0, 0.0};
+        for (int c0 = 0; c0 < P.nTri; c0 += kLocalChunk) {
+            const int t = c0 + lane;
+            if (t < P.nTri) {
+                double2 U[3];
+                int sl[3];
+                local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
+                const int g = b.ltGlobal[P.triOff + t];
+                double H6[6][6];
+                tri_hessian(U, m.A2[g], m.e0d[g], m.e1d[g], m.e01d[g], m.area[g] / P.localArea, H6);
+                for (int i = 0; i < 6; ++i)
+                    for (int j = i; j < 6; ++j) S.triH[lane][sym21(i, j)] = H6[i][j];
+                for (int k = 0; k < 3; ++k) S.triSlot[lane][k] = sl[k];
+            }
+            __syncwarp();
+            const int n = min(kLocalChunk, P.nTri - c0);
+            for (int r = 0; r < 2; ++r) {
+                const int e = lane + 32 * r;
+                if (e >= nEnt) continue;
+                // entry e -> (i, j), i <= j, row-major upper triangle
+                int i = 0, rem = e;
+                while (rem >= nDof - i) { rem -= nDof - i; ++i; }
+                const int j = i + rem;
+                double acc = hacc[r];
+                for (int q = 0; q < n; ++q)
+                    for (int a = 0; a < 3; ++a) {
+                        if (S.triSlot[q][a] != (i >> 1)) continue;
+                        for (int c = 0; c < 3; ++c)
+                            if (S.triSlot[q][c] == (j >> 1))
+                                acc = acc + S.triH[q][sym21(2 * a + (i & 1), 2 * c + (j & 1))];
+                    }
+                hacc[r] = acc;
+            }
+            __syncwarp();
+        }
+        for (int r = 0; r < 2; ++r) {
+            const int e = lane + 32 * r;
+            if (e >= nEnt) continue;
+            int i = 0, rem = e;
+            while (rem >= nDof - i) { rem -= nDof - i; ++i; }
+            const int j = i + rem;
+            S.H[i][j] = hacc[r];
+            S.H[j][i] = hacc[r];
+        }
+        __syncwarp();
+        // H d = -g by LDL^T with symmetric pivoting on the largest remaining
+        // diagonal (Eigen::LDLT); zero pivots give zero components
+        if (lane == 0) {
+            double A[2 * kLocalMaxFree][2 * kLocalMaxFree], x[2 * kLocalMaxFree];
+            int perm[2 * kLocalMaxFree];
+            for (int i = 0; i < nDof; ++i) {
+                perm[i] = i;
+                x[i] = -S.g[i];
+                for (int j = 0; j < nDof; ++j) A[i][j] = S.H[i][j];
+            }
+            double dmax = 0.0;
+            for (int i = 0; i < nDof; ++i) dmax = fmax(dmax, fabs(A[i][i]));
+            for (int k = 0; k < nDof; ++k) {
+                int piv = k;
+                for (int i = k + 1; i < nDof; ++i)
+                    if (fabs(A[i][i]) > fabs(A[piv][piv])) piv = i;
+                if (piv != k) {
+                    for (int j = 0; j < nDof; ++j) { const double t = A[k][j]; A[k][j] = A[piv][j]; A[piv][j] = t; }
+                    for (int i = 0; i < nDof; ++i) { const double t = A[i][k]; A[i][k] = A[i][piv]; A[i][piv] = t; }
+                    const int tp = perm[k]; perm[k] = perm[piv]; perm[piv] = tp;
+                }
+                const double d = A[k][k];
+                if (!(fabs(d) > 1e-300 + 1e-15 * dmax)) {
+                    A[k][k] = 0.0;
+                    for (int i = k + 1; i < nDof; ++i) A[i][k] = 0.0;
+                    continue;
+                }
+                for (int i = k + 1; i < nDof; ++i) A[i][k] = A[i][k] / d;
+                for (int i = k + 1; i < nDof; ++i)
+                    for (int j = k + 1; j <= i; ++j) {
+                        A[i][j] = A[i][j] - A[i][k] * d * A[j][k];
+                        A[j][i] = A[i][j];
+                    }
+            }
+            double y[2 * kLocalMaxFree];
+            for (int i = 0; i < nDof; ++i) y[i] = x[perm[i]];
+            for (int i = 0; i < nDof; ++i)
+                for (int k = 0; k < i; ++k) y[i] = y[i] - A[i][k] * y[k];
+            for (int i = 0; i < nDof; ++i) y[i] = (A[i][i] != 0.0) ? y[i] / A[i][i] : 0.0;
+            for (int i = nDof - 1; i >= 0; --i)
+                for (int k = i + 1; k < nDof; ++k) y[i] = y[i] - A[k][i] * y[k];
+            for (int i = 0; i < nDof; ++i) S.dir[perm[i]] = y[i];
+        }
+        __syncwarp();
+        // line search (Optimizer.cpp:575-652): injective bound x 0.99, halve
+        // until E <= E_last, relative-decrease stop test
+        double bound = 1.0;
+        for (int t = lane; t < P.nTri; t += 32) {
+            double2 U[3], D[3];
+            int sl[3];
+            local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
+            for (int k = 0; k < 3; ++k)
+                D[k] = sl[k] >= 0 ? make_double2(S.dir[2 * sl[k]], S.dir[2 * sl[k] + 1]) : make_double2(0.0, 0.0);
+            bound = fmin(bound, tri_step_bound(U[0], U[1], U[2], D[0], D[1], D[2], 1.0));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) bound = fmin(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+        double step = bound * 0.99;
+        if (lane < P.nFree) S.pos0[lane] = S.pos[lane];
+        __syncwarp();
+        bool stopped = false;
+        double testE = local_energy(m, b, P, S, S.pos0, true, step, lane);
+        while (testE > lastE) {
+            step = step / 2.0;
+            if (step == 0.0) {
+                stopped = true;
+                break;
+            }
+            testE = local_energy(m, b, P, S, S.pos0, true, step, lane);
+        }
+        if (lane < P.nFree) {
+            S.pos[lane].x = S.pos0[lane].x + step * S.dir[2 * lane];
+            S.pos[lane].y = S.pos0[lane].y + step * S.dir[2 * lane + 1];
+        }
+        __syncwarp();
+        const double lastEDec = lastE - testE;
+        if ((lastEDec / lastE < 1.0e-6 * step) && (step > 1.0e-3)) stopped = true;
+        lastE = testE;
+        finite = isfinite(lastE);
+        if (stopped) {
+            status = 1;
+            ++it;
+            break;
+        }
+    }
+    if (!finite) status = 2;
+    if (lane == 0) {
+        LocalResult r;
+        r.initE = initE;
+        r.lastE = lastE;
+        r.eDec = (initE - lastE) * P.localArea / surfaceArea;   // TriMesh.cpp:2381
+        for (int k = 0; k < kLocalMaxFree; ++k) r.pos[k] = k < P.nFree ? S.pos[k] : make_double2(0.0, 0.0);
+        r.iters = it;
+        r.status = status;
+        b.out[pi] = r;
+    }
 }
 
 } // namespace
@@ -555,6 +883,18 @@ void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, 
 {
     if (reset) k_set_bits<<<1, 1, 0, st>>>(s.minBits, stepSize);
     k_init_step<<<reduce_blocks_for(m.nF), 256, 0, st>>>(m, dir, stepSize, s.minBits);
+}
+
+void launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, cudaStream_t st)
+{
+    if (b.nProb <= 0) return;
+    k_local_newton<<<(b.nProb + kLocalWarps - 1) / kLocalWarps, 32 * kLocalWarps, 0, st>>>(m, surfaceArea, b);
+}
+
+void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st)
+{
+    k_grad_corners<<<(m.nF + 255) / 256, 256, 0, st>>>(m, 0, cornerBuf);
+    k_divgrad<<<(m.nV + 255) / 256, 256, 0, st>>>(m, cornerBuf, divGrad);
 }
 
 void launch_step_forward(const double2* uv0, const double2* dir, double alpha, double2* uv, int nV, cudaStream_t st)

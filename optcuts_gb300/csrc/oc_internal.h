@@ -40,6 +40,7 @@ struct DeviceMesh {
     double *A2 = nullptr, *w = nullptr;
     double *e0 = nullptr, *e1 = nullptr, *e01 = nullptr;
     double *e0d = nullptr, *e1d = nullptr, *e01d = nullptr;
+    double* area = nullptr;                              // triArea
     double2* uv = nullptr;                              // nV
     // vertex -> incident corners (CSR, each list sorted by triangle id);
     // corner code = k * nF + t
@@ -69,6 +70,34 @@ struct DeviceBsr {
     // (aPtr has nnzb + 1 entries; null without a scaffold)
     int *aPtr = nullptr, *aIdx = nullptr;
     Mat2d* dinv = nullptr;         // block-Jacobi inverses (FP64)
+};
+
+// One local problem of the batched topology queries: a candidate split or
+// merge evaluated on its local mesh (TriMesh::computeLocalEdDec_*).
+constexpr int kLocalMaxFree = 4;    // free local vertices (8 DOF)
+constexpr int kLocalWarps = 4;      // local problems per block (one warp each)
+struct LocalProblem {
+    int triOff, nTri;      // local triangles: rows of ltGlobal / ltCorner
+    int vertOff, nVert;    // local vertices: rows of lvPos / lvSlot
+    int initOff, nInit;    // global triangles summed for the initial energy
+    int nFree, maxIter;
+    double localArea;      // the local mesh's surfaceArea (local triangle order)
+    double targetGRes;     // (nVert - nFixed) / nVert * 1e-6
+};
+struct LocalResult {
+    double eDec, initE, lastE;
+    double2 pos[kLocalMaxFree];   // free vertices' final positions, by slot
+    int iters, status;            // status 1: converged or stopped; 0: iteration cap; 2: non-finite
+};
+struct LocalBatch {
+    const LocalProblem* prob = nullptr;
+    int nProb = 0;
+    const int* ltGlobal = nullptr;     // global triangle id (rest constants)
+    const int* ltCorner = nullptr;     // 3 local vertex ids per local triangle
+    const double2* lvPos = nullptr;    // initial UV per local vertex
+    const int* lvSlot = nullptr;       // free slot or -1 (fixed)
+    const int* initTri = nullptr;
+    LocalResult* out = nullptr;
 };
 
 struct PcgWork {
@@ -101,6 +130,11 @@ void launch_step_forward(const double2* uv0, const double2* dir, double alpha, d
 void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st);
 void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st, double* out = nullptr);
 int reduce_blocks_for(int n);
+
+// batched projected-Newton solves of the topology candidates' local problems
+void launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, cudaStream_t st);
+// SymDirichletEnergy::computeDivGradPerVert (standard-deviation filter) into divGrad (nV)
+void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st);
 
 // per-triangle PSD-projected Hessian: 21 FP64 values per triangle (SoA)
 void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st);

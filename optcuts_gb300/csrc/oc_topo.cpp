@@ -1,0 +1,611 @@
+// Topology queries (TriMesh::querySplit / queryMerge, src/TriMesh.cpp:548-951)
+// with the candidates' local solves batched on the device.
+//
+// The host enumerates the candidates exactly as the reference does (split
+// filter on the per-vertex gradient deviation, boundary and interior split
+// paths, zipper-bottom cohesive pairs with the merged-position projection),
+// builds every local mesh (TriMesh::computeLocalEdDec_inSplit / _bSplit /
+// _merge, TriMesh.cpp:2262-2794, with the local cut or split applied) as a
+// packed problem, and one launch of k_local_newton solves them all (one warp
+// per problem).  This is the bijectivity-off form of the queries: the local
+// meshes carry no air mesh.
+
+#include "oc_topo.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <utility>
+
+namespace oc {
+namespace {
+
+// vertex adjacency and directed half-edges of a triangle mesh (TriMesh's
+// vNeighbor and edge2Tri)
+struct Topo {
+    int nV = 0, nF = 0;
+    const int* F = nullptr;
+    std::vector<int> hoPtr, hoTo, hoTri;   // outgoing half-edges per vertex
+    std::vector<int> nbPtr, nb;            // sorted neighbours per vertex
+    std::vector<char> bnd;
+
+    void build(int nV_, const int* F_, int nF_)
+    {
+        nV = nV_;
+        nF = nF_;
+        F = F_;
+        hoPtr.assign(nV + 1, 0);
+        for (long long i = 0; i < 3LL * nF; ++i) hoPtr[F[i] + 1]++;
+        for (int v = 0; v < nV; ++v) hoPtr[v + 1] += hoPtr[v];
+        hoTo.resize(3 * (size_t)nF);
+        hoTri.resize(3 * (size_t)nF);
+        std::vector<int> fill(hoPtr.begin(), hoPtr.end() - 1);
+        for (int t = 0; t < nF; ++t)
+            for (int k = 0; k < 3; ++k) {
+                const int a = F[3 * t + k], b = F[3 * t + (k + 1) % 3];
+                hoTo[fill[a]] = b;
+                hoTri[fill[a]++] = t;
+            }
+        std::vector<std::vector<int>> adj(nV);
+        for (int a = 0; a < nV; ++a)
+            for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) {
+                adj[a].push_back(hoTo[p]);
+                adj[hoTo[p]].push_back(a);
+            }
+        nbPtr.assign(nV + 1, 0);
+        for (int v = 0; v < nV; ++v) {
+            std::sort(adj[v].begin(), adj[v].end());
+            adj[v].erase(std::unique(adj[v].begin(), adj[v].end()), adj[v].end());
+            nbPtr[v + 1] = nbPtr[v] + static_cast<int>(adj[v].size());
+        }
+        nb.resize(nbPtr[nV]);
+        for (int v = 0; v < nV; ++v) std::copy(adj[v].begin(), adj[v].end(), nb.begin() + nbPtr[v]);
+        bnd.assign(nV, 0);
+        for (int v = 0; v < nV; ++v)   // TriMesh::isBoundaryVert(vI), TriMesh.cpp:2069-2083
+            for (int p = nbPtr[v]; p < nbPtr[v + 1] && !bnd[v]; ++p)
+                if (edge_tri(v, nb[p]) < 0 || edge_tri(nb[p], v) < 0) bnd[v] = 1;
+    }
+
+    int edge_tri(int a, int b) const
+    {
+        for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p)
+            if (hoTo[p] == b) return hoTri[p];
+        return -1;
+    }
+
+    int degree(int v) const { return nbPtr[v + 1] - nbPtr[v]; }
+
+    bool adjacent(int a, int b) const { return std::binary_search(nb.begin() + nbPtr[a], nb.begin() + nbPtr[a + 1], b); }
+
+    int third(int t, int a, int b) const
+    {
+        for (int k = 0; k < 3; ++k)
+            if (F[3 * t + k] != a && F[3 * t + k] != b) return F[3 * t + k];
+        return -1;
+    }
+
+    // TriMesh::isBoundaryVert(vI, vI_neighbor, tri_toSep, boundaryEdge,
+    // toBound) (TriMesh.cpp:2032-2067): the fan of vI from the edge to
+    // vI_neighbor, rotating until a boundary edge (true) or back (false)
+    bool walk(int vI, int vNb, bool toBound, std::vector<int>& tris) const
+    {
+        tris.clear();
+        int f = toBound ? edge_tri(vNb, vI) : edge_tri(vI, vNb);
+        if (f < 0) return true;
+        int vNew = vNb;
+        for (int guard = 0; guard <= nF; ++guard) {
+            tris.push_back(f);
+            vNew = third(f, vI, vNew);
+            if (vNew == vNb) return false;
+            f = toBound ? edge_tri(vNew, vI) : edge_tri(vI, vNew);
+            if (f < 0) return true;
+        }
+        return false;
+    }
+};
+
+double rest_dist(const double* Vr, int a, int b)
+{
+    const double dx = Vr[3 * a] - Vr[3 * b], dy = Vr[3 * a + 1] - Vr[3 * b + 1], dz = Vr[3 * a + 2] - Vr[3 * b + 2];
+    return std::sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// packed local problems and what each one belongs to
+struct Batch {
+    std::vector<LocalProblem> prob;
+    std::vector<int> ltGlobal, ltCorner, lvSlot, initTri;
+    std::vector<double2> lvPos;
+    struct Tag {
+        int cand;          // candidate index
+        int a = -1, b = -1, c = -1;   // path entries
+        double se = 0.0;   // seam term of this problem (seInc or seDec)
+        int nRows = 0;     // newVertPos rows
+    };
+    std::vector<Tag> tag;
+};
+
+// local vertex table over a triangle list (first appearance in row order);
+// `alias` maps a global vertex to another whose local vertex it shares
+struct LocalMesh {
+    std::vector<int> gv;        // local -> global
+    std::vector<int> corner;    // 3 per triangle
+    int find(int g) const
+    {
+        for (size_t i = 0; i < gv.size(); ++i)
+            if (gv[i] == g) return static_cast<int>(i);
+        return -1;
+    }
+    void build(const Topo& T, const std::vector<int>& tris, int aliasA = -1, int aliasB = -1)
+    {
+        gv.clear();
+        corner.clear();
+        for (int t : tris)
+            for (int k = 0; k < 3; ++k) {
+                int g = T.F[3 * t + k];
+                if (g == aliasB) g = aliasA;
+                int l = find(g);
+                if (l < 0) {
+                    l = static_cast<int>(gv.size());
+                    gv.push_back(g);
+                }
+                corner.push_back(l);
+            }
+    }
+};
+
+void emit(Batch& B, const Topo& T, const double* rest, const double* UV, const std::vector<int>& tris,
+          const LocalMesh& L, const std::vector<double2>& extraPos, const std::vector<int>& slotOfLocal, int nFree,
+          int nFixed, const Batch::Tag& tag)
+{
+    (void)T;
+    LocalProblem P{};
+    P.triOff = static_cast<int>(B.ltGlobal.size());
+    P.nTri = static_cast<int>(tris.size());
+    P.vertOff = static_cast<int>(B.lvPos.size());
+    const int nLocal = static_cast<int>(L.gv.size()) + static_cast<int>(extraPos.size());
+    P.nVert = nLocal;
+    P.initOff = static_cast<int>(B.initTri.size());
+    P.nInit = static_cast<int>(tris.size());
+    P.nFree = nFree;
+    P.maxIter = 100;   // computeLocalEdDec_* default (TriMesh.hpp:166-180)
+    double area = 0.0;
+    for (int t : tris) area += rest[8 * (size_t)t];   // local computeFeatures order
+    P.localArea = area;
+    P.targetGRes = 1.0 * static_cast<double>(nLocal - nFixed) / static_cast<double>(nLocal) * 1.0e-6;
+    for (size_t i = 0; i < tris.size(); ++i) {
+        B.ltGlobal.push_back(tris[i]);
+        B.initTri.push_back(tris[i]);
+        for (int k = 0; k < 3; ++k) B.ltCorner.push_back(L.corner[3 * i + k]);
+    }
+    for (size_t l = 0; l < L.gv.size(); ++l) {
+        B.lvPos.push_back(make_double2(UV[2 * (size_t)L.gv[l]], UV[2 * (size_t)L.gv[l] + 1]));
+        B.lvSlot.push_back(slotOfLocal[l]);
+    }
+    for (size_t e = 0; e < extraPos.size(); ++e) {
+        B.lvPos.push_back(extraPos[e]);
+        B.lvSlot.push_back(slotOfLocal[L.gv.size() + e]);
+    }
+    B.prob.push_back(P);
+    B.tag.push_back(tag);
+}
+
+// the split filter: vertices sorted by -divGrad in a std::map (equal keys
+// keep the last vertex), first max(2, pow(count, exponent)) of them
+// (TriMesh.cpp:561-629)
+std::vector<int> filter_candidates(const std::vector<std::pair<double, int>>& keyed, double exponent, int& poolSize)
+{
+    std::vector<std::pair<double, int>> s(keyed);
+    std::stable_sort(s.begin(), s.end(), [](const std::pair<double, int>& x, const std::pair<double, int>& y) {
+        return x.first < y.first;
+    });
+    std::vector<std::pair<double, int>> uniq;
+    for (const auto& kv : s) {
+        if (!uniq.empty() && uniq.back().first == kv.first) uniq.back().second = kv.second;
+        else uniq.push_back(kv);
+    }
+    poolSize = static_cast<int>(uniq.size());
+    std::vector<int> out;
+    if (uniq.empty()) return out;
+    int amt = static_cast<int>(std::pow(static_cast<double>(uniq.size()), exponent));
+    if (amt < 2) amt = 2;
+    for (const auto& kv : uniq) {
+        out.push_back(kv.second);
+        if ((int)out.size() >= amt) break;
+    }
+    return out;
+}
+
+bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector<int>& tris)
+{
+    for (int t : tris) {   // TriMesh::checkInversion(triI), TriMesh.cpp:1710-1733
+        const int* f = T.F + 3 * t;
+        const double e00 = V[2 * f[1]] - V[2 * f[0]], e01 = V[2 * f[1] + 1] - V[2 * f[0] + 1];
+        const double e10 = V[2 * f[2]] - V[2 * f[0]], e11 = V[2 * f[2] + 1] - V[2 * f[0] + 1];
+        if (e00 * e11 - e01 * e10 < 0.0) return true;
+    }
+    return false;
+}
+
+} // namespace
+
+int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, bool interior, double filterExp,
+                          std::vector<int>& cands, int& pool)
+{
+    Topo T;
+    T.build(nV, F, nF);
+    std::vector<std::pair<double, int>> keyed;
+    for (int v = 0; v < nV; ++v) {
+        if (T.degree(v) <= 2) continue;
+        if (!interior) {
+            if (T.bnd[v]) keyed.push_back({-divGrad[v] / 1.0, v});
+        }
+        else if (!T.bnd[v]) {
+            bool toBound = false;
+            for (int p = T.nbPtr[v]; p < T.nbPtr[v + 1] && !toBound; ++p) toBound = T.bnd[T.nb[p]];
+            if (!toBound) keyed.push_back({-divGrad[v] / 1.0, v});
+        }
+    }
+    cands = filter_candidates(keyed, interior ? filterExp : 0.8, pool);
+    return OC_OK;
+}
+
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, std::vector<TopoCandidate>& out,
+               int& best, int& candidatePool, TopoStats& stats, std::string* err)
+{
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    out.clear();
+    best = -1;
+    candidatePool = 0;
+    stats = TopoStats{};
+    if (!in.F || !in.Vrest || !in.UV || !in.rest || !in.dm || in.nV <= 0 || in.nF <= 0) {
+        if (err) *err = "topology query: bad arguments";
+        return OC_ERR_INVALID;
+    }
+    Topo T;
+    T.build(in.nV, in.F, in.nF);
+    const double R = in.virtualRadius;
+    Batch B;
+    std::vector<int> tris, tris1, tris2;
+    LocalMesh L;
+
+    if (opType == kOpBoundarySplit || opType == kOpInteriorSplit) {
+        if (!in.divGrad) {
+            if (err) *err = "topology query: no split filter";
+            return OC_ERR_INVALID;
+        }
+        std::vector<std::pair<double, int>> keyed;
+        for (int v = 0; v < in.nV; ++v) {
+            if (T.degree(v) <= 2) continue;   // cannot be split further
+            if (opType == kOpBoundarySplit) {
+                if (T.bnd[v]) keyed.push_back({-in.divGrad[v] / 1.0, v});   // vertWeight = 1
+            }
+            else if (!T.bnd[v]) {
+                bool toBound = false;
+                for (int p = T.nbPtr[v]; p < T.nbPtr[v + 1] && !toBound; ++p) toBound = T.bnd[T.nb[p]];
+                if (!toBound) keyed.push_back({-in.divGrad[v] / 1.0, v});
+            }
+        }
+        const std::vector<int> cands =
+            filter_candidates(keyed, opType == kOpBoundarySplit ? 0.8 : filterExp, candidatePool);
+        out.resize(cands.size());
+        for (size_t ci = 0; ci < cands.size(); ++ci) {
+            const int vI = cands[ci];
+            TopoCandidate& C = out[ci];
+            C.EwDec = -DBL_MAX;
+            C.ec0 = C.ec1 = DBL_MAX;
+            const int nbMin = T.nb[T.nbPtr[vI]];
+            if (opType == kOpBoundarySplit) {
+                C.path = {0, 0};
+                // computeLocalLDec boundary branch (TriMesh.cpp:2168-2199):
+                // every interior edge at vI, queryLocalEdDec_bSplit (:2796-2862)
+                for (int p = T.nbPtr[vI]; p < T.nbPtr[vI + 1]; ++p) {
+                    const int nbVI = T.nb[p];
+                    if (T.edge_tri(vI, nbVI) < 0 || T.edge_tri(nbVI, vI) < 0) continue;
+                    const int vb = vI, vi = nbVI;
+                    const bool cutThrough = T.bnd[vi] != 0;
+                    T.walk(vb, vi, false, tris);
+                    T.walk(vb, vi, true, tris1);
+                    tris.insert(tris.end(), tris1.begin(), tris1.end());
+                    if (cutThrough)
+                        for (int cw = 0; cw < 2; ++cw) {
+                            T.walk(vi, vb, cw != 0, tris2);
+                            for (int t : tris2)
+                                if (std::find(tris.begin(), tris.end(), t) == tris.end()) tris.push_back(t);
+                        }
+                    // local split (TriMesh::splitEdgeOnBoundary on the local
+                    // mesh, TriMesh.cpp:2864-3036): the copy of vb takes the
+                    // fan on the (vi -> vb) side; with cutThrough the copy of
+                    // vi takes vi's fan from vb towards the boundary
+                    L.build(T, tris);
+                    const int lb = L.find(vb), li = L.find(vi);
+                    const int nLoc = static_cast<int>(L.gv.size());
+                    std::vector<int> sideB, sideI;
+                    T.walk(vb, vi, true, sideB);
+                    if (cutThrough) T.walk(vi, vb, true, sideI);
+                    for (size_t k = 0; k < tris.size(); ++k) {
+                        const int t = tris[k];
+                        const bool inB = std::find(sideB.begin(), sideB.end(), t) != sideB.end();
+                        const bool inI = cutThrough && std::find(sideI.begin(), sideI.end(), t) != sideI.end();
+                        for (int c = 0; c < 3; ++c) {
+                            int& lc = L.corner[3 * k + c];
+                            if (inB && lc == lb) lc = nLoc;
+                            else if (inI && lc == li) lc = nLoc + 1;
+                        }
+                    }
+                    std::vector<double2> extra;
+                    const double2 pb = make_double2(in.UV[2 * (size_t)vb], in.UV[2 * (size_t)vb + 1]);
+                    const double2 pi = make_double2(in.UV[2 * (size_t)vi], in.UV[2 * (size_t)vi + 1]);
+                    extra.push_back(pb);
+                    if (cutThrough) extra.push_back(pi);
+                    // slots in newVertPos row order: vb, copy of vb, copy of vi, vi
+                    std::vector<int> slot(nLoc + extra.size(), -1);
+                    slot[lb] = 0;
+                    slot[nLoc] = 1;
+                    int nFree = 2, nFixed = nLoc - 1;
+                    if (cutThrough) {
+                        slot[nLoc + 1] = 2;
+                        slot[li] = 3;
+                        nFree = 4;
+                        nFixed = nLoc - 2;
+                    }
+                    Batch::Tag tg;
+                    tg.cand = static_cast<int>(ci);
+                    tg.a = vb;
+                    tg.b = vi;
+                    tg.se = rest_dist(in.Vrest, vI, nbVI) / R * (1.0 + 1.0) / 2.0;   // seInc
+                    tg.nRows = cutThrough ? 4 : 2;
+                    emit(B, T, in.rest, in.UV, tris, L, extra, slot, nFree, nFixed, tg);
+                }
+            }
+            else {
+                // computeLocalLDec interior branch (TriMesh.cpp:2200-2259): all
+                // paths (p0, vI, p2) through two umbrella edges
+                C.path = {0, 0, 0};
+                std::vector<int> umbrella;
+                T.walk(vI, nbMin, false, umbrella);
+                const int n = static_cast<int>(umbrella.size());
+                auto after = [&](int t) {
+                    for (int k = 0; k < 3; ++k)
+                        if (T.F[3 * t + k] == vI) return T.F[3 * t + (k + 1) % 3];
+                    return -1;
+                };
+                L.build(T, umbrella);
+                const int lv = L.find(vI);
+                const int nLoc = static_cast<int>(L.gv.size());
+                for (int s = 0; s + 1 < n; ++s) {
+                    const int p0 = after(umbrella[s]);
+                    for (int e = s + 1; e < n; ++e) {
+                        const int p2 = after(umbrella[e]);
+                        // TriMesh::cutPath interior branch (TriMesh.cpp:1449-1475):
+                        // the triangles from edge (vI, p0) round to p2 get the copy
+                        std::vector<int> left;
+                        int vNew = p0;
+                        bool ok = true;
+                        for (int guard = 0; guard <= n; ++guard) {
+                            const int f = T.edge_tri(vI, vNew);
+                            if (f < 0) { ok = false; break; }
+                            left.push_back(f);
+                            vNew = T.third(f, vI, vNew);
+                            if (vNew == p2) break;
+                            if (vNew == p0) { ok = false; break; }
+                        }
+                        if (!ok) continue;
+                        LocalMesh Lc = L;
+                        for (int k = 0; k < n; ++k) {
+                            if (std::find(left.begin(), left.end(), umbrella[k]) == left.end()) continue;
+                            for (int c = 0; c < 3; ++c)
+                                if (Lc.corner[3 * k + c] == lv) Lc.corner[3 * k + c] = nLoc;
+                        }
+                        std::vector<double2> extra{make_double2(in.UV[2 * (size_t)vI], in.UV[2 * (size_t)vI + 1])};
+                        // newVertPos rows: the copy, then vI
+                        std::vector<int> slot(nLoc + 1, -1);
+                        slot[nLoc] = 0;
+                        slot[lv] = 1;
+                        Batch::Tag tg;
+                        tg.cand = static_cast<int>(ci);
+                        tg.a = p0;
+                        tg.b = vI;
+                        tg.c = p2;
+                        tg.se = (rest_dist(in.Vrest, p0, vI) * (1.0 + 1.0) + rest_dist(in.Vrest, vI, p2) * (1.0 + 1.0)) /
+                                R / 2.0;   // seInc (TriMesh.cpp:2246-2247)
+                        tg.nRows = 2;
+                        emit(B, T, in.rest, in.UV, umbrella, Lc, extra, slot, 2, nLoc - 1, tg);
+                    }
+                }
+            }
+        }
+    }
+    else if (opType == kOpMerge) {
+        // TriMesh::queryMerge (TriMesh.cpp:800-930): zipper-bottom pairs
+        std::vector<double> V(in.UV, in.UV + 2 * (size_t)in.nV);
+        const double eps_IC = 1.0e-6 * in.avgEdgeLen;
+        for (int ci = 0; ci < in.nCohE; ++ci) {
+            const int* ce = in.cohE + 4 * (size_t)ci;
+            int fork;
+            if (ce[0] == ce[2]) fork = 0;
+            else if (ce[1] == ce[3]) fork = 1;
+            else continue;
+            const int va = ce[1 - fork], vb = ce[3 - fork];
+            std::vector<int> triangles;
+            int firstAmt = 0;
+            for (int m2 = 0; m2 < 2; ++m2) {
+                const int v = m2 == 0 ? va : vb;
+                for (int p = T.nbPtr[v]; p < T.nbPtr[v + 1]; ++p) {
+                    const int f = T.edge_tri(v, T.nb[p]);
+                    if (f >= 0) triangles.push_back(f);
+                }
+                if (m2 == 0) firstAmt = static_cast<int>(triangles.size());
+            }
+            double mp[2] = {(V[2 * va] + V[2 * vb]) / 2.0, (V[2 * va + 1] + V[2 * vb + 1]) / 2.0};
+            const double b0[2] = {V[2 * va], V[2 * va + 1]}, b1[2] = {V[2 * vb], V[2 * vb + 1]};
+            auto place = [&](const double* p) {
+                V[2 * va] = p[0]; V[2 * va + 1] = p[1];
+                V[2 * vb] = p[0]; V[2 * vb + 1] = p[1];
+            };
+            auto restore = [&]() {
+                V[2 * va] = b0[0]; V[2 * va + 1] = b0[1];
+                V[2 * vb] = b1[0]; V[2 * vb + 1] = b1[1];
+            };
+            place(mp);
+            if (!inverted_any(T, V, triangles)) {
+                restore();
+            }
+            else {
+                // relaxation projection onto the non-inversion half-planes
+                std::vector<double> cm, cv;
+                for (size_t k = 0; k < triangles.size(); ++k) {
+                    const int t = triangles[k];
+                    const int vm = (int)k < firstAmt ? va : vb;
+                    for (int i = 0; i < 3; ++i)
+                        if (T.F[3 * t + i] == vm) {
+                            const int i1 = T.F[3 * t + (i + 1) % 3], i2 = T.F[3 * t + (i + 2) % 3];
+                            const double v1x = V[2 * i1], v1y = V[2 * i1 + 1], v2x = V[2 * i2], v2y = V[2 * i2 + 1];
+                            const double cx = v2y - v1y, cy = v1x - v2x;
+                            const double nrm = std::sqrt(cx * cx + cy * cy);
+                            cm.push_back(cx / nrm);
+                            cm.push_back(cy / nrm);
+                            cv.push_back((v1x * v2y - v1y * v2x) / nrm);
+                            break;
+                        }
+                }
+                for (int iter = 0; iter < 70; ++iter) {
+                    double maxRes = -DBL_MAX;
+                    for (size_t k = 0; k < cv.size(); ++k) {
+                        const double res = cm[2 * k] * mp[0] + cm[2 * k + 1] * mp[1] - cv[k];
+                        if (res > -eps_IC) {
+                            mp[0] -= (res + eps_IC) * cm[2 * k];
+                            mp[1] -= (res + eps_IC) * cm[2 * k + 1];
+                        }
+                        if (res > maxRes) maxRes = res;
+                    }
+                    if (maxRes < 0.0) break;
+                }
+                place(mp);
+                const bool bad = inverted_any(T, V, triangles);
+                restore();
+                if (bad) continue;   // no feasible merged position
+            }
+            const int p0 = fork ? ce[0] : ce[3], p1 = fork ? ce[1] : ce[2], p2 = fork ? ce[2] : ce[1];
+            // seam decrease, closing a split diamond (TriMesh.cpp:2121-2135)
+            double seDec = rest_dist(in.Vrest, p0, p1) / R * (1.0 + 1.0) / 2.0;
+            for (int p = T.nbPtr[p0]; p < T.nbPtr[p0 + 1]; ++p) {
+                const int nbv = T.nb[p];
+                if (nbv != p1 && T.bnd[nbv] && T.adjacent(p2, nbv)) {
+                    seDec += rest_dist(in.Vrest, p0, nbv) / R * (1.0 + 1.0) / 2.0;
+                    break;
+                }
+            }
+            // local mesh with p0 and p2 as one vertex at the merged position
+            L.build(T, triangles, p0, p2);
+            const int lm = L.find(p0);
+            std::vector<int> slot(L.gv.size(), -1);
+            slot[lm] = 0;
+            Batch::Tag tg;
+            tg.cand = static_cast<int>(out.size());
+            tg.a = p0;
+            tg.b = p1;
+            tg.c = p2;
+            tg.se = seDec;
+            tg.nRows = 1;
+            TopoCandidate C;
+            C.path = {p0, p1, p2};
+            C.EwDec = -DBL_MAX;
+            out.push_back(C);
+            const size_t before = B.lvPos.size();
+            emit(B, T, in.rest, in.UV, triangles, L, {}, slot, 1, static_cast<int>(L.gv.size()) - 1, tg);
+            B.lvPos[before + lm] = make_double2(mp[0], mp[1]);   // initMergedPos
+        }
+        candidatePool = in.nCohE;
+    }
+    else {
+        if (err) *err = "topology query: unknown operation";
+        return OC_ERR_INVALID;
+    }
+    stats.nCandidates = static_cast<int>(out.size());
+    stats.nProblems = static_cast<int>(B.prob.size());
+    const auto t1 = clk::now();
+    stats.buildMs = std::chrono::duration<double, std::milli>(t1 - t0).count();
+
+    // one batched device solve
+    std::vector<LocalResult> res(B.prob.size());
+    if (!B.prob.empty()) {
+        LocalBatch db;
+        db.nProb = static_cast<int>(B.prob.size());
+        void* bufs[7] = {};
+        size_t sizes[7] = {sizeof(LocalProblem) * B.prob.size(), sizeof(int) * B.ltGlobal.size(),
+                           sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
+                           sizeof(int) * B.lvSlot.size(), sizeof(int) * B.initTri.size(),
+                           sizeof(LocalResult) * B.prob.size()};
+        const void* src[6] = {B.prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
+                              B.initTri.data()};
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMalloc(&bufs[k], sizes[k] ? sizes[k] : 1);
+        for (int k = 0; k < 6 && e == cudaSuccess; ++k)
+            e = cudaMemcpyAsync(bufs[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
+        if (e == cudaSuccess) {
+            db.prob = static_cast<const LocalProblem*>(bufs[0]);
+            db.ltGlobal = static_cast<const int*>(bufs[1]);
+            db.ltCorner = static_cast<const int*>(bufs[2]);
+            db.lvPos = static_cast<const double2*>(bufs[3]);
+            db.lvSlot = static_cast<const int*>(bufs[4]);
+            db.initTri = static_cast<const int*>(bufs[5]);
+            db.out = static_cast<LocalResult*>(bufs[6]);
+            launch_local_newton(*in.dm, in.surfaceArea, db, in.st);
+            e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(res.data(), bufs[6], sizes[6], cudaMemcpyDeviceToHost, in.st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(in.st);
+        }
+        for (auto* p : bufs) cudaFree(p);
+        if (e != cudaSuccess) {
+            if (err) *err = std::string("topology query: ") + cudaGetErrorString(e);
+            return OC_ERR_CUDA;
+        }
+    }
+    const auto t2 = clk::now();
+    stats.solveMs = std::chrono::duration<double, std::milli>(t2 - t1).count();
+
+    // per candidate: the best of its local problems (strict >, first wins)
+    for (size_t k = 0; k < B.prob.size(); ++k) {
+        const LocalResult& r = res[k];
+        const Batch::Tag& tg = B.tag[k];
+        TopoCandidate& C = out[tg.cand];
+        stats.maxIters = std::max(stats.maxIters, r.iters);
+        stats.totalIters += r.iters;
+        if (r.status != 1) stats.nonConverged++;
+        const double SDDec = r.eDec;
+        double EwDec;
+        if (opType == kOpMerge) {
+            const double SDInc = -SDDec;
+            EwDec = lambda_t * tg.se - (1.0 - lambda_t) * SDInc;   // TriMesh.cpp:2157
+            C.ec0 = SDInc;
+            C.ec1 = -tg.se;
+            C.EwDec = EwDec;
+            C.pos = {r.pos[0].x, r.pos[0].y};
+            continue;
+        }
+        EwDec = (1.0 - lambda_t) * SDDec - lambda_t * tg.se;   // TriMesh.cpp:2187, 2248
+        if (EwDec > C.EwDec) {
+            C.EwDec = EwDec;
+            C.ec0 = -SDDec;
+            C.ec1 = tg.se;
+            C.pos.clear();
+            for (int row = 0; row < tg.nRows; ++row) {
+                C.pos.push_back(r.pos[row].x);
+                C.pos.push_back(r.pos[row].y);
+            }
+            if (opType == kOpBoundarySplit) C.path = {tg.a, tg.b};
+            else C.path = {tg.a, tg.b, tg.c};
+        }
+    }
+    if (opType == kOpInteriorSplit)   // querySplit halves interior-split decreases (TriMesh.cpp:702-704)
+        for (auto& C : out)
+            if (C.EwDec != -DBL_MAX) C.EwDec *= 0.5;
+    for (size_t c = 0; c < out.size(); ++c)
+        if (best < 0 || out[c].EwDec > out[best].EwDec) best = static_cast<int>(c);
+    return OC_OK;
+}
+
+} // namespace oc

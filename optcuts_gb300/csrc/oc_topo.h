@@ -1,0 +1,54 @@
+// Topology queries of the OptCuts outer loop (TriMesh::querySplit /
+// queryMerge, src/TriMesh.cpp:548-951) with every candidate's local
+// projected-Newton solve batched on the device (oc_fp64.cu, k_local_newton).
+#pragma once
+
+#include "oc_internal.h"
+
+#include <string>
+#include <vector>
+
+namespace oc {
+
+enum { kOpBoundarySplit = 0, kOpInteriorSplit = 1, kOpMerge = 2 };
+
+// One candidate as the reference records it in paths_* / newVertPoses_* /
+// energyChanges_* (TriMesh.cpp:688-723, 916-930).
+struct TopoCandidate {
+    std::vector<int> path;      // bSplit: (vI, nbVI); iSplit: (p0, vI, p2); merge: 3-vertex zipper path
+    std::vector<double> pos;    // newVertPos rows x 2
+    double ec0 = 0.0, ec1 = 0.0;   // energyChanges (first, second)
+    double EwDec = 0.0;         // E_w decrease used for the choice (interior splits halved)
+};
+
+struct TopoQueryIn {
+    int nV = 0, nF = 0;
+    const int* F = nullptr;          // nF x 3
+    const double* Vrest = nullptr;   // nV x 3
+    const double* rest = nullptr;    // nF x 8 rest constants (triArea first)
+    const double* UV = nullptr;      // nV x 2 (current)
+    const int* cohE = nullptr;       // nCohE x 4
+    int nCohE = 0;
+    double surfaceArea = 0.0, avgEdgeLen = 0.0, virtualRadius = 0.0;
+    const double* divGrad = nullptr; // nV (split filter)
+    const DeviceMesh* dm = nullptr;  // device copy of the same mesh (rest constants, UV)
+    cudaStream_t st = nullptr;
+};
+
+struct TopoStats {
+    int nCandidates = 0, nProblems = 0, maxIters = 0, totalIters = 0, nonConverged = 0;
+    double buildMs = 0.0, solveMs = 0.0;
+};
+
+// opType: kOpBoundarySplit / kOpInteriorSplit (querySplit with
+// splitInterior false / true) or kOpMerge (queryMerge).  filterExp is the
+// interior-split filter exponent (filterExp_in, 0.6 by default).  best is
+// the index of the largest EwDec (-1 when there is no candidate).
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, std::vector<TopoCandidate>& out,
+               int& best, int& candidatePool, TopoStats& stats, std::string* err);
+
+// the split filter alone (host): candidate vertices in the reference's order
+int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, bool interior, double filterExp,
+                          std::vector<int>& cands, int& pool);
+
+} // namespace oc

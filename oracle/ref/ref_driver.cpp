@@ -23,6 +23,11 @@
 //        time      print wall-clock seconds per Newton iteration
 //        nodump    write only the trace (for timing runs)
 //        scaf      scaffolding on even after a one-point cut of a closed mesh
+//        nobij     bijectivity off (the reference's bijectivity argument 0):
+//                  no scaffold, local topology solves without air meshes
+//        topo      after the Newton loop, run the topology queries the
+//                  outer loop makes (TriMesh::querySplit boundary and
+//                  interior, queryMerge) and dump their candidate lists
 //        scafdump  dump, per iteration, the air mesh the iteration used
 //                  (vertices, triangles, boundary map, fixed air vertices)
 //                  and the augmented gradient / direction of iteration 0
@@ -140,6 +145,7 @@ int main(int argc, char** argv)
     const double lambda_init = std::stod(argv[3]);
     const int iters = std::stoi(argv[4]);
     bool dumpHess = false, dumpStates = false, doTime = false, noDump = false, forceScaf = false, scafDump = false;
+    bool noBij = false, doTopo = false;
     for (int i = 5; i < argc; ++i) {
         if (!std::strcmp(argv[i], "hess")) dumpHess = true;
         else if (!std::strcmp(argv[i], "states")) dumpStates = true;
@@ -147,6 +153,8 @@ int main(int argc, char** argv)
         else if (!std::strcmp(argv[i], "nodump")) noDump = true;
         else if (!std::strcmp(argv[i], "scaf")) forceScaf = true;
         else if (!std::strcmp(argv[i], "scafdump")) scafDump = true;
+        else if (!std::strcmp(argv[i], "nobij")) noBij = true;
+        else if (!std::strcmp(argv[i], "topo")) doTopo = true;
     }
     outputFolderPath = out;
     logFile.open(out + "log.txt");
@@ -235,7 +243,7 @@ int main(int argc, char** argv)
     igl::harmonic(A, M, bnd_stacked, bnd_uv_stacked, 1, UV_Tutte);
     OptCuts::TriMesh mesh(V, F, UV_Tutte, temp.F, false);
 
-    const bool bijective = true;
+    const bool bijective = !noBij;
     std::vector<OptCuts::Energy*> energyTerms;
     std::vector<double> energyParams;
     energyParams.emplace_back(1.0 - lambda_init);
@@ -352,6 +360,52 @@ int main(int argc, char** argv)
     if (dumpStates) {
         const size_t nv = opt.getResult().V.rows();
         write_npy(out + "UV_iters.npy", states.data(), "<f8", 8, {states.size() / (2 * nv), nv, 2});
+    }
+    if (doTopo) {
+        // the topology queries of one outer iteration (main.cpp:1014-1020 ->
+        // Optimizer::createFracture -> TriMesh::splitOrMerge / querySplit)
+        OptCuts::TriMesh& R = opt.getResult();
+        npy_mat(out + "topo_V.npy", R.V);
+        npy_mati(out + "topo_F.npy", R.F);
+        npy_mat(out + "topo_Vrest.npy", R.V_rest);
+        npy_mati(out + "topo_cohE.npy", R.cohE);
+        std::vector<int> fixedT(R.fixedVert.begin(), R.fixedVert.end());
+        npy_veci(out + "topo_fixed.npy", fixedT);
+        OptCuts::SymDirichletEnergy SD;
+        Eigen::VectorXd dg;
+        SD.computeDivGradPerVert(R, dg);
+        npy_vec(out + "topo_divGrad.npy", dg);
+        const double lambda_t = 1.0 - energyParams[0];
+        auto dump = [&](const std::string& tag, const std::vector<std::vector<int>>& paths,
+                        const std::vector<Eigen::MatrixXd>& poses, const std::vector<std::pair<double, double>>& ec) {
+            std::vector<int> pLen, pFlat, vRows;
+            std::vector<double> vFlat, e;
+            for (size_t c = 0; c < paths.size(); ++c) {
+                pLen.push_back((int)paths[c].size());
+                pFlat.insert(pFlat.end(), paths[c].begin(), paths[c].end());
+                const Eigen::MatrixXd& P = c < poses.size() ? poses[c] : Eigen::MatrixXd();
+                vRows.push_back((int)P.rows());
+                for (int r = 0; r < P.rows(); ++r) { vFlat.push_back(P(r, 0)); vFlat.push_back(P(r, 1)); }
+                e.push_back(c < ec.size() ? ec[c].first : 0.0);
+                e.push_back(c < ec.size() ? ec[c].second : 0.0);
+            }
+            npy_veci(out + "topo_" + tag + "_pathLen.npy", pLen);
+            npy_veci(out + "topo_" + tag + "_path.npy", pFlat);
+            npy_veci(out + "topo_" + tag + "_posRows.npy", vRows);
+            npy_vecd(out + "topo_" + tag + "_pos.npy", vFlat);
+            npy_vecd(out + "topo_" + tag + "_energyChanges.npy", e);
+        };
+        double best[3];
+        std::vector<int> bestPath;
+        Eigen::MatrixXd bestPos;
+        std::pair<double, double> bestEc;
+        R.querySplit(lambda_t, false, false, best[0], bestPath, bestPos, bestEc);
+        dump("bSplit", paths_bSplit, newVertPoses_bSplit, energyChanges_bSplit);
+        R.queryMerge(lambda_t, false, best[1], bestPath, bestPos, bestEc);
+        dump("merge", paths_merge, newVertPoses_merge, energyChanges_merge);
+        R.querySplit(lambda_t, false, true, best[2], bestPath, bestPos, bestEc);
+        dump("iSplit", paths_iSplit, newVertPoses_iSplit, energyChanges_iSplit);
+        npy_vecd(out + "topo_best.npy", {best[0], best[1], best[2], lambda_t, (double)inSplitTotalAmt});
     }
     opt.flushEnergyFileOutput();
     opt.flushGradFileOutput();

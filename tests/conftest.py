@@ -36,6 +36,25 @@ def golden():
     return get
 
 
+TOPO_CASES = ["icosphere_320_topo", "sheet_3k_topo", "torus_768_topo", "ellipsoid_2k_topo"]
+
+
+def golden_candidates(g, op):
+    """The reference's candidate list of one topology query: list of dicts
+    with path, newVertPos (rows x 2) and energyChanges."""
+    L = g["topo_%s_pathLen" % op]
+    P = g["topo_%s_path" % op]
+    R = g["topo_%s_posRows" % op]
+    X = g["topo_%s_pos" % op].reshape(-1, 2)
+    E = g["topo_%s_energyChanges" % op].reshape(-1, 2)
+    out, pp, px = [], 0, 0
+    for c in range(len(L)):
+        out.append({"path": P[pp:pp + L[c]].tolist(), "newVertPos": X[px:px + R[c]], "energyChanges": tuple(E[c])})
+        pp += L[c]
+        px += R[c]
+    return out
+
+
 # cases whose golden holds the air mesh of every iteration
 SCAFFOLD_DUMPS = ["triangle", "plane", "torus_768", "sheet_3k", "icosphere_320_scaf"]
 

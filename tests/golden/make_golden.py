@@ -14,6 +14,11 @@ packs its dumps into one compressed .npz per case:
     trace_E, trace_gsq, trace_alpha    per-iteration Optimizer::solve(1) trace
     UV_iters (small cases)             UV after every iteration
     trace_Etot                         energy including the scaffold term
+    topo_*                             topology cases: the converged state,
+                                       split filter and every candidate of
+                                       querySplit (boundary, interior) and
+                                       queryMerge (paths, newVertPos,
+                                       energyChanges)
     scaf_V, scaf_F, scaf_bnd,          scaffold cases: the air mesh each
     scaf_fixed, scaf_off               iteration used (concatenated; scaf_off
                                        rows = nAirV, nAirF, nBnd, nFixed)
@@ -53,6 +58,12 @@ CASES = {
     # closed sphere after its one-point cut with the scaffold forced on
     "sheet_3k": ("sheet_3k", 0.999, 40, 256, True, ["scafdump"]),
     "icosphere_320_scaf": ("icosphere_320", 0.999, 40, None, True, ["scaf", "scafdump"]),
+    # topology queries of one outer iteration after the Newton phase
+    # converged, bijectivity off (the reference's bijectivity argument 0)
+    "icosphere_320_topo": ("icosphere_320", 0.999, 60, 16, False, ["nobij", "topo"]),
+    "sheet_3k_topo": ("sheet_3k", 0.999, 60, 16, False, ["nobij", "topo"]),
+    "torus_768_topo": ("torus_768", 0.999, 60, 16, False, ["nobij", "topo"]),
+    "ellipsoid_2k_topo": ("ellipsoid_2k", 0.999, 300, 16, False, ["nobij", "topo"]),
 }
 
 
@@ -95,6 +106,12 @@ def run_case(name, key, lam, iters, hmax, states, flags):
         if states:
             pack["UV_iters"] = ld("UV_iters")
         pack["trace_Etot"] = ld("trace_Etot")
+        if "topo" in flags:
+            for k in ("V", "F", "Vrest", "cohE", "fixed", "divGrad", "best"):
+                pack["topo_" + k] = ld("topo_" + k)
+            for op in ("bSplit", "merge", "iSplit"):
+                for k in ("pathLen", "path", "posRows", "pos", "energyChanges"):
+                    pack["topo_%s_%s" % (op, k)] = ld("topo_%s_%s" % (op, k))
         if "scafdump" in flags and os.path.exists(out + "scaf_off.npy"):
             for k in ("scaf_V", "scaf_F", "scaf_bnd", "scaf_fixed", "scaf_off", "gradw0"):
                 pack[k] = ld(k)

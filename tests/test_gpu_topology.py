@@ -1,0 +1,71 @@
+"""Topology queries on the GPU (every candidate's local projected-Newton
+solve in one batched launch) against the reference's own queries on the
+same converged state (tests/golden/*_topo, bijectivity off)."""
+import numpy as np
+import pytest
+
+import optcuts_gb300 as oc
+from conftest import TOPO_CASES, golden_candidates
+
+pytestmark = pytest.mark.gpu
+DBL_MAX = np.finfo(np.float64).max
+
+
+def topo_mesh(g):
+    m = oc.TriMesh(g["topo_Vrest"], g["topo_V"], g["topo_F"], g["topo_fixed"])
+    m.setCohesiveEdges(g["topo_cohE"])
+    return m
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_split_filter_bit_exact(golden, case):
+    g = golden(case)
+    np.testing.assert_array_equal(topo_mesh(g).splitFilter(), g["topo_divGrad"])
+
+
+def compare(ours, ref, rel=1e-6):
+    """Same candidates, paths and energy changes; the same new vertex
+    positions except for cut-through boundary splits (4 rows): their local
+    mesh falls apart into two pieces, and a piece held by a single fixed
+    vertex can rotate about it at no energy cost, so where its vertices end
+    up depends on how each LDL^T rounds that singular direction."""
+    assert len(ours["candidates"]) == len(ref)
+    for c, r in zip(ours["candidates"], ref):
+        if r["energyChanges"][0] == DBL_MAX:
+            assert c["EwDec"] == -DBL_MAX
+            continue
+        assert c["path"] == r["path"]
+        for a, b in zip(c["energyChanges"], r["energyChanges"]):
+            assert a == pytest.approx(b, rel=rel, abs=1e-12)
+        assert c["newVertPos"].shape == r["newVertPos"].shape
+        if len(r["newVertPos"]) == 4:
+            continue
+        scale = np.abs(r["newVertPos"]).max() + 1e-12
+        assert np.abs(c["newVertPos"] - r["newVertPos"]).max() <= 1e-5 * scale
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_boundary_split_query(golden, case):
+    g = golden(case)
+    lam_t = g["topo_best"][3]
+    q = topo_mesh(g).querySplit(lam_t, splitInterior=False)
+    compare(q, golden_candidates(g, "bSplit"))
+    assert q["EwDec_max"] == pytest.approx(g["topo_best"][0], rel=1e-6)
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_interior_split_query(golden, case):
+    g = golden(case)
+    lam_t = g["topo_best"][3]
+    q = topo_mesh(g).querySplit(lam_t, splitInterior=True)
+    compare(q, golden_candidates(g, "iSplit"))
+    assert q["EwDec_max"] == pytest.approx(g["topo_best"][2], rel=1e-6)
+    assert q["pool"] == int(g["topo_best"][4])
+    assert q["local_problems"] > len(q["candidates"])
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_merge_query(golden, case):
+    g = golden(case)
+    q = topo_mesh(g).queryMerge(g["topo_best"][3])
+    assert len(q["candidates"]) == len(golden_candidates(g, "merge"))
