@@ -272,6 +272,24 @@ int oc_topo_result_info(const oc_topo_result* r, int* nCand, int* best, int* poo
 int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, double* energyChanges, int* path,
                              int* pathLen, double* newVertPos, int* posRows);
 int oc_topo_result_destroy(oc_topo_result* r);
+/* Optimizer::createFracture(opType, path, newVertPos) (Optimizer.cpp:373-440):
+ * applies the operation to the optimizer's mesh (TriMesh::splitEdgeOnBoundary,
+ * cutPath or mergeBoundaryEdges with their vertex and cohesive-edge
+ * bookkeeping), rebuilds the device mesh and the Newton pattern, rebuilds
+ * the scaffold when one is set (the project's generator) and recomputes
+ * the energy.  path / newVertPos as a query candidate reports them. */
+int oc_optimizer_create_fracture(oc_optimizer* opt, int opType, const int* path, int pathLen,
+                                 const double* newVertPos, int posRows);
+/* the same operation on a mesh alone */
+int oc_mesh_apply_topology(oc_mesh* mesh, int opType, const int* path, int pathLen, const double* newVertPos,
+                           int posRows);
+/* the mesh's current topology: counts, and into non-NULL arrays F, V_rest, cohE */
+int oc_mesh_get_topology(oc_mesh* mesh, int* nV, int* nF, int* nCohE, int* F, double* Vrest, int* cohE);
+/* host only: the operation on plain arrays; outputs hold nV + 2 vertices and
+ * nCohE + 2 cohesive rows at most */
+int oc_topology_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, int nV, int nF,
+                      const int* F, const double* Vrest, const double* UV, int nCohE, const int* cohE, int* F_out,
+                      double* Vrest_out, double* UV_out, int* cohE_out, int* nV_out, int* nCohE_out);
 /* host only: the split filter's candidate vertices, in order */
 int oc_topology_split_candidates(int nV, const int* F, int nF, const double* divGrad, int interior, double filterExp,
                                  int* cands, int* nCands, int* pool);

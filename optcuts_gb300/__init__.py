@@ -106,6 +106,11 @@ _SIGS = {
     "oc_topo_result_info": [_vp, _i, _i, _i, _i, _i, _d, _d],
     "oc_topo_result_candidate": [_vp, ctypes.c_int, _d, _d, _i, _i, _d, _i],
     "oc_topo_result_destroy": [_vp],
+    "oc_optimizer_create_fracture": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
+    "oc_mesh_apply_topology": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
+    "oc_mesh_get_topology": [_vp, _i, _i, _i, _i, _d, _i],
+    "oc_topology_apply": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d,
+                          ctypes.c_int, _i, _i, _d, _d, _i, _i, _i],
     "oc_topology_split_candidates": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_double, _i, _i, _i],
     "oc_optimizer_get_scaffold": [_vp, _i, _i, _i, _d, _i, _i],
     "oc_optimizer_get_last_energy_scaffold": [_vp, _d],
@@ -284,6 +289,22 @@ class TriMesh:
         solve batched on the GPU (bijectivity off)."""
         return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp)
 
+    def applyTopology(self, op, path, newVertPos):
+        """splitEdgeOnBoundary / cutPath / mergeBoundaryEdges on this mesh."""
+        path, pos = _i4(path), _f8(newVertPos).reshape(-1, 2)
+        self.ctx.check(lib().oc_mesh_apply_topology(self.h, op, _pi(path), len(path), _pd(pos), len(pos)),
+                       "applyTopology")
+        self._sync_topology()
+
+    def _sync_topology(self):
+        nv, nf, nc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        lib().oc_mesh_get_topology(self.h, ctypes.byref(nv), ctypes.byref(nf), ctypes.byref(nc), None, None, None)
+        F = np.zeros((nf.value, 3), np.int32)
+        Vr = np.zeros((nv.value, 3))
+        C = np.zeros((nc.value, 4), np.int32)
+        lib().oc_mesh_get_topology(self.h, None, None, None, _pi(F), _pd(Vr), _pi(C))
+        self.nV, self.nF, self.F, self.V_rest, self.cohE = nv.value, nf.value, F, Vr, C
+
     def queryMerge(self, lambda_t):
         """TriMesh::queryMerge(lambda_t, false) (bijectivity off)."""
         return self._query(OP_MERGE, lambda_t, 0.6)
@@ -407,6 +428,23 @@ def energy_w(last_energy, seam_length, virtual_radius, lam):
     return last_energy + lam * seam_length / virtual_radius
 
 
+def topology_apply(op, path, newVertPos, V_rest, UV, F, cohE):
+    """Host-only topology operation (TriMesh::splitEdgeOnBoundary / cutPath /
+    mergeBoundaryEdges) on plain arrays: returns (V_rest, UV, F, cohE)."""
+    path, pos = _i4(path), _f8(newVertPos).reshape(-1, 2)
+    Vr, uv, F = _f8(V_rest), _f8(UV), _i4(F)
+    c = _i4(np.asarray(cohE).reshape(-1, 4))
+    nV = len(Vr)
+    Fo, Vo, Uo = np.zeros_like(F), np.zeros((nV + 2, 3)), np.zeros((nV + 2, 2))
+    Co = np.zeros((len(c) + 2, 4), np.int32)
+    nvo, nco = ctypes.c_int(), ctypes.c_int()
+    rc = lib().oc_topology_apply(op, _pi(path), len(path), _pd(pos), len(pos), nV, len(F), _pi(F), _pd(Vr), _pd(uv),
+                                 len(c), _pi(c), _pi(Fo), _pd(Vo), _pd(Uo), _pi(Co), ctypes.byref(nvo), ctypes.byref(nco))
+    if rc != OC_OK:
+        raise OCError(rc, "topology_apply")
+    return Vo[:nvo.value], Uo[:nvo.value], Fo, Co[:nco.value]
+
+
 def split_candidates(nV, F, divGrad, interior, filterExp=0.6):
     """Host-only split filter (TriMesh.cpp:561-629): candidate vertices in
     the reference's order and the filtered pool size."""
@@ -520,6 +558,13 @@ class Optimizer:
         self.ctx.check(lib().oc_optimizer_set_scaffold(
             self.h, _pd(scaffold.airV), len(scaffold.airV), _pi(scaffold.airF), len(scaffold.airF),
             _pi(scaffold.bnd), len(scaffold.bnd), float(areaThres)), "setScaffold")
+
+    def createFracture(self, op, path, newVertPos):
+        """Optimizer::createFracture(opType, path, newVertPos) (Optimizer.cpp:373-440)."""
+        path, pos = _i4(path), _f8(newVertPos).reshape(-1, 2)
+        self.ctx.check(lib().oc_optimizer_create_fracture(self.h, op, _pi(path), len(path), _pd(pos), len(pos)),
+                       "createFracture")
+        self.data._sync_topology()
 
     def rebuildScaffold(self):
         """Scaffold(result) for the current UV with the project's air-mesh

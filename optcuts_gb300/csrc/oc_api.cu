@@ -74,6 +74,7 @@ struct oc_optimizer {
     // scaffold (the Optimizer's scaffolding branches): an air mesh over the
     // augmented vertex numbering [mesh vertices | air-only vertices]
     // (Scaffold::localVI2Global, Scaffold.cpp:179-184)
+    int nV0 = 0, nFixed0 = 0;       // data0's vertex and fixed counts (targetGRes)
     bool scaf = false, patternStale = true, airContribStale = false, cliqueMode = false;
     oc::DeviceMesh air;
     // nWhole: system vertices incl. unused air slots (nV + capAir);
@@ -672,6 +673,77 @@ int oc_sd_init_step_size(oc_mesh* m, const double* searchDir, double* stepSize)
 }
 
 // ------------------------------------------------------------------ topology
+// Re-derives the device mesh from its host topology after an operation
+// (TriMesh::computeFeatures, TriMesh.cpp:343-518): rest constants, scalars,
+// corner lists; UV from uvHost.
+static int mesh_rebuild(oc_mesh* m, const std::vector<double>& uvHost)
+{
+    oc_ctx* ctx = m->ctx;
+    const int nV = static_cast<int>(m->Vrest.size() / 3), nF = static_cast<int>(m->F.size() / 3);
+    double surfaceArea = 0.0;
+    std::vector<double> rest;
+    if (!rest_constants(m->Vrest.data(), m->F.data(), nF, 0.0, rest, surfaceArea))
+        return fail(ctx, OC_ERR_DEGENERATE, "topology op: zero-area rest triangle");
+    m->rest.swap(rest);
+    double avg = 0.0;
+    const double* Vr = m->Vrest.data();
+    const int* F = m->F.data();
+    for (int t = 0; t < nF; ++t)
+        for (int j = 0; j < 3; ++j) {
+            const double* p = Vr + 3 * (size_t)F[3 * t + j];
+            const double* q = Vr + 3 * (size_t)F[3 * t + (j + 1) % 3];
+            avg += std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]));
+        }
+    m->scalars[0] = surfaceArea;
+    m->scalars[1] = avg / (3.0 * nF);
+    m->scalars[2] = std::sqrt(surfaceArea / M_PI);
+    std::vector<unsigned char> mask(nV, 0);
+    for (int v : m->fixed)
+        if (v < nV) mask[v] = 1;
+    const int oldNV = m->d.nV;
+    int rc = device_mesh_upload(ctx, m->d, nV, F, nF, m->rest, surfaceArea, mask);
+    if (rc) return rc;
+    if (nV != oldNV) {
+        cudaFree(m->d.uv); cudaFree(m->tmpV); cudaFree(m->divGrad);
+        m->d.uv = nullptr; m->tmpV = nullptr; m->divGrad = nullptr;
+        OC_CUDA(ctx, dalloc(&m->d.uv, nV));
+        OC_CUDA(ctx, dalloc(&m->tmpV, nV));
+    }
+    OC_CUDA(ctx, cudaMemcpyAsync(m->d.uv, uvHost.data(), sizeof(double2) * nV, cudaMemcpyHostToDevice, ctx->stream));
+    OC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return OC_OK;
+}
+
+int oc_mesh_apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, const double* newVertPos, int posRows)
+{
+    if (!m || !path || !newVertPos) return OC_ERR_INVALID;
+    std::vector<double> uv(2 * (size_t)m->d.nV);
+    OC_CUDA(m->ctx, cudaMemcpyAsync(uv.data(), m->d.uv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToHost,
+                                    m->ctx->stream));
+    OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+    std::vector<int> F(m->F), cohE(m->cohE);
+    std::vector<double> Vrest(m->Vrest);
+    std::string err;
+    int rc = oc::topo_apply(opType, path, pathLen, newVertPos, posRows, F, Vrest, uv, cohE, &err);
+    if (rc) return fail(m->ctx, rc, err);
+    m->F.swap(F);
+    m->Vrest.swap(Vrest);
+    m->cohE.swap(cohE);
+    return mesh_rebuild(m, uv);
+}
+
+int oc_mesh_get_topology(oc_mesh* m, int* nV, int* nF, int* nCohE, int* F, double* Vrest, int* cohE)
+{
+    if (!m) return OC_ERR_INVALID;
+    if (nV) *nV = m->d.nV;
+    if (nF) *nF = m->d.nF;
+    if (nCohE) *nCohE = static_cast<int>(m->cohE.size() / 4);
+    if (F) std::copy(m->F.begin(), m->F.end(), F);
+    if (Vrest) std::copy(m->Vrest.begin(), m->Vrest.end(), Vrest);
+    if (cohE) std::copy(m->cohE.begin(), m->cohE.end(), cohE);
+    return OC_OK;
+}
+
 int oc_mesh_set_cohesive_edges(oc_mesh* m, const int* cohE, int nCohE)
 {
     if (!m || nCohE < 0 || (nCohE && !cohE)) return OC_ERR_INVALID;
@@ -780,6 +852,28 @@ int oc_topology_split_candidates(int nV, const int* F, int nF, const double* div
     if (cands) std::copy(c.begin(), c.end(), cands);
     *nCands = static_cast<int>(c.size());
     if (pool) *pool = p;
+    return OC_OK;
+}
+
+int oc_topology_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, int nV, int nF,
+                      const int* F, const double* Vrest, const double* UV, int nCohE, const int* cohE, int* F_out,
+                      double* Vrest_out, double* UV_out, int* cohE_out, int* nV_out, int* nCohE_out)
+{
+    if (nV <= 0 || nF <= 0 || !F || !Vrest || !UV || nCohE < 0 || (nCohE && !cohE) || !F_out || !Vrest_out ||
+        !UV_out || !nV_out || !nCohE_out)
+        return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
+    std::vector<int> f(F, F + 3 * (size_t)nF), c(cohE, cohE + 4 * (size_t)nCohE);
+    std::vector<double> vr(Vrest, Vrest + 3 * (size_t)nV), uv(UV, UV + 2 * (size_t)nV);
+    const int rc = oc::topo_apply(opType, path, pathLen, newVertPos, posRows, f, vr, uv, c, nullptr);
+    if (rc) return rc;
+    std::copy(f.begin(), f.end(), F_out);
+    std::copy(vr.begin(), vr.end(), Vrest_out);
+    std::copy(uv.begin(), uv.end(), UV_out);
+    if (cohE_out) std::copy(c.begin(), c.end(), cohE_out);
+    *nV_out = static_cast<int>(uv.size() / 2);
+    *nCohE_out = static_cast<int>(c.size() / 4);
     return OC_OK;
 }
 
@@ -1011,6 +1105,8 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
     o->param = energyParam;
     o->wScaf = energyParam * 0.01;   // w_scaf, fixed at construction (Optimizer.cpp:87)
     o->nWhole = o->nWholeReal = o->capWhole = mesh->d.nV;
+    o->nV0 = mesh->d.nV;
+    o->nFixed0 = static_cast<int>(mesh->fixed.size());
     if (cfg) o->cfg = *cfg;
     else oc_optimizer_default_config(&o->cfg);
     if (!(o->cfg.pcgTol > 0.0)) o->cfg.pcgTol = 1e-8;
@@ -1053,9 +1149,9 @@ int oc_optimizer_destroy(oc_optimizer* o)
 static void update_target_gres(oc_optimizer* o)
 {
     // Optimizer::updateTargetGRes (Optimizer.cpp:675-678)
-    const oc_mesh* m = o->mesh;
-    o->targetGRes = o->param * static_cast<double>(m->d.nV - (int)m->fixed.size()) / static_cast<double>(m->d.nV) *
-                    o->relGL2Tol;
+    // data0 is the mesh the Optimizer was constructed with: topology
+    // operations on `result` leave this target unchanged
+    o->targetGRes = o->param * static_cast<double>(o->nV0 - o->nFixed0) / static_cast<double>(o->nV0) * o->relGL2Tol;
 }
 
 // the mesh as the optimizer's kernels see it: with a scaffold, its UV is the
@@ -1554,6 +1650,30 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     if (!samePattern) o->patternStale = true;
     o->airContribStale = true;
     return OC_OK;
+}
+
+int oc_optimizer_create_fracture(oc_optimizer* o, int opType, const int* path, int pathLen, const double* newVertPos,
+                                 int posRows)
+{
+    // Optimizer::createFracture(opType, path, newVertPos, ...) (Optimizer.cpp:373-440)
+    if (!o || !o->precomputed) return OC_ERR_INVALID;
+    oc_mesh* m = o->mesh;
+    int rc = oc_mesh_apply_topology(m, opType, path, pathLen, newVertPos, posRows);
+    if (rc) return rc;
+    const int nV = m->d.nV;
+    rc = ensure_whole(o, nV);
+    if (rc) return rc;
+    if (!o->scaf) o->nWhole = o->nWholeReal = nV;
+    o->patternStale = true;
+    if (o->scaf) {   // scaffold = Scaffold(result, ...) (:416-421)
+        rc = oc_optimizer_rebuild_scaffold(o);
+        if (rc) return rc;
+    }
+    rc = ensure_pattern(o);   // updateEnergyData(true, false, true) (:423-425)
+    if (rc) return rc;
+    if (o->scaf)
+        OC_CUDA(m->ctx, cudaMemcpyAsync(o->wuv, m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToDevice, m->ctx->stream));
+    return compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
 }
 
 int oc_optimizer_rebuild_scaffold(oc_optimizer* o)

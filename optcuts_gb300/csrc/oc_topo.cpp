@@ -229,6 +229,229 @@ bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector
 
 } // namespace
 
+namespace {
+
+// TriMesh::cohEIndex as computeFeatures builds it (TriMesh.cpp:448-455):
+// (c0, c1) -> row, (c3, c2) -> -row - 1, rows without a -1 entry only
+std::vector<std::pair<std::pair<int, int>, int>> coh_index(const std::vector<int>& cohE)
+{
+    std::vector<std::pair<std::pair<int, int>, int>> idx;
+    for (size_t i = 0; i < cohE.size() / 4; ++i) {
+        const int* c = &cohE[4 * i];
+        if (std::min(std::min(c[0], c[1]), std::min(c[2], c[3])) < 0) continue;
+        idx.push_back({{c[0], c[1]}, static_cast<int>(i)});
+        idx.push_back({{c[3], c[2]}, -static_cast<int>(i) - 1});
+    }
+    return idx;
+}
+
+int* coh_find(std::vector<std::pair<std::pair<int, int>, int>>& idx, int a, int b)
+{
+    for (auto it = idx.rbegin(); it != idx.rend(); ++it)   // a std::map keeps the last assignment
+        if (it->first.first == a && it->first.second == b) return &it->second;
+    return nullptr;
+}
+
+void coh_set(std::vector<std::pair<std::pair<int, int>, int>>& idx, int a, int b, int v)
+{
+    if (int* p = coh_find(idx, a, b)) *p = v;
+    else idx.push_back({{a, b}, v});
+}
+
+void coh_erase(std::vector<std::pair<std::pair<int, int>, int>>& idx, int a, int b)
+{
+    idx.erase(std::remove_if(idx.begin(), idx.end(),
+                             [&](const std::pair<std::pair<int, int>, int>& e) {
+                                 return e.first.first == a && e.first.second == b;
+                             }),
+              idx.end());
+}
+
+// TriMesh::isBoundaryVert(vI, vNb, tris, boundaryEdge, toBound) with its
+// boundaryEdge output
+bool walk_edge(const Topo& T, int vI, int vNb, bool toBound, std::vector<int>& tris, int bEdge[2])
+{
+    tris.clear();
+    int f = toBound ? T.edge_tri(vNb, vI) : T.edge_tri(vI, vNb);
+    if (f < 0) {
+        bEdge[0] = toBound ? vI : vNb;
+        bEdge[1] = toBound ? vNb : vI;
+        return true;
+    }
+    int vNew = vNb;
+    for (int guard = 0; guard <= T.nF; ++guard) {
+        tris.push_back(f);
+        vNew = T.third(f, vI, vNew);
+        if (vNew == vNb) return false;
+        f = toBound ? T.edge_tri(vNew, vI) : T.edge_tri(vI, vNew);
+        if (f < 0) {
+            bEdge[0] = toBound ? vI : vNew;
+            bEdge[1] = toBound ? vNew : vI;
+            return true;
+        }
+    }
+    return false;
+}
+
+void replace_in(std::vector<int>& F, const std::vector<int>& tris, int from, int to)
+{
+    for (int t : tris)
+        for (int k = 0; k < 3; ++k)
+            if (F[3 * (size_t)t + k] == from) {
+                F[3 * (size_t)t + k] = to;
+                break;
+            }
+}
+
+} // namespace
+
+int topo_apply(int opType, const int* path, int pathLen, const double* pos, int posRows, std::vector<int>& F,
+               std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err)
+{
+    auto bad = [&](const char* m) {
+        if (err) *err = m;
+        return OC_ERR_INVALID;
+    };
+    const int nV = static_cast<int>(Vrest.size() / 3), nF = static_cast<int>(F.size() / 3);
+    if (!path || !pos) return bad("topology op: bad arguments");
+    for (int i = 0; i < pathLen; ++i)
+        if (path[i] < 0 || path[i] >= nV) return bad("topology op: path vertex out of range");
+    Topo T;
+    T.build(nV, F.data(), nF);
+    auto push_vertex = [&](int copyOf, const double* uv) {
+        Vrest.insert(Vrest.end(), {Vrest[3 * (size_t)copyOf], Vrest[3 * (size_t)copyOf + 1], Vrest[3 * (size_t)copyOf + 2]});
+        UV.insert(UV.end(), {uv[0], uv[1]});
+        return static_cast<int>(UV.size() / 2) - 1;
+    };
+    if (opType == kOpBoundarySplit) {
+        // TriMesh::splitEdgeOnBoundary(edge, newVertPos) (TriMesh.cpp:2864-3036)
+        if (pathLen != 2) return bad("boundary split: path must be an edge");
+        if (T.edge_tri(path[0], path[1]) < 0 || T.edge_tri(path[1], path[0]) < 0)
+            return bad("boundary split: not an interior edge");
+        int vb = path[0], vi = path[1];
+        bool both = false;
+        if (T.bnd[path[0]]) {
+            if (T.bnd[path[1]]) both = true;
+        }
+        else {
+            if (!T.bnd[path[1]]) return bad("boundary split: the edge does not touch the boundary");
+            vb = path[1];
+            vi = path[0];
+        }
+        if (posRows != (both ? 4 : 2)) return bad("boundary split: wrong number of new positions");
+        std::vector<int> sepB, sepI;
+        int bEb[2] = {-1, -1}, bEi[2] = {-1, -1};
+        walk_edge(T, vb, vi, true, sepB, bEb);
+        if (both) walk_edge(T, vi, vb, true, sepI, bEi);
+        auto idx = coh_index(cohE);
+        const int nb = push_vertex(vb, pos + 2);
+        UV[2 * (size_t)vb] = pos[0];
+        UV[2 * (size_t)vb + 1] = pos[1];
+        replace_in(F, sepB, vb, nb);
+        const int nCE = static_cast<int>(cohE.size() / 4);
+        cohE.insert(cohE.end(), {vi, nb, vi, vb});
+        coh_set(idx, vi, nb, nCE);
+        coh_set(idx, vb, vi, -nCE - 1);
+        if (int* f = coh_find(idx, bEb[0], bEb[1])) {
+            const int r = *f;
+            if (r >= 0) cohE[4 * (size_t)r] = nb;
+            else cohE[4 * (size_t)(-r - 1) + 3] = nb;
+            coh_erase(idx, bEb[0], bEb[1]);
+            coh_set(idx, nb, bEb[1], r);
+        }
+        if (both) {
+            const int ni = push_vertex(vi, pos + 4);
+            UV[2 * (size_t)vi] = pos[6];
+            UV[2 * (size_t)vi + 1] = pos[7];
+            replace_in(F, sepI, vi, ni);
+            cohE[4 * (size_t)nCE + 2] = ni;
+            coh_erase(idx, vb, vi);
+            coh_set(idx, vb, ni, -nCE - 1);
+            if (int* f = coh_find(idx, bEi[0], bEi[1])) {
+                const int r = *f;
+                if (r >= 0) cohE[4 * (size_t)r] = ni;
+                else cohE[4 * (size_t)(-r - 1) + 3] = ni;
+            }
+        }
+        return OC_OK;
+    }
+    if (opType == kOpInteriorSplit) {
+        // TriMesh::cutPath(path, true, 1, newVertPos), interior branch (TriMesh.cpp:1449-1500)
+        if (pathLen != 3 || posRows != 2) return bad("interior split: path of 3 vertices and 2 positions expected");
+        const int vI = path[1];
+        std::vector<int> left;
+        int vNew = path[0];
+        for (int guard = 0;; ++guard) {
+            const int f = T.edge_tri(vI, vNew);
+            if (f < 0 || guard > nF) return bad("interior split: not a valid path");
+            left.push_back(f);
+            vNew = T.third(f, vI, vNew);
+            if (vNew == path[2]) break;
+            if (vNew == path[0]) return bad("interior split: not a valid path");
+        }
+        const int nn = push_vertex(vI, pos);
+        UV[2 * (size_t)vI] = pos[2];
+        UV[2 * (size_t)vI + 1] = pos[3];
+        replace_in(F, left, vI, nn);
+        cohE.insert(cohE.end(), {nn, path[0], vI, path[0]});
+        cohE.insert(cohE.end(), {path[2], nn, path[2], vI});
+        return OC_OK;
+    }
+    if (opType == kOpMerge) {
+        // TriMesh::mergeBoundaryEdges((p0, p1), (p1, p2), newVertPos.row(0)) (TriMesh.cpp:3038-3180)
+        if (pathLen != 3 || posRows < 1) return bad("merge: path of 3 vertices expected");
+        const int a = path[0], b = path[2];
+        if (T.edge_tri(path[1], path[0]) >= 0 || T.edge_tri(path[2], path[1]) >= 0)
+            return bad("merge: the edges are not boundary edges");
+        auto idx = coh_index(cohE);
+        int* ci = coh_find(idx, path[0], path[1]);
+        if (!ci) return bad("merge: the edge is not a cohesive edge");
+        const int cRow = *ci;
+        UV[2 * (size_t)a] = pos[0];
+        UV[2 * (size_t)a + 1] = pos[1];
+        const int back = nV - 1;
+        if (b < back) {
+            for (int k = 0; k < 3; ++k) Vrest[3 * (size_t)b + k] = Vrest[3 * (size_t)back + k];
+            UV[2 * (size_t)b] = UV[2 * (size_t)back];
+            UV[2 * (size_t)b + 1] = UV[2 * (size_t)back + 1];
+        }
+        Vrest.resize(3 * (size_t)back);
+        UV.resize(2 * (size_t)back);
+        for (int t = 0; t < nF; ++t)
+            for (int k = 0; k < 3; ++k)
+                if (F[3 * (size_t)t + k] == b) {
+                    F[3 * (size_t)t + k] = a;
+                    break;
+                }
+        if (b < back)
+            for (size_t i = 0; i < F.size(); ++i)
+                if (F[i] == back) F[i] = b;
+        const int nC = static_cast<int>(cohE.size() / 4), cBack = nC - 1;
+        const int row = cRow >= 0 ? cRow : -cRow - 1;
+        if (row < cBack)
+            for (int k = 0; k < 4; ++k) cohE[4 * (size_t)row + k] = cohE[4 * (size_t)cBack + k];
+        cohE.resize(4 * (size_t)cBack);
+        for (int& c : cohE)
+            if (c == b) c = a;
+        if (b < back)
+            for (int& c : cohE)
+                if (c == back) c = b;
+        // close up a diamond that became whole
+        for (size_t i = 0; i < cohE.size() / 4; ++i) {
+            int* c = &cohE[4 * i];
+            if (c[0] == c[2] && c[1] == c[3]) {
+                const size_t last = cohE.size() / 4 - 1;
+                if (i < last)
+                    for (int k = 0; k < 4; ++k) c[k] = cohE[4 * last + k];
+                cohE.resize(4 * last);
+                break;
+            }
+        }
+        return OC_OK;
+    }
+    return bad("topology op: unknown operation");
+}
+
 int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, bool interior, double filterExp,
                           std::vector<int>& cands, int& pool)
 {

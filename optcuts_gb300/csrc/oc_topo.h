@@ -47,6 +47,15 @@ struct TopoStats {
 int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, std::vector<TopoCandidate>& out,
                int& best, int& candidatePool, TopoStats& stats, std::string* err);
 
+// Applies one operation to host arrays (F nF x 3, Vrest nV x 3, UV nV x 2,
+// cohE rows x 4) with the reference's vertex and cohesive-edge bookkeeping:
+// boundary split TriMesh::splitEdgeOnBoundary (new vertices appended),
+// interior split TriMesh::cutPath (one appended vertex, two cohesive rows),
+// merge TriMesh::mergeBoundaryEdges (the merged copy removed by moving the
+// last vertex into its slot).
+int topo_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, std::vector<int>& F,
+               std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err);
+
 // the split filter alone (host): candidate vertices in the reference's order
 int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, bool interior, double filterExp,
                           std::vector<int>& cands, int& pool);

@@ -396,16 +396,56 @@ int main(int argc, char** argv)
             npy_vecd(out + "topo_" + tag + "_energyChanges.npy", e);
         };
         double best[3];
-        std::vector<int> bestPath;
-        Eigen::MatrixXd bestPos;
+        std::vector<int> bestPath, pathB, pathI;
+        Eigen::MatrixXd bestPos, posB, posI;
         std::pair<double, double> bestEc;
-        R.querySplit(lambda_t, false, false, best[0], bestPath, bestPos, bestEc);
+        R.querySplit(lambda_t, false, false, best[0], pathB, posB, bestEc);
         dump("bSplit", paths_bSplit, newVertPoses_bSplit, energyChanges_bSplit);
         R.queryMerge(lambda_t, false, best[1], bestPath, bestPos, bestEc);
         dump("merge", paths_merge, newVertPoses_merge, energyChanges_merge);
-        R.querySplit(lambda_t, false, true, best[2], bestPath, bestPos, bestEc);
+        R.querySplit(lambda_t, false, true, best[2], pathI, posI, bestEc);
         dump("iSplit", paths_iSplit, newVertPoses_iSplit, energyChanges_iSplit);
         npy_vecd(out + "topo_best.npy", {best[0], best[1], best[2], lambda_t, (double)inSplitTotalAmt});
+        // the operations themselves, applied to copies whatever their E_w
+        // change (Optimizer::createFracture, Optimizer.cpp:373-440): the best
+        // boundary split (then the merge query on that state and its best
+        // merge) and the best interior split
+        auto dumpState = [&](const std::string& tag, const OptCuts::TriMesh& M) {
+            npy_mat(out + "topo_" + tag + "_V.npy", M.V);
+            npy_mati(out + "topo_" + tag + "_F.npy", M.F);
+            npy_mat(out + "topo_" + tag + "_Vrest.npy", M.V_rest);
+            npy_mati(out + "topo_" + tag + "_cohE.npy", M.cohE);
+        };
+        npy_veci(out + "topo_opB_path.npy", pathB);
+        npy_mat(out + "topo_opB_pos.npy", posB);
+        npy_veci(out + "topo_opI_path.npy", pathI);
+        npy_mat(out + "topo_opI_pos.npy", posI);
+        if (best[0] > -1e300) {
+            OptCuts::TriMesh Rb = R;
+            Rb.splitEdgeOnBoundary(std::pair<int, int>(pathB[0], pathB[1]), posB);
+            Rb.updateFeatures();
+            dumpState("afterB", Rb);
+            Rb.computeFeatures();   // as the next outer iteration sees it
+            double bm;
+            std::vector<int> pathM;
+            Eigen::MatrixXd posM;
+            Rb.queryMerge(lambda_t, false, bm, pathM, posM, bestEc);
+            dump("mergeB", paths_merge, newVertPoses_merge, energyChanges_merge);
+            npy_vecd(out + "topo_mergeB_best.npy", {bm});
+            if (bm > -1e300) {
+                npy_veci(out + "topo_opM_path.npy", pathM);
+                npy_mat(out + "topo_opM_pos.npy", posM);
+                Rb.mergeBoundaryEdges(std::pair<int, int>(pathM[0], pathM[1]), std::pair<int, int>(pathM[1], pathM[2]),
+                                      posM.row(0));
+                Rb.computeFeatures();
+                dumpState("afterM", Rb);
+            }
+        }
+        if (best[2] > -1e300) {
+            OptCuts::TriMesh Ri = R;
+            Ri.cutPath(pathI, true, 1, posI);
+            dumpState("afterI", Ri);
+        }
     }
     opt.flushEnergyFileOutput();
     opt.flushGradFileOutput();

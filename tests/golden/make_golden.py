@@ -109,9 +109,17 @@ def run_case(name, key, lam, iters, hmax, states, flags):
         if "topo" in flags:
             for k in ("V", "F", "Vrest", "cohE", "fixed", "divGrad", "best"):
                 pack["topo_" + k] = ld("topo_" + k)
-            for op in ("bSplit", "merge", "iSplit"):
+            for op in ("bSplit", "merge", "iSplit", "mergeB"):
                 for k in ("pathLen", "path", "posRows", "pos", "energyChanges"):
-                    pack["topo_%s_%s" % (op, k)] = ld("topo_%s_%s" % (op, k))
+                    if os.path.exists(out + "topo_%s_%s.npy" % (op, k)):
+                        pack["topo_%s_%s" % (op, k)] = ld("topo_%s_%s" % (op, k))
+            for k in ("opB_path", "opB_pos", "opI_path", "opI_pos", "opM_path", "opM_pos", "mergeB_best"):
+                if os.path.exists(out + "topo_%s.npy" % k):
+                    pack["topo_" + k] = ld("topo_" + k)
+            for st in ("afterB", "afterI", "afterM"):
+                for k in ("V", "F", "Vrest", "cohE"):
+                    if os.path.exists(out + "topo_%s_%s.npy" % (st, k)):
+                        pack["topo_%s_%s" % (st, k)] = ld("topo_%s_%s" % (st, k))
         if "scafdump" in flags and os.path.exists(out + "scaf_off.npy"):
             for k in ("scaf_V", "scaf_F", "scaf_bnd", "scaf_fixed", "scaf_off", "gradw0"):
                 pack[k] = ld(k)

@@ -69,3 +69,41 @@ def test_merge_query(golden, case):
     g = golden(case)
     q = topo_mesh(g).queryMerge(g["topo_best"][3])
     assert len(q["candidates"]) == len(golden_candidates(g, "merge"))
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_merge_query_after_split(golden, case):
+    """queryMerge on the state after the reference applied its best boundary
+    split: the new zipper-bottom pair (undoing that split) and any others."""
+    g = golden(case)
+    m = oc.TriMesh(g["topo_afterB_Vrest"], g["topo_afterB_V"], g["topo_afterB_F"], g["topo_fixed"])
+    m.setCohesiveEdges(g["topo_afterB_cohE"])
+    q = m.queryMerge(g["topo_best"][3])
+    compare(q, golden_candidates(g, "mergeB"))
+    assert q["EwDec_max"] == pytest.approx(float(g["topo_mergeB_best"][0]), rel=1e-6)
+
+
+@pytest.mark.parametrize("case", ["icosphere_320_topo", "sheet_3k_topo"])
+def test_create_fracture_through_the_optimizer(golden, case):
+    """Optimizer::createFracture with a queried boundary split: the mesh
+    takes the reference's new topology, the energy is recomputed, and Newton
+    continues without inverting anything."""
+    g = golden(case)
+    m = topo_mesh(g)
+    par = 1.0 - g["topo_best"][3]
+    opt = oc.Optimizer(m, [par])
+    opt.precompute()
+    q = m.querySplit(g["topo_best"][3], splitInterior=False)
+    c = q["candidates"][q["best"]]
+    assert c["path"] == list(g["topo_opB_path"])
+    opt.createFracture(oc.OP_BOUNDARY_SPLIT, g["topo_opB_path"], g["topo_opB_pos"])
+    np.testing.assert_array_equal(m.F, g["topo_afterB_F"])
+    np.testing.assert_array_equal(m.cohE, g["topo_afterB_cohE"].reshape(-1, 4))
+    np.testing.assert_array_equal(m.V, g["topo_afterB_V"])
+    e = opt.getLastEnergyVal()
+    assert e == pytest.approx(par * oc.SymDirichletEnergy().computeEnergyVal(m), rel=1e-13)
+    for _ in range(5):
+        opt.solve(1)
+        assert opt.getLastEnergyVal() <= e
+        e = opt.getLastEnergyVal()
+    assert m.checkInversion()

@@ -45,3 +45,59 @@ def test_candidate_counts_follow_the_filter_exponents(golden):
     assert len(c_b) == max(2, int(pool_b ** 0.8))
     c_in2, _ = oc.split_candidates(nV, g["topo_F"], g["topo_divGrad"], True, 0.8)
     assert len(c_in2) == max(2, int(pool_in ** 0.8)) and list(c_in2[:len(c_in)]) == list(c_in)
+
+
+def state(g, tag):
+    return (g["topo_%s_Vrest" % tag], g["topo_%s_V" % tag], g["topo_%s_F" % tag], g["topo_%s_cohE" % tag].reshape(-1, 4))
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_boundary_split_apply_matches_reference(golden, case):
+    """TriMesh::splitEdgeOnBoundary with the reference's chosen edge and new
+    positions: identical F, V_rest, UV and cohesive edges."""
+    g = golden(case)
+    Vr, UV, F, C = oc.topology_apply(oc.OP_BOUNDARY_SPLIT, g["topo_opB_path"], g["topo_opB_pos"], g["topo_Vrest"],
+                                     g["topo_V"], g["topo_F"], g["topo_cohE"])
+    rVr, rUV, rF, rC = state(g, "afterB")
+    np.testing.assert_array_equal(F, rF)
+    np.testing.assert_array_equal(Vr, rVr)
+    np.testing.assert_array_equal(UV, rUV)
+    np.testing.assert_array_equal(C, rC)
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_interior_split_apply_matches_reference(golden, case):
+    g = golden(case)
+    Vr, UV, F, C = oc.topology_apply(oc.OP_INTERIOR_SPLIT, g["topo_opI_path"], g["topo_opI_pos"], g["topo_Vrest"],
+                                     g["topo_V"], g["topo_F"], g["topo_cohE"])
+    rVr, rUV, rF, rC = state(g, "afterI")
+    np.testing.assert_array_equal(F, rF)
+    np.testing.assert_array_equal(Vr, rVr)
+    np.testing.assert_array_equal(UV, rUV)
+    np.testing.assert_array_equal(C, rC)
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_merge_apply_matches_reference(golden, case):
+    """TriMesh::mergeBoundaryEdges on the split state, with the reference's
+    best merge (vertex removal by moving the last vertex, cohesive rows)."""
+    g = golden(case)
+    bVr, bUV, bF, bC = state(g, "afterB")
+    Vr, UV, F, C = oc.topology_apply(oc.OP_MERGE, g["topo_opM_path"], g["topo_opM_pos"], bVr, bUV, bF, bC)
+    rVr, rUV, rF, rC = state(g, "afterM")
+    np.testing.assert_array_equal(F, rF)
+    np.testing.assert_array_equal(Vr, rVr)
+    np.testing.assert_array_equal(UV, rUV)
+    np.testing.assert_array_equal(C, rC)
+
+
+def test_bad_operations_rejected(golden):
+    g = golden("icosphere_320_topo")
+    with pytest.raises(oc.OCError):   # an interior vertex's edge does not touch the boundary
+        v = int(g["topo_opI_path"][1])
+        nb = int(g["topo_opI_path"][0])
+        oc.topology_apply(oc.OP_BOUNDARY_SPLIT, [v, nb], np.zeros((2, 2)), g["topo_Vrest"], g["topo_V"],
+                          g["topo_F"], g["topo_cohE"])
+    with pytest.raises(oc.OCError):
+        oc.topology_apply(oc.OP_INTERIOR_SPLIT, [0, 1], np.zeros((2, 2)), g["topo_Vrest"], g["topo_V"],
+                          g["topo_F"], g["topo_cohE"])
