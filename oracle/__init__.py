@@ -28,16 +28,14 @@ _lib = None
 
 
 def build(force=False):
-    src = os.path.join(_HERE, "port", "oc_oracle.cpp")
-    if (not force and os.path.exists(_SO)
-            and os.path.getmtime(_SO) >= os.path.getmtime(src)
-            and os.path.getmtime(_SO) >= os.path.getmtime(os.path.join(_HERE, "port", "oc_oracle.h"))
-            and os.path.getmtime(_SO) >= os.path.getmtime(os.path.abspath(__file__))):
+    srcs = [os.path.join(_HERE, "port", f) for f in ("oc_oracle.cpp", "oc_topo_oracle.cpp")]
+    inputs = srcs + [os.path.join(_HERE, "port", "oc_oracle.h"), os.path.abspath(__file__)]
+    if not force and os.path.exists(_SO) and all(os.path.getmtime(_SO) >= os.path.getmtime(p) for p in inputs):
         return _SO
     os.makedirs(_BUILD, exist_ok=True)
     tmp = _SO + ".tmp%d" % os.getpid()
     # -ffp-contract=off: aarch64 GCC would fuse multiply-adds and change rounding
-    subprocess.check_call(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", src,
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", *srcs,
                            "-o", tmp])
     os.replace(tmp, _SO)
     return _SO
@@ -80,6 +78,9 @@ def lib():
                                  ctypes.POINTER(NewtonOpts), _d, _d, _d, _d, _i]
         L.ocr_newton_scaffold.argtypes = [_d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, _d,
                                           ctypes.POINTER(NewtonOpts), ctypes.POINTER(ScaffoldArgs), _d, _d, _d, _d, _i]
+        L.ocr_topology_query.argtypes = [ctypes.c_int, _i, ctypes.c_int, _d, _d, _i, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _d, _d, _i, _d,
+                                         _i, _i, _d]
         _lib = L
     return _lib
 
@@ -198,3 +199,26 @@ def newton(V_rest, F, fixed, UV, energy_param, iters, rel_gl2_tol=1e-12, threads
     if n < 0:
         raise ArithmeticError("factorization failed")
     return UV, {"E": tE[:n + 1], "gsq": tG[:n], "alpha": tA[:n], "seconds": tS[:n]}, int(st[0])
+
+
+def topology_query(V_rest, UV, F, cohE, op, lambda_t, filter_exp=0.6, threads=1, max_cand=100000):
+    """CPU restatement of querySplit (op 0 boundary, 1 interior) / queryMerge
+    (op 2), bijectivity off: list of candidate dicts and the seconds taken."""
+    V_rest, UV, F = _f8(V_rest), _f8(UV), _i4(F)
+    c = _i4(np.asarray(cohE).reshape(-1, 4))
+    ew = np.zeros(max_cand)
+    ec = np.zeros(2 * max_cand)
+    path = np.zeros(3 * max_cand, np.int32)
+    pos = np.zeros(8 * max_cand)
+    rows = np.zeros(max_cand, np.int32)
+    n = np.zeros(1, np.int32)
+    sec = np.zeros(1)
+    lib().ocr_topology_query(len(V_rest), _pi(F), len(F), _pd(V_rest), _pd(UV), _pi(c), len(c), op, lambda_t,
+                             filter_exp, threads, max_cand, _pd(ew), _pd(ec), _pi(path), _pd(pos), _pi(rows), _pi(n),
+                             _pd(sec))
+    out = []
+    for k in range(min(int(n[0]), max_cand)):
+        p = [int(x) for x in path[3 * k:3 * k + 3] if x >= 0]
+        out.append({"EwDec": ew[k], "energyChanges": (ec[2 * k], ec[2 * k + 1]), "path": p,
+                    "newVertPos": pos[8 * k:8 * k + 2 * rows[k]].reshape(-1, 2)})
+    return out, float(sec[0])

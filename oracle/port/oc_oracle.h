@@ -100,6 +100,16 @@ int ocr_newton_scaffold(const double* V_rest, int nV, const int* F, int nF, cons
                         double* UV, const ocr_newton_opts* opts, const ocr_scaffold* scaffold,
                         double* traceE, double* traceGsq, double* traceAlpha, double* traceSeconds, int* status);
 
+/* Topology queries, bijectivity off (oc_topo_oracle.cpp): querySplit
+ * (opType 0 boundary, 1 interior) or queryMerge (2) on the state (F, V_rest,
+ * UV, cohE), candidates run on nThreads.  Per candidate c < maxCand: EwDec,
+ * energyChanges ec[2c..2c+1], path[3c..3c+2] (-1 padded), newVertPos
+ * pos[8c..] with posRows[c] rows.  *nCand = number of candidates,
+ * *seconds = wall time of the query. */
+int ocr_topology_query(int nV, const int* F, int nF, const double* Vrest, const double* UV, const int* cohE,
+                       int nCohE, int opType, double lambda_t, double filterExp, int nThreads, int maxCand,
+                       double* EwDec, double* ec, int* path, double* pos, int* posRows, int* nCand, double* seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -399,13 +399,26 @@ int main(int argc, char** argv)
         std::vector<int> bestPath, pathB, pathI;
         Eigen::MatrixXd bestPos, posB, posI;
         std::pair<double, double> bestEc;
+        auto q0 = std::chrono::steady_clock::now();
         R.querySplit(lambda_t, false, false, best[0], pathB, posB, bestEc);
+        auto q1 = std::chrono::steady_clock::now();
         dump("bSplit", paths_bSplit, newVertPoses_bSplit, energyChanges_bSplit);
+        auto q2 = std::chrono::steady_clock::now();
         R.queryMerge(lambda_t, false, best[1], bestPath, bestPos, bestEc);
+        auto q3 = std::chrono::steady_clock::now();
         dump("merge", paths_merge, newVertPoses_merge, energyChanges_merge);
+        auto q4 = std::chrono::steady_clock::now();
         R.querySplit(lambda_t, false, true, best[2], pathI, posI, bestEc);
+        auto q5 = std::chrono::steady_clock::now();
         dump("iSplit", paths_iSplit, newVertPoses_iSplit, energyChanges_iSplit);
         npy_vecd(out + "topo_best.npy", {best[0], best[1], best[2], lambda_t, (double)inSplitTotalAmt});
+        const double tq[3] = {std::chrono::duration<double>(q1 - q0).count(),
+                              std::chrono::duration<double>(q3 - q2).count(),
+                              std::chrono::duration<double>(q5 - q4).count()};
+        npy_vecd(out + "topo_seconds.npy", {tq[0], tq[1], tq[2]});
+        if (doTime)
+            std::printf("topology queries: boundary split %.3f s, merge %.3f s, interior split %.3f s\n", tq[0], tq[1],
+                        tq[2]);
         // the operations themselves, applied to copies whatever their E_w
         // change (Optimizer::createFracture, Optimizer.cpp:373-440): the best
         // boundary split (then the merge query on that state and its best

@@ -101,3 +101,35 @@ def test_bad_operations_rejected(golden):
     with pytest.raises(oc.OCError):
         oc.topology_apply(oc.OP_INTERIOR_SPLIT, [0, 1], np.zeros((2, 2)), g["topo_Vrest"], g["topo_V"],
                           g["topo_F"], g["topo_cohE"])
+
+
+@pytest.mark.parametrize("op,tag", [(0, "bSplit"), (1, "iSplit"), (2, "merge")])
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_oracle_topology_query(golden, case, op, tag):
+    """The CPU restatement of the topology queries against the reference's."""
+    import oracle as O
+    g = golden(case)
+    cands, _ = O.topology_query(g["topo_Vrest"], g["topo_V"], g["topo_F"], g["topo_cohE"], op, g["topo_best"][3],
+                                threads=4)
+    ref = golden_candidates(g, tag)
+    assert len(cands) == len(ref)
+    for c, r in zip(cands, ref):
+        if r["energyChanges"][0] == DBL_MAX:
+            assert c["EwDec"] == -DBL_MAX
+            continue
+        assert c["path"] == r["path"]
+        for a, b in zip(c["energyChanges"], r["energyChanges"]):
+            assert a == pytest.approx(b, rel=1e-6, abs=1e-12)
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_oracle_merge_query_after_split(golden, case):
+    import oracle as O
+    g = golden(case)
+    cands, _ = O.topology_query(g["topo_afterB_Vrest"], g["topo_afterB_V"], g["topo_afterB_F"], g["topo_afterB_cohE"],
+                                2, g["topo_best"][3])
+    ref = golden_candidates(g, "mergeB")
+    assert len(cands) == len(ref)
+    for c, r in zip(cands, ref):
+        assert c["path"] == r["path"]
+        assert c["energyChanges"][0] == pytest.approx(r["energyChanges"][0], rel=1e-6, abs=1e-12)
