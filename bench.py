@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--scaffold", default="on", choices=["on", "off"])
+    p.add_argument("--no-topology", action="store_true")
+    p.add_argument("--topo-newton-iters", type=int, default=400,
+                   help="untimed Newton iterations (to convergence) before the topology step is timed")
     return p.parse_args()
 
 
@@ -209,9 +212,10 @@ def run_ours(args, rank, world):
     opt.precompute()
 
     def step():
-        opt.solve(1)
+        r = opt.solve(1)
         if scaf:
             opt.rebuildScaffold()   # Optimizer.cpp:251-257
+        return r
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
 
     def flush_l2():
@@ -261,6 +265,61 @@ def run_ours(args, rank, world):
         e2e = {"value": world * e2e_steps / e2e_max, "unit": UNIT, "h2d_bytes_per_step": 16 * nV,
                "d2h_bytes_per_step": 16 * nV}
 
+    # one topology step of the outer loop at the converged state: the
+    # candidate evaluation of TriMesh::splitOrMerge (boundary splits, merges)
+    # and of the interior-split query, every local solve on the GPU
+    topo = None
+    if not args.no_topology:
+        converged_after = None
+        for k in range(args.topo_newton_iters):
+            if step() == 1:
+                converged_after = args.warmup + args.steps + k + 1
+                break
+        mesh.setCohesiveEdges(st.cohE)
+        lam_t = 1.0 - (1.0 - args.lam)   # 1 - energyParams[0], as createFracture passes it
+
+        def topo_step(fp32=False):
+            return (mesh.querySplit(lam_t, False, fp32=fp32), mesh.queryMerge(lam_t, fp32=fp32),
+                    mesh.querySplit(lam_t, True, fp32=fp32))
+
+        topo_step()   # warm-up
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        qb, qm, qi = topo_step()
+        ctx.synchronize()
+        t_gpu = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        fb, fm, fi = topo_step(fp32=True)
+        ctx.synchronize()
+        t_fp32 = time.perf_counter() - t0
+        topo = {"metric": "topology-step s (exhaustive candidate evaluation)", "value": t_gpu, "unit": "s",
+                "higher_is_better": False, "bijectivity": "off (local solves without air meshes)",
+                "newton_iterations_before": converged_after if converged_after else
+                args.warmup + args.steps + args.topo_newton_iters,
+                "converged": converged_after is not None, "lambda": args.lam,
+                "candidates": {"boundary_split": len(qb["candidates"]), "merge": len(qm["candidates"]),
+                               "interior_split": len(qi["candidates"])},
+                "local_problems": qb["local_problems"] + qm["local_problems"] + qi["local_problems"],
+                "gpu_solve_ms": qb["solve_ms"] + qm["solve_ms"] + qi["solve_ms"],
+                "host_build_ms": qb["build_ms"] + qm["build_ms"] + qi["build_ms"],
+                "max_local_iterations": max(qb["max_local_iters"], qm["max_local_iters"], qi["max_local_iters"]),
+                "local_iterations": qb["local_iters_total"] + qm["local_iters_total"] + qi["local_iters_total"],
+                "local_capped": qb["local_capped"] + qm["local_capped"] + qi["local_capped"],
+                "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"], "interior_split": qi["EwDec_max"]},
+                "fp32_hessian_option": {"value": t_fp32, "unit": "s",
+                                        "best": {"boundary_split": fb["EwDec_max"], "merge": fm["EwDec_max"],
+                                                 "interior_split": fi["EwDec_max"]}}}
+        if rank == 0 and not args.no_cpu_baseline:
+            import oracle as O
+            threads = os.cpu_count() or 1
+            uv = mesh.V
+            secs = 0.0
+            for op in (0, 2, 1):
+                _, s = O.topology_query(mesh.V_rest, uv, mesh.F, st.cohE, op, lam_t, threads=threads)
+                secs += s
+            topo["cpu_baseline"] = {"value": secs, "unit": "s", "cores": threads, "kind": "port",
+                                    "sample": "the same three queries on the same state"}
+
     if rank != 0:
         return
     # dominant phase: the multifrontal factorisation, FP64-FMA bound; the
@@ -291,7 +350,7 @@ def run_ours(args, rank, world):
                    "l2": "flushed between timed steps (256 MB write)", "solver": "multifrontal Cholesky (FP64)",
                    "precision": "fp64 throughout (energy, gradient, Hessian eigen-clamp, LDL^T)"},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-        "energy": opt.getLastEnergyVal(),
+        "energy": opt.getLastEnergyVal(), "topology": topo,
     }
     print(json.dumps(out), flush=True)
 

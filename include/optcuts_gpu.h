@@ -260,13 +260,21 @@ int oc_mesh_set_cohesive_edges(oc_mesh* mesh, const int* cohE, int nCohE);
 int oc_mesh_split_filter(oc_mesh* mesh, double* divGrad);
 /* querySplit(lambda_t, false, opType == OC_OP_INTERIOR_SPLIT) or
  * queryMerge(lambda_t).  lambda_t as the reference passes it
- * (1 - energyParams[0]); filterExp = filterExp_in (<= 0: 0.6). */
-int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, oc_topo_result** out);
+ * (1 - energyParams[0]); filterExp = filterExp_in (<= 0: 0.6).
+ * options: OC_TOPO_FP32_HESSIAN projects the local element Hessians in
+ * FP32 (about 8x faster local solves; energies, gradients, line search and
+ * the local LDL^T stay FP64; energy changes then agree with the FP64
+ * evaluation to ~1e-4 relative instead of ~1e-8). */
+enum { OC_TOPO_FP32_HESSIAN = 1 };
+int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out);
 /* candidate count, index of the largest E_w decrease (-1: none), size of
  * the filtered pool (inSplitTotalAmt for interior splits), local problems
  * solved, their largest iteration count, host build and device solve ms */
 int oc_topo_result_info(const oc_topo_result* r, int* nCand, int* best, int* pool, int* nProblems, int* maxIters,
                         double* buildMs, double* solveMs);
+/* Newton iterations summed over all local problems, how many of them
+ * stopped at the iteration cap (100), and the line-search energy trials */
+int oc_topo_result_iterations(const oc_topo_result* r, int* totalIters, int* capped, long long* trials);
 /* candidate c as the reference records it: EwDec (interior splits halved,
  * TriMesh.cpp:702-704), energyChanges (2), path (<= 3), newVertPos (<= 4 x 2) */
 int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, double* energyChanges, int* path,

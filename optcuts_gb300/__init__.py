@@ -102,10 +102,11 @@ _SIGS = {
     "oc_air_mesh_destroy": [_vp],
     "oc_mesh_set_cohesive_edges": [_vp, _i, ctypes.c_int],
     "oc_mesh_split_filter": [_vp, _d],
-    "oc_topology_query": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_vp)],
+    "oc_topology_query": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_vp)],
     "oc_topo_result_info": [_vp, _i, _i, _i, _i, _i, _d, _d],
     "oc_topo_result_candidate": [_vp, ctypes.c_int, _d, _d, _i, _i, _d, _i],
     "oc_topo_result_destroy": [_vp],
+    "oc_topo_result_iterations": [_vp, _i, _i, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_create_fracture": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
     "oc_mesh_apply_topology": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
     "oc_mesh_get_topology": [_vp, _i, _i, _i, _i, _d, _i],
@@ -258,15 +259,17 @@ class TriMesh:
         self.ctx.check(lib().oc_mesh_split_filter(self.h, _pd(out)), "splitFilter")
         return out
 
-    def _query(self, op, lambda_t, filterExp):
+    def _query(self, op, lambda_t, filterExp, fp32):
         h = _vp()
-        self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), ctypes.byref(h)),
-                       "topology query")
+        self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), 1 if fp32 else 0,
+                                               ctypes.byref(h)), "topology query")
         try:
             n, best, pool, nprob, mit = (ctypes.c_int() for _ in range(5))
             bms, sms = ctypes.c_double(), ctypes.c_double()
             lib().oc_topo_result_info(h, ctypes.byref(n), ctypes.byref(best), ctypes.byref(pool), ctypes.byref(nprob),
                                       ctypes.byref(mit), ctypes.byref(bms), ctypes.byref(sms))
+            tot, cap, tri = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+            lib().oc_topo_result_iterations(h, ctypes.byref(tot), ctypes.byref(cap), ctypes.byref(tri))
             cands = []
             for c in range(n.value):
                 ew, ec = ctypes.c_double(), np.zeros(2)
@@ -282,12 +285,14 @@ class TriMesh:
         return {"EwDec_max": cands[b]["EwDec"] if b >= 0 else 0.0, "best": b,
                 "path_max": cands[b]["path"] if b >= 0 else [], "candidates": cands, "pool": pool.value,
                 "local_problems": nprob.value, "max_local_iters": mit.value, "build_ms": bms.value,
-                "solve_ms": sms.value}
+                "solve_ms": sms.value, "local_iters_total": tot.value, "local_capped": cap.value,
+                "local_trials_total": tri.value}
 
-    def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6):
+    def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6, fp32=False):
         """TriMesh::querySplit(lambda_t, false, splitInterior) with every local
-        solve batched on the GPU (bijectivity off)."""
-        return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp)
+        solve batched on the GPU (bijectivity off); fp32 projects the local
+        element Hessians in FP32."""
+        return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp, fp32)
 
     def applyTopology(self, op, path, newVertPos):
         """splitEdgeOnBoundary / cutPath / mergeBoundaryEdges on this mesh."""
@@ -305,9 +310,9 @@ class TriMesh:
         lib().oc_mesh_get_topology(self.h, None, None, None, _pi(F), _pd(Vr), _pi(C))
         self.nV, self.nF, self.F, self.V_rest, self.cohE = nv.value, nf.value, F, Vr, C
 
-    def queryMerge(self, lambda_t):
+    def queryMerge(self, lambda_t, fp32=False):
         """TriMesh::queryMerge(lambda_t, false) (bijectivity off)."""
-        return self._query(OP_MERGE, lambda_t, 0.6)
+        return self._query(OP_MERGE, lambda_t, 0.6, fp32)
 
     def close(self):
         if getattr(self, "h", None):

@@ -771,7 +771,7 @@ struct oc_topo_result {
     oc::TopoStats stats;
 };
 
-int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, oc_topo_result** out)
+int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out)
 {
     if (!m || !out || opType < 0 || opType > 2) return OC_ERR_INVALID;
     *out = nullptr;
@@ -802,8 +802,8 @@ int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp,
     oc_topo_result* r = new (std::nothrow) oc_topo_result;
     if (!r) return OC_ERR_NOMEM;
     std::string err;
-    const int rc = oc::topo_query(in, opType, lambda_t, filterExp > 0.0 ? filterExp : 0.6, r->cands, r->best, r->pool,
-                                  r->stats, &err);
+    const int rc = oc::topo_query(in, opType, lambda_t, filterExp > 0.0 ? filterExp : 0.6, options, r->cands, r->best,
+                                  r->pool, r->stats, &err);
     if (rc) {
         delete r;
         return fail(m->ctx, rc, err);
@@ -823,6 +823,15 @@ int oc_topo_result_info(const oc_topo_result* r, int* nCand, int* best, int* poo
     if (maxIters) *maxIters = r->stats.maxIters;
     if (buildMs) *buildMs = r->stats.buildMs;
     if (solveMs) *solveMs = r->stats.solveMs;
+    return OC_OK;
+}
+
+int oc_topo_result_iterations(const oc_topo_result* r, int* totalIters, int* capped, long long* trials)
+{
+    if (!r) return OC_ERR_INVALID;
+    if (totalIters) *totalIters = r->stats.totalIters;
+    if (capped) *capped = r->stats.nonConverged;
+    if (trials) *trials = r->stats.totalTrials;
     return OC_OK;
 }
 

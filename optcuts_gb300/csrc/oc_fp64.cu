@@ -310,11 +310,15 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
     double fro = 0.0;
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) fro += A[i][j] * A[i][j];
+    double prevOff = 0.0;
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0.0;
         for (int p = 0; p < 6; ++p)
             for (int q = p + 1; q < 6; ++q) off += A[p][q] * A[p][q];
-        if (off <= 1e-34 * fro) break;
+        // converged, or no longer decreasing (the off-diagonal mass has
+        // reached the rounding floor, below which 1e-34 is not reachable)
+        if (off <= 1e-34 * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
         for (int p = 0; p < 6; ++p) {
             for (int q = p + 1; q < 6; ++q) {
                 const double apq = A[p][q];
@@ -342,6 +346,49 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
     }
 }
 
+// FP32 cyclic Jacobi for the local topology solves (same rotations; stops
+// at FP32 convergence or stagnation).
+__device__ void jacobi_eig6f(float A[6][6], float V[6][6])
+{
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) V[i][j] = (i == j) ? 1.0f : 0.0f;
+    float fro = 0.0f;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) fro += A[i][j] * A[i][j];
+    float prevOff = 0.0f;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        float off = 0.0f;
+        for (int p = 0; p < 6; ++p)
+            for (int q = p + 1; q < 6; ++q) off += A[p][q] * A[p][q];
+        if (off <= 1e-14f * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
+        for (int p = 0; p < 6; ++p) {
+            for (int q = p + 1; q < 6; ++q) {
+                const float apq = A[p][q];
+                if (apq == 0.0f) continue;
+                const float theta = (A[q][q] - A[p][p]) / (2.0f * apq);
+                const float t = (theta >= 0 ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+                const float c = 1.0f / sqrtf(t * t + 1.0f), sn = t * c;
+                for (int k = 0; k < 6; ++k) {
+                    const float akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - sn * akq;
+                    A[k][q] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const float apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - sn * aqk;
+                    A[q][k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const float vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+        }
+    }
+}
+
 // Per-triangle Hessian (SymDirichletEnergy.cpp:440-522) projected to PSD by
 // the 6x6 eigen-clamp of IglUtils::makePD (IglUtils.hpp:71-90): unchanged
 // when the smallest eigenvalue is >= 0, otherwise V max(Lambda, 0) V^T.
@@ -350,8 +397,10 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
 // change the Newton direction, and reducing to the 4-dimensional
 // translation-free part first does not reproduce the reference.
 // Output: the upper triangle as 21 values per triangle (SoA).
+// localMode 0: exact (the global Newton); 1: skip the projection when H is
+// PSD up to rounding (local solves, FP64); 2: as 1 but project in FP32
 __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, double e1d, double e01d, double w,
-                            double H[6][6])
+                            double H[6][6], int localMode = 0)
 {
     const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
     const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
@@ -394,6 +443,47 @@ __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, do
     double A[6][6], V[6][6];
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
+    if (localMode) {
+        // LDL^T without pivoting: no pivot below -1e-13 of the largest
+        // diagonal means H is PSD up to rounding and makePD would return it
+        // unchanged up to that rounding, so the eigen-decomposition is skipped
+        double dmax = 0.0;
+        for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(A[i][i]));
+        const double tol = 1e-13 * dmax;
+        bool psd = true;
+        for (int k = 0; k < 6 && psd; ++k) {
+            const double d = A[k][k];
+            if (d < -tol) psd = false;
+            else if (d > tol)
+                for (int i = k + 1; i < 6; ++i) {
+                    const double l = A[i][k] / d;
+                    for (int j = k + 1; j <= i; ++j) A[i][j] = A[i][j] - l * A[j][k];
+                }
+        }
+        if (psd) return;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
+    }
+    if (localMode == 2) {
+        double dmax = 0.0;
+        for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(H[i][i]));
+        // FP32 projection, scaled to the block's largest diagonal entry:
+        // enough for the Newton step of a 2-8 DOF local problem
+        float Af[6][6], Vf[6][6];
+        const double scale = dmax > 0.0 ? dmax : 1.0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) Af[i][j] = static_cast<float>(H[i][j] / scale);
+        jacobi_eig6f(Af, Vf);
+        float lamf[6];
+        for (int i = 0; i < 6; ++i) lamf[i] = Af[i][i] < 0.0f ? 0.0f : Af[i][i];
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                float sum = 0.0f;
+                for (int k = 0; k < 6; ++k) sum += Vf[i][k] * lamf[k] * Vf[j][k];
+                H[i][j] = static_cast<double>(sum) * scale;
+            }
+        return;
+    }
     jacobi_eig6(A, V);
     double lam[6], lmin = A[0][0];
     for (int i = 0; i < 6; ++i) {
@@ -589,7 +679,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
     }
     initE = __shfl_sync(0xffffffffu, initE, 0);
     double lastE = local_energy(m, b, P, S, S.pos, false, 0.0, lane);   // precompute
-    int status = 0, it = 0;
+    int status = 0, it = 0, trials = 0;
     bool finite = isfinite(lastE);
     for (; it < P.maxIter && finite; ++it) {
         // gradient (fixed vertices have no slot: zero rows)
@@ -638,7 +728,8 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
                 const int g = b.ltGlobal[P.triOff + t];
                 double H6[6][6];
-                tri_hessian(U, m.A2[g], m.e0d[g], m.e1d[g], m.e01d[g], m.area[g] / P.localArea, H6);
+                tri_hessian(U, m.A2[g], m.e0d[g], m.e1d[g], m.e01d[g], m.area[g] / P.localArea, H6,
+                            b.fp32Hessian ? 2 : 1);
                 for (int i = 0; i < 6; ++i)
                     for (int j = i; j < 6; ++j) S.triH[lane][sym21(i, j)] = H6[i][j];
                 for (int k = 0; k < 3; ++k) S.triSlot[lane][k] = sl[k];
@@ -736,6 +827,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         __syncwarp();
         bool stopped = false;
         double testE = local_energy(m, b, P, S, S.pos0, true, step, lane);
+        ++trials;
         while (testE > lastE) {
             step = step / 2.0;
             if (step == 0.0) {
@@ -743,6 +835,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 break;
             }
             testE = local_energy(m, b, P, S, S.pos0, true, step, lane);
+            ++trials;
         }
         if (lane < P.nFree) {
             S.pos[lane].x = S.pos0[lane].x + step * S.dir[2 * lane];
@@ -768,6 +861,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         for (int k = 0; k < kLocalMaxFree; ++k) r.pos[k] = k < P.nFree ? S.pos[k] : make_double2(0.0, 0.0);
         r.iters = it;
         r.status = status;
+        r.trials = trials;
         b.out[pi] = r;
     }
 }

@@ -88,6 +88,7 @@ struct LocalResult {
     double eDec, initE, lastE;
     double2 pos[kLocalMaxFree];   // free vertices' final positions, by slot
     int iters, status;            // status 1: converged or stopped; 0: iteration cap; 2: non-finite
+    int trials;                   // line-search energy evaluations
 };
 struct LocalBatch {
     const LocalProblem* prob = nullptr;
@@ -98,6 +99,7 @@ struct LocalBatch {
     const int* lvSlot = nullptr;       // free slot or -1 (fixed)
     const int* initTri = nullptr;
     LocalResult* out = nullptr;
+    int fp32Hessian = 0;               // project element Hessians in FP32
 };
 
 struct PcgWork {

@@ -473,8 +473,8 @@ int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, b
     return OC_OK;
 }
 
-int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, std::vector<TopoCandidate>& out,
-               int& best, int& candidatePool, TopoStats& stats, std::string* err)
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, int options,
+               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err)
 {
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
@@ -756,6 +756,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
     if (!B.prob.empty()) {
         LocalBatch db;
         db.nProb = static_cast<int>(B.prob.size());
+        db.fp32Hessian = options & 1;
         void* bufs[7] = {};
         size_t sizes[7] = {sizeof(LocalProblem) * B.prob.size(), sizeof(int) * B.ltGlobal.size(),
                            sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
@@ -798,6 +799,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
         stats.maxIters = std::max(stats.maxIters, r.iters);
         stats.totalIters += r.iters;
         if (r.status != 1) stats.nonConverged++;
+        stats.totalTrials += r.trials;
         const double SDDec = r.eDec;
         double EwDec;
         if (opType == kOpMerge) {

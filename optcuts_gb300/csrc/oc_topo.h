@@ -37,6 +37,7 @@ struct TopoQueryIn {
 
 struct TopoStats {
     int nCandidates = 0, nProblems = 0, maxIters = 0, totalIters = 0, nonConverged = 0;
+    long long totalTrials = 0;
     double buildMs = 0.0, solveMs = 0.0;
 };
 
@@ -44,8 +45,10 @@ struct TopoStats {
 // splitInterior false / true) or kOpMerge (queryMerge).  filterExp is the
 // interior-split filter exponent (filterExp_in, 0.6 by default).  best is
 // the index of the largest EwDec (-1 when there is no candidate).
-int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, std::vector<TopoCandidate>& out,
-               int& best, int& candidatePool, TopoStats& stats, std::string* err);
+// options bit 0: project the local element Hessians in FP32 (faster; the
+// energies, gradients, line search and local LDL^T stay FP64)
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, int options,
+               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err);
 
 // Applies one operation to host arrays (F nF x 3, Vrest nV x 3, UV nV x 2,
 // cohE rows x 4) with the reference's vertex and cohesive-edge bookkeeping:

@@ -69,11 +69,14 @@ void jacobi_eig(double A[6][6], double V[6][6], int n)
     double fro = 0.0;
     for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) fro += A[i][j] * A[i][j];
+    double prevOff = 0.0;
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0.0;
         for (int p = 0; p < n; ++p)
             for (int q = p + 1; q < n; ++q) off += A[p][q] * A[p][q];
-        if (off <= 1e-34 * fro) break;
+        // converged, or no longer decreasing (rounding floor)
+        if (off <= 1e-34 * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
         for (int p = 0; p < n; ++p) {
             for (int q = p + 1; q < n; ++q) {
                 const double apq = A[p][q];

@@ -65,6 +65,25 @@ def test_interior_split_query(golden, case):
 
 
 @pytest.mark.parametrize("case", TOPO_CASES)
+def test_fp32_projection_option(golden, case):
+    """FP32 projection of the local element Hessians: the same candidates and
+    paths; energy changes within 1e-3 relative (the local solves stop at a
+    gradient tolerance, so a differently rounded Hessian stops at another
+    point of that tolerance band)."""
+    g = golden(case)
+    lam_t = g["topo_best"][3]
+    for interior, tag in ((False, "bSplit"), (True, "iSplit")):
+        q = topo_mesh(g).querySplit(lam_t, splitInterior=interior, fp32=True)
+        ref = golden_candidates(g, tag)
+        assert len(q["candidates"]) == len(ref)
+        for c, r in zip(q["candidates"], ref):
+            if r["energyChanges"][0] == DBL_MAX:
+                continue
+            assert c["path"] == r["path"]
+            assert c["energyChanges"][0] == pytest.approx(r["energyChanges"][0], rel=1e-3, abs=1e-9)
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
 def test_merge_query(golden, case):
     g = golden(case)
     q = topo_mesh(g).queryMerge(g["topo_best"][3])
