@@ -265,8 +265,50 @@ int oc_mesh_split_filter(oc_mesh* mesh, double* divGrad);
  * FP32 (about 8x faster local solves; energies, gradients, line search and
  * the local LDL^T stay FP64; energy changes then agree with the FP64
  * evaluation to ~1e-4 relative instead of ~1e-8). */
-enum { OC_TOPO_FP32_HESSIAN = 1 };
+enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2 };
 int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out);
+/* No counterpart in the reference: the learned proposal.  Every local
+ * problem first gets one Newton step (its features: energies, gradient
+ * split between the split copies, first-step decrease, ...; 32 values),
+ * the MLP predicts the fraction of its excess energy the full solve would
+ * remove, the predicted E_w decreases are ranked and only the top fraction
+ * topFrac of the problems is solved exactly; the exact solves alone decide
+ * the candidates' values (unsolved candidates report -DBL_MAX). */
+typedef struct oc_mlp oc_mlp;
+int oc_topology_query_learned(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_mlp* mlp,
+                              double topFrac, oc_topo_result** out);
+/* per local problem (rows): the 32 features, the exact target (fraction of
+ * the local excess energy removed; queries with OC_TOPO_RECORD_FEATURES)
+ * and the MLP's prediction (learned queries); NULL arrays are skipped */
+int oc_topo_result_features(const oc_topo_result* r, int* nRows, float* X, float* target, float* predicted);
+/* learned queries: problems solved exactly, ms of the one-step pass and of
+ * the exact solves */
+int oc_topo_result_timing(const oc_topo_result* r, int* nSelected, double* probeMs, double* exactMs);
+/* per local problem: its candidate, its exact E_w decrease (NaN where the
+ * learned proposal did not solve it) and the predicted decrease (learned
+ * queries; else NaN), on the candidates' scale (interior splits halved):
+ * the exhaustive pass as the judge of the proposal's recall */
+int oc_topo_result_problems(const oc_topo_result* r, int* nProblems, int* cand, double* ewExact, double* ewPred);
+/* per local problem: triangles, free vertices, Newton iterations,
+ * line-search energy evaluations and SM clock cycles of its solve (of the
+ * one-step pass where the learned proposal did not select it) */
+int oc_topo_result_problem_stats(const oc_topo_result* r, int* nProblems, int* nTri, int* nFree, int* iters,
+                                 int* trials, long long* cycles);
+
+/* ---- The MLP of the learned proposal (no counterpart in the reference) --
+ * in -> hidden -> hidden -> 1 with ReLU; BF16 weights and activations, FP32
+ * accumulation; trained on the device (MSE, Adam on FP32 master weights).
+ * Parameters: W1 (hidden x in), b1, W2 (hidden x hidden), b2, W3 (hidden), b3. */
+int oc_mlp_create(oc_ctx* ctx, int nIn, int nHidden, unsigned seed, oc_mlp** out);
+int oc_mlp_destroy(oc_mlp* mlp);
+int oc_mlp_num_params(const oc_mlp* mlp, int* n);
+int oc_mlp_get_params(oc_mlp* mlp, float* params);
+int oc_mlp_set_params(oc_mlp* mlp, const float* params);
+int oc_mlp_predict(oc_mlp* mlp, const float* X, int n, float* y);
+/* gradient of the mean squared error over n rows (and the loss) */
+int oc_mlp_gradient(oc_mlp* mlp, const float* X, const float* target, int n, float* grad, float* loss);
+int oc_mlp_train(oc_mlp* mlp, const float* X, const float* target, int n, int epochs, int batch, float lr,
+                 unsigned seed, float* finalLoss);
 /* candidate count, index of the largest E_w decrease (-1: none), size of
  * the filtered pool (inSplitTotalAmt for interior splits), local problems
  * solved, their largest iteration count, host build and device solve ms */

@@ -112,6 +112,23 @@ _SIGS = {
     "oc_mesh_get_topology": [_vp, _i, _i, _i, _i, _d, _i],
     "oc_topology_apply": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d,
                           ctypes.c_int, _i, _i, _d, _d, _i, _i, _i],
+    "oc_topology_query_learned": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
+                                  ctypes.c_double, ctypes.POINTER(_vp)],
+    "oc_topo_result_features": [_vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                ctypes.POINTER(ctypes.c_float)],
+    "oc_topo_result_timing": [_vp, _i, _d, _d],
+    "oc_topo_result_problems": [_vp, _i, _vp, _vp, _vp],
+    "oc_topo_result_problem_stats": [_vp, _i, _vp, _vp, _vp, _vp, _vp],
+    "oc_mlp_create": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)],
+    "oc_mlp_destroy": [_vp],
+    "oc_mlp_num_params": [_vp, _i],
+    "oc_mlp_get_params": [_vp, ctypes.POINTER(ctypes.c_float)],
+    "oc_mlp_set_params": [_vp, ctypes.POINTER(ctypes.c_float)],
+    "oc_mlp_predict": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_float)],
+    "oc_mlp_gradient": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+    "oc_mlp_train": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int,
+                     ctypes.c_int, ctypes.c_float, ctypes.c_uint, ctypes.POINTER(ctypes.c_float)],
     "oc_topology_split_candidates": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_double, _i, _i, _i],
     "oc_optimizer_get_scaffold": [_vp, _i, _i, _i, _d, _i, _i],
     "oc_optimizer_get_last_energy_scaffold": [_vp, _d],
@@ -152,6 +169,14 @@ def _pi(a):
 
 def _f8(a):
     return np.ascontiguousarray(a, np.float64)
+
+
+def _f4(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _pf(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
 
 
 def _i4(a):
@@ -259,10 +284,15 @@ class TriMesh:
         self.ctx.check(lib().oc_mesh_split_filter(self.h, _pd(out)), "splitFilter")
         return out
 
-    def _query(self, op, lambda_t, filterExp, fp32):
+    def _query(self, op, lambda_t, filterExp, fp32, features=False, mlp=None, topFrac=0.1):
         h = _vp()
-        self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), 1 if fp32 else 0,
-                                               ctypes.byref(h)), "topology query")
+        opt = (1 if fp32 else 0) | (2 if features else 0)
+        if mlp is not None:
+            self.ctx.check(lib().oc_topology_query_learned(self.h, op, float(lambda_t), float(filterExp), opt, mlp.h,
+                                                           float(topFrac), ctypes.byref(h)), "learned topology query")
+        else:
+            self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), opt,
+                                                   ctypes.byref(h)), "topology query")
         try:
             n, best, pool, nprob, mit = (ctypes.c_int() for _ in range(5))
             bms, sms = ctypes.c_double(), ctypes.c_double()
@@ -270,6 +300,28 @@ class TriMesh:
                                       ctypes.byref(mit), ctypes.byref(bms), ctypes.byref(sms))
             tot, cap, tri = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
             lib().oc_topo_result_iterations(h, ctypes.byref(tot), ctypes.byref(cap), ctypes.byref(tri))
+            nsel, pms, ems = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+            lib().oc_topo_result_timing(h, ctypes.byref(nsel), ctypes.byref(pms), ctypes.byref(ems))
+            nrow = ctypes.c_int()
+            lib().oc_topo_result_features(h, ctypes.byref(nrow), None, None, None)
+            X = np.zeros((nrow.value, 32), np.float32)
+            tgt = np.zeros(nrow.value, np.float32)
+            prd = np.zeros(nrow.value, np.float32)
+            if nrow.value:
+                lib().oc_topo_result_features(h, ctypes.byref(nrow), _pf(X),
+                                              _pf(tgt) if features else None, _pf(prd) if mlp is not None else None)
+            npb = ctypes.c_int()
+            lib().oc_topo_result_problems(h, ctypes.byref(npb), None, None, None)
+            pc = np.zeros(npb.value, np.int32)
+            pe, pp = np.zeros(npb.value), np.zeros(npb.value)
+            if npb.value:
+                lib().oc_topo_result_problems(h, ctypes.byref(npb), pc.ctypes.data_as(_vp), pe.ctypes.data_as(_vp),
+                                              pp.ctypes.data_as(_vp))
+            pstat = {k: np.zeros(npb.value, np.int32) for k in ("nTri", "nFree", "iters", "trials")}
+            pstat["cycles"] = np.zeros(npb.value, np.int64)
+            if npb.value:
+                lib().oc_topo_result_problem_stats(h, ctypes.byref(npb), *(pstat[k].ctypes.data_as(_vp) for k in
+                                                   ("nTri", "nFree", "iters", "trials", "cycles")))
             cands = []
             for c in range(n.value):
                 ew, ec = ctypes.c_double(), np.zeros(2)
@@ -286,13 +338,20 @@ class TriMesh:
                 "path_max": cands[b]["path"] if b >= 0 else [], "candidates": cands, "pool": pool.value,
                 "local_problems": nprob.value, "max_local_iters": mit.value, "build_ms": bms.value,
                 "solve_ms": sms.value, "local_iters_total": tot.value, "local_capped": cap.value,
-                "local_trials_total": tri.value}
+                "local_trials_total": tri.value, "selected": nsel.value, "probe_ms": pms.value,
+                "exact_ms": ems.value, "features": X, "target": tgt if features else None,
+                "predicted": prd if mlp is not None else None,
+                "problems": dict(cand=pc, EwDec=pe, EwDec_pred=pp, **pstat)}
 
-    def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6, fp32=False):
+    def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6, fp32=False, features=False, mlp=None,
+                   topFrac=0.1):
         """TriMesh::querySplit(lambda_t, false, splitInterior) with every local
         solve batched on the GPU (bijectivity off); fp32 projects the local
-        element Hessians in FP32."""
-        return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp, fp32)
+        element Hessians in FP32; features records each local problem's
+        features and exact target; mlp selects the learned proposal (only the
+        top fraction topFrac of the problems is solved exactly)."""
+        return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp, fp32,
+                           features, mlp, topFrac)
 
     def applyTopology(self, op, path, newVertPos):
         """splitEdgeOnBoundary / cutPath / mergeBoundaryEdges on this mesh."""
@@ -310,9 +369,9 @@ class TriMesh:
         lib().oc_mesh_get_topology(self.h, None, None, None, _pi(F), _pd(Vr), _pi(C))
         self.nV, self.nF, self.F, self.V_rest, self.cohE = nv.value, nf.value, F, Vr, C
 
-    def queryMerge(self, lambda_t, fp32=False):
+    def queryMerge(self, lambda_t, fp32=False, features=False, mlp=None, topFrac=0.1):
         """TriMesh::queryMerge(lambda_t, false) (bijectivity off)."""
-        return self._query(OP_MERGE, lambda_t, 0.6, fp32)
+        return self._query(OP_MERGE, lambda_t, 0.6, fp32, features, mlp, topFrac)
 
     def close(self):
         if getattr(self, "h", None):
@@ -485,6 +544,64 @@ def default_config(**kw):
     for k, v in kw.items():
         setattr(c, k, v)
     return c
+
+
+class MLP:
+    """The learned proposal's network: nIn -> nHidden -> nHidden -> 1 (ReLU),
+    BF16 weights and activations, FP32 accumulation, trained on the GPU."""
+
+    def __init__(self, nIn=32, nHidden=128, seed=0, ctx=None):
+        self.ctx = ctx or default_context()
+        self.nIn, self.nHidden = nIn, nHidden
+        h = _vp()
+        self.ctx.check(lib().oc_mlp_create(self.ctx.h, nIn, nHidden, seed, ctypes.byref(h)), "MLP")
+        self.h = h
+
+    def num_params(self):
+        n = ctypes.c_int()
+        lib().oc_mlp_num_params(self.h, ctypes.byref(n))
+        return n.value
+
+    def params(self):
+        p = np.zeros(self.num_params(), np.float32)
+        self.ctx.check(lib().oc_mlp_get_params(self.h, _pf(p)), "MLP params")
+        return p
+
+    def set_params(self, p):
+        p = _f4(p)
+        self.ctx.check(lib().oc_mlp_set_params(self.h, _pf(p)), "MLP set_params")
+
+    def predict(self, X):
+        X = _f4(X).reshape(-1, self.nIn)
+        y = np.zeros(len(X), np.float32)
+        self.ctx.check(lib().oc_mlp_predict(self.h, _pf(X), len(X), _pf(y)), "MLP predict")
+        return y
+
+    def gradient(self, X, t):
+        X, t = _f4(X).reshape(-1, self.nIn), _f4(t)
+        g = np.zeros(self.num_params(), np.float32)
+        loss = ctypes.c_float()
+        self.ctx.check(lib().oc_mlp_gradient(self.h, _pf(X), _pf(t), len(X), _pf(g), ctypes.byref(loss)),
+                       "MLP gradient")
+        return g, loss.value
+
+    def train(self, X, t, epochs=30, batch=512, lr=1e-3, seed=0):
+        X, t = _f4(X).reshape(-1, self.nIn), _f4(t)
+        loss = ctypes.c_float()
+        self.ctx.check(lib().oc_mlp_train(self.h, _pf(X), _pf(t), len(X), epochs, batch, lr, seed,
+                                          ctypes.byref(loss)), "MLP train")
+        return loss.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oc_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Scaffold:

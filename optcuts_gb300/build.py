@@ -32,8 +32,9 @@ UNITS = {
     "oc_api.cu": ["-Xcompiler", "-fvisibility=default"],
     "oc_airmesh.cpp": [],
     "oc_topo.cpp": [],
+    "oc_mlp.cu": [],
 }
-HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h"]
+HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h"]
 
 
 def _newest_input():

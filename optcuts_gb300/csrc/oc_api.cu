@@ -7,6 +7,7 @@
 #include "oc_airmesh.h"
 #include "oc_chol.h"
 #include "oc_internal.h"
+#include "oc_mlp.h"
 #include "oc_topo.h"
 
 #include <algorithm>
@@ -87,6 +88,10 @@ struct oc_optimizer {
     std::vector<int> airFw, bnd;    // air triangles in augmented ids; boundary map
     std::vector<int> airF;          // air triangles in air-mesh ids
 };
+
+namespace oc {
+cudaStream_t ctx_stream(oc_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
+} // namespace oc
 
 namespace {
 
@@ -769,9 +774,32 @@ struct oc_topo_result {
     std::vector<oc::TopoCandidate> cands;
     int best = -1, pool = 0;
     oc::TopoStats stats;
+    oc::TopoExtras extras;
 };
 
+static int topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, const oc::TopoOptions& opts,
+                          oc_topo_result** out);
+
 int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out)
+{
+    oc::TopoOptions opts;
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    return topology_query(m, opType, lambda_t, filterExp, opts, out);
+}
+
+int oc_topology_query_learned(oc_mesh* m, int opType, double lambda_t, double filterExp, int options, oc_mlp* mlp,
+                              double topFrac, oc_topo_result** out)
+{
+    if (!mlp || mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0) return OC_ERR_INVALID;
+    oc::TopoOptions opts;
+    opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+    opts.mlp = &mlp->m;
+    opts.topFrac = topFrac;
+    return topology_query(m, opType, lambda_t, filterExp, opts, out);
+}
+
+static int topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, const oc::TopoOptions& opts,
+                          oc_topo_result** out)
 {
     if (!m || !out || opType < 0 || opType > 2) return OC_ERR_INVALID;
     *out = nullptr;
@@ -802,8 +830,8 @@ int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp,
     oc_topo_result* r = new (std::nothrow) oc_topo_result;
     if (!r) return OC_ERR_NOMEM;
     std::string err;
-    const int rc = oc::topo_query(in, opType, lambda_t, filterExp > 0.0 ? filterExp : 0.6, options, r->cands, r->best,
-                                  r->pool, r->stats, &err);
+    const int rc = oc::topo_query(in, opType, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, r->cands, r->best,
+                                  r->pool, r->stats, &err, &r->extras);
     if (rc) {
         delete r;
         return fail(m->ctx, rc, err);
@@ -823,6 +851,53 @@ int oc_topo_result_info(const oc_topo_result* r, int* nCand, int* best, int* poo
     if (maxIters) *maxIters = r->stats.maxIters;
     if (buildMs) *buildMs = r->stats.buildMs;
     if (solveMs) *solveMs = r->stats.solveMs;
+    return OC_OK;
+}
+
+int oc_topo_result_timing(const oc_topo_result* r, int* nSelected, double* probeMs, double* exactMs)
+{
+    if (!r) return OC_ERR_INVALID;
+    if (nSelected) *nSelected = r->stats.nSelected;
+    if (probeMs) *probeMs = r->stats.probeMs;
+    if (exactMs) *exactMs = r->stats.exactMs;
+    return OC_OK;
+}
+
+int oc_topo_result_features(const oc_topo_result* r, int* nRows, float* X, float* target, float* predicted)
+{
+    if (!r || !nRows) return OC_ERR_INVALID;
+    *nRows = static_cast<int>(r->extras.X.size() / oc::kTopoNumFeatures);
+    if (X) std::copy(r->extras.X.begin(), r->extras.X.end(), X);
+    if (target) std::copy(r->extras.target.begin(), r->extras.target.end(), target);
+    if (predicted) std::copy(r->extras.predicted.begin(), r->extras.predicted.end(), predicted);
+    return OC_OK;
+}
+
+int oc_topo_result_problems(const oc_topo_result* r, int* nProblems, int* cand, double* ewExact, double* ewPred)
+{
+    if (!r || !nProblems) return OC_ERR_INVALID;
+    const auto& x = r->extras;
+    *nProblems = static_cast<int>(x.cand.size());
+    if (cand) std::copy(x.cand.begin(), x.cand.end(), cand);
+    if (ewExact) std::copy(x.ewExact.begin(), x.ewExact.end(), ewExact);
+    if (ewPred) {
+        if (x.ewPred.size() == x.cand.size()) std::copy(x.ewPred.begin(), x.ewPred.end(), ewPred);
+        else std::fill(ewPred, ewPred + x.cand.size(), std::nan(""));
+    }
+    return OC_OK;
+}
+
+int oc_topo_result_problem_stats(const oc_topo_result* r, int* nProblems, int* nTri, int* nFree, int* iters,
+                                 int* trials, long long* cycles)
+{
+    if (!r || !nProblems) return OC_ERR_INVALID;
+    const auto& x = r->extras;
+    *nProblems = static_cast<int>(x.nTri.size());
+    if (nTri) std::copy(x.nTri.begin(), x.nTri.end(), nTri);
+    if (nFree) std::copy(x.nFree.begin(), x.nFree.end(), nFree);
+    if (iters) std::copy(x.iters.begin(), x.iters.end(), iters);
+    if (trials) std::copy(x.trials.begin(), x.trials.end(), trials);
+    if (cycles) std::copy(x.cycles.begin(), x.cycles.end(), cycles);
     return OC_OK;
 }
 

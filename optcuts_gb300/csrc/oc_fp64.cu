@@ -660,6 +660,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
     const int pi = blockIdx.x * kLocalWarps + warp;
     if (pi >= b.nProb) return;   // uniform per warp
     LocalShared& S = shared[warp];
+    const long long clk0 = clock64();
     const LocalProblem P = b.prob[pi];
     const int nDof = 2 * P.nFree;
     for (int j = lane; j < P.nVert; j += 32) {
@@ -681,6 +682,64 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
     double lastE = local_energy(m, b, P, S, S.pos, false, 0.0, lane);   // precompute
     int status = 0, it = 0, trials = 0;
     bool finite = isfinite(lastE);
+    // raw quantities of the starting point (features of the learned proposal)
+    double raw[kLocalRaw];
+    for (int k = 0; k < kLocalRaw; ++k) raw[k] = 0.0;
+    {
+        double emax = 0.0, emin = 1e300, lsum = 0.0, lsq = 0.0;
+        double g0x = 0.0, g0y = 0.0, g1x = 0.0, g1y = 0.0, n0 = 0.0, n1 = 0.0, es0 = 0.0, es1 = 0.0;
+        for (int t = lane; t < P.nTri; t += 32) {
+            double2 U[3];
+            int sl[3];
+            local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
+            const int g = b.ltGlobal[P.triOff + t];
+            const double w = m.area[g] / P.localArea;
+            const double e = elem_energy(m, g, w, U[0], U[1], U[2]);
+            const double eu = e / (4.0 * w);
+            emax = fmax(emax, eu);
+            emin = fmin(emin, eu);
+            const double l = log(eu);
+            lsum += l;
+            lsq += l * l;
+            double2 cg[3];
+            tri_corner_grads(U[0], U[1], U[2], m.A2[g], m.e0[g], m.e1[g], m.e01[g], w, cg);
+            bool touch0 = false, touch1 = false;
+            for (int k = 0; k < 3; ++k) {
+                if (sl[k] == 0) { g0x += cg[k].x; g0y += cg[k].y; touch0 = true; }
+                if (sl[k] == 1) { g1x += cg[k].x; g1y += cg[k].y; touch1 = true; }
+            }
+            if (touch0) { n0 += 1.0; es0 += e; }
+            if (touch1) { n1 += 1.0; es1 += e; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+            emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+            lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+            lsq += __shfl_xor_sync(0xffffffffu, lsq, o);
+            g0x += __shfl_xor_sync(0xffffffffu, g0x, o);
+            g0y += __shfl_xor_sync(0xffffffffu, g0y, o);
+            g1x += __shfl_xor_sync(0xffffffffu, g1x, o);
+            g1y += __shfl_xor_sync(0xffffffffu, g1y, o);
+            n0 += __shfl_xor_sync(0xffffffffu, n0, o);
+            n1 += __shfl_xor_sync(0xffffffffu, n1, o);
+            es0 += __shfl_xor_sync(0xffffffffu, es0, o);
+            es1 += __shfl_xor_sync(0xffffffffu, es1, o);
+        }
+        raw[0] = lastE;
+        raw[5] = emax;
+        raw[6] = emin;
+        raw[7] = lsum / P.nTri;
+        raw[8] = lsq / P.nTri;
+        raw[9] = g0x * g0x + g0y * g0y;
+        raw[10] = g1x * g1x + g1y * g1y;
+        raw[11] = g0x * g1x + g0y * g1y;
+        raw[12] = n0;
+        raw[13] = n1;
+        raw[14] = es0;
+        raw[15] = es1;
+        raw[4] = lastE;   // E1: replaced after the first step
+    }
     for (; it < P.maxIter && finite; ++it) {
         // gradient (fixed vertices have no slot: zero rows)
         double gj = 0.0;
@@ -712,6 +771,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         __syncwarp();
         double gsq = 0.0;
         for (int j = 0; j < nDof; ++j) gsq = gsq + S.g[j] * S.g[j];
+        if (it == 0) raw[1] = gsq;
         if (gsq < P.targetGRes) {   // Optimizer.cpp:215-221
             status = 1;
             break;
@@ -845,6 +905,11 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         const double lastEDec = lastE - testE;
         if ((lastEDec / lastE < 1.0e-6 * step) && (step > 1.0e-3)) stopped = true;
         lastE = testE;
+        if (it == 0) {
+            raw[2] = step;
+            raw[3] = trials;
+            raw[4] = testE;
+        }
         finite = isfinite(lastE);
         if (stopped) {
             status = 1;
@@ -862,6 +927,8 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         r.iters = it;
         r.status = status;
         r.trials = trials;
+        for (int k = 0; k < kLocalRaw; ++k) r.raw[k] = raw[k];
+        r.cycles = clock64() - clk0;
         b.out[pi] = r;
     }
 }

@@ -84,11 +84,18 @@ struct LocalProblem {
     double localArea;      // the local mesh's surfaceArea (local triangle order)
     double targetGRes;     // (nVert - nFixed) / nVert * 1e-6
 };
+constexpr int kLocalRaw = 16;       // raw per-problem quantities for the learned proposal
 struct LocalResult {
     double eDec, initE, lastE;
     double2 pos[kLocalMaxFree];   // free vertices' final positions, by slot
     int iters, status;            // status 1: converged or stopped; 0: iteration cap; 2: non-finite
     int trials;                   // line-search energy evaluations
+    // at the start and after the first Newton step: E0, ||g0||^2, first
+    // step size, first-step trials, E1, max / min / mean-log / mean-log^2 of
+    // the per-triangle unweighted energies e/(4w), per free slot 0 and 1:
+    // |g_s|^2, g_0.g_1, triangles touching the slot, their energy
+    double raw[kLocalRaw];
+    long long cycles;             // SM clock cycles the problem's solve took
 };
 struct LocalBatch {
     const LocalProblem* prob = nullptr;
@@ -108,6 +115,9 @@ struct PcgWork {
     int* status = nullptr;         // [4] iterations, flag
     int grid = 0, block = 0, n = 0;
 };
+
+// the stream of a context (oc_api.cu)
+cudaStream_t ctx_stream(oc_ctx* ctx);
 
 // ---- launchers (kernels live in oc_fp64.cu / oc_kernels.cu) ----
 // energy at uv + alpha_k * dir for k < nTrials (dir may be null: alphas ignored)

@@ -11,6 +11,7 @@
 // meshes carry no air mesh.
 
 #include "oc_topo.h"
+#include "oc_mlp.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -230,6 +231,101 @@ bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector
 } // namespace
 
 namespace {
+
+// Solves the problems `which` of B (all at once, one warp each) into res[k];
+// maxIterOverride > 0 caps the Newton iterations.
+int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& which, int maxIterOverride, int fp32,
+                std::vector<LocalResult>& res, std::string* err)
+{
+    if (which.empty()) return OC_OK;
+    std::vector<LocalProblem> prob(which.size());
+    for (size_t i = 0; i < which.size(); ++i) {
+        prob[i] = B.prob[which[i]];
+        if (maxIterOverride > 0) prob[i].maxIter = maxIterOverride;
+    }
+    LocalBatch db;
+    db.nProb = static_cast<int>(prob.size());
+    db.fp32Hessian = fp32;
+    void* bufs[7] = {};
+    size_t sizes[7] = {sizeof(LocalProblem) * prob.size(), sizeof(int) * B.ltGlobal.size(),
+                       sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
+                       sizeof(int) * B.lvSlot.size(), sizeof(int) * B.initTri.size(),
+                       sizeof(LocalResult) * prob.size()};
+    const void* src[6] = {prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
+                          B.initTri.data()};
+    std::vector<LocalResult> out(prob.size());
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMalloc(&bufs[k], sizes[k] ? sizes[k] : 1);
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(bufs[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
+    if (e == cudaSuccess) {
+        db.prob = static_cast<const LocalProblem*>(bufs[0]);
+        db.ltGlobal = static_cast<const int*>(bufs[1]);
+        db.ltCorner = static_cast<const int*>(bufs[2]);
+        db.lvPos = static_cast<const double2*>(bufs[3]);
+        db.lvSlot = static_cast<const int*>(bufs[4]);
+        db.initTri = static_cast<const int*>(bufs[5]);
+        db.out = static_cast<LocalResult*>(bufs[6]);
+        launch_local_newton(*in.dm, in.surfaceArea, db, in.st);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), bufs[6], sizes[6], cudaMemcpyDeviceToHost, in.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(in.st);
+    }
+    for (auto* p : bufs) cudaFree(p);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("topology query: ") + cudaGetErrorString(e);
+        return OC_ERR_CUDA;
+    }
+    for (size_t i = 0; i < which.size(); ++i) res[which[i]] = out[i];
+    return OC_OK;
+}
+
+// Excess of the candidate's local energy over its isometric minimum, in the
+// global energy's units: (initE - 4) localArea / surfaceArea.
+double excess_global(const LocalProblem& P, const LocalResult& r, double surfaceArea)
+{
+    return (r.initE - 4.0) * P.localArea / surfaceArea;
+}
+
+// The 32 features of one local problem, from its header and the raw
+// quantities of its start and first Newton step.
+void topo_features(const LocalProblem& P, const LocalResult& r, int opType, const TopoQueryIn& in, float* f)
+{
+    for (int k = 0; k < kTopoNumFeatures; ++k) f[k] = 0.0f;
+    const double E0 = std::max(r.raw[0], 4.0 + 1e-12), E1 = std::max(r.raw[4], 4.0 + 1e-12);
+    const double gsq0 = r.raw[1], A = P.localArea;
+    auto lg = [](double x) { return std::log10(x + 1e-30) / 10.0; };
+    f[0] = opType == kOpBoundarySplit;
+    f[1] = opType == kOpInteriorSplit;
+    f[2] = opType == kOpMerge;
+    f[3] = static_cast<float>(std::log1p(static_cast<double>(P.nTri)) / 3.0);
+    f[4] = static_cast<float>(P.nFree / 4.0);
+    f[5] = static_cast<float>(std::log(E0 / 4.0));
+    f[6] = static_cast<float>(std::log(E1 / 4.0));
+    f[7] = static_cast<float>(std::max(-1.0, std::min(1.0, (E0 - E1) / std::max(E0 - 4.0, 1e-12))));
+    f[8] = static_cast<float>(r.raw[2]);
+    f[9] = static_cast<float>(std::min(r.raw[3], 20.0) / 20.0);
+    f[10] = static_cast<float>(lg(gsq0 * A / (E0 * E0)));
+    f[11] = static_cast<float>(std::log(std::max(r.raw[5], 1e-30)));
+    f[12] = static_cast<float>(std::log(std::max(r.raw[6], 1e-30)));
+    f[13] = static_cast<float>(r.raw[7]);
+    f[14] = static_cast<float>(std::sqrt(std::max(r.raw[8] - r.raw[7] * r.raw[7], 0.0)));
+    f[15] = static_cast<float>(r.raw[12] / P.nTri);
+    f[16] = static_cast<float>(r.raw[13] / P.nTri);
+    f[17] = static_cast<float>(r.raw[14] / E0);
+    f[18] = static_cast<float>(r.raw[15] / E0);
+    f[19] = static_cast<float>(lg(r.raw[9] * A / (E0 * E0)));
+    f[20] = static_cast<float>(lg(r.raw[10] * A / (E0 * E0)));
+    f[21] = static_cast<float>(r.raw[11] / std::sqrt(r.raw[9] * r.raw[10] + 1e-300));
+    f[22] = static_cast<float>(std::log(A / P.nTri * in.nF / in.surfaceArea));
+    // start and first-step quantities only, so a one-step probe and a full
+    // solve give the same row: converged at the start, stop test met at step 1
+    f[23] = gsq0 < P.targetGRes ? 1.0f : 0.0f;
+    f[24] = (r.raw[2] > 1.0e-3 && (E0 - E1) / E0 < 1.0e-6 * r.raw[2]) ? 1.0f : 0.0f;
+    f[25] = static_cast<float>(std::log(std::max(r.initE, 4.0 + 1e-12) / 4.0));
+    f[26] = static_cast<float>(std::max(-1.0, std::min(1.0, (r.initE - E1) / std::max(r.initE - 4.0, 1e-12))));
+    for (int k = 0; k < kTopoNumFeatures; ++k)
+        if (!std::isfinite(f[k])) f[k] = 0.0f;
+}
 
 // TriMesh::cohEIndex as computeFeatures builds it (TriMesh.cpp:448-455):
 // (c0, c1) -> row, (c3, c2) -> -row - 1, rows without a -1 entry only
@@ -473,8 +569,9 @@ int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, b
     return OC_OK;
 }
 
-int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, int options,
-               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err)
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, const TopoOptions& opts,
+               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err,
+               TopoExtras* extras)
 {
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
@@ -751,48 +848,102 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
     const auto t1 = clk::now();
     stats.buildMs = std::chrono::duration<double, std::milli>(t1 - t0).count();
 
-    // one batched device solve
+    // one batched device solve of all problems (exhaustive), or the learned
+    // proposal: a one-step pass over all problems gives their features, the
+    // MLP ranks them and only the top fraction gets the full solve
     std::vector<LocalResult> res(B.prob.size());
+    std::vector<char> solved(B.prob.size(), 1);
+    const bool learned = (opts.flags & kTopoLearned) && opts.mlp;
     if (!B.prob.empty()) {
-        LocalBatch db;
-        db.nProb = static_cast<int>(B.prob.size());
-        db.fp32Hessian = options & 1;
-        void* bufs[7] = {};
-        size_t sizes[7] = {sizeof(LocalProblem) * B.prob.size(), sizeof(int) * B.ltGlobal.size(),
-                           sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
-                           sizeof(int) * B.lvSlot.size(), sizeof(int) * B.initTri.size(),
-                           sizeof(LocalResult) * B.prob.size()};
-        const void* src[6] = {B.prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
-                              B.initTri.data()};
-        cudaError_t e = cudaSuccess;
-        for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMalloc(&bufs[k], sizes[k] ? sizes[k] : 1);
-        for (int k = 0; k < 6 && e == cudaSuccess; ++k)
-            e = cudaMemcpyAsync(bufs[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
-        if (e == cudaSuccess) {
-            db.prob = static_cast<const LocalProblem*>(bufs[0]);
-            db.ltGlobal = static_cast<const int*>(bufs[1]);
-            db.ltCorner = static_cast<const int*>(bufs[2]);
-            db.lvPos = static_cast<const double2*>(bufs[3]);
-            db.lvSlot = static_cast<const int*>(bufs[4]);
-            db.initTri = static_cast<const int*>(bufs[5]);
-            db.out = static_cast<LocalResult*>(bufs[6]);
-            launch_local_newton(*in.dm, in.surfaceArea, db, in.st);
-            e = cudaGetLastError();
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(res.data(), bufs[6], sizes[6], cudaMemcpyDeviceToHost, in.st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(in.st);
+        std::string e2;
+        if (learned) {
+            std::vector<int> all(B.prob.size());
+            for (size_t k = 0; k < all.size(); ++k) all[k] = static_cast<int>(k);
+            int rc = solve_batch(in, B, all, 1, opts.flags & kTopoFp32Hessian, res, &e2);
+            if (rc) { if (err) *err = e2; return rc; }
+            const auto tA = clk::now();
+            stats.probeMs = std::chrono::duration<double, std::milli>(tA - t1).count();
+            // features -> predicted fraction of excess energy removed -> E_w decrease
+            const int n = static_cast<int>(B.prob.size());
+            std::vector<float> X((size_t)n * kTopoNumFeatures), r(n);
+            for (int k = 0; k < n; ++k) topo_features(B.prob[k], res[k], opType, in, &X[(size_t)k * kTopoNumFeatures]);
+            rc = mlp_predict_host(*opts.mlp, X.data(), n, r.data());
+            if (rc) { if (err) *err = "topology query: MLP inference failed"; return rc; }
+            std::vector<std::pair<double, int>> pred(n);
+            for (int k = 0; k < n; ++k) {
+                const double sdd = static_cast<double>(r[k]) * excess_global(B.prob[k], res[k], in.surfaceArea);
+                const double ew = opType == kOpMerge ? lambda_t * B.tag[k].se + (1.0 - lambda_t) * sdd
+                                                     : (1.0 - lambda_t) * sdd - lambda_t * B.tag[k].se;
+                pred[k] = {-ew, k};
+            }
+            if (extras) {
+                extras->ewPred.resize(n);
+                for (int k = 0; k < n; ++k) extras->ewPred[k] = -pred[k].first * (opType == kOpInteriorSplit ? 0.5 : 1.0);
+            }
+            std::stable_sort(pred.begin(), pred.end());
+            int kTop = static_cast<int>(std::ceil(opts.topFrac * n));
+            kTop = std::max(1, std::min(n, kTop));
+            std::vector<int> sel(kTop);
+            for (int i = 0; i < kTop; ++i) sel[i] = pred[i].second;
+            std::sort(sel.begin(), sel.end());
+            std::fill(solved.begin(), solved.end(), 0);
+            for (int k : sel) solved[k] = 1;
+            stats.nSelected = kTop;
+            if (extras) {
+                extras->X.swap(X);
+                extras->predicted.assign(n, 0.0f);
+                for (int k = 0; k < n; ++k) extras->predicted[k] = r[k];
+            }
+            std::vector<LocalResult> full(B.prob.size());
+            const auto tB = clk::now();
+            rc = solve_batch(in, B, sel, -1, opts.flags & kTopoFp32Hessian, full, &e2);
+            if (rc) { if (err) *err = e2; return rc; }
+            for (int k : sel) res[k] = full[k];
+            stats.exactMs = std::chrono::duration<double, std::milli>(clk::now() - tB).count();
         }
-        for (auto* p : bufs) cudaFree(p);
-        if (e != cudaSuccess) {
-            if (err) *err = std::string("topology query: ") + cudaGetErrorString(e);
-            return OC_ERR_CUDA;
+        else {
+            std::vector<int> all(B.prob.size());
+            for (size_t k = 0; k < all.size(); ++k) all[k] = static_cast<int>(k);
+            const int rc = solve_batch(in, B, all, -1, opts.flags & kTopoFp32Hessian, res, &e2);
+            if (rc) { if (err) *err = e2; return rc; }
+            stats.nSelected = static_cast<int>(all.size());
+            if (extras && (opts.flags & kTopoRecordFeatures)) {
+                const int n = static_cast<int>(B.prob.size());
+                extras->X.assign((size_t)n * kTopoNumFeatures, 0.0f);
+                extras->target.assign(n, 0.0f);
+                for (int k = 0; k < n; ++k) {
+                    topo_features(B.prob[k], res[k], opType, in, &extras->X[(size_t)k * kTopoNumFeatures]);
+                    const double xs = excess_global(B.prob[k], res[k], in.surfaceArea);
+                    double t = xs > 0.0 ? res[k].eDec / xs : 0.0;
+                    extras->target[k] = static_cast<float>(std::max(-1.0, std::min(1.0, t)));
+                }
+            }
         }
     }
     const auto t2 = clk::now();
     stats.solveMs = std::chrono::duration<double, std::milli>(t2 - t1).count();
 
+    if (extras) {
+        extras->cand.resize(B.prob.size());
+        extras->ewExact.assign(B.prob.size(), std::nan(""));
+        for (size_t k = 0; k < B.prob.size(); ++k) extras->cand[k] = B.tag[k].cand;
+        const size_t n = B.prob.size();
+        extras->nTri.resize(n);
+        extras->nFree.resize(n);
+        extras->iters.resize(n);
+        extras->trials.resize(n);
+        extras->cycles.resize(n);
+        for (size_t k = 0; k < n; ++k) {
+            extras->nTri[k] = B.prob[k].nTri;
+            extras->nFree[k] = B.prob[k].nFree;
+            extras->iters[k] = res[k].iters;
+            extras->trials[k] = res[k].trials;
+            extras->cycles[k] = res[k].cycles;
+        }
+    }
     // per candidate: the best of its local problems (strict >, first wins)
     for (size_t k = 0; k < B.prob.size(); ++k) {
+        if (!solved[k]) continue;
         const LocalResult& r = res[k];
         const Batch::Tag& tg = B.tag[k];
         TopoCandidate& C = out[tg.cand];
@@ -805,6 +956,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
         if (opType == kOpMerge) {
             const double SDInc = -SDDec;
             EwDec = lambda_t * tg.se - (1.0 - lambda_t) * SDInc;   // TriMesh.cpp:2157
+            if (extras) extras->ewExact[k] = EwDec;
             C.ec0 = SDInc;
             C.ec1 = -tg.se;
             C.EwDec = EwDec;
@@ -812,6 +964,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
             continue;
         }
         EwDec = (1.0 - lambda_t) * SDDec - lambda_t * tg.se;   // TriMesh.cpp:2187, 2248
+        if (extras) extras->ewExact[k] = opType == kOpInteriorSplit ? 0.5 * EwDec : EwDec;
         if (EwDec > C.EwDec) {
             C.EwDec = EwDec;
             C.ec0 = -SDDec;

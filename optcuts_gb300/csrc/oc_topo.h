@@ -36,19 +36,48 @@ struct TopoQueryIn {
 };
 
 struct TopoStats {
-    int nCandidates = 0, nProblems = 0, maxIters = 0, totalIters = 0, nonConverged = 0;
+    int nCandidates = 0, nProblems = 0, maxIters = 0, totalIters = 0, nonConverged = 0, nSelected = 0;
     long long totalTrials = 0;
-    double buildMs = 0.0, solveMs = 0.0;
+    double buildMs = 0.0, solveMs = 0.0, probeMs = 0.0, exactMs = 0.0;
+};
+
+struct Mlp;
+constexpr int kTopoNumFeatures = 32;
+enum { kTopoFp32Hessian = 1, kTopoRecordFeatures = 2, kTopoLearned = 4 };
+struct TopoOptions {
+    int flags = 0;          // kTopoFp32Hessian | kTopoRecordFeatures | kTopoLearned
+    Mlp* mlp = nullptr;     // learned proposal: ranks the local problems
+    double topFrac = 0.1;   // fraction of them solved exactly
+};
+// per local problem: features (32), exact target (fraction of the local
+// excess energy the solve removed; exhaustive queries), MLP prediction
+// (learned queries); its candidate, its exact E_w decrease (NaN where not
+// solved exactly) and the predicted one (learned queries), both on the
+// candidate's scale (interior splits halved)
+struct TopoExtras {
+    std::vector<float> X, target, predicted;
+    std::vector<int> cand;
+    std::vector<double> ewExact, ewPred;
+    // per problem: triangles, free vertices, Newton iterations, line-search
+    // trials, SM cycles of the solve (the probe's for unselected problems)
+    std::vector<int> nTri, nFree, iters, trials;
+    std::vector<long long> cycles;
 };
 
 // opType: kOpBoundarySplit / kOpInteriorSplit (querySplit with
 // splitInterior false / true) or kOpMerge (queryMerge).  filterExp is the
 // interior-split filter exponent (filterExp_in, 0.6 by default).  best is
 // the index of the largest EwDec (-1 when there is no candidate).
-// options bit 0: project the local element Hessians in FP32 (faster; the
-// energies, gradients, line search and local LDL^T stay FP64)
-int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, int options,
-               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err);
+// opts.flags: kTopoFp32Hessian projects the local element Hessians in FP32
+// (faster; energies, gradients, line search and local LDL^T stay FP64);
+// kTopoRecordFeatures records every problem's features and exact target;
+// kTopoLearned (with opts.mlp) solves only the MLP's top fraction exactly
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, const TopoOptions& opts,
+               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err,
+               TopoExtras* extras = nullptr);
+
+// MLP inference on host rows (oc_mlp.cu)
+int mlp_predict_host(Mlp& m, const float* X, int n, float* y);
 
 // Applies one operation to host arrays (F nF x 3, Vrest nV x 3, UV nV x 2,
 // cohE rows x 4) with the reference's vertex and cohesive-edge bookkeeping:

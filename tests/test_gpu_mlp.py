@@ -1,0 +1,80 @@
+"""The learned proposal's MLP on the device (BF16 operands, FP32
+accumulation) against the NumPy oracle with the same rounding, and its
+training loop."""
+import numpy as np
+import pytest
+
+import optcuts_gb300 as oc
+from oracle import mlp as ref
+
+pytestmark = pytest.mark.gpu
+
+
+def data(n, nIn=32, seed=0):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(size=(n, nIn)).astype(np.float32)
+    t = np.tanh(X[:, 0] - 0.5 * X[:, 1] * X[:, 2] + 0.25 * X[:, 3] ** 2).astype(np.float32)
+    return X, t
+
+
+def test_params_round_trip():
+    m = oc.MLP(32, 128, seed=1)
+    p = m.params()
+    assert p.size == m.num_params() == 128 * 32 + 128 + 128 * 128 + 128 + 128 + 1
+    q = np.random.default_rng(2).normal(scale=0.05, size=p.size).astype(np.float32)
+    m.set_params(q)
+    np.testing.assert_array_equal(m.params(), q)
+
+
+@pytest.mark.parametrize("n", [1, 37, 1000])
+def test_forward_matches_oracle(n):
+    m = oc.MLP(32, 128, seed=5)
+    X, _ = data(n, seed=n)
+    y = m.predict(X)
+    yr = ref.forward(m.params(), X, 32, 128)[2]
+    # same BF16 operands; FP32 accumulation order differs (and may flip a
+    # BF16 rounding of a hidden activation): 1e-3 of the output scale
+    assert np.abs(y - yr).max() <= 1e-3 * (np.abs(yr).max() + 1e-3)
+
+
+@pytest.mark.parametrize("n", [3, 256, 3000])
+def test_gradient_matches_oracle(n):
+    m = oc.MLP(32, 128, seed=7)
+    X, t = data(n, seed=n + 1)
+    g, loss = m.gradient(X, t)
+    gr, lr = ref.gradient(m.params(), X, t, 32, 128)
+    assert loss == pytest.approx(lr, rel=1e-4)
+    # per block, relative to the block's norm
+    nH, nIn = 128, 32
+    offs = np.cumsum([0, nH * nIn, nH, nH * nH, nH, nH, 1])
+    for a, b in zip(offs[:-1], offs[1:]):
+        err = np.linalg.norm(g[a:b] - gr[a:b])
+        assert err <= 2e-3 * (np.linalg.norm(gr[a:b]) + 1e-12), (a, b)
+
+
+def test_gradient_step_decreases_loss():
+    """The device gradient is a descent direction of the exact loss."""
+    m = oc.MLP(32, 128, seed=11)
+    X, t = data(512, seed=12)
+    p = m.params()
+    g, l0 = m.gradient(X, t)
+    m.set_params(p - 1e-2 * g / (np.linalg.norm(g) + 1e-30))
+    _, l1 = m.gradient(X, t)
+    assert l1 < l0
+
+
+def test_training_fits():
+    m = oc.MLP(32, 128, seed=13)
+    X, t = data(8192, seed=14)
+    _, l0 = m.gradient(X, t)
+    lf = m.train(X, t, epochs=40, batch=256, lr=2e-3, seed=1)
+    Xv, tv = data(2048, seed=15)
+    yv = m.predict(Xv)
+    assert lf < 0.2 * l0
+    assert np.mean((yv - tv) ** 2) < 0.3 * np.var(tv)
+
+
+def test_invalid_arguments():
+    m = oc.MLP(32, 128)
+    with pytest.raises(oc.OCError):
+        m.train(np.zeros((0, 32), np.float32), np.zeros(0, np.float32))
