@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--no-topology", action="store_true")
     p.add_argument("--topo-newton-iters", type=int, default=400,
                    help="untimed Newton iterations (to convergence) before the topology step is timed")
+    p.add_argument("--train-at", default="60,120,200,300",
+                   help="Newton iterations whose states give the learned proposal's exhaustive training pairs")
+    p.add_argument("--top-frac", type=float, default=0.1, help="fraction of local problems solved exactly (learned)")
     return p.parse_args()
 
 
@@ -270,45 +273,103 @@ def run_ours(args, rank, world):
     # and of the interior-split query, every local solve on the GPU
     topo = None
     if not args.no_topology:
+        lam_t = 1.0 - (1.0 - args.lam)   # 1 - energyParams[0], as createFracture passes it
+        mesh.setCohesiveEdges(st.cohE)
+        train_at = sorted({int(x) for x in args.train_at.split(",") if x.strip()})
+        base_it = args.warmup + args.steps + (0 if args.no_e2e else max(3, args.steps))
+
+        def queries(**kw):
+            # one topology step of the outer loop: boundary splits, merges and
+            # interior splits (TriMesh::splitOrMerge and the interior-split
+            # query), the first query rebuilding the vertex adjacency as it
+            # does after an applied operation
+            mesh.dropAdjacency()
+            return (mesh.querySplit(lam_t, False, **kw), mesh.queryMerge(lam_t, **kw),
+                    mesh.querySplit(lam_t, True, **kw))
+
+        # exhaustive pairs (features, exact fraction of the local excess
+        # energy removed) from earlier states of the same run, then the
+        # Newton loop to convergence
+        Xs, ts, pair_states = [], [], []
         converged_after = None
         for k in range(args.topo_newton_iters):
+            if base_it + k in train_at:
+                for q in queries(features=True):
+                    if q["local_problems"]:
+                        Xs.append(q["features"])
+                        ts.append(q["target"])
+                pair_states.append(base_it + k)
             if step() == 1:
-                converged_after = args.warmup + args.steps + k + 1
+                converged_after = base_it + k + 1
                 break
-        mesh.setCohesiveEdges(st.cohE)
-        lam_t = 1.0 - (1.0 - args.lam)   # 1 - energyParams[0], as createFracture passes it
 
-        def topo_step(fp32=False):
-            return (mesh.querySplit(lam_t, False, fp32=fp32), mesh.queryMerge(lam_t, fp32=fp32),
-                    mesh.querySplit(lam_t, True, fp32=fp32))
+        def timed_step(**kw):
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            qs = queries(**kw)
+            ctx.synchronize()
+            return time.perf_counter() - t0, qs
 
-        topo_step()   # warm-up
-        ctx.synchronize()
-        t0 = time.perf_counter()
-        qb, qm, qi = topo_step()
-        ctx.synchronize()
-        t_gpu = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        fb, fm, fi = topo_step(fp32=True)
-        ctx.synchronize()
-        t_fp32 = time.perf_counter() - t0
+        def summary(qs):
+            qb, qm, qi = qs
+            return {"query_ms": sum(q["query_ms"] for q in qs),
+                    "gpu_solve_ms": sum(q["solve_ms"] for q in qs),
+                    "host_build_ms": sum(q["build_ms"] for q in qs),
+                    "local_problems": sum(q["local_problems"] for q in qs),
+                    "exact_solves": sum(q["selected"] for q in qs),
+                    "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"],
+                             "interior_split": qi["EwDec_max"]}}
+
+        queries()   # warm-up
+        t_gpu, (qb, qm, qi) = timed_step()
+        t_fp32, qs32 = timed_step(fp32=True)
         topo = {"metric": "topology-step s (exhaustive candidate evaluation)", "value": t_gpu, "unit": "s",
                 "higher_is_better": False, "bijectivity": "off (local solves without air meshes)",
                 "newton_iterations_before": converged_after if converged_after else
-                args.warmup + args.steps + args.topo_newton_iters,
+                base_it + args.topo_newton_iters,
                 "converged": converged_after is not None, "lambda": args.lam,
                 "candidates": {"boundary_split": len(qb["candidates"]), "merge": len(qm["candidates"]),
                                "interior_split": len(qi["candidates"])},
-                "local_problems": qb["local_problems"] + qm["local_problems"] + qi["local_problems"],
-                "gpu_solve_ms": qb["solve_ms"] + qm["solve_ms"] + qi["solve_ms"],
-                "host_build_ms": qb["build_ms"] + qm["build_ms"] + qi["build_ms"],
                 "max_local_iterations": max(qb["max_local_iters"], qm["max_local_iters"], qi["max_local_iters"]),
                 "local_iterations": qb["local_iters_total"] + qm["local_iters_total"] + qi["local_iters_total"],
                 "local_capped": qb["local_capped"] + qm["local_capped"] + qi["local_capped"],
-                "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"], "interior_split": qi["EwDec_max"]},
-                "fp32_hessian_option": {"value": t_fp32, "unit": "s",
-                                        "best": {"boundary_split": fb["EwDec_max"], "merge": fm["EwDec_max"],
-                                                 "interior_split": fi["EwDec_max"]}}}
+                **summary((qb, qm, qi)),
+                "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)}}
+        # the learned proposal on the same state, trained on the pairs above
+        if Xs:
+            X, t = np.concatenate(Xs), np.concatenate(ts)
+            mlp = oc.MLP(32, 128, seed=3, ctx=ctx)
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            loss = mlp.train(X, t, epochs=30, batch=512, lr=2e-3, seed=3)
+            ctx.synchronize()
+            train_s = time.perf_counter() - t0
+            queries(mlp=mlp, topFrac=args.top_frac)   # warm-up
+            t_l, ql = timed_step(mlp=mlp, topFrac=args.top_frac)
+            t_l32, ql32 = timed_step(mlp=mlp, topFrac=args.top_frac, fp32=True)
+            # E_w after the step: the outer loop applies the best operation
+            # found; the learned step must reach the same E_w within 0.5%
+            from optcuts_gb300 import init as I
+            seam = I.seam_sparsity(mesh.V_rest, mesh.V, st.cohE, avg_edge_len(st))
+            r = np.sqrt(mesh.surfaceArea / np.pi)
+            e_w = opt.getLastEnergyVal(excludeScaffold=True) + lam_t * seam / r
+
+            def after(qs):
+                return e_w - max(0.0, *(q["EwDec_max"] for q in qs))
+            ew_ex, ew_l = after((qb, qm, qi)), after(ql)
+            ew_ex32, ew_l32 = after(qs32), after(ql32)
+            topo["learned"] = {
+                "metric": "topology-step s (learned proposal, top %g of local problems solved exactly)" % args.top_frac,
+                "value": t_l, "unit": "s", "higher_is_better": False, **summary(ql),
+                "E_w_before": e_w, "E_w_after": ew_l, "E_w_after_exhaustive": ew_ex,
+                "E_w_rel_diff": abs(ew_l - ew_ex) / abs(ew_ex),
+                "fp32_hessian_option": {"value": t_l32, "unit": "s", **summary(ql32),
+                                        "E_w_after": ew_l32, "E_w_after_exhaustive": ew_ex32,
+                                        "E_w_rel_diff": abs(ew_l32 - ew_ex32) / abs(ew_ex32)},
+                "mlp": {"layers": [32, 128, 128, 1], "weights": "bf16 (fp32 master, Adam)", "accumulate": "fp32",
+                        "pairs": int(len(X)), "pair_states_newton_iteration": pair_states, "epochs": 30,
+                        "batch": 512, "seed": 3, "train_s": train_s, "final_mse": loss,
+                        "target_var": float(np.var(t))}}
         if rank == 0 and not args.no_cpu_baseline:
             import oracle as O
             threads = os.cpu_count() or 1

@@ -255,6 +255,11 @@ enum { OC_OP_BOUNDARY_SPLIT = 0, OC_OP_INTERIOR_SPLIT = 1, OC_OP_MERGE = 2 };
 typedef struct oc_topo_result oc_topo_result;
 /* TriMesh::cohE (nCohE x 4), needed by merge queries */
 int oc_mesh_set_cohesive_edges(oc_mesh* mesh, const int* cohE, int nCohE);
+/* The first topology query after a change of the mesh's triangles builds
+ * their vertex adjacency, the later ones reuse it; this drops it, so the
+ * next query pays for it again (timing a topology step as it follows an
+ * applied operation). */
+int oc_mesh_drop_adjacency(oc_mesh* mesh);
 /* SymDirichletEnergy::computeDivGradPerVert (SymDirichletEnergy.cpp:108-147)
  * at the mesh's current UV: the split filter, nV values */
 int oc_mesh_split_filter(oc_mesh* mesh, double* divGrad);
@@ -321,6 +326,11 @@ int oc_topo_result_iterations(const oc_topo_result* r, int* totalIters, int* cap
  * TriMesh.cpp:702-704), energyChanges (2), path (<= 3), newVertPos (<= 4 x 2) */
 int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, double* energyChanges, int* path,
                              int* pathLen, double* newVertPos, int* posRows);
+/* all candidates at once: EwDec (nCand), energyChanges (nCand x 2), path
+ * (nCand x 3, unused entries -1), newVertPos (nCand x 8, unused 0) and
+ * posRows (nCand); NULL arrays are skipped */
+int oc_topo_result_candidates(const oc_topo_result* r, double* EwDec, double* energyChanges, int* path,
+                              double* newVertPos, int* posRows);
 int oc_topo_result_destroy(oc_topo_result* r);
 /* Optimizer::createFracture(opType, path, newVertPos) (Optimizer.cpp:373-440):
  * applies the operation to the optimizer's mesh (TriMesh::splitEdgeOnBoundary,

@@ -18,6 +18,7 @@ visible, construction raises.
 from __future__ import annotations
 
 import ctypes
+import time
 import os
 
 import numpy as np
@@ -101,6 +102,7 @@ _SIGS = {
     "oc_air_mesh_get": [_vp, _d, _i, _i],
     "oc_air_mesh_destroy": [_vp],
     "oc_mesh_set_cohesive_edges": [_vp, _i, ctypes.c_int],
+    "oc_mesh_drop_adjacency": [_vp],
     "oc_mesh_split_filter": [_vp, _d],
     "oc_topology_query": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_vp)],
     "oc_topo_result_info": [_vp, _i, _i, _i, _i, _i, _d, _d],
@@ -118,6 +120,7 @@ _SIGS = {
                                 ctypes.POINTER(ctypes.c_float)],
     "oc_topo_result_timing": [_vp, _i, _d, _d],
     "oc_topo_result_problems": [_vp, _i, _vp, _vp, _vp],
+    "oc_topo_result_candidates": [_vp, _vp, _vp, _vp, _vp, _vp],
     "oc_topo_result_problem_stats": [_vp, _i, _vp, _vp, _vp, _vp, _vp],
     "oc_mlp_create": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)],
     "oc_mlp_destroy": [_vp],
@@ -278,6 +281,11 @@ class TriMesh:
         c = _i4(np.asarray(cohE).reshape(-1, 4))
         self.ctx.check(lib().oc_mesh_set_cohesive_edges(self.h, _pi(c), len(c)), "setCohesiveEdges")
 
+    def dropAdjacency(self):
+        """Forget the cached vertex adjacency: the next topology query
+        rebuilds it, as the first query after an applied operation does."""
+        self.ctx.check(lib().oc_mesh_drop_adjacency(self.h), "dropAdjacency")
+
     def splitFilter(self):
         """SymDirichletEnergy::computeDivGradPerVert at the current UV."""
         out = np.zeros(self.nV)
@@ -287,12 +295,14 @@ class TriMesh:
     def _query(self, op, lambda_t, filterExp, fp32, features=False, mlp=None, topFrac=0.1):
         h = _vp()
         opt = (1 if fp32 else 0) | (2 if features else 0)
+        t0 = time.perf_counter()
         if mlp is not None:
             self.ctx.check(lib().oc_topology_query_learned(self.h, op, float(lambda_t), float(filterExp), opt, mlp.h,
                                                            float(topFrac), ctypes.byref(h)), "learned topology query")
         else:
             self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), opt,
                                                    ctypes.byref(h)), "topology query")
+        query_ms = 1000.0 * (time.perf_counter() - t0)
         try:
             n, best, pool, nprob, mit = (ctypes.c_int() for _ in range(5))
             bms, sms = ctypes.c_double(), ctypes.c_double()
@@ -302,35 +312,37 @@ class TriMesh:
             lib().oc_topo_result_iterations(h, ctypes.byref(tot), ctypes.byref(cap), ctypes.byref(tri))
             nsel, pms, ems = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
             lib().oc_topo_result_timing(h, ctypes.byref(nsel), ctypes.byref(pms), ctypes.byref(ems))
-            nrow = ctypes.c_int()
-            lib().oc_topo_result_features(h, ctypes.byref(nrow), None, None, None)
-            X = np.zeros((nrow.value, 32), np.float32)
-            tgt = np.zeros(nrow.value, np.float32)
-            prd = np.zeros(nrow.value, np.float32)
-            if nrow.value:
-                lib().oc_topo_result_features(h, ctypes.byref(nrow), _pf(X),
-                                              _pf(tgt) if features else None, _pf(prd) if mlp is not None else None)
+            X = tgt = prd = None
+            if features or mlp is not None:
+                nrow = ctypes.c_int()
+                lib().oc_topo_result_features(h, ctypes.byref(nrow), None, None, None)
+                X = np.zeros((nrow.value, 32), np.float32)
+                tgt = np.zeros(nrow.value, np.float32) if features else None
+                prd = np.zeros(nrow.value, np.float32) if mlp is not None else None
+                if nrow.value:
+                    lib().oc_topo_result_features(h, ctypes.byref(nrow), _pf(X), None if tgt is None else _pf(tgt),
+                                                  None if prd is None else _pf(prd))
             npb = ctypes.c_int()
             lib().oc_topo_result_problems(h, ctypes.byref(npb), None, None, None)
             pc = np.zeros(npb.value, np.int32)
             pe, pp = np.zeros(npb.value), np.zeros(npb.value)
-            if npb.value:
-                lib().oc_topo_result_problems(h, ctypes.byref(npb), pc.ctypes.data_as(_vp), pe.ctypes.data_as(_vp),
-                                              pp.ctypes.data_as(_vp))
             pstat = {k: np.zeros(npb.value, np.int32) for k in ("nTri", "nFree", "iters", "trials")}
             pstat["cycles"] = np.zeros(npb.value, np.int64)
             if npb.value:
+                lib().oc_topo_result_problems(h, ctypes.byref(npb), pc.ctypes.data_as(_vp), pe.ctypes.data_as(_vp),
+                                              pp.ctypes.data_as(_vp))
                 lib().oc_topo_result_problem_stats(h, ctypes.byref(npb), *(pstat[k].ctypes.data_as(_vp) for k in
                                                    ("nTri", "nFree", "iters", "trials", "cycles")))
-            cands = []
-            for c in range(n.value):
-                ew, ec = ctypes.c_double(), np.zeros(2)
-                path, plen = np.zeros(3, np.int32), ctypes.c_int()
-                pos, rows = np.zeros(8), ctypes.c_int()
-                lib().oc_topo_result_candidate(h, c, ctypes.byref(ew), _pd(ec), _pi(path), ctypes.byref(plen),
-                                               _pd(pos), ctypes.byref(rows))
-                cands.append({"EwDec": ew.value, "energyChanges": (float(ec[0]), float(ec[1])),
-                              "path": path[:plen.value].tolist(), "newVertPos": pos[:2 * rows.value].reshape(-1, 2)})
+            nc = n.value
+            ew, ec = np.zeros(nc), np.zeros((nc, 2))
+            paths, pos, rows = np.zeros((nc, 3), np.int32), np.zeros((nc, 8)), np.zeros(nc, np.int32)
+            if nc:
+                lib().oc_topo_result_candidates(h, ew.ctypes.data_as(_vp), ec.ctypes.data_as(_vp),
+                                                paths.ctypes.data_as(_vp), pos.ctypes.data_as(_vp),
+                                                rows.ctypes.data_as(_vp))
+            cands = [{"EwDec": float(ew[c]), "energyChanges": (float(ec[c, 0]), float(ec[c, 1])),
+                      "path": [int(x) for x in paths[c] if x >= 0],
+                      "newVertPos": pos[c, :2 * rows[c]].reshape(-1, 2)} for c in range(nc)]
         finally:
             lib().oc_topo_result_destroy(h)
         b = best.value
@@ -339,9 +351,8 @@ class TriMesh:
                 "local_problems": nprob.value, "max_local_iters": mit.value, "build_ms": bms.value,
                 "solve_ms": sms.value, "local_iters_total": tot.value, "local_capped": cap.value,
                 "local_trials_total": tri.value, "selected": nsel.value, "probe_ms": pms.value,
-                "exact_ms": ems.value, "features": X, "target": tgt if features else None,
-                "predicted": prd if mlp is not None else None,
-                "problems": dict(cand=pc, EwDec=pe, EwDec_pred=pp, **pstat)}
+                "exact_ms": ems.value, "features": X, "target": tgt, "predicted": prd,
+                "problems": dict(cand=pc, EwDec=pe, EwDec_pred=pp, **pstat), "query_ms": query_ms}
 
     def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6, fp32=False, features=False, mlp=None,
                    topFrac=0.1):

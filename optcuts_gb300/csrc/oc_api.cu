@@ -40,6 +40,7 @@ struct oc_mesh {
     double2* tmpV = nullptr;        // nV scratch
     double* hb = nullptr;           // 21 x nF packed Hessians
     double* tmpF = nullptr;         // nF x 36 scratch for API outputs (lazy)
+    std::shared_ptr<oc::TopoAdjacency> adj;   // adjacency of F for topology queries (lazy)
 };
 
 struct oc_linsys {
@@ -684,6 +685,7 @@ int oc_sd_init_step_size(oc_mesh* m, const double* searchDir, double* stepSize)
 static int mesh_rebuild(oc_mesh* m, const std::vector<double>& uvHost)
 {
     oc_ctx* ctx = m->ctx;
+    m->adj.reset();
     const int nV = static_cast<int>(m->Vrest.size() / 3), nF = static_cast<int>(m->F.size() / 3);
     double surfaceArea = 0.0;
     std::vector<double> rest;
@@ -758,6 +760,13 @@ int oc_mesh_set_cohesive_edges(oc_mesh* m, const int* cohE, int nCohE)
     return OC_OK;
 }
 
+int oc_mesh_drop_adjacency(oc_mesh* m)
+{
+    if (!m) return OC_ERR_INVALID;
+    m->adj.reset();
+    return OC_OK;
+}
+
 int oc_mesh_split_filter(oc_mesh* m, double* divGrad)
 {
     if (!m || !divGrad) return OC_ERR_INVALID;
@@ -827,6 +836,8 @@ static int topology_query(oc_mesh* m, int opType, double lambda_t, double filter
     in.divGrad = dg.empty() ? nullptr : dg.data();
     in.dm = &m->d;
     in.st = m->ctx->stream;
+    if (!m->adj) m->adj = oc::topo_adjacency(nV, m->F.data(), m->d.nF);
+    in.adj = m->adj.get();
     oc_topo_result* r = new (std::nothrow) oc_topo_result;
     if (!r) return OC_ERR_NOMEM;
     std::string err;
@@ -921,6 +932,23 @@ int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, doub
     if (path) std::copy(C.path.begin(), C.path.end(), path);
     if (posRows) *posRows = static_cast<int>(C.pos.size() / 2);
     if (newVertPos) std::copy(C.pos.begin(), C.pos.end(), newVertPos);
+    return OC_OK;
+}
+
+int oc_topo_result_candidates(const oc_topo_result* r, double* EwDec, double* energyChanges, int* path,
+                              double* newVertPos, int* posRows)
+{
+    if (!r) return OC_ERR_INVALID;
+    for (size_t c = 0; c < r->cands.size(); ++c) {
+        const oc::TopoCandidate& C = r->cands[c];
+        if (EwDec) EwDec[c] = C.EwDec;
+        if (energyChanges) { energyChanges[2 * c] = C.ec0; energyChanges[2 * c + 1] = C.ec1; }
+        if (path)
+            for (int k = 0; k < 3; ++k) path[3 * c + k] = k < (int)C.path.size() ? C.path[k] : -1;
+        if (newVertPos)
+            for (int k = 0; k < 8; ++k) newVertPos[8 * c + k] = k < (int)C.pos.size() ? C.pos[k] : 0.0;
+        if (posRows) posRows[c] = static_cast<int>(C.pos.size() / 2);
+    }
     return OC_OK;
 }
 

@@ -346,47 +346,124 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
     }
 }
 
-// FP32 cyclic Jacobi for the local topology solves (same rotations; stops
-// at FP32 convergence or stagnation).
-__device__ void jacobi_eig6f(float A[6][6], float V[6][6])
+// Cyclic Jacobi eigen-decomposition of a symmetric 4x4 (A destroyed: its
+// diagonal holds the eigenvalues; V the eigenvectors as columns); stops at
+// convergence or when the off-diagonal mass stops decreasing.
+template <typename T>
+__device__ void jacobi_eig4(T A[4][4], T V[4][4], T tol)
 {
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) V[i][j] = (i == j) ? 1.0f : 0.0f;
-    float fro = 0.0f;
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) fro += A[i][j] * A[i][j];
-    float prevOff = 0.0f;
-    for (int sweep = 0; sweep < 30; ++sweep) {
-        float off = 0.0f;
-        for (int p = 0; p < 6; ++p)
-            for (int q = p + 1; q < 6; ++q) off += A[p][q] * A[p][q];
-        if (off <= 1e-14f * fro || (sweep > 0 && off >= prevOff)) break;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? T(1) : T(0);
+    T fro = T(0);
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) fro += A[i][j] * A[i][j];
+    T prevOff = T(0);
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        T off = T(0);
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) off += A[p][q] * A[p][q];
+        if (off <= tol * fro || (sweep > 0 && off >= prevOff)) break;
         prevOff = off;
-        for (int p = 0; p < 6; ++p) {
-            for (int q = p + 1; q < 6; ++q) {
-                const float apq = A[p][q];
-                if (apq == 0.0f) continue;
-                const float theta = (A[q][q] - A[p][p]) / (2.0f * apq);
-                const float t = (theta >= 0 ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
-                const float c = 1.0f / sqrtf(t * t + 1.0f), sn = t * c;
-                for (int k = 0; k < 6; ++k) {
-                    const float akp = A[k][p], akq = A[k][q];
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) {
+                const T apq = A[p][q];
+                if (apq == T(0)) continue;
+                const T theta = (A[q][q] - A[p][p]) / (T(2) * apq);
+                const T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+                const T c = T(1) / sqrt(t * t + T(1)), sn = t * c;
+                for (int k = 0; k < 4; ++k) {
+                    const T akp = A[k][p], akq = A[k][q];
                     A[k][p] = c * akp - sn * akq;
                     A[k][q] = sn * akp + c * akq;
                 }
-                for (int k = 0; k < 6; ++k) {
-                    const float apk = A[p][k], aqk = A[q][k];
+                for (int k = 0; k < 4; ++k) {
+                    const T apk = A[p][k], aqk = A[q][k];
                     A[p][k] = c * apk - sn * aqk;
                     A[q][k] = sn * apk + c * aqk;
                 }
-                for (int k = 0; k < 6; ++k) {
-                    const float vkp = V[k][p], vkq = V[k][q];
+                for (int k = 0; k < 4; ++k) {
+                    const T vkp = V[k][p], vkq = V[k][q];
                     V[k][p] = c * vkp - sn * vkq;
                     V[k][q] = sn * vkp + c * vkq;
                 }
             }
-        }
     }
+}
+
+// makePD of a triangle's 6x6 Hessian for the local topology solves, in the
+// 4-dimensional complement of the two rigid translations (H t = 0 for them,
+// so H = Q K Q^T with K = Q^T H Q): Q = B (x) I2, B the orthonormal 3x2 basis
+// [-1/sqrt2, -1/sqrt6; 1/sqrt2, -1/sqrt6; 0, 2/sqrt6] of the vectors
+// orthogonal to (1, 1, 1).  K PSD up to -1e-13 of its largest diagonal
+// leaves H unchanged (makePD's early return); otherwise K = V Lambda V^T,
+// negative eigenvalues clamped to zero and H = (Q V) Lambda+ (Q V)^T: the same
+// projection as the 6x6 eigen-clamp, at about a fifth of its arithmetic.
+// T = float projects in FP32 (scaled by the largest |K_ii|).
+template <typename T>
+__device__ void project_psd_reduced(double H[6][6])
+{
+    const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637;
+    const double B[3][2] = {{-r2, -r6}, {r2, -r6}, {0.0, 2.0 * r6}};
+    double Tm[4][6];   // Q^T H
+    for (int k = 0; k < 2; ++k)
+        for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < 6; ++c) {
+                double acc = 0.0;
+                for (int i = 0; i < 3; ++i) acc = acc + B[i][k] * H[2 * i + b][c];
+                Tm[2 * k + b][c] = acc;
+            }
+    double K[4][4];
+    for (int r = 0; r < 4; ++r)
+        for (int l = 0; l < 2; ++l)
+            for (int d = 0; d < 2; ++d) {
+                double acc = 0.0;
+                for (int j = 0; j < 3; ++j) acc = acc + Tm[r][2 * j + d] * B[j][l];
+                K[r][2 * l + d] = acc;
+            }
+    for (int r = 0; r < 4; ++r)   // symmetric up to rounding: use the mean
+        for (int c = r + 1; c < 4; ++c) {
+            const double m = 0.5 * (K[r][c] + K[c][r]);
+            K[r][c] = m;
+            K[c][r] = m;
+        }
+    double dmax = 0.0;
+    for (int i = 0; i < 4; ++i) dmax = fmax(dmax, fabs(K[i][i]));
+    {   // LDL^T without pivoting: no pivot below -1e-13 dmax -> PSD
+        double A[4][4];
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) A[i][j] = K[i][j];
+        const double tol = 1e-13 * dmax;
+        bool psd = true;
+        for (int k = 0; k < 4 && psd; ++k) {
+            const double d = A[k][k];
+            if (d < -tol) psd = false;
+            else if (d > tol)
+                for (int i = k + 1; i < 4; ++i) {
+                    const double l = A[i][k] / d;
+                    for (int j = k + 1; j <= i; ++j) A[i][j] = A[i][j] - l * A[j][k];
+                }
+        }
+        if (psd) return;
+    }
+    const double scale = dmax > 0.0 ? dmax : 1.0;
+    T A[4][4], V[4][4];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) A[i][j] = static_cast<T>(K[i][j] / scale);
+    jacobi_eig4<T>(A, V, sizeof(T) == 8 ? T(1e-34) : T(1e-14));
+    double lam[4];
+    for (int m = 0; m < 4; ++m) lam[m] = A[m][m] < T(0) ? 0.0 : static_cast<double>(A[m][m]) * scale;
+    double W[6][4];   // Q V
+    for (int i = 0; i < 3; ++i)
+        for (int a = 0; a < 2; ++a)
+            for (int m = 0; m < 4; ++m)
+                W[2 * i + a][m] = B[i][0] * static_cast<double>(V[a][m]) + B[i][1] * static_cast<double>(V[2 + a][m]);
+    for (int r = 0; r < 6; ++r)
+        for (int c = r; c < 6; ++c) {
+            double acc = 0.0;
+            for (int m = 0; m < 4; ++m) acc = acc + W[r][m] * lam[m] * W[c][m];
+            H[r][c] = acc;
+            H[c][r] = acc;
+        }
 }
 
 // Per-triangle Hessian (SymDirichletEnergy.cpp:440-522) projected to PSD by
@@ -397,8 +474,8 @@ __device__ void jacobi_eig6f(float A[6][6], float V[6][6])
 // change the Newton direction, and reducing to the 4-dimensional
 // translation-free part first does not reproduce the reference.
 // Output: the upper triangle as 21 values per triangle (SoA).
-// localMode 0: exact (the global Newton); 1: skip the projection when H is
-// PSD up to rounding (local solves, FP64); 2: as 1 but project in FP32
+// localMode 0: exact (the global Newton); 1: the reduced 4x4 projection
+// (local solves, FP64); 2: as 1 with the eigen-decomposition in FP32
 __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, double e1d, double e01d, double w,
                             double H[6][6], int localMode = 0)
 {
@@ -440,50 +517,17 @@ __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, do
             }
         }
     }
+    if (localMode == 1) {
+        project_psd_reduced<double>(H);
+        return;
+    }
+    if (localMode == 2) {
+        project_psd_reduced<float>(H);
+        return;
+    }
     double A[6][6], V[6][6];
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
-    if (localMode) {
-        // LDL^T without pivoting: no pivot below -1e-13 of the largest
-        // diagonal means H is PSD up to rounding and makePD would return it
-        // unchanged up to that rounding, so the eigen-decomposition is skipped
-        double dmax = 0.0;
-        for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(A[i][i]));
-        const double tol = 1e-13 * dmax;
-        bool psd = true;
-        for (int k = 0; k < 6 && psd; ++k) {
-            const double d = A[k][k];
-            if (d < -tol) psd = false;
-            else if (d > tol)
-                for (int i = k + 1; i < 6; ++i) {
-                    const double l = A[i][k] / d;
-                    for (int j = k + 1; j <= i; ++j) A[i][j] = A[i][j] - l * A[j][k];
-                }
-        }
-        if (psd) return;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
-    }
-    if (localMode == 2) {
-        double dmax = 0.0;
-        for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(H[i][i]));
-        // FP32 projection, scaled to the block's largest diagonal entry:
-        // enough for the Newton step of a 2-8 DOF local problem
-        float Af[6][6], Vf[6][6];
-        const double scale = dmax > 0.0 ? dmax : 1.0;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) Af[i][j] = static_cast<float>(H[i][j] / scale);
-        jacobi_eig6f(Af, Vf);
-        float lamf[6];
-        for (int i = 0; i < 6; ++i) lamf[i] = Af[i][i] < 0.0f ? 0.0f : Af[i][i];
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
-                float sum = 0.0f;
-                for (int k = 0; k < 6; ++k) sum += Vf[i][k] * lamf[k] * Vf[j][k];
-                H[i][j] = static_cast<double>(sum) * scale;
-            }
-        return;
-    }
     jacobi_eig6(A, V);
     double lam[6], lmin = A[0][0];
     for (int i = 0; i < 6; ++i) {
@@ -581,23 +625,44 @@ __global__ void __launch_bounds__(256) k_divgrad(DeviceMesh m, const double2* __
 }
 
 // ---------------------------------------------------- local topology solves
-// One warp per local problem: the projected-Newton loop the reference runs
-// on a candidate's local mesh (Optimizer with useDense, energyParams {1},
-// relGL2Tol 1e-6, solve(maxIter): Optimizer.cpp:203-261, 505-652; dense
-// Hessian SymDirichletEnergy.cpp:306-427 + LDLT).  Lanes own triangles;
-// sums over triangles are taken in triangle order by single lanes, so the
-// result is deterministic.
-constexpr int kLocalChunk = 32;
+// A group of TPP threads per local problem runs the projected-Newton loop
+// the reference runs on a candidate's local mesh (Optimizer with useDense,
+// energyParams {1}, relGL2Tol 1e-6, solve(maxIter): Optimizer.cpp:203-261,
+// 505-652; dense Hessian SymDirichletEnergy.cpp:306-427 + LDLT).  Threads
+// own triangles (t = sub, sub + TPP, ...); every sum over triangles is
+// taken in triangle order by a single thread, so the result is the same for
+// every TPP and deterministic.  TPP 8 and 32 pack several problems into a
+// 128-thread block (sub-warp groups); TPP 128 and 256 give one problem a
+// whole block, for the large fans around high-valence vertices.
 
+template <int TPP>
 struct LocalShared {
     double2 pos[kLocalMaxFree], pos0[kLocalMaxFree];
     double dir[2 * kLocalMaxFree], g[2 * kLocalMaxFree];
     double H[2 * kLocalMaxFree][2 * kLocalMaxFree];
-    double triE[kLocalChunk];
-    double triG[kLocalChunk][6];
-    double triH[kLocalChunk][21];
-    int triSlot[kLocalChunk][3];
+    double bc[2];   // broadcast slots
+    double triE[TPP];
+    double triG[TPP][6];
+    double triH[TPP][21];
+    int triSlot[TPP][3];
 };
+
+template <int TPP>
+struct LocalGroup {
+    unsigned mask;
+    int sub;
+    __device__ __forceinline__ void sync() const
+    {
+        if constexpr (TPP <= 32) __syncwarp(mask);
+        else __syncthreads();
+    }
+};
+
+template <int TPP>
+__host__ __device__ constexpr int local_groups() { return TPP >= 128 ? 1 : 128 / TPP; }
+
+template <int TPP>
+constexpr size_t local_smem() { return local_groups<TPP>() * sizeof(LocalShared<TPP>); }
 
 __device__ __forceinline__ int sym21(int i, int j)   // packed upper triangle of a 6x6
 {
@@ -606,8 +671,10 @@ __device__ __forceinline__ int sym21(int i, int j)   // packed upper triangle of
 }
 
 // corner positions and free slots of local triangle t, at pos (+ alpha dir)
-__device__ __forceinline__ void local_corners(const LocalBatch& b, const LocalProblem& P, const LocalShared& S, int t,
-                                              const double2* pos, bool withDir, double alpha, double2 U[3], int slot[3])
+template <int TPP>
+__device__ __forceinline__ void local_corners(const LocalBatch& b, const LocalProblem& P, const LocalShared<TPP>& S,
+                                              int t, const double2* pos, bool withDir, double alpha, double2 U[3],
+                                              int slot[3])
 {
     for (int k = 0; k < 3; ++k) {
         const int lv = b.ltCorner[3 * (P.triOff + t) + k];
@@ -627,13 +694,25 @@ __device__ __forceinline__ void local_corners(const LocalBatch& b, const LocalPr
     }
 }
 
+// value computed by the group's first thread, seen by all
+template <int TPP>
+__device__ __forceinline__ double local_bcast(LocalShared<TPP>& S, const LocalGroup<TPP>& G, double v)
+{
+    if (G.sub == 0) S.bc[0] = v;
+    G.sync();
+    v = S.bc[0];
+    G.sync();
+    return v;
+}
+
 // local energy (weights triArea / localArea) at pos0 + alpha dir or at pos
-__device__ double local_energy(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P, LocalShared& S,
-                               const double2* pos, bool withDir, double alpha, int lane)
+template <int TPP>
+__device__ double local_energy(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P, LocalShared<TPP>& S,
+                               const LocalGroup<TPP>& G, const double2* pos, bool withDir, double alpha)
 {
     double acc = 0.0;
-    for (int c0 = 0; c0 < P.nTri; c0 += kLocalChunk) {
-        const int t = c0 + lane;
+    for (int c0 = 0; c0 < P.nTri; c0 += TPP) {
+        const int t = c0 + G.sub;
         double e = 0.0;
         if (t < P.nTri) {
             double2 U[3];
@@ -642,89 +721,111 @@ __device__ double local_energy(const DeviceMesh& m, const LocalBatch& b, const L
             const int g = b.ltGlobal[P.triOff + t];
             e = elem_energy(m, g, m.area[g] / P.localArea, U[0], U[1], U[2]);
         }
-        S.triE[lane] = e;
-        __syncwarp();
-        if (lane == 0) {
-            const int n = min(kLocalChunk, P.nTri - c0);
+        S.triE[G.sub] = e;
+        G.sync();
+        if (G.sub == 0) {
+            const int n = min(TPP, P.nTri - c0);
             for (int k = 0; k < n; ++k) acc = acc + S.triE[k];
         }
-        __syncwarp();
+        G.sync();
     }
-    return __shfl_sync(0xffffffffu, acc, 0);
+    return local_bcast(S, G, acc);
 }
 
-__global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m, double surfaceArea, LocalBatch b)
+template <int TPP>
+__global__ void __launch_bounds__(TPP >= 128 ? TPP : 128, TPP >= 128 ? 1 : 3) k_local_newton(DeviceMesh m, double surfaceArea,
+                                                                          LocalBatch b)
 {
-    __shared__ LocalShared shared[kLocalWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pi = blockIdx.x * kLocalWarps + warp;
-    if (pi >= b.nProb) return;   // uniform per warp
-    LocalShared& S = shared[warp];
+    extern __shared__ __align__(16) unsigned char localSmem[];
+    constexpr int kGroups = local_groups<TPP>();
+    const int grp = threadIdx.x / TPP;
+    const int pi = blockIdx.x * kGroups + grp;
+    if (pi >= b.nProb) return;   // uniform per group (whole block for TPP >= 128)
+    LocalGroup<TPP> G;
+    G.sub = threadIdx.x % TPP;
+    G.mask = TPP >= 32 ? 0xffffffffu : (((1u << TPP) - 1u) << ((threadIdx.x & 31) & ~(TPP - 1)));
+    LocalShared<TPP>& S = reinterpret_cast<LocalShared<TPP>*>(localSmem)[grp];
+    const int sub = G.sub;
     const long long clk0 = clock64();
     const LocalProblem P = b.prob[pi];
     const int nDof = 2 * P.nFree;
-    for (int j = lane; j < P.nVert; j += 32) {
+    for (int j = sub; j < P.nVert; j += TPP) {
         const int sl = b.lvSlot[P.vertOff + j];
         if (sl >= 0) S.pos[sl] = b.lvPos[P.vertOff + j];
     }
-    __syncwarp();
+    G.sync();
     // initial energy: the candidate's global triangles with global weights,
     // rescaled to the local mesh (TriMesh.cpp:2355-2361)
     double initE = 0.0;
-    if (lane == 0) {
-        for (int k = 0; k < P.nInit; ++k) {
+    for (int c0 = 0; c0 < P.nInit; c0 += TPP) {
+        const int k = c0 + sub;
+        double e = 0.0;
+        if (k < P.nInit) {
             const int g = b.initTri[P.initOff + k];
-            initE = initE + elem_energy(m, g, m.w[g], m.uv[m.F0[g]], m.uv[m.F1[g]], m.uv[m.F2[g]]);
+            e = elem_energy(m, g, m.w[g], m.uv[m.F0[g]], m.uv[m.F1[g]], m.uv[m.F2[g]]);
         }
-        initE = initE * (surfaceArea / P.localArea);
+        S.triE[sub] = e;
+        G.sync();
+        if (sub == 0) {
+            const int n = min(TPP, P.nInit - c0);
+            for (int q = 0; q < n; ++q) initE = initE + S.triE[q];
+        }
+        G.sync();
     }
-    initE = __shfl_sync(0xffffffffu, initE, 0);
-    double lastE = local_energy(m, b, P, S, S.pos, false, 0.0, lane);   // precompute
+    initE = local_bcast(S, G, initE * (surfaceArea / P.localArea));
+    double lastE = local_energy(m, b, P, S, G, S.pos, false, 0.0);   // precompute
     int status = 0, it = 0, trials = 0;
     bool finite = isfinite(lastE);
-    // raw quantities of the starting point (features of the learned proposal)
+    // raw quantities of the starting point (features of the learned
+    // proposal), summed in triangle order like everything else
     double raw[kLocalRaw];
     for (int k = 0; k < kLocalRaw; ++k) raw[k] = 0.0;
     {
         double emax = 0.0, emin = 1e300, lsum = 0.0, lsq = 0.0;
         double g0x = 0.0, g0y = 0.0, g1x = 0.0, g1y = 0.0, n0 = 0.0, n1 = 0.0, es0 = 0.0, es1 = 0.0;
-        for (int t = lane; t < P.nTri; t += 32) {
-            double2 U[3];
-            int sl[3];
-            local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
-            const int g = b.ltGlobal[P.triOff + t];
-            const double w = m.area[g] / P.localArea;
-            const double e = elem_energy(m, g, w, U[0], U[1], U[2]);
-            const double eu = e / (4.0 * w);
-            emax = fmax(emax, eu);
-            emin = fmin(emin, eu);
-            const double l = log(eu);
-            lsum += l;
-            lsq += l * l;
-            double2 cg[3];
-            tri_corner_grads(U[0], U[1], U[2], m.A2[g], m.e0[g], m.e1[g], m.e01[g], w, cg);
-            bool touch0 = false, touch1 = false;
-            for (int k = 0; k < 3; ++k) {
-                if (sl[k] == 0) { g0x += cg[k].x; g0y += cg[k].y; touch0 = true; }
-                if (sl[k] == 1) { g1x += cg[k].x; g1y += cg[k].y; touch1 = true; }
+        for (int c0 = 0; c0 < P.nTri; c0 += TPP) {
+            const int t = c0 + sub;
+            if (t < P.nTri) {
+                double2 U[3];
+                int sl[3];
+                local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
+                const int g = b.ltGlobal[P.triOff + t];
+                const double w = m.area[g] / P.localArea;
+                const double e = elem_energy(m, g, w, U[0], U[1], U[2]);
+                const double eu = e / (4.0 * w);
+                double2 cg[3];
+                tri_corner_grads(U[0], U[1], U[2], m.A2[g], m.e0[g], m.e1[g], m.e01[g], w, cg);
+                double q[4] = {0.0, 0.0, 0.0, 0.0};
+                double touch0 = 0.0, touch1 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    if (sl[k] == 0) { q[0] += cg[k].x; q[1] += cg[k].y; touch0 = 1.0; }
+                    if (sl[k] == 1) { q[2] += cg[k].x; q[3] += cg[k].y; touch1 = 1.0; }
+                }
+                for (int k = 0; k < 4; ++k) S.triG[sub][k] = q[k];
+                S.triH[sub][0] = e;
+                S.triH[sub][1] = eu;
+                S.triH[sub][2] = log(eu);
+                S.triH[sub][3] = touch0;
+                S.triH[sub][4] = touch1;
             }
-            if (touch0) { n0 += 1.0; es0 += e; }
-            if (touch1) { n1 += 1.0; es1 += e; }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
-            emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, o));
-            lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
-            lsq += __shfl_xor_sync(0xffffffffu, lsq, o);
-            g0x += __shfl_xor_sync(0xffffffffu, g0x, o);
-            g0y += __shfl_xor_sync(0xffffffffu, g0y, o);
-            g1x += __shfl_xor_sync(0xffffffffu, g1x, o);
-            g1y += __shfl_xor_sync(0xffffffffu, g1y, o);
-            n0 += __shfl_xor_sync(0xffffffffu, n0, o);
-            n1 += __shfl_xor_sync(0xffffffffu, n1, o);
-            es0 += __shfl_xor_sync(0xffffffffu, es0, o);
-            es1 += __shfl_xor_sync(0xffffffffu, es1, o);
+            G.sync();
+            if (sub == 0) {
+                const int n = min(TPP, P.nTri - c0);
+                for (int k = 0; k < n; ++k) {
+                    const double e = S.triH[k][0], eu = S.triH[k][1], l = S.triH[k][2];
+                    emax = fmax(emax, eu);
+                    emin = fmin(emin, eu);
+                    lsum += l;
+                    lsq += l * l;
+                    g0x += S.triG[k][0];
+                    g0y += S.triG[k][1];
+                    g1x += S.triG[k][2];
+                    g1y += S.triG[k][3];
+                    if (S.triH[k][3] != 0.0) { n0 += 1.0; es0 += e; }
+                    if (S.triH[k][4] != 0.0) { n1 += 1.0; es1 += e; }
+                }
+            }
+            G.sync();
         }
         raw[0] = lastE;
         raw[5] = emax;
@@ -740,11 +841,12 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         raw[15] = es1;
         raw[4] = lastE;   // E1: replaced after the first step
     }
+    constexpr int kEntRounds = (36 + TPP - 1) / TPP;
     for (; it < P.maxIter && finite; ++it) {
         // gradient (fixed vertices have no slot: zero rows)
         double gj = 0.0;
-        for (int c0 = 0; c0 < P.nTri; c0 += kLocalChunk) {
-            const int t = c0 + lane;
+        for (int c0 = 0; c0 < P.nTri; c0 += TPP) {
+            const int t = c0 + sub;
             if (t < P.nTri) {
                 double2 U[3];
                 int sl[3];
@@ -753,22 +855,22 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 double2 cg[3];
                 tri_corner_grads(U[0], U[1], U[2], m.A2[g], m.e0[g], m.e1[g], m.e01[g], m.area[g] / P.localArea, cg);
                 for (int k = 0; k < 3; ++k) {
-                    S.triG[lane][2 * k] = cg[k].x;
-                    S.triG[lane][2 * k + 1] = cg[k].y;
-                    S.triSlot[lane][k] = sl[k];
+                    S.triG[sub][2 * k] = cg[k].x;
+                    S.triG[sub][2 * k + 1] = cg[k].y;
+                    S.triSlot[sub][k] = sl[k];
                 }
             }
-            __syncwarp();
-            if (lane < nDof) {
-                const int n = min(kLocalChunk, P.nTri - c0);
+            G.sync();
+            if (sub < nDof) {
+                const int n = min(TPP, P.nTri - c0);
                 for (int q = 0; q < n; ++q)
                     for (int k = 0; k < 3; ++k)
-                        if (S.triSlot[q][k] == (lane >> 1)) gj = gj + S.triG[q][2 * k + (lane & 1)];
+                        if (S.triSlot[q][k] == (sub >> 1)) gj = gj + S.triG[q][2 * k + (sub & 1)];
             }
-            __syncwarp();
+            G.sync();
         }
-        if (lane < nDof) S.g[lane] = gj;
-        __syncwarp();
+        if (sub < nDof) S.g[sub] = gj;
+        G.sync();
         double gsq = 0.0;
         for (int j = 0; j < nDof; ++j) gsq = gsq + S.g[j] * S.g[j];
         if (it == 0) raw[1] = gsq;
@@ -779,9 +881,10 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         // dense Hessian of the free DOFs: projected triangle blocks summed in
         // triangle order (IglUtils::addBlockToMatrix, IglUtils.cpp:453-489)
         const int nEnt = nDof * (nDof + 1) / 2;
-        double hacc[2] = {0.0, 0.0};
-        for (int c0 = 0; c0 < P.nTri; c0 += kLocalChunk) {
-            const int t = c0 + lane;
+        double hacc[kEntRounds];
+        for (int r = 0; r < kEntRounds; ++r) hacc[r] = 0.0;
+        for (int c0 = 0; c0 < P.nTri; c0 += TPP) {
+            const int t = c0 + sub;
             if (t < P.nTri) {
                 double2 U[3];
                 int sl[3];
@@ -791,13 +894,13 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 tri_hessian(U, m.A2[g], m.e0d[g], m.e1d[g], m.e01d[g], m.area[g] / P.localArea, H6,
                             b.fp32Hessian ? 2 : 1);
                 for (int i = 0; i < 6; ++i)
-                    for (int j = i; j < 6; ++j) S.triH[lane][sym21(i, j)] = H6[i][j];
-                for (int k = 0; k < 3; ++k) S.triSlot[lane][k] = sl[k];
+                    for (int j = i; j < 6; ++j) S.triH[sub][sym21(i, j)] = H6[i][j];
+                for (int k = 0; k < 3; ++k) S.triSlot[sub][k] = sl[k];
             }
-            __syncwarp();
-            const int n = min(kLocalChunk, P.nTri - c0);
-            for (int r = 0; r < 2; ++r) {
-                const int e = lane + 32 * r;
+            G.sync();
+            const int n = min(TPP, P.nTri - c0);
+            for (int r = 0; r < kEntRounds; ++r) {
+                const int e = sub + TPP * r;
                 if (e >= nEnt) continue;
                 // entry e -> (i, j), i <= j, row-major upper triangle
                 int i = 0, rem = e;
@@ -813,10 +916,10 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                     }
                 hacc[r] = acc;
             }
-            __syncwarp();
+            G.sync();
         }
-        for (int r = 0; r < 2; ++r) {
-            const int e = lane + 32 * r;
+        for (int r = 0; r < kEntRounds; ++r) {
+            const int e = sub + TPP * r;
             if (e >= nEnt) continue;
             int i = 0, rem = e;
             while (rem >= nDof - i) { rem -= nDof - i; ++i; }
@@ -824,10 +927,10 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
             S.H[i][j] = hacc[r];
             S.H[j][i] = hacc[r];
         }
-        __syncwarp();
+        G.sync();
         // H d = -g by LDL^T with symmetric pivoting on the largest remaining
         // diagonal (Eigen::LDLT); zero pivots give zero components
-        if (lane == 0) {
+        if (sub == 0) {
             double A[2 * kLocalMaxFree][2 * kLocalMaxFree], x[2 * kLocalMaxFree];
             int perm[2 * kLocalMaxFree];
             for (int i = 0; i < nDof; ++i) {
@@ -868,11 +971,11 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 for (int k = i + 1; k < nDof; ++k) y[i] = y[i] - A[k][i] * y[k];
             for (int i = 0; i < nDof; ++i) S.dir[perm[i]] = y[i];
         }
-        __syncwarp();
+        G.sync();
         // line search (Optimizer.cpp:575-652): injective bound x 0.99, halve
         // until E <= E_last, relative-decrease stop test
         double bound = 1.0;
-        for (int t = lane; t < P.nTri; t += 32) {
+        for (int t = sub; t < P.nTri; t += TPP) {
             double2 U[3], D[3];
             int sl[3];
             local_corners(b, P, S, t, S.pos, false, 0.0, U, sl);
@@ -880,13 +983,16 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 D[k] = sl[k] >= 0 ? make_double2(S.dir[2 * sl[k]], S.dir[2 * sl[k] + 1]) : make_double2(0.0, 0.0);
             bound = fmin(bound, tri_step_bound(U[0], U[1], U[2], D[0], D[1], D[2], 1.0));
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) bound = fmin(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+        S.triE[sub] = bound;
+        G.sync();
+        if (sub == 0)
+            for (int k = 1; k < TPP; ++k) bound = fmin(bound, S.triE[k]);
+        bound = local_bcast(S, G, bound);
         double step = bound * 0.99;
-        if (lane < P.nFree) S.pos0[lane] = S.pos[lane];
-        __syncwarp();
+        if (sub < P.nFree) S.pos0[sub] = S.pos[sub];
+        G.sync();
         bool stopped = false;
-        double testE = local_energy(m, b, P, S, S.pos0, true, step, lane);
+        double testE = local_energy(m, b, P, S, G, S.pos0, true, step);
         ++trials;
         while (testE > lastE) {
             step = step / 2.0;
@@ -894,14 +1000,14 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
                 stopped = true;
                 break;
             }
-            testE = local_energy(m, b, P, S, S.pos0, true, step, lane);
+            testE = local_energy(m, b, P, S, G, S.pos0, true, step);
             ++trials;
         }
-        if (lane < P.nFree) {
-            S.pos[lane].x = S.pos0[lane].x + step * S.dir[2 * lane];
-            S.pos[lane].y = S.pos0[lane].y + step * S.dir[2 * lane + 1];
+        if (sub < P.nFree) {
+            S.pos[sub].x = S.pos0[sub].x + step * S.dir[2 * sub];
+            S.pos[sub].y = S.pos0[sub].y + step * S.dir[2 * sub + 1];
         }
-        __syncwarp();
+        G.sync();
         const double lastEDec = lastE - testE;
         if ((lastEDec / lastE < 1.0e-6 * step) && (step > 1.0e-3)) stopped = true;
         lastE = testE;
@@ -918,7 +1024,7 @@ __global__ void __launch_bounds__(32 * kLocalWarps) k_local_newton(DeviceMesh m,
         }
     }
     if (!finite) status = 2;
-    if (lane == 0) {
+    if (sub == 0) {
         LocalResult r;
         r.initE = initE;
         r.lastE = lastE;
@@ -1046,10 +1152,38 @@ void launch_init_step(const DeviceMesh& m, const double2* dir, double stepSize, 
     k_init_step<<<reduce_blocks_for(m.nF), 256, 0, st>>>(m, dir, stepSize, s.minBits);
 }
 
-void launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, cudaStream_t st)
+namespace {
+template <int TPP>
+cudaError_t launch_local_tpp(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, cudaStream_t st)
 {
-    if (b.nProb <= 0) return;
-    k_local_newton<<<(b.nProb + kLocalWarps - 1) / kLocalWarps, 32 * kLocalWarps, 0, st>>>(m, surfaceArea, b);
+    constexpr size_t smem = local_smem<TPP>();
+    static const cudaError_t attr = cudaFuncSetAttribute(k_local_newton<TPP>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         static_cast<int>(smem));
+    if (attr != cudaSuccess) return attr;
+    constexpr int groups = local_groups<TPP>();
+    constexpr int threads = TPP >= 128 ? TPP : 128;
+    k_local_newton<TPP><<<(b.nProb + groups - 1) / groups, threads, smem, st>>>(m, surfaceArea, b);
+    return cudaGetLastError();
+}
+} // namespace
+
+int local_tpp_for(int nTri)
+{
+    return nTri <= 8 ? 8 : nTri <= 40 ? 32 : nTri <= 160 ? 128 : 256;
+}
+
+cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, int tpp,
+                                cudaStream_t st)
+{
+    if (b.nProb <= 0) return cudaSuccess;
+    switch (tpp) {
+    case 8: return launch_local_tpp<8>(m, surfaceArea, b, st);
+    case 32: return launch_local_tpp<32>(m, surfaceArea, b, st);
+    case 128: return launch_local_tpp<128>(m, surfaceArea, b, st);
+    case 256: return launch_local_tpp<256>(m, surfaceArea, b, st);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st)

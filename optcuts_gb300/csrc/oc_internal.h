@@ -75,7 +75,6 @@ struct DeviceBsr {
 // One local problem of the batched topology queries: a candidate split or
 // merge evaluated on its local mesh (TriMesh::computeLocalEdDec_*).
 constexpr int kLocalMaxFree = 4;    // free local vertices (8 DOF)
-constexpr int kLocalWarps = 4;      // local problems per block (one warp each)
 struct LocalProblem {
     int triOff, nTri;      // local triangles: rows of ltGlobal / ltCorner
     int vertOff, nVert;    // local vertices: rows of lvPos / lvSlot
@@ -143,8 +142,12 @@ void launch_check_inversion(const DeviceMesh& m, Scratch& s, cudaStream_t st);
 void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st, double* out = nullptr);
 int reduce_blocks_for(int n);
 
-// batched projected-Newton solves of the topology candidates' local problems
-void launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, cudaStream_t st);
+// batched projected-Newton solves of the topology candidates' local
+// problems, tpp threads per problem (8, 32, 128 or 256; local_tpp_for picks
+// it from the problem's triangle count); results do not depend on tpp
+cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, int tpp,
+                                cudaStream_t st);
+int local_tpp_for(int nTri);
 // SymDirichletEnergy::computeDivGradPerVert (standard-deviation filter) into divGrad (nV)
 void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st);
 

@@ -48,20 +48,45 @@ struct Topo {
                 hoTo[fill[a]] = b;
                 hoTri[fill[a]++] = t;
             }
-        std::vector<std::vector<int>> adj(nV);
+        // out-half-edges of each vertex sorted by target (edge_tri bisects)
+        {
+            std::vector<std::pair<int, int>> seg;
+            for (int a = 0; a < nV; ++a) {
+                const int p0 = hoPtr[a], p1 = hoPtr[a + 1];
+                if (p1 - p0 < 2) continue;
+                seg.clear();
+                for (int p = p0; p < p1; ++p) seg.push_back({hoTo[p], hoTri[p]});
+                std::sort(seg.begin(), seg.end());
+                for (int p = p0; p < p1; ++p) {
+                    hoTo[p] = seg[p - p0].first;
+                    hoTri[p] = seg[p - p0].second;
+                }
+            }
+        }
+        // undirected neighbours: out- and in-half-edges, sorted, unique
+        std::vector<int> cnt(nV + 1, 0);
+        for (int a = 0; a < nV; ++a) {
+            cnt[a + 1] += hoPtr[a + 1] - hoPtr[a];
+            for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) cnt[hoTo[p] + 1]++;
+        }
+        for (int v = 0; v < nV; ++v) cnt[v + 1] += cnt[v];
+        std::vector<int> all(cnt[nV]);
+        std::vector<int> pos(cnt.begin(), cnt.end() - 1);
         for (int a = 0; a < nV; ++a)
             for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) {
-                adj[a].push_back(hoTo[p]);
-                adj[hoTo[p]].push_back(a);
+                all[pos[a]++] = hoTo[p];
+                all[pos[hoTo[p]]++] = a;
             }
         nbPtr.assign(nV + 1, 0);
+        nb.clear();
+        nb.reserve(all.size() / 2 + nV);
         for (int v = 0; v < nV; ++v) {
-            std::sort(adj[v].begin(), adj[v].end());
-            adj[v].erase(std::unique(adj[v].begin(), adj[v].end()), adj[v].end());
-            nbPtr[v + 1] = nbPtr[v] + static_cast<int>(adj[v].size());
+            auto b0 = all.begin() + cnt[v], b1 = all.begin() + cnt[v + 1];
+            std::sort(b0, b1);
+            b1 = std::unique(b0, b1);
+            nb.insert(nb.end(), b0, b1);
+            nbPtr[v + 1] = static_cast<int>(nb.size());
         }
-        nb.resize(nbPtr[nV]);
-        for (int v = 0; v < nV; ++v) std::copy(adj[v].begin(), adj[v].end(), nb.begin() + nbPtr[v]);
         bnd.assign(nV, 0);
         for (int v = 0; v < nV; ++v)   // TriMesh::isBoundaryVert(vI), TriMesh.cpp:2069-2083
             for (int p = nbPtr[v]; p < nbPtr[v + 1] && !bnd[v]; ++p)
@@ -70,9 +95,13 @@ struct Topo {
 
     int edge_tri(int a, int b) const
     {
-        for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p)
-            if (hoTo[p] == b) return hoTri[p];
-        return -1;
+        int lo = hoPtr[a], hi = hoPtr[a + 1];
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (hoTo[mid] < b) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo < hoPtr[a + 1] && hoTo[lo] == b ? hoTri[lo] : -1;
     }
 
     int degree(int v) const { return nbPtr[v + 1] - nbPtr[v]; }
@@ -106,6 +135,21 @@ struct Topo {
     }
 };
 
+} // namespace
+
+struct TopoAdjacency {
+    Topo T;
+};
+
+std::shared_ptr<TopoAdjacency> topo_adjacency(int nV, const int* F, int nF)
+{
+    auto a = std::make_shared<TopoAdjacency>();
+    a->T.build(nV, F, nF);
+    return a;
+}
+
+namespace {
+
 double rest_dist(const double* Vr, int a, int b)
 {
     const double dx = Vr[3 * a] - Vr[3 * b], dy = Vr[3 * a + 1] - Vr[3 * b + 1], dz = Vr[3 * a + 2] - Vr[3 * b + 2];
@@ -131,14 +175,20 @@ struct Batch {
 struct LocalMesh {
     std::vector<int> gv;        // local -> global
     std::vector<int> corner;    // 3 per triangle
+    std::vector<int>* map = nullptr;   // global -> local of the last build (-1 elsewhere), nV entries
     int find(int g) const
     {
+        if (map) return (*map)[g];
         for (size_t i = 0; i < gv.size(); ++i)
             if (gv[i] == g) return static_cast<int>(i);
         return -1;
     }
     void build(const Topo& T, const std::vector<int>& tris, int aliasA = -1, int aliasB = -1)
     {
+        if (map) {
+            if (map->size() != static_cast<size_t>(T.nV)) map->assign(T.nV, -1);
+            for (int g : gv) (*map)[g] = -1;
+        }
         gv.clear();
         corner.clear();
         for (int t : tris)
@@ -149,6 +199,7 @@ struct LocalMesh {
                 if (l < 0) {
                     l = static_cast<int>(gv.size());
                     gv.push_back(g);
+                    if (map) (*map)[g] = l;
                 }
                 corner.push_back(l);
             }
@@ -232,19 +283,38 @@ bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector
 
 namespace {
 
-// Solves the problems `which` of B (all at once, one warp each) into res[k];
+// Solves the problems `which` of B into res[k], grouped by size class
+// (threads per problem from local_tpp_for), the classes launched on their
+// own streams so that the few large fans overlap the many small problems;
 // maxIterOverride > 0 caps the Newton iterations.
 int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& which, int maxIterOverride, int fp32,
                 std::vector<LocalResult>& res, std::string* err)
 {
     if (which.empty()) return OC_OK;
+    constexpr int kClasses = 4;
+    const int tppOf[kClasses] = {256, 128, 32, 8};   // largest first: the long poles start first
+    auto classOf = [&](int nTri) {
+        const int t = local_tpp_for(nTri);
+        for (int c = 0; c < kClasses; ++c)
+            if (tppOf[c] == t) return c;
+        return kClasses - 1;
+    };
+    int count[kClasses] = {};
+    for (int k : which) count[classOf(B.prob[k].nTri)]++;
+    int start[kClasses + 1] = {};
+    for (int c = 0; c < kClasses; ++c) start[c + 1] = start[c] + count[c];
+    std::vector<int> order(which.size());   // position in the class-sorted batch -> index into which
+    {
+        int fill[kClasses];
+        for (int c = 0; c < kClasses; ++c) fill[c] = start[c];
+        for (size_t i = 0; i < which.size(); ++i) order[fill[classOf(B.prob[which[i]].nTri)]++] = static_cast<int>(i);
+    }
     std::vector<LocalProblem> prob(which.size());
-    for (size_t i = 0; i < which.size(); ++i) {
-        prob[i] = B.prob[which[i]];
-        if (maxIterOverride > 0) prob[i].maxIter = maxIterOverride;
+    for (size_t p = 0; p < which.size(); ++p) {
+        prob[p] = B.prob[which[order[p]]];
+        if (maxIterOverride > 0) prob[p].maxIter = maxIterOverride;
     }
     LocalBatch db;
-    db.nProb = static_cast<int>(prob.size());
     db.fp32Hessian = fp32;
     void* bufs[7] = {};
     size_t sizes[7] = {sizeof(LocalProblem) * prob.size(), sizeof(int) * B.ltGlobal.size(),
@@ -254,28 +324,48 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& w
     const void* src[6] = {prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
                           B.initTri.data()};
     std::vector<LocalResult> out(prob.size());
+    cudaStream_t aux[kClasses] = {};
+    cudaEvent_t ev[kClasses + 1] = {};
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMalloc(&bufs[k], sizes[k] ? sizes[k] : 1);
     for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(bufs[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
+    for (int c = 0; c <= kClasses && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[kClasses], in.st);   // uploads done
     if (e == cudaSuccess) {
-        db.prob = static_cast<const LocalProblem*>(bufs[0]);
         db.ltGlobal = static_cast<const int*>(bufs[1]);
         db.ltCorner = static_cast<const int*>(bufs[2]);
         db.lvPos = static_cast<const double2*>(bufs[3]);
         db.lvSlot = static_cast<const int*>(bufs[4]);
         db.initTri = static_cast<const int*>(bufs[5]);
-        db.out = static_cast<LocalResult*>(bufs[6]);
-        launch_local_newton(*in.dm, in.surfaceArea, db, in.st);
-        e = cudaGetLastError();
+        for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
+            if (!count[c]) continue;
+            e = cudaStreamCreateWithFlags(&aux[c], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(aux[c], ev[kClasses], 0);
+            LocalBatch cb = db;
+            cb.prob = static_cast<const LocalProblem*>(bufs[0]) + start[c];
+            cb.out = static_cast<LocalResult*>(bufs[6]) + start[c];
+            cb.nProb = count[c];
+            if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, tppOf[c], aux[c]);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[c], aux[c]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(in.st, ev[c], 0);
+        }
         if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), bufs[6], sizes[6], cudaMemcpyDeviceToHost, in.st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(in.st);
     }
+    if (e != cudaSuccess) cudaStreamSynchronize(in.st);
+    for (int c = 0; c < kClasses; ++c)
+        if (aux[c]) {
+            cudaStreamSynchronize(aux[c]);
+            cudaStreamDestroy(aux[c]);
+        }
+    for (auto& x : ev)
+        if (x) cudaEventDestroy(x);
     for (auto* p : bufs) cudaFree(p);
     if (e != cudaSuccess) {
         if (err) *err = std::string("topology query: ") + cudaGetErrorString(e);
         return OC_ERR_CUDA;
     }
-    for (size_t i = 0; i < which.size(); ++i) res[which[i]] = out[i];
+    for (size_t p = 0; p < which.size(); ++p) res[which[order[p]]] = out[p];
     return OC_OK;
 }
 
@@ -583,12 +673,20 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
         if (err) *err = "topology query: bad arguments";
         return OC_ERR_INVALID;
     }
-    Topo T;
-    T.build(in.nV, in.F, in.nF);
+    Topo ownT;
+    if (!in.adj) ownT.build(in.nV, in.F, in.nF);
+    const Topo& T = in.adj ? in.adj->T : ownT;
+    if (T.nV != in.nV || T.nF != in.nF || T.F != in.F) {
+        if (err) *err = "topology query: adjacency of another mesh";
+        return OC_ERR_INVALID;
+    }
     const double R = in.virtualRadius;
     Batch B;
     std::vector<int> tris, tris1, tris2;
+    std::vector<int> vmap(in.nV, -1);
+    std::vector<char> triMark(in.nF, 0), sideMarkB(in.nF, 0), sideMarkI(in.nF, 0);
     LocalMesh L;
+    L.map = &vmap;
 
     if (opType == kOpBoundarySplit || opType == kOpInteriorSplit) {
         if (!in.divGrad) {
@@ -628,12 +726,18 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
                     T.walk(vb, vi, false, tris);
                     T.walk(vb, vi, true, tris1);
                     tris.insert(tris.end(), tris1.begin(), tris1.end());
-                    if (cutThrough)
+                    if (cutThrough) {
+                        for (int t : tris) triMark[t] = 1;
                         for (int cw = 0; cw < 2; ++cw) {
                             T.walk(vi, vb, cw != 0, tris2);
                             for (int t : tris2)
-                                if (std::find(tris.begin(), tris.end(), t) == tris.end()) tris.push_back(t);
+                                if (!triMark[t]) {
+                                    triMark[t] = 1;
+                                    tris.push_back(t);
+                                }
                         }
+                        for (int t : tris) triMark[t] = 0;
+                    }
                     // local split (TriMesh::splitEdgeOnBoundary on the local
                     // mesh, TriMesh.cpp:2864-3036): the copy of vb takes the
                     // fan on the (vi -> vb) side; with cutThrough the copy of
@@ -644,16 +748,21 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
                     std::vector<int> sideB, sideI;
                     T.walk(vb, vi, true, sideB);
                     if (cutThrough) T.walk(vi, vb, true, sideI);
+                    else sideI.clear();
+                    for (int t : sideB) sideMarkB[t] = 1;
+                    for (int t : sideI) sideMarkI[t] = 1;
                     for (size_t k = 0; k < tris.size(); ++k) {
                         const int t = tris[k];
-                        const bool inB = std::find(sideB.begin(), sideB.end(), t) != sideB.end();
-                        const bool inI = cutThrough && std::find(sideI.begin(), sideI.end(), t) != sideI.end();
+                        const bool inB = sideMarkB[t] != 0;
+                        const bool inI = cutThrough && sideMarkI[t] != 0;
                         for (int c = 0; c < 3; ++c) {
                             int& lc = L.corner[3 * k + c];
                             if (inB && lc == lb) lc = nLoc;
                             else if (inI && lc == li) lc = nLoc + 1;
                         }
                     }
+                    for (int t : sideB) sideMarkB[t] = 0;
+                    for (int t : sideI) sideMarkI[t] = 0;
                     std::vector<double2> extra;
                     const double2 pb = make_double2(in.UV[2 * (size_t)vb], in.UV[2 * (size_t)vb + 1]);
                     const double2 pi = make_double2(in.UV[2 * (size_t)vi], in.UV[2 * (size_t)vi + 1]);
@@ -712,12 +821,16 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
                             if (vNew == p0) { ok = false; break; }
                         }
                         if (!ok) continue;
-                        LocalMesh Lc = L;
+                        LocalMesh Lc;
+                        Lc.gv = L.gv;
+                        Lc.corner = L.corner;
+                        for (int t : left) triMark[t] = 1;
                         for (int k = 0; k < n; ++k) {
-                            if (std::find(left.begin(), left.end(), umbrella[k]) == left.end()) continue;
+                            if (!triMark[umbrella[k]]) continue;
                             for (int c = 0; c < 3; ++c)
                                 if (Lc.corner[3 * k + c] == lv) Lc.corner[3 * k + c] = nLoc;
                         }
+                        for (int t : left) triMark[t] = 0;
                         std::vector<double2> extra{make_double2(in.UV[2 * (size_t)vI], in.UV[2 * (size_t)vI + 1])};
                         // newVertPos rows: the copy, then vI
                         std::vector<int> slot(nLoc + 1, -1);

@@ -5,6 +5,7 @@
 
 #include "oc_internal.h"
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -21,6 +22,11 @@ struct TopoCandidate {
     double EwDec = 0.0;         // E_w decrease used for the choice (interior splits halved)
 };
 
+// vertex adjacency and half-edges of one mesh topology, built once and
+// shared by the queries of a topology step (opaque; oc_topo.cpp)
+struct TopoAdjacency;
+std::shared_ptr<TopoAdjacency> topo_adjacency(int nV, const int* F, int nF);
+
 struct TopoQueryIn {
     int nV = 0, nF = 0;
     const int* F = nullptr;          // nF x 3
@@ -32,6 +38,7 @@ struct TopoQueryIn {
     double surfaceArea = 0.0, avgEdgeLen = 0.0, virtualRadius = 0.0;
     const double* divGrad = nullptr; // nV (split filter)
     const DeviceMesh* dm = nullptr;  // device copy of the same mesh (rest constants, UV)
+    const TopoAdjacency* adj = nullptr;   // adjacency of F (built here when null)
     cudaStream_t st = nullptr;
 };
 

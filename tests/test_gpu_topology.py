@@ -126,3 +126,37 @@ def test_create_fracture_through_the_optimizer(golden, case):
         assert opt.getLastEnergyVal() <= e
         e = opt.getLastEnergyVal()
     assert m.checkInversion()
+
+
+@pytest.mark.parametrize("nlon,nlat", [(24, 8), (72, 10), (200, 10)])
+def test_problem_size_classes_match_oracle(nlon, nlat):
+    """Pole fans of 24, 72 and 200 triangles put boundary-split problems in
+    every threads-per-problem class (8, 32, 128, 256 threads); each class
+    sums in triangle order, so every candidate's E_w decrease and new
+    positions agree with the oracle's to rounding at the converged state
+    (the local solves project the element Hessians in the translation-free
+    4x4 form, the oracle with the reference's 6x6 eigen-clamp)."""
+    import os
+
+    import oracle as O
+    from optcuts_gb300 import init as I
+    from optcuts_gb300 import meshes as M
+    V, F = M.ellipsoid(nlon, nlat, (1.0, 0.6, 0.4), 8, 6, 0.02, 2)
+    st = I.init_uv(V, F)
+    mesh = oc.TriMesh(st.V_rest, st.UV, st.F, st.fixedVert)
+    opt = oc.Optimizer(mesh, [0.001])
+    opt.precompute()
+    opt.solve(300)
+    mesh.setCohesiveEdges(st.cohE)
+    sizes = set()
+    for op in (oc.OP_BOUNDARY_SPLIT, oc.OP_INTERIOR_SPLIT):
+        q = mesh.querySplit(0.999, splitInterior=op == oc.OP_INTERIOR_SPLIT)
+        ref, _ = O.topology_query(mesh.V_rest, mesh.V, mesh.F, st.cohE, op, 0.999, threads=os.cpu_count() or 1)
+        assert len(q["candidates"]) == len(ref)
+        for c, r in zip(q["candidates"], ref):
+            assert c["EwDec"] == pytest.approx(r["EwDec"], rel=1e-8, abs=1e-12)
+            assert c["path"] == r["path"]
+            if len(r["newVertPos"]) != 4:   # cut-through splits: see compare()
+                np.testing.assert_allclose(c["newVertPos"], r["newVertPos"], rtol=1e-6, atol=1e-9)
+        sizes.update(int(n) for n in q["problems"]["nTri"])
+    assert max(sizes) >= nlon and min(sizes) <= 8
