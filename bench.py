@@ -313,6 +313,9 @@ def run_ours(args, rank, world):
         def summary(qs):
             qb, qm, qi = qs
             return {"query_ms": sum(q["query_ms"] for q in qs),
+                    "per_query_ms": {name: {"query": q["query_ms"], "build": q["build_ms"], "solve": q["solve_ms"],
+                                            "probe": q["probe_ms"], "exact": q["exact_ms"]}
+                                     for name, q in zip(("boundary_split", "merge", "interior_split"), qs)},
                     "gpu_solve_ms": sum(q["solve_ms"] for q in qs),
                     "host_build_ms": sum(q["build_ms"] for q in qs),
                     "local_problems": sum(q["local_problems"] for q in qs),

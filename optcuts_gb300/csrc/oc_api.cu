@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -838,6 +839,14 @@ static int topology_query(oc_mesh* m, int opType, double lambda_t, double filter
     in.st = m->ctx->stream;
     if (!m->adj) m->adj = oc::topo_adjacency(nV, m->F.data(), m->d.nF);
     in.adj = m->adj.get();
+    // largest cluster of blocks per local problem: the device's (16 or 8)
+    // unless the OC_LOCAL_CLUSTER environment variable caps it at 1, 2, 4 or 8
+    static const int bigCluster = [] {
+        const char* e = std::getenv("OC_LOCAL_CLUSTER");
+        const int v = e ? std::atoi(e) : 0;
+        return (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
+    }();
+    in.bigCluster = bigCluster;
     oc_topo_result* r = new (std::nothrow) oc_topo_result;
     if (!r) return OC_ERR_NOMEM;
     std::string err;

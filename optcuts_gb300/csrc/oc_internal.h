@@ -143,11 +143,18 @@ void launch_reduce_final(Scratch& s, int nBlocks, int nVals, cudaStream_t st, do
 int reduce_blocks_for(int n);
 
 // batched projected-Newton solves of the topology candidates' local
-// problems, tpp threads per problem (8, 32, 128 or 256; local_tpp_for picks
-// it from the problem's triangle count); results do not depend on tpp
-cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, int tpp,
+// problems: tpp threads per problem, or per block of a cluster of `cluster`
+// blocks (schedules 8/1, 32/1, 128/1, 64/2, 64/4, 64/8, 64/16);
+// local_schedule picks one for a size class (largest triangle count, number
+// of problems), local_max_cluster is 16 where the device runs 16-block
+// clusters of this kernel, else 8
+struct LocalSchedule {
+    int tpp = 32, cluster = 1, block = 128;   // block: threads per block (several problems for tpp <= 32)
+};
+LocalSchedule local_schedule(int maxTri, int count, int numSMs, int maxCluster);
+int local_max_cluster();
+cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, LocalSchedule sc,
                                 cudaStream_t st);
-int local_tpp_for(int nTri);
 // SymDirichletEnergy::computeDivGradPerVert (standard-deviation filter) into divGrad (nV)
 void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st);
 

@@ -49,48 +49,57 @@ struct Topo {
                 hoTri[fill[a]++] = t;
             }
         // out-half-edges of each vertex sorted by target (edge_tri bisects)
-        {
-            std::vector<std::pair<int, int>> seg;
-            for (int a = 0; a < nV; ++a) {
-                const int p0 = hoPtr[a], p1 = hoPtr[a + 1];
-                if (p1 - p0 < 2) continue;
-                seg.clear();
-                for (int p = p0; p < p1; ++p) seg.push_back({hoTo[p], hoTri[p]});
-                std::sort(seg.begin(), seg.end());
-                for (int p = p0; p < p1; ++p) {
-                    hoTo[p] = seg[p - p0].first;
-                    hoTri[p] = seg[p - p0].second;
-                }
-            }
-        }
-        // undirected neighbours: out- and in-half-edges, sorted, unique
-        std::vector<int> cnt(nV + 1, 0);
         for (int a = 0; a < nV; ++a) {
-            cnt[a + 1] += hoPtr[a + 1] - hoPtr[a];
-            for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) cnt[hoTo[p] + 1]++;
-        }
-        for (int v = 0; v < nV; ++v) cnt[v + 1] += cnt[v];
-        std::vector<int> all(cnt[nV]);
-        std::vector<int> pos(cnt.begin(), cnt.end() - 1);
-        for (int a = 0; a < nV; ++a)
-            for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) {
-                all[pos[a]++] = hoTo[p];
-                all[pos[hoTo[p]]++] = a;
+            const int p0 = hoPtr[a], p1 = hoPtr[a + 1];
+            for (int p = p0 + 1; p < p1; ++p) {   // insertion sort: a handful per vertex
+                const int to = hoTo[p], tri = hoTri[p];
+                int q = p;
+                for (; q > p0 && hoTo[q - 1] > to; --q) {
+                    hoTo[q] = hoTo[q - 1];
+                    hoTri[q] = hoTri[q - 1];
+                }
+                hoTo[q] = to;
+                hoTri[q] = tri;
             }
+        }
+        // in-half-edges of each vertex (sources ascending: counting sort
+        // over sources in order)
+        std::vector<int> hiPtr(nV + 1, 0), hiFrom(3 * (size_t)nF);
+        for (int a = 0; a < nV; ++a)
+            for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) hiPtr[hoTo[p] + 1]++;
+        for (int v = 0; v < nV; ++v) hiPtr[v + 1] += hiPtr[v];
+        {
+            std::vector<int> pos(hiPtr.begin(), hiPtr.end() - 1);
+            for (int a = 0; a < nV; ++a)
+                for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) hiFrom[pos[hoTo[p]]++] = a;
+        }
+        // neighbours = out-targets merged with in-sources; a neighbour in
+        // only one of the two lists is across a boundary edge
+        // (TriMesh::isBoundaryVert, TriMesh.cpp:2069-2083)
         nbPtr.assign(nV + 1, 0);
         nb.clear();
-        nb.reserve(all.size() / 2 + nV);
+        nb.reserve(3 * (size_t)nF + nV);
+        bnd.assign(nV, 0);
         for (int v = 0; v < nV; ++v) {
-            auto b0 = all.begin() + cnt[v], b1 = all.begin() + cnt[v + 1];
-            std::sort(b0, b1);
-            b1 = std::unique(b0, b1);
-            nb.insert(nb.end(), b0, b1);
+            int i = hoPtr[v], j = hiPtr[v];
+            const int ie = hoPtr[v + 1], je = hiPtr[v + 1];
+            while (i < ie || j < je) {
+                if (j >= je || (i < ie && hoTo[i] < hiFrom[j])) {
+                    nb.push_back(hoTo[i++]);
+                    bnd[v] = 1;
+                }
+                else if (i >= ie || hiFrom[j] < hoTo[i]) {
+                    nb.push_back(hiFrom[j++]);
+                    bnd[v] = 1;
+                }
+                else {
+                    nb.push_back(hoTo[i]);
+                    ++i;
+                    ++j;
+                }
+            }
             nbPtr[v + 1] = static_cast<int>(nb.size());
         }
-        bnd.assign(nV, 0);
-        for (int v = 0; v < nV; ++v)   // TriMesh::isBoundaryVert(vI), TriMesh.cpp:2069-2083
-            for (int p = nbPtr[v]; p < nbPtr[v + 1] && !bnd[v]; ++p)
-                if (edge_tri(v, nb[p]) < 0 || edge_tri(nb[p], v) < 0) bnd[v] = 1;
     }
 
     int edge_tri(int a, int b) const
@@ -284,23 +293,29 @@ bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector
 namespace {
 
 // Solves the problems `which` of B into res[k], grouped by size class
-// (threads per problem from local_tpp_for), the classes launched on their
-// own streams so that the few large fans overlap the many small problems;
+// (threads per problem and cluster size from local_schedule_for), the
+// classes launched on their own streams so that the few large fans overlap
+// the many small problems;
 // maxIterOverride > 0 caps the Newton iterations.
 int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& which, int maxIterOverride, int fp32,
                 std::vector<LocalResult>& res, std::string* err)
 {
     if (which.empty()) return OC_OK;
+    // size classes, largest first so that the long poles start first, each
+    // with the schedule its size and count call for
     constexpr int kClasses = 4;
-    const int tppOf[kClasses] = {256, 128, 32, 8};   // largest first: the long poles start first
-    auto classOf = [&](int nTri) {
-        const int t = local_tpp_for(nTri);
-        for (int c = 0; c < kClasses; ++c)
-            if (tppOf[c] == t) return c;
-        return kClasses - 1;
-    };
-    int count[kClasses] = {};
-    for (int k : which) count[classOf(B.prob[k].nTri)]++;
+    auto classOf = [&](int nTri) { return nTri > 160 ? 0 : nTri > 40 ? 1 : nTri > 8 ? 2 : 3; };
+    int count[kClasses] = {}, maxTri[kClasses] = {};
+    for (int k : which) {
+        const int c = classOf(B.prob[k].nTri);
+        count[c]++;
+        maxTri[c] = std::max(maxTri[c], B.prob[k].nTri);
+    }
+    int dev = 0, numSMs = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
+    const int maxCluster = in.bigCluster > 0 ? in.bigCluster : local_max_cluster();
+    LocalSchedule sched[kClasses];
+    for (int c = 0; c < kClasses; ++c) sched[c] = local_schedule(maxTri[c], count[c], numSMs, maxCluster);
     int start[kClasses + 1] = {};
     for (int c = 0; c < kClasses; ++c) start[c + 1] = start[c] + count[c];
     std::vector<int> order(which.size());   // position in the class-sorted batch -> index into which
@@ -345,7 +360,7 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& w
             cb.prob = static_cast<const LocalProblem*>(bufs[0]) + start[c];
             cb.out = static_cast<LocalResult*>(bufs[6]) + start[c];
             cb.nProb = count[c];
-            if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, tppOf[c], aux[c]);
+            if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, sched[c], aux[c]);
             if (e == cudaSuccess) e = cudaEventRecord(ev[c], aux[c]);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(in.st, ev[c], 0);
         }

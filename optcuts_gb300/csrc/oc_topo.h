@@ -39,6 +39,7 @@ struct TopoQueryIn {
     const double* divGrad = nullptr; // nV (split filter)
     const DeviceMesh* dm = nullptr;  // device copy of the same mesh (rest constants, UV)
     const TopoAdjacency* adj = nullptr;   // adjacency of F (built here when null)
+    int bigCluster = 0;              // largest cluster of blocks per local problem (0: the device's, 16 or 8)
     cudaStream_t st = nullptr;
 };
 

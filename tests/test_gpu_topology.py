@@ -160,3 +160,12 @@ def test_problem_size_classes_match_oracle(nlon, nlat):
                 np.testing.assert_allclose(c["newVertPos"], r["newVertPos"], rtol=1e-6, atol=1e-9)
         sizes.update(int(n) for n in q["problems"]["nTri"])
     assert max(sizes) >= nlon and min(sizes) <= 8
+    # a learned query solves few problems exactly, so its large fans run on
+    # clusters of blocks: the same decreases as the exhaustive pass
+    mlp = oc.MLP(32, 128, seed=3)
+    for op in (oc.OP_BOUNDARY_SPLIT, oc.OP_INTERIOR_SPLIT):
+        ex = mesh.querySplit(0.999, splitInterior=op == oc.OP_INTERIOR_SPLIT)
+        le = mesh.querySplit(0.999, splitInterior=op == oc.OP_INTERIOR_SPLIT, mlp=mlp, topFrac=0.05)
+        sel = np.isfinite(le["problems"]["EwDec"])
+        assert sel.sum() == le["selected"]
+        np.testing.assert_allclose(le["problems"]["EwDec"][sel], ex["problems"]["EwDec"][sel], rtol=1e-8, atol=1e-12)
