@@ -314,6 +314,16 @@ int oc_mlp_predict(oc_mlp* mlp, const float* X, int n, float* y);
 int oc_mlp_gradient(oc_mlp* mlp, const float* X, const float* target, int n, float* grad, float* loss);
 int oc_mlp_train(oc_mlp* mlp, const float* X, const float* target, int n, int epochs, int batch, float lr,
                  unsigned seed, float* finalLoss);
+/* the hidden-layer products (K and N >= 16) on the 5th-generation tensor
+ * cores (tcgen05.mma, FP32 accumulator in tensor memory; on = 1, the
+ * default) or on the CUDA cores (on = 0); OC_ERR_TIMEOUT if a tensor-core
+ * wait ran out */
+int oc_mlp_set_tensor_cores(oc_mlp* mlp, int on);
+/* the network's product on host arrays: C (M x N, row-major) =
+ * sum_k A[m*sam + k*sak] B[k*sbk + n*sbn], BF16 operands, FP32 accumulation,
+ * on the tensor cores (tensorCores 1) or the CUDA cores (0) */
+int oc_bf16_gemm(oc_ctx* ctx, int M, int N, int K, const float* A, long long sam, long long sak, const float* B,
+                 long long sbk, long long sbn, float* C, int tensorCores);
 /* candidate count, index of the largest E_w decrease (-1: none), size of
  * the filtered pool (inSplitTotalAmt for interior splits), local problems
  * solved, their largest iteration count, host build and device solve ms */

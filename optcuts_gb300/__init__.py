@@ -130,6 +130,10 @@ _SIGS = {
     "oc_mlp_predict": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.POINTER(ctypes.c_float)],
     "oc_mlp_gradient": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int,
                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)],
+    "oc_mlp_set_tensor_cores": [_vp, ctypes.c_int],
+    "oc_bf16_gemm": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_longlong,
+                     ctypes.c_longlong, ctypes.POINTER(ctypes.c_float), ctypes.c_longlong, ctypes.c_longlong,
+                     ctypes.POINTER(ctypes.c_float), ctypes.c_int],
     "oc_mlp_train": [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int,
                      ctypes.c_int, ctypes.c_float, ctypes.c_uint, ctypes.POINTER(ctypes.c_float)],
     "oc_topology_split_candidates": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_double, _i, _i, _i],
@@ -557,6 +561,25 @@ def default_config(**kw):
     return c
 
 
+def bf16_gemm(A, B, tensor_cores=True, a_transposed=False, b_transposed=False, ctx=None):
+    """C = op(A) @ op(B) with BF16 operands and FP32 accumulation on the
+    device (the MLP's product), on the tensor cores or the CUDA cores.
+    a_transposed: A holds op(A) transposed (K x M, row-major), read through
+    strides (1, M) as the network's backward products read theirs; likewise
+    b_transposed (B is N x K)."""
+    ctx = ctx or default_context()
+    A = _f4(A)
+    B = _f4(B)
+    M, K = (A.shape[1], A.shape[0]) if a_transposed else A.shape
+    N = B.shape[0] if b_transposed else B.shape[1]
+    sam, sak = (1, M) if a_transposed else (K, 1)
+    sbk, sbn = (1, K) if b_transposed else (N, 1)
+    C = np.zeros((M, N), np.float32)
+    ctx.check(lib().oc_bf16_gemm(ctx.h, M, N, K, _pf(A), sam, sak, _pf(B), sbk, sbn, _pf(C),
+                                 1 if tensor_cores else 0), "bf16_gemm")
+    return C
+
+
 class MLP:
     """The learned proposal's network: nIn -> nHidden -> nHidden -> 1 (ReLU),
     BF16 weights and activations, FP32 accumulation, trained on the GPU."""
@@ -602,6 +625,10 @@ class MLP:
         self.ctx.check(lib().oc_mlp_train(self.h, _pf(X), _pf(t), len(X), epochs, batch, lr, seed,
                                           ctypes.byref(loss)), "MLP train")
         return loss.value
+
+    def set_tensor_cores(self, on=True):
+        """Hidden-layer products on the tensor cores (tcgen05) or the CUDA cores."""
+        self.ctx.check(lib().oc_mlp_set_tensor_cores(self.h, 1 if on else 0), "MLP set_tensor_cores")
 
     def close(self):
         if getattr(self, "h", None):

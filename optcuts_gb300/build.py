@@ -33,8 +33,9 @@ UNITS = {
     "oc_airmesh.cpp": [],
     "oc_topo.cpp": [],
     "oc_mlp.cu": [],
+    "oc_tc.cu": [],
 }
-HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h"]
+HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h"]
 
 
 def _newest_input():

@@ -3,13 +3,14 @@
 // products, trained on the device by the project's own forward / backward
 // kernels and Adam on FP32 master weights.
 //
-// The products are small (at most a few 10^4 rows x 128 x 128 per step), so
-// a tiled CUDA-core kernel with BF16 operands in shared memory and FP32
-// accumulators carries them; every product has the form
-//   C[M x N] (+)= op(A)[M x K] * op(B)[K x N]
-// with A, B given with explicit strides (no transposed copies needed).
+// Every product has the form C[M x N] (+)= op(A)[M x K] * op(B)[K x N] with
+// A, B given with explicit strides (no transposed copies).  Those with K and
+// N of at least 16 (both hidden layers, forward and backward) run on the
+// tensor cores (oc_tc.cu, tcgen05.mma); the one-column products of the
+// output layer on the CUDA cores.
 
 #include "oc_mlp.h"
+#include "oc_tc.h"
 
 #include <cuda_bf16.h>
 
@@ -22,61 +23,6 @@
 
 namespace oc {
 namespace {
-
-constexpr int kTileM = 64, kTileN = 64, kTileK = 16;
-
-// C[m, n] = alpha * sum_k A(m, k) B(k, n) + beta * C[m, n] (+ bias[n]),
-// A(m, k) = A[m * sam + k * sak], B(k, n) = B[k * sbk + n * sbn]; operands
-// rounded to BF16 on the way into shared memory, FP32 accumulation.
-__global__ void __launch_bounds__(256) k_gemm_bf16(int M, int N, int K, const float* __restrict__ A, long long sam,
-                                                   long long sak, const float* __restrict__ B, long long sbk,
-                                                   long long sbn, float* __restrict__ C, long long ldc, float alpha,
-                                                   float beta, const float* __restrict__ bias)
-{
-    __shared__ __nv_bfloat16 As[kTileK][kTileM + 2];
-    __shared__ __nv_bfloat16 Bs[kTileK][kTileN + 2];
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 4 x 4 outputs each
-    const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += kTileK) {
-        for (int e = threadIdx.x; e < kTileK * kTileM; e += 256) {
-            const int kk = e / kTileM, mm = e % kTileM;
-            const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = __float2bfloat16(m < M && k < K ? A[m * sam + k * sak] : 0.0f);
-        }
-        for (int e = threadIdx.x; e < kTileK * kTileN; e += 256) {
-            const int kk = e / kTileN, nn = e % kTileN;
-            const int n = n0 + nn, k = k0 + kk;
-            Bs[kk][nn] = __float2bfloat16(n < N && k < K ? B[k * sbk + n * sbn] : 0.0f);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kTileK; ++kk) {
-            float a[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = __bfloat162float(As[kk][ty * 4 + i]);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = __bfloat162float(Bs[kk][tx * 4 + j]);
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int m = m0 + ty * 4 + i, n = n0 + tx * 4 + j;
-            if (m < M && n < N) {
-                float v = alpha * acc[i][j];
-                if (beta != 0.0f) v += beta * C[m * ldc + n];
-                if (bias) v += bias[n];
-                C[m * ldc + n] = v;
-            }
-        }
-}
 
 __global__ void k_relu(float* __restrict__ x, long long n)
 {
@@ -136,17 +82,22 @@ __global__ void k_round_bf16(const float* __restrict__ w, float* __restrict__ ou
     if (i < n) out[i] = __bfloat162float(__float2bfloat16(w[i]));
 }
 
-void gemm(cudaStream_t st, int M, int N, int K, const float* A, long long sam, long long sak, const float* B,
-          long long sbk, long long sbn, float* C, long long ldc, float alpha, float beta, const float* bias)
-{
-    if (M <= 0 || N <= 0) return;
-    dim3 grid((N + kTileN - 1) / kTileN, (M + kTileM - 1) / kTileM);
-    k_gemm_bf16<<<grid, 256, 0, st>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, alpha, beta, bias);
-}
-
 int blocks(long long n, int t = 256) { return static_cast<int>((n + t - 1) / t); }
 
 } // namespace
+
+void Mlp::gemm(int M, int N, int K, const float* A, long long sam, long long sak, const float* B, long long sbk,
+               long long sbn, float* C, long long ldc, float alpha, float beta, const float* bias)
+{
+    if (tensorCores && K >= 16 && N >= 16) {
+        const cudaError_t e = gemm_tc(st, M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, alpha, beta, bias, errFlag);
+        if (e != cudaSuccess) launchError = e;
+    }
+    else {
+        gemm_cuda_cores(st, M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, alpha, beta, bias);
+    }
+}
+
 
 void k_round_bf16_launch(const float* w, float* out, int n, cudaStream_t st)
 {
@@ -177,6 +128,8 @@ int Mlp::init(int nIn, int nHidden, unsigned seed, cudaStream_t s, std::string* 
         if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, sizeof(float) * P, st);
     }
     if (e == cudaSuccess) e = cudaMalloc(&sse, sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&errFlag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(errFlag, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(master, w.data(), sizeof(float) * P, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) k_round_bf16<<<blocks(P), 256, 0, st>>>(master, wbf, P);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -193,7 +146,25 @@ void Mlp::release()
     for (float* p : {master, wbf, m1, v1, grad, sse, bufX, bufT, bufH1, bufH2, bufY, bufD1, bufD2, bufDy}) cudaFree(p);
     master = wbf = m1 = v1 = grad = sse = nullptr;
     bufX = bufT = bufH1 = bufH2 = bufY = bufD1 = bufD2 = bufDy = nullptr;
+    cudaFree(errFlag);
+    errFlag = nullptr;
     capRows = 0;
+}
+
+int Mlp::check()
+{
+    int flag = 0;
+    if (cudaMemcpyAsync(&flag, errFlag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return OC_ERR_CUDA;
+    const cudaError_t le = launchError;
+    launchError = cudaSuccess;
+    if (le != cudaSuccess) return OC_ERR_CUDA;
+    if (flag) {
+        cudaMemsetAsync(errFlag, 0, sizeof(int), st);
+        return OC_ERR_TIMEOUT;
+    }
+    return OC_OK;
 }
 
 int Mlp::ensure_rows(int n)
@@ -225,11 +196,11 @@ void Mlp::forward(int n)
     const float* W3 = b2 + hidden;
     const float* b3 = W3 + hidden;
     // H1 = X W1^T + b1: A = X (n x in), B(k, j) = W1[j * in + k]
-    gemm(st, n, hidden, in, bufX, in, 1, W1, 1, in, bufH1, hidden, 1.0f, 0.0f, b1);
+    gemm(n, hidden, in, bufX, in, 1, W1, 1, in, bufH1, hidden, 1.0f, 0.0f, b1);
     k_relu<<<blocks((long long)n * hidden), 256, 0, st>>>(bufH1, (long long)n * hidden);
-    gemm(st, n, hidden, hidden, bufH1, hidden, 1, W2, 1, hidden, bufH2, hidden, 1.0f, 0.0f, b2);
+    gemm(n, hidden, hidden, bufH1, hidden, 1, W2, 1, hidden, bufH2, hidden, 1.0f, 0.0f, b2);
     k_relu<<<blocks((long long)n * hidden), 256, 0, st>>>(bufH2, (long long)n * hidden);
-    gemm(st, n, 1, hidden, bufH2, hidden, 1, W3, 1, hidden, bufY, 1, 1.0f, 0.0f, b3);
+    gemm(n, 1, hidden, bufH2, hidden, 1, W3, 1, hidden, bufY, 1, 1.0f, 0.0f, b3);
 }
 
 // gradient of the mean squared error over n rows (bufX, bufT) into grad
@@ -246,17 +217,17 @@ void Mlp::backward(int n)
     cudaMemsetAsync(sse, 0, sizeof(float), st);
     k_mse_grad<<<blocks(n), 256, 0, st>>>(bufY, bufT, n, bufDy, sse);
     // layer 3: gW3[j] = sum_m dy[m] H2[m, j]; gb3 = sum dy; dH2 = dy W3 (x) relu'
-    gemm(st, 1, hidden, n, bufDy, 0, 1, bufH2, hidden, 1, gW3, hidden, 1.0f, 0.0f, nullptr);
+    gemm(1, hidden, n, bufDy, 0, 1, bufH2, hidden, 1, gW3, hidden, 1.0f, 0.0f, nullptr);
     k_colsum<<<1, 32, 0, st>>>(bufDy, n, 1, 1, gb3);
-    gemm(st, n, hidden, 1, bufDy, 1, 1, W3, 0, 1, bufD2, hidden, 1.0f, 0.0f, nullptr);
+    gemm(n, hidden, 1, bufDy, 1, 1, W3, 0, 1, bufD2, hidden, 1.0f, 0.0f, nullptr);
     k_relu_back<<<blocks((long long)n * hidden), 256, 0, st>>>(bufD2, bufH2, (long long)n * hidden);
     // layer 2: gW2[j, k] = sum_m dH2[m, j] H1[m, k]; dH1 = dH2 W2 (x) relu'
-    gemm(st, hidden, hidden, n, bufD2, 1, hidden, bufH1, hidden, 1, gW2, hidden, 1.0f, 0.0f, nullptr);
+    gemm(hidden, hidden, n, bufD2, 1, hidden, bufH1, hidden, 1, gW2, hidden, 1.0f, 0.0f, nullptr);
     k_colsum<<<blocks(hidden, 128), 128, 0, st>>>(bufD2, n, hidden, hidden, gb2);
-    gemm(st, n, hidden, hidden, bufD2, hidden, 1, W2, hidden, 1, bufD1, hidden, 1.0f, 0.0f, nullptr);
+    gemm(n, hidden, hidden, bufD2, hidden, 1, W2, hidden, 1, bufD1, hidden, 1.0f, 0.0f, nullptr);
     k_relu_back<<<blocks((long long)n * hidden), 256, 0, st>>>(bufD1, bufH1, (long long)n * hidden);
     // layer 1: gW1[j, k] = sum_m dH1[m, j] X[m, k]
-    gemm(st, hidden, in, n, bufD1, 1, hidden, bufX, in, 1, gW1, in, 1.0f, 0.0f, nullptr);
+    gemm(hidden, in, n, bufD1, 1, hidden, bufX, in, 1, gW1, in, 1.0f, 0.0f, nullptr);
     k_colsum<<<blocks(hidden, 128), 128, 0, st>>>(bufD1, n, hidden, hidden, gb1);
 }
 
@@ -299,7 +270,8 @@ int mlp_predict_host(Mlp& m, const float* X, int n, float* y)
         if (cudaMemcpyAsync(y + r0, m.bufY, sizeof(float) * r, cudaMemcpyDeviceToHost, m.st) != cudaSuccess)
             return OC_ERR_CUDA;
     }
-    return cudaStreamSynchronize(m.st) == cudaSuccess && cudaGetLastError() == cudaSuccess ? OC_OK : OC_ERR_CUDA;
+    if (cudaStreamSynchronize(m.st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return OC_ERR_CUDA;
+    return m.check();
 }
 
 } // namespace oc
@@ -382,6 +354,7 @@ OC_EXPORT int oc_mlp_gradient(oc_mlp* p, const float* X, const float* t, int n, 
     cudaMemcpyAsync(grad, m.grad, sizeof(float) * m.nParams(), cudaMemcpyDeviceToHost, m.st);
     cudaMemcpyAsync(&sse, m.sse, sizeof(float), cudaMemcpyDeviceToHost, m.st);
     if (cudaStreamSynchronize(m.st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return OC_ERR_CUDA;
+    if (const int rc = m.check()) return rc;
     if (loss) *loss = sse / n;
     return OC_OK;
 }
@@ -427,10 +400,55 @@ OC_EXPORT int oc_mlp_train(oc_mlp* p, const float* X, const float* t, int n, int
             }
         }
         // the host shuffle of the next epoch reuses dIdx: wait for this one
-        cudaStreamSynchronize(m.st);
+        if (const int rc = m.check()) {
+            cudaFree(dX); cudaFree(dT); cudaFree(dIdx);
+            return rc;
+        }
     }
     const bool ok = cudaStreamSynchronize(m.st) == cudaSuccess && cudaGetLastError() == cudaSuccess;
     cudaFree(dX); cudaFree(dT); cudaFree(dIdx);
     if (finalLoss) *finalLoss = lastRows ? static_cast<float>(lastSse / lastRows) : 0.0f;
     return ok ? OC_OK : OC_ERR_CUDA;
+}
+
+// products of the network on the tensor cores (1, the default) or on the
+// CUDA cores (0)
+OC_EXPORT int oc_mlp_set_tensor_cores(oc_mlp* p, int on)
+{
+    if (!p) return OC_ERR_INVALID;
+    p->m.tensorCores = on != 0;
+    return OC_OK;
+}
+
+// C (M x N, row-major, host) = A(m, k) B(k, n) with host operands and
+// strides in elements, BF16 operands and FP32 accumulation, on the tensor
+// cores (tensorCores 1) or the CUDA cores (0)
+OC_EXPORT int oc_bf16_gemm(oc_ctx* ctx, int M, int N, int K, const float* A, long long sam, long long sak,
+                           const float* B, long long sbk, long long sbn, float* C, int tensorCores)
+{
+    if (!ctx || !A || !B || !C || M <= 0 || N <= 0 || K <= 0 || sam < 0 || sak < 0 || sbk < 0 || sbn < 0)
+        return OC_ERR_INVALID;
+    const long long aSpan = (M - 1) * sam + (K - 1) * sak + 1, bSpan = (K - 1) * sbk + (N - 1) * sbn + 1;
+    cudaStream_t st = oc::ctx_stream(ctx);
+    float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    int* dErr = nullptr;
+    cudaError_t e = cudaMalloc(&dA, sizeof(float) * aSpan);
+    if (e == cudaSuccess) e = cudaMalloc(&dB, sizeof(float) * bSpan);
+    if (e == cudaSuccess) e = cudaMalloc(&dC, sizeof(float) * (size_t)M * N);
+    if (e == cudaSuccess) e = cudaMalloc(&dErr, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(dErr, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dA, A, sizeof(float) * aSpan, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dB, B, sizeof(float) * bSpan, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        if (tensorCores) e = oc::gemm_tc(st, M, N, K, dA, sam, sak, dB, sbk, sbn, dC, N, 1.0f, 0.0f, nullptr, dErr);
+        else oc::gemm_cuda_cores(st, M, N, K, dA, sam, sak, dB, sbk, sbn, dC, N, 1.0f, 0.0f, nullptr);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(C, dC, sizeof(float) * (size_t)M * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, dErr, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dA); cudaFree(dB); cudaFree(dC); cudaFree(dErr);
+    if (e != cudaSuccess) return OC_ERR_CUDA;
+    return flag ? OC_ERR_TIMEOUT : OC_OK;
 }

@@ -18,6 +18,13 @@ struct Mlp {
     float *bufX = nullptr, *bufT = nullptr, *bufH1 = nullptr, *bufH2 = nullptr, *bufY = nullptr;
     float *bufD1 = nullptr, *bufD2 = nullptr, *bufDy = nullptr;
 
+    // products on the tensor cores (else the CUDA-core kernel); a device
+    // flag the tensor-core kernel sets when a wait runs out; the last launch
+    // error of a product
+    bool tensorCores = true;
+    int* errFlag = nullptr;
+    cudaError_t launchError = cudaSuccess;
+
     int nParams() const;
     int init(int nIn, int nHidden, unsigned seed, cudaStream_t s, std::string* err);
     void release();
@@ -25,6 +32,10 @@ struct Mlp {
     void forward(int n);    // rows in bufX -> bufY
     void backward(int n);   // targets in bufT -> grad, sum of squared errors in *sse
     void adam(float lr);
+    void gemm(int M, int N, int K, const float* A, long long sam, long long sak, const float* B, long long sbk,
+              long long sbn, float* C, long long ldc, float alpha, float beta, const float* bias);
+    // after a synchronize: OC_OK, or OC_ERR_TIMEOUT / OC_ERR_CUDA (flags cleared)
+    int check();
 };
 
 void k_round_bf16_launch(const float* w, float* out, int n, cudaStream_t st);

@@ -78,3 +78,46 @@ def test_invalid_arguments():
     m = oc.MLP(32, 128)
     with pytest.raises(oc.OCError):
         m.train(np.zeros((0, 32), np.float32), np.zeros(0, np.float32))
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb", [
+    (128, 128, 64, False, False),   # one tile, one stage
+    (1000, 128, 32, False, True),   # X W1^T: the first layer (K = 32, half a stage)
+    (300, 128, 128, False, True),   # H1 W2^T: ragged rows, two stages
+    (128, 128, 777, True, False),   # dH2^T H1: reduction over rows, ragged K
+    (128, 32, 513, True, False),    # dH1^T X: N = 32
+    (77, 200, 48, False, False),    # two tiles along N, ragged everything
+])
+def test_tensor_core_gemm_matches_cuda_cores(M, N, K, ta, tb):
+    """tcgen05.mma (BF16 from shared memory, FP32 in tensor memory) against
+    the CUDA-core kernel with the same BF16 operands, and both against the
+    BF16-rounded float64 product."""
+    rng = np.random.default_rng(M + N + K)
+    A = rng.normal(size=(K, M) if ta else (M, K)).astype(np.float32)
+    B = rng.normal(size=(N, K) if tb else (K, N)).astype(np.float32)
+    tc = oc.bf16_gemm(A, B, True, ta, tb)
+    cc = oc.bf16_gemm(A, B, False, ta, tb)
+    a64 = ref.bf16(A).astype(np.float64)
+    b64 = ref.bf16(B).astype(np.float64)
+    exact = (a64.T if ta else a64) @ (b64.T if tb else b64)
+    scale = np.sqrt(K) * 4.0
+    assert np.abs(tc - exact).max() <= 1e-5 * scale
+    assert np.abs(cc - exact).max() <= 1e-5 * scale
+    np.testing.assert_allclose(tc, cc, rtol=0, atol=2e-5 * scale)
+
+
+def test_network_on_tensor_cores_matches_cuda_cores():
+    """The two product kernels accumulate in a different order, so a hidden
+    activation can round to the neighbouring BF16 value (2^-8 relative) on
+    one of them: agreement to that scale."""
+    X, t = data(700, seed=21)
+    a = oc.MLP(32, 128, seed=22)
+    b = oc.MLP(32, 128, seed=22)
+    b.set_tensor_cores(False)
+    ya, yb = a.predict(X), b.predict(X)
+    assert np.abs(ya - yb).max() <= 4e-3 * np.abs(yb).max()
+    assert np.median(np.abs(ya - yb)) <= 1e-5 * np.abs(yb).max()
+    ga, la = a.gradient(X, t)
+    gb, lb = b.gradient(X, t)
+    assert la == pytest.approx(lb, rel=1e-3)
+    assert np.linalg.norm(ga - gb) <= 2e-3 * np.linalg.norm(gb)
