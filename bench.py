@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--train-at", default="60,120,200,300",
                    help="Newton iterations whose states give the learned proposal's exhaustive training pairs")
     p.add_argument("--top-frac", type=float, default=0.1, help="fraction of local problems solved exactly (learned)")
+    p.add_argument("--train-epochs", type=int, default=30, help="MLP training epochs over the exhaustive pairs")
     return p.parse_args()
 
 
@@ -344,7 +345,7 @@ def run_ours(args, rank, world):
             mlp = oc.MLP(32, 128, seed=3, ctx=ctx)
             ctx.synchronize()
             t0 = time.perf_counter()
-            loss = mlp.train(X, t, epochs=30, batch=512, lr=2e-3, seed=3)
+            loss = mlp.train(X, t, epochs=args.train_epochs, batch=512, lr=2e-3, seed=3)
             ctx.synchronize()
             train_s = time.perf_counter() - t0
             queries(mlp=mlp, topFrac=args.top_frac)   # warm-up
@@ -370,7 +371,8 @@ def run_ours(args, rank, world):
                                         "E_w_after": ew_l32, "E_w_after_exhaustive": ew_ex32,
                                         "E_w_rel_diff": abs(ew_l32 - ew_ex32) / abs(ew_ex32)},
                 "mlp": {"layers": [32, 128, 128, 1], "weights": "bf16 (fp32 master, Adam)", "accumulate": "fp32",
-                        "pairs": int(len(X)), "pair_states_newton_iteration": pair_states, "epochs": 30,
+                        "pairs": int(len(X)), "pair_states_newton_iteration": pair_states,
+                        "epochs": args.train_epochs,
                         "batch": 512, "seed": 3, "train_s": train_s, "final_mse": loss,
                         "target_var": float(np.var(t))}}
         if rank == 0 and not args.no_cpu_baseline:
