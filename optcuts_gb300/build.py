@@ -4,7 +4,7 @@
 
 Translation units are compiled in parallel; oc_fp64.cu is compiled with
 -fmad=false so its FP64 arithmetic rounds exactly as the reference's scalar
-host code does.
+host code does (oc_local.cu, the local topology solves, contracts FMAs).
 """
 from __future__ import annotations
 
@@ -34,8 +34,9 @@ UNITS = {
     "oc_topo.cpp": [],
     "oc_mlp.cu": [],
     "oc_tc.cu": [],
+    "oc_local.cu": [],
 }
-HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h"]
+HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h", "oc_elem.cuh"]
 
 
 def _newest_input():

@@ -1,0 +1,345 @@
+// Per-triangle symmetric Dirichlet kernels shared by the global Newton step
+// (oc_fp64.cu, compiled with -fmad=false so its FP64 rounding follows the
+// reference's scalar host code operation by operation) and the local
+// topology solves (oc_local.cu, compiled with FMA contraction): energy,
+// corner gradients, injective step bound, element Hessian with its PSD
+// projection.  Each translation unit gets its own copy with its own
+// floating-point contraction.
+#pragma once
+
+#include "oc_internal.h"
+
+namespace oc {
+namespace {
+
+// SymDirichletEnergy::getEnergyValPerElem body (SymDirichletEnergy.cpp:32-44).
+__device__ __forceinline__ double elem_energy(const DeviceMesh& m, int t, double w, const double2 U1,
+                                              const double2 U2, const double2 U3)
+{
+    const double a0 = U2.x - U1.x, a1 = U2.y - U1.y;   // U2m1
+    const double b0 = U3.x - U1.x, b1 = U3.y - U1.y;   // U3m1
+    const double area_U = 0.5 * (a0 * b1 - a1 * b0);
+    const double A2 = m.A2[t];
+    return w * (1.0 + A2 / area_U / area_U) *
+           (((b0 * b0 + b1 * b1) * m.e0[t] + (a0 * a0 + a1 * a1) * m.e1[t]) / 4 / A2 -
+            (b0 * a0 + b1 * a1) * m.e01[t] / 2 / A2);
+}
+
+
+// SymDirichletEnergy::computeGradient per-corner terms (SymDirichletEnergy.cpp:
+// 267-297; also computeLocalGradient, :215-256) of one triangle.
+__device__ __forceinline__ void tri_corner_grads(const double2 U1, const double2 U2, const double2 U3, double A2,
+                                                 double e0, double e1, double e01, double w, double2 g[3])
+{
+    const double a0 = U2.x - U1.x, a1 = U2.y - U1.y;   // U2m1
+    const double b0 = U3.x - U1.x, b1 = U3.y - U1.y;   // U3m1
+    const double area_U = 0.5 * (a0 * b1 - a1 * b0);
+    const double leftTerm = 1.0 + A2 / area_U / area_U;
+    const double rightTerm = ((b0 * b0 + b1 * b1) * e0 + (a0 * a0 + a1 * a1) * e1) / 4 / A2 -
+                             (b0 * a0 + b1 * a1) * e01 / 2 / A2;
+    const double areaRatio = A2 / area_U / area_U / area_U;
+    {
+        const double eo0 = U3.x - U2.x, eo1 = U3.y - U2.y;
+        const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
+        const double dR0 = ((e01 - e0) * b0 + (e01 - e1) * a0) / 2.0 / A2;
+        const double dR1 = ((e01 - e0) * b1 + (e01 - e1) * a1) / 2.0 / A2;
+        g[0] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+    }
+    {
+        const double eo0 = U1.x - U3.x, eo1 = U1.y - U3.y;
+        const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
+        const double dR0 = (e1 * a0 - e01 * b0) / 2.0 / A2;
+        const double dR1 = (e1 * a1 - e01 * b1) / 2.0 / A2;
+        g[1] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+    }
+    {
+        const double eo0 = U2.x - U1.x, eo1 = U2.y - U1.y;
+        const double dL0 = areaRatio * eo1, dL1 = areaRatio * -eo0;
+        const double dR0 = (e0 * b0 - e01 * a0) / 2.0 / A2;
+        const double dR1 = (e0 * b1 - e01 * a1) / 2.0 / A2;
+        g[2] = make_double2(w * (dL0 * rightTerm + dR0 * leftTerm), w * (dL1 * rightTerm + dR1 * leftTerm));
+    }
+}
+
+// SymDirichletEnergy::initStepSize per triangle (SymDirichletEnergy.cpp:
+// 555-609): the bound from det(U + alpha V) > 0, or stepSize when none.
+__device__ __forceinline__ double tri_step_bound(const double2 U1, const double2 U2, const double2 U3, const double2 V1,
+                                                 const double2 V2, const double2 V3, double stepSize)
+{
+    const double U2m1x = U2.x - U1.x, U2m1y = U2.y - U1.y;
+    const double U3m1x = U3.x - U1.x, U3m1y = U3.y - U1.y;
+    const double V2m1x = V2.x - V1.x, V2m1y = V2.y - V1.y;
+    const double V3m1x = V3.x - V1.x, V3m1y = V3.y - V1.y;
+    const double a = V2m1x * V3m1y - V2m1y * V3m1x;
+    const double b = U2m1x * V3m1y - U2m1y * V3m1x + V2m1x * U3m1y - V2m1y * U3m1x;
+    const double c = U2m1x * U3m1y - U2m1y * U3m1x;
+    const double delta = b * b - 4.0 * a * c;
+    double bound = stepSize;
+    if (a > 0.0) {
+        if ((b < 0.0) && (delta >= 0.0)) bound = 2.0 * c / (-b + sqrt(delta));
+    }
+    else if (a < 0.0) {
+        if (b < 0.0) bound = 2.0 * c / (-b + sqrt(delta));
+        else bound = (-b - sqrt(delta)) / 2.0 / a;
+    }
+    else {
+        if (b < 0.0) bound = -c / b;
+    }
+    return bound;
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 6x6: A is destroyed (its
+// diagonal holds the eigenvalues), V receives the eigenvectors as columns.
+__device__ void jacobi_eig6(double A[6][6], double V[6][6])
+{
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+    double fro = 0.0;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) fro += A[i][j] * A[i][j];
+    double prevOff = 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 6; ++p)
+            for (int q = p + 1; q < 6; ++q) off += A[p][q] * A[p][q];
+        // converged, or no longer decreasing (the off-diagonal mass has
+        // reached the rounding floor, below which 1e-34 is not reachable)
+        if (off <= 1e-34 * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
+        for (int p = 0; p < 6; ++p) {
+            for (int q = p + 1; q < 6; ++q) {
+                const double apq = A[p][q];
+                if (apq == 0.0) continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 6; ++k) {
+                    const double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - s * akq;
+                    A[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - s * aqk;
+                    A[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ double recip_sqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float recip_sqrt(float x) { return rsqrtf(x); }
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 4x4 (A destroyed: its
+// diagonal holds the eigenvalues; V the eigenvectors as columns); stops at
+// convergence or when the off-diagonal mass stops decreasing.
+template <typename T>
+__device__ void jacobi_eig4(T A[4][4], T V[4][4], T tol)
+{
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? T(1) : T(0);
+    T fro = T(0);
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) fro += A[i][j] * A[i][j];
+    T prevOff = T(0);
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        T off = T(0);
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) off += A[p][q] * A[p][q];
+        if (off <= tol * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) {
+                const T apq = A[p][q];
+                if (apq == T(0)) continue;
+                // the rotation of the classical formula t = sgn(theta) /
+                // (|theta| + sqrt(theta^2 + 1)), theta = delta / apq, written
+                // with one division and one square root (the entries are
+                // scaled to O(1) by the caller, so delta^2 + apq^2 cannot
+                // overflow), and c = 1 / sqrt(1 + t^2) as a reciprocal root
+                const T delta = (A[q][q] - A[p][p]) * T(0.5);
+                const T t = (delta >= T(0) ? apq : -apq) / (fabs(delta) + sqrt(delta * delta + apq * apq));
+                const T c = recip_sqrt(t * t + T(1)), sn = t * c;
+                for (int k = 0; k < 4; ++k) {
+                    const T akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - sn * akq;
+                    A[k][q] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    const T apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - sn * aqk;
+                    A[q][k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    const T vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+}
+
+// makePD of a triangle's 6x6 Hessian for the local topology solves, in the
+// 4-dimensional complement of the two rigid translations (H t = 0 for them,
+// so H = Q K Q^T with K = Q^T H Q): Q = B (x) I2, B the orthonormal 3x2 basis
+// [-1/sqrt2, -1/sqrt6; 1/sqrt2, -1/sqrt6; 0, 2/sqrt6] of the vectors
+// orthogonal to (1, 1, 1).  K PSD up to -1e-13 of its largest diagonal
+// leaves H unchanged (makePD's early return); otherwise K = V Lambda V^T,
+// negative eigenvalues clamped to zero and H = (Q V) Lambda+ (Q V)^T: the same
+// projection as the 6x6 eigen-clamp, at about a fifth of its arithmetic.
+// T = float projects in FP32 (scaled by the largest |K_ii|).
+template <typename T>
+__device__ void project_psd_reduced(double H[6][6])
+{
+    const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637;
+    const double B[3][2] = {{-r2, -r6}, {r2, -r6}, {0.0, 2.0 * r6}};
+    double Tm[4][6];   // Q^T H
+    for (int k = 0; k < 2; ++k)
+        for (int b = 0; b < 2; ++b)
+            for (int c = 0; c < 6; ++c) {
+                double acc = 0.0;
+                for (int i = 0; i < 3; ++i) acc = acc + B[i][k] * H[2 * i + b][c];
+                Tm[2 * k + b][c] = acc;
+            }
+    double K[4][4];
+    for (int r = 0; r < 4; ++r)
+        for (int l = 0; l < 2; ++l)
+            for (int d = 0; d < 2; ++d) {
+                double acc = 0.0;
+                for (int j = 0; j < 3; ++j) acc = acc + Tm[r][2 * j + d] * B[j][l];
+                K[r][2 * l + d] = acc;
+            }
+    for (int r = 0; r < 4; ++r)   // symmetric up to rounding: use the mean
+        for (int c = r + 1; c < 4; ++c) {
+            const double m = 0.5 * (K[r][c] + K[c][r]);
+            K[r][c] = m;
+            K[c][r] = m;
+        }
+    double dmax = 0.0;
+    for (int i = 0; i < 4; ++i) dmax = fmax(dmax, fabs(K[i][i]));
+    {   // LDL^T without pivoting: no pivot below -1e-13 dmax -> PSD
+        double A[4][4];
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) A[i][j] = K[i][j];
+        const double tol = 1e-13 * dmax;
+        bool psd = true;
+        for (int k = 0; k < 4 && psd; ++k) {
+            const double d = A[k][k];
+            if (d < -tol) psd = false;
+            else if (d > tol)
+                for (int i = k + 1; i < 4; ++i) {
+                    const double l = A[i][k] / d;
+                    for (int j = k + 1; j <= i; ++j) A[i][j] = A[i][j] - l * A[j][k];
+                }
+        }
+        if (psd) return;
+    }
+    const double scale = dmax > 0.0 ? dmax : 1.0;
+    T A[4][4], V[4][4];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) A[i][j] = static_cast<T>(K[i][j] / scale);
+    jacobi_eig4<T>(A, V, sizeof(T) == 8 ? T(1e-34) : T(1e-14));
+    double lam[4];
+    for (int m = 0; m < 4; ++m) lam[m] = A[m][m] < T(0) ? 0.0 : static_cast<double>(A[m][m]) * scale;
+    double W[6][4];   // Q V
+    for (int i = 0; i < 3; ++i)
+        for (int a = 0; a < 2; ++a)
+            for (int m = 0; m < 4; ++m)
+                W[2 * i + a][m] = B[i][0] * static_cast<double>(V[a][m]) + B[i][1] * static_cast<double>(V[2 + a][m]);
+    for (int r = 0; r < 6; ++r)
+        for (int c = r; c < 6; ++c) {
+            double acc = 0.0;
+            for (int m = 0; m < 4; ++m) acc = acc + W[r][m] * lam[m] * W[c][m];
+            H[r][c] = acc;
+            H[c][r] = acc;
+        }
+}
+
+// Per-triangle Hessian (SymDirichletEnergy.cpp:440-522) projected to PSD by
+// the 6x6 eigen-clamp of IglUtils::makePD (IglUtils.hpp:71-90): unchanged
+// when the smallest eigenvalue is >= 0, otherwise V max(Lambda, 0) V^T.
+// The full 6x6 decomposition matters: for stiff elements (entries up to
+// ~1e26 at a Tutte start) the rounding-level translation components it keeps
+// change the Newton direction, and reducing to the 4-dimensional
+// translation-free part first does not reproduce the reference.
+// Output: the upper triangle as 21 values per triangle (SoA).
+// localMode 0: exact (the global Newton); 1: the reduced 4x4 projection
+// (local solves, FP64); 2: as 1 with the eigen-decomposition in FP32
+__device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, double e1d, double e01d, double w,
+                            double H[6][6], int localMode = 0)
+{
+    const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
+    const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
+    const double area_U = 0.5 * (U2m1[0] * U3m1[1] - U2m1[1] * U3m1[0]);
+    const double areaRatio = triAreaSq / area_U / area_U / area_U;
+    const double dAR = 3.0 / 2.0 * areaRatio / area_U;
+    const double leftTerm = 1.0 + triAreaSq / area_U / area_U;
+    const double rightTerm = ((U3m1[0] * U3m1[0] + U3m1[1] * U3m1[1]) * e0d +
+                              (U2m1[0] * U2m1[0] + U2m1[1] * U2m1[1]) * e1d) / 2. -
+                             (U3m1[0] * U2m1[0] + U3m1[1] * U2m1[1]) * e01d;
+    double ort[3][2];
+    ort[0][0] = U[2].y - U[1].y; ort[0][1] = -(U[2].x - U[1].x);
+    ort[1][0] = U[0].y - U[2].y; ort[1][1] = -(U[0].x - U[2].x);
+    ort[2][0] = U[1].y - U[0].y; ort[2][1] = -(U[1].x - U[0].x);
+    double dL[3][2], dR[3][2];
+    for (int k = 0; k < 3; ++k) { dL[k][0] = areaRatio * ort[k][0]; dL[k][1] = areaRatio * ort[k][1]; }
+    for (int c = 0; c < 2; ++c) {
+        dR[0][c] = (e01d - e0d) * U3m1[c] + (e01d - e1d) * U2m1[c];
+        dR[1][c] = e1d * U2m1[c] - e01d * U3m1[c];
+        dR[2][c] = e0d * U3m1[c] - e01d * U2m1[c];
+    }
+    const double d2R[3][3] = {{e0d + e1d - 2.0 * e01d, e01d - e1d, e01d - e0d},
+                              {e01d - e1d, e1d, -e01d},
+                              {e01d - e0d, -e01d, e0d}};
+    const double skew[3][3] = {{0, 1, -1}, {-1, 0, 1}, {1, -1, 0}};
+    for (int i = 0; i < 3; ++i) {
+        for (int j = i; j < 3; ++j) {
+            for (int a = 0; a < 2; ++a) {
+                for (int b = 0; b < 2; ++b) {
+                    double d2L = dAR * ort[i][a] * ort[j][b];
+                    if (i != j) d2L += areaRatio * skew[i][j] * ((a == 0 && b == 1) ? -1.0 : ((a == 1 && b == 0) ? 1.0 : 0.0));
+                    const double v = w * (d2L * rightTerm + dL[i][a] * dR[j][b] +
+                                          (a == b ? d2R[i][j] * leftTerm : 0.0) + dR[i][a] * dL[j][b]);
+                    H[2 * i + a][2 * j + b] = v;
+                    H[2 * j + b][2 * i + a] = v;
+                }
+            }
+        }
+    }
+    if (localMode == 1) {
+        project_psd_reduced<double>(H);
+        return;
+    }
+    if (localMode == 2) {
+        project_psd_reduced<float>(H);
+        return;
+    }
+    double A[6][6], V[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
+    jacobi_eig6(A, V);
+    double lam[6], lmin = A[0][0];
+    for (int i = 0; i < 6; ++i) {
+        lam[i] = A[i][i];
+        if (lam[i] < lmin) lmin = lam[i];
+    }
+    if (lmin < 0.0) {
+        for (int i = 0; i < 6; ++i)
+            if (lam[i] < 0.0) lam[i] = 0.0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += V[i][k] * lam[k] * V[j][k];
+                H[i][j] = s;
+            }
+    }
+}
+
+} // namespace
+} // namespace oc
