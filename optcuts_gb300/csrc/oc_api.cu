@@ -42,6 +42,7 @@ struct oc_mesh {
     double* hb = nullptr;           // 21 x nF packed Hessians
     double* tmpF = nullptr;         // nF x 36 scratch for API outputs (lazy)
     std::shared_ptr<oc::TopoAdjacency> adj;   // adjacency of F for topology queries (lazy)
+    std::shared_ptr<oc::TopoWorkspace> topoWs;   // device buffers of the batched local solves (lazy)
 };
 
 struct oc_linsys {
@@ -847,6 +848,8 @@ static int topology_query(oc_mesh* m, int opType, double lambda_t, double filter
         return (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
     }();
     in.bigCluster = bigCluster;
+    if (!m->topoWs) m->topoWs = std::make_shared<oc::TopoWorkspace>();
+    in.ws = m->topoWs.get();
     oc_topo_result* r = new (std::nothrow) oc_topo_result;
     if (!r) return OC_ERR_NOMEM;
     std::string err;

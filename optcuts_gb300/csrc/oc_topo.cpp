@@ -17,7 +17,11 @@
 #include <cfloat>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 #include <utility>
+#include <memory>
+#include <thread>
 
 namespace oc {
 namespace {
@@ -150,6 +154,18 @@ struct TopoAdjacency {
     Topo T;
 };
 
+TopoWorkspace::~TopoWorkspace()
+{
+    for (auto s : aux)
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    for (auto x : ev)
+        if (x) cudaEventDestroy(x);
+    for (auto* p : buf) cudaFree(p);
+}
+
 std::shared_ptr<TopoAdjacency> topo_adjacency(int nV, const int* F, int nF)
 {
     auto a = std::make_shared<TopoAdjacency>();
@@ -256,10 +272,44 @@ void emit(Batch& B, const Topo& T, const double* rest, const double* UV, const s
 // (TriMesh.cpp:561-629)
 std::vector<int> filter_candidates(const std::vector<std::pair<double, int>>& keyed, double exponent, int& poolSize)
 {
-    std::vector<std::pair<double, int>> s(keyed);
-    std::stable_sort(s.begin(), s.end(), [](const std::pair<double, int>& x, const std::pair<double, int>& y) {
-        return x.first < y.first;
-    });
+    // stable sort by key: contiguous chunks stable-sorted on host threads,
+    // then merged pairwise (std::merge takes equal keys from the earlier
+    // chunk first), which is the stable sort of the whole list
+    auto byKey = [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first < y.first; };
+    const size_t n = keyed.size();
+    std::vector<std::pair<double, int>> s(keyed), tmp(n);
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::max<size_t>(1, std::min<size_t>({hw, 16, n / 4096}));
+    std::vector<size_t> cut(nt + 1);
+    for (size_t t = 0; t <= nt; ++t) cut[t] = n * t / nt;
+    {
+        std::vector<std::thread> th;
+        for (size_t t = 1; t < nt; ++t)
+            th.emplace_back([&, t] { std::stable_sort(s.begin() + cut[t], s.begin() + cut[t + 1], byKey); });
+        std::stable_sort(s.begin() + cut[0], s.begin() + cut[1], byKey);
+        for (auto& x : th) x.join();
+    }
+    while (cut.size() > 2) {
+        std::vector<size_t> next;
+        std::vector<std::thread> th;
+        for (size_t k = 0; k + 1 < cut.size(); k += 2) {
+            next.push_back(cut[k]);
+            if (k + 2 < cut.size()) {
+                const size_t a0 = cut[k], a1 = cut[k + 1], a2 = cut[k + 2];
+                th.emplace_back([&, a0, a1, a2] {
+                    std::merge(s.begin() + a0, s.begin() + a1, s.begin() + a1, s.begin() + a2, tmp.begin() + a0, byKey);
+                });
+            }
+            else {
+                const size_t a0 = cut[k], a1 = cut[k + 1];
+                std::copy(s.begin() + a0, s.begin() + a1, tmp.begin() + a0);
+            }
+        }
+        for (auto& x : th) x.join();
+        next.push_back(n);
+        s.swap(tmp);
+        cut.swap(next);
+    }
     std::vector<std::pair<double, int>> uniq;
     for (const auto& kv : s) {
         if (!uniq.empty() && uniq.back().first == kv.first) uniq.back().second = kv.second;
@@ -293,14 +343,17 @@ bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector
 namespace {
 
 // Solves the problems `which` of B into res[k], grouped by size class
-// (threads per problem and cluster size from local_schedule_for), the
-// classes launched on their own streams so that the few large fans overlap
-// the many small problems;
-// maxIterOverride > 0 caps the Newton iterations.
-int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& which, int maxIterOverride, int fp32,
-                std::vector<LocalResult>& res, std::string* err)
+// (threads per problem and cluster size from local_schedule), the classes
+// launched on their own streams so that the few large fans overlap the many
+// small problems; maxIterOverride > 0 caps the Newton iterations.  batchId
+// names B: a second call for the same batch (the learned proposal's exact
+// pass after its probe) reuses the problem arrays already on the device.
+int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchId, const std::vector<int>& which,
+                int maxIterOverride, int fp32, std::vector<LocalResult>& res, std::string* err)
 {
     if (which.empty()) return OC_OK;
+    TopoWorkspace tmp;
+    TopoWorkspace& W = in.ws ? *in.ws : tmp;
     // size classes, largest first so that the long poles start first, each
     // with the schedule its size and count call for
     constexpr int kClasses = 4;
@@ -331,52 +384,58 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, const std::vector<int>& w
     }
     LocalBatch db;
     db.fp32Hessian = fp32;
-    void* bufs[7] = {};
-    size_t sizes[7] = {sizeof(LocalProblem) * prob.size(), sizeof(int) * B.ltGlobal.size(),
-                       sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
-                       sizeof(int) * B.lvSlot.size(), sizeof(int) * B.initTri.size(),
-                       sizeof(LocalResult) * prob.size()};
+    const size_t sizes[7] = {sizeof(LocalProblem) * prob.size(), sizeof(int) * B.ltGlobal.size(),
+                             sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
+                             sizeof(int) * B.lvSlot.size(), sizeof(int) * B.initTri.size(),
+                             sizeof(LocalResult) * prob.size()};
     const void* src[6] = {prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
                           B.initTri.data()};
     std::vector<LocalResult> out(prob.size());
-    cudaStream_t aux[kClasses] = {};
-    cudaEvent_t ev[kClasses + 1] = {};
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMalloc(&bufs[k], sizes[k] ? sizes[k] : 1);
-    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(bufs[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
-    for (int c = 0; c <= kClasses && e == cudaSuccess; ++c) e = cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[kClasses], in.st);   // uploads done
+    const bool reuse = batchId != 0 && W.uploaded == batchId;
+    for (int k = 0; k < 7 && e == cudaSuccess; ++k)
+        if (W.cap[k] < sizes[k] || !W.buf[k]) {
+            if (k >= 1 && k <= 5) W.uploaded = 0;
+            cudaFree(W.buf[k]);
+            W.buf[k] = nullptr;
+            W.cap[k] = 0;
+            const size_t want = std::max<size_t>(sizes[k] + sizes[k] / 4, 256);
+            e = cudaMalloc(&W.buf[k], want);
+            if (e == cudaSuccess) W.cap[k] = want;
+        }
+    const bool upload = !(reuse && W.uploaded == batchId);
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k)
+        if (k == 0 || upload) e = cudaMemcpyAsync(W.buf[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
+    if (e == cudaSuccess) W.uploaded = batchId;
+    for (int c = 0; c <= kClasses && e == cudaSuccess; ++c)
+        if (!W.ev[c]) e = cudaEventCreateWithFlags(&W.ev[c], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(W.ev[kClasses], in.st);   // uploads done
     if (e == cudaSuccess) {
-        db.ltGlobal = static_cast<const int*>(bufs[1]);
-        db.ltCorner = static_cast<const int*>(bufs[2]);
-        db.lvPos = static_cast<const double2*>(bufs[3]);
-        db.lvSlot = static_cast<const int*>(bufs[4]);
-        db.initTri = static_cast<const int*>(bufs[5]);
+        db.ltGlobal = static_cast<const int*>(W.buf[1]);
+        db.ltCorner = static_cast<const int*>(W.buf[2]);
+        db.lvPos = static_cast<const double2*>(W.buf[3]);
+        db.lvSlot = static_cast<const int*>(W.buf[4]);
+        db.initTri = static_cast<const int*>(W.buf[5]);
         for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
             if (!count[c]) continue;
-            e = cudaStreamCreateWithFlags(&aux[c], cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(aux[c], ev[kClasses], 0);
+            if (!W.aux[c]) e = cudaStreamCreateWithFlags(&W.aux[c], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(W.aux[c], W.ev[kClasses], 0);
             LocalBatch cb = db;
-            cb.prob = static_cast<const LocalProblem*>(bufs[0]) + start[c];
-            cb.out = static_cast<LocalResult*>(bufs[6]) + start[c];
+            cb.prob = static_cast<const LocalProblem*>(W.buf[0]) + start[c];
+            cb.out = static_cast<LocalResult*>(W.buf[6]) + start[c];
             cb.nProb = count[c];
-            if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, sched[c], aux[c]);
-            if (e == cudaSuccess) e = cudaEventRecord(ev[c], aux[c]);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(in.st, ev[c], 0);
+            if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, sched[c], W.aux[c]);
+            if (e == cudaSuccess) e = cudaEventRecord(W.ev[c], W.aux[c]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(in.st, W.ev[c], 0);
         }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), bufs[6], sizes[6], cudaMemcpyDeviceToHost, in.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), W.buf[6], sizes[6], cudaMemcpyDeviceToHost, in.st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(in.st);
     }
-    if (e != cudaSuccess) cudaStreamSynchronize(in.st);
-    for (int c = 0; c < kClasses; ++c)
-        if (aux[c]) {
-            cudaStreamSynchronize(aux[c]);
-            cudaStreamDestroy(aux[c]);
-        }
-    for (auto& x : ev)
-        if (x) cudaEventDestroy(x);
-    for (auto* p : bufs) cudaFree(p);
     if (e != cudaSuccess) {
+        cudaStreamSynchronize(in.st);
+        for (auto s : W.aux)
+            if (s) cudaStreamSynchronize(s);
+        W.uploaded = 0;
         if (err) *err = std::string("topology query: ") + cudaGetErrorString(e);
         return OC_ERR_CUDA;
     }
@@ -674,6 +733,86 @@ int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, b
     return OC_OK;
 }
 
+namespace {
+
+// per-thread scratch and problem batch of the parallel problem assembly
+struct BuildCtx {
+    std::vector<int> tris, tris1, tris2, vmap;
+    std::vector<char> triMark, sideMarkB, sideMarkI;
+    LocalMesh L;
+    Batch B;
+};
+
+// appends src's problems to dst, rebasing their offsets
+void append_batch(Batch& dst, const Batch& src)
+{
+    const int triBase = static_cast<int>(dst.ltGlobal.size()), vertBase = static_cast<int>(dst.lvPos.size()),
+              initBase = static_cast<int>(dst.initTri.size());
+    for (LocalProblem P : src.prob) {
+        P.triOff += triBase;
+        P.vertOff += vertBase;
+        P.initOff += initBase;
+        dst.prob.push_back(P);
+    }
+    dst.ltGlobal.insert(dst.ltGlobal.end(), src.ltGlobal.begin(), src.ltGlobal.end());
+    dst.ltCorner.insert(dst.ltCorner.end(), src.ltCorner.begin(), src.ltCorner.end());
+    dst.lvPos.insert(dst.lvPos.end(), src.lvPos.begin(), src.lvPos.end());
+    dst.lvSlot.insert(dst.lvSlot.end(), src.lvSlot.begin(), src.lvSlot.end());
+    dst.initTri.insert(dst.initTri.end(), src.initTri.begin(), src.initTri.end());
+    dst.tag.insert(dst.tag.end(), src.tag.begin(), src.tag.end());
+}
+
+// the threads' contexts, kept across queries of one mesh size (their
+// marker arrays are left all clear and their vertex maps are reset by the
+// next local-mesh build, so they are reused without clearing)
+struct BuildCache {
+    std::vector<std::unique_ptr<BuildCtx>> ctx;
+    int nV = -1, nF = -1;
+};
+
+// Runs body(ctx, item) for items [0, n) on up to 16 host threads, each a
+// contiguous range, and appends the threads' batches to B in item order
+// (the same problems in the same order as one thread would build).
+template <typename Body>
+void build_parallel(const TopoQueryIn& in, size_t n, Batch& B, const Body& body)
+{
+    BuildCache local;
+    BuildCache* cache = &local;
+    if (in.ws) {
+        if (!in.ws->host) in.ws->host = std::make_shared<BuildCache>();
+        cache = static_cast<BuildCache*>(in.ws->host.get());
+    }
+    if (cache->nV != in.nV || cache->nF != in.nF) {
+        cache->ctx.clear();
+        cache->nV = in.nV;
+        cache->nF = in.nF;
+    }
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = static_cast<int>(std::max<size_t>(1, std::min<size_t>({hw, 16, n / 16 + 1})));
+    if (static_cast<int>(cache->ctx.size()) < nt) cache->ctx.resize(nt);
+    auto work = [&](int t) {
+        std::unique_ptr<BuildCtx>& X = cache->ctx[t];
+        if (!X) {
+            X = std::make_unique<BuildCtx>();
+            X->vmap.assign(in.nV, -1);
+            X->triMark.assign(in.nF, 0);
+            X->sideMarkB.assign(in.nF, 0);
+            X->sideMarkI.assign(in.nF, 0);
+            X->L.map = &X->vmap;
+        }
+        X->B = Batch{};
+        const size_t a = n * t / nt, b = n * (t + 1) / nt;
+        for (size_t i = a; i < b; ++i) body(*X, i);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+    for (int t = 0; t < nt; ++t) append_batch(B, cache->ctx[t]->B);
+}
+
+} // namespace
+
 int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, const TopoOptions& opts,
                std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err,
                TopoExtras* extras)
@@ -724,89 +863,112 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
             filter_candidates(keyed, opType == kOpBoundarySplit ? 0.8 : filterExp, candidatePool);
         out.resize(cands.size());
         for (size_t ci = 0; ci < cands.size(); ++ci) {
-            const int vI = cands[ci];
             TopoCandidate& C = out[ci];
             C.EwDec = -DBL_MAX;
             C.ec0 = C.ec1 = DBL_MAX;
-            const int nbMin = T.nb[T.nbPtr[vI]];
-            if (opType == kOpBoundarySplit) {
-                C.path = {0, 0};
-                // computeLocalLDec boundary branch (TriMesh.cpp:2168-2199):
-                // every interior edge at vI, queryLocalEdDec_bSplit (:2796-2862)
+            C.path = opType == kOpBoundarySplit ? std::vector<int>{0, 0} : std::vector<int>{0, 0, 0};
+        }
+        if (opType == kOpBoundarySplit) {
+            // computeLocalLDec boundary branch (TriMesh.cpp:2168-2199): every
+            // interior edge at each candidate, queryLocalEdDec_bSplit
+            // (:2796-2862); one work item per edge
+            std::vector<std::pair<int, int>> items;   // (candidate, neighbour)
+            for (size_t ci = 0; ci < cands.size(); ++ci) {
+                const int vI = cands[ci];
                 for (int p = T.nbPtr[vI]; p < T.nbPtr[vI + 1]; ++p) {
                     const int nbVI = T.nb[p];
                     if (T.edge_tri(vI, nbVI) < 0 || T.edge_tri(nbVI, vI) < 0) continue;
-                    const int vb = vI, vi = nbVI;
-                    const bool cutThrough = T.bnd[vi] != 0;
-                    T.walk(vb, vi, false, tris);
-                    T.walk(vb, vi, true, tris1);
-                    tris.insert(tris.end(), tris1.begin(), tris1.end());
-                    if (cutThrough) {
-                        for (int t : tris) triMark[t] = 1;
-                        for (int cw = 0; cw < 2; ++cw) {
-                            T.walk(vi, vb, cw != 0, tris2);
-                            for (int t : tris2)
-                                if (!triMark[t]) {
-                                    triMark[t] = 1;
-                                    tris.push_back(t);
-                                }
-                        }
-                        for (int t : tris) triMark[t] = 0;
-                    }
-                    // local split (TriMesh::splitEdgeOnBoundary on the local
-                    // mesh, TriMesh.cpp:2864-3036): the copy of vb takes the
-                    // fan on the (vi -> vb) side; with cutThrough the copy of
-                    // vi takes vi's fan from vb towards the boundary
-                    L.build(T, tris);
-                    const int lb = L.find(vb), li = L.find(vi);
-                    const int nLoc = static_cast<int>(L.gv.size());
-                    std::vector<int> sideB, sideI;
-                    T.walk(vb, vi, true, sideB);
-                    if (cutThrough) T.walk(vi, vb, true, sideI);
-                    else sideI.clear();
-                    for (int t : sideB) sideMarkB[t] = 1;
-                    for (int t : sideI) sideMarkI[t] = 1;
-                    for (size_t k = 0; k < tris.size(); ++k) {
-                        const int t = tris[k];
-                        const bool inB = sideMarkB[t] != 0;
-                        const bool inI = cutThrough && sideMarkI[t] != 0;
-                        for (int c = 0; c < 3; ++c) {
-                            int& lc = L.corner[3 * k + c];
-                            if (inB && lc == lb) lc = nLoc;
-                            else if (inI && lc == li) lc = nLoc + 1;
-                        }
-                    }
-                    for (int t : sideB) sideMarkB[t] = 0;
-                    for (int t : sideI) sideMarkI[t] = 0;
-                    std::vector<double2> extra;
-                    const double2 pb = make_double2(in.UV[2 * (size_t)vb], in.UV[2 * (size_t)vb + 1]);
-                    const double2 pi = make_double2(in.UV[2 * (size_t)vi], in.UV[2 * (size_t)vi + 1]);
-                    extra.push_back(pb);
-                    if (cutThrough) extra.push_back(pi);
-                    // slots in newVertPos row order: vb, copy of vb, copy of vi, vi
-                    std::vector<int> slot(nLoc + extra.size(), -1);
-                    slot[lb] = 0;
-                    slot[nLoc] = 1;
-                    int nFree = 2, nFixed = nLoc - 1;
-                    if (cutThrough) {
-                        slot[nLoc + 1] = 2;
-                        slot[li] = 3;
-                        nFree = 4;
-                        nFixed = nLoc - 2;
-                    }
-                    Batch::Tag tg;
-                    tg.cand = static_cast<int>(ci);
-                    tg.a = vb;
-                    tg.b = vi;
-                    tg.se = rest_dist(in.Vrest, vI, nbVI) / R * (1.0 + 1.0) / 2.0;   // seInc
-                    tg.nRows = cutThrough ? 4 : 2;
-                    emit(B, T, in.rest, in.UV, tris, L, extra, slot, nFree, nFixed, tg);
+                    items.push_back({static_cast<int>(ci), nbVI});
                 }
             }
-            else {
-                // computeLocalLDec interior branch (TriMesh.cpp:2200-2259): all
-                // paths (p0, vI, p2) through two umbrella edges
-                C.path = {0, 0, 0};
+            build_parallel(in, items.size(), B, [&](BuildCtx& X, size_t it) {
+                auto& tris = X.tris;
+                auto& tris1 = X.tris1;
+                auto& tris2 = X.tris2;
+                auto& triMark = X.triMark;
+                auto& sideMarkB = X.sideMarkB;
+                auto& sideMarkI = X.sideMarkI;
+                auto& L = X.L;
+                Batch& B = X.B;
+                const size_t ci = static_cast<size_t>(items[it].first);
+                const int vI = cands[ci], nbVI = items[it].second;
+                const int vb = vI, vi = nbVI;
+                const bool cutThrough = T.bnd[vi] != 0;
+                T.walk(vb, vi, false, tris);
+                T.walk(vb, vi, true, tris1);
+                tris.insert(tris.end(), tris1.begin(), tris1.end());
+                if (cutThrough) {
+                    for (int t : tris) triMark[t] = 1;
+                    for (int cw = 0; cw < 2; ++cw) {
+                        T.walk(vi, vb, cw != 0, tris2);
+                        for (int t : tris2)
+                            if (!triMark[t]) {
+                                triMark[t] = 1;
+                                tris.push_back(t);
+                            }
+                    }
+                    for (int t : tris) triMark[t] = 0;
+                }
+                // local split (TriMesh::splitEdgeOnBoundary on the local
+                // mesh, TriMesh.cpp:2864-3036): the copy of vb takes the
+                // fan on the (vi -> vb) side; with cutThrough the copy of
+                // vi takes vi's fan from vb towards the boundary
+                L.build(T, tris);
+                const int lb = L.find(vb), li = L.find(vi);
+                const int nLoc = static_cast<int>(L.gv.size());
+                std::vector<int> sideB, sideI;
+                T.walk(vb, vi, true, sideB);
+                if (cutThrough) T.walk(vi, vb, true, sideI);
+                else sideI.clear();
+                for (int t : sideB) sideMarkB[t] = 1;
+                for (int t : sideI) sideMarkI[t] = 1;
+                for (size_t k = 0; k < tris.size(); ++k) {
+                    const int t = tris[k];
+                    const bool inB = sideMarkB[t] != 0;
+                    const bool inI = cutThrough && sideMarkI[t] != 0;
+                    for (int c = 0; c < 3; ++c) {
+                        int& lc = L.corner[3 * k + c];
+                        if (inB && lc == lb) lc = nLoc;
+                        else if (inI && lc == li) lc = nLoc + 1;
+                    }
+                }
+                for (int t : sideB) sideMarkB[t] = 0;
+                for (int t : sideI) sideMarkI[t] = 0;
+                std::vector<double2> extra;
+                const double2 pb = make_double2(in.UV[2 * (size_t)vb], in.UV[2 * (size_t)vb + 1]);
+                const double2 pi = make_double2(in.UV[2 * (size_t)vi], in.UV[2 * (size_t)vi + 1]);
+                extra.push_back(pb);
+                if (cutThrough) extra.push_back(pi);
+                // slots in newVertPos row order: vb, copy of vb, copy of vi, vi
+                std::vector<int> slot(nLoc + extra.size(), -1);
+                slot[lb] = 0;
+                slot[nLoc] = 1;
+                int nFree = 2, nFixed = nLoc - 1;
+                if (cutThrough) {
+                    slot[nLoc + 1] = 2;
+                    slot[li] = 3;
+                    nFree = 4;
+                    nFixed = nLoc - 2;
+                }
+                Batch::Tag tg;
+                tg.cand = static_cast<int>(ci);
+                tg.a = vb;
+                tg.b = vi;
+                tg.se = rest_dist(in.Vrest, vI, nbVI) / R * (1.0 + 1.0) / 2.0;   // seInc
+                tg.nRows = cutThrough ? 4 : 2;
+                emit(B, T, in.rest, in.UV, tris, L, extra, slot, nFree, nFixed, tg);
+            });
+        }
+        else {
+            // computeLocalLDec interior branch (TriMesh.cpp:2200-2259): all
+            // paths (p0, vI, p2) through two umbrella edges; one work item
+            // per candidate
+            build_parallel(in, cands.size(), B, [&](BuildCtx& X, size_t ci) {
+                auto& triMark = X.triMark;
+                auto& L = X.L;
+                Batch& B = X.B;
+                const int vI = cands[ci];
+                const int nbMin = T.nb[T.nbPtr[vI]];
                 std::vector<int> umbrella;
                 T.walk(vI, nbMin, false, umbrella);
                 const int n = static_cast<int>(umbrella.size());
@@ -862,7 +1024,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
                         emit(B, T, in.rest, in.UV, umbrella, Lc, extra, slot, 2, nLoc - 1, tg);
                     }
                 }
-            }
+            });
         }
     }
     else if (opType == kOpMerge) {
@@ -981,13 +1143,14 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
     // MLP ranks them and only the top fraction gets the full solve
     std::vector<LocalResult> res(B.prob.size());
     std::vector<char> solved(B.prob.size(), 1);
+    const unsigned long long batchId = in.ws ? in.ws->nextBatch++ : 0;
     const bool learned = (opts.flags & kTopoLearned) && opts.mlp;
     if (!B.prob.empty()) {
         std::string e2;
         if (learned) {
             std::vector<int> all(B.prob.size());
             for (size_t k = 0; k < all.size(); ++k) all[k] = static_cast<int>(k);
-            int rc = solve_batch(in, B, all, 1, opts.flags & kTopoFp32Hessian, res, &e2);
+            int rc = solve_batch(in, B, batchId, all, 1, opts.flags & kTopoFp32Hessian, res, &e2);
             if (rc) { if (err) *err = e2; return rc; }
             const auto tA = clk::now();
             stats.probeMs = std::chrono::duration<double, std::milli>(tA - t1).count();
@@ -1024,7 +1187,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
             }
             std::vector<LocalResult> full(B.prob.size());
             const auto tB = clk::now();
-            rc = solve_batch(in, B, sel, -1, opts.flags & kTopoFp32Hessian, full, &e2);
+            rc = solve_batch(in, B, batchId, sel, -1, opts.flags & kTopoFp32Hessian, full, &e2);
             if (rc) { if (err) *err = e2; return rc; }
             for (int k : sel) res[k] = full[k];
             stats.exactMs = std::chrono::duration<double, std::milli>(clk::now() - tB).count();
@@ -1032,7 +1195,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
         else {
             std::vector<int> all(B.prob.size());
             for (size_t k = 0; k < all.size(); ++k) all[k] = static_cast<int>(k);
-            const int rc = solve_batch(in, B, all, -1, opts.flags & kTopoFp32Hessian, res, &e2);
+            const int rc = solve_batch(in, B, batchId, all, -1, opts.flags & kTopoFp32Hessian, res, &e2);
             if (rc) { if (err) *err = e2; return rc; }
             stats.nSelected = static_cast<int>(all.size());
             if (extras && (opts.flags & kTopoRecordFeatures)) {

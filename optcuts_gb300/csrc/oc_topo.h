@@ -27,6 +27,22 @@ struct TopoCandidate {
 struct TopoAdjacency;
 std::shared_ptr<TopoAdjacency> topo_adjacency(int nV, const int* F, int nF);
 
+// device buffers, streams and events of the batched local solves, kept
+// across queries (one per mesh; not for concurrent queries)
+struct TopoWorkspace {
+    void* buf[7] = {};
+    size_t cap[7] = {};
+    cudaStream_t aux[4] = {};
+    cudaEvent_t ev[5] = {};
+    unsigned long long uploaded = 0;    // batch whose problem arrays buf[1..5] hold
+    unsigned long long nextBatch = 1;
+    std::shared_ptr<void> host;         // per-thread scratch of the host problem assembly
+    TopoWorkspace() = default;
+    TopoWorkspace(const TopoWorkspace&) = delete;
+    TopoWorkspace& operator=(const TopoWorkspace&) = delete;
+    ~TopoWorkspace();
+};
+
 struct TopoQueryIn {
     int nV = 0, nF = 0;
     const int* F = nullptr;          // nF x 3
@@ -40,6 +56,7 @@ struct TopoQueryIn {
     const DeviceMesh* dm = nullptr;  // device copy of the same mesh (rest constants, UV)
     const TopoAdjacency* adj = nullptr;   // adjacency of F (built here when null)
     int bigCluster = 0;              // largest cluster of blocks per local problem (0: the device's, 16 or 8)
+    TopoWorkspace* ws = nullptr;     // reused device buffers (a temporary one when null)
     cudaStream_t st = nullptr;
 };
 
