@@ -385,6 +385,22 @@ def run_ours(args, rank, world):
                 secs += s
             topo["cpu_baseline"] = {"value": secs, "unit": "s", "cores": threads, "kind": "port",
                                     "sample": "the same three queries on the same state"}
+        # the rest of the outer loop's topology step: applying the chosen
+        # operation (Optimizer::createFracture: mesh edit, device mesh, Newton
+        # pattern and symbolic analysis, scaffold, energy), timed once
+        cands = [(q["EwDec_max"], op, q) for op, q in ((oc.OP_BOUNDARY_SPLIT, qb), (oc.OP_MERGE, qm))
+                 if q["best"] >= 0]
+        if cands:
+            ew, op, q = max(cands, key=lambda x: x[0])
+            c = q["candidates"][q["best"]]
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            opt.createFracture(op, c["path"], c["newVertPos"])
+            ctx.synchronize()
+            topo["apply"] = {"value": time.perf_counter() - t0, "unit": "s",
+                             "op": {0: "boundary_split", 1: "interior_split", 2: "merge"}[op], "EwDec": ew,
+                             "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and "
+                                     "analysis, scaffold, energy"}
 
     if rank != 0:
         return

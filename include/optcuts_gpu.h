@@ -342,6 +342,17 @@ int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, doub
 int oc_topo_result_candidates(const oc_topo_result* r, double* EwDec, double* energyChanges, int* path,
                               double* newVertPos, int* posRows);
 int oc_topo_result_destroy(oc_topo_result* r);
+/* Optimizer::createFracture(EDecThres, 0, false, splitInterior)
+ * (Optimizer.cpp:440-503) -> TriMesh::splitOrMerge (TriMesh.cpp:978-1052):
+ * the boundary-split and merge queries (or the interior-split query) on the
+ * optimizer's current state with lambda_t = 1 - energyParams[0], the larger
+ * E_w decrease (split on ties) applied as oc_optimizer_create_fracture does
+ * when it exceeds EDecThres.  With mlp, the queries are the learned
+ * proposal's (top fraction topFrac solved exactly).  *changed = 1 when an
+ * operation was applied; *opType and *EwDecMax report the best candidate
+ * (-DBL_MAX: none). */
+int oc_optimizer_split_or_merge(oc_optimizer* opt, double EDecThres, int splitInterior, double filterExp, int options,
+                                oc_mlp* mlp, double topFrac, int* changed, int* opType, double* EwDecMax);
 /* Optimizer::createFracture(opType, path, newVertPos) (Optimizer.cpp:373-440):
  * applies the operation to the optimizer's mesh (TriMesh::splitEdgeOnBoundary,
  * cutPath or mergeBoundaryEdges with their vertex and cohesive-edge

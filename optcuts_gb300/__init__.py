@@ -110,6 +110,8 @@ _SIGS = {
     "oc_topo_result_destroy": [_vp],
     "oc_topo_result_iterations": [_vp, _i, _i, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_create_fracture": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
+    "oc_optimizer_split_or_merge": [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, _vp,
+                                    ctypes.c_double, _i, _i, _d],
     "oc_mesh_apply_topology": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
     "oc_mesh_get_topology": [_vp, _i, _i, _i, _i, _d, _i],
     "oc_topology_apply": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d,
@@ -725,6 +727,21 @@ class Optimizer:
         self.ctx.check(lib().oc_optimizer_create_fracture(self.h, op, _pi(path), len(path), _pd(pos), len(pos)),
                        "createFracture")
         self.data._sync_topology()
+
+    def splitOrMerge(self, EDecThres, splitInterior=False, filterExp=0.6, fp32=False, mlp=None, topFrac=0.1):
+        """Optimizer::createFracture(EDecThres, 0, false, splitInterior)
+        (Optimizer.cpp:440-503) -> TriMesh::splitOrMerge (TriMesh.cpp:978-1052):
+        query, pick the larger E_w decrease of split and merge, apply it when
+        above EDecThres.  Returns (changed, opType, EwDec_max)."""
+        ch, op, ew = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self.ctx.check(lib().oc_optimizer_split_or_merge(self.h, float(EDecThres), 1 if splitInterior else 0,
+                                                         float(filterExp), 1 if fp32 else 0,
+                                                         mlp.h if mlp is not None else None, float(topFrac),
+                                                         ctypes.byref(ch), ctypes.byref(op), ctypes.byref(ew)),
+                       "splitOrMerge")
+        if ch.value:
+            self.data._sync_topology()
+        return bool(ch.value), op.value, ew.value
 
     def rebuildScaffold(self):
         """Scaffold(result) for the current UV with the project's air-mesh

@@ -11,6 +11,7 @@
 #include "oc_topo.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1798,6 +1799,49 @@ int oc_optimizer_create_fracture(oc_optimizer* o, int opType, const int* path, i
     if (o->scaf)
         OC_CUDA(m->ctx, cudaMemcpyAsync(o->wuv, m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToDevice, m->ctx->stream));
     return compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
+}
+
+int oc_optimizer_split_or_merge(oc_optimizer* o, double EDecThres, int splitInterior, double filterExp, int options,
+                                oc_mlp* mlp, double topFrac, int* changed, int* opType, double* EwDecMax)
+{
+    // Optimizer::createFracture(stressThres, 0, false, allowInSplit)
+    // (Optimizer.cpp:440-503) -> TriMesh::splitOrMerge (TriMesh.cpp:978-1052)
+    if (!o || !o->precomputed || !changed) return OC_ERR_INVALID;
+    *changed = 0;
+    oc_mesh* m = o->mesh;
+    const double lambda_t = 1.0 - o->param;
+    auto run = [&](int op, oc_topo_result** r) {
+        return mlp ? oc_topology_query_learned(m, op, lambda_t, filterExp, options, mlp, topFrac, r)
+                   : oc_topology_query(m, op, lambda_t, filterExp, options, r);
+    };
+    auto bestOf = [](const oc_topo_result* r) { return r->best >= 0 ? r->cands[r->best].EwDec : -DBL_MAX; };
+    oc_topo_result *a = nullptr, *b = nullptr;
+    int rc = run(splitInterior ? oc::kOpInteriorSplit : oc::kOpBoundarySplit, &a);
+    if (!rc && !splitInterior) rc = run(oc::kOpMerge, &b);
+    if (rc) {
+        oc_topo_result_destroy(a);
+        oc_topo_result_destroy(b);
+        return rc;
+    }
+    // the larger decrease of split and merge, split on ties (TriMesh.cpp:1002-1013)
+    const oc_topo_result* pick = a;
+    int op = splitInterior ? oc::kOpInteriorSplit : oc::kOpBoundarySplit;
+    if (b && bestOf(b) > bestOf(a)) {
+        pick = b;
+        op = oc::kOpMerge;
+    }
+    const double best = bestOf(pick);
+    if (opType) *opType = op;
+    if (EwDecMax) *EwDecMax = best;
+    if (best > EDecThres && pick->best >= 0) {   // TriMesh.cpp:1015
+        const oc::TopoCandidate& C = pick->cands[pick->best];
+        rc = oc_optimizer_create_fracture(o, op, C.path.data(), static_cast<int>(C.path.size()), C.pos.data(),
+                                          static_cast<int>(C.pos.size() / 2));
+        if (!rc) *changed = 1;
+    }
+    oc_topo_result_destroy(a);
+    oc_topo_result_destroy(b);
+    return rc;
 }
 
 int oc_optimizer_rebuild_scaffold(oc_optimizer* o)

@@ -173,7 +173,12 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
     const int groups = static_cast<int>(blockDim.x) / TPP;   // problems per block (TPP <= 32: 1-16)
     const int grp = threadIdx.x / TPP;
     const int pi = CL > 1 ? static_cast<int>(blockIdx.x) / CL : static_cast<int>(blockIdx.x) * groups + grp;
-    if (pi >= b.nProb) return;   // uniform per group, block and cluster
+    // packed groups (TPP < 32) stay alive past the last problem, solving a
+    // copy of it without writing a result, so that their warp can reconverge
+    // once per Newton iteration; the other forms leave (uniform per block
+    // and cluster)
+    const bool valid = pi < b.nProb;
+    if (TPP >= 32 && !valid) return;
     LocalGroup<TPP, CL> G;
     G.sub = threadIdx.x % TPP;
     G.mask = TPP >= 32 ? 0xffffffffu : (((1u << TPP) - 1u) << ((threadIdx.x & 31) & ~(TPP - 1)));
@@ -182,7 +187,7 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
     LocalShared<TPP>& S = reinterpret_cast<LocalShared<TPP>*>(localSmem)[grp];
     const int sub = G.sub;
     const long long clk0 = clock64();
-    const LocalProblem P = b.prob[pi];
+    const LocalProblem P = b.prob[valid ? pi : b.nProb - 1];
     const int nDof = 2 * P.nFree;
     // this block's triangles [lo, hi) and initial-energy triangles [ilo, ihi)
     const int per = (P.nTri + CL - 1) / CL, iper = (P.nInit + CL - 1) / CL;
@@ -294,7 +299,16 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
         raw[4] = lastE;   // E1: replaced after the first step
     }
     constexpr int kEntRounds = (36 + TPP - 1) / TPP;
-    for (; it < P.maxIter && finite; ++it) {
+    bool running = true;
+    for (;;) {
+        running = running && it < P.maxIter && finite;
+        if constexpr (TPP < 32) {
+            if (!__any_sync(0xffffffffu, running)) break;
+        }
+        else {
+            if (!running) break;
+        }
+        if (running) do {
         // gradient (fixed vertices have no slot: zero rows)
         double gj = 0.0;
         for (int c0 = lo; c0 < hi; c0 += TPP) {
@@ -329,6 +343,7 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
         if (it == 0) raw[1] = gsq;
         if (gsq < P.targetGRes) {   // Optimizer.cpp:215-221
             status = 1;
+            running = false;
             break;
         }
         // dense Hessian of the free DOFs: projected triangle blocks summed in
@@ -477,11 +492,18 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
         if (stopped) {
             status = 1;
             ++it;
+            running = false;
             break;
         }
+        ++it;
+        } while (false);
+        // packed groups: reconverge the warp once per iteration, so that the
+        // next iteration's element Hessians run for all of its problems at
+        // once instead of one group after another
+        if constexpr (TPP < 32) __syncwarp();
     }
     if (!finite) status = 2;
-    if (sub == 0 && G.rank == 0) {
+    if (valid && sub == 0 && G.rank == 0) {
         LocalResult r;
         r.initE = initE;
         r.lastE = lastE;

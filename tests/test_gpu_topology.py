@@ -128,6 +128,35 @@ def test_create_fracture_through_the_optimizer(golden, case):
     assert m.checkInversion()
 
 
+@pytest.mark.parametrize("case", ["icosphere_320_topo", "sheet_3k_topo"])
+@pytest.mark.parametrize("learned", [False, True])
+def test_split_or_merge(golden, case, learned):
+    """Optimizer::createFracture(thres, 0, ...) -> TriMesh::splitOrMerge: the
+    larger of the best boundary split and the best merge, applied when above
+    the threshold; the reference's applied boundary split comes out (its
+    topology bit-exact, positions to the candidates' tolerance). The learned
+    form with every problem selected takes the same decision."""
+    g = golden(case)
+    par = 1.0 - g["topo_best"][3]
+    m = topo_mesh(g)
+    opt = oc.Optimizer(m, [par])
+    opt.precompute()
+    F0 = m.F.copy()
+    mlp = oc.MLP(32, 128, seed=3) if learned else None
+    changed, op, ew = opt.splitOrMerge(1e300, mlp=mlp, topFrac=1.0)
+    assert not changed and op == oc.OP_BOUNDARY_SPLIT
+    assert ew == pytest.approx(g["topo_best"][0], rel=1e-6)
+    np.testing.assert_array_equal(m.F, F0)
+    changed, op, ew = opt.splitOrMerge(-1e300, mlp=mlp, topFrac=1.0)
+    assert changed and op == oc.OP_BOUNDARY_SPLIT
+    np.testing.assert_array_equal(m.F, g["topo_afterB_F"])
+    np.testing.assert_array_equal(m.cohE, g["topo_afterB_cohE"].reshape(-1, 4))
+    ref = g["topo_afterB_V"]
+    assert np.abs(m.V - ref).max() <= 1e-5 * np.abs(ref).max()
+    e = opt.getLastEnergyVal()
+    assert e == pytest.approx(par * oc.SymDirichletEnergy().computeEnergyVal(m), rel=1e-13)
+
+
 @pytest.mark.parametrize("nlon,nlat", [(24, 8), (72, 10), (200, 10)])
 def test_problem_size_classes_match_oracle(nlon, nlat):
     """Pole fans of 24, 72 and 200 triangles put boundary-split problems in
