@@ -285,8 +285,7 @@ def run_ours(args, rank, world):
             # query), the first query rebuilding the vertex adjacency as it
             # does after an applied operation
             mesh.dropAdjacency()
-            return (mesh.querySplit(lam_t, False, **kw), mesh.queryMerge(lam_t, **kw),
-                    mesh.querySplit(lam_t, True, **kw))
+            return mesh.topologyStep(lam_t, **kw)
 
         # exhaustive pairs (features, exact fraction of the local excess
         # energy removed) from earlier states of the same run, then the
@@ -312,13 +311,13 @@ def run_ours(args, rank, world):
             return time.perf_counter() - t0, qs
 
         def summary(qs):
+            # the three queries run as one step: one library call, one shared
+            # device solve (probe and exact passes for the learned proposal)
             qb, qm, qi = qs
-            return {"query_ms": sum(q["query_ms"] for q in qs),
-                    "per_query_ms": {name: {"query": q["query_ms"], "build": q["build_ms"], "solve": q["solve_ms"],
-                                            "probe": q["probe_ms"], "exact": q["exact_ms"]}
-                                     for name, q in zip(("boundary_split", "merge", "interior_split"), qs)},
-                    "gpu_solve_ms": sum(q["solve_ms"] for q in qs),
-                    "host_build_ms": sum(q["build_ms"] for q in qs),
+            return {"query_ms": qb["query_ms"], "gpu_solve_ms": qb["solve_ms"], "probe_ms": qb["probe_ms"],
+                    "exact_ms": qb["exact_ms"],
+                    "host_build_ms": {name: q["build_ms"]
+                                      for name, q in zip(("boundary_split", "merge", "interior_split"), qs)},
                     "local_problems": sum(q["local_problems"] for q in qs),
                     "exact_solves": sum(q["selected"] for q in qs),
                     "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"],
@@ -327,7 +326,8 @@ def run_ours(args, rank, world):
         queries()   # warm-up
         t_gpu, (qb, qm, qi) = timed_step()
         t_fp32, qs32 = timed_step(fp32=True)
-        topo = {"metric": "topology-step s (exhaustive candidate evaluation)", "value": t_gpu, "unit": "s",
+        topo = {"metric": "topology-step s (exhaustive candidate evaluation: boundary split, merge and interior "
+                          "split queries of one state, solved together)", "value": t_gpu, "unit": "s",
                 "higher_is_better": False, "bijectivity": "off (local solves without air meshes)",
                 "newton_iterations_before": converged_after if converged_after else
                 base_it + args.topo_newton_iters,

@@ -282,6 +282,15 @@ int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterE
 typedef struct oc_mlp oc_mlp;
 int oc_topology_query_learned(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_mlp* mlp,
                               double topFrac, oc_topo_result** out);
+/* One topology step's three queries on the same state — boundary split,
+ * merge, interior split (querySplit / queryMerge / querySplit(splitInterior),
+ * as createFracture with and without allowInSplit ask for them) — built
+ * together and solved in the same launches; each result equals its own
+ * query's.  mlp NULL: exhaustive (options as oc_topology_query); else the
+ * learned proposal with the top fraction topFrac of each operation's local
+ * problems solved exactly. */
+int oc_topology_step(oc_mesh* mesh, double lambda_t, double filterExp, int options, oc_mlp* mlp, double topFrac,
+                     oc_topo_result** split, oc_topo_result** merge, oc_topo_result** interior);
 /* per local problem (rows): the 32 features, the exact target (fraction of
  * the local excess energy removed; queries with OC_TOPO_RECORD_FEATURES)
  * and the MLP's prediction (learned queries); NULL arrays are skipped */

@@ -123,6 +123,8 @@ _SIGS = {
     "oc_topo_result_timing": [_vp, _i, _d, _d],
     "oc_topo_result_problems": [_vp, _i, _vp, _vp, _vp],
     "oc_topo_result_candidates": [_vp, _vp, _vp, _vp, _vp, _vp],
+    "oc_topology_step": [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp, ctypes.c_double,
+                         ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)],
     "oc_topo_result_problem_stats": [_vp, _i, _vp, _vp, _vp, _vp, _vp],
     "oc_mlp_create": [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(_vp)],
     "oc_mlp_destroy": [_vp],
@@ -309,6 +311,25 @@ class TriMesh:
             self.ctx.check(lib().oc_topology_query(self.h, op, float(lambda_t), float(filterExp), opt,
                                                    ctypes.byref(h)), "topology query")
         query_ms = 1000.0 * (time.perf_counter() - t0)
+        return self._result(h, features, mlp, query_ms)
+
+    def topologyStep(self, lambda_t, filterExp=0.6, fp32=False, features=False, mlp=None, topFrac=0.1):
+        """The three queries of one topology step on the current state —
+        boundary split, merge, interior split — built together and solved in
+        the same launches (each result equals its own query's); with mlp the
+        learned proposal (top fraction topFrac of each operation's problems
+        solved exactly).  Returns (split, merge, interior); query_ms of each is
+        the whole step's library time."""
+        hs = [_vp(), _vp(), _vp()]
+        opt = (1 if fp32 else 0) | (2 if features else 0)
+        t0 = time.perf_counter()
+        self.ctx.check(lib().oc_topology_step(self.h, float(lambda_t), float(filterExp), opt,
+                                              mlp.h if mlp is not None else None, float(topFrac),
+                                              *(ctypes.byref(h) for h in hs)), "topology step")
+        step_ms = 1000.0 * (time.perf_counter() - t0)
+        return tuple(self._result(h, features, mlp, step_ms) for h in hs)
+
+    def _result(self, h, features, mlp, query_ms):
         try:
             n, best, pool, nprob, mit = (ctypes.c_int() for _ in range(5))
             bms, sms = ctypes.c_double(), ctypes.c_double()

@@ -810,16 +810,22 @@ int oc_topology_query_learned(oc_mesh* m, int opType, double lambda_t, double fi
     return topology_query(m, opType, lambda_t, filterExp, opts, out);
 }
 
-static int topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, const oc::TopoOptions& opts,
-                          oc_topo_result** out)
+// the operations ops[0..nOps) on the mesh's current state, solved together
+static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, double filterExp,
+                            const oc::TopoOptions& opts, oc_topo_result** out)
 {
-    if (!m || !out || opType < 0 || opType > 2) return OC_ERR_INVALID;
-    *out = nullptr;
+    if (!m || !out || nOps <= 0) return OC_ERR_INVALID;
+    bool split = false;
+    for (int i = 0; i < nOps; ++i) {
+        out[i] = nullptr;
+        if (ops[i] < 0 || ops[i] > 2) return OC_ERR_INVALID;
+        split = split || ops[i] != oc::kOpMerge;
+    }
     const int nV = m->d.nV;
     std::vector<double> uv(2 * (size_t)nV), dg;
     OC_CUDA(m->ctx, cudaMemcpyAsync(uv.data(), m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToHost, m->ctx->stream));
     OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
-    if (opType != oc::kOpMerge) {
+    if (split) {
         dg.resize(nV);
         int rc = oc_mesh_split_filter(m, dg.data());
         if (rc) return rc;
@@ -851,16 +857,56 @@ static int topology_query(oc_mesh* m, int opType, double lambda_t, double filter
     in.bigCluster = bigCluster;
     if (!m->topoWs) m->topoWs = std::make_shared<oc::TopoWorkspace>();
     in.ws = m->topoWs.get();
-    oc_topo_result* r = new (std::nothrow) oc_topo_result;
-    if (!r) return OC_ERR_NOMEM;
+    std::vector<oc::TopoOpResult> res(nOps);
     std::string err;
-    const int rc = oc::topo_query(in, opType, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, r->cands, r->best,
-                                  r->pool, r->stats, &err, &r->extras);
-    if (rc) {
-        delete r;
-        return fail(m->ctx, rc, err);
+    const int rc = oc::topo_query_ops(in, ops, nOps, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, res.data(),
+                                      &err);
+    if (rc) return fail(m->ctx, rc, err);
+    for (int i = 0; i < nOps; ++i) {
+        oc_topo_result* r = new (std::nothrow) oc_topo_result;
+        if (!r) {
+            for (int j = 0; j < i; ++j) {
+                delete out[j];
+                out[j] = nullptr;
+            }
+            return OC_ERR_NOMEM;
+        }
+        r->cands.swap(res[i].cands);
+        r->best = res[i].best;
+        r->pool = res[i].pool;
+        r->stats = res[i].stats;
+        r->extras = std::move(res[i].extras);
+        out[i] = r;
     }
-    *out = r;
+    return OC_OK;
+}
+
+static int topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, const oc::TopoOptions& opts,
+                          oc_topo_result** out)
+{
+    if (!m || !out || opType < 0 || opType > 2) return OC_ERR_INVALID;
+    return topology_queries(m, &opType, 1, lambda_t, filterExp, opts, out);
+}
+
+int oc_topology_step(oc_mesh* m, double lambda_t, double filterExp, int options, oc_mlp* mlp, double topFrac,
+                     oc_topo_result** split, oc_topo_result** merge, oc_topo_result** interior)
+{
+    if (!split || !merge || !interior) return OC_ERR_INVALID;
+    if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
+    oc::TopoOptions opts;
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    if (mlp) {
+        opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+        opts.mlp = &mlp->m;
+        opts.topFrac = topFrac;
+    }
+    const int ops[3] = {oc::kOpBoundarySplit, oc::kOpMerge, oc::kOpInteriorSplit};
+    oc_topo_result* r[3] = {};
+    const int rc = topology_queries(m, ops, 3, lambda_t, filterExp, opts, r);
+    if (rc) return rc;
+    *split = r[0];
+    *merge = r[1];
+    *interior = r[2];
     return OC_OK;
 }
 

@@ -144,7 +144,7 @@ int reduce_blocks_for(int n);
 
 // batched projected-Newton solves of the topology candidates' local
 // problems: tpp threads per problem, or per block of a cluster of `cluster`
-// blocks (schedules 8/1, 32/1, 128/1, 64/2, 64/4, 64/8, 64/16);
+// blocks (schedules 8/1, 32/1, 128/1, 64/2..16);
 // local_schedule picks one for a size class (largest triangle count, number
 // of problems), local_max_cluster is 16 where the device runs 16-block
 // clusters of this kernel, else 8

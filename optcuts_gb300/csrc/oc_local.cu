@@ -20,13 +20,13 @@ namespace {
 // (Optimizer with useDense, energyParams {1}, relGL2Tol 1e-6,
 // solve(maxIter): Optimizer.cpp:203-261, 505-652; dense Hessian
 // SymDirichletEnergy.cpp:306-427 + LDLT), one local problem per group of
-// TPP threads (CL = 1) or per thread-block cluster of CL blocks of TPP
-// threads.  Threads own triangles; a block sums its contiguous range of
+// TPP threads (CL = 1) or per thread-block cluster of blocks of TPP threads
+// (CL = 2: clustered, the cluster's size read at run time).  Threads own triangles; a block sums its contiguous range of
 // triangles in triangle order on single threads, and a cluster adds its
 // blocks' partial sums in rank order (every block reads them all through
 // distributed shared memory, so all blocks hold the same totals and run
-// the same serial steps).  The arithmetic depends only on (TPP, CL), which
-// the host picks from the triangle count, so results are deterministic.
+// the same serial steps).  The arithmetic depends only on the schedule,
+// which the host picks from the triangle count, so results are deterministic.
 // TPP 8 and 32 pack several problems into a 128-thread block (sub-warp
 // groups); TPP 128 gives one problem a block; clusters spread the
 // few-hundred-triangle fans around high-valence vertices over several SMs.
@@ -50,7 +50,7 @@ struct LocalShared {
 template <int TPP, int CL>
 struct LocalGroup {
     unsigned mask;
-    int sub, rank, buf;
+    int sub, rank, ncl, buf;   // ncl: blocks in this problem's cluster (1 unclustered)
     __device__ __forceinline__ void sync() const
     {
         if constexpr (TPP <= 32) __syncwarp(mask);
@@ -123,7 +123,7 @@ __device__ __forceinline__ double cluster_combine(LocalShared<TPP>& S, LocalGrou
         cl.sync();
         double tot = v;
         if (slot >= 0)
-            for (int r = 0; r < CL; ++r) {
+            for (int r = 0; r < G.ncl; ++r) {
                 const double x = cl.map_shared_rank(part, r)[slot];
                 tot = r == 0 ? x : (op == 0 ? tot + x : (op == 1 ? fmin(tot, x) : fmax(tot, x)));
             }
@@ -172,7 +172,13 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
     extern __shared__ __align__(16) unsigned char localSmem[];
     const int groups = static_cast<int>(blockDim.x) / TPP;   // problems per block (TPP <= 32: 1-16)
     const int grp = threadIdx.x / TPP;
-    const int pi = CL > 1 ? static_cast<int>(blockIdx.x) / CL : static_cast<int>(blockIdx.x) * groups + grp;
+    int ncl = 1, rank = 0;
+    if constexpr (CL > 1) {
+        cg::cluster_group cl = cg::this_cluster();
+        ncl = static_cast<int>(cl.num_blocks());
+        rank = static_cast<int>(cl.block_rank());
+    }
+    const int pi = CL > 1 ? static_cast<int>(blockIdx.x) / ncl : static_cast<int>(blockIdx.x) * groups + grp;
     // packed groups (TPP < 32) stay alive past the last problem, solving a
     // copy of it without writing a result, so that their warp can reconverge
     // once per Newton iteration; the other forms leave (uniform per block
@@ -182,7 +188,8 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
     LocalGroup<TPP, CL> G;
     G.sub = threadIdx.x % TPP;
     G.mask = TPP >= 32 ? 0xffffffffu : (((1u << TPP) - 1u) << ((threadIdx.x & 31) & ~(TPP - 1)));
-    G.rank = CL > 1 ? static_cast<int>(blockIdx.x) % CL : 0;
+    G.rank = rank;
+    G.ncl = ncl;
     G.buf = 0;
     LocalShared<TPP>& S = reinterpret_cast<LocalShared<TPP>*>(localSmem)[grp];
     const int sub = G.sub;
@@ -190,7 +197,7 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
     const LocalProblem P = b.prob[valid ? pi : b.nProb - 1];
     const int nDof = 2 * P.nFree;
     // this block's triangles [lo, hi) and initial-energy triangles [ilo, ihi)
-    const int per = (P.nTri + CL - 1) / CL, iper = (P.nInit + CL - 1) / CL;
+    const int per = (P.nTri + ncl - 1) / ncl, iper = (P.nInit + ncl - 1) / ncl;
     const int lo = min(P.nTri, G.rank * per), hi = min(P.nTri, lo + per);
     const int ilo = min(P.nInit, G.rank * iper), ihi = min(P.nInit, ilo + iper);
     for (int j = sub; j < P.nVert; j += TPP) {
@@ -524,7 +531,8 @@ __global__ void __launch_bounds__(local_threads<TPP, CL>(), (TPP >= 128 || CL > 
 
 namespace {
 template <int TPP, int CL>
-cudaError_t launch_local_tpp(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, int block, cudaStream_t st)
+cudaError_t launch_local_tpp(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, int block, int cluster,
+                             cudaStream_t st)
 {
     constexpr int maxThreads = local_threads<TPP, CL>();
     const int threads = (TPP >= 128 || CL > 1) ? maxThreads : std::max(TPP, std::min(maxThreads, block));
@@ -533,7 +541,7 @@ cudaError_t launch_local_tpp(const DeviceMesh& m, double surfaceArea, const Loca
     static const cudaError_t attr = [] {
         cudaError_t e = cudaFuncSetAttribute(k_local_newton<TPP, CL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smemMax));
-        if (e == cudaSuccess && CL > 8)
+        if (e == cudaSuccess && CL > 1)
             e = cudaFuncSetAttribute(k_local_newton<TPP, CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         return e;
     }();
@@ -545,13 +553,13 @@ cudaError_t launch_local_tpp(const DeviceMesh& m, double surfaceArea, const Loca
     }
     else {
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(static_cast<unsigned>(b.nProb) * CL, 1, 1);
+        cfg.gridDim = dim3(static_cast<unsigned>(b.nProb) * cluster, 1, 1);
         cfg.blockDim = dim3(threads, 1, 1);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = st;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = CL;
+        at[0].val.clusterDim.x = cluster;
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
@@ -565,16 +573,16 @@ cudaError_t launch_local_tpp(const DeviceMesh& m, double surfaceArea, const Loca
 // 5-8 triangle problems pack four to a warp (a warp's FP64 instruction costs
 // the same however many lanes are active), in 128-thread blocks when there
 // are enough of them to give every SM two blocks, else in single-warp blocks
-// spread over more SMs; larger problems spread over a cluster of blocks so
-// that count x cluster blocks give at most about four blocks per SM, each
-// block keeping at least 16 triangles.
+// spread over more SMs; larger problems spread over a cluster of blocks, one
+// warp's worth (32) of triangles per block, as long as count x cluster
+// blocks stay within about four blocks per SM.
 LocalSchedule local_schedule(int maxTri, int count, int numSMs, int maxCluster)
 {
     if (maxTri <= 8) return {8, 1, count / 16 >= 2 * numSMs ? 128 : 32};
     if (maxTri <= 40) return {32, 1, count / 4 >= 2 * numSMs ? 128 : 32};
-    int c = 1;
-    while (c < maxCluster && 2 * c * count <= 4 * numSMs && maxTri / (2 * c) >= 16) c *= 2;
-    if (c == 1) return {128, 1, 128};
+    int c = std::min(maxCluster, (maxTri + 31) / 32);
+    while (c > 1 && c * count > 4 * numSMs) --c;
+    if (c <= 1) return {128, 1, 128};
     return {64, c, 64};
 }
 
@@ -585,7 +593,7 @@ int local_max_cluster()
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(16, 1, 1);
         cfg.blockDim = dim3(64, 1, 1);
-        cfg.dynamicSmemBytes = local_smem<64, 16>(64);
+        cfg.dynamicSmemBytes = local_smem<64, 2>(64);
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = 16;
@@ -594,11 +602,11 @@ int local_max_cluster()
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int n = 0;
-        if (cudaFuncSetAttribute(k_local_newton<64, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+        if (cudaFuncSetAttribute(k_local_newton<64, 2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                 cudaSuccess ||
-            cudaFuncSetAttribute(k_local_newton<64, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(local_smem<64, 16>(64))) != cudaSuccess ||
-            cudaOccupancyMaxActiveClusters(&n, k_local_newton<64, 16>, &cfg) != cudaSuccess) {
+            cudaFuncSetAttribute(k_local_newton<64, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(local_smem<64, 2>(64))) != cudaSuccess ||
+            cudaOccupancyMaxActiveClusters(&n, k_local_newton<64, 2>, &cfg) != cudaSuccess) {
             cudaGetLastError();
             return 8;
         }
@@ -612,13 +620,15 @@ cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const L
 {
     if (b.nProb <= 0) return cudaSuccess;
     const int bl = sc.block;
-    if (sc.tpp == 8 && sc.cluster == 1) return launch_local_tpp<8, 1>(m, surfaceArea, b, bl, st);
-    if (sc.tpp == 32 && sc.cluster == 1) return launch_local_tpp<32, 1>(m, surfaceArea, b, bl, st);
-    if (sc.tpp == 128 && sc.cluster == 1) return launch_local_tpp<128, 1>(m, surfaceArea, b, bl, st);
-    if (sc.tpp == 64 && sc.cluster == 2) return launch_local_tpp<64, 2>(m, surfaceArea, b, bl, st);
-    if (sc.tpp == 64 && sc.cluster == 4) return launch_local_tpp<64, 4>(m, surfaceArea, b, bl, st);
-    if (sc.tpp == 64 && sc.cluster == 8) return launch_local_tpp<64, 8>(m, surfaceArea, b, bl, st);
-    if (sc.tpp == 64 && sc.cluster == 16) return launch_local_tpp<64, 16>(m, surfaceArea, b, bl, st);
+    if (sc.cluster == 1) {
+        if (sc.tpp == 8) return launch_local_tpp<8, 1>(m, surfaceArea, b, bl, 1, st);
+        if (sc.tpp == 32) return launch_local_tpp<32, 1>(m, surfaceArea, b, bl, 1, st);
+        if (sc.tpp == 128) return launch_local_tpp<128, 1>(m, surfaceArea, b, bl, 1, st);
+    }
+    else if (sc.tpp == 64 && sc.cluster >= 2 && sc.cluster <= 16) {
+        // clustered form: the cluster size is read at run time
+        return launch_local_tpp<64, 2>(m, surfaceArea, b, bl, sc.cluster, st);
+    }
     return cudaErrorInvalidValue;
 }
 

@@ -418,8 +418,20 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
         db.initTri = static_cast<const int*>(W.buf[5]);
         for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
             if (!count[c]) continue;
-            if (!W.aux[c]) e = cudaStreamCreateWithFlags(&W.aux[c], cudaStreamNonBlocking);
+            if (!W.aux[c]) {
+                // the largest problems (the long pole, on clusters when few)
+                // on the highest-priority stream, so that the block scheduler
+                // places them before the many small problems' blocks
+                int least = 0, greatest = 0;
+                cudaDeviceGetStreamPriorityRange(&least, &greatest);
+                e = cudaStreamCreateWithPriority(&W.aux[c], cudaStreamNonBlocking, c == 0 ? greatest : least);
+            }
             if (e == cudaSuccess) e = cudaStreamWaitEvent(W.aux[c], W.ev[kClasses], 0);
+            // clustered large problems (few, latency-bound: the long pole)
+            // run alone; the other classes start after them instead of
+            // taking their SMs' FP64 pipes
+            if (e == cudaSuccess && c > 0 && count[0] && sched[0].cluster > 1)
+                e = cudaStreamWaitEvent(W.aux[c], W.ev[0], 0);
             LocalBatch cb = db;
             cb.prob = static_cast<const LocalProblem*>(W.buf[0]) + start[c];
             cb.out = static_cast<LocalResult*>(W.buf[6]) + start[c];
@@ -813,29 +825,15 @@ void build_parallel(const TopoQueryIn& in, size_t n, Batch& B, const Body& body)
 
 } // namespace
 
-int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, const TopoOptions& opts,
-               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err,
-               TopoExtras* extras)
+namespace {
+
+// Candidates and local problems of one operation (the enumeration of
+// querySplit / queryMerge) appended to B; candidatePool as the reference
+// reports it.
+int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp, std::vector<TopoCandidate>& out,
+             int& candidatePool, Batch& B, std::string* err)
 {
-    using clk = std::chrono::steady_clock;
-    const auto t0 = clk::now();
-    out.clear();
-    best = -1;
-    candidatePool = 0;
-    stats = TopoStats{};
-    if (!in.F || !in.Vrest || !in.UV || !in.rest || !in.dm || in.nV <= 0 || in.nF <= 0) {
-        if (err) *err = "topology query: bad arguments";
-        return OC_ERR_INVALID;
-    }
-    Topo ownT;
-    if (!in.adj) ownT.build(in.nV, in.F, in.nF);
-    const Topo& T = in.adj ? in.adj->T : ownT;
-    if (T.nV != in.nV || T.nF != in.nF || T.F != in.F) {
-        if (err) *err = "topology query: adjacency of another mesh";
-        return OC_ERR_INVALID;
-    }
     const double R = in.virtualRadius;
-    Batch B;
     std::vector<int> tris, tris1, tris2;
     std::vector<int> vmap(in.nV, -1);
     std::vector<char> triMark(in.nF, 0), sideMarkB(in.nF, 0), sideMarkI(in.nF, 0);
@@ -1133,107 +1131,35 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
         if (err) *err = "topology query: unknown operation";
         return OC_ERR_INVALID;
     }
-    stats.nCandidates = static_cast<int>(out.size());
-    stats.nProblems = static_cast<int>(B.prob.size());
-    const auto t1 = clk::now();
-    stats.buildMs = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    return OC_OK;
+}
 
-    // one batched device solve of all problems (exhaustive), or the learned
-    // proposal: a one-step pass over all problems gives their features, the
-    // MLP ranks them and only the top fraction gets the full solve
-    std::vector<LocalResult> res(B.prob.size());
-    std::vector<char> solved(B.prob.size(), 1);
-    const unsigned long long batchId = in.ws ? in.ws->nextBatch++ : 0;
-    const bool learned = (opts.flags & kTopoLearned) && opts.mlp;
-    if (!B.prob.empty()) {
-        std::string e2;
-        if (learned) {
-            std::vector<int> all(B.prob.size());
-            for (size_t k = 0; k < all.size(); ++k) all[k] = static_cast<int>(k);
-            int rc = solve_batch(in, B, batchId, all, 1, opts.flags & kTopoFp32Hessian, res, &e2);
-            if (rc) { if (err) *err = e2; return rc; }
-            const auto tA = clk::now();
-            stats.probeMs = std::chrono::duration<double, std::milli>(tA - t1).count();
-            // features -> predicted fraction of excess energy removed -> E_w decrease
-            const int n = static_cast<int>(B.prob.size());
-            std::vector<float> X((size_t)n * kTopoNumFeatures), r(n);
-            for (int k = 0; k < n; ++k) topo_features(B.prob[k], res[k], opType, in, &X[(size_t)k * kTopoNumFeatures]);
-            rc = mlp_predict_host(*opts.mlp, X.data(), n, r.data());
-            if (rc) { if (err) *err = "topology query: MLP inference failed"; return rc; }
-            std::vector<std::pair<double, int>> pred(n);
-            for (int k = 0; k < n; ++k) {
-                const double sdd = static_cast<double>(r[k]) * excess_global(B.prob[k], res[k], in.surfaceArea);
-                const double ew = opType == kOpMerge ? lambda_t * B.tag[k].se + (1.0 - lambda_t) * sdd
-                                                     : (1.0 - lambda_t) * sdd - lambda_t * B.tag[k].se;
-                pred[k] = {-ew, k};
-            }
-            if (extras) {
-                extras->ewPred.resize(n);
-                for (int k = 0; k < n; ++k) extras->ewPred[k] = -pred[k].first * (opType == kOpInteriorSplit ? 0.5 : 1.0);
-            }
-            std::stable_sort(pred.begin(), pred.end());
-            int kTop = static_cast<int>(std::ceil(opts.topFrac * n));
-            kTop = std::max(1, std::min(n, kTop));
-            std::vector<int> sel(kTop);
-            for (int i = 0; i < kTop; ++i) sel[i] = pred[i].second;
-            std::sort(sel.begin(), sel.end());
-            std::fill(solved.begin(), solved.end(), 0);
-            for (int k : sel) solved[k] = 1;
-            stats.nSelected = kTop;
-            if (extras) {
-                extras->X.swap(X);
-                extras->predicted.assign(n, 0.0f);
-                for (int k = 0; k < n; ++k) extras->predicted[k] = r[k];
-            }
-            std::vector<LocalResult> full(B.prob.size());
-            const auto tB = clk::now();
-            rc = solve_batch(in, B, batchId, sel, -1, opts.flags & kTopoFp32Hessian, full, &e2);
-            if (rc) { if (err) *err = e2; return rc; }
-            for (int k : sel) res[k] = full[k];
-            stats.exactMs = std::chrono::duration<double, std::milli>(clk::now() - tB).count();
-        }
-        else {
-            std::vector<int> all(B.prob.size());
-            for (size_t k = 0; k < all.size(); ++k) all[k] = static_cast<int>(k);
-            const int rc = solve_batch(in, B, batchId, all, -1, opts.flags & kTopoFp32Hessian, res, &e2);
-            if (rc) { if (err) *err = e2; return rc; }
-            stats.nSelected = static_cast<int>(all.size());
-            if (extras && (opts.flags & kTopoRecordFeatures)) {
-                const int n = static_cast<int>(B.prob.size());
-                extras->X.assign((size_t)n * kTopoNumFeatures, 0.0f);
-                extras->target.assign(n, 0.0f);
-                for (int k = 0; k < n; ++k) {
-                    topo_features(B.prob[k], res[k], opType, in, &extras->X[(size_t)k * kTopoNumFeatures]);
-                    const double xs = excess_global(B.prob[k], res[k], in.surfaceArea);
-                    double t = xs > 0.0 ? res[k].eDec / xs : 0.0;
-                    extras->target[k] = static_cast<float>(std::max(-1.0, std::min(1.0, t)));
-                }
-            }
-        }
-    }
-    const auto t2 = clk::now();
-    stats.solveMs = std::chrono::duration<double, std::milli>(t2 - t1).count();
-
+// Per candidate of one operation: the best of its solved local problems
+// (strict >, first wins) over problems [p0, p1) of B; interior splits halved.
+void finish_op(int opType, double lambda_t, const Batch& B, size_t p0, size_t p1, const std::vector<LocalResult>& res,
+               const std::vector<char>& solved, std::vector<TopoCandidate>& out, int& best, TopoStats& stats,
+               TopoExtras* extras)
+{
+    best = -1;
     if (extras) {
-        extras->cand.resize(B.prob.size());
-        extras->ewExact.assign(B.prob.size(), std::nan(""));
-        for (size_t k = 0; k < B.prob.size(); ++k) extras->cand[k] = B.tag[k].cand;
-        const size_t n = B.prob.size();
+        const size_t n = p1 - p0;
+        extras->cand.resize(n);
+        extras->ewExact.assign(n, std::nan(""));
         extras->nTri.resize(n);
         extras->nFree.resize(n);
         extras->iters.resize(n);
         extras->trials.resize(n);
         extras->cycles.resize(n);
-        for (size_t k = 0; k < n; ++k) {
-            extras->nTri[k] = B.prob[k].nTri;
-            extras->nFree[k] = B.prob[k].nFree;
-            extras->iters[k] = res[k].iters;
-            extras->trials[k] = res[k].trials;
-            extras->cycles[k] = res[k].cycles;
+        for (size_t k = p0; k < p1; ++k) {
+            extras->cand[k - p0] = B.tag[k].cand;
+            extras->nTri[k - p0] = B.prob[k].nTri;
+            extras->nFree[k - p0] = B.prob[k].nFree;
+            extras->iters[k - p0] = res[k].iters;
+            extras->trials[k - p0] = res[k].trials;
+            extras->cycles[k - p0] = res[k].cycles;
         }
     }
-    // per candidate: the best of its local problems (strict >, first wins)
-    for (size_t k = 0; k < B.prob.size(); ++k) {
+    for (size_t k = p0; k < p1; ++k) {
         if (!solved[k]) continue;
         const LocalResult& r = res[k];
         const Batch::Tag& tg = B.tag[k];
@@ -1247,7 +1173,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
         if (opType == kOpMerge) {
             const double SDInc = -SDDec;
             EwDec = lambda_t * tg.se - (1.0 - lambda_t) * SDInc;   // TriMesh.cpp:2157
-            if (extras) extras->ewExact[k] = EwDec;
+            if (extras) extras->ewExact[k - p0] = EwDec;
             C.ec0 = SDInc;
             C.ec1 = -tg.se;
             C.EwDec = EwDec;
@@ -1255,7 +1181,7 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
             continue;
         }
         EwDec = (1.0 - lambda_t) * SDDec - lambda_t * tg.se;   // TriMesh.cpp:2187, 2248
-        if (extras) extras->ewExact[k] = opType == kOpInteriorSplit ? 0.5 * EwDec : EwDec;
+        if (extras) extras->ewExact[k - p0] = opType == kOpInteriorSplit ? 0.5 * EwDec : EwDec;
         if (EwDec > C.EwDec) {
             C.EwDec = EwDec;
             C.ec0 = -SDDec;
@@ -1274,6 +1200,152 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
             if (C.EwDec != -DBL_MAX) C.EwDec *= 0.5;
     for (size_t c = 0; c < out.size(); ++c)
         if (best < 0 || out[c].EwDec > out[best].EwDec) best = static_cast<int>(c);
+}
+
+} // namespace
+
+int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambda_t, double filterExp,
+                   const TopoOptions& opts, TopoOpResult* results, std::string* err)
+{
+    using clk = std::chrono::steady_clock;
+    if (!in.F || !in.Vrest || !in.UV || !in.rest || !in.dm || in.nV <= 0 || in.nF <= 0 || nOps <= 0 || !ops ||
+        !results) {
+        if (err) *err = "topology query: bad arguments";
+        return OC_ERR_INVALID;
+    }
+    for (int i = 0; i < nOps; ++i) results[i] = TopoOpResult{};
+    Topo ownT;
+    if (!in.adj) ownT.build(in.nV, in.F, in.nF);
+    const Topo& T = in.adj ? in.adj->T : ownT;
+    if (T.nV != in.nV || T.nF != in.nF || T.F != in.F) {
+        if (err) *err = "topology query: adjacency of another mesh";
+        return OC_ERR_INVALID;
+    }
+    // every operation's problems in one batch, op i owning [start[i], start[i + 1])
+    Batch B;
+    std::vector<size_t> start(nOps + 1, 0);
+    std::vector<int> opOf;
+    for (int i = 0; i < nOps; ++i) {
+        const auto t0 = clk::now();
+        Batch Bi;
+        const int rc = build_op(in, T, ops[i], filterExp, results[i].cands, results[i].pool, Bi, err);
+        if (rc) return rc;
+        append_batch(B, Bi);
+        start[i + 1] = B.prob.size();
+        opOf.insert(opOf.end(), Bi.prob.size(), ops[i]);
+        results[i].stats.nCandidates = static_cast<int>(results[i].cands.size());
+        results[i].stats.nProblems = static_cast<int>(Bi.prob.size());
+        results[i].stats.buildMs = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    }
+    const auto t1 = clk::now();
+    // one batched device solve of all problems (exhaustive), or the learned
+    // proposal: a one-step pass over all problems gives their features, the
+    // MLP ranks each operation's problems and only the top fraction of each
+    // gets the full solve
+    const size_t n = B.prob.size();
+    std::vector<LocalResult> res(n);
+    std::vector<char> solved(n, 1);
+    const unsigned long long batchId = in.ws ? in.ws->nextBatch++ : 0;
+    const bool learned = (opts.flags & kTopoLearned) && opts.mlp;
+    const int fp32 = opts.flags & kTopoFp32Hessian;
+    double probeMs = 0.0, exactMs = 0.0;
+    if (n) {
+        std::string e2;
+        std::vector<int> all(n);
+        for (size_t k = 0; k < n; ++k) all[k] = static_cast<int>(k);
+        if (learned) {
+            int rc = solve_batch(in, B, batchId, all, 1, fp32, res, &e2);
+            if (rc) { if (err) *err = e2; return rc; }
+            const auto tA = clk::now();
+            probeMs = std::chrono::duration<double, std::milli>(tA - t1).count();
+            // features -> predicted fraction of excess energy removed -> E_w decrease
+            std::vector<float> X(n * kTopoNumFeatures), r(n);
+            for (size_t k = 0; k < n; ++k) topo_features(B.prob[k], res[k], opOf[k], in, &X[k * kTopoNumFeatures]);
+            rc = mlp_predict_host(*opts.mlp, X.data(), static_cast<int>(n), r.data());
+            if (rc) { if (err) *err = "topology query: MLP inference failed"; return rc; }
+            std::fill(solved.begin(), solved.end(), 0);
+            std::vector<int> sel;
+            for (int i = 0; i < nOps; ++i) {
+                const int op = ops[i];
+                const int ni = static_cast<int>(start[i + 1] - start[i]);
+                if (!ni) continue;
+                std::vector<std::pair<double, int>> pred(ni);
+                for (int j = 0; j < ni; ++j) {
+                    const size_t k = start[i] + j;
+                    const double sdd = static_cast<double>(r[k]) * excess_global(B.prob[k], res[k], in.surfaceArea);
+                    const double ew = op == kOpMerge ? lambda_t * B.tag[k].se + (1.0 - lambda_t) * sdd
+                                                     : (1.0 - lambda_t) * sdd - lambda_t * B.tag[k].se;
+                    pred[j] = {-ew, j};
+                }
+                TopoExtras& ex = results[i].extras;
+                ex.ewPred.resize(ni);
+                for (int j = 0; j < ni; ++j) ex.ewPred[j] = -pred[j].first * (op == kOpInteriorSplit ? 0.5 : 1.0);
+                std::stable_sort(pred.begin(), pred.end());
+                int kTop = static_cast<int>(std::ceil(opts.topFrac * ni));
+                kTop = std::max(1, std::min(ni, kTop));
+                for (int q = 0; q < kTop; ++q) {
+                    solved[start[i] + pred[q].second] = 1;
+                    sel.push_back(static_cast<int>(start[i] + pred[q].second));
+                }
+                results[i].stats.nSelected = kTop;
+                ex.X.assign(X.begin() + start[i] * kTopoNumFeatures, X.begin() + start[i + 1] * kTopoNumFeatures);
+                ex.predicted.assign(r.begin() + start[i], r.begin() + start[i + 1]);
+            }
+            std::sort(sel.begin(), sel.end());
+            std::vector<LocalResult> full(n);
+            const auto tB = clk::now();
+            rc = solve_batch(in, B, batchId, sel, -1, fp32, full, &e2);
+            if (rc) { if (err) *err = e2; return rc; }
+            for (int k : sel) res[k] = full[k];
+            exactMs = std::chrono::duration<double, std::milli>(clk::now() - tB).count();
+        }
+        else {
+            const int rc = solve_batch(in, B, batchId, all, -1, fp32, res, &e2);
+            if (rc) { if (err) *err = e2; return rc; }
+            for (int i = 0; i < nOps; ++i) {
+                results[i].stats.nSelected = static_cast<int>(start[i + 1] - start[i]);
+                if (!(opts.flags & kTopoRecordFeatures)) continue;
+                TopoExtras& ex = results[i].extras;
+                const size_t ni = start[i + 1] - start[i];
+                ex.X.assign(ni * kTopoNumFeatures, 0.0f);
+                ex.target.assign(ni, 0.0f);
+                for (size_t j = 0; j < ni; ++j) {
+                    const size_t k = start[i] + j;
+                    topo_features(B.prob[k], res[k], ops[i], in, &ex.X[j * kTopoNumFeatures]);
+                    const double xs = excess_global(B.prob[k], res[k], in.surfaceArea);
+                    const double t = xs > 0.0 ? res[k].eDec / xs : 0.0;
+                    ex.target[j] = static_cast<float>(std::max(-1.0, std::min(1.0, t)));
+                }
+            }
+        }
+    }
+    const double solveMs = std::chrono::duration<double, std::milli>(clk::now() - t1).count();
+    for (int i = 0; i < nOps; ++i) {
+        TopoOpResult& R = results[i];
+        R.stats.solveMs = solveMs;   // shared by the operations solved together
+        R.stats.probeMs = probeMs;
+        R.stats.exactMs = exactMs;
+        finish_op(ops[i], lambda_t, B, start[i], start[i + 1], res, solved, R.cands, R.best, R.stats, &R.extras);
+    }
+    return OC_OK;
+}
+
+int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filterExp, const TopoOptions& opts,
+               std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err,
+               TopoExtras* extras)
+{
+    out.clear();
+    best = -1;
+    candidatePool = 0;
+    stats = TopoStats{};
+    TopoOpResult r;
+    const int rc = topo_query_ops(in, &opType, 1, lambda_t, filterExp, opts, &r, err);
+    if (rc) return rc;
+    out.swap(r.cands);
+    best = r.best;
+    candidatePool = r.pool;
+    stats = r.stats;
+    if (extras) *extras = std::move(r.extras);
     return OC_OK;
 }
 

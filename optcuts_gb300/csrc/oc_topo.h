@@ -101,6 +101,22 @@ int topo_query(const TopoQueryIn& in, int opType, double lambda_t, double filter
                std::vector<TopoCandidate>& out, int& best, int& candidatePool, TopoStats& stats, std::string* err,
                TopoExtras* extras = nullptr);
 
+// One query's outputs (topo_query's, together)
+struct TopoOpResult {
+    std::vector<TopoCandidate> cands;
+    int best = -1, pool = 0;
+    TopoStats stats;
+    TopoExtras extras;
+};
+
+// Several queries of one state at once (a topology step: boundary split,
+// merge, interior split): their local problems built on host threads and
+// solved in the same launches (probe and exact passes of the learned
+// proposal shared), so the few large fans of one operation overlap the many
+// small problems of another.  The result of each equals its topo_query.
+int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambda_t, double filterExp,
+                   const TopoOptions& opts, TopoOpResult* results, std::string* err);
+
 // MLP inference on host rows (oc_mlp.cu)
 int mlp_predict_host(Mlp& m, const float* X, int n, float* y);
 

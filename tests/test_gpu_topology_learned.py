@@ -140,3 +140,30 @@ def test_learned_proposal_gain(golden):
                 rt = np.corrcoef(rank(pt), rank(tgt))[0, 1]
                 ru = np.corrcoef(rank(pu), rank(tgt))[0, 1]
                 assert rt > 0.5 and rt > ru + 0.1, (held, name, rt, ru)
+
+
+@pytest.mark.parametrize("case", TOPO_CASES)
+def test_topology_step_equals_separate_queries(golden, case):
+    """The three queries of a step built and solved together give each
+    query's own result (the local solves depend only on their own problem;
+    schedules may differ, so to rounding), exhaustive and learned."""
+    g = golden(case)
+    lam = g["topo_best"][3]
+    m = topo_mesh(g)
+    sep = [query(m, op, lam, features=True) for op in (oc.OP_BOUNDARY_SPLIT, oc.OP_MERGE, oc.OP_INTERIOR_SPLIT)]
+    step = m.topologyStep(lam, features=True)
+    for a, b in zip(sep, step):
+        assert len(a["candidates"]) == len(b["candidates"])
+        assert a["best"] == b["best"]
+        for ca, cb in zip(a["candidates"], b["candidates"]):
+            assert ca["path"] == cb["path"]
+            assert ca["EwDec"] == pytest.approx(cb["EwDec"], rel=1e-9, abs=1e-14)
+        np.testing.assert_allclose(a["features"], b["features"], rtol=1e-6, atol=1e-7)
+    mlp = oc.MLP(32, 128, seed=3)
+    full = m.topologyStep(lam, mlp=mlp, topFrac=1.0)
+    for a, b in zip(step, full):
+        assert [c["EwDec"] for c in a["candidates"]] == [c["EwDec"] for c in b["candidates"]]
+    part = m.topologyStep(lam, mlp=mlp, topFrac=0.2)
+    for a, b in zip(sep, part):
+        if a["local_problems"]:
+            assert b["selected"] == max(1, int(np.ceil(0.2 * a["local_problems"])))
