@@ -7,6 +7,9 @@ Restates the "no input UV" initialisation of the reference's src/main.cpp
 * a closed genus-0 single-component mesh: one-point cut at the first
   vertex of the first triangle (TriMesh::onePointCut, TriMesh.cpp:1054-1074,
   through the interior branch of TriMesh::cutPath, TriMesh.cpp:1449-1500);
+* a single component of genus >= 1: the reference's cut_to_disk loop
+  (main.cpp:1397-1484, cut_to_disk below, TriMesh::cutPath through the
+  library's topology operations);
 * a topological disk: no cut.
 
 then the boundary loop (igl::boundary_loop: smallest boundary vertex first,
@@ -17,7 +20,8 @@ The result is the TriMesh the reference builds with
 ``TriMesh(V, F, UV_Tutte, F_cut, false)`` (main.cpp:1534, TriMesh.cpp:122-189):
 the rest positions are re-indexed to the cut mesh and vertex 0 is fixed.
 
-High-genus meshes (igl::cut_to_disk) are not handled here.
+Several components (the reference's grid layout of their UV disks) are not
+handled here.
 """
 from __future__ import annotations
 
@@ -129,6 +133,239 @@ def one_point_cut(V, F):
     return V2, F, path
 
 
+def cut_to_disk(F):
+    """The cut graph the reference's initialisation asks for on a surface of
+    genus >= 1 (igl::cut_to_disk as vendored in src/Utils/cut_to_disk.cpp):
+
+    1. edges numbered in (min, max) vertex order; faces are peeled from each
+       not yet deleted face outwards, a face being deleted through an
+       interior edge with exactly one deleted neighbour (a breadth-first
+       queue of such edges);
+    2. the edges left form a graph whose degree-1 vertices are pruned
+       repeatedly (a queue, vertices in index order);
+    3. the remaining edges are walked into cycles (a walk that meets its own
+       vertex again: the cut is the loop from that vertex, closed) or, after
+       a dead end and a walk the other way from the reversed list, chains.
+
+    Returns the cuts as vertex lists (a closed loop repeats its first
+    vertex).  Step 3 keeps the source's vertex-position map across the
+    reversal, so a cycle found on the second walk is read from the reversed
+    list with the first walk's positions; the same happens here."""
+    F = np.asarray(F)
+    nf = len(F)
+    if nf == 0:
+        return []
+    edges = {}
+    for i in range(nf):
+        for j in range(3):
+            v0, v1 = int(F[i, j]), int(F[i, (j + 1) % 3])
+            edges.setdefault((min(v0, v1), max(v0, v1)), []).append(i)
+    keys = sorted(edges)
+    eidx = {k: n for n, k in enumerate(keys)}
+    ev = [k for k in keys]
+    ef = [(edges[k][0], edges[k][1] if len(edges[k]) > 1 else -1) for k in keys]
+    bnd_e = {n for n, k in enumerate(keys) if len(edges[k]) == 1}
+    fe = [[eidx[(min(int(F[i, j]), int(F[i, (j + 1) % 3])), max(int(F[i, j]), int(F[i, (j + 1) % 3])))]
+           for j in range(3)] for i in range(nf)]
+    deleted = [False] * nf
+    deleted_e = set()
+
+    def n_deleted(e):
+        return int(deleted[ef[e][0]]) + int(deleted[ef[e][1]])
+
+    from collections import deque
+    for face in range(nf):
+        if deleted[face]:
+            continue
+        deleted[face] = True
+        q = deque(e for e in fe[face] if e not in bnd_e and n_deleted(e) == 1)
+        while q:
+            e = q.popleft()
+            todel = nf
+            if not deleted[ef[e][0]]:
+                todel = ef[e][0]
+            if not deleted[ef[e][1]]:
+                todel = ef[e][1]
+            if todel != nf:
+                deleted_e.add(e)
+                deleted[todel] = True
+                q.extend(e2 for e2 in fe[todel] if e2 not in bnd_e and n_deleted(e2) == 1)
+    left = [e for e in range(len(keys)) if e not in deleted_e]
+    # prune spines
+    deleted_e = set()
+    vert_edges = {}
+    for e in left:
+        vert_edges.setdefault(ev[e][0], []).append(e)
+        vert_edges.setdefault(ev[e][1], []).append(e)
+    nbs = {v: len(es) for v, es in vert_edges.items()}
+    q = deque(v for v in sorted(vert_edges) if len(vert_edges[v]) == 1)
+    while q:
+        v = q.popleft()
+        for e in vert_edges[v]:
+            if e in deleted_e:
+                continue
+            deleted_e.add(e)
+            for w in ev[e]:
+                nbs[w] -= 1
+                if nbs[w] == 1:
+                    q.append(w)
+    loop = [e for e in left if e not in deleted_e]
+    if not loop:
+        return []
+    loop_vert_edges = {}
+    for e in loop:
+        loop_vert_edges.setdefault(ev[e][0], []).append(e)
+        loop_vert_edges.setdefault(ev[e][1], []).append(e)
+    used = set()
+    cuts = []
+
+    def walk(verts, edges_, pos, cur, cure):
+        """Extends verts / edges_ from cur; returns True when a cycle closes."""
+        while cur != -1:
+            nxt, nxe = -1, -1
+            for c in loop_vert_edges.get(cur, []):
+                if c not in used and c != cure:
+                    nxt = ev[c][1] if cur == ev[c][0] else ev[c][0]
+                    nxe = c
+                    break
+            if nxt != -1:
+                if nxt in pos:
+                    i0 = pos[nxt]
+                    cuts.append(verts[i0:] + [nxt])
+                    used.update(edges_[i0:])
+                    used.add(nxe)
+                    return True
+                pos[nxt] = len(verts)
+                verts.append(nxt)
+                edges_.append(nxe)
+            cur, cure = nxt, nxe
+        return False
+
+    for e in loop:
+        while e not in used:
+            verts = [ev[e][0], ev[e][1]]
+            edges_ = [e]
+            pos = {verts[0]: 0, verts[1]: 1}
+            if walk(verts, edges_, pos, ev[e][1], e):
+                continue
+            verts.reverse()
+            edges_.reverse()
+            if walk(verts, edges_, pos, verts[-1], edges_[-1]):
+                continue
+            cuts.append(list(verts))
+            used.update(edges_)
+    return cuts
+
+
+class _Incidence:
+    """Faces around each vertex, kept up to date across topology operations
+    (they change a few faces' vertex ids and append vertices): whether an
+    edge is interior and whether a vertex is on the boundary
+    (TriMesh::isBoundaryVert) without rescanning the mesh."""
+
+    def __init__(self, F):
+        self.F = np.asarray(F, np.int32)
+        self.inc = {}
+        for t, row in enumerate(self.F.tolist()):
+            for v in row:
+                self.inc.setdefault(v, set()).add(t)
+
+    def update(self, F_new):
+        F_new = np.asarray(F_new, np.int32)
+        for t in np.nonzero(np.any(F_new != self.F, axis=1))[0].tolist():
+            for v in self.F[t].tolist():
+                self.inc[v].discard(t)
+            for v in F_new[t].tolist():
+                self.inc.setdefault(v, set()).add(t)
+        self.F = F_new
+
+    def _around(self, v):
+        nxt, prv = [], []
+        for t in self.inc.get(v, ()):
+            r = self.F[t].tolist()
+            k = r.index(v)
+            nxt.append(r[(k + 1) % 3])
+            prv.append(r[(k + 2) % 3])
+        return nxt, prv
+
+    def boundary(self, v):
+        nxt, prv = self._around(v)
+        return sorted(nxt) != sorted(prv)
+
+    def interior_edge(self, a, b):
+        nxt, prv = self._around(a)
+        return b in nxt and b in prv
+
+
+def cut_path(path, V_rest, UV, F, cohE):
+    """TriMesh::cutPath(path, makeCoh = true) (TriMesh.cpp:1393-1517) as the
+    initialisation calls it: from a boundary end, every interior edge of the
+    path split on the boundary in turn (cut through where both of its ends
+    are on the boundary); for an interior path, the interior cut of its
+    first three vertices, then its remaining edges split on the boundary.
+    The operations are the library's (topology_apply).  Returns the new
+    arrays and the number of edges split."""
+    from optcuts_gb300 import OP_BOUNDARY_SPLIT, OP_INTERIOR_SPLIT, topology_apply
+    path = [int(v) for v in path]
+    made = 0
+    inc = _Incidence(F)
+
+    def split_edges(vs, V_rest, UV, F, cohE, made):
+        for a, b in zip(vs[:-1], vs[1:]):
+            if not inc.interior_edge(a, b):
+                continue
+            rows = 4 if (inc.boundary(a) and inc.boundary(b)) else 2
+            V_rest, UV, F, cohE = topology_apply(OP_BOUNDARY_SPLIT, [a, b], np.repeat(UV[[a]], rows, axis=0),
+                                                 V_rest, UV, F, cohE)
+            inc.update(F)
+            made += 1
+        return V_rest, UV, F, cohE, made
+
+    if inc.boundary(path[0]) or inc.boundary(path[-1]):
+        if not inc.boundary(path[0]):
+            path = path[::-1]   # always start the cut from the boundary
+        return split_edges(path, V_rest, UV, F, cohE, made)
+    if len(path) < 3:
+        raise ValueError("an interior cut path needs three vertices")
+    V_rest, UV, F, cohE = topology_apply(OP_INTERIOR_SPLIT, path[:3], np.repeat(UV[[path[1]]], 2, axis=0),
+                                         V_rest, UV, F, cohE)
+    inc.update(F)
+    return split_edges(path[2:], V_rest, UV, F, cohE, made)
+
+
+def cut_high_genus(V, F):
+    """The reference's initial cutting of one component of genus >= 1
+    (main.cpp:1397-1484): cut_to_disk on the current mesh, then the first of
+    its seams that cuts anything (a closed loop first through the interior
+    cut of its last three vertices, then the rest of it), repeated until the
+    component is a disk.  Returns (V_rest, F) of the cut mesh."""
+    V_rest = np.asarray(V, np.float64)
+    F = np.asarray(F, np.int32)
+    UV = np.zeros((len(V_rest), 2))
+    cohE = np.zeros((0, 4), np.int32)
+    for _ in range(10000):
+        ec = euler_characteristic(V_rest, F)
+        if ec == 1:
+            return V_rest, F
+        if ec > 1:
+            raise NotImplementedError("a component turned closed genus 0 while being cut")
+        made = 0
+        for seam in cut_to_disk(F):
+            seam = list(seam)
+            if seam[0] == seam[-1]:
+                # (an interior cut of three vertices counts no split, as in cutPath)
+                V_rest, UV, F, cohE, m = cut_path(seam[-3:], V_rest, UV, F, cohE)
+                made += m
+                seam = seam[:-2]
+            V_rest, UV, F, cohE, m = cut_path(seam, V_rest, UV, F, cohE)
+            made += m
+            if made:
+                break
+        if not made:
+            raise ValueError("no cut made while cutting to a disk")
+    raise ValueError("cutting to a disk did not finish")
+
+
 def boundary_loop(F):
     """igl::boundary_loop for a single-boundary manifold: start at the
     smallest boundary vertex, follow the boundary half-edges."""
@@ -190,8 +427,11 @@ def init_uv(V, F):
     path = None
     if ec == 2:
         V, F, path = one_point_cut(V, F)
+    elif ec < 1:
+        V, F = cut_high_genus(V, F)
+        path = []
     elif ec != 1:
-        raise NotImplementedError("only closed genus-0 meshes and disks are initialised here")
+        raise NotImplementedError("only single-component meshes are initialised here")
     bnd = boundary_loop(F)
     if not bnd:
         raise ValueError("mesh has no boundary after the cut")

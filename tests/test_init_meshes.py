@@ -8,21 +8,40 @@ from optcuts_gb300 import meshes as M
 
 
 @pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle",
-                                  "sheet_3k"])
+                                  "sheet_3k", "torus_768"])
 def test_init_matches_reference(golden, case):
+    """The cut mesh (one-point cut for genus 0; for the genus-1 torus the
+    reference's cut_to_disk loop), its boundary loop and cohesive edges, and
+    the Tutte embedding, against the reference's own initial state."""
     g = golden(case)
     st = I.init_uv(g["mesh_V"], g["mesh_F"])
     np.testing.assert_array_equal(st.F, g["F"])
     np.testing.assert_array_equal(st.V_rest, g["V_rest"])
     np.testing.assert_array_equal(st.bnd, g["bnd"])
+    np.testing.assert_array_equal(st.cohE, g["cohE"].reshape(-1, 4))
     # the harmonic solve differs (SuperLU here, Eigen in the reference)
     assert np.abs(st.UV - g["UV0"]).max() < 1e-10
 
 
-def test_high_genus_not_handled():
+def test_cut_to_disk_on_a_torus():
+    """A closed torus (Euler characteristic 0): the cut graph holds two
+    loops through a common vertex; cutting along them leaves a disk."""
     V, F = M.CONFIGS["torus_768"]()
-    with pytest.raises(NotImplementedError):
-        I.init_uv(V, F)
+    cuts = I.cut_to_disk(F)
+    assert len(cuts) >= 2 and all(len(c) >= 3 for c in cuts)
+    Vc, Fc = I.cut_high_genus(V, F)
+    assert I.euler_characteristic(Vc, Fc) == 1 and len(I.boundary_loop(Fc)) > 0
+
+
+def test_torus_41k_initialises():
+    """The genus-1 41k-triangle torus (the plain-method configuration) gets
+    a valid start: a disk whose Tutte map inverts no triangle."""
+    V, F = M.CONFIGS["torus_41k"]()
+    st = I.init_uv(V, F)
+    assert I.euler_characteristic(st.V_rest, st.F) == 1
+    U = st.UV[st.F]
+    det = (U[:, 1, 0] - U[:, 0, 0]) * (U[:, 2, 1] - U[:, 0, 1]) - (U[:, 1, 1] - U[:, 0, 1]) * (U[:, 2, 0] - U[:, 0, 0])
+    assert (det > 0).all()
 
 
 @pytest.mark.parametrize("key,nf", [("icosphere_5k", 5120), ("torus_41k", 40960), ("ellipsoid_199k", 199080)])
