@@ -399,6 +399,7 @@ def run_ours(args, rank, world):
             ctx.synchronize()
             topo["apply"] = {"value": time.perf_counter() - t0, "unit": "s",
                              "op": {0: "boundary_split", 1: "interior_split", 2: "merge"}[op], "EwDec": ew,
+                             "phases_ms": {k: round(v, 2) for k, v in opt.applyTiming().items()},
                              "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and "
                                      "analysis, scaffold, energy"}
 

@@ -80,6 +80,27 @@ int oc_sd_gradient(oc_mesh* mesh, int uniformWeight, double* gradient);
  * row-major 6x6 in local order (u1,v1,u2,v2,u3,v3), before fixed-vertex
  * removal and before energyParams scaling. */
 int oc_sd_hessian_blocks(oc_mesh* mesh, int uniformWeight, double* blocks);
+/* The PSD projection of the element Hessians:
+ *   OC_HESSIAN_REDUCED  H = Q K Q^T with K = Q^T H Q over the 4-dimensional
+ *                       complement of the two translations (Q orthonormal),
+ *                       K clamped by a 4x4 cyclic Jacobi: the same projection
+ *                       as the 6x6 eigen-clamp up to rounding (about 1e-15 of
+ *                       each block's largest entry), at a fifth of its FP64
+ *                       arithmetic
+ *   OC_HESSIAN_JACOBI6  the 6x6 cyclic Jacobi eigen-clamp without FMA
+ *                       contraction (rounds as the oracle restatement does);
+ *                       the optimizer's default and oc_sd_hessian_blocks's
+ *                       form
+ *   OC_HESSIAN_HYBRID   the 4x4 form for elements whose energy density is at
+ *                       most 1e3, the 6x6 form for the rest
+ * The 6x6 form keeps each element's rounding-level translation components;
+ * for the stiff elements of a Tutte start (entries up to ~1e26) they change
+ * the Newton direction, and Newton runs with the 4x4 form everywhere
+ * converge far more slowly from such starts.  Where no element is stiff the
+ * three forms agree to rounding. */
+enum { OC_HESSIAN_REDUCED = 0, OC_HESSIAN_JACOBI6 = 1, OC_HESSIAN_HYBRID = 2 };
+/* oc_sd_hessian_blocks with the projection chosen */
+int oc_sd_hessian_blocks_projected(oc_mesh* mesh, int uniformWeight, int projection, double* blocks);
 /* SymDirichletEnergy::initStepSize (SymDirichletEnergy.cpp:551-610): lowers
  * *stepSize in place to the largest inversion-free step along searchDir. */
 int oc_sd_init_step_size(oc_mesh* mesh, const double* searchDir, double* stepSize);
@@ -170,6 +191,8 @@ typedef struct {
                              air mesh keeps the analysis; 1: always the exact
                              pattern (analysed again when the air mesh's
                              connectivity changes) */
+    int hessianProjection; /* OC_HESSIAN_JACOBI6 (default), OC_HESSIAN_REDUCED or
+                              OC_HESSIAN_HYBRID */
 } oc_optimizer_config;
 
 int oc_optimizer_default_config(oc_optimizer_config* cfg);
@@ -370,6 +393,10 @@ int oc_optimizer_split_or_merge(oc_optimizer* opt, double EDecThres, int splitIn
  * the energy.  path / newVertPos as a query candidate reports them. */
 int oc_optimizer_create_fracture(oc_optimizer* opt, int opType, const int* path, int pathLen,
                                  const double* newVertPos, int posRows);
+/* durations (ms) of the last oc_optimizer_create_fracture's phases: host mesh
+ * edit, device mesh rebuild, scaffold rebuild, Newton pattern and symbolic
+ * analysis (host), their device allocation and upload, energy evaluation */
+int oc_optimizer_apply_timing(oc_optimizer* opt, double* out6);
 /* the same operation on a mesh alone */
 int oc_mesh_apply_topology(oc_mesh* mesh, int opType, const int* path, int pathLen, const double* newVertPos,
                            int posRows);

@@ -46,11 +46,12 @@ _vp = ctypes.c_void_p
 class OptimizerConfig(ctypes.Structure):
     _fields_ = [("pcgTol", ctypes.c_double), ("pcgMaxIter", ctypes.c_int), ("relGL2Tol", ctypes.c_double),
                 ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int), ("linearSolver", ctypes.c_int),
-                ("scaffoldPattern", ctypes.c_int)]
+                ("scaffoldPattern", ctypes.c_int), ("hessianProjection", ctypes.c_int)]
 
 
 SOLVER_DIRECT = 0
 SOLVER_PCG = 1
+HESSIAN_REDUCED, HESSIAN_JACOBI6, HESSIAN_HYBRID = 0, 1, 2
 OP_BOUNDARY_SPLIT, OP_INTERIOR_SPLIT, OP_MERGE = 0, 1, 2
 
 
@@ -69,6 +70,7 @@ _SIGS = {
     "oc_sd_energy_per_elem": [_vp, ctypes.c_int, _d],
     "oc_sd_gradient": [_vp, ctypes.c_int, _d],
     "oc_sd_hessian_blocks": [_vp, ctypes.c_int, _d],
+    "oc_sd_hessian_blocks_projected": [_vp, ctypes.c_int, ctypes.c_int, _d],
     "oc_sd_init_step_size": [_vp, _d, _d],
     "oc_linsys_create": [_vp, ctypes.POINTER(_vp)],
     "oc_linsys_destroy": [_vp],
@@ -110,6 +112,7 @@ _SIGS = {
     "oc_topo_result_destroy": [_vp],
     "oc_topo_result_iterations": [_vp, _i, _i, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_create_fracture": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
+    "oc_optimizer_apply_timing": [_vp, _d],
     "oc_optimizer_split_or_merge": [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int, _vp,
                                     ctypes.c_double, _i, _i, _d],
     "oc_mesh_apply_topology": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
@@ -443,10 +446,15 @@ class SymDirichletEnergy:
         data.ctx.check(lib().oc_sd_gradient(data.h, int(uniformWeight), _pd(g)), "computeGradient")
         return g
 
-    def computeHessian(self, data, uniformWeight=False):
-        """Per-triangle PSD-projected 6x6 blocks, shape (nF, 6, 6)."""
+    def computeHessian(self, data, uniformWeight=False, projection=HESSIAN_JACOBI6):
+        """Per-triangle PSD-projected 6x6 blocks, shape (nF, 6, 6).
+        projection: HESSIAN_JACOBI6 (the 6x6 eigen-clamp, the optimizer's
+        default), HESSIAN_REDUCED (the same projection over the
+        translation-free 4x4 form) or HESSIAN_HYBRID (4x4 where the element's
+        energy density is at most 1e3)."""
         out = np.empty((data.nF, 6, 6))
-        data.ctx.check(lib().oc_sd_hessian_blocks(data.h, int(uniformWeight), _pd(out)), "computeHessian")
+        data.ctx.check(lib().oc_sd_hessian_blocks_projected(data.h, int(uniformWeight), int(projection), _pd(out)),
+                       "computeHessian")
         return out
 
     def initStepSize(self, data, searchDir, stepSize=1.0):
@@ -748,6 +756,15 @@ class Optimizer:
         self.ctx.check(lib().oc_optimizer_create_fracture(self.h, op, _pi(path), len(path), _pd(pos), len(pos)),
                        "createFracture")
         self.data._sync_topology()
+
+    def applyTiming(self):
+        """Phase durations (ms) of the last createFracture: mesh edit, device
+        mesh, scaffold, pattern + symbolic analysis (host), their device
+        allocation and upload, energy."""
+        out = np.zeros(6)
+        self.ctx.check(lib().oc_optimizer_apply_timing(self.h, _pd(out)), "applyTiming")
+        keys = ["mesh_edit", "device_mesh", "scaffold", "pattern_host", "pattern_device", "energy"]
+        return dict(zip(keys, [float(x) for x in out]))
 
     def splitOrMerge(self, EDecThres, splitInterior=False, filterExp=0.6, fp32=False, mlp=None, topFrac=0.1):
         """Optimizer::createFracture(EDecThres, 0, false, splitInterior)

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -58,6 +59,8 @@ struct oc_linsys {
     bool patternSet = false;
     int kind = OC_SOLVER_DIRECT;
     oc::CholPlan chol;
+    // last set_pattern: host pattern + symbolic analysis, device allocation + upload (ms)
+    double patternHostMs = 0.0, patternDevMs = 0.0;
 };
 
 struct oc_optimizer {
@@ -76,6 +79,9 @@ struct oc_optimizer {
     int badPivots = 0;
     cudaEvent_t ev[9] = {};
     double phaseMs[7] = {0, 0, 0, 0, 0, 0, 0};
+    // last createFracture: mesh edit, device mesh, scaffold, pattern (host),
+    // pattern (device), energy (ms)
+    double applyMs[6] = {0, 0, 0, 0, 0, 0};
     // scaffold (the Optimizer's scaffolding branches): an air mesh over the
     // augmented vertex numbering [mesh vertices | air-only vertices]
     // (Scaffold::localVI2Global, Scaffold.cpp:179-184)
@@ -96,6 +102,15 @@ struct oc_optimizer {
 namespace oc {
 cudaStream_t ctx_stream(oc_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
 } // namespace oc
+
+// milliseconds since t; t moves to now
+static double ms_since(std::chrono::steady_clock::time_point& t)
+{
+    const auto n = std::chrono::steady_clock::now();
+    const double ms = std::chrono::duration<double, std::milli>(n - t).count();
+    t = n;
+    return ms;
+}
 
 namespace {
 
@@ -272,53 +287,79 @@ void build_pattern(int nV, const int* F, int nF, const std::vector<unsigned char
                    std::vector<int>& cPtr, std::vector<int>& cIdx, const int* extraF = nullptr, int nExtraF = 0,
                    const std::vector<int>* clique = nullptr)
 {
-    std::vector<std::vector<int>> nb(nV);
-    for (int v = 0; v < nV; ++v) nb[v].push_back(v);
-    auto add_tris = [&](const int* T, int n) {
+    // candidate neighbours per row (counted, then filled), then each row
+    // sorted and deduplicated on host threads and compacted
+    std::vector<int> cnt(nV + 1, 0);
+    auto count_tris = [&](const int* T, int n) {
+        for (int t = 0; t < n; ++t)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    if (a != b && !fixedMask[T[3 * t + a]] && !fixedMask[T[3 * t + b]]) cnt[T[3 * t + a] + 1]++;
+    };
+    for (int v = 0; v < nV; ++v) cnt[v + 1] = 1;   // the diagonal
+    count_tris(F, nF);
+    if (extraF) count_tris(extraF, nExtraF);
+    std::vector<int> cliqueFree;
+    if (clique)
+        for (int va : *clique)
+            if (!fixedMask[va]) cliqueFree.push_back(va);
+    for (int va : cliqueFree) cnt[va + 1] += static_cast<int>(cliqueFree.size()) - 1;
+    for (int v = 0; v < nV; ++v) cnt[v + 1] += cnt[v];
+    std::vector<int> raw(cnt[nV]);
+    std::vector<int> fillPos(cnt.begin(), cnt.end() - 1);
+    for (int v = 0; v < nV; ++v) raw[fillPos[v]++] = v;
+    auto fill_tris = [&](const int* T, int n) {
         for (int t = 0; t < n; ++t)
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) {
                     if (a == b) continue;
                     const int va = T[3 * t + a], vb = T[3 * t + b];
                     if (fixedMask[va] || fixedMask[vb]) continue;
-                    nb[va].push_back(vb);
+                    raw[fillPos[va]++] = vb;
                 }
     };
-    add_tris(F, nF);
-    if (extraF) add_tris(extraF, nExtraF);
-    if (clique)
-        for (int va : *clique) {
-            if (fixedMask[va]) continue;
-            for (int vb : *clique)
-                if (vb != va && !fixedMask[vb]) nb[va].push_back(vb);
+    fill_tris(F, nF);
+    if (extraF) fill_tris(extraF, nExtraF);
+    for (int va : cliqueFree)
+        for (int vb : cliqueFree)
+            if (vb != va) raw[fillPos[va]++] = vb;
+    std::vector<int> uniq(nV);
+    oc::host_parallel_for(nV, 4096, [&](size_t v0, size_t v1) {
+        for (size_t v = v0; v < v1; ++v) {
+            int* b = raw.data() + cnt[v];
+            int* e = raw.data() + cnt[v + 1];
+            std::sort(b, e);
+            uniq[v] = static_cast<int>(std::unique(b, e) - b);
         }
+    });
     rowPtr.assign(nV + 1, 0);
-    for (int v = 0; v < nV; ++v) {
-        std::sort(nb[v].begin(), nb[v].end());
-        nb[v].erase(std::unique(nb[v].begin(), nb[v].end()), nb[v].end());
-        rowPtr[v + 1] = rowPtr[v] + static_cast<int>(nb[v].size());
-    }
+    for (int v = 0; v < nV; ++v) rowPtr[v + 1] = rowPtr[v] + uniq[v];
     col.resize(rowPtr[nV]);
     diagSlot.resize(nV);
-    for (int v = 0; v < nV; ++v) {
-        std::copy(nb[v].begin(), nb[v].end(), col.begin() + rowPtr[v]);
-        diagSlot[v] = rowPtr[v] + static_cast<int>(std::lower_bound(nb[v].begin(), nb[v].end(), v) - nb[v].begin());
-        std::vector<int>().swap(nb[v]);
-    }
+    oc::host_parallel_for(nV, 4096, [&](size_t v0, size_t v1) {
+        for (size_t v = v0; v < v1; ++v) {
+            const int* b = raw.data() + cnt[v];
+            std::copy(b, b + uniq[v], col.begin() + rowPtr[v]);
+            diagSlot[v] = rowPtr[v] + static_cast<int>(std::lower_bound(b, b + uniq[v], (int)v) - b);
+        }
+    });
+    std::vector<int>().swap(raw);
     const int nnzb = rowPtr[nV];
     std::vector<int> slotOf(9 * (size_t)nF, -1);
+    oc::host_parallel_for(nF, 8192, [&](size_t t0, size_t t1) {
+        for (size_t t = t0; t < t1; ++t)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    const int va = F[3 * t + a], vb = F[3 * t + b];
+                    if (fixedMask[va] || fixedMask[vb]) continue;
+                    const int* lo = col.data() + rowPtr[va];
+                    const int* hi = col.data() + rowPtr[va + 1];
+                    slotOf[9 * t + 3 * a + b] = static_cast<int>(std::lower_bound(lo, hi, vb) - col.data());
+                }
+    });
     cPtr.assign(nnzb + 1, 0);
-    for (int t = 0; t < nF; ++t)
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) {
-                const int va = F[3 * t + a], vb = F[3 * t + b];
-                if (fixedMask[va] || fixedMask[vb]) continue;
-                const int* lo = col.data() + rowPtr[va];
-                const int* hi = col.data() + rowPtr[va + 1];
-                const int s = static_cast<int>(std::lower_bound(lo, hi, vb) - col.data());
-                slotOf[9 * (size_t)t + 3 * a + b] = s;
-                cPtr[s + 1]++;
-            }
+    for (size_t k = 0; k < 9 * (size_t)nF; ++k)
+        if (slotOf[k] >= 0) cPtr[slotOf[k] + 1]++;
     for (int s = 0; s < nnzb; ++s) cPtr[s + 1] += cPtr[s];
     cIdx.resize(cPtr[nnzb]);
     std::vector<int> fill(cPtr.begin(), cPtr.end() - 1);
@@ -375,8 +416,11 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
                        const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr)
 {
     oc_ctx* ctx = ls->ctx;
+    auto t = std::chrono::steady_clock::now();
     std::vector<int> cPtr, cIdx;
     build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx, extraF, nExtraF, clique);
+    ls->patternHostMs = ms_since(t);
+    ls->patternDevMs = 0.0;
     ls->rowFixed = mask;
     free_bsr(ls->b);
     oc::pcg_free(ls->wk);
@@ -414,11 +458,14 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     if (ls->kind == OC_SOLVER_DIRECT) {
         // analyze_pattern (EigenLibSolver.cpp:71-77): symbolic factorisation;
         // a clique (scaffold boundary + air vertices) is eliminated last
+        ls->patternDevMs += ms_since(t);
         oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique);
+        ls->patternHostMs += ms_since(t);
         std::string err;
         int rc = oc::chol_upload(ls->chol, &err);
         if (rc) return fail(ctx, rc, err);
     }
+    ls->patternDevMs += ms_since(t);
     return OC_OK;
 }
 
@@ -658,9 +705,14 @@ int oc_sd_gradient(oc_mesh* m, int uniformWeight, double* gradient)
 
 int oc_sd_hessian_blocks(oc_mesh* m, int uniformWeight, double* blocks)
 {
-    if (!m || !blocks) return OC_ERR_INVALID;
+    return oc_sd_hessian_blocks_projected(m, uniformWeight, OC_HESSIAN_JACOBI6, blocks);
+}
+
+int oc_sd_hessian_blocks_projected(oc_mesh* m, int uniformWeight, int projection, double* blocks)
+{
+    if (!m || !blocks || projection < OC_HESSIAN_REDUCED || projection > OC_HESSIAN_HYBRID) return OC_ERR_INVALID;
     if (!m->tmpF) OC_CUDA(m->ctx, dalloc(&m->tmpF, 36 * (size_t)m->d.nF));
-    oc::launch_hessian(m->d, uniformWeight, m->hb, m->ctx->stream);
+    oc::launch_hessian(m->d, uniformWeight, m->hb, m->ctx->stream, projection);
     oc::launch_hessian_expand(m->hb, m->d.nF, m->tmpF, m->ctx->stream);
     OC_CUDA(m->ctx, cudaGetLastError());
     OC_CUDA(m->ctx, cudaMemcpyAsync(blocks, m->tmpF, sizeof(double) * 36 * (size_t)m->d.nF, cudaMemcpyDeviceToHost,
@@ -724,9 +776,12 @@ static int mesh_rebuild(oc_mesh* m, const std::vector<double>& uvHost)
     return OC_OK;
 }
 
-int oc_mesh_apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, const double* newVertPos, int posRows)
+// host edit, then the device mesh; ms2 (optional) gets the two durations
+static int apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, const double* newVertPos, int posRows,
+                          double* ms2)
 {
     if (!m || !path || !newVertPos) return OC_ERR_INVALID;
+    auto t = std::chrono::steady_clock::now();
     std::vector<double> uv(2 * (size_t)m->d.nV);
     OC_CUDA(m->ctx, cudaMemcpyAsync(uv.data(), m->d.uv, sizeof(double2) * m->d.nV, cudaMemcpyDeviceToHost,
                                     m->ctx->stream));
@@ -739,7 +794,15 @@ int oc_mesh_apply_topology(oc_mesh* m, int opType, const int* path, int pathLen,
     m->F.swap(F);
     m->Vrest.swap(Vrest);
     m->cohE.swap(cohE);
-    return mesh_rebuild(m, uv);
+    if (ms2) ms2[0] = ms_since(t);
+    rc = mesh_rebuild(m, uv);
+    if (ms2) ms2[1] = ms_since(t);
+    return rc;
+}
+
+int oc_mesh_apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, const double* newVertPos, int posRows)
+{
+    return apply_topology(m, opType, path, pathLen, newVertPos, posRows, nullptr);
 }
 
 int oc_mesh_get_topology(oc_mesh* m, int* nV, int* nF, int* nCohE, int* F, double* Vrest, int* cohE)
@@ -1264,6 +1327,7 @@ int oc_optimizer_default_config(oc_optimizer_config* c)
     c->timing = 0;
     c->linearSolver = OC_SOLVER_DIRECT;
     c->scaffoldPattern = 0;
+    c->hessianProjection = OC_HESSIAN_JACOBI6;
     return OC_OK;
 }
 
@@ -1291,6 +1355,8 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
     if (dalloc(&o->g, nV) != cudaSuccess || dalloc(&o->dir, nV) != cudaSuccess || dalloc(&o->uv0, nV) != cudaSuccess)
         rc = fail(ctx, OC_ERR_CUDA, "optimizer alloc");
     if (o->cfg.linearSolver != OC_SOLVER_PCG) o->cfg.linearSolver = OC_SOLVER_DIRECT;
+    if (o->cfg.hessianProjection < OC_HESSIAN_REDUCED || o->cfg.hessianProjection > OC_HESSIAN_HYBRID)
+        o->cfg.hessianProjection = OC_HESSIAN_JACOBI6;
     if (rc == OC_OK) rc = oc_linsys_create(ctx, &o->ls);
     if (rc == OC_OK) rc = oc_linsys_set_type(o->ls, o->cfg.linearSolver);
     if (rc == OC_OK && o->cfg.timing)
@@ -1515,8 +1581,8 @@ static int solve_one(oc_optimizer* o, int* converged)
         return OC_OK;
     }
     // Hessian + PSD projection (computeHessian), block assembly (update_a)
-    oc::launch_hessian(md, 0, m->hb, st);
-    if (o->scaf) oc::launch_hessian(o->air, 1, o->airHb, st);
+    oc::launch_hessian(md, 0, m->hb, st, o->cfg.hessianProjection);
+    if (o->scaf) oc::launch_hessian(o->air, 1, o->airHb, st, o->cfg.hessianProjection);
     record(o, 2);
     if (o->scaf) oc::launch_assemble_scaf(o->ls->b, m->hb, m->d.nF, o->param, o->airHb, o->air.nF, o->airScale, st);
     else oc::launch_assemble(o->ls->b, m->hb, m->d.nF, o->param, st);
@@ -1829,8 +1895,10 @@ int oc_optimizer_create_fracture(oc_optimizer* o, int opType, const int* path, i
     // Optimizer::createFracture(opType, path, newVertPos, ...) (Optimizer.cpp:373-440)
     if (!o || !o->precomputed) return OC_ERR_INVALID;
     oc_mesh* m = o->mesh;
-    int rc = oc_mesh_apply_topology(m, opType, path, pathLen, newVertPos, posRows);
+    std::fill(o->applyMs, o->applyMs + 6, 0.0);
+    int rc = apply_topology(m, opType, path, pathLen, newVertPos, posRows, o->applyMs);
     if (rc) return rc;
+    auto t = std::chrono::steady_clock::now();
     const int nV = m->d.nV;
     rc = ensure_whole(o, nV);
     if (rc) return rc;
@@ -1840,11 +1908,25 @@ int oc_optimizer_create_fracture(oc_optimizer* o, int opType, const int* path, i
         rc = oc_optimizer_rebuild_scaffold(o);
         if (rc) return rc;
     }
+    o->applyMs[2] = ms_since(t);
+    o->ls->patternHostMs = o->ls->patternDevMs = 0.0;
     rc = ensure_pattern(o);   // updateEnergyData(true, false, true) (:423-425)
     if (rc) return rc;
+    ms_since(t);
+    o->applyMs[3] = o->ls->patternHostMs;
+    o->applyMs[4] = o->ls->patternDevMs;
     if (o->scaf)
         OC_CUDA(m->ctx, cudaMemcpyAsync(o->wuv, m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToDevice, m->ctx->stream));
-    return compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
+    rc = compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
+    o->applyMs[5] = ms_since(t);
+    return rc;
+}
+
+int oc_optimizer_apply_timing(oc_optimizer* o, double* out6)
+{
+    if (!o || !out6) return OC_ERR_INVALID;
+    std::copy(o->applyMs, o->applyMs + 6, out6);
+    return OC_OK;
 }
 
 int oc_optimizer_split_or_merge(oc_optimizer* o, double EDecThres, int splitInterior, double filterExp, int options,

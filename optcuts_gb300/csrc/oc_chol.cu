@@ -28,12 +28,14 @@
 #include "oc_chol.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <deque>
 #include <functional>
 #include <numeric>
+#include <thread>
 
 namespace oc {
 
@@ -45,17 +47,22 @@ struct NdNode {
     std::vector<int> children;
 };
 
-// Nested dissection of `verts` (all with tag == curTag on entry) by BFS
-// level sets from a pseudo-peripheral vertex.  Returns the node id.
-int nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::vector<int>& tag, int& tagCounter,
-             std::vector<int>& level, std::vector<NdNode>& nodes, int leafSize)
+// Nested dissection of `verts` by BFS level sets from a pseudo-peripheral
+// vertex, into `nodes` in postorder (children first, the separator last;
+// node ids local to this call's list).  Subtrees of more than kNdParallel
+// vertices are dissected on their own host threads and spliced in the same
+// order, so the result equals the sequential dissection.  tag / level are
+// shared arrays over all vertices (the subtrees' vertex sets are disjoint);
+// tags only need to be distinct, so the counter is atomic.
+constexpr size_t kNdParallel = 4096;
+
+void nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::vector<int>& tag,
+              std::atomic<int>& tagCounter, std::vector<int>& level, std::vector<NdNode>& nodes, int leafSize,
+              int depth)
 {
     const int myTag = ++tagCounter;
     for (int v : verts) tag[v] = myTag;
-    auto make_leaf = [&]() {
-        nodes.push_back(NdNode{verts, {}});
-        return static_cast<int>(nodes.size()) - 1;
-    };
+    auto make_leaf = [&]() { nodes.push_back(NdNode{verts, {}}); };
     if ((int)verts.size() <= leafSize) return make_leaf();
     // two BFS passes: the second starts at the last vertex reached by the first
     std::vector<int> q;
@@ -98,11 +105,34 @@ int nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::ve
         else sep.push_back(v);
     }
     if (sep.empty() || (left.empty() && right.empty())) return make_leaf();
+    // the two halves: each into its own node list, the larger of them on a
+    // second thread when both are big
+    std::vector<NdNode> ln, rn;
+    const bool par = depth < 6 && left.size() > kNdParallel && right.size() > kNdParallel;
+    if (par) {
+        std::thread th([&] { nd_build(rowPtr, col, right, tag, tagCounter, level, rn, leafSize, depth + 1); });
+        nd_build(rowPtr, col, left, tag, tagCounter, level, ln, leafSize, depth + 1);
+        th.join();
+    }
+    else {
+        if (!left.empty()) nd_build(rowPtr, col, left, tag, tagCounter, level, ln, leafSize, depth + 1);
+        if (!right.empty()) nd_build(rowPtr, col, right, tag, tagCounter, level, rn, leafSize, depth + 1);
+    }
+    // splice: left subtree, right subtree (ids shifted), then the separator
+    const int base = static_cast<int>(nodes.size());
     std::vector<int> kids;
-    if (!left.empty()) kids.push_back(nd_build(rowPtr, col, left, tag, tagCounter, level, nodes, leafSize));
-    if (!right.empty()) kids.push_back(nd_build(rowPtr, col, right, tag, tagCounter, level, nodes, leafSize));
+    for (auto& n : ln) {
+        for (int& c : n.children) c += base;
+        nodes.push_back(std::move(n));
+    }
+    if (!ln.empty()) kids.push_back(static_cast<int>(nodes.size()) - 1);
+    const int base2 = static_cast<int>(nodes.size());
+    for (auto& n : rn) {
+        for (int& c : n.children) c += base2;
+        nodes.push_back(std::move(n));
+    }
+    if (!rn.empty()) kids.push_back(static_cast<int>(nodes.size()) - 1);
     nodes.push_back(NdNode{std::move(sep), std::move(kids)});
-    return static_cast<int>(nodes.size()) - 1;
 }
 
 int tiles_of(int k, int m) { return (k + kTile - 1) / kTile + (m - k + kTile - 1) / kTile; }
@@ -117,7 +147,7 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     P.nDof = 2 * nV;
     std::vector<NdNode> nodes;
     std::vector<int> tag(nV, 0), level(nV, -1);
-    int tagCounter = 0;
+    std::atomic<int> tagCounter{0};
     // components: run the dissection on every connected set of vertices
     // (the forced root vertices excluded: tag 0 keeps the BFS out of them)
     std::vector<int> roots;
@@ -134,7 +164,14 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
                 for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p)
                     if (!seen[col[p]]) { seen[col[p]] = 1; comp.push_back(col[p]); }
             }
-            roots.push_back(nd_build(rowPtr, col, comp, tag, tagCounter, level, nodes, leafSize));
+            std::vector<NdNode> sub;
+            nd_build(rowPtr, col, comp, tag, tagCounter, level, sub, leafSize, 0);
+            const int base = static_cast<int>(nodes.size());
+            for (auto& n : sub) {
+                for (int& c : n.children) c += base;
+                nodes.push_back(std::move(n));
+            }
+            roots.push_back(static_cast<int>(nodes.size()) - 1);
         }
     }
     if (rootVerts && !rootVerts->empty()) nodes.push_back(NdNode{*rootVerts, roots});
@@ -159,21 +196,41 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
         P.permDof[2 * k] = 2 * P.vertOrder[k];
         P.permDof[2 * k + 1] = 2 * P.vertOrder[k] + 1;
     }
-    // boundary sets (ancestor vertices each subtree touches), bottom-up
-    std::vector<std::vector<int>> B(nF);
+    // front levels (leaves 0) and the fronts of each level
+    std::vector<int> flev(nF, 0);
+    int nLev = 0;
     for (int f = 0; f < nF; ++f) {
-        const int last = vstart[f] + static_cast<int>(nodes[f].S.size()) - 1;
-        std::vector<int> cand;
-        for (int v : nodes[f].S)
-            for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p)
-                if (pos[col[p]] > last) cand.push_back(pos[col[p]]);
-        for (int c : nodes[f].children)
-            for (int u : B[c])
-                if (u > last) cand.push_back(u);
-        std::sort(cand.begin(), cand.end());
-        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-        B[f] = std::move(cand);   // elimination positions, ascending
+        for (int c : nodes[f].children) flev[f] = std::max(flev[f], flev[c] + 1);
+        nLev = std::max(nLev, flev[f] + 1);
     }
+    std::vector<int> levOff(nLev + 1, 0), levList(nF);
+    for (int f = 0; f < nF; ++f) levOff[flev[f] + 1]++;
+    for (int l = 0; l < nLev; ++l) levOff[l + 1] += levOff[l];
+    {
+        std::vector<int> fill(levOff.begin(), levOff.end() - 1);
+        for (int f = 0; f < nF; ++f) levList[fill[flev[f]]++] = f;
+    }
+    // boundary sets (ancestor vertices each subtree touches), bottom-up: the
+    // fronts of one level are independent
+    std::vector<std::vector<int>> B(nF);
+    for (int l = 0; l < nLev; ++l)
+        host_parallel_for(levOff[l + 1] - levOff[l], 64, [&](size_t i0, size_t i1) {
+            std::vector<int> cand;
+            for (size_t i = i0; i < i1; ++i) {
+                const int f = levList[levOff[l] + i];
+                const int last = vstart[f] + static_cast<int>(nodes[f].S.size()) - 1;
+                cand.clear();
+                for (int v : nodes[f].S)
+                    for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p)
+                        if (pos[col[p]] > last) cand.push_back(pos[col[p]]);
+                for (int c : nodes[f].children)
+                    for (int u : B[c])
+                        if (u > last) cand.push_back(u);
+                std::sort(cand.begin(), cand.end());
+                cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+                B[f].assign(cand.begin(), cand.end());   // elimination positions, ascending
+            }
+        });
     // fronts
     P.fk.resize(nF); P.fm.resize(nF); P.fparent = parent; P.flevel.assign(nF, 0); P.fdofStart.resize(nF);
     P.foff.resize(nF); P.fupd.resize(nF); P.frowOff.resize(nF); P.relOff.resize(nF);
@@ -205,19 +262,32 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     for (int f = 0; f < nF; ++f)
         for (int c : nodes[f].children) P.childList.push_back(c);
     // child update row -> parent row (both row lists ascending)
+    std::atomic<int> bad{0};
     for (int f = 0; f < nF; ++f) {
         P.relOff[f] = static_cast<int>(P.relIdx.size());
-        const int pf = parent[f];
-        if (pf < 0) continue;
-        const int* prow = P.rowIdx.data() + P.frowOff[pf];
-        const int pm = P.fm[pf];
-        for (int i = P.fk[f]; i < P.fm[f]; ++i) {
-            const int dof = P.rowIdx[P.frowOff[f] + i];
-            const int* it = std::lower_bound(prow, prow + pm, dof);
-            if (it == prow + pm || *it != dof) P.valid = false;   // structure invariant violated
-            P.relIdx.push_back(it == prow + pm ? 0 : static_cast<int>(it - prow));
-        }
+        if (parent[f] >= 0) P.relIdx.resize(P.relIdx.size() + (P.fm[f] - P.fk[f]));
     }
+    host_parallel_for(nF, 256, [&](size_t f0, size_t f1) {
+        for (size_t f = f0; f < f1; ++f) {
+            const int pf = parent[f];
+            if (pf < 0) continue;
+            const int* prow = P.rowIdx.data() + P.frowOff[pf];
+            const int pm = P.fm[pf];
+            const int* it = prow;
+            int* out = P.relIdx.data() + P.relOff[f];
+            for (int i = P.fk[f]; i < P.fm[f]; ++i) {
+                const int dof = P.rowIdx[P.frowOff[f] + i];
+                it = std::lower_bound(it, prow + pm, dof);
+                if (it == prow + pm || *it != dof) {   // structure invariant violated
+                    bad = 1;
+                    *out++ = 0;
+                    it = prow;
+                    continue;
+                }
+                *out++ = static_cast<int>(it - prow);
+            }
+        }
+    });
     // levels
     for (int f = 0; f < nF; ++f) P.nLevels = std::max(P.nLevels, P.flevel[f] + 1);
     P.levelFrontOff.assign(P.nLevels + 1, 0);
@@ -228,8 +298,9 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
         std::vector<int> fill(P.levelFrontOff.begin(), P.levelFrontOff.end() - 1);
         for (int f = 0; f < nF; ++f) P.levelFronts[fill[P.flevel[f]]++] = f;
     }
-    // launch schedule: per level, extend-add per child slot, then per panel
-    // the diagonal-tile Cholesky, the panel solve and the trailing update
+    // launch schedule: per level, extend-add per child slot, the first
+    // panel's diagonal tiles, then per panel the panel solve and the trailing
+    // update (whose first block also factors the next panel's diagonal tile)
     for (int l = 0; l < P.nLevels; ++l) {
         const int* lf = P.levelFronts.data() + P.levelFrontOff[l];
         const int nl = P.levelFrontOff[l + 1] - P.levelFrontOff[l];
@@ -251,17 +322,21 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             const int cnt = static_cast<int>(P.tasks.size()) - off;
             if (cnt) P.launches.push_back({0, l, 0, off, cnt, c});
         }
+        {   // the first panel's diagonal tiles (the later ones are factored
+            // at the end of the previous panel's trailing update)
+            const int off = static_cast<int>(P.tasks.size());
+            for (int i = 0; i < nl; ++i)
+                if (P.fk[lf[i]] > 0) P.tasks.push_back(TileTask{lf[i], 0, 0, 0});
+            if ((int)P.tasks.size() > off) P.launches.push_back({4, l, 0, off, (int)P.tasks.size() - off, 0});
+        }
         for (int p = 0; p < maxPanels; ++p) {
-            // panel: every CTA factors the diagonal tile (redundantly, it is
-            // small) and solves one tile row below it; the first writes the
-            // factored diagonal tile back (task.j = 1)
+            // panel: one CTA per tile row below the factored diagonal tile
             int off = static_cast<int>(P.tasks.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
                 const int nt = tiles_of(P.fk[f], P.fm[f]);
-                if (nt == p + 1) P.tasks.push_back(TileTask{f, p, 1, p});
-                for (int ti = p + 1; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, ti == p + 1 ? 1 : 0, p});
+                for (int ti = p + 1; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, 0, p});
             }
             if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
             off = static_cast<int>(P.tasks.size());
@@ -299,24 +374,27 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     P.asmDest.assign(nnzb, -1);
     P.asmLd.assign(nnzb, 0);
     P.asmDiag.assign(nnzb, 0);
-    for (int r = 0; r < nV; ++r)
-        for (int s = rowPtr[r]; s < rowPtr[r + 1]; ++s) {
-            const int c = col[s];
-            if (pos[r] < pos[c]) continue;
-            const int f = owner[c];
-            const int m = P.fm[f];
-            const int jc = 2 * (pos[c] - vstart[f]);
-            const int* prow = P.rowIdx.data() + P.frowOff[f];
-            const int* it = std::lower_bound(prow, prow + m, 2 * pos[r]);
-            if (it == prow + m || *it != 2 * pos[r] || jc + 1 >= P.fk[f]) {
-                P.valid = false;
-                continue;
+    host_parallel_for(nV, 2048, [&](size_t r0, size_t r1) {
+        for (int r = static_cast<int>(r0); r < static_cast<int>(r1); ++r)
+            for (int s = rowPtr[r]; s < rowPtr[r + 1]; ++s) {
+                const int c = col[s];
+                if (pos[r] < pos[c]) continue;
+                const int f = owner[c];
+                const int m = P.fm[f];
+                const int jc = 2 * (pos[c] - vstart[f]);
+                const int* prow = P.rowIdx.data() + P.frowOff[f];
+                const int* it = std::lower_bound(prow, prow + m, 2 * pos[r]);
+                if (it == prow + m || *it != 2 * pos[r] || jc + 1 >= P.fk[f]) {
+                    bad = 1;
+                    continue;
+                }
+                const int ir = static_cast<int>(it - prow);
+                P.asmDest[s] = P.foff[f] + ir + (long long)jc * m;
+                P.asmLd[s] = m;
+                P.asmDiag[s] = (r == c) ? 1 : 0;
             }
-            const int ir = static_cast<int>(it - prow);
-            P.asmDest[s] = P.foff[f] + ir + (long long)jc * m;
-            P.asmLd[s] = m;
-            P.asmDiag[s] = (r == c) ? 1 : 0;
-        }
+    });
+    if (bad) P.valid = false;
 }
 
 // ------------------------------------------------------------------ kernels
@@ -372,72 +450,97 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
     }
 }
 
-// One panel step of the front factorisation, for one tile row below the
-// diagonal tile: LDL^T of the w x w diagonal tile of panel p in shared memory
-// (unit-lower L, D on the diagonal -- the factorisation SimplicialLDLT
+// LDL^T of the w x w diagonal tile at (s0, s0) of a front, in place (unit-
+// lower L below the diagonal, D on it -- the factorisation SimplicialLDLT
 // computes; negative pivots pass, a zero or non-finite one is replaced by
-// 1e-300 and counted), then L(i, p) = A(i, p) L(p, p)^-T D^-1.  Every CTA of
-// the panel factors the (small) diagonal tile itself, so the factorisation
-// and the panel solve are one launch; the CTA flagged in task.j writes the
-// factored diagonal tile back.  A panel without tile rows below gets one
-// diagonal-only task (task.i == task.p).
+// 1e-300 and counted in *flag).  Run by one warp, a row per lane, in the
+// 32 x 33 shared tile T; the same operation order as a column-by-column
+// right-looking elimination.
+__device__ void ldl_diag_tile(double* __restrict__ F, int m, int s0, int w, double (*T)[kTile + 1], int* flag)
+{
+    const int lane = threadIdx.x & 31;
+    for (int c = 0; c < w; ++c)
+        if (lane < w) T[lane][c] = lane >= c ? F[(s0 + lane) + (long long)(s0 + c) * m] : 0.0;
+    __syncwarp();
+    int nBad = 0;
+    for (int c = 0; c < w; ++c) {
+        const double dRaw = T[c][c];
+        const bool bad = !(dRaw != 0.0) || !isfinite(dRaw);
+        const double d = bad ? 1e-300 : dRaw;
+        nBad += bad;
+        const double id = 1.0 / d;
+        const double u = lane < w ? T[lane][c] * id : 0.0;   // L(lane, c) for lane > c
+        for (int c2 = c + 1; c2 < w; ++c2)
+            if (lane >= c2 && lane < w) T[lane][c2] -= u * T[c2][c];
+        __syncwarp();
+        if (lane > c && lane < w) T[lane][c] = u;
+        else if (lane == c) T[c][c] = d;
+        __syncwarp();
+    }
+    for (int c = 0; c < w; ++c)
+        if (lane < w && lane >= c) F[(s0 + lane) + (long long)(s0 + c) * m] = T[lane][c];
+    if (lane == 0 && nBad) atomicAdd(flag, nBad);
+}
+
+// The diagonal tile of every front's first panel (one warp per front of the
+// level; the later panels' tiles are factored by k_ldl_update).
+__global__ void __launch_bounds__(32) k_ldl_diag(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
+                                                 const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                 double* __restrict__ pool, int* flag)
+{
+    __shared__ double T[kTile][kTile + 1];
+    const TileTask t = tasks[blockIdx.x];
+    const int k = fk[t.front], m = fm[t.front];
+    int s0, w;
+    tile_bounds(k, m, t.p, s0, w);
+    ldl_diag_tile(pool + foff[t.front], m, s0, w, T, flag);
+}
+
+// Panel solve of one tile row below the (already factored) diagonal tile of
+// panel p: L(i, p) = A(i, p) L(p, p)^-T D^-1.  Each warp takes rows warp,
+// warp + 8, warp + 16, warp + 24 of the tile row, a column per lane, in the
+// operation order of a column-by-column substitution.
 __global__ void __launch_bounds__(256) k_ldl_panel(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
                                                    const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                   double* __restrict__ pool, int* flag)
+                                                   double* __restrict__ pool)
 {
+    static_assert(kTile == 32, "one warp lane per tile column");
     __shared__ double A[kTile][kTile + 1];
     __shared__ double X[kTile][kTile + 1];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
-    int s0, w, r0 = 0, h = 0;
+    int s0, w, r0, h;
     tile_bounds(k, m, t.p, s0, w);
-    const bool hasRow = t.i > t.p;
-    if (hasRow) tile_bounds(k, m, t.i, r0, h);
+    tile_bounds(k, m, t.i, r0, h);
     double* F = pool + foff[t.front];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the factored tile (identity beyond w) and the tile row (zero beyond h x w)
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
-        const int r = e % kTile, c = e / kTile;
-        A[r][c] = (r < w && c < w && r >= c) ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
-        X[r][c] = (hasRow && r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
+        const int r = e & (kTile - 1), c = e / kTile;
+        double a = r == c ? 1.0 : 0.0;
+        if (r < w && c < w && r >= c) a = F[(s0 + r) + (long long)(s0 + c) * m];
+        A[r][c] = a;
+        X[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
     }
     __syncthreads();
-    for (int c = 0; c < w; ++c) {
-        double d = A[c][c];
-        const bool bad = !(d != 0.0) || !isfinite(d);
-        if (bad) d = 1e-300;
-        const double id = 1.0 / d;
-        const int n = w - c - 1;
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-            const int rr = c + 1 + e % n, c2 = c + 1 + e / n;
-            if (rr >= c2) A[rr][c2] -= A[rr][c] * id * A[c2][c];
-        }
-        __syncthreads();
-        // scale column c (the next step reads only columns > c)
-        for (int rr = c + 1 + threadIdx.x; rr < w; rr += blockDim.x) A[rr][c] *= id;
-        if (threadIdx.x == 0 && bad) {
-            A[c][c] = d;
-            if (t.j) atomicAdd(flag, 1);
+    double x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[q] = X[warp + 8 * q][lane];
+    for (int c = 0; c + 1 < w; ++c) {
+        const double lc = A[lane][c];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double xc = __shfl_sync(0xffffffffu, x[q], c);
+            if (lane > c) x[q] -= xc * lc;
         }
     }
+    const double dl = A[lane][lane];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) X[warp + 8 * q][lane] = x[q] / dl;
     __syncthreads();
-    if (hasRow) {
-        for (int c = 0; c + 1 < w; ++c) {
-            const int n = w - c - 1;
-            for (int e = threadIdx.x; e < h * n; e += blockDim.x) {
-                const int r = e % h, c2 = c + 1 + e / h;
-                X[r][c2] -= X[r][c] * A[c2][c];
-            }
-            __syncthreads();
-        }
-        for (int e = threadIdx.x; e < h * w; e += blockDim.x) {
-            const int r = e % h, c = e / h;
-            F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c] / A[c][c];
-        }
-    }
-    if (t.j) {
-        for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
-            const int r = e % w, c = e / w;
-            if (r >= c) F[(s0 + r) + (long long)(s0 + c) * m] = A[r][c];
-        }
+    for (int e = threadIdx.x; e < kTile * w; e += blockDim.x) {
+        const int r = e & (kTile - 1), c = e / kTile;
+        if (r < h) F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c];
     }
 }
 
@@ -448,7 +551,7 @@ __global__ void __launch_bounds__(256) k_ldl_panel(const TileTask* __restrict__ 
 // thread's four rows (or columns) are one 32-byte read.
 __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
                                                     const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                    double* __restrict__ pool)
+                                                    double* __restrict__ pool, int* flag)
 {
     __shared__ __align__(16) double Ai[kTile][kUpd];
     __shared__ __align__(16) double Aj[kTile][kUpd];
@@ -503,6 +606,14 @@ __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__
             if (cc < hc && (!diag || r >= cc)) F[(r0 + r) + (long long)(c0 + cc) * m] -= acc[i][j];
         }
     }
+    // the next panel's diagonal tile is the corner of this front's first
+    // trailing block: once the block is updated, one warp factors it (in
+    // Ai's shared memory), so the next panel launch reads it factored
+    if (t.i == 0 && t.j == 0 && s < k) {
+        __syncthreads();
+        if (threadIdx.x < 32)
+            ldl_diag_tile(F, m, s, min(kTile, k - s), reinterpret_cast<double(*)[kTile + 1]>(&Ai[0][0]), flag);
+    }
 }
 
 __global__ void k_permute_in(const double* __restrict__ rhs, const int* __restrict__ perm, double sign, int n,
@@ -547,13 +658,21 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
         __syncthreads();
     }
     const double* L = pool + foff[f];
+    __shared__ double tile[32 * 33];   // the diagonal block, row-major (padded)
     for (int c0 = 0; c0 < k; c0 += 32) {
         const int w = min(32, k - c0);
+        // stage the diagonal block (all loads in flight at once) so that the
+        // dependent chain below reads shared memory, not global memory
+        for (int e = threadIdx.x; e < 32 * w; e += blockDim.x) {
+            const int col = e >> 5, row = e & 31;
+            if (row < w) tile[row * 33 + col] = L[(c0 + row) + (long long)(c0 + col) * m];
+        }
+        __syncthreads();
         if (warp == 0) {
             double v = lane < w ? sh[c0 + lane] : 0.0;
             for (int c = 0; c < w; ++c) {
                 const double yc = __shfl_sync(0xffffffffu, v, c);
-                if (lane > c && lane < w) v -= L[(c0 + lane) + (long long)(c0 + c) * m] * yc;
+                if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
             }
             if (lane < w) sh[c0 + lane] = v;
         }
@@ -629,6 +748,7 @@ __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, con
 {
     extern __shared__ double sh[];
     __shared__ double dots[32];
+    __shared__ double tile[32 * 33];   // the diagonal block, row-major (padded)
     const int f = fronts[blockIdx.x];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -640,6 +760,10 @@ __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, con
     const int nBlocks = (k + 31) / 32;
     for (int b = nBlocks - 1; b >= 0; --b) {
         const int c0 = 32 * b, w = min(32, k - c0);
+        for (int e = threadIdx.x; e < 32 * w; e += blockDim.x) {
+            const int col = e >> 5, row = e & 31;
+            if (row < w) tile[row * 33 + col] = L[(c0 + row) + (long long)(c0 + col) * m];
+        }
         for (int c = warp; c < w; c += nw) {
             const double* lc = L + (long long)(c0 + c) * m;
             double s = 0.0;
@@ -652,7 +776,7 @@ __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, con
             double v = lane < w ? sh[c0 + lane] - dots[lane] : 0.0;
             for (int r = w - 1; r >= 0; --r) {
                 const double xr = __shfl_sync(0xffffffffu, v, r);
-                if (lane < r) v -= L[(c0 + r) + (long long)(c0 + lane) * m] * xr;
+                if (lane < r) v -= tile[r * 33 + lane] * xr;
             }
             if (lane < w) sh[c0 + lane] = v;
         }
@@ -738,8 +862,9 @@ static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)
         const TileTask* t = P.dTasks + L.taskOff;
         switch (L.kind) {
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
-        case 1: k_ldl_panel<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        case 1: k_ldl_panel<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        case 4: k_ldl_diag<<<L.taskCount, 32, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
         }
     }
 }

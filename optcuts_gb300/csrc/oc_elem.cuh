@@ -272,7 +272,7 @@ __device__ void project_psd_reduced(double H[6][6])
 // localMode 0: exact (the global Newton); 1: the reduced 4x4 projection
 // (local solves, FP64); 2: as 1 with the eigen-decomposition in FP32
 __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, double e1d, double e01d, double w,
-                            double H[6][6], int localMode = 0)
+                            double H[6][6], int localMode = 0, double reducedDensity = 0.0)
 {
     const double U2m1[2] = {U[1].x - U[0].x, U[1].y - U[0].y};
     const double U3m1[2] = {U[2].x - U[0].x, U[2].y - U[0].y};
@@ -312,7 +312,7 @@ __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, do
             }
         }
     }
-    if (localMode == 1) {
+    if (localMode == 1 || (localMode == 3 && leftTerm * rightTerm <= reducedDensity)) {
         project_psd_reduced<double>(H);
         return;
     }
@@ -339,6 +339,26 @@ __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, do
                 H[i][j] = s;
             }
     }
+}
+
+
+// The 21 distinct entries of a symmetric 6x6 element block, stored
+// structure-of-arrays over the nF triangles: the three diagonal 2x2 blocks
+// (xx, xy, yy) in slots 0-8, then the 2x2 blocks of corner pairs (0,1),
+// (0,2), (1,2) row-major in slots 9-20.
+__device__ inline void store_hessian_blocks(const double H[6][6], int t, int nF, double* __restrict__ hb)
+{
+    for (int a = 0; a < 3; ++a) {
+        hb[(3 * a + 0) * (size_t)nF + t] = H[2 * a][2 * a];
+        hb[(3 * a + 1) * (size_t)nF + t] = H[2 * a][2 * a + 1];
+        hb[(3 * a + 2) * (size_t)nF + t] = H[2 * a + 1][2 * a + 1];
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = a + 1; b < 3; ++b) {
+            const int p = a + b - 1;   // (0,1) -> 0, (0,2) -> 1, (1,2) -> 2
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] = H[2 * a + i][2 * b + j];
+        }
 }
 
 } // namespace

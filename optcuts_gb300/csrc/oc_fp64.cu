@@ -232,21 +232,10 @@ __global__ void __launch_bounds__(128) k_hessian(DeviceMesh m, int uniform, doub
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= m.nF) return;
-    const int nF = m.nF;
     const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
     double H[6][6];
     tri_hessian(U, m.A2[t], m.e0d[t], m.e1d[t], m.e01d[t], uniform ? 1.0 : m.w[t], H);
-    for (int a = 0; a < 3; ++a) {
-        hb[(3 * a + 0) * (size_t)nF + t] = H[2 * a][2 * a];
-        hb[(3 * a + 1) * (size_t)nF + t] = H[2 * a][2 * a + 1];
-        hb[(3 * a + 2) * (size_t)nF + t] = H[2 * a + 1][2 * a + 1];
-    }
-    for (int a = 0; a < 3; ++a)
-        for (int b = a + 1; b < 3; ++b) {
-            const int p = a + b - 1;   // (0,1) -> 0, (0,2) -> 1, (1,2) -> 2
-            for (int i = 0; i < 2; ++i)
-                for (int j = 0; j < 2; ++j) hb[(9 + 4 * p + 2 * i + j) * (size_t)nF + t] = H[2 * a + i][2 * b + j];
-        }
+    store_hessian_blocks(H, t, m.nF, hb);
 }
 
 __global__ void k_set_bits(unsigned long long* dst, double v)
@@ -362,8 +351,10 @@ double* g_noallocPtr[256] = {};
 
 } // namespace
 
-void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st)
+void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st, int projection)
 {
+    if (projection == OC_HESSIAN_REDUCED) return launch_hessian_reduced(m, uniform, hb, st, 0.0);
+    if (projection == OC_HESSIAN_HYBRID) return launch_hessian_reduced(m, uniform, hb, st, kHybridDensity);
     k_hessian<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, hb);
 }
 

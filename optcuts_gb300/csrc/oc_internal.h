@@ -5,10 +5,29 @@
 
 #include "optcuts_gpu.h"
 
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace oc {
+
+// fn(begin, end) over contiguous chunks of [0, n) on up to 16 host threads
+// (the calling thread takes the first chunk); one chunk below 2 * minChunk
+template <class Fn>
+void host_parallel_for(size_t n, size_t minChunk, Fn&& fn)
+{
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::max<size_t>(1, std::min<size_t>({hw, 16, n / std::max<size_t>(1, minChunk)}));
+    if (nt == 1) {
+        if (n) fn(size_t(0), n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; ++t) th.emplace_back([&fn, n, nt, t] { fn(n * t / nt, n * (t + 1) / nt); });
+    fn(size_t(0), n / nt);
+    for (auto& x : th) x.join();
+}
 
 // 2x2 FP64 matrix, row-major (block-Jacobi inverse of one vertex row).
 struct __align__(32) Mat2d {
@@ -159,7 +178,18 @@ cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const L
 void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st);
 
 // per-triangle PSD-projected Hessian: 21 FP64 values per triangle (SoA)
-void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st);
+// element Hessians with the PSD projection: OC_HESSIAN_JACOBI6 the 6x6
+// cyclic Jacobi without FMA contraction (oc_fp64.cu), OC_HESSIAN_REDUCED the
+// translation-free 4x4 form, OC_HESSIAN_HYBRID the 4x4 form where the
+// element's energy density is at most kHybridDensity and the 6x6 form
+// elsewhere (both oc_local.cu)
+void launch_hessian(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st,
+                    int projection = OC_HESSIAN_JACOBI6);
+// density <= 0: the 4x4 form everywhere
+void launch_hessian_reduced(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st, double density);
+// symmetric Dirichlet energy density (4 at an isometry) above which the
+// hybrid projection keeps the 6x6 form
+constexpr double kHybridDensity = 1e3;
 // expand the 21 packed values to full 6x6 FP64 (for the API / tests)
 void launch_hessian_expand(const double* hb, int nF, double* out, cudaStream_t st);
 void launch_assemble(const DeviceBsr& b, const double* hb, int nF, double scale, cudaStream_t st);

@@ -615,6 +615,29 @@ int local_max_cluster()
     return v;
 }
 
+namespace {
+
+// Element Hessians of the global Newton step with the translation-free 4x4
+// PSD projection (FMA contraction on; the 6x6 form is k_hessian in oc_fp64.cu)
+__global__ void __launch_bounds__(128) k_hessian_reduced(DeviceMesh m, int uniform, double density,
+                                                         double* __restrict__ hb)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m.nF) return;
+    const double2 U[3] = {m.uv[m.F0[t]], m.uv[m.F1[t]], m.uv[m.F2[t]]};
+    double H[6][6];
+    tri_hessian(U, m.A2[t], m.e0d[t], m.e1d[t], m.e01d[t], uniform ? 1.0 : m.w[t], H, density > 0.0 ? 3 : 1,
+                density);
+    store_hessian_blocks(H, t, m.nF, hb);
+}
+
+} // namespace
+
+void launch_hessian_reduced(const DeviceMesh& m, int uniform, double* hb, cudaStream_t st, double density)
+{
+    if (m.nF > 0) k_hessian_reduced<<<(m.nF + 127) / 128, 128, 0, st>>>(m, uniform, density, hb);
+}
+
 cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, LocalSchedule sc,
                                 cudaStream_t st)
 {

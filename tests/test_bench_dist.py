@@ -4,6 +4,7 @@ the barrier and the max-over-ranks reduction the timed region uses agree on
 every rank."""
 import json
 import os
+import re
 import socket
 import subprocess
 import sys
@@ -57,5 +58,6 @@ def test_barrier_and_max_over_ranks(tmp_path):
     script.write_text(SCRIPT)
     r = torchrun([str(script)])
     assert r.returncode == 0, r.stderr[-2000:]
-    got = sorted(l for l in r.stdout.splitlines() if l.startswith("RANK"))
+    # the two ranks share stdout: their lines may arrive unseparated
+    got = sorted(re.findall(r"RANK\d \S+ \d", r.stdout))
     assert got == ["RANK0 2 2", "RANK1 2 2"]

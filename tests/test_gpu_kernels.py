@@ -233,3 +233,22 @@ def test_invalid_inputs_rejected(golden):
     with pytest.raises(oc.OCError) as e:
         oc.TriMesh(Vr, g["UV0"], g["F"], g["fixedVert"])
     assert e.value.status == 7
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_hessian_reduced_projection(golden, case):
+    """The translation-free 4x4 form of the eigen-clamp (the optimizer's
+    default) against the oracle's 6x6 Jacobi: the same projection up to
+    rounding relative to each block's largest entry."""
+    g = golden(case)
+    ref_all = O.hessian_blocks(g["rest"], g["F"], g["UV0"])
+    scale = np.abs(ref_all).reshape(len(ref_all), -1).max(axis=1)[:, None, None]
+    H = oc.SymDirichletEnergy().computeHessian(mesh_of(g), projection=oc.HESSIAN_REDUCED)
+    assert (np.abs(H - ref_all) / scale).max() < 1e-12
+    assert np.array_equal(H, np.transpose(H, (0, 2, 1)))
+    # translations stay in the null space
+    t = np.tile([1.0, 0.0], 3)
+    assert (np.abs(H @ t) / scale[:, :, 0]).max() < 1e-12
+    # the hybrid: the 4x4 form or the 6x6 one per element, both to rounding
+    Hh = oc.SymDirichletEnergy().computeHessian(mesh_of(g), projection=oc.HESSIAN_HYBRID)
+    assert (np.abs(Hh - ref_all) / scale).max() < 1e-12
