@@ -137,6 +137,19 @@ void nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::v
 
 int tiles_of(int k, int m) { return (k + kTile - 1) / kTile + (m - k + kTile - 1) / kTile; }
 
+// Tile t of a front's columns (pivot tiles first, then the rows below):
+// first row/column and extent.
+__host__ __device__ __forceinline__ void tile_bounds(int k, int m, int t, int& start, int& len)
+{
+    const int nP = (k + kTile - 1) / kTile;
+    start = t < nP ? t * kTile : k + (t - nP) * kTile;
+    const int end = t < nP ? k : m;
+    len = end - start < kTile ? end - start : kTile;
+}
+
+// rows of a tile row per panel-solve block (one warp per row)
+constexpr int kPanelRows = 8;
+
 } // namespace
 
 void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize,
@@ -336,7 +349,11 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
                 const int nt = tiles_of(P.fk[f], P.fm[f]);
-                for (int ti = p + 1; ti < nt; ++ti) P.tasks.push_back(TileTask{f, ti, 0, p});
+                for (int ti = p + 1; ti < nt; ++ti) {
+                    int r0, h;
+                    tile_bounds(P.fk[f], P.fm[f], ti, r0, h);
+                    for (int g = 0; g * kPanelRows < h; ++g) P.tasks.push_back(TileTask{f, ti, g, p});
+                }
             }
             if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
             off = static_cast<int>(P.tasks.size());
@@ -400,19 +417,6 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
 // ------------------------------------------------------------------ kernels
 namespace {
 
-__device__ __forceinline__ void tile_bounds(int k, int m, int t, int& start, int& len)
-{
-    const int nP = (k + kTile - 1) / kTile;
-    if (t < nP) {
-        start = t * kTile;
-        len = min(kTile, k - start);
-    }
-    else {
-        start = k + (t - nP) * kTile;
-        len = min(kTile, m - start);
-    }
-}
-
 __global__ void k_asm_fronts(const Blk2* __restrict__ val, const long long* __restrict__ dest,
                              const int* __restrict__ ld, const unsigned char* __restrict__ diag, int nnzb,
                              double* __restrict__ pool)
@@ -453,93 +457,127 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
 // LDL^T of the w x w diagonal tile at (s0, s0) of a front, in place (unit-
 // lower L below the diagonal, D on it -- the factorisation SimplicialLDLT
 // computes; negative pivots pass, a zero or non-finite one is replaced by
-// 1e-300 and counted in *flag).  Run by one warp, a row per lane, in the
-// 32 x 33 shared tile T; the same operation order as a column-by-column
-// right-looking elimination.
-__device__ void ldl_diag_tile(double* __restrict__ F, int m, int s0, int w, double (*T)[kTile + 1], int* flag)
+// 1e-300 and counted in *flag).  Run by the first kDiagThreads threads of
+// the block (four warps, one per SM sub-partition, so the elimination uses
+// every FP64 unit of the SM; named barrier 1) in the 32 x 33 shared tile T
+// with 32 doubles of scratch Lc: elimination step c updates the entries
+// (r, c2), c < c2 <= r < w, of the packed lower triangle in column-major
+// order, with the operation order of a column-by-column right-looking
+// elimination.
+constexpr int kDiagThreads = 128;
+
+__device__ __forceinline__ int tri_col_start(int j, int w) { return j * w - (j * (j - 1)) / 2; }
+
+__device__ __forceinline__ void diag_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kDiagThreads) : "memory"); }
+
+__device__ void ldl_diag_tile(double* __restrict__ F, int m, int s0, int w, double (*T)[kTile + 1], double* Lc,
+                              int* flag)
 {
-    const int lane = threadIdx.x & 31;
-    for (int c = 0; c < w; ++c)
-        if (lane < w) T[lane][c] = lane >= c ? F[(s0 + lane) + (long long)(s0 + c) * m] : 0.0;
-    __syncwarp();
+    const int q = threadIdx.x;   // < kDiagThreads
+    for (int e = q; e < kTile * w; e += kDiagThreads) {
+        const int r = e & (kTile - 1), c = e / kTile;
+        if (r < w) T[r][c] = r >= c ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
+    }
+    diag_barrier();
+    const int total = tri_col_start(w, w);
+    const float b = 2.0f * w + 1.0f;
     int nBad = 0;
     for (int c = 0; c < w; ++c) {
         const double dRaw = T[c][c];
         const bool bad = !(dRaw != 0.0) || !isfinite(dRaw);
         const double d = bad ? 1e-300 : dRaw;
         nBad += bad;
-        const double id = 1.0 / d;
-        const double u = lane < w ? T[lane][c] * id : 0.0;   // L(lane, c) for lane > c
-        for (int c2 = c + 1; c2 < w; ++c2)
-            if (lane >= c2 && lane < w) T[lane][c2] -= u * T[c2][c];
-        __syncwarp();
-        if (lane > c && lane < w) T[lane][c] = u;
-        else if (lane == c) T[c][c] = d;
-        __syncwarp();
+        double lc = 0.0;
+        if (q > c && q < w) {
+            lc = T[q][c] * (1.0 / d);   // L(q, c)
+            Lc[q] = lc;
+        }
+        diag_barrier();
+        for (int e = tri_col_start(c + 1, w) + q; e < total; e += kDiagThreads) {
+            // column c2 of packed entry e: the largest j with start(j) <= e
+            int c2 = static_cast<int>(0.5f * (b - sqrtf(b * b - 8.0f * e)));
+            c2 = max(c + 1, min(c2, w - 1));
+            while (c2 + 1 < w && tri_col_start(c2 + 1, w) <= e) ++c2;
+            while (tri_col_start(c2, w) > e) --c2;
+            const int r = c2 + (e - tri_col_start(c2, w));
+            T[r][c2] -= Lc[r] * T[c2][c];
+        }
+        diag_barrier();
+        if (q > c && q < w) T[q][c] = lc;
+        else if (q == c) T[c][c] = d;
+        // the next step reads column c + 1 only; column c's writes are
+        // ordered before the final copy by the barriers of later steps
     }
-    for (int c = 0; c < w; ++c)
-        if (lane < w && lane >= c) F[(s0 + lane) + (long long)(s0 + c) * m] = T[lane][c];
-    if (lane == 0 && nBad) atomicAdd(flag, nBad);
+    diag_barrier();
+    for (int e = q; e < kTile * w; e += kDiagThreads) {
+        const int r = e & (kTile - 1), c = e / kTile;
+        if (r < w && r >= c) F[(s0 + r) + (long long)(s0 + c) * m] = T[r][c];
+    }
+    if (q == 0 && nBad) atomicAdd(flag, nBad);
 }
 
-// The diagonal tile of every front's first panel (one warp per front of the
-// level; the later panels' tiles are factored by k_ldl_update).
-__global__ void __launch_bounds__(32) k_ldl_diag(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                 const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                 double* __restrict__ pool, int* flag)
+// The diagonal tile of every front's first panel (one block of four warps
+// per front of the level; the later panels' tiles are factored by
+// k_ldl_update).
+__global__ void __launch_bounds__(kDiagThreads) k_ldl_diag(const TileTask* __restrict__ tasks,
+                                                           const int* __restrict__ fk, const int* __restrict__ fm,
+                                                           const long long* __restrict__ foff,
+                                                           double* __restrict__ pool, int* flag)
 {
     __shared__ double T[kTile][kTile + 1];
+    __shared__ double Lc[kTile];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w;
     tile_bounds(k, m, t.p, s0, w);
-    ldl_diag_tile(pool + foff[t.front], m, s0, w, T, flag);
+    ldl_diag_tile(pool + foff[t.front], m, s0, w, T, Lc, flag);
 }
 
-// Panel solve of one tile row below the (already factored) diagonal tile of
-// panel p: L(i, p) = A(i, p) L(p, p)^-T D^-1.  Each warp takes rows warp,
-// warp + 8, warp + 16, warp + 24 of the tile row, a column per lane, in the
-// operation order of a column-by-column substitution.
-__global__ void __launch_bounds__(256) k_ldl_panel(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
-                                                   const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                   double* __restrict__ pool)
+// Panel solve below the (already factored) diagonal tile of panel p:
+// L(i, p) = A(i, p) L(p, p)^-T D^-1 for kPanelRows rows of tile row i (task
+// j: which group of rows), a row per warp and a column per lane, in the
+// operation order of a column-by-column substitution.  A tile row is split
+// over several blocks so that the few tile rows of the top fronts spread
+// over more SMs.
+__global__ void __launch_bounds__(32 * kPanelRows) k_ldl_panel(const TileTask* __restrict__ tasks,
+                                                               const int* __restrict__ fk,
+                                                               const int* __restrict__ fm,
+                                                               const long long* __restrict__ foff,
+                                                               double* __restrict__ pool)
 {
     static_assert(kTile == 32, "one warp lane per tile column");
-    __shared__ double A[kTile][kTile + 1];
-    __shared__ double X[kTile][kTile + 1];
+    __shared__ double L[kTile][kTile + 1];
+    __shared__ double X[kPanelRows][kTile + 1];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w, r0, h;
     tile_bounds(k, m, t.p, s0, w);
     tile_bounds(k, m, t.i, r0, h);
+    r0 += kPanelRows * t.j;
+    h = min(kPanelRows, h - kPanelRows * t.j);
     double* F = pool + foff[t.front];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // the factored tile (identity beyond w) and the tile row (zero beyond h x w)
+    // the factored tile (identity beyond w) and the rows (zero beyond h x w)
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
         const int r = e & (kTile - 1), c = e / kTile;
         double a = r == c ? 1.0 : 0.0;
         if (r < w && c < w && r >= c) a = F[(s0 + r) + (long long)(s0 + c) * m];
-        A[r][c] = a;
+        L[r][c] = a;
+    }
+    for (int e = threadIdx.x; e < kPanelRows * kTile; e += blockDim.x) {
+        const int r = e % kPanelRows, c = e / kPanelRows;
         X[r][c] = (r < h && c < w) ? F[(r0 + r) + (long long)(s0 + c) * m] : 0.0;
     }
     __syncthreads();
-    double x[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) x[q] = X[warp + 8 * q][lane];
+    double x = X[warp][lane];
     for (int c = 0; c + 1 < w; ++c) {
-        const double lc = A[lane][c];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const double xc = __shfl_sync(0xffffffffu, x[q], c);
-            if (lane > c) x[q] -= xc * lc;
-        }
+        const double xc = __shfl_sync(0xffffffffu, x, c);
+        if (lane > c) x -= xc * L[lane][c];
     }
-    const double dl = A[lane][lane];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) X[warp + 8 * q][lane] = x[q] / dl;
+    X[warp][lane] = x / L[lane][lane];
     __syncthreads();
-    for (int e = threadIdx.x; e < kTile * w; e += blockDim.x) {
-        const int r = e & (kTile - 1), c = e / kTile;
+    for (int e = threadIdx.x; e < kPanelRows * w; e += blockDim.x) {
+        const int r = e % kPanelRows, c = e / kPanelRows;
         if (r < h) F[(r0 + r) + (long long)(s0 + c) * m] = X[r][c];
     }
 }
@@ -611,8 +649,9 @@ __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__
     // Ai's shared memory), so the next panel launch reads it factored
     if (t.i == 0 && t.j == 0 && s < k) {
         __syncthreads();
-        if (threadIdx.x < 32)
-            ldl_diag_tile(F, m, s, min(kTile, k - s), reinterpret_cast<double(*)[kTile + 1]>(&Ai[0][0]), flag);
+        if (threadIdx.x < kDiagThreads)
+            ldl_diag_tile(F, m, s, min(kTile, k - s), reinterpret_cast<double(*)[kTile + 1]>(&Ai[0][0]), &Aj[0][0],
+                          flag);
     }
 }
 
@@ -862,8 +901,8 @@ static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)
         const TileTask* t = P.dTasks + L.taskOff;
         switch (L.kind) {
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
-        case 1: k_ldl_panel<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
-        case 4: k_ldl_diag<<<L.taskCount, 32, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        case 1: k_ldl_panel<<<L.taskCount, 32 * kPanelRows, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+        case 4: k_ldl_diag<<<L.taskCount, kDiagThreads, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
         default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
         }
     }
