@@ -149,6 +149,10 @@ __host__ __device__ __forceinline__ void tile_bounds(int k, int m, int t, int& s
 
 // rows of a tile row per panel-solve block (one warp per row)
 constexpr int kPanelRows = 8;
+// trailing updates: 32 x 32 blocks when a launch has fewer 64 x 64 blocks
+// than two waves of one block per SM on 152 SMs
+constexpr int kUpdSmall = 32;
+constexpr long long kUpdSplitBlocks = 2 * 152;
 
 } // namespace
 
@@ -356,18 +360,32 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
                 }
             }
             if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
+            // trailing region [s, m) x [s, m), s = end of panel p, in the
+            // lower triangle of 64 x 64 blocks, or of 32 x 32 blocks when the
+            // 64 x 64 ones would not fill two waves of the GPU
+            auto blocks_of = [&](int f, int edge) {
+                const int s = std::min((p + 1) * kTile, P.fk[f]);
+                const int nb = (P.fm[f] - s + edge - 1) / edge;
+                return nb;
+            };
+            long long n64 = 0;
+            for (int i = 0; i < nl; ++i) {
+                const int f = lf[i];
+                if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
+                const long long nb = blocks_of(f, kUpd);
+                n64 += nb * (nb + 1) / 2;
+            }
+            const int edge = n64 < kUpdSplitBlocks ? kUpdSmall : kUpd;
             off = static_cast<int>(P.tasks.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
-                // trailing region [s, m) x [s, m), s = end of panel p, in
-                // 64 x 64 blocks (lower triangle of blocks)
-                const int s = std::min((p + 1) * kTile, P.fk[f]);
-                const int nb = (P.fm[f] - s + kUpd - 1) / kUpd;
+                const int nb = blocks_of(f, edge);
                 for (int bj = 0; bj < nb; ++bj)
                     for (int bi = bj; bi < nb; ++bi) P.tasks.push_back(TileTask{f, bi, bj, p});
             }
-            if ((int)P.tasks.size() > off) P.launches.push_back({3, l, p, off, (int)P.tasks.size() - off, 0});
+            if ((int)P.tasks.size() > off)
+                P.launches.push_back({edge == kUpd ? 3 : 5, l, p, off, (int)P.tasks.size() - off, 0});
         }
     }
     // substitution chunks of the rectangular part of each front, per level
@@ -583,26 +601,33 @@ __global__ void __launch_bounds__(32 * kPanelRows) k_ldl_panel(const TileTask* _
 }
 
 // Trailing update C -= L(:, p) * D_p * L(:, p)^T of the region below and right
-// of panel p, in 64 x 64 blocks (task: block row bi, block column bj >= ...,
-// lower triangle only).  256 threads, 4 x 4 accumulators each; the panel
-// columns of both block rows are staged column-major in shared memory so a
-// thread's four rows (or columns) are one 32-byte read.
+// of panel p, in B x B blocks (task: block row bi, block column bj <= bi,
+// lower triangle only).  256 threads, P x P accumulators each (B = 16 P);
+// the panel columns of both block rows are staged column-major in shared
+// memory so a thread's rows (or columns) are 16-byte reads.  B = 64 in
+// general; B = 32 for launches too small to fill the GPU with 64 x 64
+// blocks (four times the blocks, a quarter of the work each).
+template <int B, int P>
 __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
                                                     const int* __restrict__ fm, const long long* __restrict__ foff,
                                                     double* __restrict__ pool, int* flag)
 {
-    __shared__ __align__(16) double Ai[kTile][kUpd];
-    __shared__ __align__(16) double Aj[kTile][kUpd];
+    static_assert(B == 16 * P && P % 2 == 0, "16 x 16 threads of P x P");
+    // Ai, Aj, and in the tail the diagonal tile (32 x 33) and its scratch
+    constexpr int kSm = 2 * kTile * B > kTile * (kTile + 1) + kTile ? 2 * kTile * B : kTile * (kTile + 1) + kTile;
+    __shared__ __align__(16) double sm[kSm];
+    double (*Ai)[B] = reinterpret_cast<double(*)[B]>(sm);
+    double (*Aj)[B] = reinterpret_cast<double(*)[B]>(sm + kTile * B);
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w;
     tile_bounds(k, m, t.p, s0, w);
     const int s = s0 + w;                       // first row/column after the panel
-    const int r0 = s + kUpd * t.i, c0 = s + kUpd * t.j;
-    const int h = min(kUpd, m - r0), hc = min(kUpd, m - c0);
+    const int r0 = s + B * t.i, c0 = s + B * t.j;
+    const int h = min(B, m - r0), hc = min(B, m - c0);
     double* F = pool + foff[t.front];
-    for (int e = threadIdx.x; e < kTile * kUpd; e += blockDim.x) {
-        const int r = e % kUpd, c = e / kUpd;
+    for (int e = threadIdx.x; e < kTile * B; e += blockDim.x) {
+        const int r = e % B, c = e / B;
         double ai = 0.0, aj = 0.0;
         if (c < w) {
             const double* col = F + (long long)(s0 + c) * m;
@@ -613,45 +638,48 @@ __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__
         Aj[c][r] = aj;
     }
     __syncthreads();
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, 4 x 4 each
-    double acc[4][4];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;   // 16 x 16 threads, P x P each
+    double acc[P][P];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < P; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-    // threads whose 4 x 4 patch lies outside the block's rows/columns, or
-    // wholly above the diagonal of a diagonal block, have nothing to update
-    const bool idle = (4 * ty >= h) || (4 * tx >= hc) || (t.i == t.j && 4 * ty + 3 < 4 * tx);
+        for (int j = 0; j < P; ++j) acc[i][j] = 0.0;
+    // threads whose patch lies outside the block's rows/columns, or wholly
+    // above the diagonal of a diagonal block, have nothing to update
+    const bool idle = (P * ty >= h) || (P * tx >= hc) || (t.i == t.j && P * ty + P - 1 < P * tx);
     for (int c = 0; c < (idle ? 0 : w); ++c) {
-        const double2 a01 = *reinterpret_cast<const double2*>(&Ai[c][4 * ty]);
-        const double2 a23 = *reinterpret_cast<const double2*>(&Ai[c][4 * ty + 2]);
-        const double2 b01 = *reinterpret_cast<const double2*>(&Aj[c][4 * tx]);
-        const double2 b23 = *reinterpret_cast<const double2*>(&Aj[c][4 * tx + 2]);
-        const double a[4] = {a01.x, a01.y, a23.x, a23.y}, b[4] = {b01.x, b01.y, b23.x, b23.y};
+        double a[P], b[P];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < P; i += 2) {
+            const double2 av = *reinterpret_cast<const double2*>(&Ai[c][P * ty + i]);
+            const double2 bv = *reinterpret_cast<const double2*>(&Aj[c][P * tx + i]);
+            a[i] = av.x; a[i + 1] = av.y;
+            b[i] = bv.x; b[i + 1] = bv.y;
+        }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        for (int i = 0; i < P; ++i)
+#pragma unroll
+            for (int j = 0; j < P; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
     const bool diag = (t.i == t.j);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int r = 4 * ty + i;
+    for (int i = 0; i < P; ++i) {
+        const int r = P * ty + i;
         if (r >= h) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int cc = 4 * tx + j;
+        for (int j = 0; j < P; ++j) {
+            const int cc = P * tx + j;
             if (cc < hc && (!diag || r >= cc)) F[(r0 + r) + (long long)(c0 + cc) * m] -= acc[i][j];
         }
     }
     // the next panel's diagonal tile is the corner of this front's first
-    // trailing block: once the block is updated, one warp factors it (in
-    // Ai's shared memory), so the next panel launch reads it factored
+    // trailing block: once the block is updated, four warps factor it (in
+    // the staging buffers), so the next panel launch reads it factored
     if (t.i == 0 && t.j == 0 && s < k) {
         __syncthreads();
         if (threadIdx.x < kDiagThreads)
-            ldl_diag_tile(F, m, s, min(kTile, k - s), reinterpret_cast<double(*)[kTile + 1]>(&Ai[0][0]), &Aj[0][0],
-                          flag);
+            ldl_diag_tile(F, m, s, min(kTile, k - s), reinterpret_cast<double(*)[kTile + 1]>(sm),
+                          sm + kTile * (kTile + 1), flag);
     }
 }
 
@@ -903,7 +931,8 @@ static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
         case 1: k_ldl_panel<<<L.taskCount, 32 * kPanelRows, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         case 4: k_ldl_diag<<<L.taskCount, kDiagThreads, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        default: k_ldl_update<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        case 5: k_ldl_update<32, 2><<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        default: k_ldl_update<kUpd, 4><<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
         }
     }
 }

@@ -38,8 +38,8 @@ struct CholPlan {
     // per-level front lists and tiled task lists
     std::vector<int> levelFrontOff, levelFronts;
     // kind: 0 extend-add of child slot `child`, 1 panel solve, 3 trailing
-    // update (also factors the next panel's diagonal tile), 4 the first
-    // panel's diagonal tiles
+    // update in 64 x 64 blocks, 5 in 32 x 32 blocks (both also factor the
+    // next panel's diagonal tile), 4 the first panel's diagonal tiles
     struct Launch { int kind; int level; int p; int taskOff; int taskCount; int child; };
     std::vector<Launch> launches;        // in execution order
     std::vector<TileTask> tasks;
