@@ -744,10 +744,30 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
             if (lane < w) sh[c0 + lane] = v;
         }
         __syncthreads();
-        for (int r = c0 + w + threadIdx.x; r < k; r += blockDim.x) {
-            double s = 0.0;
-            for (int c = 0; c < w; ++c) s = fma(L[r + (long long)(c0 + c) * m], sh[c0 + c], s);
-            sh[r] -= s;
+        // a thread's rows r, r + T, r + 2T, r + 3T (T = block size) at once:
+        // four independent FMA chains, each row summed in column order
+        const int T = blockDim.x;
+        for (int rb = c0 + w + threadIdx.x; rb < k; rb += 4 * T) {
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int cb = 0; cb < w; cb += 8) {
+                double lv[4][8];   // eight columns' loads in flight before the FMAs
+#pragma unroll
+                for (int cc = 0; cc < 8; ++cc)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        lv[q][cc] = (cb + cc < w && rb + q * T < k) ? L[rb + q * T + (long long)(c0 + cb + cc) * m]
+                                                                     : 0.0;
+#pragma unroll
+                for (int cc = 0; cc < 8; ++cc) {
+                    if (cb + cc >= w) break;
+                    const double yc = sh[c0 + cb + cc];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] = fma(lv[q][cc], yc, acc[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (rb + q * T < k) sh[rb + q * T] -= acc[q];
         }
         __syncthreads();
     }
@@ -831,12 +851,36 @@ __global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, con
             const int col = e >> 5, row = e & 31;
             if (row < w) tile[row * 33 + col] = L[(c0 + row) + (long long)(c0 + col) * m];
         }
-        for (int c = warp; c < w; c += nw) {
-            const double* lc = L + (long long)(c0 + c) * m;
-            double s = 0.0;
-            for (int r = c0 + w + lane; r < k; r += 32) s = fma(lc[r], sh[r], s);
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0) dots[c] = s;
+        // a warp's columns warp, warp + nw, ... (at most four: nw = 8) at
+        // once: independent FMA chains, each column summed in row order
+        {
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int rb = c0 + w + lane; rb < k; rb += 4 * 32) {
+                double lv[4][4];   // four rows' loads in flight before the FMAs
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int c = warp + q * nw, r = rb + 32 * i;
+                        lv[i][q] = (c < w && r < k) ? L[r + (long long)(c0 + c) * m] : 0.0;
+                    }
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = rb + 32 * i;
+                    if (r >= k) break;
+                    const double xr = sh[r];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] = fma(lv[i][q], xr, acc[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int c = warp + q * nw;
+                if (c >= w) continue;
+                double v = acc[q];
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                if (lane == 0) dots[c] = v;
+            }
         }
         __syncthreads();
         if (warp == 0) {
