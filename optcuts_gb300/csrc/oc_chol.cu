@@ -477,54 +477,82 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
 // computes; negative pivots pass, a zero or non-finite one is replaced by
 // 1e-300 and counted in *flag).  Run by the first kDiagThreads threads of
 // the block (four warps, one per SM sub-partition, so the elimination uses
-// every FP64 unit of the SM; named barrier 1) in the 32 x 33 shared tile T
-// with 32 doubles of scratch Lc: elimination step c updates the entries
-// (r, c2), c < c2 <= r < w, of the packed lower triangle in column-major
-// order, with the operation order of a column-by-column right-looking
-// elimination.
+// every FP64 unit of the SM; named barrier 1), in kDiagScratch doubles of
+// shared memory: the 32 x 33 tile, the scaled column, the current pivot and
+// its reciprocal, and a table of the packed lower triangle's entries in
+// column-major order.  Elimination step c scales column c by the pivot's
+// reciprocal, which thread 0 computed during step c - 1 right after updating
+// that diagonal entry first, while warps 1-3 update the step's other entries
+// (r, c2), c < c2 <= r < w.  The operation order of a column-by-column
+// right-looking elimination.
 constexpr int kDiagThreads = 128;
+constexpr int kDiagScratch = kTile * (kTile + 1) + kTile + 2 + (kTile * (kTile + 1) / 2 + 3) / 4;
 
 __device__ __forceinline__ int tri_col_start(int j, int w) { return j * w - (j * (j - 1)) / 2; }
 
 __device__ __forceinline__ void diag_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kDiagThreads) : "memory"); }
 
-__device__ void ldl_diag_tile(double* __restrict__ F, int m, int s0, int w, double (*T)[kTile + 1], double* Lc,
-                              int* flag)
+// pivot d (a zero or non-finite value replaced by 1e-300) and 1 / d
+__device__ __forceinline__ void diag_pivot(double dRaw, double* piv, int& nBad)
 {
+    const bool bad = !(dRaw != 0.0) || !isfinite(dRaw);
+    const double d = bad ? 1e-300 : dRaw;
+    nBad += bad;
+    piv[0] = d;
+    piv[1] = 1.0 / d;
+}
+
+__device__ void ldl_diag_tile(double* __restrict__ F, int m, int s0, int w, double* scratch, int* flag)
+{
+    double (*T)[kTile + 1] = reinterpret_cast<double(*)[kTile + 1]>(scratch);
+    double* Lc = scratch + kTile * (kTile + 1);
+    double* piv = Lc + kTile;
+    unsigned short* tab = reinterpret_cast<unsigned short*>(piv + 2);   // entry -> (r << 5) | c2
     const int q = threadIdx.x;   // < kDiagThreads
     for (int e = q; e < kTile * w; e += kDiagThreads) {
         const int r = e & (kTile - 1), c = e / kTile;
         if (r < w) T[r][c] = r >= c ? F[(s0 + r) + (long long)(s0 + c) * m] : 0.0;
     }
-    diag_barrier();
     const int total = tri_col_start(w, w);
     const float b = 2.0f * w + 1.0f;
-    int nBad = 0;
+    for (int e = q; e < total; e += kDiagThreads) {
+        // column c2 of packed entry e: the largest j with start(j) <= e
+        int c2 = static_cast<int>(0.5f * (b - sqrtf(b * b - 8.0f * e)));
+        c2 = max(0, min(c2, w - 1));
+        while (c2 + 1 < w && tri_col_start(c2 + 1, w) <= e) ++c2;
+        while (tri_col_start(c2, w) > e) --c2;
+        tab[e] = static_cast<unsigned short>(((c2 + (e - tri_col_start(c2, w))) << 5) | c2);
+    }
+    diag_barrier();
+    int nBad = 0;   // thread 0's count
+    if (q == 0) diag_pivot(T[0][0], piv, nBad);
+    diag_barrier();
     for (int c = 0; c < w; ++c) {
-        const double dRaw = T[c][c];
-        const bool bad = !(dRaw != 0.0) || !isfinite(dRaw);
-        const double d = bad ? 1e-300 : dRaw;
-        nBad += bad;
+        const double d = piv[0], id = piv[1];
         double lc = 0.0;
         if (q > c && q < w) {
-            lc = T[q][c] * (1.0 / d);   // L(q, c)
+            lc = T[q][c] * id;   // L(q, c)
             Lc[q] = lc;
         }
         diag_barrier();
-        for (int e = tri_col_start(c + 1, w) + q; e < total; e += kDiagThreads) {
-            // column c2 of packed entry e: the largest j with start(j) <= e
-            int c2 = static_cast<int>(0.5f * (b - sqrtf(b * b - 8.0f * e)));
-            c2 = max(c + 1, min(c2, w - 1));
-            while (c2 + 1 < w && tri_col_start(c2 + 1, w) <= e) ++c2;
-            while (tri_col_start(c2, w) > e) --c2;
-            const int r = c2 + (e - tri_col_start(c2, w));
-            T[r][c2] -= Lc[r] * T[c2][c];
+        const int e0 = tri_col_start(c + 1, w);   // entry (c + 1, c + 1): the next pivot
+        if (q == 0) {
+            if (c + 1 < w) {
+                T[c + 1][c + 1] -= Lc[c + 1] * T[c + 1][c];
+                diag_pivot(T[c + 1][c + 1], piv, nBad);
+            }
+        }
+        else if (q >= 32) {
+            for (int e = e0 + 1 + (q - 32); e < total; e += kDiagThreads - 32) {
+                const int rc = tab[e], r = rc >> 5, c2 = rc & 31;
+                T[r][c2] -= Lc[r] * T[c2][c];
+            }
         }
         diag_barrier();
         if (q > c && q < w) T[q][c] = lc;
         else if (q == c) T[c][c] = d;
-        // the next step reads column c + 1 only; column c's writes are
-        // ordered before the final copy by the barriers of later steps
+        // the next step reads column c + 1 and the pivot only; column c's
+        // writes are ordered before the final copy by later barriers
     }
     diag_barrier();
     for (int e = q; e < kTile * w; e += kDiagThreads) {
@@ -542,13 +570,12 @@ __global__ void __launch_bounds__(kDiagThreads) k_ldl_diag(const TileTask* __res
                                                            const long long* __restrict__ foff,
                                                            double* __restrict__ pool, int* flag)
 {
-    __shared__ double T[kTile][kTile + 1];
-    __shared__ double Lc[kTile];
+    __shared__ double scratch[kDiagScratch];
     const TileTask t = tasks[blockIdx.x];
     const int k = fk[t.front], m = fm[t.front];
     int s0, w;
     tile_bounds(k, m, t.p, s0, w);
-    ldl_diag_tile(pool + foff[t.front], m, s0, w, T, Lc, flag);
+    ldl_diag_tile(pool + foff[t.front], m, s0, w, scratch, flag);
 }
 
 // Panel solve below the (already factored) diagonal tile of panel p:
@@ -613,8 +640,8 @@ __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__
                                                     double* __restrict__ pool, int* flag)
 {
     static_assert(B == 16 * P && P % 2 == 0, "16 x 16 threads of P x P");
-    // Ai, Aj, and in the tail the diagonal tile (32 x 33) and its scratch
-    constexpr int kSm = 2 * kTile * B > kTile * (kTile + 1) + kTile ? 2 * kTile * B : kTile * (kTile + 1) + kTile;
+    // Ai, Aj, and in the tail the diagonal tile's scratch
+    constexpr int kSm = 2 * kTile * B > kDiagScratch ? 2 * kTile * B : kDiagScratch;
     __shared__ __align__(16) double sm[kSm];
     double (*Ai)[B] = reinterpret_cast<double(*)[B]>(sm);
     double (*Aj)[B] = reinterpret_cast<double(*)[B]>(sm + kTile * B);
@@ -677,9 +704,7 @@ __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__
     // the staging buffers), so the next panel launch reads it factored
     if (t.i == 0 && t.j == 0 && s < k) {
         __syncthreads();
-        if (threadIdx.x < kDiagThreads)
-            ldl_diag_tile(F, m, s, min(kTile, k - s), reinterpret_cast<double(*)[kTile + 1]>(sm),
-                          sm + kTile * (kTile + 1), flag);
+        if (threadIdx.x < kDiagThreads) ldl_diag_tile(F, m, s, min(kTile, k - s), sm, flag);
     }
 }
 
