@@ -407,6 +407,16 @@ int oc_mesh_get_topology(oc_mesh* mesh, int* nV, int* nF, int* nCohE, int* F, do
 int oc_topology_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, int nV, int nF,
                       const int* F, const double* Vrest, const double* UV, int nCohE, const int* cohE, int* F_out,
                       double* Vrest_out, double* UV_out, int* cohE_out, int* nV_out, int* nCohE_out);
+/* host only: TriMesh::cutPath(path, makeCoh = true) (TriMesh.cpp:1393-1517) as
+ * the initial cutting of a genus >= 1 mesh calls it (main.cpp:1397-1484):
+ * from a boundary end every interior edge of the path split on the boundary
+ * (cut through where both ends are on the boundary); an interior path first
+ * cut through its first three vertices.  Outputs hold nV + 2 * pathLen
+ * vertices and nCohE + 2 * pathLen cohesive rows at most; *nSplit (may be
+ * NULL) = edges split on the boundary */
+int oc_topology_cut_path(const int* path, int pathLen, int nV, int nF, const int* F, const double* Vrest,
+                         const double* UV, int nCohE, const int* cohE, int* F_out, double* Vrest_out, double* UV_out,
+                         int* cohE_out, int* nV_out, int* nCohE_out, int* nSplit);
 /* host only: the split filter's candidate vertices, in order */
 int oc_topology_split_candidates(int nV, const int* F, int nF, const double* divGrad, int interior, double filterExp,
                                  int* cands, int* nCands, int* pool);

@@ -119,6 +119,8 @@ _SIGS = {
     "oc_mesh_get_topology": [_vp, _i, _i, _i, _i, _d, _i],
     "oc_topology_apply": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d,
                           ctypes.c_int, _i, _i, _d, _d, _i, _i, _i],
+    "oc_topology_cut_path": [_i, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d, ctypes.c_int, _i, _i, _d, _d,
+                             _i, _i, _i, _i],
     "oc_topology_query_learned": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
                                   ctypes.c_double, ctypes.POINTER(_vp)],
     "oc_topo_result_features": [_vp, _i, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
@@ -553,6 +555,26 @@ def topology_apply(op, path, newVertPos, V_rest, UV, F, cohE):
     if rc != OC_OK:
         raise OCError(rc, "topology_apply")
     return Vo[:nvo.value], Uo[:nvo.value], Fo, Co[:nco.value]
+
+
+def topology_cut_path(path, V_rest, UV, F, cohE):
+    """Host-only TriMesh::cutPath(path, makeCoh = true) as the initial cutting
+    of a genus >= 1 mesh calls it (boundary splits along the path; an
+    interior path first cut through its first three vertices): returns
+    (V_rest, UV, F, cohE, edges split)."""
+    path = _i4(path)
+    Vr, uv, F = _f8(V_rest), _f8(UV), _i4(F)
+    c = _i4(np.asarray(cohE).reshape(-1, 4))
+    nV, extra = len(Vr), 2 * len(path)
+    Fo, Vo, Uo = np.zeros_like(F), np.zeros((nV + extra, 3)), np.zeros((nV + extra, 2))
+    Co = np.zeros((len(c) + extra, 4), np.int32)
+    nvo, nco, made = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    rc = lib().oc_topology_cut_path(_pi(path), len(path), nV, len(F), _pi(F), _pd(Vr), _pd(uv), len(c), _pi(c),
+                                    _pi(Fo), _pd(Vo), _pd(Uo), _pi(Co), ctypes.byref(nvo), ctypes.byref(nco),
+                                    ctypes.byref(made))
+    if rc != OC_OK:
+        raise OCError(rc, "topology_cut_path")
+    return Vo[:nvo.value], Uo[:nvo.value], Fo, Co[:nco.value], made.value
 
 
 def split_candidates(nV, F, divGrad, interior, filterExp=0.6):

@@ -1111,6 +1111,30 @@ int oc_topology_apply(int opType, const int* path, int pathLen, const double* ne
     return OC_OK;
 }
 
+int oc_topology_cut_path(const int* path, int pathLen, int nV, int nF, const int* F, const double* Vrest,
+                         const double* UV, int nCohE, const int* cohE, int* F_out, double* Vrest_out, double* UV_out,
+                         int* cohE_out, int* nV_out, int* nCohE_out, int* nSplit)
+{
+    if (!path || pathLen < 2 || nV <= 0 || nF <= 0 || !F || !Vrest || !UV || nCohE < 0 || (nCohE && !cohE) ||
+        !F_out || !Vrest_out || !UV_out || !nV_out || !nCohE_out)
+        return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
+    std::vector<int> f(F, F + 3 * (size_t)nF), c(cohE, cohE + 4 * (size_t)nCohE);
+    std::vector<double> vr(Vrest, Vrest + 3 * (size_t)nV), uv(UV, UV + 2 * (size_t)nV);
+    int made = 0;
+    const int rc = oc::topo_cut_path(path, pathLen, f, vr, uv, c, made, nullptr);
+    if (rc) return rc;
+    std::copy(f.begin(), f.end(), F_out);
+    std::copy(vr.begin(), vr.end(), Vrest_out);
+    std::copy(uv.begin(), uv.end(), UV_out);
+    if (cohE_out) std::copy(c.begin(), c.end(), cohE_out);
+    *nV_out = static_cast<int>(uv.size() / 2);
+    *nCohE_out = static_cast<int>(c.size() / 4);
+    if (nSplit) *nSplit = made;
+    return OC_OK;
+}
+
 int oc_topo_result_destroy(oc_topo_result* r)
 {
     if (!r) return OC_ERR_INVALID;

@@ -724,6 +724,111 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
     return bad("topology op: unknown operation");
 }
 
+// TriMesh::cutPath(path, makeCoh = true) (TriMesh.cpp:1393-1517) as the
+// initial cutting of a genus >= 1 mesh calls it (main.cpp:1397-1484): from a
+// boundary end, every interior edge of the path split on the boundary in
+// turn (cut through where both ends are on the boundary); for an interior
+// path, the interior cut of its first three vertices, then its remaining
+// edges split on the boundary.  Each operation is topo_apply on the faces
+// around the path vertices only (global vertex ids): those faces hold every
+// half-edge the operation reads (interior edge, boundary vertex, the walk
+// around a vertex), so a long path costs the faces it touches, not a
+// rebuild of the whole mesh per edge.  made: edges split on the boundary.
+int topo_cut_path(const int* path, int pathLen, std::vector<int>& F, std::vector<double>& Vrest,
+                  std::vector<double>& UV, std::vector<int>& cohE, int& made, std::string* err)
+{
+    made = 0;
+    const int nF = static_cast<int>(F.size() / 3);
+    std::vector<std::vector<int>> inc(Vrest.size() / 3);   // faces around each vertex
+    for (int t = 0; t < nF; ++t)
+        for (int k = 0; k < 3; ++k) inc[F[3 * (size_t)t + k]].push_back(t);
+    std::vector<int> nxt, prv;
+    auto around = [&](int v) {
+        nxt.clear();
+        prv.clear();
+        for (int t : inc[v]) {
+            const int* r = &F[3 * (size_t)t];
+            const int k = r[0] == v ? 0 : (r[1] == v ? 1 : 2);
+            nxt.push_back(r[(k + 1) % 3]);
+            prv.push_back(r[(k + 2) % 3]);
+        }
+    };
+    auto boundary = [&](int v) {   // TriMesh::isBoundaryVert: the fan does not close
+        around(v);
+        std::sort(nxt.begin(), nxt.end());
+        std::sort(prv.begin(), prv.end());
+        return nxt != prv;
+    };
+    auto interior_edge = [&](int a, int b) {
+        around(a);
+        return std::find(nxt.begin(), nxt.end(), b) != nxt.end() && std::find(prv.begin(), prv.end(), b) != prv.end();
+    };
+    auto apply_local = [&](int op, const int* p, int pl, const double* pos, int rows) -> int {
+        std::vector<int> faces;
+        for (int i = 0; i < pl; ++i) faces.insert(faces.end(), inc[p[i]].begin(), inc[p[i]].end());
+        std::sort(faces.begin(), faces.end());
+        faces.erase(std::unique(faces.begin(), faces.end()), faces.end());
+        std::vector<int> Fs(3 * faces.size());
+        for (size_t i = 0; i < faces.size(); ++i)
+            for (int k = 0; k < 3; ++k) Fs[3 * i + k] = F[3 * (size_t)faces[i] + k];
+        const int rc = topo_apply(op, p, pl, pos, rows, Fs, Vrest, UV, cohE, err);
+        if (rc) return rc;
+        inc.resize(Vrest.size() / 3);
+        for (size_t i = 0; i < faces.size(); ++i) {
+            const int t = faces[i];
+            for (int k = 0; k < 3; ++k) {
+                const int o = F[3 * (size_t)t + k], n = Fs[3 * i + k];
+                if (o == n) continue;
+                auto& lo = inc[o];
+                lo.erase(std::find(lo.begin(), lo.end(), t));
+                inc[n].push_back(t);
+                F[3 * (size_t)t + k] = n;
+            }
+        }
+        return OC_OK;
+    };
+    auto split_edges = [&](const int* vs, int n) -> int {
+        for (int i = 0; i + 1 < n; ++i) {
+            const int ab[2] = {vs[i], vs[i + 1]};
+            if (!interior_edge(ab[0], ab[1])) continue;
+            const int rows = (boundary(ab[0]) && boundary(ab[1])) ? 4 : 2;
+            double pos[8];
+            for (int r = 0; r < rows; ++r) {
+                pos[2 * r] = UV[2 * (size_t)ab[0]];
+                pos[2 * r + 1] = UV[2 * (size_t)ab[0] + 1];
+            }
+            const int rc = apply_local(kOpBoundarySplit, ab, 2, pos, rows);
+            if (rc) return rc;
+            ++made;
+        }
+        return OC_OK;
+    };
+    const int nV = static_cast<int>(Vrest.size() / 3);
+    if (pathLen < 2 || !path) {
+        if (err) *err = "cut path: fewer than two vertices";
+        return OC_ERR_INVALID;
+    }
+    for (int i = 0; i < pathLen; ++i)
+        if (path[i] < 0 || path[i] >= nV) {
+            if (err) *err = "cut path: vertex out of range";
+            return OC_ERR_INVALID;
+        }
+    std::vector<int> pth(path, path + pathLen);
+    if (boundary(pth.front()) || boundary(pth.back())) {
+        if (!boundary(pth.front())) std::reverse(pth.begin(), pth.end());   // start the cut from the boundary
+        return split_edges(pth.data(), pathLen);
+    }
+    if (pathLen < 3) {
+        if (err) *err = "cut path: an interior cut path needs three vertices";
+        return OC_ERR_INVALID;
+    }
+    const double pos[4] = {UV[2 * (size_t)pth[1]], UV[2 * (size_t)pth[1] + 1], UV[2 * (size_t)pth[1]],
+                           UV[2 * (size_t)pth[1] + 1]};
+    const int rc = apply_local(kOpInteriorSplit, pth.data(), 3, pos, 2);
+    if (rc) return rc;
+    return split_edges(pth.data() + 2, pathLen - 2);
+}
+
 int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, bool interior, double filterExp,
                           std::vector<int>& cands, int& pool)
 {

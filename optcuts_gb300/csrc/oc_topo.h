@@ -129,6 +129,12 @@ int mlp_predict_host(Mlp& m, const float* X, int n, float* y);
 int topo_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, std::vector<int>& F,
                std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err);
 
+// TriMesh::cutPath(path, makeCoh = true) as the initial cutting uses it:
+// boundary splits along the path (an interior path opened by the interior
+// cut of its first three vertices), on host arrays; made: edges split
+int topo_cut_path(const int* path, int pathLen, std::vector<int>& F, std::vector<double>& Vrest,
+                  std::vector<double>& UV, std::vector<int>& cohE, int& made, std::string* err);
+
 // the split filter alone (host): candidate vertices in the reference's order
 int topo_split_candidates(int nV, const int* F, int nF, const double* divGrad, bool interior, double filterExp,
                           std::vector<int>& cands, int& pool);

@@ -257,80 +257,17 @@ def cut_to_disk(F):
     return cuts
 
 
-class _Incidence:
-    """Faces around each vertex, kept up to date across topology operations
-    (they change a few faces' vertex ids and append vertices): whether an
-    edge is interior and whether a vertex is on the boundary
-    (TriMesh::isBoundaryVert) without rescanning the mesh."""
-
-    def __init__(self, F):
-        self.F = np.asarray(F, np.int32)
-        self.inc = {}
-        for t, row in enumerate(self.F.tolist()):
-            for v in row:
-                self.inc.setdefault(v, set()).add(t)
-
-    def update(self, F_new):
-        F_new = np.asarray(F_new, np.int32)
-        for t in np.nonzero(np.any(F_new != self.F, axis=1))[0].tolist():
-            for v in self.F[t].tolist():
-                self.inc[v].discard(t)
-            for v in F_new[t].tolist():
-                self.inc.setdefault(v, set()).add(t)
-        self.F = F_new
-
-    def _around(self, v):
-        nxt, prv = [], []
-        for t in self.inc.get(v, ()):
-            r = self.F[t].tolist()
-            k = r.index(v)
-            nxt.append(r[(k + 1) % 3])
-            prv.append(r[(k + 2) % 3])
-        return nxt, prv
-
-    def boundary(self, v):
-        nxt, prv = self._around(v)
-        return sorted(nxt) != sorted(prv)
-
-    def interior_edge(self, a, b):
-        nxt, prv = self._around(a)
-        return b in nxt and b in prv
-
-
 def cut_path(path, V_rest, UV, F, cohE):
     """TriMesh::cutPath(path, makeCoh = true) (TriMesh.cpp:1393-1517) as the
     initialisation calls it: from a boundary end, every interior edge of the
     path split on the boundary in turn (cut through where both of its ends
     are on the boundary); for an interior path, the interior cut of its
     first three vertices, then its remaining edges split on the boundary.
-    The operations are the library's (topology_apply).  Returns the new
-    arrays and the number of edges split."""
-    from optcuts_gb300 import OP_BOUNDARY_SPLIT, OP_INTERIOR_SPLIT, topology_apply
-    path = [int(v) for v in path]
-    made = 0
-    inc = _Incidence(F)
-
-    def split_edges(vs, V_rest, UV, F, cohE, made):
-        for a, b in zip(vs[:-1], vs[1:]):
-            if not inc.interior_edge(a, b):
-                continue
-            rows = 4 if (inc.boundary(a) and inc.boundary(b)) else 2
-            V_rest, UV, F, cohE = topology_apply(OP_BOUNDARY_SPLIT, [a, b], np.repeat(UV[[a]], rows, axis=0),
-                                                 V_rest, UV, F, cohE)
-            inc.update(F)
-            made += 1
-        return V_rest, UV, F, cohE, made
-
-    if inc.boundary(path[0]) or inc.boundary(path[-1]):
-        if not inc.boundary(path[0]):
-            path = path[::-1]   # always start the cut from the boundary
-        return split_edges(path, V_rest, UV, F, cohE, made)
-    if len(path) < 3:
-        raise ValueError("an interior cut path needs three vertices")
-    V_rest, UV, F, cohE = topology_apply(OP_INTERIOR_SPLIT, path[:3], np.repeat(UV[[path[1]]], 2, axis=0),
-                                         V_rest, UV, F, cohE)
-    inc.update(F)
-    return split_edges(path[2:], V_rest, UV, F, cohE, made)
+    The library's topology operations, applied by topology_cut_path on the
+    faces around each edge.  Returns the new arrays and the number of edges
+    split."""
+    from optcuts_gb300 import topology_cut_path
+    return topology_cut_path([int(v) for v in path], V_rest, UV, F, cohE)
 
 
 def cut_high_genus(V, F):

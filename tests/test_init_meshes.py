@@ -33,6 +33,70 @@ def test_cut_to_disk_on_a_torus():
     assert I.euler_characteristic(Vc, Fc) == 1 and len(I.boundary_loop(Fc)) > 0
 
 
+def _cut_path_edge_by_edge(path, V_rest, UV, F, cohE):
+    """cutPath as a loop of single operations on the whole mesh (each one
+    topology_apply, pinned against the reference's splitEdgeOnBoundary and
+    cutPath): the sequence topology_cut_path applies on local faces."""
+    import optcuts_gb300 as oc
+
+    def fan(F, v):
+        rows = F[np.any(F == v, axis=1)]
+        k = np.argmax(rows == v, axis=1)
+        return rows[np.arange(len(rows)), (k + 1) % 3], rows[np.arange(len(rows)), (k + 2) % 3]
+
+    def boundary(F, v):
+        nxt, prv = fan(F, v)
+        return sorted(nxt.tolist()) != sorted(prv.tolist())
+
+    def interior_edge(F, a, b):
+        nxt, prv = fan(F, a)
+        return b in nxt and b in prv
+
+    def split_edges(vs, V_rest, UV, F, cohE, made):
+        for a, b in zip(vs[:-1], vs[1:]):
+            if not interior_edge(F, a, b):
+                continue
+            rows = 4 if (boundary(F, a) and boundary(F, b)) else 2
+            V_rest, UV, F, cohE = oc.topology_apply(oc.OP_BOUNDARY_SPLIT, [a, b], np.repeat(UV[[a]], rows, axis=0),
+                                                    V_rest, UV, F, cohE)
+            made += 1
+        return V_rest, UV, F, cohE, made
+
+    path = [int(v) for v in path]
+    if boundary(F, path[0]) or boundary(F, path[-1]):
+        if not boundary(F, path[0]):
+            path = path[::-1]
+        return split_edges(path, V_rest, UV, F, cohE, 0)
+    V_rest, UV, F, cohE = oc.topology_apply(oc.OP_INTERIOR_SPLIT, path[:3], np.repeat(UV[[path[1]]], 2, axis=0),
+                                            V_rest, UV, F, cohE)
+    return split_edges(path[2:], V_rest, UV, F, cohE, 0)
+
+
+def test_cut_path_equals_single_operations():
+    """topology_cut_path (each edge on the faces around it) leaves the same
+    arrays as the same operations applied one by one to the whole mesh, for
+    every path the initial cutting of a torus takes."""
+    V, F = M.torus(40, 32)
+    calls = []
+    orig = I.cut_path
+
+    def record(path, V_rest, UV, F, cohE):
+        out = orig(path, V_rest, UV, F, cohE)
+        calls.append(((list(path), V_rest, UV, F, cohE), out))
+        return out
+
+    I.cut_path = record
+    try:
+        I.cut_high_genus(V, F)
+    finally:
+        I.cut_path = orig
+    assert len(calls) >= 2 and any(out[4] > 0 for _, out in calls)
+    for args, out in calls:
+        ref = _cut_path_edge_by_edge(*args)
+        for a, b in zip(out, ref):
+            np.testing.assert_array_equal(np.asarray(a), np.asarray(b))
+
+
 def test_torus_41k_initialises():
     """The genus-1 41k-triangle torus (the plain-method configuration) gets
     a valid start: a disk whose Tutte map inverts no triangle."""
