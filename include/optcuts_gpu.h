@@ -417,6 +417,14 @@ int oc_topology_apply(int opType, const int* path, int pathLen, const double* ne
 int oc_topology_cut_path(const int* path, int pathLen, int nV, int nF, const int* F, const double* Vrest,
                          const double* UV, int nCohE, const int* cohE, int* F_out, double* Vrest_out, double* UV_out,
                          int* cohE_out, int* nV_out, int* nCohE_out, int* nSplit);
+/* host only: igl::cut_to_disk as the reference vendors it
+ * (src/Utils/cut_to_disk.cpp; called at main.cpp:1429): the cut graph of a
+ * genus >= 1 surface, cut i = cutVerts[cutOff[i] .. cutOff[i + 1]) (a closed
+ * loop repeats its first vertex).  With cutVerts or cutOff NULL only
+ * *nCuts and *nVerts are set; else capCuts >= *nCuts + 1 and
+ * capVerts >= *nVerts are required */
+int oc_cut_to_disk(const int* F, int nF, int* cutVerts, int capVerts, int* cutOff, int capCuts, int* nCuts,
+                   int* nVerts);
 /* host only: the split filter's candidate vertices, in order */
 int oc_topology_split_candidates(int nV, const int* F, int nF, const double* divGrad, int interior, double filterExp,
                                  int* cands, int* nCands, int* pool);

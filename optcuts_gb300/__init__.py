@@ -119,6 +119,7 @@ _SIGS = {
     "oc_mesh_get_topology": [_vp, _i, _i, _i, _i, _d, _i],
     "oc_topology_apply": [ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d,
                           ctypes.c_int, _i, _i, _d, _d, _i, _i, _i],
+    "oc_cut_to_disk": [_i, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, _i, _i],
     "oc_topology_cut_path": [_i, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i, _d, _d, ctypes.c_int, _i, _i, _d, _d,
                              _i, _i, _i, _i],
     "oc_topology_query_learned": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
@@ -555,6 +556,24 @@ def topology_apply(op, path, newVertPos, V_rest, UV, F, cohE):
     if rc != OC_OK:
         raise OCError(rc, "topology_apply")
     return Vo[:nvo.value], Uo[:nvo.value], Fo, Co[:nco.value]
+
+
+def cut_to_disk(F):
+    """Host-only igl::cut_to_disk as the reference vendors it: the cut graph
+    of a genus >= 1 surface as vertex lists (a closed loop repeats its first
+    vertex)."""
+    F = _i4(F)
+    nc, nv = ctypes.c_int(), ctypes.c_int()
+    rc = lib().oc_cut_to_disk(_pi(F), len(F), None, 0, None, 0, ctypes.byref(nc), ctypes.byref(nv))
+    if rc != OC_OK:
+        raise OCError(rc, "cut_to_disk")
+    verts = np.zeros(max(nv.value, 1), np.int32)
+    off = np.zeros(nc.value + 1, np.int32)
+    rc = lib().oc_cut_to_disk(_pi(F), len(F), _pi(verts), len(verts), _pi(off), len(off), ctypes.byref(nc),
+                              ctypes.byref(nv))
+    if rc != OC_OK:
+        raise OCError(rc, "cut_to_disk")
+    return [verts[off[i]:off[i + 1]].tolist() for i in range(nc.value)]
 
 
 def topology_cut_path(path, V_rest, UV, F, cohE):

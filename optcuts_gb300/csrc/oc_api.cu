@@ -1135,6 +1135,30 @@ int oc_topology_cut_path(const int* path, int pathLen, int nV, int nF, const int
     return OC_OK;
 }
 
+int oc_cut_to_disk(const int* F, int nF, int* cutVerts, int capVerts, int* cutOff, int capCuts, int* nCuts,
+                   int* nVerts)
+{
+    if (nF < 0 || (nF && !F) || !nCuts || !nVerts) return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0) return OC_ERR_INVALID;
+    std::vector<std::vector<int>> cuts;
+    oc::topo_cut_to_disk(F, nF, cuts);
+    long long total = 0;
+    for (const auto& c : cuts) total += static_cast<long long>(c.size());
+    *nCuts = static_cast<int>(cuts.size());
+    *nVerts = static_cast<int>(total);
+    if (!cutVerts || !cutOff) return OC_OK;   // sizes only
+    if (capCuts < *nCuts + 1 || capVerts < total) return OC_ERR_INVALID;
+    int o = 0;
+    cutOff[0] = 0;
+    for (size_t i = 0; i < cuts.size(); ++i) {
+        std::copy(cuts[i].begin(), cuts[i].end(), cutVerts + o);
+        o += static_cast<int>(cuts[i].size());
+        cutOff[i + 1] = o;
+    }
+    return OC_OK;
+}
+
 int oc_topo_result_destroy(oc_topo_result* r)
 {
     if (!r) return OC_ERR_INVALID;

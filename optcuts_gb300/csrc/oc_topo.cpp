@@ -14,6 +14,8 @@
 #include "oc_mlp.h"
 
 #include <algorithm>
+#include <deque>
+#include <unordered_map>
 #include <cfloat>
 #include <chrono>
 #include <cmath>
@@ -722,6 +724,154 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
         return OC_OK;
     }
     return bad("topology op: unknown operation");
+}
+
+// The cut graph of a surface of genus >= 1 (igl::cut_to_disk as vendored in
+// src/Utils/cut_to_disk.cpp), as the reference's initialisation uses it:
+// 1. edges numbered in (min, max) vertex order; faces peeled from each not
+//    yet deleted face outwards, a face deleted through an interior edge with
+//    exactly one deleted neighbour (a breadth-first queue of such edges);
+// 2. degree-1 vertices of the remaining edge graph pruned repeatedly (a
+//    queue seeded with the vertices in index order);
+// 3. the remaining edges walked into cycles (a walk meeting its own vertex:
+//    the loop from that vertex, closed) or, after a dead end and a walk the
+//    other way from the reversed list, chains.  The vertex-position map of
+//    the first walk is kept across the reversal, as in the source.
+// cuts: vertex lists (a closed loop repeats its first vertex).
+void topo_cut_to_disk(const int* F, int nF, std::vector<std::vector<int>>& cuts)
+{
+    cuts.clear();
+    if (nF <= 0) return;
+    // edges in (min, max) order; faces of each edge in face-corner order
+    std::vector<std::pair<long long, int>> he(3 * (size_t)nF);   // (key, corner)
+    for (int i = 0; i < nF; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const long long a = F[3 * (size_t)i + j], b = F[3 * (size_t)i + (j + 1) % 3];
+            he[3 * (size_t)i + j] = {(std::min(a, b) << 32) | std::max(a, b), 3 * i + j};
+        }
+    std::sort(he.begin(), he.end());
+    std::vector<int> evA, evB, ef0, ef1, fe(3 * (size_t)nF);
+    std::vector<char> bndE;
+    for (size_t k = 0; k < he.size();) {
+        size_t l = k;
+        while (l < he.size() && he[l].first == he[k].first) ++l;
+        const int e = static_cast<int>(evA.size());
+        evA.push_back(static_cast<int>(he[k].first >> 32));
+        evB.push_back(static_cast<int>(he[k].first & 0xffffffffLL));
+        ef0.push_back(he[k].second / 3);
+        ef1.push_back(l - k > 1 ? he[k + 1].second / 3 : -1);
+        bndE.push_back(l - k == 1);
+        for (size_t t = k; t < l; ++t) fe[he[t].second] = e;
+        k = l;
+    }
+    const int nE = static_cast<int>(evA.size());
+    std::vector<char> delF(nF, 0), delE(nE, 0);
+    auto nDel = [&](int e) { return delF[ef0[e]] + delF[ef1[e]]; };
+    std::deque<int> q;
+    for (int face = 0; face < nF; ++face) {
+        if (delF[face]) continue;
+        delF[face] = 1;
+        for (int j = 0; j < 3; ++j) {
+            const int e = fe[3 * (size_t)face + j];
+            if (!bndE[e] && nDel(e) == 1) q.push_back(e);
+        }
+        while (!q.empty()) {
+            const int e = q.front();
+            q.pop_front();
+            int todel = nF;
+            if (!delF[ef0[e]]) todel = ef0[e];
+            if (!delF[ef1[e]]) todel = ef1[e];
+            if (todel == nF) continue;
+            delE[e] = 1;
+            delF[todel] = 1;
+            for (int j = 0; j < 3; ++j) {
+                const int e2 = fe[3 * (size_t)todel + j];
+                if (!bndE[e2] && nDel(e2) == 1) q.push_back(e2);
+            }
+        }
+    }
+    // prune the spines
+    std::vector<int> left;
+    for (int e = 0; e < nE; ++e)
+        if (!delE[e]) left.push_back(e);
+    int nV = 0;
+    for (long long i = 0; i < 3LL * nF; ++i) nV = std::max(nV, F[i] + 1);
+    std::vector<std::vector<int>> vertEdges(nV);
+    for (int e : left) {
+        vertEdges[evA[e]].push_back(e);
+        vertEdges[evB[e]].push_back(e);
+    }
+    std::vector<int> nbs(nV);
+    for (int v = 0; v < nV; ++v) nbs[v] = static_cast<int>(vertEdges[v].size());
+    std::fill(delE.begin(), delE.end(), 0);
+    for (int v = 0; v < nV; ++v)
+        if (vertEdges[v].size() == 1) q.push_back(v);
+    while (!q.empty()) {
+        const int v = q.front();
+        q.pop_front();
+        for (int e : vertEdges[v]) {
+            if (delE[e]) continue;
+            delE[e] = 1;
+            for (int w : {evA[e], evB[e]})
+                if (--nbs[w] == 1) q.push_back(w);
+        }
+    }
+    std::vector<int> loop;
+    for (int e : left)
+        if (!delE[e]) loop.push_back(e);
+    if (loop.empty()) return;
+    std::vector<std::vector<int>> loopVE(nV);
+    for (int e : loop) {
+        loopVE[evA[e]].push_back(e);
+        loopVE[evB[e]].push_back(e);
+    }
+    std::vector<char> used(nE, 0);
+    std::vector<int> verts, edges;
+    std::unordered_map<int, int> pos;
+    auto walk = [&](int cur, int cure) {   // true when a cycle closes
+        while (cur != -1) {
+            int nxt = -1, nxe = -1;
+            for (int c : loopVE[cur])
+                if (!used[c] && c != cure) {
+                    nxt = cur == evA[c] ? evB[c] : evA[c];
+                    nxe = c;
+                    break;
+                }
+            if (nxt != -1) {
+                auto it = pos.find(nxt);
+                if (it != pos.end()) {
+                    const int i0 = it->second;
+                    std::vector<int> cut(verts.begin() + i0, verts.end());
+                    cut.push_back(nxt);
+                    cuts.push_back(std::move(cut));
+                    for (size_t i = i0; i < edges.size(); ++i) used[edges[i]] = 1;
+                    used[nxe] = 1;
+                    return true;
+                }
+                pos[nxt] = static_cast<int>(verts.size());
+                verts.push_back(nxt);
+                edges.push_back(nxe);
+            }
+            cur = nxt;
+            cure = nxe;
+        }
+        return false;
+    };
+    for (int e : loop) {
+        while (!used[e]) {
+            verts = {evA[e], evB[e]};
+            edges = {e};
+            pos.clear();
+            pos[verts[0]] = 0;
+            pos[verts[1]] = 1;
+            if (walk(evB[e], e)) continue;
+            std::reverse(verts.begin(), verts.end());
+            std::reverse(edges.begin(), edges.end());
+            if (walk(verts.back(), edges.back())) continue;
+            cuts.push_back(verts);
+            for (int x : edges) used[x] = 1;
+        }
+    }
 }
 
 // TriMesh::cutPath(path, makeCoh = true) (TriMesh.cpp:1393-1517) as the

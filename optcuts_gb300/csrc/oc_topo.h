@@ -129,6 +129,11 @@ int mlp_predict_host(Mlp& m, const float* X, int n, float* y);
 int topo_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, std::vector<int>& F,
                std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err);
 
+// igl::cut_to_disk as the reference vendors it (src/Utils/cut_to_disk.cpp):
+// the cut graph of a genus >= 1 surface as vertex lists (a closed loop
+// repeats its first vertex), host only
+void topo_cut_to_disk(const int* F, int nF, std::vector<std::vector<int>>& cuts);
+
 // TriMesh::cutPath(path, makeCoh = true) as the initial cutting uses it:
 // boundary splits along the path (an interior path opened by the interior
 // cut of its first three vertices), on host arrays; made: edges split

@@ -150,111 +150,13 @@ def cut_to_disk(F):
     Returns the cuts as vertex lists (a closed loop repeats its first
     vertex).  Step 3 keeps the source's vertex-position map across the
     reversal, so a cycle found on the second walk is read from the reversed
-    list with the first walk's positions; the same happens here."""
+    list with the first walk's positions.  Computed on the host by the
+    library (oc_cut_to_disk)."""
+    from optcuts_gb300 import cut_to_disk as lib_cut_to_disk
     F = np.asarray(F)
-    nf = len(F)
-    if nf == 0:
+    if len(F) == 0:
         return []
-    edges = {}
-    for i in range(nf):
-        for j in range(3):
-            v0, v1 = int(F[i, j]), int(F[i, (j + 1) % 3])
-            edges.setdefault((min(v0, v1), max(v0, v1)), []).append(i)
-    keys = sorted(edges)
-    eidx = {k: n for n, k in enumerate(keys)}
-    ev = [k for k in keys]
-    ef = [(edges[k][0], edges[k][1] if len(edges[k]) > 1 else -1) for k in keys]
-    bnd_e = {n for n, k in enumerate(keys) if len(edges[k]) == 1}
-    fe = [[eidx[(min(int(F[i, j]), int(F[i, (j + 1) % 3])), max(int(F[i, j]), int(F[i, (j + 1) % 3])))]
-           for j in range(3)] for i in range(nf)]
-    deleted = [False] * nf
-    deleted_e = set()
-
-    def n_deleted(e):
-        return int(deleted[ef[e][0]]) + int(deleted[ef[e][1]])
-
-    from collections import deque
-    for face in range(nf):
-        if deleted[face]:
-            continue
-        deleted[face] = True
-        q = deque(e for e in fe[face] if e not in bnd_e and n_deleted(e) == 1)
-        while q:
-            e = q.popleft()
-            todel = nf
-            if not deleted[ef[e][0]]:
-                todel = ef[e][0]
-            if not deleted[ef[e][1]]:
-                todel = ef[e][1]
-            if todel != nf:
-                deleted_e.add(e)
-                deleted[todel] = True
-                q.extend(e2 for e2 in fe[todel] if e2 not in bnd_e and n_deleted(e2) == 1)
-    left = [e for e in range(len(keys)) if e not in deleted_e]
-    # prune spines
-    deleted_e = set()
-    vert_edges = {}
-    for e in left:
-        vert_edges.setdefault(ev[e][0], []).append(e)
-        vert_edges.setdefault(ev[e][1], []).append(e)
-    nbs = {v: len(es) for v, es in vert_edges.items()}
-    q = deque(v for v in sorted(vert_edges) if len(vert_edges[v]) == 1)
-    while q:
-        v = q.popleft()
-        for e in vert_edges[v]:
-            if e in deleted_e:
-                continue
-            deleted_e.add(e)
-            for w in ev[e]:
-                nbs[w] -= 1
-                if nbs[w] == 1:
-                    q.append(w)
-    loop = [e for e in left if e not in deleted_e]
-    if not loop:
-        return []
-    loop_vert_edges = {}
-    for e in loop:
-        loop_vert_edges.setdefault(ev[e][0], []).append(e)
-        loop_vert_edges.setdefault(ev[e][1], []).append(e)
-    used = set()
-    cuts = []
-
-    def walk(verts, edges_, pos, cur, cure):
-        """Extends verts / edges_ from cur; returns True when a cycle closes."""
-        while cur != -1:
-            nxt, nxe = -1, -1
-            for c in loop_vert_edges.get(cur, []):
-                if c not in used and c != cure:
-                    nxt = ev[c][1] if cur == ev[c][0] else ev[c][0]
-                    nxe = c
-                    break
-            if nxt != -1:
-                if nxt in pos:
-                    i0 = pos[nxt]
-                    cuts.append(verts[i0:] + [nxt])
-                    used.update(edges_[i0:])
-                    used.add(nxe)
-                    return True
-                pos[nxt] = len(verts)
-                verts.append(nxt)
-                edges_.append(nxe)
-            cur, cure = nxt, nxe
-        return False
-
-    for e in loop:
-        while e not in used:
-            verts = [ev[e][0], ev[e][1]]
-            edges_ = [e]
-            pos = {verts[0]: 0, verts[1]: 1}
-            if walk(verts, edges_, pos, ev[e][1], e):
-                continue
-            verts.reverse()
-            edges_.reverse()
-            if walk(verts, edges_, pos, verts[-1], edges_[-1]):
-                continue
-            cuts.append(list(verts))
-            used.update(edges_)
-    return cuts
+    return lib_cut_to_disk(F)
 
 
 def cut_path(path, V_rest, UV, F, cohE):
