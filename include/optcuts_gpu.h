@@ -99,6 +99,7 @@ int oc_sd_hessian_blocks(oc_mesh* mesh, int uniformWeight, double* blocks);
  * converge far more slowly from such starts.  Where no element is stiff the
  * three forms agree to rounding. */
 enum { OC_HESSIAN_REDUCED = 0, OC_HESSIAN_JACOBI6 = 1, OC_HESSIAN_HYBRID = 2 };
+enum { OC_ORDER_AUTO = 0, OC_ORDER_BFS = 1 };
 /* oc_sd_hessian_blocks with the projection chosen */
 int oc_sd_hessian_blocks_projected(oc_mesh* mesh, int uniformWeight, int projection, double* blocks);
 /* SymDirichletEnergy::initStepSize (SymDirichletEnergy.cpp:551-610): lowers
@@ -150,6 +151,11 @@ int oc_linsys_stats(oc_linsys* ls, double* out8);
 /* The same symbolic analysis without any device call (host only). */
 int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
                           double* out8);
+/* the same with the geometric nested dissection: vertex coordinates xy
+ * (nV x 2) bisected at the median along the longer extent (the ordering the
+ * optimizer uses for a scaffold's full pattern) */
+int oc_chol_analyze_stats_xy(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
+                             const double* xy, double* out8);
 /* Its vertex elimination order (nV entries), host only. */
 int oc_chol_analyze_order(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
                           int* vertexOrder);
@@ -193,6 +199,10 @@ typedef struct {
                              connectivity changes) */
     int hessianProjection; /* OC_HESSIAN_JACOBI6 (default), OC_HESSIAN_REDUCED or
                               OC_HESSIAN_HYBRID */
+    int ordering;         /* direct solver's nested dissection: OC_ORDER_AUTO
+                             (default: at every node the smaller balanced
+                             separator of a BFS level set and a bisection of
+                             the current UV positions) or OC_ORDER_BFS */
 } oc_optimizer_config;
 
 int oc_optimizer_default_config(oc_optimizer_config* cfg);

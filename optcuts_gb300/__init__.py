@@ -46,12 +46,13 @@ _vp = ctypes.c_void_p
 class OptimizerConfig(ctypes.Structure):
     _fields_ = [("pcgTol", ctypes.c_double), ("pcgMaxIter", ctypes.c_int), ("relGL2Tol", ctypes.c_double),
                 ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int), ("linearSolver", ctypes.c_int),
-                ("scaffoldPattern", ctypes.c_int), ("hessianProjection", ctypes.c_int)]
+                ("scaffoldPattern", ctypes.c_int), ("hessianProjection", ctypes.c_int), ("ordering", ctypes.c_int)]
 
 
 SOLVER_DIRECT = 0
 SOLVER_PCG = 1
 HESSIAN_REDUCED, HESSIAN_JACOBI6, HESSIAN_HYBRID = 0, 1, 2
+ORDER_AUTO, ORDER_BFS = 0, 1
 OP_BOUNDARY_SPLIT, OP_INTERIOR_SPLIT, OP_MERGE = 0, 1, 2
 
 
@@ -78,6 +79,7 @@ _SIGS = {
     "oc_linsys_analyze_pattern": [_vp],
     "oc_linsys_stats": [_vp, _d],
     "oc_chol_analyze_stats": [ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_int, _d],
+    "oc_chol_analyze_stats_xy": [ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_int, _d, _d],
     "oc_linsys_set_pattern": [_vp, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int],
     "oc_linsys_update_a": [_vp, _i, _i, _d, ctypes.c_int],
     "oc_linsys_factorize": [_vp],
@@ -614,11 +616,21 @@ def symbolic_stats_dict(out):
     return dict(zip(keys, [float(x) for x in out]))
 
 
-def chol_analyze_stats(nV, F, fixedVert=(0,), leafSize=16):
-    """Symbolic analysis of the direct solver, host only (no GPU needed)."""
+def chol_analyze_stats(nV, F, fixedVert=(0,), leafSize=16, xy=None):
+    """Symbolic analysis of the direct solver, host only (no GPU needed);
+    with vertex coordinates xy (nV x 2) the geometric nested dissection."""
     F = _i4(F)
     fx = _i4(np.asarray(fixedVert).reshape(-1))
     out = np.zeros(8)
+    if xy is not None:
+        xy = _f8(xy).reshape(-1, 2)
+        if len(xy) != nV:
+            raise ValueError("xy: one row per vertex")
+        rc = lib().oc_chol_analyze_stats_xy(int(nV), _pi(F), len(F), _pi(fx), len(fx), int(leafSize), _pd(xy),
+                                            _pd(out))
+        if rc != OC_OK:
+            raise OCError(rc, "oc_chol_analyze_stats_xy")
+        return symbolic_stats_dict(out)
     rc = lib().oc_chol_analyze_stats(int(nV), _pi(F), len(F), _pi(fx), len(fx), int(leafSize), _pd(out))
     if rc != OC_OK:
         raise OCError(rc, "oc_chol_analyze_stats")

@@ -413,7 +413,8 @@ void free_bsr(oc::DeviceBsr& b)
 }
 
 int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::vector<unsigned char>& mask,
-                       const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr)
+                       const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr,
+                       const double* xy = nullptr)
 {
     oc_ctx* ctx = ls->ctx;
     auto t = std::chrono::steady_clock::now();
@@ -459,7 +460,7 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
         // analyze_pattern (EigenLibSolver.cpp:71-77): symbolic factorisation;
         // a clique (scaffold boundary + air vertices) is eliminated last
         ls->patternDevMs += ms_since(t);
-        oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique);
+        oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique, xy);
         ls->patternHostMs += ms_since(t);
         std::string err;
         int rc = oc::chol_upload(ls->chol, &err);
@@ -1228,6 +1229,12 @@ int oc_linsys_stats(oc_linsys* ls, double* out8)
 
 int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize, double* out8)
 {
+    return oc_chol_analyze_stats_xy(nV, F, nF, fixedVert, nFixed, leafSize, nullptr, out8);
+}
+
+int oc_chol_analyze_stats_xy(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
+                             const double* xy, double* out8)
+{
     if (nV <= 0 || nF < 0 || (nF && !F) || nFixed < 0 || (nFixed && !fixedVert) || !out8) return OC_ERR_INVALID;
     for (long long i = 0; i < 3LL * nF; ++i)
         if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
@@ -1239,7 +1246,7 @@ int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, in
     std::vector<int> rowPtr, col, diagSlot, cPtr, cIdx;
     build_pattern(nV, F, nF, mask, rowPtr, col, diagSlot, cPtr, cIdx);
     oc::CholPlan P;
-    oc::chol_analyze(P, nV, rowPtr.data(), col.data(), leafSize > 0 ? leafSize : 16);
+    oc::chol_analyze(P, nV, rowPtr.data(), col.data(), leafSize > 0 ? leafSize : 16, nullptr, xy);
     chol_stats(P, out8);
     return P.valid ? OC_OK : OC_ERR_INVALID;
 }
@@ -1376,6 +1383,7 @@ int oc_optimizer_default_config(oc_optimizer_config* c)
     c->linearSolver = OC_SOLVER_DIRECT;
     c->scaffoldPattern = 0;
     c->hessianProjection = OC_HESSIAN_JACOBI6;
+    c->ordering = OC_ORDER_AUTO;
     return OC_OK;
 }
 
@@ -1405,6 +1413,7 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
     if (o->cfg.linearSolver != OC_SOLVER_PCG) o->cfg.linearSolver = OC_SOLVER_DIRECT;
     if (o->cfg.hessianProjection < OC_HESSIAN_REDUCED || o->cfg.hessianProjection > OC_HESSIAN_HYBRID)
         o->cfg.hessianProjection = OC_HESSIAN_JACOBI6;
+    if (o->cfg.ordering != OC_ORDER_BFS) o->cfg.ordering = OC_ORDER_AUTO;
     if (rc == OC_OK) rc = oc_linsys_create(ctx, &o->ls);
     if (rc == OC_OK) rc = oc_linsys_set_type(o->ls, o->cfg.linearSolver);
     if (rc == OC_OK && o->cfg.timing)
@@ -1501,10 +1510,20 @@ static int ensure_pattern(oc_optimizer* o)
     const int nV = m->d.nV;
     if (o->patternStale) {
         int rc;
+        // current positions of the system's vertices: the ordering's
+        // geometric bisection reads them
+        const int nXY = o->cfg.ordering == OC_ORDER_BFS ? 0 : (o->scaf ? o->nWhole : nV);
+        std::vector<double> xy(2 * (size_t)nXY);
+        if (nXY) {
+            OC_CUDA(m->ctx, cudaMemcpyAsync(xy.data(), o->scaf ? o->wuv : m->d.uv, sizeof(double2) * nXY,
+                                            cudaMemcpyDeviceToHost, m->ctx->stream));
+            OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
+        }
+        const double* xyp = nXY ? xy.data() : nullptr;
         if (!o->scaf) {
             std::vector<unsigned char> mask(nV, 0);
             for (int v : m->fixed) mask[v] = 1;
-            rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask);
+            rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask, nullptr, 0, nullptr, xyp);
         }
         else {
             // rowFixed: 1 = fixed mesh vertex or unused air slot, 2 = fixed in
@@ -1518,11 +1537,11 @@ static int ensure_pattern(oc_optimizer* o)
             if (o->cliqueMode) {
                 std::vector<int> clique(o->bnd);
                 for (int v = nV; v < o->nWhole; ++v) clique.push_back(v);
-                rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, nullptr, 0, &clique);
+                rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, nullptr, 0, &clique, xyp);
             }
             else {
                 rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, o->airFw.data(),
-                                        static_cast<int>(o->airFw.size() / 3));
+                                        static_cast<int>(o->airFw.size() / 3), nullptr, xyp);
             }
         }
         if (rc) return rc;

@@ -58,65 +58,124 @@ constexpr size_t kNdParallel = 4096;
 
 void nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::vector<int>& tag,
               std::atomic<int>& tagCounter, std::vector<int>& level, std::vector<NdNode>& nodes, int leafSize,
-              int depth)
+              int depth, const double* xy)
 {
     const int myTag = ++tagCounter;
     for (int v : verts) tag[v] = myTag;
     auto make_leaf = [&]() { nodes.push_back(NdNode{verts, {}}); };
     if ((int)verts.size() <= leafSize) return make_leaf();
-    // two BFS passes: the second starts at the last vertex reached by the first
-    std::vector<int> q;
-    q.reserve(verts.size());
-    auto bfs = [&](int s) {
-        q.clear();
-        for (int v : verts) level[v] = -1;
-        level[s] = 0;
-        q.push_back(s);
-        for (size_t h = 0; h < q.size(); ++h) {
-            const int v = q[h];
-            for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p) {
-                const int u = col[p];
-                if (tag[u] == myTag && level[u] < 0) {
-                    level[u] = level[v] + 1;
-                    q.push_back(u);
+    std::vector<int> left, right, sep;
+    // BFS level sets: two passes, the second from the last vertex the first
+    // reached; the separator is the level holding the median vertex.
+    // false when the set is too shallow to split
+    auto bfs_split = [&](std::vector<int>& L, std::vector<int>& R, std::vector<int>& S) {
+        std::vector<int> q;
+        q.reserve(verts.size());
+        auto bfs = [&](int s0) {
+            q.clear();
+            for (int v : verts) level[v] = -1;
+            level[s0] = 0;
+            q.push_back(s0);
+            for (size_t h = 0; h < q.size(); ++h) {
+                const int v = q[h];
+                for (int p = rowPtr[v]; p < rowPtr[v + 1]; ++p) {
+                    const int u = col[p];
+                    if (tag[u] == myTag && level[u] < 0) {
+                        level[u] = level[v] + 1;
+                        q.push_back(u);
+                    }
                 }
             }
+        };
+        bfs(verts[0]);
+        bfs(q.back());
+        const int reached = static_cast<int>(q.size());
+        const int maxLevel = level[q.back()];
+        if (maxLevel < 2) return false;
+        std::vector<int> cnt(maxLevel + 1, 0);
+        for (int i = 0; i < reached; ++i) cnt[level[q[i]]]++;
+        const int total = static_cast<int>(verts.size());
+        int sepLevel = 1, cum = 0;
+        for (int l = 0; l <= maxLevel; ++l) {
+            cum += cnt[l];
+            if (2 * cum >= total) { sepLevel = l; break; }
+        }
+        sepLevel = std::max(1, std::min(sepLevel, maxLevel - 1));
+        for (int v : verts) {
+            const int l = level[v];
+            if (l < 0 || l > sepLevel) R.push_back(v);
+            else if (l < sepLevel) L.push_back(v);
+            else S.push_back(v);
+        }
+        return true;
+    };
+    // geometric bisection at the median along the longer extent: the lower
+    // half's vertices with a neighbour in the upper half are the separator
+    auto geo_split = [&](std::vector<int>& L, std::vector<int>& R, std::vector<int>& S) {
+        double lo[2] = {xy[2 * (size_t)verts[0]], xy[2 * (size_t)verts[0] + 1]}, hi[2] = {lo[0], lo[1]};
+        for (int v : verts)
+            for (int a = 0; a < 2; ++a) {
+                lo[a] = std::min(lo[a], xy[2 * (size_t)v + a]);
+                hi[a] = std::max(hi[a], xy[2 * (size_t)v + a]);
+            }
+        const int ax = (hi[0] - lo[0]) >= (hi[1] - lo[1]) ? 0 : 1;
+        std::vector<int> byCoord(verts);
+        const size_t half = byCoord.size() / 2;
+        std::nth_element(byCoord.begin(), byCoord.begin() + half, byCoord.end(), [&](int a, int b) {
+            const double xa = xy[2 * (size_t)a + ax], xb = xy[2 * (size_t)b + ax];
+            return xa < xb || (xa == xb && a < b);
+        });
+        for (size_t i = 0; i < byCoord.size(); ++i) level[byCoord[i]] = i < half ? 0 : 1;
+        for (int v : verts) {
+            if (level[v] == 1) {
+                R.push_back(v);
+                continue;
+            }
+            bool cut = false;
+            for (int p = rowPtr[v]; p < rowPtr[v + 1] && !cut; ++p) {
+                const int u = col[p];
+                cut = tag[u] == myTag && level[u] == 1;
+            }
+            (cut ? S : L).push_back(v);
+        }
+        if (S.empty() && !L.empty()) {   // halves not connected here: one vertex as the separator
+            S.push_back(L.back());
+            L.pop_back();
         }
     };
-    bfs(verts[0]);
-    bfs(q.back());
-    const int reached = static_cast<int>(q.size());
-    const int maxLevel = level[q.back()];
-    if (maxLevel < 2) return make_leaf();
-    std::vector<int> cnt(maxLevel + 1, 0);
-    for (int i = 0; i < reached; ++i) cnt[level[q[i]]]++;
-    const int total = static_cast<int>(verts.size());
-    int sepLevel = 1, cum = 0;
-    for (int l = 0; l <= maxLevel; ++l) {
-        cum += cnt[l];
-        if (2 * cum >= total) { sepLevel = l; break; }
+    // with coordinates, the smaller of the two separators among the
+    // balanced splits (neither side above 70% of the rest); BFS alone without
+    std::vector<int> gl, gr, gs;
+    if (xy) geo_split(gl, gr, gs);
+    const bool bfsOk = bfs_split(left, right, sep);
+    if (xy) {
+        auto balanced = [](const std::vector<int>& L, const std::vector<int>& R) {
+            const size_t n = L.size() + R.size();
+            return 10 * std::max(L.size(), R.size()) <= 7 * n;
+        };
+        const bool gb = balanced(gl, gr), bb = bfsOk && balanced(left, right);
+        const bool useGeo = !bfsOk || (gb && !bb) || (gb == bb && gs.size() < sep.size());
+        if (useGeo) {
+            left.swap(gl);
+            right.swap(gr);
+            sep.swap(gs);
+        }
     }
-    sepLevel = std::max(1, std::min(sepLevel, maxLevel - 1));
-    std::vector<int> left, right, sep;
-    for (int v : verts) {
-        const int l = level[v];
-        if (l < 0 || l > sepLevel) right.push_back(v);
-        else if (l < sepLevel) left.push_back(v);
-        else sep.push_back(v);
-    }
+    else if (!bfsOk)
+        return make_leaf();
     if (sep.empty() || (left.empty() && right.empty())) return make_leaf();
     // the two halves: each into its own node list, the larger of them on a
     // second thread when both are big
     std::vector<NdNode> ln, rn;
     const bool par = depth < 6 && left.size() > kNdParallel && right.size() > kNdParallel;
     if (par) {
-        std::thread th([&] { nd_build(rowPtr, col, right, tag, tagCounter, level, rn, leafSize, depth + 1); });
-        nd_build(rowPtr, col, left, tag, tagCounter, level, ln, leafSize, depth + 1);
+        std::thread th([&] { nd_build(rowPtr, col, right, tag, tagCounter, level, rn, leafSize, depth + 1, xy); });
+        nd_build(rowPtr, col, left, tag, tagCounter, level, ln, leafSize, depth + 1, xy);
         th.join();
     }
     else {
-        if (!left.empty()) nd_build(rowPtr, col, left, tag, tagCounter, level, ln, leafSize, depth + 1);
-        if (!right.empty()) nd_build(rowPtr, col, right, tag, tagCounter, level, rn, leafSize, depth + 1);
+        if (!left.empty()) nd_build(rowPtr, col, left, tag, tagCounter, level, ln, leafSize, depth + 1, xy);
+        if (!right.empty()) nd_build(rowPtr, col, right, tag, tagCounter, level, rn, leafSize, depth + 1, xy);
     }
     // splice: left subtree, right subtree (ids shifted), then the separator
     const int base = static_cast<int>(nodes.size());
@@ -157,7 +216,7 @@ constexpr long long kUpdSplitBlocks = 2 * 152;
 } // namespace
 
 void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize,
-                  const std::vector<int>* rootVerts)
+                  const std::vector<int>* rootVerts, const double* xy)
 {
     P = CholPlan{};
     P.nV = nV;
@@ -182,7 +241,7 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
                     if (!seen[col[p]]) { seen[col[p]] = 1; comp.push_back(col[p]); }
             }
             std::vector<NdNode> sub;
-            nd_build(rowPtr, col, comp, tag, tagCounter, level, sub, leafSize, 0);
+            nd_build(rowPtr, col, comp, tag, tagCounter, level, sub, leafSize, 0, xy);
             const int base = static_cast<int>(nodes.size());
             for (auto& n : sub) {
                 for (int& c : n.children) c += base;

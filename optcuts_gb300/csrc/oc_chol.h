@@ -79,11 +79,15 @@ struct CholPlan {
 };
 
 // Symbolic analysis from a full-symmetric vertex block pattern (rowPtr/col
-// over vertices incl. the diagonal).  Nested dissection by BFS level sets;
-// rootVerts (optional) are kept out of the dissection and eliminated last,
-// as one front above the dissection's roots.
+// over vertices incl. the diagonal).  Nested dissection by BFS level sets,
+// or, given vertex coordinates xy (nV x 2), by geometric bisection at the
+// median along the longer extent (for patterns whose few long edges -- a
+// scaffold's air mesh around the UV domain -- would let BFS level sets wrap
+// around the domain into long rings); rootVerts (optional) are kept out of
+// the dissection and eliminated last, as one front above the dissection's
+// roots.
 void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize = 16,
-                  const std::vector<int>* rootVerts = nullptr);
+                  const std::vector<int>* rootVerts = nullptr, const double* xy = nullptr);
 int chol_upload(CholPlan& P, std::string* err);
 void chol_free(CholPlan& P);
 // Numeric factorisation of the block-CSR values (FP32 storage, FP64 fronts).
