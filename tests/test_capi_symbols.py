@@ -68,3 +68,34 @@ def test_symbolic_analysis_rejects_bad_input():
     F = np.array([[0, 1, 5]], np.int32)
     with pytest.raises(oc.OCError):
         oc.chol_analyze_stats(3, F)
+
+
+def test_ordering_with_coordinates_handles_an_air_ring():
+    """Host-only symbolic analysis of a torus knot's cut mesh with its air
+    mesh: BFS level sets wrap around the air ring into separators as long as
+    the boundary; with the UV coordinates each dissection node keeps the
+    smaller balanced separator of the two, so the tree stays shallow and the
+    factorisation several times cheaper.  Without air (and on the one-point
+    cut ellipsoid) the choice costs no more than BFS."""
+    import optcuts_gb300 as oc
+    from optcuts_gb300 import init as I
+    from optcuts_gb300 import meshes as M
+    V, F = M.torus_knot_tube(200, 64, 2, 3, 0.15, 0.002, 4)
+    st = I.init_uv(V, F)
+    e = np.concatenate([st.F[:, [0, 1]], st.F[:, [1, 2]], st.F[:, [2, 0]]])
+    avg = float(np.linalg.norm(st.V_rest[e[:, 0]] - st.V_rest[e[:, 1]], axis=1).mean())
+    am = oc.Scaffold.build(st.UV, st.F, avg)
+    nV = len(st.UV)
+    Fa = am.localVI2Global(nV)[am.airF]
+    Fall = np.vstack([st.F, Fa])
+    xy = np.vstack([st.UV, am.airV[len(am.bnd):]])
+    n = len(xy)
+    bfs = oc.chol_analyze_stats(n, Fall, st.fixedVert)
+    geo = oc.chol_analyze_stats(n, Fall, st.fixedVert, xy=xy)
+    assert geo["dof"] == bfs["dof"] == 2 * n
+    assert geo["flops"] < 0.5 * bfs["flops"] and geo["levels"] < bfs["levels"]
+    for V2, F2 in (M.torus_knot_tube(200, 64, 2, 3, 0.15, 0.002, 4), M.ellipsoid(60, 60)):
+        s2 = I.init_uv(V2, F2)
+        b = oc.chol_analyze_stats(len(s2.UV), s2.F, s2.fixedVert)
+        g = oc.chol_analyze_stats(len(s2.UV), s2.F, s2.fixedVert, xy=s2.UV)
+        assert g["flops"] <= 1.05 * b["flops"]
