@@ -221,6 +221,13 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     P = CholPlan{};
     P.nV = nV;
     P.nDof = 2 * nV;
+    // the bisection needs an order on the coordinates: BFS alone unless all are finite
+    if (xy)
+        for (long long i = 0; i < 2LL * nV; ++i)
+            if (!std::isfinite(xy[i])) {
+                xy = nullptr;
+                break;
+            }
     std::vector<NdNode> nodes;
     std::vector<int> tag(nV, 0), level(nV, -1);
     std::atomic<int> tagCounter{0};

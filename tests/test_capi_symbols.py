@@ -99,3 +99,7 @@ def test_ordering_with_coordinates_handles_an_air_ring():
         b = oc.chol_analyze_stats(len(s2.UV), s2.F, s2.fixedVert)
         g = oc.chol_analyze_stats(len(s2.UV), s2.F, s2.fixedVert, xy=s2.UV)
         assert g["flops"] <= 1.05 * b["flops"]
+    # a non-finite coordinate: BFS alone
+    bad = s2.UV.copy()
+    bad[3, 1] = np.nan
+    assert oc.chol_analyze_stats(len(s2.UV), s2.F, s2.fixedVert, xy=bad) == b
