@@ -227,7 +227,11 @@ void device_mesh_free(oc::DeviceMesh& d)
 int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int nF, const std::vector<double>& rest,
                        double surfaceArea, const std::vector<unsigned char>& mask)
 {
-    device_mesh_free(d);
+    // the arrays are reused while the mesh fits them (a scaffold's air mesh
+    // is rebuilt every iteration with about the same size); otherwise they
+    // are reallocated with some headroom
+    const bool reuse = d.F0 && nF <= d.capF && nV <= d.capV;
+    if (!reuse) device_mesh_free(d);
     d.nV = nV;
     d.nF = nF;
     std::vector<int> f0(nF), f1(nF), f2(nF);
@@ -257,12 +261,19 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
     auto chk = [&](cudaError_t e, const char* what) {
         if (rc == OC_OK && e != cudaSuccess) rc = fail(ctx, OC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     };
-    chk(dalloc(&d.F0, nF), "alloc"); chk(dalloc(&d.F1, nF), "alloc"); chk(dalloc(&d.F2, nF), "alloc");
     double** dcols[9] = {&d.A2, &d.w, &d.e0, &d.e1, &d.e01, &d.e0d, &d.e1d, &d.e01d, &d.area};
-    for (int k = 0; k < 9; ++k) chk(dalloc(dcols[k], nF), "alloc");
-    chk(dalloc(&d.vcPtr, nV + 1), "alloc");
-    chk(dalloc(&d.vcIdx, 3 * (size_t)nF), "alloc");
-    chk(dalloc(&d.fixedMask, nV), "alloc");
+    if (!reuse) {
+        const int capF = nF + nF / 4 + 64, capV = nV + nV / 16 + 64;
+        chk(dalloc(&d.F0, capF), "alloc"); chk(dalloc(&d.F1, capF), "alloc"); chk(dalloc(&d.F2, capF), "alloc");
+        for (int k = 0; k < 9; ++k) chk(dalloc(dcols[k], capF), "alloc");
+        chk(dalloc(&d.vcPtr, capV + 1), "alloc");
+        chk(dalloc(&d.vcIdx, 3 * (size_t)capF), "alloc");
+        chk(dalloc(&d.fixedMask, capV), "alloc");
+        if (rc == OC_OK) {
+            d.capF = capF;
+            d.capV = capV;
+        }
+    }
     if (rc == OC_OK) {
         chk(upload(d.F0, f0.data(), nF, st), "upload"); chk(upload(d.F1, f1.data(), nF, st), "upload");
         chk(upload(d.F2, f2.data(), nF, st), "upload");

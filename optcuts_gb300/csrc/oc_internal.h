@@ -65,6 +65,7 @@ struct DeviceMesh {
     // corner code = k * nF + t
     int *vcPtr = nullptr, *vcIdx = nullptr;
     unsigned char* fixedMask = nullptr;                 // nV
+    int capV = 0, capF = 0;   // allocated vertex / triangle capacity (host bookkeeping)
 };
 
 // Reduction scratch: per-block partials then a fixed-order final pass.
