@@ -572,14 +572,14 @@ private:
 
 } // namespace
 
-int air_mesh_build(const double* UV, int nV, const int* F, int nF, double avgEdgeLen, AirMesh& out, std::string* err,
-                   double minAngleDeg)
+int air_mesh_boundary(int nV, const int* F, int nF, std::vector<int>& bnd, std::vector<int>& loopStart,
+                      std::vector<int>& seedTris, std::string* err)
 {
     auto bad = [&](const char* m) {
         if (err) *err = m;
         return OC_ERR_INVALID;
     };
-    if (!UV || !F || nV <= 0 || nF <= 0 || !(avgEdgeLen > 0.0)) return bad("air mesh: bad arguments");
+    if (!F || nV <= 0 || nF <= 0) return bad("air mesh: bad arguments");
     for (long long i = 0; i < 3LL * nF; ++i)
         if (F[i] < 0 || F[i] >= nV) return bad("air mesh: vertex index out of range");
     // outgoing half-edges per vertex (CSR); (a, b) is on the boundary when
@@ -602,26 +602,81 @@ int air_mesh_build(const double* UV, int nV, const int* F, int nF, double avgEdg
             if (next[a] >= 0) return bad("air mesh: non-manifold boundary vertex");
             next[a] = b;
         }
-    out = AirMesh{};
+    bnd.clear();
+    loopStart.clear();
     std::vector<char> used(nV, 0);
-    std::vector<std::pair<int, int>> segs;
     for (int v = 0; v < nV; ++v) {
         if (next[v] < 0 || used[v]) continue;
-        const int first = static_cast<int>(out.bnd.size());
+        loopStart.push_back(static_cast<int>(bnd.size()));
         int w = v;
         while (!used[w]) {
             used[w] = 1;
-            out.bnd.push_back(w);
+            bnd.push_back(w);
             w = next[w];
             if (w < 0) return bad("air mesh: open boundary chain");
         }
         if (w != v) return bad("air mesh: boundary chains merge");
-        const int last = static_cast<int>(out.bnd.size()) - 1;
+    }
+    loopStart.push_back(static_cast<int>(bnd.size()));
+    if (bnd.size() < 3) return bad("air mesh: the mesh has no boundary");
+    // the first triangle of each connected component (union-find over
+    // vertices), whose centroid seeds the removal of the mesh's own region
+    seedTris.clear();
+    std::vector<int> root(nV);
+    for (int v = 0; v < nV; ++v) root[v] = v;
+    auto find = [&](int v) {
+        while (root[v] != v) v = root[v] = root[root[v]];
+        return v;
+    };
+    for (int t = 0; t < nF; ++t) {
+        const int r0 = find(F[3 * t]);
+        for (int k = 1; k < 3; ++k) {
+            const int r = find(F[3 * t + k]);
+            if (r != r0) root[r] = r0;
+        }
+    }
+    std::vector<char> seeded(nV, 0);
+    for (int t = 0; t < nF; ++t) {
+        const int r = find(F[3 * t]);
+        if (seeded[r]) continue;
+        seeded[r] = 1;
+        seedTris.insert(seedTris.end(), F + 3 * t, F + 3 * t + 3);
+    }
+    return OC_OK;
+}
+
+int air_mesh_build(const double* UV, int nV, const int* F, int nF, double avgEdgeLen, AirMesh& out, std::string* err,
+                   double minAngleDeg)
+{
+    std::vector<int> bnd, loopStart, seedTris;
+    const int rc = air_mesh_boundary(nV, F, nF, bnd, loopStart, seedTris, err);
+    if (rc) return rc;
+    return air_mesh_build_loops(UV, nV, bnd, loopStart, seedTris, avgEdgeLen, out, err, minAngleDeg);
+}
+
+int air_mesh_build_loops(const double* UV, int nV, const std::vector<int>& bnd, const std::vector<int>& loopStart,
+                         const std::vector<int>& seedTris, double avgEdgeLen, AirMesh& out, std::string* err,
+                         double minAngleDeg)
+{
+    auto bad = [&](const char* m) {
+        if (err) *err = m;
+        return OC_ERR_INVALID;
+    };
+    if (!UV || nV <= 0 || !(avgEdgeLen > 0.0) || bnd.size() < 3 || loopStart.size() < 2)
+        return bad("air mesh: bad arguments");
+    for (int b : bnd)
+        if (b < 0 || b >= nV) return bad("air mesh: boundary vertex out of range");
+    for (int v : seedTris)
+        if (v < 0 || v >= nV) return bad("air mesh: seed vertex out of range");
+    out = AirMesh{};
+    out.bnd = bnd;
+    std::vector<std::pair<int, int>> segs;
+    for (size_t l = 0; l + 1 < loopStart.size(); ++l) {
+        const int first = loopStart[l], last = loopStart[l + 1] - 1;
         for (int i = first; i < last; ++i) segs.push_back({i, i + 1});
         segs.push_back({last, first});
     }
     const int nBnd = static_cast<int>(out.bnd.size());
-    if (nBnd < 3) return bad("air mesh: the mesh has no boundary");
     // bounding box and its segmentation (Scaffold.cpp:63-95)
     double minX = UV[0], maxX = UV[0], minY = UV[1], maxY = UV[1];
     for (int v = 1; v < nV; ++v) {
@@ -651,32 +706,12 @@ int air_mesh_build(const double* UV, int nV, const int* F, int nF, double avgEdg
     for (const auto& sg : segs)
         if (!cdt.constrain(sg.first, sg.second)) return bad("air mesh: boundary segments cross or touch");
     cdt.carve(cdt.triangle_with_super_vertex());
-    // one seed per connected component (union-find over vertices): the
-    // centroid of the component's first triangle
-    {
-        std::vector<int> root(nV);
-        for (int v = 0; v < nV; ++v) root[v] = v;
-        auto find = [&](int v) {
-            while (root[v] != v) v = root[v] = root[root[v]];
-            return v;
-        };
-        for (int t = 0; t < nF; ++t) {
-            const int r0 = find(F[3 * t]);
-            for (int k = 1; k < 3; ++k) {
-                const int r = find(F[3 * t + k]);
-                if (r != r0) root[r] = r0;
-            }
-        }
-        std::vector<char> seeded(nV, 0);
-        for (int t = 0; t < nF; ++t) {
-            const int r = find(F[3 * t]);
-            if (seeded[r]) continue;
-            seeded[r] = 1;
-            const int* f = F + 3 * t;
-            const P2 c = {(UV[2 * f[0]] + UV[2 * f[1]] + UV[2 * f[2]]) / 3.0,
-                          (UV[2 * f[0] + 1] + UV[2 * f[1] + 1] + UV[2 * f[2] + 1]) / 3.0};
-            cdt.carve(cdt.locate(c));
-        }
+    // one seed per connected component: the centroid of its first triangle
+    for (size_t i = 0; i + 2 < seedTris.size(); i += 3) {
+        const int* f = seedTris.data() + i;
+        const P2 c = {(UV[2 * f[0]] + UV[2 * f[1]] + UV[2 * f[2]]) / 3.0,
+                      (UV[2 * f[0] + 1] + UV[2 * f[1] + 1] + UV[2 * f[2] + 1]) / 3.0};
+        cdt.carve(cdt.locate(c));
     }
     if (minAngleDeg > 0.0) cdt.refine(minAngleDeg, 4 * nPts + 1024);
     // output: input points, then Steiner points (stored after the three

@@ -21,5 +21,14 @@ struct AirMesh {
 constexpr double kAirMinAngle = 20.0;   // Triangle's "q" default
 int air_mesh_build(const double* UV, int nV, const int* F, int nF, double avgEdgeLen, AirMesh& out,
                    std::string* err, double minAngleDeg = kAirMinAngle);
+// the same in two parts: what depends on the topology only -- the boundary
+// loops of F (bnd loop by loop, loop l = bnd[loopStart[l] .. loopStart[l +
+// 1])) and the first triangle of each connected component (seedTris, 3
+// vertex ids each) -- and the air mesh for a UV layout from those
+int air_mesh_boundary(int nV, const int* F, int nF, std::vector<int>& bnd, std::vector<int>& loopStart,
+                      std::vector<int>& seedTris, std::string* err);
+int air_mesh_build_loops(const double* UV, int nV, const std::vector<int>& bnd, const std::vector<int>& loopStart,
+                         const std::vector<int>& seedTris, double avgEdgeLen, AirMesh& out, std::string* err,
+                         double minAngleDeg = kAirMinAngle);
 
 } // namespace oc

@@ -31,6 +31,7 @@ struct oc_ctx {
 
 struct oc_mesh {
     oc_ctx* ctx = nullptr;
+    unsigned long long topoVersion = 0;   // advanced whenever F changes
     oc::DeviceMesh d;
     oc::Scratch scratch;
     std::vector<double> rest;       // nF x 8, TriMesh feature layout
@@ -97,6 +98,10 @@ struct oc_optimizer {
     double* airHb = nullptr;        // 21 x capAirF
     std::vector<int> airFw, bnd;    // air triangles in augmented ids; boundary map
     std::vector<int> airF;          // air triangles in air-mesh ids
+    // the mesh's boundary loops for the air-mesh rebuilds, kept while the
+    // topology (the mesh's topoVersion) is the same
+    std::vector<int> bndLoops, bndLoopStart, bndSeeds;
+    unsigned long long bndVersion = ~0ULL;
 };
 
 namespace oc {
@@ -752,6 +757,7 @@ int oc_sd_init_step_size(oc_mesh* m, const double* searchDir, double* stepSize)
 static int mesh_rebuild(oc_mesh* m, const std::vector<double>& uvHost)
 {
     oc_ctx* ctx = m->ctx;
+    ++m->topoVersion;
     m->adj.reset();
     const int nV = static_cast<int>(m->Vrest.size() / 3), nF = static_cast<int>(m->F.size() / 3);
     double surfaceArea = 0.0;
@@ -2060,7 +2066,14 @@ int oc_optimizer_rebuild_scaffold(oc_optimizer* o)
     OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
     oc::AirMesh am;
     std::string err;
-    const int rc = oc::air_mesh_build(uv.data(), m->d.nV, m->F.data(), m->d.nF, m->scalars[1], am, &err);
+    if (o->bndVersion != m->topoVersion) {
+        const int rb = oc::air_mesh_boundary(m->d.nV, m->F.data(), m->d.nF, o->bndLoops, o->bndLoopStart,
+                                             o->bndSeeds, &err);
+        if (rb) return fail(m->ctx, rb, err);
+        o->bndVersion = m->topoVersion;
+    }
+    const int rc = oc::air_mesh_build_loops(uv.data(), m->d.nV, o->bndLoops, o->bndLoopStart, o->bndSeeds,
+                                            m->scalars[1], am, &err);
     if (rc) return fail(m->ctx, rc, err);
     return oc_optimizer_set_scaffold(o, am.V.data(), static_cast<int>(am.V.size() / 2), am.F.data(),
                                      static_cast<int>(am.F.size() / 3), am.bnd.data(), am.nBnd, -1.0);
