@@ -334,7 +334,7 @@ int oc_topo_result_timing(const oc_topo_result* r, int* nSelected, double* probe
 /* per local problem: its candidate, its exact E_w decrease (NaN where the
  * learned proposal did not solve it) and the predicted decrease (learned
  * queries; else NaN), on the candidates' scale (interior splits halved):
- * the exhaustive pass as the judge of the proposal's recall */
+ * an exhaustive query's values measure the proposal's recall */
 int oc_topo_result_problems(const oc_topo_result* r, int* nProblems, int* cand, double* ewExact, double* ewPred);
 /* per local problem: triangles, free vertices, Newton iterations,
  * line-search energy evaluations and SM clock cycles of its solve (of the

@@ -100,7 +100,7 @@ def test_energy_param_update(golden):
 
 
 def test_pcg_solver_option_runs(golden):
-    """The block-Jacobi PCG solver behind the same Optimizer (spec form)."""
+    """The block-Jacobi PCG solver behind the same Optimizer (the iterative option)."""
     g = golden("icosphere_320")
     m, opt, E, steps, status = run(g, iters=5, linearSolver=oc.SOLVER_PCG, pcgMaxIter=50000)
     assert np.all(np.diff(E) <= 0.0) and m.checkInversion()
