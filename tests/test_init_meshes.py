@@ -151,3 +151,35 @@ def test_cohesive_edges_and_seam_term_match_reference(golden, case):
     # E_se before division by virtualRadius (TriMesh::computeSeamSparsity)
     avg = g["scalars"][1]
     assert I.seam_sparsity(st.V_rest, st.UV, st.cohE, avg) == pytest.approx(g["scalars"][3], rel=1e-15, abs=0)
+
+
+def test_cut_to_disk_and_cut_path_edge_cases():
+    """A closed sphere has no cut graph; on a disk the boundary edges are
+    never peeled, so the boundary loop is what remains (the initialisation
+    calls it for closed surfaces of genus >= 1 only); the C call reports
+    sizes first and refuses short output arrays; a cut path with a vertex
+    out of range is an error, not a crash."""
+    import ctypes
+
+    import optcuts_gb300 as oc
+    V, F = M.icosphere(2)
+    assert oc.cut_to_disk(F) == []
+    Vp, Fp = M.CONFIGS["plane"]()
+    cuts = oc.cut_to_disk(Fp)
+    assert len(cuts) == 1 and cuts[0][0] == cuts[0][-1]
+    assert sorted(cuts[0][:-1]) == sorted(I.boundary_loop(Fp))
+    Vt, Ft = M.torus(12, 10)
+    Ft = np.ascontiguousarray(Ft, np.int32)
+    nc, nv = ctypes.c_int(), ctypes.c_int()
+    P = ctypes.POINTER(ctypes.c_int)
+    lib = oc.lib()
+    assert lib.oc_cut_to_disk(Ft.ctypes.data_as(P), len(Ft), None, 0, None, 0, ctypes.byref(nc),
+                              ctypes.byref(nv)) == oc.OC_OK
+    assert nc.value == 2 and nv.value == sum(len(c) for c in oc.cut_to_disk(Ft))
+    short = np.zeros(1, np.int32)
+    off = np.zeros(nc.value + 1, np.int32)
+    assert lib.oc_cut_to_disk(Ft.ctypes.data_as(P), len(Ft), short.ctypes.data_as(P), 1, off.ctypes.data_as(P),
+                              len(off), ctypes.byref(nc), ctypes.byref(nv)) != oc.OC_OK
+    UV = np.zeros((len(Vt), 2))
+    with pytest.raises(oc.OCError):
+        oc.topology_cut_path([0, len(Vt) + 5], Vt, UV, Ft, np.zeros((0, 4), np.int32))
