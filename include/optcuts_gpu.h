@@ -12,10 +12,13 @@
  *            (src/Energy/SymDirichletEnergy.cpp:262, src/Optimizer.cpp:666-669)
  *   fixed vertices: list of vertex ids (TriMesh::fixedVert, src/TriMesh.hpp:56)
  *
- * Precision: energies, gradients, injective-step roots, line-search
- * acceptance and Krylov dot products / vector updates are float64; the
- * per-triangle Hessian's PSD projection and the stored sparse matrix values
- * are float32 (SpMV accumulates in float64).
+ * Precision: the geometry step is float64 throughout -- energies,
+ * gradients, the per-triangle 6x6 Hessians and their PSD projection, the
+ * assembled Newton matrix, its LDL^T factorization and substitutions, the
+ * injective-step roots and the line search.  The local topology solves are
+ * float64 with an optional float32 element-Hessian projection
+ * (OC_TOPO_FP32_HESSIAN); the learned proposal's network computes in bf16
+ * with float32 accumulation.
  */
 #ifndef OPTCUTS_GPU_H
 #define OPTCUTS_GPU_H
@@ -106,14 +109,13 @@ int oc_sd_hessian_blocks_projected(oc_mesh* mesh, int uniformWeight, int project
  * *stepSize in place to the largest inversion-free step along searchDir. */
 int oc_sd_init_step_size(oc_mesh* mesh, const double* searchDir, double* stepSize);
 
-/* Allocation-free energy evaluation (no counterpart in the reference; an
- * addition for callers that cannot allocate device memory themselves -- e.g.
- * code running inside a host framework that owns every allocation, or work
- * recorded into an externally managed CUDA graph).  Computes, on the given
- * stream, E_k = sum over triangles of the symmetric Dirichlet energy at
- * UV + alphas[k] * dir for k < nTrials (dir NULL: the energy at UV), the
- * line-search evaluation of Optimizer::lineSearch (Optimizer.cpp:593-610).
- * All pointers except `alphas` (host, nTrials values) are DEVICE pointers
+/* Allocation-free energy evaluation.  It has no counterpart in the
+ * reference: it is an addition for callers that cannot allocate device
+ * memory themselves -- e.g. code running inside a host framework that owns
+ * every allocation, or work recorded into an externally managed CUDA graph.
+ * Computes, on the given stream, E_k = sum over triangles of the symmetric
+ * Dirichlet energy at UV + alphas[k] * dir for k < nTrials (dir NULL: the
+ * energy at UV).  All pointers except `alphas` (host, nTrials values) are DEVICE pointers
  * owned by the caller:
  *   F        nF x 3 int32 row-major       UV, dir   nV x 2 float64 row-major
  *   rest     nF x 8 float64, the layout of oc_mesh_rest_constants
@@ -212,8 +214,14 @@ int oc_optimizer_destroy(oc_optimizer* opt);
 /* Optimizer::precompute (Optimizer.cpp:154-201) */
 int oc_optimizer_precompute(oc_optimizer* opt);
 /* Optimizer::solve (Optimizer.cpp:203-261): *result = 0 (not converged) or
- * 1 (converged, or the line search stopped). */
+ * 1 (converged, or the line search stopped).  A zero or non-finite pivot in
+ * the Newton matrix's factorization ends the call with OC_ERR_NOT_SPD
+ * before any step is taken (the reference dumps the matrix and exits,
+ * Optimizer.cpp:548-554); oc_optimizer_bad_pivots reports the count. */
 int oc_optimizer_solve(oc_optimizer* opt, int maxIter, int* result);
+/* Pivots of the last factorization that were zero or non-finite (replaced
+ * by 1e-300 inside the factorization so that it completes). */
+int oc_optimizer_bad_pivots(oc_optimizer* opt, int* nBad);
 /* Optimizer::getLastEnergyVal (Optimizer.cpp:845-850) */
 int oc_optimizer_get_last_energy(oc_optimizer* opt, double* energy);
 int oc_optimizer_get_iter_num(oc_optimizer* opt, int* iterNum);

@@ -29,7 +29,10 @@ LIB_PATH = os.path.join(_HERE, "_lib", "liboc_gpu.so")
 _lib = None
 
 OC_OK = 0
+OC_ERR_INVALID = 1
+OC_ERR_INVERTED = 2
 OC_ERR_NOT_CONVERGED = 3
+OC_ERR_NOT_SPD = 8
 
 
 class OCError(RuntimeError):
@@ -153,6 +156,7 @@ _SIGS = {
     "oc_optimizer_get_last_energy_scaffold": [_vp, _d],
     "oc_optimizer_system_size": [_vp, _i],
     "oc_optimizer_last_vectors": [_vp, _d, _d],
+    "oc_optimizer_bad_pivots": [_vp, _i],
     "oc_sd_energy_trials_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
                                     _vp, _vp],
 }
@@ -870,6 +874,13 @@ class Optimizer:
         g, d = np.zeros(2 * n), np.zeros(2 * n)
         self.ctx.check(lib().oc_optimizer_last_vectors(self.h, _pd(g), _pd(d)), "lastVectors")
         return g, d
+
+    def badPivots(self):
+        """Zero or non-finite pivots of the last factorization (a solve that
+        met any raised OCError with status OC_ERR_NOT_SPD)."""
+        n = ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_bad_pivots(self.h, ctypes.byref(n)), "badPivots")
+        return n.value
 
     def getIterNum(self):
         n = ctypes.c_int()

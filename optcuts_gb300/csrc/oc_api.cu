@@ -625,7 +625,7 @@ int oc_mesh_create(oc_ctx* ctx, const double* V_rest, const double* UV, int nV, 
     chk(dalloc(&m->cornerBuf, 3 * (size_t)nF), "alloc");
     chk(dalloc(&m->tmpV, nV), "alloc");
     chk(dalloc(&m->hb, 21 * (size_t)nF), "alloc");
-    m->scratch.maxBlocks = 1216;
+    m->scratch.maxBlocks = oc::kMaxReduceBlocks;
     chk(dalloc(&m->scratch.partials, (size_t)m->scratch.maxBlocks * oc::kMaxTrials), "alloc");
     chk(dalloc(&m->scratch.result, 16), "alloc");
     chk(dalloc(&m->scratch.minBits, 2), "alloc");
@@ -1679,6 +1679,9 @@ static int solve_one(oc_optimizer* o, int* converged)
     if (rc) return rc;
     o->badPivots = bad;
     o->launches += 1 + (o->ls->kind == OC_SOLVER_DIRECT ? 3 + (long long)o->ls->chol.launches.size() : 0);
+    if (bad > 0)   // Optimizer.cpp:548-554 dumps the matrix and exits
+        return fail(ctx, OC_ERR_NOT_SPD,
+                    "solve: " + std::to_string(bad) + " zero or non-finite pivot(s) in the Newton matrix");
     record(o, 4);
     // search direction: H d = -g
     std::string err;
@@ -1856,6 +1859,13 @@ int oc_optimizer_last_step(oc_optimizer* o, double* stepSize, int* pcgIters, dou
     if (pcgRelRes) *pcgRelRes = o->lastRelRes;
     if (lsLaunches) *lsLaunches = o->lastLsLaunches;
     if (gsq) *gsq = o->lastGsq;
+    return OC_OK;
+}
+
+int oc_optimizer_bad_pivots(oc_optimizer* o, int* nBad)
+{
+    if (!o || !nBad) return OC_ERR_INVALID;
+    *nBad = o->badPivots;
     return OC_OK;
 }
 

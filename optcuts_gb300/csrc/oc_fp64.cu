@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256) k_divgrad(DeviceMesh m, const double2* __
 int reduce_blocks_for(int n)
 {
     int b = (n + 255) / 256;
-    if (b > 1216) b = 1216;   // 152 SMs x 8 resident 256-thread blocks
+    if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
     return b < 1 ? 1 : b;
 }
 
@@ -312,7 +312,7 @@ int reduce_blocks_for(int n)
 // oc_sd_energy_trials_noalloc.
 namespace {
 
-constexpr int kNoAllocBlocks = 1216;
+constexpr int kNoAllocBlocks = kMaxReduceBlocks;
 static __device__ __align__(256) double g_noallocPartials[kNoAllocBlocks * kMaxTrials];
 
 template <int NT>
@@ -461,7 +461,8 @@ oc_sd_energy_trials_noalloc(const int* F, const double* UV, const double* dir, c
     Alphas a = {{0, 0, 0, 0, 0, 0, 0, 0}};
     for (int k = 0; k < nTrials; ++k) a.a[k] = alphas ? alphas[k] : 0.0;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int nb = reduce_blocks_for(nF);   // <= kNoAllocBlocks
+    const int nb = reduce_blocks_for(nF);
+    if (nb > kNoAllocBlocks) return OC_ERR_INVALID;   // the static partials hold kNoAllocBlocks blocks
     const double2* uv = reinterpret_cast<const double2*>(UV);
     const double2* d = reinterpret_cast<const double2*>(dir);
     if (nTrials == 1)

@@ -46,6 +46,9 @@ struct Alphas {
 
 constexpr int kMaxTrials = 8;       // line-search step sizes per energy launch
 constexpr int kReduceThreads = 256; // block size of the reduction kernels
+// Grid cap of the block-partial reductions (152 SMs x 8 resident 256-thread
+// blocks); every partials buffer holds kMaxReduceBlocks x kMaxTrials values.
+constexpr int kMaxReduceBlocks = 1216;
 
 // Device-resident triangle mesh (structure of arrays for per-triangle data,
 // vertex-major double2 for UV so a corner gather is one 16-byte load).

@@ -44,8 +44,8 @@ from optcuts_gb300 import meshes  # noqa: E402
 
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
-# case -> (mesh generator key, lambda, Newton iterations, max Hessian triangles, dump UV per iteration,
-#          extra driver flags)
+# case -> (mesh generator key, lambda, Newton iterations, max Hessian triangles, dump UV per iteration
+#          (True, or the number of leading iterations kept), extra driver flags)
 CASES = {
     "triangle": ("triangle", 0.999, 20, None, True, ["scafdump"]),
     "plane": ("plane", 0.999, 20, None, True, ["scafdump"]),
@@ -53,7 +53,9 @@ CASES = {
     "icosphere_320": ("icosphere_320", 0.999, 40, None, True, []),
     "ellipsoid_2k": ("ellipsoid_2k", 0.999, 300, None, False, []),
     "torus_768": ("torus_768", 0.999, 30, None, False, ["scafdump"]),
-    "icosphere_5k": ("icosphere_5k", 0.999, 120, 512, False, []),
+    # UV of the first 21 iterations: the start points of the one-step parity
+    # test (one Newton step from the reference's own iterate k)
+    "icosphere_5k": ("icosphere_5k", 0.999, 120, 512, 21, []),
     # scaffold on: an open bumpy sheet (disk, 156 boundary vertices) and a
     # closed sphere after its one-point cut with the scaffold forced on
     "sheet_3k": ("sheet_3k", 0.999, 40, 256, True, ["scafdump"]),
@@ -64,7 +66,17 @@ CASES = {
     "sheet_3k_topo": ("sheet_3k", 0.999, 60, 16, False, ["nobij", "topo"]),
     "torus_768_topo": ("torus_768", 0.999, 60, 16, False, ["nobij", "topo"]),
     "ellipsoid_2k_topo": ("ellipsoid_2k", 0.999, 300, 16, False, ["nobij", "topo"]),
+    # slim cases (large meshes: only the traces, scalars and air meshes kept)
+    # the 199k-triangle ellipsoid benchmark workload from its Tutte start with
+    # the scaffold on: the reference's air mesh of that start and its first
+    # Newton iteration
+    "ellipsoid_199k_start": ("ellipsoid_199k", 0.999, 1, 16, False, ["scaf", "scafdump", "slim"]),
+    # the genus-1 torus workload (cut_to_disk + Tutte, scaffold on) run to
+    # convergence
+    "torus_41k_conv": ("torus_41k", 0.999, 3000, 16, False, ["slim"]),
 }
+SLIM_KEYS = ("scalars", "trace_E", "trace_Etot", "trace_gsq", "trace_alpha", "trace_status", "scaf_V", "scaf_F",
+             "scaf_bnd", "scaf_fixed", "scaf_off", "uv0_check")
 
 
 def per_tri_blocks(F, fixed, Hv, ntri):
@@ -86,15 +98,28 @@ def per_tri_blocks(F, fixed, Hv, ntri):
 
 def run_case(name, key, lam, iters, hmax, states, flags):
     V, F = meshes.CONFIGS[key]()
+    slim = "slim" in flags
+    flags = [f for f in flags if f != "slim"]
     with tempfile.TemporaryDirectory() as td:
         obj = os.path.join(td, "mesh.obj")
         meshes.write_obj(obj, V, F)
         out = os.path.join(td, "out") + "/"
         os.makedirs(out)
-        args = [DRIVER, obj, out, repr(lam), str(iters), "hess"] + (["states"] if states else []) + flags
+        args = [DRIVER, obj, out, repr(lam), str(iters)] + ([] if slim else ["hess"]) + \
+            (["states"] if states else []) + flags
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
                        env=dict(os.environ, OC_REF_THREADS="1"))
         ld = lambda n: np.load(out + n + ".npy")  # noqa: E731
+        if slim:
+            uv0 = ld("UV0")
+            # identifies the start state: UV sums, its first and last rows, size
+            pack = {"uv0_check": np.concatenate([uv0.sum(0), uv0[0], uv0[-1], [len(uv0), len(ld("F"))]])}
+            for k in SLIM_KEYS:
+                if k != "uv0_check" and os.path.exists(out + k + ".npy"):
+                    pack[k] = ld(k)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack)
+            pack.update(UV0=uv0, F=ld("F"))
+            return pack
         Fm, fixed = ld("F"), ld("fixedVert")
         nt = len(Fm) if hmax is None else min(hmax, len(Fm))
         blocks = per_tri_blocks(Fm, fixed, ld("H0_V"), nt)
@@ -105,6 +130,8 @@ def run_case(name, key, lam, iters, hmax, states, flags):
                     mesh_V=V, mesh_F=F)
         if states:
             pack["UV_iters"] = ld("UV_iters")
+            if states is not True:
+                pack["UV_iters"] = pack["UV_iters"][:states]
         pack["trace_Etot"] = ld("trace_Etot")
         if "topo" in flags:
             for k in ("V", "F", "Vrest", "cohE", "fixed", "divGrad", "best"):

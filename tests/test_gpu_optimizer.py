@@ -1,13 +1,16 @@
 """The projected-Newton Optimizer on the GPU against the reference's traces.
 
 The reference solves each Newton system exactly (SimplicialLDLT); the GPU
-path uses block-Jacobi PCG to a relative residual of 1e-8.  At a Tutte start
-the Newton matrix has condition numbers near 1e14, so the search directions
-differ in near-null modes and the per-iteration energies separate by up to
-~10-20% in the first iterations (two exact LDL^T orderings already differ at
-1e-4); both runs converge to the same stationary energy, which is what these
-tests pin (relative 1e-4 .. 5e-3), together with the invariants: monotone
-energy, no inverted triangle, determinism."""
+path solves it exactly too, with a multifrontal LDL^T under its own
+nested-dissection ordering (block-Jacobi PCG remains an option).  At a
+Tutte start the Newton matrix has condition numbers near 1e14, so two exact
+factorizations with different orderings give directions that differ at
+cond x eps; the trajectories accumulate that and separate by up to ~10-20%
+in the first iterations, while both runs converge to the same stationary
+energy, which is what these tests pin (relative 1e-6 .. 5e-3), together with
+the invariants: monotone energy, no inverted triangle, determinism.  Single
+steps from the reference's own iterates are pinned to 1e-6 in
+tests/test_gpu_parity_steps.py."""
 import numpy as np
 import pytest
 
@@ -173,3 +176,21 @@ def test_deterministic_multiwave_factorization():
         runs.append((np.array(E), m.V.copy()))
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
     np.testing.assert_array_equal(runs[0][1], runs[1][1])
+
+
+def test_zero_pivot_is_an_error(golden):
+    """A vertex no triangle references leaves a zero diagonal block in the
+    Newton matrix, a zero pivot: the step ends with OC_ERR_NOT_SPD (the
+    reference dumps the matrix and exits, Optimizer.cpp:548-554) and the
+    mesh keeps its UV."""
+    g = golden("icosphere_320")
+    Vr = np.vstack([g["V_rest"], [[0.0, 0.0, 2.0]]])
+    uv = np.vstack([g["UV0"], [[3.0, 3.0]]])
+    m = oc.TriMesh(Vr, uv, g["F"], g["fixedVert"])
+    opt = oc.Optimizer(m, [0.001])
+    opt.precompute()
+    with pytest.raises(oc.OCError) as e:
+        opt.solve(1)
+    assert e.value.status == oc.OC_ERR_NOT_SPD
+    assert opt.badPivots() >= 1
+    np.testing.assert_array_equal(m.V, uv)

@@ -91,3 +91,52 @@ def test_newton_trace_matches_reference(golden, case):
     # the converged energy is not
     assert rel.max() < 5e-3, rel
     assert abs(tr["E"][-1] - g["trace_E"][-1]) / g["trace_E"][-1] < 1e-4
+
+
+@pytest.mark.parametrize("case", ["cube", "icosphere_320", "icosphere_5k"])
+def test_one_step_from_reference_iterate(golden, case):
+    """The CPU oracle's column of the per-iteration table: one oracle Newton
+    step from the reference's own iterate k (UV after its iteration k-1)
+    against the reference's energy after iteration k, for k < 20.  1e-6
+    relative, except the icosphere's first three steps from its Tutte start
+    (Newton matrix scale ~1e14; two exact factorizations differ at cond x
+    eps), held to 2e-4; the GPU column is tests/test_gpu_parity_steps.py."""
+    g = golden(case)
+    par = 1.0 - g["scalars"][4]
+    n = min(20, len(g["UV_iters"]), len(g["trace_E"]) - 1)
+    for k in range(n):
+        uv = g["UV0"] if k == 0 else g["UV_iters"][k - 1]
+        _, tr, _ = O.newton(g["V_rest"], g["F"], g["fixedVert"], uv, par, 1)
+        ref = g["trace_E"][k + 1]
+        tol = 2e-4 if (case == "icosphere_5k" and k < 3) else 1e-6
+        assert len(tr["E"]) == 2 and abs(tr["E"][1] - ref) / ref <= tol, (k, tr["E"])
+
+
+@pytest.mark.parametrize("case", SCAFFOLD_OFF)
+def test_oracle_initial_state(golden, case):
+    """The oracle's restatement of the closed genus-0 start (one-point cut,
+    cohesive edges, boundary loop, Tutte map) against the reference's own
+    initial state: topology bit-exact, UV to 1e-10."""
+    from oracle import init as OI
+    g = golden(case)
+    s = OI.init_genus0(g["mesh_V"], g["mesh_F"])
+    np.testing.assert_array_equal(s["F"], g["F"])
+    np.testing.assert_array_equal(s["V_rest"], g["V_rest"])
+    np.testing.assert_array_equal(s["bnd"], g["bnd"])
+    np.testing.assert_array_equal(s["cohE"], g["cohE"])
+    np.testing.assert_array_equal(s["fixedVert"], g["fixedVert"])
+    assert np.abs(s["UV"] - g["UV0"]).max() < 1e-10
+
+
+def test_reference_start_fixture_matches_oracle_start():
+    """The 199k-triangle benchmark start: the reference's own air mesh and
+    first-iteration energies were recorded from this exact start state."""
+    import bench
+    from oracle import init as OI
+    from optcuts_gb300 import meshes as M
+    V, F = M.CONFIGS["ellipsoid_199k"]()
+    s = OI.init_genus0(V, F)
+    ref = bench.reference_start("ellipsoid_199k", s["UV"])
+    assert ref is not None and len(ref["bnd"]) == len(s["bnd"]) == 4
+    assert set(ref["bnd"].tolist()) == set(s["bnd"].tolist())
+    assert ref["E_tot"][1] < ref["E_tot"][0]
