@@ -1979,6 +1979,23 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     o->airScale = o->wScaf / nAirF;   // w_scaf / airMesh.F.rows() (Optimizer.cpp:776)
     o->scaf = true;
     if (!samePattern) o->patternStale = true;
+    else if (cliqueMode) {
+        // the kept pattern's padding may now cover slots the previous air mesh
+        // used (or the reverse): unused slots are fixed rows, so that their
+        // decoupled diagonal blocks hold param * I instead of zero
+        oc_linsys* ls = o->ls;
+        bool changed = false;
+        for (int v = nV; v < nWhole; ++v) {
+            const unsigned char f = v >= nV + nAirOnly ? 1 : 0;
+            if (ls->rowFixed[v] != f) {
+                ls->rowFixed[v] = f;
+                changed = true;
+            }
+        }
+        if (changed)
+            OC_CUDA(ctx, cudaMemcpyAsync(ls->b.rowFixed + nV, ls->rowFixed.data() + nV, nWhole - nV,
+                                         cudaMemcpyHostToDevice, st));
+    }
     o->airContribStale = true;
     return OC_OK;
 }

@@ -31,6 +31,11 @@
 //        scafdump  dump, per iteration, the air mesh the iteration used
 //                  (vertices, triangles, boundary map, fixed air vertices)
 //                  and the augmented gradient / direction of iteration 0
+//        outer     instead of <newton_iters> Newton iterations, the whole
+//                  OptCuts run (src/main.cpp:913-1086, ref_outer.cpp) with
+//                  b_d = 4.1 (bound=<b_d> to change it) for at most
+//                  <newton_iters> outer passes; dumps the event record and
+//                  the final state
 // Outputs are .npy files in outdir (which must exist).
 
 #include "Optimizer.hpp"
@@ -39,6 +44,7 @@
 #include "IglUtils.hpp"
 #include "Timer.hpp"
 #include "cut_to_disk.hpp"
+#include "ref_outer.hpp"
 
 #include <igl/readOBJ.h>
 #include <igl/boundary_loop.h>
@@ -145,7 +151,8 @@ int main(int argc, char** argv)
     const double lambda_init = std::stod(argv[3]);
     const int iters = std::stoi(argv[4]);
     bool dumpHess = false, dumpStates = false, doTime = false, noDump = false, forceScaf = false, scafDump = false;
-    bool noBij = false, doTopo = false;
+    bool noBij = false, doTopo = false, doOuter = false;
+    double bound = 4.1;
     for (int i = 5; i < argc; ++i) {
         if (!std::strcmp(argv[i], "hess")) dumpHess = true;
         else if (!std::strcmp(argv[i], "states")) dumpStates = true;
@@ -155,6 +162,8 @@ int main(int argc, char** argv)
         else if (!std::strcmp(argv[i], "scafdump")) scafDump = true;
         else if (!std::strcmp(argv[i], "nobij")) noBij = true;
         else if (!std::strcmp(argv[i], "topo")) doTopo = true;
+        else if (!std::strcmp(argv[i], "outer")) doOuter = true;
+        else if (!std::strncmp(argv[i], "bound=", 6)) bound = std::stod(argv[i] + 6);
     }
     outputFolderPath = out;
     logFile.open(out + "log.txt");
@@ -294,6 +303,23 @@ int main(int argc, char** argv)
     opt.precompute();
     auto t1 = std::chrono::steady_clock::now();
     if (lambda_init > 0.0) fractureMode = true;
+
+    if (doOuter) {
+        RefOuterResult r = ref_outer_run(opt, energyParams, bound, bijective, rand1PInitCut, iters);
+        const OptCuts::TriMesh& R = opt.getResult();
+        write_npy(out + "outer_events.npy", r.events.data(), "<f8", 8, {r.events.size() / 6, 6});
+        npy_vecd(out + "outer_final.npy", {r.E_SD, r.E_se, r.lambda, (double)r.iterNum, (double)r.topoIter,
+                                           r.finished ? 1.0 : 0.0, r.seconds, bound});
+        npy_mat(out + "outer_V.npy", R.V);
+        npy_mati(out + "outer_F.npy", R.F);
+        npy_mat(out + "outer_Vrest.npy", R.V_rest);
+        npy_mati(out + "outer_cohE.npy", R.cohE);
+        if (doTime)
+            std::printf("outer loop: %s after %d Newton iterations, %d topology steps, %.2f s: E_SD %.9g E_se %.9g "
+                        "lambda %.9g\n", r.finished ? "finished" : "stopped", r.iterNum, r.topoIter, r.seconds,
+                        r.E_SD, r.E_se, r.lambda);
+        return 0;
+    }
 
     std::vector<double> trE, trESD, trG, trAlpha, trTime, trStatus, trEtot;
     trE.push_back(opt.getLastEnergyVal(true));
