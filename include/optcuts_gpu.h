@@ -418,6 +418,79 @@ int oc_optimizer_apply_timing(oc_optimizer* opt, double* out6);
 /* the same operation on a mesh alone */
 int oc_mesh_apply_topology(oc_mesh* mesh, int opType, const int* path, int pathLen, const double* newVertPos,
                            int posRows);
+
+/* ---- the outer loop's pieces ------------------------------------------
+ * Several queries of one state solved together (ops: up to three of
+ * OC_OP_*; out: one result per op), as oc_topology_step does for all three;
+ * mlp / topFrac select the learned proposal (mlp NULL: exhaustive). */
+int oc_topology_queries(oc_mesh* mesh, const int* ops, int nOps, double lambda_t, double filterExp, int options,
+                        oc_mlp* mlp, double topFrac, oc_topo_result** out);
+/* querySplit / queryMerge with propagate = true (TriMesh.cpp:637-665,
+ * 828-833): OC_OP_BOUNDARY_SPLIT evaluates the boundary splits at the
+ * current fracture tail (or at both ends of the last interior split),
+ * OC_OP_MERGE the zipper pair forking at the tail. */
+int oc_topology_query_tail(oc_mesh* mesh, int opType, double lambda_t, int options, oc_topo_result** out);
+/* TriMesh::curFracTail and curInteriorFracTails (-1: none) as the applied
+ * operations leave them (TriMesh.cpp:2891-2899, 3046-3048, 3169-3171;
+ * Optimizer.cpp:397-399) */
+int oc_mesh_fracture_tails(oc_mesh* mesh, int* tails3);
+int oc_mesh_set_fracture_tails(oc_mesh* mesh, const int* tails3);
+/* TriMesh::computeSeamSparsity (TriMesh.cpp:1542-1558) before the division
+ * by virtualRadius: rest length of the interior cohesive edges */
+int oc_mesh_seam_length(oc_mesh* mesh, double* seamLen);
+/* Optimizer::lastEDec: the last line search's energy decrease */
+int oc_optimizer_last_edec(oc_optimizer* opt, double* eDec);
+/* Optimizer::setAllowEDecRelTol (Optimizer.cpp:148-151): off, a Newton
+ * iteration stops only at the gradient tolerance or a zero step */
+int oc_optimizer_set_allow_edec_rel_tol(oc_optimizer* opt, int allow);
+/* energyParams[0] as the optimizer holds it */
+int oc_optimizer_get_energy_param(oc_optimizer* opt, double* energyParam);
+/* Optimizer::setConfig (Optimizer.cpp:287-300): the optimizer's mesh
+ * replaced by a recorded state of the same run (same triangle count; rest
+ * positions, UV, triangles, cohesive edges, fracture tails or NULL), the
+ * scaffold rebuilt when one is set, the energy recomputed and the Newton
+ * iteration count set to iterNum. */
+int oc_optimizer_set_state(oc_optimizer* opt, int nV, const double* Vrest, const double* UV, int nF, const int* F,
+                           int nCohE, const int* cohE, const int* tails3, int iterNum);
+
+/* ---- OptCuts outer loop (src/main.cpp:538-1086 preDrawFunc offline,
+ * updateLambda_stationaryV, converge_preDrawFunc) ---------------------------
+ * Alternates the inner Newton loop (with fracture propagation after each
+ * iteration, Optimizer.cpp:232-262) and the topology step, updates lambda
+ * (the dual step) with oscillation detection and best-feasible rollback,
+ * and ends at the distortion bound b_d.  It drives an optimizer that
+ * precompute has prepared; the mesh carries the cohesive edges of its
+ * initial cut (oc_mesh_set_cohesive_edges). */
+typedef struct oc_optcuts oc_optcuts;
+typedef struct {
+    double upperBound;   /* b_d (4.1; values <= 4 become 4.1, main.cpp:1266-1269) */
+    int bijective;       /* 0: bijectivity off (the only form built) */
+    int topoLineSearch;  /* 1: fracture propagation after each operation */
+    double filterExp;    /* filterExp_in, the interior-split filter (0.6) */
+    int topoOptions;     /* OC_TOPO_FP32_HESSIAN */
+    oc_mlp* mlp;         /* learned proposal for the queries (NULL: exhaustive) */
+    double topFrac;      /* its fraction solved exactly (0.1) */
+    int maxNewtonIters;  /* stop (OC_ERR_NOT_CONVERGED) past this many Newton iterations */
+} oc_optcuts_config;
+int oc_optcuts_default_config(oc_optcuts_config* cfg);
+int oc_optcuts_create(oc_optimizer* opt, oc_mesh* mesh, const oc_optcuts_config* cfg, oc_optcuts** out);
+int oc_optcuts_destroy(oc_optcuts* oc);
+/* at most maxSteps passes of preDrawFunc; *finished = 1 once the outer loop
+ * ended (converge_preDrawFunc, incl. its exact final solve) */
+int oc_optcuts_run(oc_optcuts* oc, int maxSteps, int* finished);
+/* out[12]: E_SD, E_se (seam length / virtualRadius), lambda, E_w, Newton
+ * iterations, topology steps, finished, vertices, and the milliseconds spent
+ * in Newton iterations, topology queries, applied operations, in total */
+int oc_optcuts_state(oc_optcuts* oc, double* out12);
+/* one row per outer event: Newton iterations, E_SD, E_se, lambda,
+ * vertices, code (0 inner loop converged, 1 boundary split or merge applied,
+ * 2 interior split, 3 interior split after widening the filter, 4/5/6
+ * critical-lambda boundary split / interior split / merge, 10 oscillation
+ * (rolled back to the best feasible state), 11 converged at the bound,
+ * 12 no merge left) */
+int oc_optcuts_events(const oc_optcuts* oc, int* nRows, double* rows);
+/* one row per Newton iteration: iterations, E_w, E_SD, E_se, lambda, vertices */
+int oc_optcuts_trace(const oc_optcuts* oc, int* nRows, double* rows);
 /* the mesh's current topology: counts, and into non-NULL arrays F, V_rest, cohE */
 int oc_mesh_get_topology(oc_mesh* mesh, int* nV, int* nF, int* nCohE, int* F, double* Vrest, int* cohE);
 /* host only: the operation on plain arrays; outputs hold nV + 2 vertices and

@@ -52,6 +52,12 @@ class OptimizerConfig(ctypes.Structure):
                 ("scaffoldPattern", ctypes.c_int), ("hessianProjection", ctypes.c_int), ("ordering", ctypes.c_int)]
 
 
+class OptCutsConfig(ctypes.Structure):
+    _fields_ = [("upperBound", ctypes.c_double), ("bijective", ctypes.c_int), ("topoLineSearch", ctypes.c_int),
+                ("filterExp", ctypes.c_double), ("topoOptions", ctypes.c_int), ("mlp", _vp),
+                ("topFrac", ctypes.c_double), ("maxNewtonIters", ctypes.c_int)]
+
+
 SOLVER_DIRECT = 0
 SOLVER_PCG = 1
 HESSIAN_REDUCED, HESSIAN_JACOBI6, HESSIAN_HYBRID = 0, 1, 2
@@ -157,6 +163,23 @@ _SIGS = {
     "oc_optimizer_system_size": [_vp, _i],
     "oc_optimizer_last_vectors": [_vp, _d, _d],
     "oc_optimizer_bad_pivots": [_vp, _i],
+    "oc_topology_queries": [_vp, _i, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
+                            ctypes.c_double, ctypes.POINTER(_vp)],
+    "oc_topology_query_tail": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_vp)],
+    "oc_mesh_fracture_tails": [_vp, _i],
+    "oc_mesh_set_fracture_tails": [_vp, _i],
+    "oc_mesh_seam_length": [_vp, _d],
+    "oc_optimizer_last_edec": [_vp, _d],
+    "oc_optimizer_set_allow_edec_rel_tol": [_vp, ctypes.c_int],
+    "oc_optimizer_get_energy_param": [_vp, _d],
+    "oc_optimizer_set_state": [_vp, ctypes.c_int, _d, _d, ctypes.c_int, _i, ctypes.c_int, _i, _i, ctypes.c_int],
+    "oc_optcuts_default_config": [_vp],
+    "oc_optcuts_create": [_vp, _vp, _vp, ctypes.POINTER(_vp)],
+    "oc_optcuts_destroy": [_vp],
+    "oc_optcuts_run": [_vp, ctypes.c_int, _i],
+    "oc_optcuts_state": [_vp, _d],
+    "oc_optcuts_events": [_vp, _i, _d],
+    "oc_optcuts_trace": [_vp, _i, _d],
     "oc_sd_energy_trials_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
                                     _vp, _vp],
 }
@@ -666,6 +689,74 @@ def bf16_gemm(A, B, tensor_cores=True, a_transposed=False, b_transposed=False, c
     ctx.check(lib().oc_bf16_gemm(ctx.h, M, N, K, _pf(A), sam, sak, _pf(B), sbk, sbn, _pf(C),
                                  1 if tensor_cores else 0), "bf16_gemm")
     return C
+
+
+class OptCuts:
+    """The OptCuts outer loop (src/main.cpp:538-1086, offline preDrawFunc with
+    updateLambda_stationaryV and converge_preDrawFunc) over a precomputed
+    Optimizer: inner Newton loops with fracture propagation, topology steps,
+    dual lambda updates, oscillation rollback, convergence at b_d.  The
+    optimizer's mesh must carry the cohesive edges of its initial cut."""
+
+    STATE = ["E_SD", "E_se", "lambda", "E_w", "newton_iterations", "topology_steps", "finished", "vertices",
+             "newton_ms", "query_ms", "apply_ms", "total_ms"]
+    EVENTS = {0: "inner converged", 1: "split or merge", 2: "interior split", 3: "interior split (wider filter)",
+              4: "critical-lambda split", 5: "critical-lambda interior split", 6: "critical-lambda merge",
+              10: "oscillation", 11: "converged at bound", 12: "no merge left"}
+
+    def __init__(self, optimizer, upperBound=4.1, bijective=False, topoLineSearch=True, filterExp=0.6, fp32=False,
+                 mlp=None, topFrac=0.1, maxNewtonIters=100000):
+        self.opt = optimizer
+        self.ctx = optimizer.ctx
+        cfg = OptCutsConfig()
+        lib().oc_optcuts_default_config(ctypes.byref(cfg))
+        cfg.upperBound, cfg.bijective, cfg.topoLineSearch = float(upperBound), int(bool(bijective)), int(topoLineSearch)
+        cfg.filterExp, cfg.topoOptions = float(filterExp), 1 if fp32 else 0
+        cfg.mlp = mlp.h if mlp is not None else None
+        cfg.topFrac, cfg.maxNewtonIters = float(topFrac), int(maxNewtonIters)
+        self._mlp = mlp
+        h = _vp()
+        self.ctx.check(lib().oc_optcuts_create(optimizer.h, optimizer.data.h, ctypes.byref(cfg), ctypes.byref(h)),
+                       "OptCuts")
+        self.h = h
+
+    def run(self, maxSteps=1000000):
+        """Outer passes until the loop ends; returns whether it finished."""
+        f = ctypes.c_int()
+        self.ctx.check(lib().oc_optcuts_run(self.h, int(maxSteps), ctypes.byref(f)), "OptCuts.run")
+        self.opt.data._sync_topology()
+        return bool(f.value)
+
+    def state(self):
+        out = np.zeros(12)
+        self.ctx.check(lib().oc_optcuts_state(self.h, _pd(out)), "OptCuts.state")
+        return dict(zip(self.STATE, out.tolist()))
+
+    def _rows(self, fn):
+        n = ctypes.c_int()
+        self.ctx.check(fn(self.h, ctypes.byref(n), None), "OptCuts")
+        out = np.zeros((n.value, 6))
+        self.ctx.check(fn(self.h, ctypes.byref(n), _pd(out)), "OptCuts")
+        return out
+
+    def events(self):
+        """rows: Newton iterations, E_SD, E_se, lambda, vertices, event code"""
+        return self._rows(lib().oc_optcuts_events)
+
+    def trace(self):
+        """rows per Newton iteration: iterations, E_w, E_SD, E_se, lambda, vertices"""
+        return self._rows(lib().oc_optcuts_trace)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().oc_optcuts_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class MLP:

@@ -35,6 +35,7 @@ UNITS = {
     "oc_mlp.cu": [],
     "oc_tc.cu": [],
     "oc_local.cu": [],
+    "oc_outer.cpp": ["-Xcompiler", "-fvisibility=default"],
 }
 HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h", "oc_elem.cuh"]
 

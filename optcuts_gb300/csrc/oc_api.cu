@@ -46,6 +46,9 @@ struct oc_mesh {
     double* tmpF = nullptr;         // nF x 36 scratch for API outputs (lazy)
     std::shared_ptr<oc::TopoAdjacency> adj;   // adjacency of F for topology queries (lazy)
     std::shared_ptr<oc::TopoWorkspace> topoWs;   // device buffers of the batched local solves (lazy)
+    // fracture tails (TriMesh::curFracTail, curInteriorFracTails), kept by
+    // the applied operations for fracture propagation
+    int tails[3] = {-1, -1, -1};
 };
 
 struct oc_linsys {
@@ -72,6 +75,7 @@ struct oc_optimizer {
     double lastEnergyVal = 0.0, lastEDec = 0.0;
     int globalIterNum = 0;
     bool precomputed = false;
+    bool allowEDecRelTol = true;   // Optimizer::setAllowEDecRelTol (Optimizer.cpp:148-151)
     double2 *g = nullptr, *dir = nullptr, *uv0 = nullptr;
     // last-step diagnostics
     double lastStep = 0.0, lastRelRes = 0.0, lastGsq = 0.0;
@@ -428,9 +432,12 @@ void free_bsr(oc::DeviceBsr& b)
     b = oc::DeviceBsr{};
 }
 
+// mask: fixed rows for the pattern (diagonal only); rowFixed (optional):
+// the fixed rows for the values where they differ (rows kept in the pattern
+// but assembled as fixed, e.g. the padding slots of a scaffold clique)
 int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::vector<unsigned char>& mask,
                        const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr,
-                       const double* xy = nullptr)
+                       const double* xy = nullptr, const std::vector<unsigned char>* rowFixed = nullptr)
 {
     oc_ctx* ctx = ls->ctx;
     auto t = std::chrono::steady_clock::now();
@@ -438,7 +445,7 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx, extraF, nExtraF, clique);
     ls->patternHostMs = ms_since(t);
     ls->patternDevMs = 0.0;
-    ls->rowFixed = mask;
+    ls->rowFixed = rowFixed ? *rowFixed : mask;
     free_bsr(ls->b);
     oc::pcg_free(ls->wk);
     cudaFree(ls->tmpIn); cudaFree(ls->tmpOut);
@@ -458,7 +465,7 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     OC_CUDA(ctx, upload(b.rowPtr, ls->rowPtr.data(), nV + 1, st));
     OC_CUDA(ctx, upload(b.col, ls->col.data(), b.nnzb, st));
     OC_CUDA(ctx, upload(b.diagSlot, ls->diagSlot.data(), nV, st));
-    OC_CUDA(ctx, upload(b.rowFixed, mask.data(), nV, st));
+    OC_CUDA(ctx, upload(b.rowFixed, ls->rowFixed.data(), nV, st));
     OC_CUDA(ctx, upload(b.cPtr, cPtr.data(), cPtr.size(), st));
     OC_CUDA(ctx, upload(b.cIdx, cIdx.data(), cIdx.size(), st));
     OC_CUDA(ctx, cudaMemsetAsync(b.val, 0, sizeof(oc::Blk2) * (size_t)(b.nnzb ? b.nnzb : 1), st));
@@ -807,8 +814,10 @@ static int apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, 
     std::vector<int> F(m->F), cohE(m->cohE);
     std::vector<double> Vrest(m->Vrest);
     std::string err;
-    int rc = oc::topo_apply(opType, path, pathLen, newVertPos, posRows, F, Vrest, uv, cohE, &err);
+    int tails[3] = {m->tails[0], m->tails[1], m->tails[2]};
+    int rc = oc::topo_apply(opType, path, pathLen, newVertPos, posRows, F, Vrest, uv, cohE, &err, tails);
     if (rc) return fail(m->ctx, rc, err);
+    std::copy(tails, tails + 3, m->tails);
     m->F.swap(F);
     m->Vrest.swap(Vrest);
     m->cohE.swap(cohE);
@@ -893,7 +902,8 @@ int oc_topology_query_learned(oc_mesh* m, int opType, double lambda_t, double fi
 
 // the operations ops[0..nOps) on the mesh's current state, solved together
 static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, double filterExp,
-                            const oc::TopoOptions& opts, oc_topo_result** out)
+                            const oc::TopoOptions& opts, oc_topo_result** out, const int* candVerts = nullptr,
+                            int nCandVerts = 0, int mergeFork = -2)
 {
     if (!m || !out || nOps <= 0) return OC_ERR_INVALID;
     bool split = false;
@@ -906,7 +916,7 @@ static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_
     std::vector<double> uv(2 * (size_t)nV), dg;
     OC_CUDA(m->ctx, cudaMemcpyAsync(uv.data(), m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToHost, m->ctx->stream));
     OC_CUDA(m->ctx, cudaStreamSynchronize(m->ctx->stream));
-    if (split) {
+    if (split && !candVerts) {
         dg.resize(nV);
         int rc = oc_mesh_split_filter(m, dg.data());
         if (rc) return rc;
@@ -938,6 +948,9 @@ static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_
     in.bigCluster = bigCluster;
     if (!m->topoWs) m->topoWs = std::make_shared<oc::TopoWorkspace>();
     in.ws = m->topoWs.get();
+    in.candVerts = candVerts;
+    in.nCandVerts = nCandVerts;
+    in.mergeFork = mergeFork;
     std::vector<oc::TopoOpResult> res(nOps);
     std::string err;
     const int rc = oc::topo_query_ops(in, ops, nOps, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, res.data(),
@@ -988,6 +1001,75 @@ int oc_topology_step(oc_mesh* m, double lambda_t, double filterExp, int options,
     *split = r[0];
     *merge = r[1];
     *interior = r[2];
+    return OC_OK;
+}
+
+int oc_topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, double filterExp, int options,
+                        oc_mlp* mlp, double topFrac, oc_topo_result** out)
+{
+    if (!ops || !out || nOps <= 0 || nOps > 3) return OC_ERR_INVALID;
+    if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
+    oc::TopoOptions opts;
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    if (mlp) {
+        opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+        opts.mlp = &mlp->m;
+        opts.topFrac = topFrac;
+    }
+    return topology_queries(m, ops, nOps, lambda_t, filterExp, opts, out);
+}
+
+int oc_topology_query_tail(oc_mesh* m, int opType, double lambda_t, int options, oc_topo_result** out)
+{
+    // querySplit / queryMerge with propagate = true (TriMesh.cpp:637-665,
+    // 828-833): boundary splits at the current fracture tail (or at the two
+    // ends of the last interior split), merges of the pair forking there
+    if (!m || !out || (opType != oc::kOpBoundarySplit && opType != oc::kOpMerge)) return OC_ERR_INVALID;
+    oc::TopoOptions opts;
+    opts.flags = options & oc::kTopoFp32Hessian;
+    if (opType == oc::kOpMerge) return topology_queries(m, &opType, 1, lambda_t, 0.6, opts, out, nullptr, 0, m->tails[0]);
+    int verts[2] = {-1, -1};
+    int n = 0;
+    if (m->tails[0] >= 0) verts[n++] = m->tails[0];
+    else if (m->tails[1] >= 0) {
+        verts[n++] = m->tails[1];
+        verts[n++] = m->tails[2];
+    }
+    return topology_queries(m, &opType, 1, lambda_t, 0.6, opts, out, verts, n);
+}
+
+int oc_mesh_fracture_tails(oc_mesh* m, int* tails3)
+{
+    if (!m || !tails3) return OC_ERR_INVALID;
+    std::copy(m->tails, m->tails + 3, tails3);
+    return OC_OK;
+}
+
+int oc_mesh_set_fracture_tails(oc_mesh* m, const int* tails3)
+{
+    if (!m || !tails3) return OC_ERR_INVALID;
+    for (int k = 0; k < 3; ++k)
+        if (tails3[k] < -1 || tails3[k] >= m->d.nV) return fail(m->ctx, OC_ERR_INVALID, "fracture tail out of range");
+    std::copy(tails3, tails3 + 3, m->tails);
+    return OC_OK;
+}
+
+int oc_mesh_seam_length(oc_mesh* m, double* seamLen)
+{
+    // TriMesh::computeSeamSparsity (TriMesh.cpp:1542-1558), triSoup off and
+    // no initial seam length: rest length of every interior cohesive pair
+    if (!m || !seamLen) return OC_ERR_INVALID;
+    double s = 0.0;
+    const double* Vr = m->Vrest.data();
+    for (size_t r = 0; r < m->cohE.size() / 4; ++r) {
+        const int* c = &m->cohE[4 * r];
+        if (std::min(std::min(c[0], c[1]), std::min(c[2], c[3])) < 0) continue;
+        const double dx = Vr[3 * (size_t)c[0]] - Vr[3 * (size_t)c[1]];
+        const double dy = Vr[3 * (size_t)c[0] + 1] - Vr[3 * (size_t)c[1] + 1];
+        const double dz = Vr[3 * (size_t)c[0] + 2] - Vr[3 * (size_t)c[1] + 2];
+        s += std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    *seamLen = s;
     return OC_OK;
 }
 
@@ -1552,9 +1634,15 @@ static int ensure_pattern(oc_optimizer* o)
                     if (o->bnd[i] == v) mask[v] = 2;
             for (int v = o->nWholeReal; v < o->nWhole; ++v) mask[v] = 1;
             if (o->cliqueMode) {
+                // every air slot keeps its clique rows in the pattern, so that
+                // a later air mesh with more air vertices fits it; the slots
+                // this air mesh leaves unused are assembled as fixed rows
                 std::vector<int> clique(o->bnd);
                 for (int v = nV; v < o->nWhole; ++v) clique.push_back(v);
-                rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, nullptr, 0, &clique, xyp);
+                std::vector<unsigned char> pmask(mask);
+                for (int v = o->nWholeReal; v < o->nWhole; ++v) pmask[v] = 0;
+                rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, pmask, nullptr, 0, &clique, xyp,
+                                        &mask);
             }
             else {
                 rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, o->airFw.data(),
@@ -1774,7 +1862,8 @@ static int solve_one(oc_optimizer* o, int* converged)
     record(o, 7);
     o->lastEDec = o->lastEnergyVal - testE;
     if (o->scaf) o->lastEDec += (-lastScaf0 + testScaf);   // Optimizer.cpp:632-634
-    if ((o->lastEDec / o->lastEnergyVal < 1.0e-6 * accepted) && (accepted > 1.0e-3)) stopped = true;   // :635-638
+    if (o->allowEDecRelTol && (o->lastEDec / o->lastEnergyVal < 1.0e-6 * accepted) && (accepted > 1.0e-3))
+        stopped = true;   // :635-638
     o->lastEnergyVal = testE;
     o->eScaf = testScaf;
     o->lastStep = accepted;
@@ -1860,6 +1949,72 @@ int oc_optimizer_last_step(oc_optimizer* o, double* stepSize, int* pcgIters, dou
     if (lsLaunches) *lsLaunches = o->lastLsLaunches;
     if (gsq) *gsq = o->lastGsq;
     return OC_OK;
+}
+
+int oc_optimizer_last_edec(oc_optimizer* o, double* eDec)
+{
+    if (!o || !eDec) return OC_ERR_INVALID;
+    *eDec = o->lastEDec;
+    return OC_OK;
+}
+
+int oc_optimizer_set_allow_edec_rel_tol(oc_optimizer* o, int allow)
+{
+    if (!o) return OC_ERR_INVALID;
+    o->allowEDecRelTol = allow != 0;
+    return OC_OK;
+}
+
+int oc_optimizer_get_energy_param(oc_optimizer* o, double* energyParam)
+{
+    if (!o || !energyParam) return OC_ERR_INVALID;
+    *energyParam = o->param;
+    return OC_OK;
+}
+
+int oc_optimizer_set_state(oc_optimizer* o, int nV, const double* Vrest, const double* UV, int nF, const int* F,
+                           int nCohE, const int* cohE, const int* tails3, int iterNum)
+{
+    // Optimizer::setConfig (Optimizer.cpp:287-300): the result mesh replaced
+    // by a recorded one, the scaffold rebuilt, the energy data updated
+    if (!o || !o->precomputed || nV <= 0 || nF <= 0 || nCohE < 0 || !Vrest || !UV || !F || (nCohE && !cohE) ||
+        iterNum < 0)
+        return OC_ERR_INVALID;
+    oc_mesh* m = o->mesh;
+    // topology operations keep the triangle count (splits and merges move
+    // corners between vertices), so a recorded state of this run has it too
+    if (nF != m->d.nF) return fail(m->ctx, OC_ERR_INVALID, "set_state: triangle count differs from the mesh's");
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return fail(m->ctx, OC_ERR_INVALID, "set_state: vertex index out of range");
+    for (long long i = 0; i < 4LL * nCohE; ++i)
+        if (cohE[i] < -1 || cohE[i] >= nV) return fail(m->ctx, OC_ERR_INVALID, "set_state: cohesive edge out of range");
+    for (int v : m->fixed)
+        if (v >= nV) return fail(m->ctx, OC_ERR_INVALID, "set_state: fixed vertex out of range");
+    if (tails3)
+        for (int k = 0; k < 3; ++k)
+            if (tails3[k] < -1 || tails3[k] >= nV) return fail(m->ctx, OC_ERR_INVALID, "set_state: tail out of range");
+    m->F.assign(F, F + 3 * (size_t)nF);
+    m->Vrest.assign(Vrest, Vrest + 3 * (size_t)nV);
+    m->cohE.assign(cohE, cohE + 4 * (size_t)nCohE);
+    if (tails3) std::copy(tails3, tails3 + 3, m->tails);
+    std::vector<double> uv(UV, UV + 2 * (size_t)nV);
+    int rc = mesh_rebuild(m, uv);
+    if (rc) return rc;
+    rc = ensure_whole(o, nV);
+    if (rc) return rc;
+    if (!o->scaf) o->nWhole = o->nWholeReal = nV;
+    o->patternStale = true;
+    if (o->scaf) {
+        rc = oc_optimizer_rebuild_scaffold(o);
+        if (rc) return rc;
+    }
+    rc = ensure_pattern(o);
+    if (rc) return rc;
+    if (o->scaf)
+        OC_CUDA(m->ctx, cudaMemcpyAsync(o->wuv, m->d.uv, sizeof(double2) * nV, cudaMemcpyDeviceToDevice, m->ctx->stream));
+    o->globalIterNum = iterNum;
+    update_target_gres(o);
+    return compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
 }
 
 int oc_optimizer_bad_pivots(oc_optimizer* o, int* nBad)

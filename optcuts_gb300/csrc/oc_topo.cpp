@@ -580,7 +580,8 @@ void replace_in(std::vector<int>& F, const std::vector<int>& tris, int from, int
 } // namespace
 
 int topo_apply(int opType, const int* path, int pathLen, const double* pos, int posRows, std::vector<int>& F,
-               std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err)
+               std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err,
+               int* tails)
 {
     auto bad = [&](const char* m) {
         if (err) *err = m;
@@ -647,6 +648,10 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
                 else cohE[4 * (size_t)(-r - 1) + 3] = ni;
             }
         }
+        if (tails) {   // the interior end is the new tail, none for a cut-through
+            tails[0] = both ? -1 : vi;
+            tails[1] = tails[2] = -1;
+        }
         return OC_OK;
     }
     if (opType == kOpInteriorSplit) {
@@ -669,6 +674,11 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
         replace_in(F, left, vI, nn);
         cohE.insert(cohE.end(), {nn, path[0], vI, path[0]});
         cohE.insert(cohE.end(), {path[2], nn, path[2], vI});
+        if (tails) {
+            tails[0] = -1;
+            tails[1] = path[0];
+            tails[2] = path[2];
+        }
         return OC_OK;
     }
     if (opType == kOpMerge) {
@@ -710,6 +720,9 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
         if (b < back)
             for (int& c : cohE)
                 if (c == back) c = b;
+        // the merged vertex is the new tail (where it was the last vertex it
+        // now sits in b's slot; the reference keeps its old, removed index)
+        if (tails) tails[0] = (a == back && b < back) ? b : a;
         // close up a diamond that became whole
         for (size_t i = 0; i < cohE.size() / 4; ++i) {
             int* c = &cohE[4 * i];
@@ -718,6 +731,7 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
                 if (i < last)
                     for (int k = 0; k < 4; ++k) c[k] = cohE[4 * last + k];
                 cohE.resize(4 * last);
+                if (tails) tails[0] = -1;
                 break;
             }
         }
@@ -1096,12 +1110,12 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
     L.map = &vmap;
 
     if (opType == kOpBoundarySplit || opType == kOpInteriorSplit) {
-        if (!in.divGrad) {
+        if (!in.divGrad && !in.candVerts) {
             if (err) *err = "topology query: no split filter";
             return OC_ERR_INVALID;
         }
         std::vector<std::pair<double, int>> keyed;
-        for (int v = 0; v < in.nV; ++v) {
+        for (int v = 0; v < in.nV && !in.candVerts; ++v) {
             if (T.degree(v) <= 2) continue;   // cannot be split further
             if (opType == kOpBoundarySplit) {
                 if (T.bnd[v]) keyed.push_back({-in.divGrad[v] / 1.0, v});   // vertWeight = 1
@@ -1112,8 +1126,19 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
                 if (!toBound) keyed.push_back({-in.divGrad[v] / 1.0, v});
             }
         }
-        const std::vector<int> cands =
-            filter_candidates(keyed, opType == kOpBoundarySplit ? 0.8 : filterExp, candidatePool);
+        std::vector<int> cands;
+        if (in.candVerts) {
+            // propagation: the fracture tails themselves, evaluated as boundary
+            // splits (querySplit sets splitInterior = false, TriMesh.cpp:650-665;
+            // computeLocalLDec's boundary branch needs a boundary vertex)
+            for (int i = 0; i < in.nCandVerts; ++i)
+                if (in.candVerts[i] >= 0 && in.candVerts[i] < in.nV && T.bnd[in.candVerts[i]])
+                    cands.push_back(in.candVerts[i]);
+            candidatePool = static_cast<int>(cands.size());
+        }
+        else {
+            cands = filter_candidates(keyed, opType == kOpBoundarySplit ? 0.8 : filterExp, candidatePool);
+        }
         out.resize(cands.size());
         for (size_t ci = 0; ci < cands.size(); ++ci) {
             TopoCandidate& C = out[ci];
@@ -1290,6 +1315,7 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
             if (ce[0] == ce[2]) fork = 0;
             else if (ce[1] == ce[3]) fork = 1;
             else continue;
+            if (in.mergeFork != -2 && ce[fork] != in.mergeFork) continue;   // propagation (TriMesh.cpp:828-833)
             const int va = ce[1 - fork], vb = ce[3 - fork];
             std::vector<int> triangles;
             int firstAmt = 0;

@@ -58,6 +58,13 @@ struct TopoQueryIn {
     int bigCluster = 0;              // largest cluster of blocks per local problem (0: the device's, 16 or 8)
     TopoWorkspace* ws = nullptr;     // reused device buffers (a temporary one when null)
     cudaStream_t st = nullptr;
+    // fracture propagation (querySplit / queryMerge with propagate = true,
+    // TriMesh.cpp:637-665, 828-833): the split candidates are exactly these
+    // vertices (no filter), the merge candidates only the zipper-bottom pairs
+    // forking at mergeFork (-1: none); mergeFork -2 = no restriction
+    const int* candVerts = nullptr;
+    int nCandVerts = 0;
+    int mergeFork = -2;
 };
 
 struct TopoStats {
@@ -126,8 +133,14 @@ int mlp_predict_host(Mlp& m, const float* X, int n, float* y);
 // interior split TriMesh::cutPath (one appended vertex, two cohesive rows),
 // merge TriMesh::mergeBoundaryEdges (the merged copy removed by moving the
 // last vertex into its slot).
+// tails (optional, in/out): the fracture tails the reference keeps on the
+// TriMesh -- curFracTail and curInteriorFracTails -- updated as
+// splitEdgeOnBoundary (TriMesh.cpp:2891-2899), an interior split through
+// createFracture / splitOrMerge (Optimizer.cpp:397-399, TriMesh.cpp:1039-1043)
+// and mergeBoundaryEdges (TriMesh.cpp:3046-3048, 3169-3171) do.
 int topo_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, std::vector<int>& F,
-               std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err);
+               std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err,
+               int* tails = nullptr);
 
 // igl::cut_to_disk as the reference vendors it (src/Utils/cut_to_disk.cpp):
 // the cut graph of a genus >= 1 surface as vertex lists (a closed loop

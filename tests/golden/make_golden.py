@@ -74,7 +74,13 @@ CASES = {
     # the genus-1 torus workload (cut_to_disk + Tutte, scaffold on) run to
     # convergence
     "torus_41k_conv": ("torus_41k", 0.999, 3000, 16, False, ["slim"]),
+    # whole OptCuts runs (outer loop: dual updates, topology steps,
+    # propagation, rollback) to b_d = 4.1, bijectivity off
+    "icosphere_320_outer": ("icosphere_320", 0.999, 5000, 16, False, ["outer", "nobij"]),
+    "icosphere_1k_outer": ("icosphere_1k", 0.999, 5000, 16, False, ["outer", "nobij"]),
+    "icosphere_5k_outer": ("icosphere_5k", 0.999, 5000, 16, False, ["outer", "nobij"]),
 }
+OUTER_KEYS = ("outer_events", "outer_final", "outer_V", "outer_F", "outer_Vrest", "outer_cohE")
 SLIM_KEYS = ("scalars", "trace_E", "trace_Etot", "trace_gsq", "trace_alpha", "trace_status", "scaf_V", "scaf_F",
              "scaf_bnd", "scaf_fixed", "scaf_off", "uv0_check")
 
@@ -105,7 +111,7 @@ def run_case(name, key, lam, iters, hmax, states, flags):
         meshes.write_obj(obj, V, F)
         out = os.path.join(td, "out") + "/"
         os.makedirs(out)
-        args = [DRIVER, obj, out, repr(lam), str(iters)] + ([] if slim else ["hess"]) + \
+        args = [DRIVER, obj, out, repr(lam), str(iters)] + ([] if slim or "outer" in flags else ["hess"]) + \
             (["states"] if states else []) + flags
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
                        env=dict(os.environ, OC_REF_THREADS="1"))
@@ -119,6 +125,14 @@ def run_case(name, key, lam, iters, hmax, states, flags):
                     pack[k] = ld(k)
             np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack)
             pack.update(UV0=uv0, F=ld("F"))
+            return pack
+        if "outer" in flags:
+            pack = dict(V_rest=ld("V_rest"), UV0=ld("UV0"), F=ld("F"), fixedVert=ld("fixedVert"), cohE=ld("cohE"),
+                        scalars=ld("scalars"), mesh_V=V, mesh_F=F)
+            for k in OUTER_KEYS:
+                pack[k] = ld(k)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), **pack)
+            pack["trace_E"] = pack["outer_final"][:1]
             return pack
         Fm, fixed = ld("F"), ld("fixedVert")
         nt = len(Fm) if hmax is None else min(hmax, len(Fm))

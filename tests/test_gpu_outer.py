@@ -1,0 +1,76 @@
+"""The OptCuts outer loop on the GPU against whole runs of the reference.
+
+The reference driver (oracle/ref/ref_outer.cpp restating src/main.cpp's
+offline preDrawFunc, updateLambda_stationaryV and converge_preDrawFunc)
+ran each mesh from its Tutte start to the end of the outer loop with
+b_d = 4.1 and bijectivity off (tests/golden/*_outer.npz).  The GPU run
+starts from the same state and must end the same way: finished, E_SD at the
+bound (b_d - 1e-3 <= E_SD <= b_d, or the oscillation stop below it), E_SD,
+E_se and lambda within 0.5% of the reference's, and no inverted triangle.
+The sequence of operations is compared up to the first divergence: the
+runs are the same discrete process, and a topology decision taken on energy
+changes that agree to 1e-6 may still flip on a near-tie."""
+import numpy as np
+import pytest
+
+import optcuts_gb300 as oc
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["icosphere_320_outer", "icosphere_1k_outer", "icosphere_5k_outer"]
+
+
+def run_outer(g, **kw):
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"])
+    m.setCohesiveEdges(g["cohE"])
+    opt = oc.Optimizer(m, [1.0 - g["scalars"][4]])
+    opt.precompute()
+    o = oc.OptCuts(opt, upperBound=4.1, **kw)
+    finished = o.run()
+    return m, opt, o, finished
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_outer_loop_matches_reference(golden, case):
+    g = golden(case)
+    m, opt, o, finished = run_outer(g)
+    ref = g["outer_final"]
+    st = o.state()
+    assert finished and ref[5] == 1
+    assert m.checkInversion()
+    assert st["E_SD"] <= 4.1 + 1e-12
+    for k, i in (("E_SD", 0), ("E_se", 1), ("lambda", 2)):
+        assert abs(st[k] - ref[i]) <= 5e-3 * abs(ref[i]), (k, st[k], ref[i])
+    ev, rev = o.events(), g["outer_events"]
+    assert len(ev) > 0 and ev[0, 5] == 0 and rev[0, 5] == 0
+    # the first inner loop converges to the same state before any topology change
+    assert abs(ev[0, 1] - rev[0, 1]) <= 1e-3 * rev[0, 1]
+
+
+def test_outer_loop_first_decisions_match(golden):
+    """On the 1k icosphere the first topology steps (the dual update, the
+    first boundary split and the critical-lambda splits after it) are the
+    reference's: same event codes and vertex counts until the first
+    divergence, which must not come before the third operation."""
+    g = golden("icosphere_1k_outer")
+    _, _, o, _ = run_outer(g)
+    ev, rev = o.events(), g["outer_events"]
+    n = min(len(ev), len(rev))
+    same = 0
+    while same < n and ev[same, 5] == rev[same, 5] and ev[same, 4] == rev[same, 4]:
+        same += 1
+    assert same >= 6, (ev[:8], rev[:8])
+
+
+def test_outer_loop_trace_and_state(golden):
+    g = golden("icosphere_320_outer")
+    m, opt, o, finished = run_outer(g)
+    tr = o.trace()
+    st = o.state()
+    assert finished and len(tr) > 0
+    assert tr[-1, 0] <= st["newton_iterations"]
+    assert st["topology_steps"] >= 1 and st["vertices"] == m.nV
+    assert st["total_ms"] >= st["newton_ms"] >= 0.0
+    # E_w of every row is lambda-weighted: (1 - lambda) E_SD + lambda E_se
+    lam = tr[:, 4]
+    np.testing.assert_allclose(tr[:, 1], (1 - lam) * tr[:, 2] + lam * tr[:, 3], rtol=1e-12)
