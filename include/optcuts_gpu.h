@@ -168,6 +168,13 @@ int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF,
 /* update_a(I, J, V) (LinSysSolver.hpp:138-159): triplets with I <= J are summed
  * into the matrix (mirrored to the lower half), the rest are ignored. */
 int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* V, int nTriplets);
+/* LinSysSolver::set_pattern(vNeighbor, fixedVert) (LinSysSolver.hpp:37-135,
+ * called by Optimizer.cpp:174, 358, 524): the pattern from per-vertex
+ * neighbour lists (CSR: the neighbours of v are nbIdx[nbPtr[v] .. nbPtr[v+1]),
+ * either or both directions of a pair may be listed); fixed vertices keep
+ * only their diagonal block.  Then analyze_pattern as oc_linsys_set_pattern. */
+int oc_linsys_set_pattern_neighbors(oc_linsys* ls, int nV, const int* nbPtr, const int* nbIdx, const int* fixedVert,
+                                   int nFixed);
 /* factorize() (EigenLibSolver.cpp:80-93): numeric Cholesky (direct) or the
  * block-Jacobi preconditioner (PCG).  OC_ERR_NOT_SPD if a pivot or diagonal
  * block was not positive (the factorisation still completes). */

@@ -163,6 +163,7 @@ _SIGS = {
     "oc_optimizer_system_size": [_vp, _i],
     "oc_optimizer_last_vectors": [_vp, _d, _d],
     "oc_optimizer_bad_pivots": [_vp, _i],
+    "oc_linsys_set_pattern_neighbors": [_vp, ctypes.c_int, _i, _i, _i, ctypes.c_int],
     "oc_topology_queries": [_vp, _i, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
                             ctypes.c_double, ctypes.POINTER(_vp)],
     "oc_topology_query_tail": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_vp)],
@@ -515,6 +516,18 @@ class LinSysSolver:
     def set_pattern(self, nV, F, fixedVert):
         F, fx = _i4(F), _i4(np.asarray(fixedVert).reshape(-1))
         self.ctx.check(lib().oc_linsys_set_pattern(self.h, nV, _pi(F), len(F), _pi(fx), len(fx)), "set_pattern")
+        self.numRows = 2 * nV
+
+    def set_pattern_neighbors(self, vNeighbor, fixedVert):
+        """set_pattern(vNeighbor, fixedVert) as the reference's Optimizer calls
+        it: vNeighbor a list of neighbour-index lists, one per vertex."""
+        nV = len(vNeighbor)
+        ptr = np.zeros(nV + 1, np.int32)
+        ptr[1:] = np.cumsum([len(n) for n in vNeighbor])
+        idx = _i4(np.concatenate([np.asarray(list(n), np.int32) for n in vNeighbor]) if nV else np.zeros(0))
+        fx = _i4(np.asarray(list(fixedVert)).reshape(-1))
+        self.ctx.check(lib().oc_linsys_set_pattern_neighbors(self.h, nV, _pi(ptr), _pi(idx), _pi(fx), len(fx)),
+                       "set_pattern")
         self.numRows = 2 * nV
 
     def update_a(self, I, J, V):

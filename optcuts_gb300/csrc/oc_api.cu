@@ -305,7 +305,7 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
 void build_pattern(int nV, const int* F, int nF, const std::vector<unsigned char>& fixedMask,
                    std::vector<int>& rowPtr, std::vector<int>& col, std::vector<int>& diagSlot,
                    std::vector<int>& cPtr, std::vector<int>& cIdx, const int* extraF = nullptr, int nExtraF = 0,
-                   const std::vector<int>* clique = nullptr)
+                   const std::vector<int>* clique = nullptr, const int* nbPtr = nullptr, const int* nbIdx = nullptr)
 {
     // candidate neighbours per row (counted, then filled), then each row
     // sorted and deduplicated on host threads and compacted
@@ -324,6 +324,17 @@ void build_pattern(int nV, const int* F, int nF, const std::vector<unsigned char
         for (int va : *clique)
             if (!fixedMask[va]) cliqueFree.push_back(va);
     for (int va : cliqueFree) cnt[va + 1] += static_cast<int>(cliqueFree.size()) - 1;
+    // vertex neighbour lists (TriMesh::vNeighbor): both directions of each
+    // listed pair between free vertices
+    if (nbPtr)
+        for (int va = 0; va < nV; ++va)
+            for (int p = nbPtr[va]; p < nbPtr[va + 1]; ++p) {
+                const int vb = nbIdx[p];
+                if (vb != va && !fixedMask[va] && !fixedMask[vb]) {
+                    cnt[va + 1]++;
+                    cnt[vb + 1]++;
+                }
+            }
     for (int v = 0; v < nV; ++v) cnt[v + 1] += cnt[v];
     std::vector<int> raw(cnt[nV]);
     std::vector<int> fillPos(cnt.begin(), cnt.end() - 1);
@@ -343,6 +354,15 @@ void build_pattern(int nV, const int* F, int nF, const std::vector<unsigned char
     for (int va : cliqueFree)
         for (int vb : cliqueFree)
             if (vb != va) raw[fillPos[va]++] = vb;
+    if (nbPtr)
+        for (int va = 0; va < nV; ++va)
+            for (int p = nbPtr[va]; p < nbPtr[va + 1]; ++p) {
+                const int vb = nbIdx[p];
+                if (vb != va && !fixedMask[va] && !fixedMask[vb]) {
+                    raw[fillPos[va]++] = vb;
+                    raw[fillPos[vb]++] = va;
+                }
+            }
     std::vector<int> uniq(nV);
     oc::host_parallel_for(nV, 4096, [&](size_t v0, size_t v1) {
         for (size_t v = v0; v < v1; ++v) {
@@ -437,12 +457,14 @@ void free_bsr(oc::DeviceBsr& b)
 // but assembled as fixed, e.g. the padding slots of a scaffold clique)
 int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::vector<unsigned char>& mask,
                        const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr,
-                       const double* xy = nullptr, const std::vector<unsigned char>* rowFixed = nullptr)
+                       const double* xy = nullptr, const std::vector<unsigned char>* rowFixed = nullptr,
+                       const int* nbPtr = nullptr, const int* nbIdx = nullptr)
 {
     oc_ctx* ctx = ls->ctx;
     auto t = std::chrono::steady_clock::now();
     std::vector<int> cPtr, cIdx;
-    build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx, extraF, nExtraF, clique);
+    build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx, extraF, nExtraF, clique, nbPtr,
+                  nbIdx);
     ls->patternHostMs = ms_since(t);
     ls->patternDevMs = 0.0;
     ls->rowFixed = rowFixed ? *rowFixed : mask;
@@ -1380,6 +1402,25 @@ int oc_linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const int
         mask[fixedVert[i]] = 1;
     }
     return linsys_set_pattern(ls, nV, F, nF, mask);
+}
+
+int oc_linsys_set_pattern_neighbors(oc_linsys* ls, int nV, const int* nbPtr, const int* nbIdx, const int* fixedVert,
+                                   int nFixed)
+{
+    // LinSysSolver::set_pattern(vNeighbor, fixedVert) (LinSysSolver.hpp:37-135)
+    if (!ls || nV <= 0 || !nbPtr || nFixed < 0 || (nFixed && !fixedVert)) return OC_ERR_INVALID;
+    if (nbPtr[0] != 0) return fail(ls->ctx, OC_ERR_INVALID, "set_pattern: neighbour offsets must start at 0");
+    for (int v = 0; v < nV; ++v)
+        if (nbPtr[v + 1] < nbPtr[v]) return fail(ls->ctx, OC_ERR_INVALID, "set_pattern: decreasing neighbour offsets");
+    if (nbPtr[nV] && !nbIdx) return OC_ERR_INVALID;
+    for (int p = 0; p < nbPtr[nV]; ++p)
+        if (nbIdx[p] < 0 || nbIdx[p] >= nV) return fail(ls->ctx, OC_ERR_INVALID, "set_pattern: neighbour out of range");
+    std::vector<unsigned char> mask(nV, 0);
+    for (int i = 0; i < nFixed; ++i) {
+        if (fixedVert[i] < 0 || fixedVert[i] >= nV) return fail(ls->ctx, OC_ERR_INVALID, "set_pattern: fixed vertex out of range");
+        mask[fixedVert[i]] = 1;
+    }
+    return linsys_set_pattern(ls, nV, nullptr, 0, mask, nullptr, 0, nullptr, nullptr, nullptr, nbPtr, nbIdx);
 }
 
 int oc_linsys_update_a(oc_linsys* ls, const int* I, const int* J, const double* V, int n)
