@@ -496,8 +496,30 @@ int oc_optcuts_state(oc_optcuts* oc, double* out12);
  * (rolled back to the best feasible state), 11 converged at the bound,
  * 12 no merge left) */
 int oc_optcuts_events(const oc_optcuts* oc, int* nRows, double* rows);
-/* one row per Newton iteration: iterations, E_w, E_SD, E_se, lambda, vertices */
+/* one row per Newton iteration: iterations, E_w, E_SD, E_se, lambda,
+ * vertices, ||gradient||^2 at the iteration's start */
 int oc_optcuts_trace(const oc_optcuts* oc, int* nRows, double* rows);
+/* The reference's output files of a run into directory dir (which must
+ * exist): energyValPerIter.txt and gradientPerIter.txt
+ * (Optimizer::writeEnergyValToFile / writeGradL2NormToFile,
+ * Optimizer.cpp:706-740: per Newton iteration E_w, E_SD, E_se/virtualRadius,
+ * energyParams[0]; ||g||^2 and the distortion term's own), info.txt
+ * (saveInfoForPresent, main.cpp:346-387: sizes, iteration counts, lambda,
+ * timings, E_SD and seam length, the four standard stretch measures, the
+ * initial seams) and finalResult_mesh.obj (TriMesh::saveAsMesh,
+ * TriMesh.cpp:1758-1969).  F0 (nF x 3, the input mesh's triangles, NULL:
+ * vertices merged along the cohesive edges) and nV0 give the OBJ's 3D
+ * vertex numbering; lambdaInit is info.txt's initial lambda. */
+int oc_optcuts_write(oc_optcuts* oc, const char* dir, const int* F0, int nV0, double lambdaInit);
+/* the mesh the outer loop edits, and TriMesh::initSeams (the cohesive edges
+ * of the initial cut, rows x 4, as the loop started) */
+int oc_optcuts_mesh(const oc_optcuts* oc, oc_mesh** mesh);
+int oc_optcuts_initial_seams(const oc_optcuts* oc, int* nRows, int* rows);
+/* TriMesh::saveAsMesh (TriMesh.cpp:1805-1969): rest positions indexed by F0
+ * (the input mesh's triangles, nF x 3; NULL: the cut mesh's vertices merged
+ * back along the cohesive edges), the current UV as texture coordinates
+ * (scaleUV: normalised to the unit square), faces "f v/vt". */
+int oc_mesh_write_obj(oc_mesh* mesh, const char* path, const int* F0, int nV0, int scaleUV);
 /* the mesh's current topology: counts, and into non-NULL arrays F, V_rest, cohE */
 int oc_mesh_get_topology(oc_mesh* mesh, int* nV, int* nF, int* nCohE, int* F, double* Vrest, int* cohE);
 /* host only: the operation on plain arrays; outputs hold nV + 2 vertices and

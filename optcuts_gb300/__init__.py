@@ -181,6 +181,10 @@ _SIGS = {
     "oc_optcuts_state": [_vp, _d],
     "oc_optcuts_events": [_vp, _i, _d],
     "oc_optcuts_trace": [_vp, _i, _d],
+    "oc_optcuts_write": [_vp, ctypes.c_char_p, _i, ctypes.c_int, ctypes.c_double],
+    "oc_optcuts_mesh": [_vp, ctypes.POINTER(_vp)],
+    "oc_optcuts_initial_seams": [_vp, _i, _i],
+    "oc_mesh_write_obj": [_vp, ctypes.c_char_p, _i, ctypes.c_int, ctypes.c_int],
     "oc_sd_energy_trials_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
                                     _vp, _vp],
 }
@@ -433,6 +437,13 @@ class TriMesh:
         self.ctx.check(lib().oc_mesh_apply_topology(self.h, op, _pi(path), len(path), _pd(pos), len(pos)),
                        "applyTopology")
         self._sync_topology()
+
+    def saveAsMesh(self, path, F0=None, nV0=0, scaleUV=False):
+        """TriMesh::saveAsMesh: OBJ with rest positions (in F0's input
+        numbering, or the copies glued along the seams) and the UV."""
+        f0 = _i4(F0) if F0 is not None else None
+        self.ctx.check(lib().oc_mesh_write_obj(self.h, os.fsencode(path), _pi(f0) if f0 is not None else None,
+                                               int(nV0), int(bool(scaleUV))), "saveAsMesh")
 
     def _sync_topology(self):
         nv, nf, nc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
@@ -745,20 +756,29 @@ class OptCuts:
         self.ctx.check(lib().oc_optcuts_state(self.h, _pd(out)), "OptCuts.state")
         return dict(zip(self.STATE, out.tolist()))
 
-    def _rows(self, fn):
+    def _rows(self, fn, cols):
         n = ctypes.c_int()
         self.ctx.check(fn(self.h, ctypes.byref(n), None), "OptCuts")
-        out = np.zeros((n.value, 6))
+        out = np.zeros((n.value, cols))
         self.ctx.check(fn(self.h, ctypes.byref(n), _pd(out)), "OptCuts")
         return out
 
     def events(self):
         """rows: Newton iterations, E_SD, E_se, lambda, vertices, event code"""
-        return self._rows(lib().oc_optcuts_events)
+        return self._rows(lib().oc_optcuts_events, 6)
 
     def trace(self):
-        """rows per Newton iteration: iterations, E_w, E_SD, E_se, lambda, vertices"""
-        return self._rows(lib().oc_optcuts_trace)
+        """rows per Newton iteration: iterations, E_w, E_SD, E_se, lambda,
+        vertices, ||gradient||^2"""
+        return self._rows(lib().oc_optcuts_trace, 7)
+
+    def write(self, folder, F0=None, nV0=0, lambdaInit=0.999):
+        """The reference's output files of the run into folder:
+        energyValPerIter.txt, gradientPerIter.txt, info.txt and
+        finalResult_mesh.obj (F0: the input mesh's triangles)."""
+        f0 = _i4(F0) if F0 is not None else None
+        self.ctx.check(lib().oc_optcuts_write(self.h, os.fsencode(folder), _pi(f0) if f0 is not None else None,
+                                              int(nV0), float(lambdaInit)), "OptCuts.write")
 
     def close(self):
         if getattr(self, "h", None):

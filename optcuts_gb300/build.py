@@ -36,6 +36,7 @@ UNITS = {
     "oc_tc.cu": [],
     "oc_local.cu": [],
     "oc_outer.cpp": ["-Xcompiler", "-fvisibility=default"],
+    "oc_output.cpp": ["-Xcompiler", "-fvisibility=default"],
 }
 HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h", "oc_elem.cuh"]
 

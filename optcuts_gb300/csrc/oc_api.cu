@@ -1843,6 +1843,12 @@ static int solve_one(oc_optimizer* o, int* converged)
     double step = 1.0;
     rc = read_min(m, &step);
     if (rc) return rc;
+    if (o->ls->kind == OC_SOLVER_DIRECT) {   // the substitutions' bounded waits
+        int timedOut = 0;
+        rc = oc::chol_solve_status(o->ls->chol, st, &timedOut);
+        if (rc) return fail(ctx, rc, "solve: substitution status");
+        if (timedOut) return fail(ctx, OC_ERR_TIMEOUT, "solve: a substitution wait ran out");
+    }
     record(o, 6);
     step *= 0.99;
     OC_CUDA(ctx, cudaMemcpyAsync(o->uv0, current_uv(o), sizeof(double2) * nSys, cudaMemcpyDeviceToDevice, st));

@@ -788,25 +788,85 @@ __global__ void k_permute_out(const double* __restrict__ xp, const int* __restri
     if (j < n) x[perm[j]] = xp[j];
 }
 
+// Bounded waits on shared-memory mbarriers inside one CTA.  A wait that runs
+// out (or sees that another thread gave up) sets the CTA's abort flag and
+// returns false; every loop then ends, the host reads the kernel's flag.
+constexpr int kSolveWaitPolls = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, int count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(b)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, uint32_t parity, volatile int* abort)
+{
+    const uint32_t a = smem_addr(b);
+    for (int i = 0; i < kSolveWaitPolls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+
+constexpr int kFwdThreads = 512;               // warp 0 solves, the other warps update
+constexpr int kFwdUpd = kFwdThreads - 32;
+
 // Forward substitution, pivot part of one front (one CTA per front of the
 // level): gather this front's right-hand side plus the children's update
-// vectors (fixed child order), solve the unit-lower L11 y = b in 32-column
-// blocks (warp-shuffle diagonal block, coalesced column updates of the
-// remaining pivot rows), store y (not yet divided by D) and the gathered
+// vectors (fixed child order), then solve the unit-lower L11 y = b in
+// 32-column blocks and store y (not yet divided by D) and the gathered
 // right-hand side of the non-pivot rows, which k_fwd_rect then updates.
-__global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
-                                             const int* __restrict__ fm, const long long* __restrict__ foff,
-                                             const long long* __restrict__ fupd, const int* __restrict__ fdof,
-                                             const int* __restrict__ childOff, const int* __restrict__ childList,
-                                             const int* __restrict__ relOff, const int* __restrict__ relIdx,
-                                             const double* __restrict__ pool, double* __restrict__ upd,
-                                             double* __restrict__ y)
+// Warp specialised, with one block of lookahead: warp 0 solves block j
+// (warp-shuffle chain on the staged diagonal block) after applying block
+// j-1's columns to block j's own rows; the other warps apply each solved
+// block's columns to the rows from block j+2 on.  A block's rows thus take
+// the blocks' columns in increasing order and, per block, one FMA chain in
+// column order -- the arithmetic of a plain right-looking sweep -- while the
+// bulk updates run behind the dependent chain instead of between its steps.
+// Hand-offs: per block an mbarrier "solved" (warp 0's 32 lanes) and
+// "updated" (the updaters), two of each alternating; waits are bounded.
+__global__ void __launch_bounds__(kFwdThreads) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
+                                                     const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                     const long long* __restrict__ fupd, const int* __restrict__ fdof,
+                                                     const int* __restrict__ childOff, const int* __restrict__ childList,
+                                                     const int* __restrict__ relOff, const int* __restrict__ relIdx,
+                                                     const double* __restrict__ pool, double* __restrict__ upd,
+                                                     double* __restrict__ y, int* __restrict__ flag)
 {
     extern __shared__ double sh[];
+    __shared__ double tile[32 * 33];   // the diagonal block, row-major (padded)
+    __shared__ unsigned long long solved[2], updated[2];
+    __shared__ int abortFlag;
     const int f = fronts[blockIdx.x];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : 0.0;
+    if (threadIdx.x == 0) {
+        mbar_init(&solved[0], 32);
+        mbar_init(&solved[1], 32);
+        mbar_init(&updated[0], kFwdUpd);
+        mbar_init(&updated[1], kFwdUpd);
+        abortFlag = 0;
+    }
     __syncthreads();
     for (int c = childOff[f]; c < childOff[f + 1]; ++c) {
         const int ch = childList[c];
@@ -817,56 +877,79 @@ __global__ void __launch_bounds__(256) k_fwd(const int* __restrict__ fronts, con
         __syncthreads();
     }
     const double* L = pool + foff[f];
-    __shared__ double tile[32 * 33];   // the diagonal block, row-major (padded)
-    for (int c0 = 0; c0 < k; c0 += 32) {
-        const int w = min(32, k - c0);
-        // stage the diagonal block (all loads in flight at once) so that the
-        // dependent chain below reads shared memory, not global memory
-        for (int e = threadIdx.x; e < 32 * w; e += blockDim.x) {
-            const int col = e >> 5, row = e & 31;
-            if (row < w) tile[row * 33 + col] = L[(c0 + row) + (long long)(c0 + col) * m];
-        }
-        __syncthreads();
-        if (warp == 0) {
-            double v = lane < w ? sh[c0 + lane] : 0.0;
+    const int nb = (k + 31) / 32;
+    if (warp == 0) {
+        for (int j = 0; j < nb; ++j) {
+            const int c0 = 32 * j, w = min(32, k - c0);
+            const int r = c0 + lane;
+            // the diagonal block's entries of this lane's row, loads first
+            double dl[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) dl[c] = (lane < w && c < w) ? L[r + (long long)(c0 + c) * m] : 0.0;
+            // the updaters are done with block j-2 on this block's rows
+            if (j >= 2 && !mbar_wait_bounded(&updated[j & 1], ((j - 2) >> 1) & 1, &abortFlag)) break;
+            if (j >= 1 && lane < w) {   // block j-1's columns on this block's rows
+                const int p0 = c0 - 32;
+                double lv[32];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) lv[c] = L[r + (long long)(p0 + c) * m];
+                double acc = 0.0;
+#pragma unroll
+                for (int c = 0; c < 32; ++c) acc = fma(lv[c], sh[p0 + c], acc);
+                sh[r] -= acc;
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                if (lane < w) tile[lane * 33 + c] = dl[c];
+            __syncwarp();
+            double v = lane < w ? sh[r] : 0.0;
             for (int c = 0; c < w; ++c) {
                 const double yc = __shfl_sync(0xffffffffu, v, c);
                 if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
             }
-            if (lane < w) sh[c0 + lane] = v;
+            if (lane < w) sh[r] = v;
+            __syncwarp();
+            mbar_arrive(&solved[j & 1]);
         }
-        __syncthreads();
-        // a thread's rows r, r + T, r + 2T, r + 3T (T = block size) at once:
-        // four independent FMA chains, each row summed in column order
-        const int T = blockDim.x;
-        for (int rb = c0 + w + threadIdx.x; rb < k; rb += 4 * T) {
-            double acc[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int cb = 0; cb < w; cb += 8) {
-                double lv[4][8];   // eight columns' loads in flight before the FMAs
-#pragma unroll
-                for (int cc = 0; cc < 8; ++cc)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q)
-                        lv[q][cc] = (cb + cc < w && rb + q * T < k) ? L[rb + q * T + (long long)(c0 + cb + cc) * m]
-                                                                     : 0.0;
-#pragma unroll
-                for (int cc = 0; cc < 8; ++cc) {
-                    if (cb + cc >= w) break;
-                    const double yc = sh[c0 + cb + cc];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q] = fma(lv[q][cc], yc, acc[q]);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (rb + q * T < k) sh[rb + q * T] -= acc[q];
-        }
-        __syncthreads();
     }
+    else {
+        const int T = kFwdUpd, t = threadIdx.x - 32;
+        for (int b = 0; b < nb; ++b) {
+            if (!mbar_wait_bounded(&solved[b & 1], (b >> 1) & 1, &abortFlag)) break;
+            const int c0 = 32 * b, w = min(32, k - c0);
+            // a thread's rows r, r + T, r + 2T, r + 3T at once: four
+            // independent FMA chains, each row summed in column order
+            for (int rb = c0 + 64 + t; rb < k; rb += 4 * T) {
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int cb = 0; cb < w; cb += 8) {
+                    double lv[4][8];   // eight columns' loads in flight before the FMAs
+#pragma unroll
+                    for (int cc = 0; cc < 8; ++cc)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            lv[q][cc] = (cb + cc < w && rb + q * T < k) ? L[rb + q * T + (long long)(c0 + cb + cc) * m]
+                                                                         : 0.0;
+#pragma unroll
+                    for (int cc = 0; cc < 8; ++cc) {
+                        if (cb + cc >= w) break;
+                        const double yc = sh[c0 + cb + cc];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[q] = fma(lv[q][cc], yc, acc[q]);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (rb + q * T < k) sh[rb + q * T] -= acc[q];
+            }
+            mbar_arrive(&updated[b & 1]);
+        }
+    }
+    __syncthreads();
     for (int r = threadIdx.x; r < m; r += blockDim.x) {
         if (r < k) y[d0 + r] = sh[r];
         else upd[fupd[f] + (r - k)] = sh[r];
     }
+    if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
 }
 
 // Forward substitution, non-pivot rows: upd_r -= sum_c L21[r][c] y_c, one CTA
@@ -1020,6 +1103,8 @@ int chol_upload(CholPlan& P, std::string* err)
     chk(up(&P.dRectRowTasks, P.rectRowTasks)); chk(up(&P.dRectColTasks, P.rectColTasks));
     chk(cudaMalloc(&P.tmpDot, sizeof(double) * (size_t)std::max(P.nDof, 1)));
     chk(cudaMalloc(&P.dFlag, sizeof(int)));
+    chk(cudaMalloc(&P.dSolveFlag, sizeof(int)));
+    chk(cudaMemset(P.dSolveFlag, 0, sizeof(int)));
     if (e != cudaSuccess) {
         if (err) *err = std::string("chol upload: ") + cudaGetErrorString(e);
         chol_free(P);
@@ -1040,7 +1125,7 @@ void chol_free(CholPlan& P)
     cudaFree(P.dPermDof); cudaFree(P.dFk); cudaFree(P.dFm); cudaFree(P.dFdofStart); cudaFree(P.dFrowOff);
     cudaFree(P.dFoff); cudaFree(P.dFupd); cudaFree(P.dRowIdx); cudaFree(P.dChildOff); cudaFree(P.dChildList);
     cudaFree(P.dRelOff); cudaFree(P.dRelIdx); cudaFree(P.dLevelFronts); cudaFree(P.dTasks);
-    cudaFree(P.dAsmDest); cudaFree(P.dAsmLd); cudaFree(P.dAsmDiag); cudaFree(P.dFlag);
+    cudaFree(P.dAsmDest); cudaFree(P.dAsmLd); cudaFree(P.dAsmDiag); cudaFree(P.dFlag); cudaFree(P.dSolveFlag);
     cudaFree(P.dRectRowTasks); cudaFree(P.dRectColTasks); cudaFree(P.tmpDot);
     P.dRectRowTasks = P.dRectColTasks = nullptr;
     P.tmpDot = nullptr;
@@ -1053,6 +1138,7 @@ void chol_free(CholPlan& P)
     P.dAsmLd = nullptr;
     P.dAsmDiag = nullptr;
     P.dFlag = nullptr;
+    P.dSolveFlag = nullptr;
     P.onDevice = false;
 }
 
@@ -1117,8 +1203,9 @@ static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double si
     k_permute_in<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(rhs), P.dPermDof, sign, n, P.yperm);
     for (int l = 0; l < P.nLevels; ++l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
-        k_fwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart, P.dChildOff,
-                                     P.dChildList, P.dRelOff, P.dRelIdx, P.pool, P.upd, P.yperm);
+        k_fwd<<<cnt, kFwdThreads, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart,
+                                             P.dChildOff, P.dChildList, P.dRelOff, P.dRelIdx, P.pool, P.upd, P.yperm,
+                                             P.dSolveFlag);
         const int ro = P.rectRowOff[l], rc = P.rectRowOff[l + 1] - ro;
         if (rc)
             k_fwd_rect<<<rc, kRectRows, shmK, st>>>(P.dRectRowTasks + ro, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart,
@@ -1134,6 +1221,14 @@ static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double si
                                      P.tmpDot, P.xperm);
     }
     k_permute_out<<<(n + 255) / 256, 256, 0, st>>>(P.xperm, P.dPermDof, n, reinterpret_cast<double*>(x));
+}
+
+int chol_solve_status(CholPlan& P, cudaStream_t st, int* timedOut)
+{
+    if (!P.onDevice || !timedOut) return OC_ERR_INVALID;
+    cudaError_t e = cudaMemcpyAsync(timedOut, P.dSolveFlag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? OC_OK : OC_ERR_CUDA;
 }
 
 // Forward/backward substitution; captured into a CUDA graph per

@@ -69,6 +69,7 @@ struct CholPlan {
     int* dAsmLd = nullptr;
     unsigned char* dAsmDiag = nullptr;
     int* dFlag = nullptr;        // non-positive pivot count
+    int* dSolveFlag = nullptr;   // set when a substitution's bounded wait ran out (sticky)
     bool onDevice = false;
     // captured launch sequences (fixed per topology)
     bool useGraphs = true;
@@ -94,5 +95,8 @@ void chol_free(CholPlan& P);
 int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBadPivots);
 // Solves A x = sign * rhs.
 int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, std::string* err);
+// whether a substitution kernel gave up a bounded wait since the upload
+// (synchronises the stream)
+int chol_solve_status(CholPlan& P, cudaStream_t st, int* timedOut);
 
 } // namespace oc

@@ -77,9 +77,10 @@ struct oc_optcuts {
     std::map<double, std::vector<std::pair<double, double>>> configs;
     // record
     std::vector<double> events;   // rows: Newton iterations, E_SD, E_se, lambda, vertices, event code
-    std::vector<double> trace;    // rows: Newton iterations, E_w, E_SD, E_se, lambda, vertices
+    std::vector<double> trace;    // rows: Newton iterations, E_w, E_SD, E_se, lambda, vertices, ||g||^2
     double ms[4] = {0, 0, 0, 0};  // Newton, queries, operations, total
     int rc = OC_OK;               // first error met
+    std::vector<int> initSeams;   // TriMesh::initSeams: the cohesive edges of the initial cut
 
     // ---- state access -------------------------------------------------
     double lam()
@@ -120,7 +121,10 @@ struct oc_optcuts {
     void traceRow()
     {
         const double sd = energySD(), se = seam(), l = lam();
-        trace.insert(trace.end(), {(double)iterNum, l * sd + (1.0 - l) * se, sd, se, 1.0 - l, (double)nVerts()});
+        double gsq = 0.0;
+        keep(oc_optimizer_last_step(opt, nullptr, nullptr, nullptr, nullptr, &gsq));
+        trace.insert(trace.end(),
+                     {(double)iterNum, l * sd + (1.0 - l) * se, sd, se, 1.0 - l, (double)nVerts(), gsq});
     }
     Snapshot snapshot()
     {
@@ -564,7 +568,27 @@ int oc_optcuts_create(oc_optimizer* opt, oc_mesh* mesh, const oc_optcuts_config*
     oc_mesh_rest_constants(mesh, nullptr, sc);
     o->virtualRadius = sc[2] > 0.0 ? sc[2] : 1.0;
     oc_optimizer_get_iter_num(opt, &o->iterNum);
+    int nC = 0;
+    oc_mesh_get_topology(mesh, nullptr, nullptr, &nC, nullptr, nullptr, nullptr);
+    std::vector<int> C(4 * (size_t)nC);
+    if (nC) oc_mesh_get_topology(mesh, nullptr, nullptr, nullptr, nullptr, nullptr, C.data());
+    o->initSeams.swap(C);
     *out = o;
+    return OC_OK;
+}
+
+int oc_optcuts_mesh(const oc_optcuts* o, oc_mesh** mesh)
+{
+    if (!o || !mesh) return OC_ERR_INVALID;
+    *mesh = o->mesh;
+    return OC_OK;
+}
+
+int oc_optcuts_initial_seams(const oc_optcuts* o, int* nRows, int* rows)
+{
+    if (!o || !nRows) return OC_ERR_INVALID;
+    *nRows = static_cast<int>(o->initSeams.size() / 4);
+    if (rows) std::copy(o->initSeams.begin(), o->initSeams.end(), rows);
     return OC_OK;
 }
 
@@ -606,7 +630,7 @@ int oc_optcuts_events(const oc_optcuts* o, int* nRows, double* rows)
 int oc_optcuts_trace(const oc_optcuts* o, int* nRows, double* rows)
 {
     if (!o || !nRows) return OC_ERR_INVALID;
-    *nRows = static_cast<int>(o->trace.size() / 6);
+    *nRows = static_cast<int>(o->trace.size() / 7);
     if (rows) std::copy(o->trace.begin(), o->trace.end(), rows);
     return OC_OK;
 }

@@ -72,5 +72,38 @@ def test_outer_loop_trace_and_state(golden):
     assert st["topology_steps"] >= 1 and st["vertices"] == m.nV
     assert st["total_ms"] >= st["newton_ms"] >= 0.0
     # E_w of every row is lambda-weighted: (1 - lambda) E_SD + lambda E_se
+    assert tr.shape[1] == 7 and np.all(tr[:, 6] >= 0.0)
     lam = tr[:, 4]
     np.testing.assert_allclose(tr[:, 1], (1 - lam) * tr[:, 2] + lam * tr[:, 3], rtol=1e-12)
+
+
+def test_outer_loop_writes_reference_outputs(golden, tmp_path):
+    """energyValPerIter.txt, gradientPerIter.txt, info.txt and
+    finalResult_mesh.obj as the reference writes them (Optimizer.cpp:706-740,
+    main.cpp:346-387, TriMesh.cpp:1758-1969)."""
+    g = golden("icosphere_320_outer")
+    m, opt, o, finished = run_outer(g)
+    tr = o.trace()
+    o.write(str(tmp_path), F0=g["mesh_F"], nV0=len(g["mesh_V"]), lambdaInit=0.999)
+    E = np.loadtxt(tmp_path / "energyValPerIter.txt")
+    G = np.loadtxt(tmp_path / "gradientPerIter.txt")
+    assert E.shape == (len(tr), 4) and G.shape == (len(tr), 2)
+    np.testing.assert_allclose(E[:, 1], tr[:, 2], rtol=1e-5)          # E_SD, six digits
+    np.testing.assert_allclose(E[:, 3], 1.0 - tr[:, 4], rtol=1e-5)    # energyParams[0]
+    info = (tmp_path / "info.txt").read_text().splitlines()
+    assert info[0].split() == [str(len(g["mesh_V"])), str(len(g["mesh_F"]))]
+    st = o.state()
+    assert int(info[1].split()[0]) == int(st["newton_iterations"])
+    dist, seam = (float(x) for x in info[3].split())
+    assert dist == pytest.approx(st["E_SD"], rel=1e-5) and seam == pytest.approx(st["E_se"], rel=1e-5)
+    stretch = [float(x) for x in info[4].split()]
+    assert len(stretch) == 4 and stretch[0] >= 1.0 - 1e-9 and stretch[3] <= 1.0 + 1e-9
+    assert info[5] == "initialSeams %d" % len(g["cohE"])
+    lines = (tmp_path / "finalResult_mesh.obj").read_text().splitlines()
+    v = np.array([[float(x) for x in l.split()[1:]] for l in lines if l.startswith("v ")])
+    vt = [l for l in lines if l.startswith("vt ")]
+    f = [l for l in lines if l.startswith("f ")]
+    assert len(v) == len(g["mesh_V"]) and len(vt) == m.nV and len(f) == len(g["mesh_F"])
+    np.testing.assert_allclose(v, g["mesh_V"], rtol=1e-6, atol=1e-6)   # rest positions in the input numbering
+    first = [int(x.split("/")[0]) - 1 for x in f[0].split()[1:]]
+    assert first == g["mesh_F"][0].tolist()
