@@ -432,6 +432,16 @@ int oc_mesh_apply_topology(oc_mesh* mesh, int opType, const int* path, int pathL
  * mlp / topFrac select the learned proposal (mlp NULL: exhaustive). */
 int oc_topology_queries(oc_mesh* mesh, const int* ops, int nOps, double lambda_t, double filterExp, int options,
                         oc_mlp* mlp, double topFrac, oc_topo_result** out);
+/* The same queries sharded over shardCount processes (one GPU each): the
+ * candidate lists are enumerated in full on every shard, but only candidates
+ * c with c % shardCount == shardRank get their local solves; the others
+ * report EwDec -DBL_MAX and energyChanges (DBL_MAX, DBL_MAX).  Merging the
+ * shards' lists (candidate c from shard c % shardCount) gives the unsharded
+ * result; the argmax over it is the topology step's choice (one exchange of
+ * the lists per step, e.g. an all-gather). */
+int oc_topology_queries_sharded(oc_mesh* mesh, const int* ops, int nOps, double lambda_t, double filterExp,
+                                int options, oc_mlp* mlp, double topFrac, int shardRank, int shardCount,
+                                oc_topo_result** out);
 /* querySplit / queryMerge with propagate = true (TriMesh.cpp:637-665,
  * 828-833): OC_OP_BOUNDARY_SPLIT evaluates the boundary splits at the
  * current fracture tail (or at both ends of the last interior split),

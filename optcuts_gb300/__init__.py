@@ -167,6 +167,8 @@ _SIGS = {
     "oc_topology_queries": [_vp, _i, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
                             ctypes.c_double, ctypes.POINTER(_vp)],
     "oc_topology_query_tail": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_vp)],
+    "oc_topology_queries_sharded": [_vp, _i, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
+                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)],
     "oc_mesh_fracture_tails": [_vp, _i],
     "oc_mesh_set_fracture_tails": [_vp, _i],
     "oc_mesh_seam_length": [_vp, _d],
@@ -368,6 +370,31 @@ class TriMesh:
                                               *(ctypes.byref(h) for h in hs)), "topology step")
         step_ms = 1000.0 * (time.perf_counter() - t0)
         return tuple(self._result(h, features, mlp, step_ms) for h in hs)
+
+    def topologyStepShard(self, lambda_t, rank, world, filterExp=0.6, fp32=False, ops=(0, 2, 1)):
+        """One topology step's queries with only this shard's candidates
+        solved (candidate c belongs to shard c % world); returns one raw
+        list per op for optcuts_gb300.shard.merge."""
+        o = _i4(list(ops))
+        hs = (_vp * len(o))()
+        self.ctx.check(lib().oc_topology_queries_sharded(self.h, _pi(o), len(o), float(lambda_t), float(filterExp),
+                                                         1 if fp32 else 0, None, 0.1, int(rank), int(world), hs),
+                       "sharded topology step")
+        out = []
+        for h in hs:
+            try:
+                n, pool = ctypes.c_int(), ctypes.c_int()
+                lib().oc_topo_result_info(h, ctypes.byref(n), None, ctypes.byref(pool), None, None, None, None)
+                nc = n.value
+                d = {"EwDec": np.zeros(nc), "energyChanges": np.zeros((nc, 2)), "path": np.zeros((nc, 3), np.int32),
+                     "newVertPos": np.zeros((nc, 8)), "posRows": np.zeros(nc, np.int32), "pool": pool.value}
+                if nc:
+                    lib().oc_topo_result_candidates(h, *(d[k].ctypes.data_as(_vp) for k in
+                                                         ("EwDec", "energyChanges", "path", "newVertPos", "posRows")))
+                out.append(d)
+            finally:
+                lib().oc_topo_result_destroy(h)
+        return out
 
     def _result(self, h, features, mlp, query_ms):
         try:

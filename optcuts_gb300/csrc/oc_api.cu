@@ -925,7 +925,7 @@ int oc_topology_query_learned(oc_mesh* m, int opType, double lambda_t, double fi
 // the operations ops[0..nOps) on the mesh's current state, solved together
 static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, double filterExp,
                             const oc::TopoOptions& opts, oc_topo_result** out, const int* candVerts = nullptr,
-                            int nCandVerts = 0, int mergeFork = -2)
+                            int nCandVerts = 0, int mergeFork = -2, int shardRank = 0, int shardCount = 1)
 {
     if (!m || !out || nOps <= 0) return OC_ERR_INVALID;
     bool split = false;
@@ -973,6 +973,8 @@ static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_
     in.candVerts = candVerts;
     in.nCandVerts = nCandVerts;
     in.mergeFork = mergeFork;
+    in.shardRank = shardRank;
+    in.shardCount = shardCount;
     std::vector<oc::TopoOpResult> res(nOps);
     std::string err;
     const int rc = oc::topo_query_ops(in, ops, nOps, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, res.data(),
@@ -1039,6 +1041,22 @@ int oc_topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, d
         opts.topFrac = topFrac;
     }
     return topology_queries(m, ops, nOps, lambda_t, filterExp, opts, out);
+}
+
+int oc_topology_queries_sharded(oc_mesh* m, const int* ops, int nOps, double lambda_t, double filterExp, int options,
+                                oc_mlp* mlp, double topFrac, int shardRank, int shardCount, oc_topo_result** out)
+{
+    if (!ops || !out || nOps <= 0 || nOps > 3 || shardCount < 1 || shardRank < 0 || shardRank >= shardCount)
+        return OC_ERR_INVALID;
+    if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
+    oc::TopoOptions opts;
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    if (mlp) {
+        opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+        opts.mlp = &mlp->m;
+        opts.topFrac = topFrac;
+    }
+    return topology_queries(m, ops, nOps, lambda_t, filterExp, opts, out, nullptr, 0, -2, shardRank, shardCount);
 }
 
 int oc_topology_query_tail(oc_mesh* m, int opType, double lambda_t, int options, oc_topo_result** out)

@@ -1152,6 +1152,7 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
             // (:2796-2862); one work item per edge
             std::vector<std::pair<int, int>> items;   // (candidate, neighbour)
             for (size_t ci = 0; ci < cands.size(); ++ci) {
+                if ((int)(ci % in.shardCount) != in.shardRank) continue;   // another shard's candidate
                 const int vI = cands[ci];
                 for (int p = T.nbPtr[vI]; p < T.nbPtr[vI + 1]; ++p) {
                     const int nbVI = T.nb[p];
@@ -1242,6 +1243,7 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
             // paths (p0, vI, p2) through two umbrella edges; one work item
             // per candidate
             build_parallel(in, cands.size(), B, [&](BuildCtx& X, size_t ci) {
+                if ((int)(ci % in.shardCount) != in.shardRank) return;   // another shard's candidate
                 auto& triMark = X.triMark;
                 auto& L = X.L;
                 Batch& B = X.B;
@@ -1401,6 +1403,11 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
             TopoCandidate C;
             C.path = {p0, p1, p2};
             C.EwDec = -DBL_MAX;
+            if ((int)(out.size() % in.shardCount) != in.shardRank) {   // another shard's candidate
+                C.ec0 = C.ec1 = DBL_MAX;
+                out.push_back(C);
+                continue;
+            }
             out.push_back(C);
             const size_t before = B.lvPos.size();
             emit(B, T, in.rest, in.UV, triangles, L, {}, slot, 1, static_cast<int>(L.gv.size()) - 1, tg);

@@ -65,6 +65,11 @@ struct TopoQueryIn {
     const int* candVerts = nullptr;
     int nCandVerts = 0;
     int mergeFork = -2;
+    // candidate sharding across processes: only candidates c with
+    // c % shardCount == shardRank are solved; the others keep EwDec -DBL_MAX
+    // and energyChanges (DBL_MAX, DBL_MAX) (the list itself is the same on
+    // every shard)
+    int shardRank = 0, shardCount = 1;
 };
 
 struct TopoStats {

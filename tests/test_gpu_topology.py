@@ -208,3 +208,21 @@ def test_problem_size_classes_match_oracle(nlon, nlat):
         sel = np.isfinite(le["problems"]["EwDec"])
         assert sel.sum() == le["selected"]
         np.testing.assert_allclose(le["problems"]["EwDec"][sel], ex["problems"]["EwDec"][sel], rtol=1e-8, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", ["icosphere_320_topo", "ellipsoid_2k_topo"])
+@pytest.mark.parametrize("world", [2, 3])
+def test_sharded_step_equals_unsharded(golden, case, world):
+    """Each shard solves only its candidates; merged (optcuts_gb300.shard),
+    the lists equal the unsharded step's bit for bit."""
+    from optcuts_gb300 import shard
+    g = golden(case)
+    m = topo_mesh(g)
+    lam = float(g["topo_best"][3])
+    full = [q for q in m.topologyStep(lam)]
+    merged = shard.merge([m.topologyStepShard(lam, r, world) for r in range(world)])
+    for q, s in zip(full, merged):
+        np.testing.assert_array_equal(np.array([c["EwDec"] for c in q["candidates"]]), s["EwDec"])
+        np.testing.assert_array_equal(np.array([c["energyChanges"] for c in q["candidates"]]).reshape(-1, 2),
+                                      s["energyChanges"])
+        assert q["best"] == s["best"]
