@@ -54,9 +54,11 @@ def parse():
     p.add_argument("--scaffold", default="on", choices=["on", "off"])
     p.add_argument("--no-topology", action="store_true")
     p.add_argument("--topo-newton-iters", type=int, default=400,
-                   help="untimed Newton iterations (to convergence) before the topology step is timed")
-    p.add_argument("--train-at", default="60,120,200,300",
-                   help="Newton iterations whose states give the learned proposal's exhaustive training pairs")
+                   help="Newton iterations (to convergence) after the outer loop's last operation")
+    p.add_argument("--outer-steps", type=int, default=5,
+                   help="topology operations of the outer loop before the topology step is timed")
+    p.add_argument("--outer-newton-cap", type=int, default=4000,
+                   help="Newton iterations the outer loop may spend reaching that state")
     p.add_argument("--top-frac", type=float, default=0.1, help="fraction of local problems solved exactly (learned)")
     p.add_argument("--train-epochs", type=int, default=30, help="MLP training epochs over the exhaustive pairs")
     return p.parse_args()
@@ -270,6 +272,204 @@ def run_reference(args, rank, world):
     }), flush=True)
 
 
+def spearman(a, b):
+    """Rank correlation of two equally long arrays (average ranks for ties)."""
+    from scipy.stats import spearmanr
+    if len(a) < 3:
+        return None
+    r = spearmanr(a, b).correlation
+    return None if r != r else float(r)
+
+
+def ranking(ex, le, top_frac):
+    """How the learned pass ranked the exhaustive pass's local problems:
+    recall of the exact top-k problems among those it solved exactly (k =
+    the number it solved), whether each op's best problem was among them,
+    and the rank correlation of predicted and exact E_w decreases."""
+    pe, pl = ex["problems"], le["problems"]
+    exact, pred = pe["EwDec"], pl["EwDec_pred"]
+    sel = ~np.isnan(pl["EwDec"])
+    n, k = len(exact), int(sel.sum())
+    ok = np.isfinite(exact) & (exact > -1e300)
+    out = {"problems": n, "solved_exactly": k, "spearman": spearman(pred[ok], exact[ok])}
+    if n and k:
+        top = np.argsort(-np.where(ok, exact, -np.inf), kind="stable")[:k]
+        out["recall_at_k"] = float(sel[top].mean())
+        out["best_selected"] = bool(sel[int(np.argmax(np.where(ok, exact, -np.inf)))])
+    return out
+
+
+def topology_section(args, oc, ctx, opt, mesh, st, rank):
+    """The topology step on the state the outer loop reaches after
+    args.outer_steps topology operations (the bijectivity-off outer loop of
+    the library: dual updates, propagation; its first inner loop converges
+    the Newton phase), timed exhaustive and with the learned proposal trained
+    on the (features, target) pairs the outer loop's own exhaustive queries
+    recorded on the way."""
+    opt.clearScaffold()            # bijectivity off: no air mesh
+    mesh.setCohesiveEdges(st.cohE)
+    outer = oc.OptCuts(opt, recordFeatures=True, maxNewtonIters=args.outer_newton_cap)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    passes, finished = 0, False
+    while outer.state()["topology_steps"] < args.outer_steps and passes < 400 and not finished:
+        finished = outer.run(1)
+        passes += 1
+    converged = False
+    for _ in range(args.topo_newton_iters):   # the inner loop after the last operation
+        if opt.solve(1) == 1:
+            converged = True
+            break
+    ctx.synchronize()
+    outer_s = time.perf_counter() - t0
+    so = outer.state()
+    X, t = outer.features()
+    lam_t = so["lambda"]
+
+    def queries(**kw):
+        # one topology step: boundary splits, merges and interior splits
+        # solved together; the first query rebuilds the vertex adjacency as
+        # it does after an applied operation
+        mesh.dropAdjacency()
+        return mesh.topologyStep(lam_t, **kw)
+
+    def timed_step(**kw):
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        qs = queries(**kw)
+        ctx.synchronize()
+        return time.perf_counter() - t1, qs
+
+    def summary(qs):
+        qb, qm, qi = qs
+        return {"query_ms": qb["query_ms"], "gpu_solve_ms": qb["solve_ms"], "probe_ms": qb["probe_ms"],
+                "exact_ms": qb["exact_ms"],
+                "host_build_ms": {name: q["build_ms"] for name, q in zip(("boundary_split", "merge", "interior_split"),
+                                                                        qs)},
+                "local_problems": sum(q["local_problems"] for q in qs),
+                "exact_solves": sum(q["selected"] for q in qs),
+                "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"], "interior_split": qi["EwDec_max"]}}
+
+    queries()   # warm-up
+    t_gpu, qs = timed_step(features=True)
+    t_fp32, qs32 = timed_step(fp32=True)
+    qb, qm, qi = qs
+    topo = {"metric": "topology-step s (exhaustive candidate evaluation: boundary split, merge and interior split "
+                      "queries of one state, solved together)", "value": t_gpu, "unit": "s",
+            "higher_is_better": False, "bijectivity": "off (outer loop and local solves without air meshes)",
+            "state": {"what": "after %d topology operations of the outer loop, inner loop converged" %
+                              int(so["topology_steps"]),
+                      "newton_iterations": opt.getIterNum(), "topology_steps": int(so["topology_steps"]),
+                      "converged": converged, "finished": bool(finished), "lambda": lam_t, "E_SD": so["E_SD"],
+                      "E_se": so["E_se"], "vertices": int(so["vertices"]), "outer_loop_s": outer_s,
+                      "outer_loop_ms": {k: so[k] for k in ("newton_ms", "query_ms", "apply_ms")}},
+            "candidates": {"boundary_split": len(qb["candidates"]), "merge": len(qm["candidates"]),
+                           "interior_split": len(qi["candidates"])},
+            "max_local_iterations": max(q["max_local_iters"] for q in qs),
+            "local_iterations": sum(q["local_iters_total"] for q in qs),
+            "local_capped": sum(q["local_capped"] for q in qs),
+            **summary(qs), "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)}}
+    e_w = opt.getLastEnergyVal(excludeScaffold=True) + lam_t * so["E_se"]
+
+    def after(qs_):
+        return e_w - max(0.0, *(q["EwDec_max"] for q in qs_))
+    if len(X):
+        mlp = oc.MLP(32, 128, seed=3, ctx=ctx)
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        loss = mlp.train(X, t, epochs=args.train_epochs, batch=512, lr=2e-3, seed=3)
+        ctx.synchronize()
+        train_s = time.perf_counter() - t1
+        queries(mlp=mlp, topFrac=args.top_frac)   # warm-up
+        t_l, ql = timed_step(mlp=mlp, topFrac=args.top_frac)
+        t_l32, ql32 = timed_step(mlp=mlp, topFrac=args.top_frac, fp32=True)
+        ew_ex, ew_l, ew_ex32, ew_l32 = after(qs), after(ql), after(qs32), after(ql32)
+        # the exhaustive pass's own pairs at this state: held out from training
+        Xh = np.concatenate([q["features"] for q in qs])
+        th = np.concatenate([q["target"] for q in qs])
+        ph = mlp.predict(Xh) if len(Xh) else np.zeros(0)
+        r2 = 1.0 - float(np.mean((ph - th) ** 2)) / float(np.var(th)) if len(th) > 1 and np.var(th) > 0 else None
+        topo["learned"] = {
+            "metric": "topology-step s (learned proposal, top %g of local problems solved exactly)" % args.top_frac,
+            "value": t_l, "unit": "s", "higher_is_better": False, **summary(ql),
+            "speedup_vs_exhaustive": t_gpu / t_l,
+            "E_w_before": e_w, "E_w_after": ew_l, "E_w_after_exhaustive": ew_ex,
+            "E_w_rel_diff": abs(ew_l - ew_ex) / abs(ew_ex),
+            "ranking": {op: ranking(a, b, args.top_frac) for op, a, b in
+                        zip(("boundary_split", "merge", "interior_split"), qs, ql)},
+            "fp32_hessian_option": {"value": t_l32, "unit": "s", **summary(ql32), "E_w_after": ew_l32,
+                                    "E_w_after_exhaustive": ew_ex32,
+                                    "E_w_rel_diff": abs(ew_l32 - ew_ex32) / abs(ew_ex32)},
+            "mlp": {"layers": [32, 128, 128, 1], "weights": "bf16 (fp32 master, Adam)", "accumulate": "fp32",
+                    "pairs": int(len(X)), "pairs_from": "the outer loop's exhaustive queries before this state",
+                    "epochs": args.train_epochs, "batch": 512, "seed": 3, "train_s": train_s, "final_mse": loss,
+                    "target_var": float(np.var(t)), "train_r2": 1.0 - loss / float(np.var(t)) if np.var(t) else None,
+                    "heldout_r2": r2}}
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle as O
+        threads = os.cpu_count() or 1
+        uv = mesh.V
+        secs = 0.0
+        for op in (0, 2, 1):
+            _, s_ = O.topology_query(mesh.V_rest, uv, mesh.F, mesh.cohE, op, lam_t, threads=threads)
+            secs += s_
+        topo["cpu_baseline"] = {"value": secs, "unit": "s", "cores": threads, "kind": "port",
+                                "sample": "the same three queries on the same state"}
+    # applying the chosen operation (Optimizer::createFracture: mesh edit,
+    # device mesh, Newton pattern and analysis, energy), timed once
+    cands = [(q["EwDec_max"], op, q) for op, q in ((oc.OP_BOUNDARY_SPLIT, qb), (oc.OP_MERGE, qm)) if q["best"] >= 0]
+    if cands:
+        ew, op, q = max(cands, key=lambda x: x[0])
+        c = q["candidates"][q["best"]]
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        opt.createFracture(op, c["path"], c["newVertPos"])
+        ctx.synchronize()
+        topo["apply"] = {"value": time.perf_counter() - t1, "unit": "s",
+                         "op": {0: "boundary_split", 1: "interior_split", 2: "merge"}[op], "EwDec": ew,
+                         "phases_ms": {k: round(v, 2) for k, v in opt.applyTiming().items()},
+                         "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and analysis, energy"}
+    return topo
+
+
+def outer_config0(oc, ctx):
+    """The whole OptCuts run (outer loop, bijectivity off, b_d = 4.1) on the
+    5,120-triangle icosphere from its Tutte start, against the reference's
+    own run of the same input (tests/golden/icosphere_5k_outer.npz, made by
+    the reference's sources on one x86-64 host thread)."""
+    path = os.path.join(ROOT, "tests", "golden", "icosphere_5k_outer.npz")
+    if not os.path.exists(path):
+        return None
+    with np.load(path) as z:
+        g = {k: z[k] for k in z.files}
+    m = oc.TriMesh(g["V_rest"], g["UV0"], g["F"], g["fixedVert"], ctx=ctx)
+    m.setCohesiveEdges(g["cohE"])
+    opt = oc.Optimizer(m, [1.0 - g["scalars"][4]])
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    opt.precompute()
+    o = oc.OptCuts(opt, upperBound=4.1)
+    finished = o.run()
+    ctx.synchronize()
+    secs = time.perf_counter() - t0
+    st = o.state()
+    ref = g["outer_final"]
+    out = {"metric": "time to converge s (whole OptCuts run, bijectivity off, b_d 4.1)", "value": secs, "unit": "s",
+           "higher_is_better": False, "workload": "icosphere_5k (5,120 triangles)", "finished": bool(finished),
+           "newton_iterations": int(st["newton_iterations"]), "topology_steps": int(st["topology_steps"]),
+           "E_SD": st["E_SD"], "E_se": st["E_se"], "lambda": st["lambda"],
+           "reference": {"seconds": float(ref[6]), "newton_iterations": int(ref[3]), "topology_steps": int(ref[4]),
+                         "E_SD": float(ref[0]), "E_se": float(ref[1]), "lambda": float(ref[2]),
+                         "host": "x86-64, one thread (recorded with the golden run)"},
+           "rel_diff": {"E_SD": abs(st["E_SD"] - ref[0]) / ref[0], "E_se": abs(st["E_se"] - ref[1]) / ref[1],
+                        "lambda": abs(st["lambda"] - ref[2]) / ref[2]},
+           "phases_ms": {k: st[k] for k in ("newton_ms", "query_ms", "apply_ms")}}
+    o.close()
+    opt.close()
+    m.close()
+    return out
+
+
 def run_ours(args, rank, world):
     import optcuts_gb300 as oc
     device = int(os.environ.get("LOCAL_RANK", "0"))
@@ -367,137 +567,11 @@ def run_ours(args, rank, world):
     # and of the interior-split query, every local solve on the GPU
     topo = None
     if not args.no_topology:
-        lam_t = 1.0 - (1.0 - args.lam)   # 1 - energyParams[0], as createFracture passes it
-        mesh.setCohesiveEdges(st.cohE)
-        train_at = sorted({int(x) for x in args.train_at.split(",") if x.strip()})
-        base_it = args.warmup + args.steps + (0 if args.no_e2e else max(3, args.steps))
-
-        def queries(**kw):
-            # one topology step of the outer loop: boundary splits, merges and
-            # interior splits (TriMesh::splitOrMerge and the interior-split
-            # query), the first query rebuilding the vertex adjacency as it
-            # does after an applied operation
-            mesh.dropAdjacency()
-            return mesh.topologyStep(lam_t, **kw)
-
-        # exhaustive pairs (features, exact fraction of the local excess
-        # energy removed) from earlier states of the same run, then the
-        # Newton loop to convergence
-        Xs, ts, pair_states = [], [], []
-        converged_after = None
-        for k in range(args.topo_newton_iters):
-            if base_it + k in train_at:
-                for q in queries(features=True):
-                    if q["local_problems"]:
-                        Xs.append(q["features"])
-                        ts.append(q["target"])
-                pair_states.append(base_it + k)
-            if step() == 1:
-                converged_after = base_it + k + 1
-                break
-
-        def timed_step(**kw):
-            ctx.synchronize()
-            t0 = time.perf_counter()
-            qs = queries(**kw)
-            ctx.synchronize()
-            return time.perf_counter() - t0, qs
-
-        def summary(qs):
-            # the three queries run as one step: one library call, one shared
-            # device solve (probe and exact passes for the learned proposal)
-            qb, qm, qi = qs
-            return {"query_ms": qb["query_ms"], "gpu_solve_ms": qb["solve_ms"], "probe_ms": qb["probe_ms"],
-                    "exact_ms": qb["exact_ms"],
-                    "host_build_ms": {name: q["build_ms"]
-                                      for name, q in zip(("boundary_split", "merge", "interior_split"), qs)},
-                    "local_problems": sum(q["local_problems"] for q in qs),
-                    "exact_solves": sum(q["selected"] for q in qs),
-                    "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"],
-                             "interior_split": qi["EwDec_max"]}}
-
-        queries()   # warm-up
-        t_gpu, (qb, qm, qi) = timed_step()
-        t_fp32, qs32 = timed_step(fp32=True)
-        topo = {"metric": "topology-step s (exhaustive candidate evaluation: boundary split, merge and interior "
-                          "split queries of one state, solved together)", "value": t_gpu, "unit": "s",
-                "higher_is_better": False, "bijectivity": "off (local solves without air meshes)",
-                "newton_iterations_before": converged_after if converged_after else
-                base_it + args.topo_newton_iters,
-                "converged": converged_after is not None, "lambda": args.lam,
-                "candidates": {"boundary_split": len(qb["candidates"]), "merge": len(qm["candidates"]),
-                               "interior_split": len(qi["candidates"])},
-                "max_local_iterations": max(qb["max_local_iters"], qm["max_local_iters"], qi["max_local_iters"]),
-                "local_iterations": qb["local_iters_total"] + qm["local_iters_total"] + qi["local_iters_total"],
-                "local_capped": qb["local_capped"] + qm["local_capped"] + qi["local_capped"],
-                **summary((qb, qm, qi)),
-                "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)}}
-        # the learned proposal on the same state, trained on the pairs above
-        if Xs:
-            X, t = np.concatenate(Xs), np.concatenate(ts)
-            mlp = oc.MLP(32, 128, seed=3, ctx=ctx)
-            ctx.synchronize()
-            t0 = time.perf_counter()
-            loss = mlp.train(X, t, epochs=args.train_epochs, batch=512, lr=2e-3, seed=3)
-            ctx.synchronize()
-            train_s = time.perf_counter() - t0
-            queries(mlp=mlp, topFrac=args.top_frac)   # warm-up
-            t_l, ql = timed_step(mlp=mlp, topFrac=args.top_frac)
-            t_l32, ql32 = timed_step(mlp=mlp, topFrac=args.top_frac, fp32=True)
-            # E_w after the step: the outer loop applies the best operation
-            # found; the learned step must reach the same E_w within 0.5%
-            from optcuts_gb300 import init as I
-            seam = I.seam_sparsity(mesh.V_rest, mesh.V, st.cohE, avg_edge_len(st))
-            r = np.sqrt(mesh.surfaceArea / np.pi)
-            e_w = opt.getLastEnergyVal(excludeScaffold=True) + lam_t * seam / r
-
-            def after(qs):
-                return e_w - max(0.0, *(q["EwDec_max"] for q in qs))
-            ew_ex, ew_l = after((qb, qm, qi)), after(ql)
-            ew_ex32, ew_l32 = after(qs32), after(ql32)
-            topo["learned"] = {
-                "metric": "topology-step s (learned proposal, top %g of local problems solved exactly)" % args.top_frac,
-                "value": t_l, "unit": "s", "higher_is_better": False, **summary(ql),
-                "E_w_before": e_w, "E_w_after": ew_l, "E_w_after_exhaustive": ew_ex,
-                "E_w_rel_diff": abs(ew_l - ew_ex) / abs(ew_ex),
-                "fp32_hessian_option": {"value": t_l32, "unit": "s", **summary(ql32),
-                                        "E_w_after": ew_l32, "E_w_after_exhaustive": ew_ex32,
-                                        "E_w_rel_diff": abs(ew_l32 - ew_ex32) / abs(ew_ex32)},
-                "mlp": {"layers": [32, 128, 128, 1], "weights": "bf16 (fp32 master, Adam)", "accumulate": "fp32",
-                        "pairs": int(len(X)), "pair_states_newton_iteration": pair_states,
-                        "epochs": args.train_epochs,
-                        "batch": 512, "seed": 3, "train_s": train_s, "final_mse": loss,
-                        "target_var": float(np.var(t))}}
-        if rank == 0 and not args.no_cpu_baseline:
-            import oracle as O
-            threads = os.cpu_count() or 1
-            uv = mesh.V
-            secs = 0.0
-            for op in (0, 2, 1):
-                _, s = O.topology_query(mesh.V_rest, uv, mesh.F, st.cohE, op, lam_t, threads=threads)
-                secs += s
-            topo["cpu_baseline"] = {"value": secs, "unit": "s", "cores": threads, "kind": "port",
-                                    "sample": "the same three queries on the same state"}
-        # the rest of the outer loop's topology step: applying the chosen
-        # operation (Optimizer::createFracture: mesh edit, device mesh, Newton
-        # pattern and symbolic analysis, scaffold, energy), timed once
-        cands = [(q["EwDec_max"], op, q) for op, q in ((oc.OP_BOUNDARY_SPLIT, qb), (oc.OP_MERGE, qm))
-                 if q["best"] >= 0]
-        if cands:
-            ew, op, q = max(cands, key=lambda x: x[0])
-            c = q["candidates"][q["best"]]
-            ctx.synchronize()
-            t0 = time.perf_counter()
-            opt.createFracture(op, c["path"], c["newVertPos"])
-            ctx.synchronize()
-            topo["apply"] = {"value": time.perf_counter() - t0, "unit": "s",
-                             "op": {0: "boundary_split", 1: "interior_split", 2: "merge"}[op], "EwDec": ew,
-                             "phases_ms": {k: round(v, 2) for k, v in opt.applyTiming().items()},
-                             "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and "
-                                     "analysis, scaffold, energy"}
+        topo = topology_section(args, oc, ctx, opt, mesh, st, rank)
 
     if rank != 0:
         return
+    outer0 = None if args.no_topology else outer_config0(oc, ctx)
     # dominant phase: the multifrontal factorisation, FP64-FMA bound; the
     # algorithmic flops are the dense partial-Cholesky counts of its fronts
     ph_mean = {k: statistics.mean(p[k] for p in phases) for k in phases[0]}
@@ -541,7 +615,7 @@ def run_ours(args, rank, world):
                    "precision": "fp64 throughout (energy, gradient, Hessian eigen-clamp, LDL^T)"},
         "roofline": roofline, "roofline_solve": roofline_solve, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clocks, "energy_after": energy_after, "first_step": first,
-        "topology": topo,
+        "topology": topo, "outer_loop": outer0,
     }
     print(json.dumps(out), flush=True)
 

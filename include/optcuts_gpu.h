@@ -488,6 +488,8 @@ typedef struct {
     oc_mlp* mlp;         /* learned proposal for the queries (NULL: exhaustive) */
     double topFrac;      /* its fraction solved exactly (0.1) */
     int maxNewtonIters;  /* stop (OC_ERR_NOT_CONVERGED) past this many Newton iterations */
+    int recordFeatures;  /* 1: keep the (features, target) pairs of every exhaustive
+                            topology query (training data for the learned proposal) */
 } oc_optcuts_config;
 int oc_optcuts_default_config(oc_optcuts_config* cfg);
 int oc_optcuts_create(oc_optimizer* opt, oc_mesh* mesh, const oc_optcuts_config* cfg, oc_optcuts** out);
@@ -524,6 +526,9 @@ int oc_optcuts_write(oc_optcuts* oc, const char* dir, const int* F0, int nV0, do
 /* the mesh the outer loop edits, and TriMesh::initSeams (the cohesive edges
  * of the initial cut, rows x 4, as the loop started) */
 int oc_optcuts_mesh(const oc_optcuts* oc, oc_mesh** mesh);
+/* the pairs recorded with recordFeatures: nRows x 32 features and nRows
+ * targets (NULL arrays: the count only) */
+int oc_optcuts_features(const oc_optcuts* oc, int* nRows, float* X, float* target);
 int oc_optcuts_initial_seams(const oc_optcuts* oc, int* nRows, int* rows);
 /* TriMesh::saveAsMesh (TriMesh.cpp:1805-1969): rest positions indexed by F0
  * (the input mesh's triangles, nF x 3; NULL: the cut mesh's vertices merged

@@ -55,7 +55,7 @@ class OptimizerConfig(ctypes.Structure):
 class OptCutsConfig(ctypes.Structure):
     _fields_ = [("upperBound", ctypes.c_double), ("bijective", ctypes.c_int), ("topoLineSearch", ctypes.c_int),
                 ("filterExp", ctypes.c_double), ("topoOptions", ctypes.c_int), ("mlp", _vp),
-                ("topFrac", ctypes.c_double), ("maxNewtonIters", ctypes.c_int)]
+                ("topFrac", ctypes.c_double), ("maxNewtonIters", ctypes.c_int), ("recordFeatures", ctypes.c_int)]
 
 
 SOLVER_DIRECT = 0
@@ -185,6 +185,7 @@ _SIGS = {
     "oc_optcuts_trace": [_vp, _i, _d],
     "oc_optcuts_write": [_vp, ctypes.c_char_p, _i, ctypes.c_int, ctypes.c_double],
     "oc_optcuts_mesh": [_vp, ctypes.POINTER(_vp)],
+    "oc_optcuts_features": [_vp, _i, _vp, _vp],
     "oc_optcuts_initial_seams": [_vp, _i, _i],
     "oc_mesh_write_obj": [_vp, ctypes.c_char_p, _i, ctypes.c_int, ctypes.c_int],
     "oc_sd_energy_trials_noalloc": [_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int,
@@ -756,7 +757,7 @@ class OptCuts:
               10: "oscillation", 11: "converged at bound", 12: "no merge left"}
 
     def __init__(self, optimizer, upperBound=4.1, bijective=False, topoLineSearch=True, filterExp=0.6, fp32=False,
-                 mlp=None, topFrac=0.1, maxNewtonIters=100000):
+                 mlp=None, topFrac=0.1, maxNewtonIters=100000, recordFeatures=False):
         self.opt = optimizer
         self.ctx = optimizer.ctx
         cfg = OptCutsConfig()
@@ -765,6 +766,7 @@ class OptCuts:
         cfg.filterExp, cfg.topoOptions = float(filterExp), 1 if fp32 else 0
         cfg.mlp = mlp.h if mlp is not None else None
         cfg.topFrac, cfg.maxNewtonIters = float(topFrac), int(maxNewtonIters)
+        cfg.recordFeatures = int(bool(recordFeatures))
         self._mlp = mlp
         h = _vp()
         self.ctx.check(lib().oc_optcuts_create(optimizer.h, optimizer.data.h, ctypes.byref(cfg), ctypes.byref(h)),
@@ -798,6 +800,17 @@ class OptCuts:
         """rows per Newton iteration: iterations, E_w, E_SD, E_se, lambda,
         vertices, ||gradient||^2"""
         return self._rows(lib().oc_optcuts_trace, 7)
+
+    def features(self):
+        """(X, target) pairs the exhaustive queries of the run recorded
+        (recordFeatures=True): the learned proposal's training data."""
+        n = ctypes.c_int()
+        self.ctx.check(lib().oc_optcuts_features(self.h, ctypes.byref(n), None, None), "OptCuts.features")
+        X = np.zeros((n.value, 32), np.float32)
+        t = np.zeros(n.value, np.float32)
+        if n.value:
+            self.ctx.check(lib().oc_optcuts_features(self.h, ctypes.byref(n), _pf(X), _pf(t)), "OptCuts.features")
+        return X, t
 
     def write(self, folder, F0=None, nV0=0, lambdaInit=0.999):
         """The reference's output files of the run into folder:

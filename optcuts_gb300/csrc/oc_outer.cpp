@@ -81,6 +81,7 @@ struct oc_optcuts {
     double ms[4] = {0, 0, 0, 0};  // Newton, queries, operations, total
     int rc = OC_OK;               // first error met
     std::vector<int> initSeams;   // TriMesh::initSeams: the cohesive edges of the initial cut
+    std::vector<float> featX, featT;   // recorded (features, target) pairs
 
     // ---- state access -------------------------------------------------
     double lam()
@@ -181,6 +182,20 @@ struct oc_optcuts {
     }
     // EwDec_max of a query and its best candidate (querySplit returns 0 when
     // no vertex passes its filter, TriMesh.cpp:601-604, 618-621)
+    int queryOptions() const
+    {
+        return cfg.topoOptions | (cfg.recordFeatures && !cfg.mlp ? OC_TOPO_RECORD_FEATURES : 0);
+    }
+    void keepFeatures(const oc_topo_result* r)
+    {
+        if (!cfg.recordFeatures || cfg.mlp) return;
+        int n = 0;
+        if (oc_topo_result_features(r, &n, nullptr, nullptr, nullptr) || n <= 0) return;
+        const size_t x0 = featX.size(), t0 = featT.size();
+        featX.resize(x0 + 32 * (size_t)n);
+        featT.resize(t0 + n);
+        keep(oc_topo_result_features(r, &n, featX.data() + x0, featT.data() + t0, nullptr));
+    }
     static double bestOf(const oc_topo_result* r, bool split, Cand* best)
     {
         int n = 0, b = -1, pool = 0;
@@ -222,8 +237,9 @@ struct oc_optcuts {
             if (allowInSplit) {
                 const int op = kISplit;
                 oc_topo_result* r = nullptr;
-                if (!keep(oc_topology_queries(mesh, &op, 1, lt, filterExp, cfg.topoOptions, cfg.mlp, cfg.topFrac, &r)))
+                if (!keep(oc_topology_queries(mesh, &op, 1, lt, filterExp, queryOptions(), cfg.mlp, cfg.topFrac, &r)))
                     return false;
+                keepFeatures(r);
                 readList(r, lists[kISplit]);
                 oc_topo_result_info(r, nullptr, nullptr, &inSplitTotalAmt, nullptr, nullptr, nullptr, nullptr);
                 best = bestOf(r, true, &pick);
@@ -233,8 +249,10 @@ struct oc_optcuts {
             else {
                 const int ops[2] = {kBSplit, kMerge};
                 oc_topo_result* r[2] = {};
-                if (!keep(oc_topology_queries(mesh, ops, 2, lt, filterExp, cfg.topoOptions, cfg.mlp, cfg.topFrac, r)))
+                if (!keep(oc_topology_queries(mesh, ops, 2, lt, filterExp, queryOptions(), cfg.mlp, cfg.topFrac, r)))
                     return false;
+                keepFeatures(r[0]);
+                keepFeatures(r[1]);
                 readList(r[0], lists[kBSplit]);
                 readList(r[1], lists[kMerge]);
                 Cand cs, cm;
@@ -542,6 +560,7 @@ int oc_optcuts_default_config(oc_optcuts_config* c)
     c->mlp = nullptr;
     c->topFrac = 0.1;
     c->maxNewtonIters = 100000;
+    c->recordFeatures = 0;
     return OC_OK;
 }
 
@@ -581,6 +600,15 @@ int oc_optcuts_mesh(const oc_optcuts* o, oc_mesh** mesh)
 {
     if (!o || !mesh) return OC_ERR_INVALID;
     *mesh = o->mesh;
+    return OC_OK;
+}
+
+int oc_optcuts_features(const oc_optcuts* o, int* nRows, float* X, float* target)
+{
+    if (!o || !nRows) return OC_ERR_INVALID;
+    *nRows = static_cast<int>(o->featT.size());
+    if (X) std::copy(o->featX.begin(), o->featX.end(), X);
+    if (target) std::copy(o->featT.begin(), o->featT.end(), target);
     return OC_OK;
 }
 
