@@ -196,6 +196,10 @@ void nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::v
 
 int tiles_of(int k, int m) { return (k + kTile - 1) / kTile + (m - k + kTile - 1) / kTile; }
 
+// rows of L21 per forward-GEMV task on a level whose largest pivot count is
+// maxK: 256 for the narrow kernel of small fronts, else 32 (k_fwd_rect)
+int kRectRowsFor(int maxK) { return maxK <= kNarrowK ? kNarrowRows : kRectRows; }
+
 // Tile t of a front's columns (pivot tiles first, then the rows below):
 // first row/column and extent.
 __host__ __device__ __forceinline__ void tile_bounds(int k, int m, int t, int& start, int& len)
@@ -458,10 +462,18 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     // substitution chunks of the rectangular part of each front, per level
     P.rectRowOff.assign(P.nLevels + 1, 0);
     P.rectColOff.assign(P.nLevels + 1, 0);
+    P.levelMaxK.assign(P.nLevels, 0);
+    P.levelMaxM.assign(P.nLevels, 0);
     for (int l = 0; l < P.nLevels; ++l) {
         for (int i = P.levelFrontOff[l]; i < P.levelFrontOff[l + 1]; ++i) {
             const int f = P.levelFronts[i];
-            for (int r0 = P.fk[f]; r0 < P.fm[f]; r0 += kRectRows) P.rectRowTasks.push_back(make_int2(f, r0));
+            P.levelMaxK[l] = std::max(P.levelMaxK[l], P.fk[f]);
+            P.levelMaxM[l] = std::max(P.levelMaxM[l], P.fm[f]);
+        }
+        for (int i = P.levelFrontOff[l]; i < P.levelFrontOff[l + 1]; ++i) {
+            const int f = P.levelFronts[i];
+            const int chunk = kRectRowsFor(P.levelMaxK[l]);
+            for (int r0 = P.fk[f]; r0 < P.fm[f]; r0 += chunk) P.rectRowTasks.push_back(make_int2(f, r0));
             if (P.fm[f] > P.fk[f])
                 for (int c0 = 0; c0 < P.fk[f]; c0 += kRectCols) P.rectColTasks.push_back(make_int2(f, c0));
         }
@@ -827,8 +839,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, uint32_
     return false;
 }
 
-constexpr int kFwdThreads = 512;               // warp 0 solves, the other warps update
-constexpr int kFwdUpd = kFwdThreads - 32;
+// Block sizes of the pivot-part kernels: warp 0 solves, the other NT - 32
+// threads update; a level's launch takes the size its largest front needs.
+constexpr int kFwdThreads = 512;
+constexpr int kSolveThreadsFor(int maxK) { return maxK <= 64 ? 64 : (maxK <= 384 ? 256 : kFwdThreads); }
 
 // Forward substitution, pivot part of one front (one CTA per front of the
 // level): gather this front's right-hand side plus the children's update
@@ -844,7 +858,8 @@ constexpr int kFwdUpd = kFwdThreads - 32;
 // bulk updates run behind the dependent chain instead of between its steps.
 // Hand-offs: per block an mbarrier "solved" (warp 0's 32 lanes) and
 // "updated" (the updaters), two of each alternating; waits are bounded.
-__global__ void __launch_bounds__(kFwdThreads) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
+template <int NT>
+__global__ void __launch_bounds__(NT) k_fwd(const int* __restrict__ fronts, const int* __restrict__ fk,
                                                      const int* __restrict__ fm, const long long* __restrict__ foff,
                                                      const long long* __restrict__ fupd, const int* __restrict__ fdof,
                                                      const int* __restrict__ childOff, const int* __restrict__ childList,
@@ -863,8 +878,8 @@ __global__ void __launch_bounds__(kFwdThreads) k_fwd(const int* __restrict__ fro
     if (threadIdx.x == 0) {
         mbar_init(&solved[0], 32);
         mbar_init(&solved[1], 32);
-        mbar_init(&updated[0], kFwdUpd);
-        mbar_init(&updated[1], kFwdUpd);
+        mbar_init(&updated[0], NT - 32);
+        mbar_init(&updated[1], NT - 32);
         abortFlag = 0;
     }
     __syncthreads();
@@ -913,33 +928,21 @@ __global__ void __launch_bounds__(kFwdThreads) k_fwd(const int* __restrict__ fro
         }
     }
     else {
-        const int T = kFwdUpd, t = threadIdx.x - 32;
+        const int t = threadIdx.x - 32;
         for (int b = 0; b < nb; ++b) {
             if (!mbar_wait_bounded(&solved[b & 1], (b >> 1) & 1, &abortFlag)) break;
             const int c0 = 32 * b, w = min(32, k - c0);
-            // a thread's rows r, r + T, r + 2T, r + 3T at once: four
-            // independent FMA chains, each row summed in column order
-            for (int rb = c0 + 64 + t; rb < k; rb += 4 * T) {
-                double acc[4] = {0.0, 0.0, 0.0, 0.0};
-                for (int cb = 0; cb < w; cb += 8) {
-                    double lv[4][8];   // eight columns' loads in flight before the FMAs
+            // one row per thread and pass, the block's columns loaded at once;
+            // each row summed in column order
+            for (int r = c0 + 64 + t; r < k; r += NT - 32) {
+                double lv[32];
 #pragma unroll
-                    for (int cc = 0; cc < 8; ++cc)
+                for (int c = 0; c < 32; ++c) lv[c] = c < w ? L[r + (long long)(c0 + c) * m] : 0.0;
+                double acc = 0.0;
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            lv[q][cc] = (cb + cc < w && rb + q * T < k) ? L[rb + q * T + (long long)(c0 + cb + cc) * m]
-                                                                         : 0.0;
-#pragma unroll
-                    for (int cc = 0; cc < 8; ++cc) {
-                        if (cb + cc >= w) break;
-                        const double yc = sh[c0 + cb + cc];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) acc[q] = fma(lv[q][cc], yc, acc[q]);
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (rb + q * T < k) sh[rb + q * T] -= acc[q];
+                for (int c = 0; c < 32; ++c)
+                    if (c < w) acc = fma(lv[c], sh[c0 + c], acc);
+                sh[r] -= acc;
             }
             mbar_arrive(&updated[b & 1]);
         }
@@ -952,15 +955,30 @@ __global__ void __launch_bounds__(kFwdThreads) k_fwd(const int* __restrict__ fro
     if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
 }
 
-// Forward substitution, non-pivot rows: upd_r -= sum_c L21[r][c] y_c, one CTA
-// per chunk of kRectRows rows of one front (all fronts of a level per launch).
-__global__ void __launch_bounds__(kRectRows) k_fwd_rect(const int2* __restrict__ tasks, const int* __restrict__ fk,
-                                                        const int* __restrict__ fm, const long long* __restrict__ foff,
-                                                        const long long* __restrict__ fupd, const int* __restrict__ fdof,
-                                                        const double* __restrict__ pool, double* __restrict__ upd,
-                                                        const double* __restrict__ y)
+// Forward substitution, non-pivot rows: upd_r -= sum_c L21[r][c] y_c for a
+// chunk of kRectRows (32) rows of one front (all fronts of a level per
+// launch).  The columns are split over kFwdRectGroups warps, a warp's lanes
+// over the chunk's rows (coalesced column segments); each lane keeps
+// kRectIlp independent FMA chains (columns c = c0 + j, c0 + j + kRectIlp, ...
+// of its warp's range) so that many loads are in flight, the chains are
+// added pairwise, and the warps' partial sums are added in warp order: a
+// fixed summation order whatever the timing.
+constexpr int kFwdRectGroups = 16;
+constexpr int kRectIlp = 8;
+
+// Levels of small fronts (every front's pivot count <= kNarrowK): one thread
+// per row and all its columns in two chains, kNarrowRows rows per CTA --
+// short rows, many fronts, so occupancy matters more than chain length.
+__global__ void __launch_bounds__(kNarrowRows) k_fwd_rect_narrow(const int2* __restrict__ tasks,
+                                                                const int* __restrict__ fk,
+                                                                const int* __restrict__ fm,
+                                                                const long long* __restrict__ foff,
+                                                                const long long* __restrict__ fupd,
+                                                                const int* __restrict__ fdof,
+                                                                const double* __restrict__ pool,
+                                                                double* __restrict__ upd, const double* __restrict__ y)
 {
-    extern __shared__ double ys[];
+    __shared__ double ys[kNarrowK];
     const int2 t = tasks[blockIdx.x];
     const int f = t.x, k = fk[f], m = fm[f], d0 = fdof[f];
     for (int c = threadIdx.x; c < k; c += blockDim.x) ys[c] = y[d0 + c];
@@ -977,9 +995,56 @@ __global__ void __launch_bounds__(kRectRows) k_fwd_rect(const int2* __restrict__
     if (c < k) s0 = fma(L[(long long)c * m], ys[c], s0);
     upd[fupd[f] + (r - k)] -= s0 + s1;
 }
+__global__ void __launch_bounds__(32 * kFwdRectGroups) k_fwd_rect(const int2* __restrict__ tasks,
+                                                                 const int* __restrict__ fk, const int* __restrict__ fm,
+                                                                 const long long* __restrict__ foff,
+                                                                 const long long* __restrict__ fupd,
+                                                                 const int* __restrict__ fdof,
+                                                                 const double* __restrict__ pool,
+                                                                 double* __restrict__ upd, const double* __restrict__ y)
+{
+    extern __shared__ double ys[];
+    __shared__ double part[kFwdRectGroups][32];
+    const int2 t = tasks[blockIdx.x];
+    const int f = t.x, k = fk[f], m = fm[f], d0 = fdof[f];
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+    for (int c = threadIdx.x; c < k; c += blockDim.x) ys[c] = y[d0 + c];
+    __syncthreads();
+    const int r = t.y + lane;
+    const int span = (k + kFwdRectGroups - 1) / kFwdRectGroups;
+    const int cBeg = g * span, cEnd = min(k, cBeg + span);
+    double acc[kRectIlp];
+#pragma unroll
+    for (int j = 0; j < kRectIlp; ++j) acc[j] = 0.0;
+    if (r < m) {
+        const double* L = pool + foff[f] + r;
+        for (int c = cBeg; c < cEnd; c += kRectIlp) {
+            double lv[kRectIlp];
+#pragma unroll
+            for (int j = 0; j < kRectIlp; ++j) lv[j] = c + j < cEnd ? L[(long long)(c + j) * m] : 0.0;
+#pragma unroll
+            for (int j = 0; j < kRectIlp; ++j)
+                if (c + j < cEnd) acc[j] = fma(lv[j], ys[c + j], acc[j]);
+        }
+    }
+#pragma unroll
+    for (int w = kRectIlp / 2; w > 0; w /= 2)
+#pragma unroll
+        for (int j = 0; j < w; ++j) acc[j] += acc[j + w];
+    part[g][lane] = acc[0];
+    __syncthreads();
+    if (g == 0 && r < m) {
+        double s = 0.0;
+        for (int q = 0; q < kFwdRectGroups; ++q) s += part[q][lane];
+        upd[fupd[f] + (r - k)] -= s;
+    }
+}
 
 // Backward substitution, non-pivot part: t_c = sum_{r >= k} L21[r][c] x_r for
-// a chunk of kRectCols pivot columns of one front (a warp per column).
+// a chunk of kRectCols pivot columns of one front (a warp per column, its
+// lanes over the rows; kRectIlp independent chains per lane, added pairwise,
+// then the lanes' sums in a fixed shuffle tree).
+template <int ILP>
 __global__ void __launch_bounds__(256) k_bwd_rect(const int2* __restrict__ tasks, const int* __restrict__ fk,
                                                   const int* __restrict__ fm, const long long* __restrict__ foff,
                                                   const int* __restrict__ fdof, const int* __restrict__ frowOff,
@@ -993,82 +1058,126 @@ __global__ void __launch_bounds__(256) k_bwd_rect(const int2* __restrict__ tasks
     if (c >= k || warp >= kRectCols) return;
     const int* rows = rowIdx + frowOff[f];
     const double* lc = pool + foff[f] + (long long)c * m;
-    double s = 0.0;
-    for (int r = k + lane; r < m; r += 32) s = fma(lc[r], x[rows[r]], s);
+    double acc[ILP];
+#pragma unroll
+    for (int j = 0; j < ILP; ++j) acc[j] = 0.0;
+    for (int r0 = k + lane; r0 < m; r0 += 32 * ILP) {
+        double lv[ILP], xv[ILP];
+#pragma unroll
+        for (int j = 0; j < ILP; ++j) {
+            const int r = r0 + 32 * j;
+            lv[j] = r < m ? lc[r] : 0.0;
+            xv[j] = r < m ? x[rows[r]] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < ILP; ++j) acc[j] = fma(lv[j], xv[j], acc[j]);
+    }
+#pragma unroll
+    for (int w = ILP / 2; w > 0; w /= 2)
+#pragma unroll
+        for (int j = 0; j < w; ++j) acc[j] += acc[j + w];
+    double s = acc[0];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) tdot[d0 + c] = s;
 }
 
 // Backward substitution, pivot part of one front: x_S = L11^-T (D^-1 y_S - t)
 // with t = L21^T x_B from k_bwd_rect (zero for fronts without ancestors), in
-// 32-column blocks from the last.
-__global__ void __launch_bounds__(256) k_bwd(const int* __restrict__ fronts, const int* __restrict__ fk,
-                                             const int* __restrict__ fm, const long long* __restrict__ foff,
-                                             const int* __restrict__ fdof, const double* __restrict__ pool,
-                                             const double* __restrict__ y, const double* __restrict__ tdot,
-                                             double* __restrict__ x)
+// 32-column blocks from the last, right-looking: once block s is solved, its
+// rows' contributions L(s, c) x_s are subtracted from every earlier column c.
+// Warp specialised like k_fwd: warp 0 subtracts block s + 1's rows from
+// block s's own columns (32 x 32) and back-solves block s on the staged
+// diagonal block; the other warps subtract each solved block's rows from the
+// columns before the block below it, one block behind.  Per column the
+// blocks' contributions are subtracted in decreasing block order, each as
+// one FMA chain in row order (a fixed order whatever the timing).
+template <int NT>
+__global__ void __launch_bounds__(NT) k_bwd(const int* __restrict__ fronts, const int* __restrict__ fk,
+                                                     const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                     const int* __restrict__ fdof, const double* __restrict__ pool,
+                                                     const double* __restrict__ y, const double* __restrict__ tdot,
+                                                     double* __restrict__ x, int* __restrict__ flag)
 {
     extern __shared__ double sh[];
-    __shared__ double dots[32];
     __shared__ double tile[32 * 33];   // the diagonal block, row-major (padded)
+    __shared__ unsigned long long solved[2], updated[2];
+    __shared__ int abortFlag;
     const int f = fronts[blockIdx.x];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double* L = pool + foff[f];
     const bool rect = m > k;
     for (int r = threadIdx.x; r < k; r += blockDim.x)
         sh[r] = y[d0 + r] / L[r + (long long)r * m] - (rect ? tdot[d0 + r] : 0.0);
+    if (threadIdx.x == 0) {
+        mbar_init(&solved[0], 32);
+        mbar_init(&solved[1], 32);
+        mbar_init(&updated[0], NT - 32);
+        mbar_init(&updated[1], NT - 32);
+        abortFlag = 0;
+    }
     __syncthreads();
-    const int nBlocks = (k + 31) / 32;
-    for (int b = nBlocks - 1; b >= 0; --b) {
-        const int c0 = 32 * b, w = min(32, k - c0);
-        for (int e = threadIdx.x; e < 32 * w; e += blockDim.x) {
-            const int col = e >> 5, row = e & 31;
-            if (row < w) tile[row * 33 + col] = L[(c0 + row) + (long long)(c0 + col) * m];
-        }
-        // a warp's columns warp, warp + nw, ... (at most four: nw = 8) at
-        // once: independent FMA chains, each column summed in row order
-        {
-            double acc[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int rb = c0 + w + lane; rb < k; rb += 4 * 32) {
-                double lv[4][4];   // four rows' loads in flight before the FMAs
+    const int nb = (k + 31) / 32;
+    // phase parity of block s's hand-off on barrier s & 1 (blocks go from
+    // nb - 1 down; a barrier serves every second one)
+    auto parity = [nb](int s) { return (uint32_t)(((nb - 1 - s) >> 1) & 1); };
+    if (warp == 0) {
+        for (int b = nb - 1; b >= 0; --b) {
+            const int c0 = 32 * b, w = min(32, k - c0);
+            const int c = c0 + lane;
+            double dl[32];   // the diagonal block's column of this lane, loads first
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
+            for (int r = 0; r < 32; ++r) dl[r] = (lane < w && r < w) ? L[(c0 + r) + (long long)c * m] : 0.0;
+            // the other warps are done with blocks b + 2 and above on these columns
+            if (b + 2 <= nb - 1 && !mbar_wait_bounded(&updated[b & 1], parity(b + 2), &abortFlag)) break;
+            if (b + 1 <= nb - 1 && lane < w) {   // block b + 1's rows on this block's columns
+                const int r0 = c0 + 32, w1 = min(32, k - r0);
+                double lv[32];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int c = warp + q * nw, r = rb + 32 * i;
-                        lv[i][q] = (c < w && r < k) ? L[r + (long long)(c0 + c) * m] : 0.0;
-                    }
+                for (int r = 0; r < 32; ++r) lv[r] = r < w1 ? L[(r0 + r) + (long long)c * m] : 0.0;
+                double acc = 0.0;
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int r = rb + 32 * i;
-                    if (r >= k) break;
-                    const double xr = sh[r];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[q] = fma(lv[i][q], xr, acc[q]);
-                }
+                for (int r = 0; r < 32; ++r)
+                    if (r < w1) acc = fma(lv[r], sh[r0 + r], acc);
+                sh[c] -= acc;
             }
+            // tile[r][lane] = L(c0 + r, c0 + lane)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int c = warp + q * nw;
-                if (c >= w) continue;
-                double v = acc[q];
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-                if (lane == 0) dots[c] = v;
-            }
-        }
-        __syncthreads();
-        if (warp == 0) {
-            double v = lane < w ? sh[c0 + lane] - dots[lane] : 0.0;
+            for (int r = 0; r < 32; ++r)
+                if (lane < w) tile[r * 33 + lane] = dl[r];
+            __syncwarp();
+            double v = lane < w ? sh[c] : 0.0;
             for (int r = w - 1; r >= 0; --r) {
                 const double xr = __shfl_sync(0xffffffffu, v, r);
                 if (lane < r) v -= tile[r * 33 + lane] * xr;
             }
-            if (lane < w) sh[c0 + lane] = v;
+            if (lane < w) sh[c] = v;
+            __syncwarp();
+            mbar_arrive(&solved[b & 1]);
         }
-        __syncthreads();
     }
+    else {
+        const int t = threadIdx.x - 32;
+        for (int s = nb - 1; s >= 1; --s) {
+            if (!mbar_wait_bounded(&solved[s & 1], parity(s), &abortFlag)) break;
+            const int r0 = 32 * s, w = min(32, k - r0);
+            // block s's rows on the columns before block s - 1
+            for (int c = t; c < 32 * (s - 1); c += NT - 32) {
+                double lv[32];
+#pragma unroll
+                for (int r = 0; r < 32; ++r) lv[r] = r < w ? L[(r0 + r) + (long long)c * m] : 0.0;
+                double acc = 0.0;
+#pragma unroll
+                for (int r = 0; r < 32; ++r)
+                    if (r < w) acc = fma(lv[r], sh[r0 + r], acc);
+                sh[c] -= acc;
+            }
+            mbar_arrive(&updated[s & 1]);
+        }
+    }
+    __syncthreads();
     for (int r = threadIdx.x; r < k; r += blockDim.x) x[d0 + r] = sh[r];
+    if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
 }
 
 template <typename T>
@@ -1203,22 +1312,44 @@ static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double si
     k_permute_in<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(rhs), P.dPermDof, sign, n, P.yperm);
     for (int l = 0; l < P.nLevels; ++l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
-        k_fwd<<<cnt, kFwdThreads, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart,
-                                             P.dChildOff, P.dChildList, P.dRelOff, P.dRelIdx, P.pool, P.upd, P.yperm,
-                                             P.dSolveFlag);
+        const size_t lshm = sizeof(double) * (size_t)std::max(P.levelMaxM[l], 1);
+        switch (kSolveThreadsFor(P.levelMaxK[l])) {
+#define OC_FWD(NT)                                                                                                      \
+    k_fwd<NT><<<cnt, NT, lshm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart, P.dChildOff,     \
+                                     P.dChildList, P.dRelOff, P.dRelIdx, P.pool, P.upd, P.yperm, P.dSolveFlag)
+        case 64: OC_FWD(64); break;
+        case 256: OC_FWD(256); break;
+        default: OC_FWD(kFwdThreads); break;
+#undef OC_FWD
+        }
         const int ro = P.rectRowOff[l], rc = P.rectRowOff[l + 1] - ro;
-        if (rc)
-            k_fwd_rect<<<rc, kRectRows, shmK, st>>>(P.dRectRowTasks + ro, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart,
-                                                    P.pool, P.upd, P.yperm);
+        if (rc && P.levelMaxK[l] <= kNarrowK)
+            k_fwd_rect_narrow<<<rc, kNarrowRows, 0, st>>>(P.dRectRowTasks + ro, P.dFk, P.dFm, P.dFoff, P.dFupd,
+                                                          P.dFdofStart, P.pool, P.upd, P.yperm);
+        else if (rc)
+            k_fwd_rect<<<rc, 32 * kFwdRectGroups, shmK, st>>>(P.dRectRowTasks + ro, P.dFk, P.dFm, P.dFoff, P.dFupd,
+                                                              P.dFdofStart, P.pool, P.upd, P.yperm);
     }
     for (int l = P.nLevels - 1; l >= 0; --l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
         const int co = P.rectColOff[l], cc = P.rectColOff[l + 1] - co;
-        if (cc)
-            k_bwd_rect<<<cc, 32 * kRectCols, 0, st>>>(P.dRectColTasks + co, P.dFk, P.dFm, P.dFoff, P.dFdofStart,
-                                                      P.dFrowOff, P.dRowIdx, P.pool, P.xperm, P.tmpDot);
-        k_bwd<<<cnt, 256, shm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFdofStart, P.pool, P.yperm,
-                                     P.tmpDot, P.xperm);
+        if (cc && P.levelMaxK[l] <= kNarrowK)
+            k_bwd_rect<1><<<cc, 32 * kRectCols, 0, st>>>(P.dRectColTasks + co, P.dFk, P.dFm, P.dFoff, P.dFdofStart,
+                                                         P.dFrowOff, P.dRowIdx, P.pool, P.xperm, P.tmpDot);
+        else if (cc)
+            k_bwd_rect<kRectIlp><<<cc, 32 * kRectCols, 0, st>>>(P.dRectColTasks + co, P.dFk, P.dFm, P.dFoff,
+                                                                P.dFdofStart, P.dFrowOff, P.dRowIdx, P.pool, P.xperm,
+                                                                P.tmpDot);
+        const size_t lshm = sizeof(double) * (size_t)std::max(P.levelMaxM[l], 1);
+        switch (kSolveThreadsFor(P.levelMaxK[l])) {
+#define OC_BWD(NT)                                                                                                      \
+    k_bwd<NT><<<cnt, NT, lshm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFdofStart, P.pool, P.yperm,          \
+                                     P.tmpDot, P.xperm, P.dSolveFlag)
+        case 64: OC_BWD(64); break;
+        case 256: OC_BWD(256); break;
+        default: OC_BWD(kFwdThreads); break;
+#undef OC_BWD
+        }
     }
     k_permute_out<<<(n + 255) / 256, 256, 0, st>>>(P.xperm, P.dPermDof, n, reinterpret_cast<double*>(x));
 }
@@ -1240,8 +1371,12 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
     for (int f = 0; f < P.nFronts; ++f) maxK = std::max(maxK, P.fk[f]);
     const size_t shm = sizeof(double) * (size_t)P.maxM, shmK = sizeof(double) * (size_t)std::max(maxK, 1);
     if (shm > 48 * 1024) {
-        cudaFuncSetAttribute(k_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-        cudaFuncSetAttribute(k_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_fwd<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_fwd<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_fwd<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bwd<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bwd<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bwd<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     }
     if (shmK > 48 * 1024) cudaFuncSetAttribute(k_fwd_rect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmK);
     if (P.useGraphs && (!P.solveGraph || P.solveKey[0] != rhs || P.solveKey[1] != x || P.solveSign != sign)) {

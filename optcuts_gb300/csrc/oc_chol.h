@@ -12,8 +12,12 @@ namespace oc {
 
 constexpr int kTile = 32;      // dense tile edge (FP64) of the front kernels
 constexpr int kUpd = 64;       // edge of the trailing-update blocks (FP64, 4x4 per thread)
-constexpr int kRectRows = 256; // rows of L21 per CTA in the forward GEMV
-constexpr int kRectCols = 8;   // columns of L21 per CTA in the backward GEMV^T
+constexpr int kRectRows = 32;  // rows of L21 per CTA in the forward GEMV (a warp's lanes)
+constexpr int kRectCols = 8;   // columns of L21 per CTA in the backward GEMV^T (a warp each)
+// levels whose fronts all have at most kNarrowK pivots use the narrow
+// forward GEMV (a thread per row, kNarrowRows rows per CTA)
+constexpr int kNarrowK = 64;
+constexpr int kNarrowRows = 256;
 
 struct TileTask {           // one CTA's work item in a tiled front kernel
     int front, i, j, p;
@@ -46,6 +50,7 @@ struct CholPlan {
     // substitution work split: per level, (front, first row/column) chunks of
     // the rectangular part L21 (rows k..m) for the multi-CTA GEMV kernels
     std::vector<int> rectRowOff, rectColOff;   // nLevels + 1
+    std::vector<int> levelMaxK, levelMaxM;     // per level: largest pivot count and front size
     std::vector<int2> rectRowTasks, rectColTasks;
     int2* dRectRowTasks = nullptr;
     int2* dRectColTasks = nullptr;
