@@ -353,6 +353,8 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
     queries()   # warm-up
     t_gpu, qs = timed_step(features=True)
     t_fp32, qs32 = timed_step(fp32=True)
+    queries(autotune=True)   # the schedule autotuner measures its candidates on this state
+    t_tuned, qs_t = timed_step(autotune=True)
     qb, qm, qi = qs
     topo = {"metric": "topology-step s (exhaustive candidate evaluation: boundary split, merge and interior split "
                       "queries of one state, solved together)", "value": t_gpu, "unit": "s",
@@ -368,7 +370,9 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
             "max_local_iterations": max(q["max_local_iters"] for q in qs),
             "local_iterations": sum(q["local_iters_total"] for q in qs),
             "local_capped": sum(q["local_capped"] for q in qs),
-            **summary(qs), "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)}}
+            **summary(qs), "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)},
+            "autotuned_schedules": {"value": t_tuned, "unit": "s", **summary(qs_t),
+                                    "table": oc.topology_schedules()}}
     e_w = opt.getLastEnergyVal(excludeScaffold=True) + lam_t * so["E_se"]
 
     def after(qs_):

@@ -318,7 +318,7 @@ int oc_mesh_split_filter(oc_mesh* mesh, double* divGrad);
  * FP32 (about 8x faster local solves; energies, gradients, line search and
  * the local LDL^T stay FP64; energy changes then agree with the FP64
  * evaluation to ~1e-4 relative instead of ~1e-8). */
-enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2 };
+enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2, OC_TOPO_AUTOTUNE = 8 };
 int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out);
 /* No counterpart in the reference: the learned proposal.  Every local
  * problem first gets one Newton step (its features: energies, gradient
@@ -432,6 +432,17 @@ int oc_mesh_apply_topology(oc_mesh* mesh, int opType, const int* path, int pathL
  * mlp / topFrac select the learned proposal (mlp NULL: exhaustive). */
 int oc_topology_queries(oc_mesh* mesh, const int* ops, int nOps, double lambda_t, double filterExp, int options,
                         oc_mlp* mlp, double topFrac, oc_topo_result** out);
+/* The local solves' schedule autotuner (queries with OC_TOPO_AUTOTUNE): on
+ * the first batch of each (device, size class, problem-count bucket,
+ * triangle-count bucket) the class's candidate schedules (threads per
+ * problem, block size, cluster size) are timed on the batch itself and the
+ * fastest is kept for later batches of that key; without the flag the fixed
+ * rule applies, so that the schedule (and the rounding of clustered sums)
+ * does not depend on timing.  The table, one row per key: rows (n x 11:
+ * device, class (+4 for one-iteration probe passes), log2 count, log2
+ * triangles, the chosen tpp / cluster / block, the rule's tpp / cluster /
+ * block, candidates timed) and ms (n x 2: chosen, rule). */
+int oc_topology_schedules(int* nRows, int* rows, float* ms);
 /* The same queries sharded over shardCount processes (one GPU each): the
  * candidate lists are enumerated in full on every shard, but only candidates
  * c with c % shardCount == shardRank get their local solves; the others

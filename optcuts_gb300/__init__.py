@@ -164,6 +164,7 @@ _SIGS = {
     "oc_optimizer_last_vectors": [_vp, _d, _d],
     "oc_optimizer_bad_pivots": [_vp, _i],
     "oc_linsys_set_pattern_neighbors": [_vp, ctypes.c_int, _i, _i, _i, ctypes.c_int],
+    "oc_topology_schedules": [_i, _i, _vp],
     "oc_topology_queries": [_vp, _i, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _vp,
                             ctypes.c_double, ctypes.POINTER(_vp)],
     "oc_topology_query_tail": [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(_vp)],
@@ -356,7 +357,8 @@ class TriMesh:
         query_ms = 1000.0 * (time.perf_counter() - t0)
         return self._result(h, features, mlp, query_ms)
 
-    def topologyStep(self, lambda_t, filterExp=0.6, fp32=False, features=False, mlp=None, topFrac=0.1):
+    def topologyStep(self, lambda_t, filterExp=0.6, fp32=False, features=False, mlp=None, topFrac=0.1,
+                     autotune=False):
         """The three queries of one topology step on the current state —
         boundary split, merge, interior split — built together and solved in
         the same launches (each result equals its own query's); with mlp the
@@ -364,7 +366,7 @@ class TriMesh:
         solved exactly).  Returns (split, merge, interior); query_ms of each is
         the whole step's library time."""
         hs = [_vp(), _vp(), _vp()]
-        opt = (1 if fp32 else 0) | (2 if features else 0)
+        opt = (1 if fp32 else 0) | (2 if features else 0) | (8 if autotune else 0)
         t0 = time.perf_counter()
         self.ctx.check(lib().oc_topology_step(self.h, float(lambda_t), float(filterExp), opt,
                                               mlp.h if mlp is not None else None, float(topFrac),
@@ -714,6 +716,25 @@ def chol_analyze_stats(nV, F, fixedVert=(0,), leafSize=16, xy=None):
     if rc != OC_OK:
         raise OCError(rc, "oc_chol_analyze_stats")
     return symbolic_stats_dict(out)
+
+
+def topology_schedules():
+    """The local-solve schedule autotuner's table (OC_TOPO_AUTOTUNE queries):
+    one dict per key with the chosen and the fixed rule's schedule and their
+    measured milliseconds."""
+    n = ctypes.c_int()
+    lib().oc_topology_schedules(ctypes.byref(n), None, None)
+    rows = np.zeros((n.value, 11), np.int32)
+    ms = np.zeros((n.value, 2), np.float32)
+    if n.value:
+        lib().oc_topology_schedules(ctypes.byref(n), _pi(rows), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    out = []
+    for r, t in zip(rows, ms):
+        out.append({"class": int(r[1]) % 4, "probe": bool(r[1] >= 4), "count_log2": int(r[2]), "tri_log2": int(r[3]),
+                    "chosen": {"tpp": int(r[4]), "cluster": int(r[5]), "block": int(r[6]), "ms": float(t[0])},
+                    "rule": {"tpp": int(r[7]), "cluster": int(r[8]), "block": int(r[9]), "ms": float(t[1])},
+                    "candidates": int(r[10])})
+    return out
 
 
 def default_config(**kw):

@@ -907,7 +907,7 @@ static int topology_query(oc_mesh* m, int opType, double lambda_t, double filter
 int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out)
 {
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
     return topology_query(m, opType, lambda_t, filterExp, opts, out);
 }
 
@@ -916,7 +916,7 @@ int oc_topology_query_learned(oc_mesh* m, int opType, double lambda_t, double fi
 {
     if (!mlp || mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+    opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
     opts.mlp = &mlp->m;
     opts.topFrac = topFrac;
     return topology_query(m, opType, lambda_t, filterExp, opts, out);
@@ -1012,9 +1012,9 @@ int oc_topology_step(oc_mesh* m, double lambda_t, double filterExp, int options,
     if (!split || !merge || !interior) return OC_ERR_INVALID;
     if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
     if (mlp) {
-        opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
         opts.mlp = &mlp->m;
         opts.topFrac = topFrac;
     }
@@ -1034,9 +1034,9 @@ int oc_topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, d
     if (!ops || !out || nOps <= 0 || nOps > 3) return OC_ERR_INVALID;
     if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
     if (mlp) {
-        opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
         opts.mlp = &mlp->m;
         opts.topFrac = topFrac;
     }
@@ -1050,9 +1050,9 @@ int oc_topology_queries_sharded(oc_mesh* m, const int* ops, int nOps, double lam
         return OC_ERR_INVALID;
     if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
     if (mlp) {
-        opts.flags = (options & oc::kTopoFp32Hessian) | oc::kTopoLearned;
+        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
         opts.mlp = &mlp->m;
         opts.topFrac = topFrac;
     }
@@ -1076,6 +1076,26 @@ int oc_topology_query_tail(oc_mesh* m, int opType, double lambda_t, int options,
         verts[n++] = m->tails[2];
     }
     return topology_queries(m, &opType, 1, lambda_t, 0.6, opts, out, verts, n);
+}
+
+int oc_topology_schedules(int* nRows, int* rows, float* ms)
+{
+    if (!nRows) return OC_ERR_INVALID;
+    const auto t = oc::topo_schedule_table();
+    *nRows = static_cast<int>(t.size());
+    for (size_t i = 0; i < t.size(); ++i) {
+        const oc::ScheduleRecord& r = t[i];
+        if (rows) {
+            const int v[11] = {r.device, r.cls, r.countBucket, r.triBucket, r.best.tpp, r.best.cluster, r.best.block,
+                               r.rule.tpp, r.rule.cluster, r.rule.block, r.candidates};
+            std::copy(v, v + 11, rows + 11 * i);
+        }
+        if (ms) {
+            ms[2 * i] = r.bestMs;
+            ms[2 * i + 1] = r.ruleMs;
+        }
+    }
+    return OC_OK;
 }
 
 int oc_mesh_fracture_tails(oc_mesh* m, int* tails3)

@@ -14,6 +14,9 @@
 #include "oc_mlp.h"
 
 #include <algorithm>
+#include <array>
+#include <map>
+#include <mutex>
 #include <deque>
 #include <unordered_map>
 #include <cfloat>
@@ -344,6 +347,50 @@ bool inverted_any(const Topo& T, const std::vector<double>& V, const std::vector
 
 namespace {
 
+// ---- schedule autotuner ------------------------------------------------
+// On first use of a (device, size class, problem-count bucket, largest
+// triangle-count bucket) the candidate schedules of the class are timed on
+// the batch itself (CUDA events on the class's stream, one run each after
+// the first) and the fastest is kept for later batches of that key.  Opt-in
+// (kTopoAutotune): the fixed rule is the default, so that a run's schedule
+// -- and with it the rounding of the clustered sums -- does not depend on
+// timing.
+std::mutex g_schedMu;
+std::map<std::array<int, 4>, ScheduleRecord> g_schedTable;
+
+int log2_bucket(int x)
+{
+    int b = 0;
+    while ((1 << (b + 1)) <= x) ++b;
+    return b;
+}
+
+std::vector<LocalSchedule> schedule_candidates(int cls, int maxTri, int maxCluster)
+{
+    std::vector<LocalSchedule> c;
+    if (cls == 3) c = {{8, 1, 32}, {8, 1, 128}, {32, 1, 32}, {32, 1, 128}};
+    else if (cls == 2) c = {{32, 1, 32}, {32, 1, 128}, {128, 1, 128}, {8, 1, 128}};
+    else {
+        c = {{128, 1, 128}, {32, 1, 128}};
+        const int need = (maxTri + 31) / 32;
+        for (int cl = 2; cl <= maxCluster && cl <= 16; cl *= 2)
+            if (cl <= 2 * need) c.push_back({64, cl, 64});
+    }
+    return c;
+}
+
+} // namespace
+
+std::vector<ScheduleRecord> topo_schedule_table()
+{
+    std::lock_guard<std::mutex> lock(g_schedMu);
+    std::vector<ScheduleRecord> out;
+    for (const auto& kv : g_schedTable) out.push_back(kv.second);
+    return out;
+}
+
+namespace {
+
 // Solves the problems `which` of B into res[k], grouped by size class
 // (threads per problem and cluster size from local_schedule), the classes
 // launched on their own streams so that the few large fans overlap the many
@@ -351,7 +398,7 @@ namespace {
 // names B: a second call for the same batch (the learned proposal's exact
 // pass after its probe) reuses the problem arrays already on the device.
 int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchId, const std::vector<int>& which,
-                int maxIterOverride, int fp32, std::vector<LocalResult>& res, std::string* err)
+                int maxIterOverride, int fp32, std::vector<LocalResult>& res, std::string* err, bool autotune = false)
 {
     if (which.empty()) return OC_OK;
     TopoWorkspace tmp;
@@ -438,6 +485,54 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
             cb.prob = static_cast<const LocalProblem*>(W.buf[0]) + start[c];
             cb.out = static_cast<LocalResult*>(W.buf[6]) + start[c];
             cb.nProb = count[c];
+            if (e == cudaSuccess && autotune) {
+                // (a one-iteration probe pass is its own workload)
+                const std::array<int, 4> key = {dev, c + (maxIterOverride == 1 ? kClasses : 0), log2_bucket(count[c]),
+                                                log2_bucket(maxTri[c])};
+                bool known = false;
+                {
+                    std::lock_guard<std::mutex> lock(g_schedMu);
+                    auto it = g_schedTable.find(key);
+                    if (it != g_schedTable.end()) {
+                        sched[c] = it->second.best;
+                        known = true;
+                    }
+                }
+                if (!known) {
+                    ScheduleRecord rec{dev, key[1], key[2], key[3], sched[c], sched[c], 0.f, 0.f, 0};
+                    cudaEvent_t a = nullptr, z = nullptr;
+                    e = cudaEventCreate(&a);
+                    if (e == cudaSuccess) e = cudaEventCreate(&z);
+                    const auto cands = schedule_candidates(c, maxTri[c], maxCluster);
+                    float bestMs = -1.f;
+                    for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass)   // pass 0 warms every candidate up
+                        for (const LocalSchedule& cs : cands) {
+                            if (e != cudaSuccess) break;
+                            e = cudaEventRecord(a, W.aux[c]);
+                            if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, cs, W.aux[c]);
+                            if (e == cudaSuccess) e = cudaEventRecord(z, W.aux[c]);
+                            if (e == cudaSuccess) e = cudaEventSynchronize(z);
+                            float ms = 0.f;
+                            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, z);
+                            if (e != cudaSuccess || pass == 0) continue;
+                            if (cs.tpp == rec.rule.tpp && cs.cluster == rec.rule.cluster && cs.block == rec.rule.block)
+                                rec.ruleMs = ms;
+                            if (bestMs < 0.f || ms < bestMs) {
+                                bestMs = ms;
+                                rec.best = cs;
+                            }
+                        }
+                    if (a) cudaEventDestroy(a);
+                    if (z) cudaEventDestroy(z);
+                    if (e == cudaSuccess) {
+                        rec.bestMs = bestMs;
+                        rec.candidates = static_cast<int>(cands.size());
+                        sched[c] = rec.best;
+                        std::lock_guard<std::mutex> lock(g_schedMu);
+                        g_schedTable[key] = rec;
+                    }
+                }
+            }
             if (e == cudaSuccess) e = launch_local_newton(*in.dm, in.surfaceArea, cb, sched[c], W.aux[c]);
             if (e == cudaSuccess) e = cudaEventRecord(W.ev[c], W.aux[c]);
             if (e == cudaSuccess) e = cudaStreamWaitEvent(in.st, W.ev[c], 0);
@@ -1536,13 +1631,14 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
     const unsigned long long batchId = in.ws ? in.ws->nextBatch++ : 0;
     const bool learned = (opts.flags & kTopoLearned) && opts.mlp;
     const int fp32 = opts.flags & kTopoFp32Hessian;
+    const bool tune = (opts.flags & kTopoAutotune) != 0;
     double probeMs = 0.0, exactMs = 0.0;
     if (n) {
         std::string e2;
         std::vector<int> all(n);
         for (size_t k = 0; k < n; ++k) all[k] = static_cast<int>(k);
         if (learned) {
-            int rc = solve_batch(in, B, batchId, all, 1, fp32, res, &e2);
+            int rc = solve_batch(in, B, batchId, all, 1, fp32, res, &e2, tune);
             if (rc) { if (err) *err = e2; return rc; }
             const auto tA = clk::now();
             probeMs = std::chrono::duration<double, std::milli>(tA - t1).count();
@@ -1582,13 +1678,13 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
             std::sort(sel.begin(), sel.end());
             std::vector<LocalResult> full(n);
             const auto tB = clk::now();
-            rc = solve_batch(in, B, batchId, sel, -1, fp32, full, &e2);
+            rc = solve_batch(in, B, batchId, sel, -1, fp32, full, &e2, tune);
             if (rc) { if (err) *err = e2; return rc; }
             for (int k : sel) res[k] = full[k];
             exactMs = std::chrono::duration<double, std::milli>(clk::now() - tB).count();
         }
         else {
-            const int rc = solve_batch(in, B, batchId, all, -1, fp32, res, &e2);
+            const int rc = solve_batch(in, B, batchId, all, -1, fp32, res, &e2, tune);
             if (rc) { if (err) *err = e2; return rc; }
             for (int i = 0; i < nOps; ++i) {
                 results[i].stats.nSelected = static_cast<int>(start[i + 1] - start[i]);

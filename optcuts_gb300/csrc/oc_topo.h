@@ -80,7 +80,17 @@ struct TopoStats {
 
 struct Mlp;
 constexpr int kTopoNumFeatures = 32;
-enum { kTopoFp32Hessian = 1, kTopoRecordFeatures = 2, kTopoLearned = 4 };
+enum { kTopoFp32Hessian = 1, kTopoRecordFeatures = 2, kTopoLearned = 4, kTopoAutotune = 8 };
+// the autotuner's table: one row per (device, size class, count bucket,
+// triangle bucket): the schedule it measured fastest and its milliseconds,
+// next to the fixed rule's
+struct ScheduleRecord {
+    int device, cls, countBucket, triBucket;
+    LocalSchedule best, rule;
+    float bestMs, ruleMs;
+    int candidates;
+};
+std::vector<ScheduleRecord> topo_schedule_table();
 struct TopoOptions {
     int flags = 0;          // kTopoFp32Hessian | kTopoRecordFeatures | kTopoLearned
     Mlp* mlp = nullptr;     // learned proposal: ranks the local problems

@@ -226,3 +226,23 @@ def test_sharded_step_equals_unsharded(golden, case, world):
         np.testing.assert_array_equal(np.array([c["energyChanges"] for c in q["candidates"]]).reshape(-1, 2),
                                       s["energyChanges"])
         assert q["best"] == s["best"]
+
+
+def test_autotuned_schedules_same_candidates(golden):
+    """The measured schedule autotuner: the step with the tuned schedules
+    reports the same candidates (energy changes to 1e-8 relative: clustered
+    sums may group differently) and fills the table with timings."""
+    g = golden("ellipsoid_2k_topo")
+    m = topo_mesh(g)
+    lam = float(g["topo_best"][3])
+    ref = m.topologyStep(lam)
+    for _ in range(2):   # the first call tunes, the second reuses the table
+        got = m.topologyStep(lam, autotune=True)
+        for q, r in zip(got, ref):
+            assert len(q["candidates"]) == len(r["candidates"]) and q["best"] == r["best"]
+            for a, b in zip(q["candidates"], r["candidates"]):
+                if b["EwDec"] > -1e300:
+                    assert abs(a["EwDec"] - b["EwDec"]) <= 1e-8 * abs(b["EwDec"]) + 1e-14
+    table = oc.topology_schedules()
+    assert table and all(t["chosen"]["ms"] > 0.0 and t["candidates"] >= 2 for t in table)
+    assert all(t["chosen"]["ms"] <= t["rule"]["ms"] + 1e-6 for t in table if t["rule"]["ms"] > 0.0)
