@@ -170,3 +170,32 @@ def test_rebuilt_scaffold_keeps_analysis(golden):
     opt.solve(1)
     s1 = opt.solver_stats()
     assert s0 == s1
+
+
+def test_torus_41k_converges_to_reference_energy(golden):
+    """The genus-1 torus workload (40,960 triangles: cut_to_disk + Tutte,
+    scaffold on, the project's own air mesh rebuilt after every iteration)
+    from the reference's own start state to convergence: the converged
+    energy within 1e-3 of the reference's run (tests/golden/torus_41k_conv)."""
+    from optcuts_gb300 import init as I
+    from optcuts_gb300 import meshes as M
+    g = golden("torus_41k_conv")
+    V, F = M.CONFIGS["torus_41k"]()
+    st = I.init_uv(V, F)
+    chk = np.concatenate([st.UV.sum(0), st.UV[0], st.UV[-1]])
+    assert len(st.UV) == int(g["uv0_check"][6]) and len(st.F) == int(g["uv0_check"][7])
+    np.testing.assert_allclose(chk, g["uv0_check"][:6], rtol=0, atol=1e-8 * len(st.UV))
+    m = oc.TriMesh(st.V_rest, st.UV, st.F, st.fixedVert)
+    opt = oc.Optimizer(m, [1.0 - g["scalars"][4]])
+    opt.rebuildScaffold()
+    opt.precompute()
+    assert opt.getLastEnergyVal(excludeScaffold=True) == pytest.approx(g["trace_E"][0], rel=1e-12)
+    E = [opt.getLastEnergyVal(True)]
+    for _ in range(200):
+        status = opt.solve(1)
+        opt.rebuildScaffold()
+        E.append(opt.getLastEnergyVal(True))
+        if status == 1:
+            break
+    assert status == 1 and m.checkInversion()
+    assert abs(E[-1] - g["trace_E"][-1]) / g["trace_E"][-1] < 1e-3, (E[-1], g["trace_E"][-1])
