@@ -20,8 +20,8 @@ The result is the TriMesh the reference builds with
 ``TriMesh(V, F, UV_Tutte, F_cut, false)`` (main.cpp:1534, TriMesh.cpp:122-189):
 the rest positions are re-indexed to the cut mesh and vertex 0 is fixed.
 
-Several components (the reference's grid layout of their UV disks) are not
-handled here.
+Several components are handled as the reference handles them: each cut by
+its own Euler characteristic, their UV disks on a grid.
 """
 from __future__ import annotations
 
@@ -94,11 +94,11 @@ def euler_characteristic(V, F):
     return nV - nE + len(F)
 
 
-def one_point_cut(V, F):
-    """Split vertex vI = F[0,0] along path [n0, vI, n2] (n0, n2: its first and
-    third neighbours in index order).  Returns (V', F', path)."""
+def one_point_cut(V, F, vI=None):
+    """Split vertex vI (default F[0,0]) along path [n0, vI, n2] (n0, n2: its
+    first and third neighbours in index order).  Returns (V', F', path)."""
     F = np.array(F, np.int32, copy=True)
-    vI = int(F[0, 0])
+    vI = int(F[0, 0]) if vI is None else int(vI)
     nbrs = set()
     inc = np.nonzero((F == vI).any(axis=1))[0]
     for t in inc:
@@ -131,6 +131,38 @@ def one_point_cut(V, F):
     for t in tri_left:
         F[t][F[t] == vI] = nV
     return V2, F, path
+
+
+def facet_components(F):
+    """Component label of every triangle (triangles sharing an edge are
+    connected; igl::facet_components), labels in order of first appearance."""
+    F = np.asarray(F)
+    n = len(F)
+    parent = np.arange(n)
+
+    def root(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+    edge = {}
+    for t in range(n):
+        for k in range(3):
+            a, b = int(F[t, k]), int(F[t, (k + 1) % 3])
+            key = (min(a, b), max(a, b))
+            if key in edge:
+                ra, rb = root(edge[key]), root(t)
+                if ra != rb:
+                    parent[max(ra, rb)] = min(ra, rb)
+            else:
+                edge[key] = t
+    labels, C = {}, np.zeros(n, np.int64)
+    for t in range(n):
+        r = root(t)
+        if r not in labels:
+            labels[r] = len(labels)
+        C[t] = labels[r]
+    return C
 
 
 def cut_to_disk(F):
@@ -188,21 +220,55 @@ def cut_high_genus(V, F):
             return V_rest, F
         if ec > 1:
             raise NotImplementedError("a component turned closed genus 0 while being cut")
-        made = 0
-        for seam in cut_to_disk(F):
-            seam = list(seam)
-            if seam[0] == seam[-1]:
-                # (an interior cut of three vertices counts no split, as in cutPath)
-                V_rest, UV, F, cohE, m = cut_path(seam[-3:], V_rest, UV, F, cohE)
-                made += m
-                seam = seam[:-2]
-            V_rest, UV, F, cohE, m = cut_path(seam, V_rest, UV, F, cohE)
-            made += m
-            if made:
-                break
+        V_rest, UV, F, cohE, made = cut_component_once(F, V_rest, UV, F, cohE)
         if not made:
             raise ValueError("no cut made while cutting to a disk")
     raise ValueError("cutting to a disk did not finish")
+
+
+def cut_component_once(F_comp, V_rest, UV, F, cohE):
+    """One pass of the reference's cut_to_disk loop for one component
+    (main.cpp:1423-1451): the component's cut graph, then the first seam
+    that cuts anything applied to the whole mesh."""
+    made = 0
+    for seam in cut_to_disk(F_comp):
+        seam = list(seam)
+        if seam[0] == seam[-1]:
+            # (an interior cut of three vertices counts no split, as in cutPath)
+            V_rest, UV, F, cohE, m = cut_path(seam[-3:], V_rest, UV, F, cohE)
+            made += m
+            seam = seam[:-2]
+        V_rest, UV, F, cohE, m = cut_path(seam, V_rest, UV, F, cohE)
+        made += m
+        if made:
+            break
+    return V_rest, UV, F, cohE, made
+
+
+def boundary_loops(F):
+    """igl::boundary_loop's loops: each starts at the smallest boundary
+    vertex not yet on a loop and follows the boundary half-edges."""
+    F = np.asarray(F)
+    he = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+    key = he[:, 0].astype(np.int64) * (F.max() + 1) + he[:, 1]
+    rkey = he[:, 1].astype(np.int64) * (F.max() + 1) + he[:, 0]
+    bhe = he[~np.isin(key, rkey)]
+    nxt = {}
+    for a, b in bhe.tolist():
+        nxt.setdefault(a, b)
+    loops, seen = [], set()
+    for start in sorted(nxt):
+        if start in seen:
+            continue
+        loop = [start]
+        seen.add(start)
+        v = nxt[start]
+        while v not in seen and v in nxt:
+            loop.append(v)
+            seen.add(v)
+            v = nxt[v]
+        loops.append(loop)
+    return loops
 
 
 def boundary_loop(F):
@@ -258,25 +324,66 @@ def harmonic(F, n, bnd, bnd_uv):
 
 
 def init_uv(V, F):
-    """Cut (if closed genus 0) and Tutte-embed; returns an InitState."""
+    """Cut every component to a disk and Tutte-embed the whole mesh, as the
+    reference's "no input UV" start does (main.cpp:1379-1534): per component
+    by its Euler characteristic -- closed genus 0: the one-point cut at its
+    first triangle's first vertex; genus >= 1: the cut_to_disk loop; a disk:
+    nothing -- repeated until every component is a disk; then per component
+    its longest boundary loop on a unit circle, the circles on a grid 2.1
+    apart (main.cpp:1503-1527), and one harmonic map with every loop held.
+    Returns an InitState."""
     V = np.asarray(V, np.float64)
     F_mesh = np.asarray(F, np.int32)
-    F = F_mesh
-    ec = euler_characteristic(V, F)
+    C = facet_components(F_mesh)
+    nComp = int(C.max()) + 1 if len(C) else 0
+    V_rest, F = V, F_mesh
+    UV = np.zeros((len(V_rest), 2))
+    cohE = np.zeros((0, 4), np.int32)
     path = None
-    if ec == 2:
-        V, F, path = one_point_cut(V, F)
-    elif ec < 1:
-        V, F = cut_high_genus(V, F)
-        path = []
-    elif ec != 1:
-        raise NotImplementedError("only single-component meshes are initialised here")
-    bnd = boundary_loop(F)
-    if not bnd:
-        raise ValueError("mesh has no boundary after the cut")
-    bnd = np.asarray(bnd, np.int64)
-    UV = harmonic(F, len(V), bnd, map_vertices_to_circle(V, bnd))
+    cut_any = False
+    for _ in range(10000):
+        todo = []
+        for ci in range(nComp):
+            Fc = F[C == ci]
+            ec = euler_characteristic(V_rest, Fc)
+            if ec < 1 or ec == 2:
+                todo.append((ci, ec))
+            elif ec != 1:
+                raise NotImplementedError("component %d: unsupported Euler characteristic %d" % (ci, ec))
+        if not todo:
+            break
+        for ci, ec in todo:
+            Fc = F[C == ci]
+            if ec == 2:
+                V_rest, F, p = one_point_cut(V_rest, F, int(Fc[0, 0]))
+                UV = np.vstack([UV, np.zeros((len(V_rest) - len(UV), 2))])
+                path = p if nComp == 1 else path
+            else:
+                V_rest, UV, F, cohE, made = cut_component_once(Fc, V_rest, UV, F, cohE)
+                if not made:
+                    raise ValueError("no cut made while cutting component %d to a disk" % ci)
+                if path is None:
+                    path = []
+            cut_any = True
+    grid = 0
+    while grid * grid < nComp:
+        grid += 1
+    bnd, bnd_uv = [], []
+    for ci in range(nComp):
+        loops = boundary_loops(F[C == ci])
+        if not loops:
+            raise ValueError("component %d has no boundary after the cut" % ci)
+        longest = max(range(len(loops)), key=lambda i: (len(loops[i]), -i))
+        loop = np.asarray(loops[longest], np.int64)
+        uv = map_vertices_to_circle(V_rest, loop)
+        uv = uv + np.array([ci % grid * 2.1, ci // grid * 2.1])
+        bnd.append(loop)
+        bnd_uv.append(uv)
+    bnd = np.concatenate(bnd)
+    UV = harmonic(F, len(V_rest), bnd, np.vstack(bnd_uv))
     # a cut mesh is built from (F_mesh, F_uv) with cohesive edges along the
-    # cut (TriMesh.cpp:122-189); an uncut disk has none (TriMesh.cpp:116-120)
-    cohE = cohesive_edges(F_mesh, F) if path is not None else np.zeros((0, 4), np.int32)
-    return InitState(V, UV, F, np.array([0], np.int32), path, bnd, cohE)
+    # cuts (TriMesh.cpp:122-189); an uncut disk has none (TriMesh.cpp:116-120)
+    cohE = cohesive_edges(F_mesh, F) if cut_any else np.zeros((0, 4), np.int32)
+    if nComp == 1 and path is None:
+        path = None
+    return InitState(V_rest, UV, F, np.array([0], np.int32), path, bnd, cohE)

@@ -246,6 +246,19 @@ def cube():
     return V, np.asarray(F, np.int32)
 
 
+def components_mesh():
+    """Three components in one mesh: a sphere, a torus and a bumpy sheet
+    (the reference cuts each by its own Euler characteristic and lays their
+    UV disks out on a grid)."""
+    parts = [icosphere(2, 0.01, 0), torus(24, 16, 1.0, 0.35, 1), bumpy_sheet(12, 0.25, 0.01, 5)]
+    V, F, off = [], [], 0
+    for k, (v, f) in enumerate(parts):
+        V.append(np.asarray(v, np.float64) + np.array([3.0 * k, 0.0, 0.0]))
+        F.append(np.asarray(f, np.int32) + off)
+        off += len(v)
+    return np.vstack(V), np.vstack(F).astype(np.int32)
+
+
 CONFIGS = {
     # the five synthetic workloads, by the reference's own sizes
     "icosphere_5k": lambda: icosphere(4, 0.01, 0),
@@ -262,4 +275,5 @@ CONFIGS = {
     "cube": cube,
     "plane": plane,
     "triangle": single_triangle,
+    "components": components_mesh,
 }

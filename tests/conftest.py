@@ -20,7 +20,7 @@ def load_golden(name):
 
 
 GOLDEN_CASES = ["triangle", "plane", "cube", "icosphere_320", "ellipsoid_2k", "torus_768", "icosphere_5k",
-                "sheet_3k", "icosphere_320_scaf"]
+                "sheet_3k", "icosphere_320_scaf", "components"]
 # closed genus-0 inputs: the reference runs its first Newton phase without the scaffold
 SCAFFOLD_OFF = ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k"]
 
@@ -56,7 +56,7 @@ def golden_candidates(g, op):
 
 
 # cases whose golden holds the air mesh of every iteration
-SCAFFOLD_DUMPS = ["triangle", "plane", "torus_768", "sheet_3k", "icosphere_320_scaf"]
+SCAFFOLD_DUMPS = ["triangle", "plane", "torus_768", "sheet_3k", "icosphere_320_scaf", "components"]
 
 
 def golden_scaffolds(g):

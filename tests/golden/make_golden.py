@@ -66,6 +66,9 @@ CASES = {
     "sheet_3k_topo": ("sheet_3k", 0.999, 60, 16, False, ["nobij", "topo"]),
     "torus_768_topo": ("torus_768", 0.999, 60, 16, False, ["nobij", "topo"]),
     "ellipsoid_2k_topo": ("ellipsoid_2k", 0.999, 300, 16, False, ["nobij", "topo"]),
+    # three components (sphere, torus, sheet): each cut by its own Euler
+    # characteristic, their UV disks on a grid; the scaffold holds them apart
+    "components": ("components", 0.999, 30, 16, False, ["scafdump"]),
     # slim cases (large meshes: only the traces, scalars and air meshes kept)
     # the 199k-triangle ellipsoid benchmark workload from its Tutte start with
     # the scaffold on: the reference's air mesh of that start and its first

@@ -112,7 +112,8 @@ def test_bad_scaffold_rejected(golden):
         opt.setScaffold(oc.Scaffold(airV, airF, bnd2))
 
 
-@pytest.mark.parametrize("case,tol", [("sheet_3k", 1e-4), ("torus_768", 1e-3), ("icosphere_320_scaf", 1e-4)])
+@pytest.mark.parametrize("case,tol", [("sheet_3k", 1e-4), ("torus_768", 1e-3), ("icosphere_320_scaf", 1e-4),
+                                      ("components", 1e-3)])
 def test_own_air_meshes_reach_reference_energy(golden, case, tol):
     """The reference's loop with the project's air meshes: rebuild the
     scaffold from the current UV after every iteration (Optimizer.cpp:251-257)."""

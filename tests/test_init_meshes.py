@@ -8,11 +8,13 @@ from optcuts_gb300 import meshes as M
 
 
 @pytest.mark.parametrize("case", ["cube", "icosphere_320", "ellipsoid_2k", "icosphere_5k", "plane", "triangle",
-                                  "sheet_3k", "torus_768"])
+                                  "sheet_3k", "torus_768", "components"])
 def test_init_matches_reference(golden, case):
     """The cut mesh (one-point cut for genus 0; for the genus-1 torus the
-    reference's cut_to_disk loop), its boundary loop and cohesive edges, and
-    the Tutte embedding, against the reference's own initial state."""
+    reference's cut_to_disk loop; for a mesh of three components each by its
+    own Euler characteristic), its boundary loops and cohesive edges, and the
+    Tutte embedding (the components' disks on the reference's grid), against
+    the reference's own initial state."""
     g = golden(case)
     st = I.init_uv(g["mesh_V"], g["mesh_F"])
     np.testing.assert_array_equal(st.F, g["F"])
