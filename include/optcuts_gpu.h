@@ -318,7 +318,22 @@ int oc_mesh_split_filter(oc_mesh* mesh, double* divGrad);
  * FP32 (about 8x faster local solves; energies, gradients, line search and
  * the local LDL^T stay FP64; energy changes then agree with the FP64
  * evaluation to ~1e-4 relative instead of ~1e-8). */
-enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2, OC_TOPO_AUTOTUNE = 8 };
+enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2, OC_TOPO_AUTOTUNE = 8, OC_TOPO_BIJECTIVE = 16 };
+/* OC_TOPO_BIJECTIVE: the bijective form, as the reference queries when its
+ * TriMesh has a scaffold (bijectivity on; TriMesh.cpp:2322-2372,
+ * 2406-2497, 2597-2756): each candidate's split copies are first moved
+ * apart along their inward normals, and its local solve carries an air
+ * mesh of the candidate's air loop -- the slit an interior split opens,
+ * the split vertex's air fan opened at a boundary split
+ * (Scaffold::get1RingAirLoop), the corner loop of a merge
+ * (Scaffold::getCornerAirLoop, merges that close a diamond excepted) --
+ * re-meshed from the current layout at every local Newton iteration (the
+ * mesher of oc_air_loop_mesh), weighted 0.01 / |F_air| with uniform
+ * weights.  Problems the reference abandons (air loops that share a vertex
+ * or self-intersect) report an energy decrease of -DBL_MAX.  The air loops
+ * come from the scaffold of the Optimizer last given this mesh
+ * (oc_optimizer_set_scaffold / _build_scaffold); OC_ERR_INVALID without
+ * one, and with the learned proposal or OC_TOPO_RECORD_FEATURES. */
 int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out);
 /* No counterpart in the reference: the learned proposal.  Every local
  * problem first gets one Newton step (its features: energies, gradient
@@ -398,6 +413,10 @@ int oc_topo_result_candidate(const oc_topo_result* r, int c, double* EwDec, doub
  * posRows (nCand); NULL arrays are skipped */
 int oc_topo_result_candidates(const oc_topo_result* r, double* EwDec, double* energyChanges, int* path,
                               double* newVertPos, int* posRows);
+/* bijective queries: local problems with an air loop, those abandoned,
+ * the most Steiner points one of their air meshes got, and the problems
+ * whose loop refinement stopped at the mesher's limits (0 expected) */
+int oc_topo_result_air(const oc_topo_result* r, int* problems, int* rejected, int* steinerMax, int* capped);
 int oc_topo_result_destroy(oc_topo_result* r);
 /* Optimizer::createFracture(EDecThres, 0, false, splitInterior)
  * (Optimizer.cpp:440-503) -> TriMesh::splitOrMerge (TriMesh.cpp:978-1052):
@@ -592,6 +611,18 @@ int oc_air_mesh_build(const double* UV, int nV, const int* F, int nF, double avg
 int oc_air_mesh_sizes(const oc_air_mesh* am, int* nAirV, int* nAirF, int* nBnd);
 int oc_air_mesh_get(const oc_air_mesh* am, double* airV, int* airF, int* bnd);
 int oc_air_mesh_destroy(oc_air_mesh* am);
+/* The local air loops of the bijective topology solves (Triangle "qYQ" on
+ * the loop, Scaffold.cpp:150-170, as the local Scaffold constructor calls
+ * it): the region inside the simple polygon pts (nPts x 2, either
+ * orientation, 3 <= nPts <= 48) as its constrained Delaunay triangulation,
+ * refined towards a 20 degree minimum angle with at most maxSteiner
+ * (<= 12) interior Steiner points and none on the polygon.  Host-only; the
+ * same code runs inside the bijective local solves.  V (nV x 2: the
+ * polygon's points, then the Steiner points; room for nPts + 12 rows) and
+ * T (nT x 3, counter-clockwise; room for nPts + 22 rows); status: 0, or 8
+ * / 16 when refinement stopped at the Steiner / queue limit. */
+int oc_air_loop_mesh(const double* pts, int nPts, int maxSteiner, int* nV, double* V, int* nT, int* T,
+                     int* status);
 
 #ifdef __cplusplus
 }

@@ -121,6 +121,8 @@ _SIGS = {
     "oc_topo_result_info": [_vp, _i, _i, _i, _i, _i, _d, _d],
     "oc_topo_result_candidate": [_vp, ctypes.c_int, _d, _d, _i, _i, _d, _i],
     "oc_topo_result_destroy": [_vp],
+    "oc_topo_result_air": [_vp, _i, _i, _i, _i],
+    "oc_air_loop_mesh": [_vp, ctypes.c_int, ctypes.c_int, _i, _vp, _i, _vp, _i],
     "oc_topo_result_iterations": [_vp, _i, _i, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_create_fracture": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
     "oc_optimizer_apply_timing": [_vp, _d],
@@ -344,9 +346,9 @@ class TriMesh:
         self.ctx.check(lib().oc_mesh_split_filter(self.h, _pd(out)), "splitFilter")
         return out
 
-    def _query(self, op, lambda_t, filterExp, fp32, features=False, mlp=None, topFrac=0.1):
+    def _query(self, op, lambda_t, filterExp, fp32, features=False, mlp=None, topFrac=0.1, bijective=False):
         h = _vp()
-        opt = (1 if fp32 else 0) | (2 if features else 0)
+        opt = (1 if fp32 else 0) | (2 if features else 0) | (16 if bijective else 0)
         t0 = time.perf_counter()
         if mlp is not None:
             self.ctx.check(lib().oc_topology_query_learned(self.h, op, float(lambda_t), float(filterExp), opt, mlp.h,
@@ -358,15 +360,17 @@ class TriMesh:
         return self._result(h, features, mlp, query_ms)
 
     def topologyStep(self, lambda_t, filterExp=0.6, fp32=False, features=False, mlp=None, topFrac=0.1,
-                     autotune=False):
+                     autotune=False, bijective=False):
         """The three queries of one topology step on the current state —
         boundary split, merge, interior split — built together and solved in
         the same launches (each result equals its own query's); with mlp the
         learned proposal (top fraction topFrac of each operation's problems
         solved exactly).  Returns (split, merge, interior); query_ms of each is
-        the whole step's library time."""
+        the whole step's library time.  bijective: the reference's form with
+        its scaffold on (the air loops of the scaffold last given to an
+        Optimizer of this mesh)."""
         hs = [_vp(), _vp(), _vp()]
-        opt = (1 if fp32 else 0) | (2 if features else 0) | (8 if autotune else 0)
+        opt = (1 if fp32 else 0) | (2 if features else 0) | (8 if autotune else 0) | (16 if bijective else 0)
         t0 = time.perf_counter()
         self.ctx.check(lib().oc_topology_step(self.h, float(lambda_t), float(filterExp), opt,
                                               mlp.h if mlp is not None else None, float(topFrac),
@@ -430,6 +434,8 @@ class TriMesh:
                                               pp.ctypes.data_as(_vp))
                 lib().oc_topo_result_problem_stats(h, ctypes.byref(npb), *(pstat[k].ctypes.data_as(_vp) for k in
                                                    ("nTri", "nFree", "iters", "trials", "cycles")))
+            ap, ar, asx, acap = (ctypes.c_int() for _ in range(4))
+            lib().oc_topo_result_air(h, ctypes.byref(ap), ctypes.byref(ar), ctypes.byref(asx), ctypes.byref(acap))
             nc = n.value
             ew, ec = np.zeros(nc), np.zeros((nc, 2))
             paths, pos, rows = np.zeros((nc, 3), np.int32), np.zeros((nc, 8)), np.zeros(nc, np.int32)
@@ -449,17 +455,19 @@ class TriMesh:
                 "solve_ms": sms.value, "local_iters_total": tot.value, "local_capped": cap.value,
                 "local_trials_total": tri.value, "selected": nsel.value, "probe_ms": pms.value,
                 "exact_ms": ems.value, "features": X, "target": tgt, "predicted": prd,
-                "problems": dict(cand=pc, EwDec=pe, EwDec_pred=pp, **pstat), "query_ms": query_ms}
+                "problems": dict(cand=pc, EwDec=pe, EwDec_pred=pp, **pstat), "query_ms": query_ms,
+                "air": {"problems": ap.value, "rejected": ar.value, "steiner_max": asx.value, "capped": acap.value}}
 
     def querySplit(self, lambda_t, splitInterior=False, filterExp=0.6, fp32=False, features=False, mlp=None,
-                   topFrac=0.1):
+                   topFrac=0.1, bijective=False):
         """TriMesh::querySplit(lambda_t, false, splitInterior) with every local
-        solve batched on the GPU (bijectivity off); fp32 projects the local
+        solve batched on the GPU (bijective: with the local air loops of the
+        scaffold last given to an Optimizer of this mesh); fp32 projects the local
         element Hessians in FP32; features records each local problem's
         features and exact target; mlp selects the learned proposal (only the
         top fraction topFrac of the problems is solved exactly)."""
         return self._query(OP_INTERIOR_SPLIT if splitInterior else OP_BOUNDARY_SPLIT, lambda_t, filterExp, fp32,
-                           features, mlp, topFrac)
+                           features, mlp, topFrac, bijective)
 
     def applyTopology(self, op, path, newVertPos):
         """splitEdgeOnBoundary / cutPath / mergeBoundaryEdges on this mesh."""
@@ -484,9 +492,9 @@ class TriMesh:
         lib().oc_mesh_get_topology(self.h, None, None, None, _pi(F), _pd(Vr), _pi(C))
         self.nV, self.nF, self.F, self.V_rest, self.cohE = nv.value, nf.value, F, Vr, C
 
-    def queryMerge(self, lambda_t, fp32=False, features=False, mlp=None, topFrac=0.1):
-        """TriMesh::queryMerge(lambda_t, false) (bijectivity off)."""
-        return self._query(OP_MERGE, lambda_t, 0.6, fp32, features, mlp, topFrac)
+    def queryMerge(self, lambda_t, fp32=False, features=False, mlp=None, topFrac=0.1, bijective=False):
+        """TriMesh::queryMerge(lambda_t, false)."""
+        return self._query(OP_MERGE, lambda_t, 0.6, fp32, features, mlp, topFrac, bijective)
 
     def close(self):
         if getattr(self, "h", None):
@@ -716,6 +724,23 @@ def chol_analyze_stats(nV, F, fixedVert=(0,), leafSize=16, xy=None):
     if rc != OC_OK:
         raise OCError(rc, "oc_chol_analyze_stats")
     return symbolic_stats_dict(out)
+
+
+def air_loop_mesh(pts, maxSteiner=12):
+    """The bijective local solves' loop mesher on the host (oc_air_loop_mesh:
+    Triangle's "qYQ" on a simple polygon): returns (V, T, status) -- the
+    polygon's points then the Steiner points, counter-clockwise triangles,
+    and the mesher's status bits (8 / 16: refinement stopped at a limit)."""
+    p = _f8(pts).reshape(-1, 2)
+    n = len(p)
+    V = np.zeros((n + 12, 2))
+    T = np.zeros((n + 22, 3), np.int32)
+    nV, nT, st = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    rc = lib().oc_air_loop_mesh(p.ctypes.data_as(_vp), n, int(maxSteiner), ctypes.byref(nV), V.ctypes.data_as(_vp),
+                                ctypes.byref(nT), T.ctypes.data_as(_vp), ctypes.byref(st))
+    if rc != OC_OK:
+        raise OCError(rc, "air_loop_mesh: not a simple polygon of 3..48 points")
+    return V[:nV.value], T[:nT.value], st.value
 
 
 def topology_schedules():

@@ -35,10 +35,12 @@ UNITS = {
     "oc_mlp.cu": [],
     "oc_tc.cu": [],
     "oc_local.cu": [],
+    "oc_local_bij.cu": [],
     "oc_outer.cpp": ["-Xcompiler", "-fvisibility=default"],
     "oc_output.cpp": ["-Xcompiler", "-fvisibility=default"],
 }
-HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h", "oc_elem.cuh"]
+HEADERS = ["oc_internal.h", "oc_chol.h", "oc_airmesh.h", "oc_topo.h", "oc_mlp.h", "oc_tc.h", "oc_elem.cuh",
+           "oc_loopmesh.cuh"]
 
 
 def _newest_input():

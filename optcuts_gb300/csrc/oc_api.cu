@@ -29,8 +29,13 @@ struct oc_ctx {
     std::string err;
 };
 
+struct oc_optimizer;
+
 struct oc_mesh {
     oc_ctx* ctx = nullptr;
+    // the Optimizer whose scaffold is this mesh's (TriMesh::scaffold): the
+    // air mesh the bijective topology queries take their local loops from
+    oc_optimizer* scafOwner = nullptr;
     unsigned long long topoVersion = 0;   // advanced whenever F changes
     oc::DeviceMesh d;
     oc::Scratch scratch;
@@ -907,7 +912,7 @@ static int topology_query(oc_mesh* m, int opType, double lambda_t, double filter
 int oc_topology_query(oc_mesh* m, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out)
 {
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune | oc::kTopoBijective);
     return topology_query(m, opType, lambda_t, filterExp, opts, out);
 }
 
@@ -916,7 +921,7 @@ int oc_topology_query_learned(oc_mesh* m, int opType, double lambda_t, double fi
 {
     if (!mlp || mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
+    opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune | oc::kTopoBijective)) | oc::kTopoLearned;
     opts.mlp = &mlp->m;
     opts.topFrac = topFrac;
     return topology_query(m, opType, lambda_t, filterExp, opts, out);
@@ -975,6 +980,29 @@ static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_
     in.mergeFork = mergeFork;
     in.shardRank = shardRank;
     in.shardCount = shardCount;
+    // bijective form: the scaffold's air mesh as it stands (air-only
+    // vertices where the last step moved them)
+    std::vector<double> airV;
+    std::vector<int> airF, airBnd;
+    if (opts.flags & oc::kTopoBijective) {
+        oc_optimizer* o = m->scafOwner;
+        if (!o) return fail(m->ctx, OC_ERR_INVALID, "bijective topology query: the mesh has no scaffold");
+        int nAirV = 0, nAirF = 0, nBnd = 0;
+        int rc = oc_optimizer_get_scaffold(o, &nAirV, &nAirF, &nBnd, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+        airV.resize(2 * (size_t)nAirV);
+        airF.resize(3 * (size_t)nAirF);
+        airBnd.resize(nBnd);
+        rc = oc_optimizer_get_scaffold(o, nullptr, nullptr, nullptr, airV.data(), airF.data(), airBnd.data());
+        if (rc) return rc;
+        in.bijective = true;
+        in.airV = airV.data();
+        in.airF = airF.data();
+        in.airBnd = airBnd.data();
+        in.nAirV = nAirV;
+        in.nAirF = nAirF;
+        in.nAirBnd = nBnd;
+    }
     std::vector<oc::TopoOpResult> res(nOps);
     std::string err;
     const int rc = oc::topo_query_ops(in, ops, nOps, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, res.data(),
@@ -1012,9 +1040,9 @@ int oc_topology_step(oc_mesh* m, double lambda_t, double filterExp, int options,
     if (!split || !merge || !interior) return OC_ERR_INVALID;
     if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune | oc::kTopoBijective);
     if (mlp) {
-        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
+        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune | oc::kTopoBijective)) | oc::kTopoLearned;
         opts.mlp = &mlp->m;
         opts.topFrac = topFrac;
     }
@@ -1034,9 +1062,9 @@ int oc_topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_t, d
     if (!ops || !out || nOps <= 0 || nOps > 3) return OC_ERR_INVALID;
     if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune | oc::kTopoBijective);
     if (mlp) {
-        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
+        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune | oc::kTopoBijective)) | oc::kTopoLearned;
         opts.mlp = &mlp->m;
         opts.topFrac = topFrac;
     }
@@ -1050,9 +1078,9 @@ int oc_topology_queries_sharded(oc_mesh* m, const int* ops, int nOps, double lam
         return OC_ERR_INVALID;
     if (mlp && (mlp->m.in != oc::kTopoNumFeatures || !(topFrac > 0.0) || topFrac > 1.0)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune);
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoRecordFeatures | oc::kTopoAutotune | oc::kTopoBijective);
     if (mlp) {
-        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune)) | oc::kTopoLearned;
+        opts.flags = (options & (oc::kTopoFp32Hessian | oc::kTopoAutotune | oc::kTopoBijective)) | oc::kTopoLearned;
         opts.mlp = &mlp->m;
         opts.topFrac = topFrac;
     }
@@ -1066,7 +1094,7 @@ int oc_topology_query_tail(oc_mesh* m, int opType, double lambda_t, int options,
     // ends of the last interior split), merges of the pair forking there
     if (!m || !out || (opType != oc::kOpBoundarySplit && opType != oc::kOpMerge)) return OC_ERR_INVALID;
     oc::TopoOptions opts;
-    opts.flags = options & oc::kTopoFp32Hessian;
+    opts.flags = options & (oc::kTopoFp32Hessian | oc::kTopoBijective);
     if (opType == oc::kOpMerge) return topology_queries(m, &opType, 1, lambda_t, 0.6, opts, out, nullptr, 0, m->tails[0]);
     int verts[2] = {-1, -1};
     int n = 0;
@@ -1316,6 +1344,16 @@ int oc_cut_to_disk(const int* F, int nF, int* cutVerts, int capVerts, int* cutOf
         o += static_cast<int>(cuts[i].size());
         cutOff[i + 1] = o;
     }
+    return OC_OK;
+}
+
+int oc_topo_result_air(const oc_topo_result* r, int* problems, int* rejected, int* steinerMax, int* capped)
+{
+    if (!r) return OC_ERR_INVALID;
+    if (problems) *problems = r->stats.airProblems;
+    if (rejected) *rejected = r->stats.airRejected;
+    if (steinerMax) *steinerMax = r->stats.airSteinerMax;
+    if (capped) *capped = r->stats.airCapped;
     return OC_OK;
 }
 
@@ -1607,6 +1645,7 @@ int oc_optimizer_create(oc_mesh* mesh, double energyParam, const oc_optimizer_co
 int oc_optimizer_destroy(oc_optimizer* o)
 {
     if (!o) return OC_ERR_INVALID;
+    if (o->mesh && o->mesh->scafOwner == o) o->mesh->scafOwner = nullptr;
     cudaFree(o->g); cudaFree(o->dir); cudaFree(o->uv0);
     cudaFree(o->wuv); cudaFree(o->airCorner); cudaFree(o->airHb);
     o->air.uv = nullptr;
@@ -2218,6 +2257,7 @@ int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, co
     o->nBnd = nBnd;
     o->airScale = o->wScaf / nAirF;   // w_scaf / airMesh.F.rows() (Optimizer.cpp:776)
     o->scaf = true;
+    m->scafOwner = o;   // result.scaffold = &scaffold
     if (!samePattern) o->patternStale = true;
     else if (cliqueMode) {
         // the kept pattern's padding may now cover slots the previous air mesh
@@ -2351,6 +2391,7 @@ int oc_optimizer_clear_scaffold(oc_optimizer* o)
     if (!o) return OC_ERR_INVALID;
     if (o->scaf) o->patternStale = true;
     o->scaf = false;
+    if (o->mesh && o->mesh->scafOwner == o) o->mesh->scafOwner = nullptr;
     o->eScaf = 0.0;
     o->nWhole = o->nWholeReal = o->mesh->d.nV;
     return OC_OK;

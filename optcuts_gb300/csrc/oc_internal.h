@@ -105,6 +105,11 @@ struct LocalProblem {
     int nFree, maxIter;
     double localArea;      // the local mesh's surfaceArea (local triangle order)
     double targetGRes;     // (nVert - nFixed) / nVert * 1e-6
+    // bijective form: the local air loop, points [airOff, airOff + nAir) of
+    // LocalBatch::apLocal / apPos (nAir 0: no air mesh); its degenerate-air
+    // area clamp areaThres_AM (Scaffold.cpp:34, 150, 189)
+    int airOff, nAir;
+    double airThres;
 };
 constexpr int kLocalRaw = 16;       // raw per-problem quantities for the learned proposal
 struct LocalResult {
@@ -118,6 +123,8 @@ struct LocalResult {
     // |g_s|^2, g_0.g_1, triangles touching the slot, their energy
     double raw[kLocalRaw];
     long long cycles;             // SM clock cycles the problem's solve took
+    int airStatus;                // bijective: loop-mesher status bits seen (0: every mesh as asked)
+    int airSteiner;               // bijective: most Steiner points in one of its air meshes
 };
 struct LocalBatch {
     const LocalProblem* prob = nullptr;
@@ -129,6 +136,10 @@ struct LocalBatch {
     const int* initTri = nullptr;
     LocalResult* out = nullptr;
     int fp32Hessian = 0;               // project element Hessians in FP32
+    // bijective form: per air-loop point, the local vertex it is (>= 0) or
+    // -1 for a fixed air point at apPos
+    const int* apLocal = nullptr;
+    const double2* apPos = nullptr;
 };
 
 struct PcgWork {
@@ -178,6 +189,9 @@ LocalSchedule local_schedule(int maxTri, int count, int numSMs, int maxCluster);
 int local_max_cluster();
 cudaError_t launch_local_newton(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, LocalSchedule sc,
                                 cudaStream_t st);
+// the bijective form (problems with an air loop): one warp per problem, the
+// loop re-meshed at the start of every local Newton iteration
+cudaError_t launch_local_newton_bij(const DeviceMesh& m, double surfaceArea, const LocalBatch& b, cudaStream_t st);
 // SymDirichletEnergy::computeDivGradPerVert (standard-deviation filter) into divGrad (nV)
 void launch_divgrad(const DeviceMesh& m, double2* cornerBuf, double* divGrad, cudaStream_t st);
 

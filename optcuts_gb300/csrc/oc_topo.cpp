@@ -12,6 +12,7 @@
 
 #include "oc_topo.h"
 #include "oc_mlp.h"
+#include "oc_loopmesh.cuh"
 
 #include <algorithm>
 #include <array>
@@ -191,6 +192,8 @@ struct Batch {
     std::vector<LocalProblem> prob;
     std::vector<int> ltGlobal, ltCorner, lvSlot, initTri;
     std::vector<double2> lvPos;
+    std::vector<int> apLocal;       // bijective: air-loop points (local vertex or -1)
+    std::vector<double2> apPos;     // and their positions when fixed
     struct Tag {
         int cand;          // candidate index
         int a = -1, b = -1, c = -1;   // path entries
@@ -270,6 +273,344 @@ void emit(Batch& B, const Topo& T, const double* rest, const double* UV, const s
     }
     B.prob.push_back(P);
     B.tag.push_back(tag);
+}
+
+// ---------------------------------------------------------------------
+// Bijective form: the local air loops (Scaffold::get1RingAirLoop /
+// getCornerAirLoop, Scaffold.cpp:339-520) and the separation of the split
+// copies (TriMesh::computeLocalEdDec_inSplit / _bSplit, TriMesh.cpp:2326-2372,
+// 2597-2660) that the local Scaffold's air loop needs.
+
+double2 d2(double x, double y) { return make_double2(x, y); }
+
+// SymDirichletEnergy::initStepSize per triangle (SymDirichletEnergy.cpp:
+// 555-609): the bound from det(U + alpha V) > 0, or stepSize when none
+double step_bound_host(double2 U1, double2 U2, double2 U3, double2 V1, double2 V2, double2 V3, double stepSize)
+{
+    const double U2m1x = U2.x - U1.x, U2m1y = U2.y - U1.y;
+    const double U3m1x = U3.x - U1.x, U3m1y = U3.y - U1.y;
+    const double V2m1x = V2.x - V1.x, V2m1y = V2.y - V1.y;
+    const double V3m1x = V3.x - V1.x, V3m1y = V3.y - V1.y;
+    const double a = V2m1x * V3m1y - V2m1y * V3m1x;
+    const double b = U2m1x * V3m1y - U2m1y * V3m1x + V2m1x * U3m1y - V2m1y * U3m1x;
+    const double c = U2m1x * U3m1y - U2m1y * U3m1x;
+    const double delta = b * b - 4.0 * a * c;
+    double bound = stepSize;
+    if (a > 0.0) {
+        if ((b < 0.0) && (delta >= 0.0)) bound = 2.0 * c / (-b + std::sqrt(delta));
+    }
+    else if (a < 0.0) {
+        if (b < 0.0) bound = 2.0 * c / (-b + std::sqrt(delta));
+        else bound = (-b - std::sqrt(delta)) / 2.0 / a;
+    }
+    else {
+        if (b < 0.0) bound = -c / b;
+    }
+    return bound < stepSize ? bound : stepSize;
+}
+
+// the whole-mesh air mesh with its adjacency
+struct AirSrc {
+    int nAirV = 0, nBnd = 0;
+    const double* V = nullptr;
+    const int* bnd = nullptr;
+    std::vector<int> F;
+    Topo T;
+    std::vector<int> meshToAir;
+    void build(const TopoQueryIn& in)
+    {
+        nAirV = in.nAirV;
+        nBnd = in.nAirBnd;
+        V = in.airV;
+        bnd = in.airBnd;
+        F.assign(in.airF, in.airF + 3 * (size_t)in.nAirF);
+        T.build(nAirV, F.data(), in.nAirF);
+        meshToAir.assign(in.nV, -1);
+        for (int i = 0; i < nBnd; ++i)
+            if (bnd[i] >= 0 && bnd[i] < in.nV) meshToAir[bnd[i]] = i;
+    }
+    double2 pos(int a) const { return d2(V[2 * (size_t)a], V[2 * (size_t)a + 1]); }
+    int mesh_of(int a) const { return a >= 0 && a < nBnd ? bnd[a] : -1; }
+};
+
+// Scaffold::get1RingAirLoop (Scaffold.cpp:339-388) for mesh vertex v: air
+// vertex ids, [1] = v, [2] and [0] the two ends of its air fan (the mesh
+// boundary neighbours), [3..] the fan's outer vertices from [2]'s side round
+// to [0]'s; false when v has no air fan
+bool ring_loop(const AirSrc& A, int v, std::vector<int>& rows)
+{
+    rows.clear();
+    const int a = v >= 0 && v < static_cast<int>(A.meshToAir.size()) ? A.meshToAir[v] : -1;
+    if (a < 0 || A.T.degree(a) == 0) return false;
+    const int nb0 = A.T.nb[A.T.nbPtr[a]];
+    std::vector<int> u0, u;
+    A.T.walk(a, nb0, false, u0);
+    A.T.walk(a, nb0, true, u);
+    std::reverse(u.begin(), u.end());
+    u.insert(u.end(), u0.begin(), u0.end());
+    if (u.empty()) return false;
+    rows.assign(u.size() + 2, -1);
+    rows[1] = a;
+    for (size_t ti = 0; ti < u.size(); ++ti) {
+        const int t = u[ti];
+        int k = 0;
+        while (k < 3 && A.F[3 * (size_t)t + k] != a) ++k;
+        if (k == 3) return false;
+        rows[ti + 2] = A.F[3 * (size_t)t + (k + 1) % 3];
+        if (ti + 1 == u.size()) rows[0] = A.F[3 * (size_t)t + (k + 2) % 3];
+    }
+    return A.mesh_of(rows[0]) >= 0 && A.mesh_of(rows[2]) >= 0;
+}
+
+// IglUtils::Test2DSegmentSegment with eps = 0 (IglUtils.cpp:647-705; after
+// Ericson, Real-Time Collision Detection)
+double signed_area2(double2 a, double2 b, double2 c) { return (a.x - c.x) * (b.y - c.y) - (a.y - c.y) * (b.x - c.x); }
+bool segments_intersect(double2 a, double2 b, double2 c, double2 d)
+{
+    const double a1 = signed_area2(a, b, d), a2 = signed_area2(a, b, c);
+    if (a1 * a2 <= 0.0) {
+        const double a3 = signed_area2(c, d, a), a4 = a3 + a2 - a1;
+        if (a3 * a4 <= 0.0) {
+            if (std::abs(a1) <= 0.0 && std::abs(a2) <= 0.0) {
+                const double abx = b.x - a.x, aby = b.y - a.y;
+                const double sq = abx * abx + aby * aby;
+                double cc = ((c.x - a.x) * abx + (c.y - a.y) * aby) / sq;
+                double cd = ((d.x - a.x) * abx + (d.y - a.y) * aby) / sq;
+                if (cc > cd) std::swap(cc, cd);
+                return !((cc > 1.0) || (cd < 0.0));
+            }
+            return true;
+        }
+    }
+    return false;
+}
+
+// IglUtils::computeRotAngle (IglUtils.cpp:637-641)
+double rot_angle(double2 from, double2 to)
+{
+    const double nf = std::sqrt(from.x * from.x + from.y * from.y), nt = std::sqrt(to.x * to.x + to.y * to.y);
+    const double angle = std::acos(std::max(-1.0, std::min(1.0, (from.x * to.x + from.y * to.y) / nf / nt)));
+    return (from.x * to.y - from.y * to.x < 0.0) ? -angle : angle;
+}
+
+// Scaffold::getCornerAirLoop (Scaffold.cpp:390-519) for the merge of corner
+// (p0, p1, p2): the air loop around the three corners' air fans with p1 and
+// p2 removed, started one before p0 (air ids in loop, positions in pts,
+// pts[1] = mergedPos); false when the reference abandons the query (the
+// loop self-intersects or turns clockwise) or the loop is not found
+bool corner_loop(const AirSrc& A, const int corner_mesh[3], double2 mergedPos, std::vector<int>& loop,
+                 std::vector<double2>& pts)
+{
+    int corner[3];
+    for (int i = 0; i < 3; ++i) {
+        corner[i] = A.meshToAir[corner_mesh[i]];
+        if (corner[i] < 0 || A.T.degree(corner[i]) == 0) return false;
+    }
+    std::vector<int> inc, tmp;
+    for (int i = 0; i < 3; ++i) {
+        const int nb0 = A.T.nb[A.T.nbPtr[corner[i]]];
+        A.T.walk(corner[i], nb0, false, tmp);
+        inc.insert(inc.end(), tmp.begin(), tmp.end());
+        A.T.walk(corner[i], nb0, true, tmp);
+        inc.insert(inc.end(), tmp.begin(), tmp.end());
+    }
+    std::sort(inc.begin(), inc.end());   // std::set order
+    inc.erase(std::unique(inc.begin(), inc.end()), inc.end());
+    if (inc.empty()) return false;
+    // igl::boundary_loop of the incident triangles: loops traced along the
+    // triangles' orientation from the smallest unvisited border vertex, the
+    // longest kept
+    const int nI = static_cast<int>(inc.size());
+    std::vector<int> verts;
+    for (int t : inc)
+        for (int k = 0; k < 3; ++k) verts.push_back(A.F[3 * (size_t)t + k]);
+    std::sort(verts.begin(), verts.end());
+    verts.erase(std::unique(verts.begin(), verts.end()), verts.end());
+    auto lid = [&](int a) { return static_cast<int>(std::lower_bound(verts.begin(), verts.end(), a) - verts.begin()); };
+    const int nVl = static_cast<int>(verts.size());
+    std::vector<int> Fl(3 * (size_t)nI);
+    for (int f = 0; f < nI; ++f)
+        for (int k = 0; k < 3; ++k) Fl[3 * f + k] = lid(A.F[3 * (size_t)inc[f] + k]);
+    std::vector<std::vector<int>> VF(nVl);
+    for (int f = 0; f < nI; ++f)
+        for (int k = 0; k < 3; ++k) VF[Fl[3 * f + k]].push_back(f);
+    auto has_edge = [&](int u, int v) {   // a triangle with u -> v
+        for (int f : VF[u])
+            for (int k = 0; k < 3; ++k)
+                if (Fl[3 * f + k] == u && Fl[3 * f + (k + 1) % 3] == v) return true;
+        return false;
+    };
+    std::vector<char> border(nVl, 0);
+    for (int f = 0; f < nI; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const int u = Fl[3 * f + k], v = Fl[3 * f + (k + 1) % 3];
+            if (!has_edge(v, u)) border[u] = border[v] = 1;
+        }
+    std::vector<char> unvisited(border);
+    std::vector<int> best;
+    for (int s0 = 0; s0 < nVl; ++s0) {
+        if (!unvisited[s0]) continue;
+        std::vector<int> l{s0};
+        unvisited[s0] = 0;
+        for (int guard = 0; guard <= nVl; ++guard) {
+            const int v = l.back();
+            int next = -1;
+            for (int f : VF[v]) {
+                int k = 0;
+                while (Fl[3 * f + k] != v) ++k;
+                const int vn = Fl[3 * f + (k + 1) % 3];
+                if (unvisited[vn] && !has_edge(vn, v)) {
+                    next = vn;
+                    break;
+                }
+            }
+            if (next < 0) break;
+            l.push_back(next);
+            unvisited[next] = 0;
+        }
+        if (l.size() > best.size()) best.swap(l);
+    }
+    std::vector<int> L;
+    for (int x : best) L.push_back(verts[x]);
+    const int n = static_cast<int>(L.size());
+    if (n < 5) return false;
+    int startI = -1;
+    for (int i = 0; i < n && startI < 0; ++i)
+        if (L[i] == corner[0]) {
+            if (L[(i - 1 + n) % n] == corner[1] && L[(i - 2 + n) % n] == corner[2]) startI = i;
+            else return false;
+        }
+    if (startI < 0) return false;
+    // remove corner[2] and corner[1]; start one before corner[0]
+    std::vector<int> rest;
+    for (int i = 0; i < n; ++i)
+        if (i != (startI - 1 + n) % n && i != (startI - 2 + n) % n) rest.push_back(L[i]);
+    const int m = n - 2;
+    int c0 = 0;
+    while (rest[c0] != corner[0]) ++c0;
+    loop.clear();
+    for (int i = 0; i < m; ++i) loop.push_back(rest[(c0 - 1 + m + i) % m]);
+    for (int i = 0; i < 3; ++i)
+        if (A.mesh_of(loop[i]) < 0) return false;
+    pts.resize(m);
+    for (int i = 0; i < m; ++i) pts[i] = A.pos(loop[i]);
+    pts[1] = mergedPos;
+    // loop edges (i, i + 1), (m - 1, 0): no two non-adjacent ones may meet
+    auto e0 = [&](int e) { return pts[e]; };
+    auto e1 = [&](int e) { return pts[(e + 1) % m]; };
+    for (int eJ = 2; eJ + 1 < m; ++eJ)
+        if (segments_intersect(e0(0), e1(0), e0(eJ), e1(eJ))) return false;
+    for (int eI = 1; eI + 2 < m; ++eI)
+        for (int eJ = eI + 2; eJ < m; ++eJ)
+            if (segments_intersect(e0(eI), e1(eI), e0(eJ), e1(eJ))) return false;
+    double rot = 0.0;
+    auto dir = [&](int e) { return d2(e1(e).x - e0(e).x, e1(e).y - e0(e).y); };
+    for (int e = 0; e + 1 < m; ++e) rot += rot_angle(dir(e), dir(e + 1));
+    rot += rot_angle(dir(m - 1), dir(0));
+    return rot > 0.0;
+}
+
+// TriMesh::compute2DInwardNormal (TriMesh.cpp:2085-2103) of local vertex v
+// of the local mesh LT at positions P
+double2 inward_normal(const Topo& LT, const std::vector<double2>& P, int v)
+{
+    if (LT.degree(v) == 0) return d2(0.0, 0.0);
+    const int nb = LT.nb[LT.nbPtr[v]];
+    // the fan's two ends: rotating from nb one way, then the other
+    int ends[2] = {-1, -1};
+    for (int side = 0; side < 2; ++side) {
+        const bool toBound = side == 1;
+        int f = toBound ? LT.edge_tri(nb, v) : LT.edge_tri(v, nb);
+        int vNew = nb;
+        for (int guard = 0; f >= 0 && guard <= LT.nF; ++guard) {
+            vNew = LT.third(f, v, vNew);
+            if (vNew == nb) return d2(0.0, 0.0);   // interior vertex
+            f = toBound ? LT.edge_tri(vNew, v) : LT.edge_tri(v, vNew);
+        }
+        ends[side] = vNew;
+    }
+    auto unit = [](double2 x) {
+        const double z = x.x * x.x + x.y * x.y;
+        if (z > 0.0) {
+            const double r = std::sqrt(z);
+            return d2(x.x / r, x.y / r);
+        }
+        return x;
+    };
+    const double2 b0 = unit(d2(P[ends[0]].x - P[v].x, P[ends[0]].y - P[v].y));
+    const double2 b1 = unit(d2(P[ends[1]].x - P[v].x, P[ends[1]].y - P[v].y));
+    double2 nrm = unit(d2(b0.x + b1.x, b0.y + b1.y));
+    if (b1.x * nrm.y - b1.y * nrm.x < 0.0) nrm = d2(-nrm.x, -nrm.y);
+    return nrm;
+}
+
+// moves the two copies va, vb apart along their inward normals, a tenth of
+// their injective step at a time, until their squared distance reaches
+// epsSep or stops growing (TriMesh.cpp:2344-2366)
+void separate_copies(const Topo& LT, std::vector<double2>& P, const std::vector<int>& corner, int va, int vb,
+                     double epsSep)
+{
+    double2 sv[2] = {P[va], P[vb]};
+    const double2 nrm[2] = {inward_normal(LT, P, va), inward_normal(LT, P, vb)};
+    auto sqdist = [](double2 a, double2 b) { return (a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y); };
+    double cur = sqdist(sv[0], sv[1]);
+    const int nT = static_cast<int>(corner.size() / 3);
+    for (int guard = 0; cur < epsSep && guard < 4096; ++guard) {
+        for (int i = 0; i < 2; ++i) {
+            const int v = i == 0 ? va : vb;
+            double step = 1.0;
+            for (int t = 0; t < nT; ++t) {
+                const int c[3] = {corner[3 * t], corner[3 * t + 1], corner[3 * t + 2]};
+                if (c[0] != v && c[1] != v && c[2] != v) continue;
+                double2 D[3];
+                for (int k = 0; k < 3; ++k) D[k] = c[k] == v ? nrm[i] : d2(0.0, 0.0);
+                step = step_bound_host(P[c[0]], P[c[1]], P[c[2]], D[0], D[1], D[2], step);
+            }
+            sv[i].x += 0.1 * step * nrm[i].x;
+            sv[i].y += 0.1 * step * nrm[i].y;
+        }
+        P[va] = sv[0];
+        P[vb] = sv[1];
+        const double last = cur;
+        cur = sqdist(sv[0], sv[1]);
+        if (std::abs(cur - last) / last < 1.0e-3) break;
+    }
+}
+
+// areaThres_AM of a local Scaffold: sqrt(3)/4 (avgEdgeLen / 2 / 10)^2 with
+// the local mesh's igl::avg_edge_length (every triangle's three edges)
+// (Scaffold.cpp:34, 150, 189)
+double local_air_thres(const double* Vrest, const int* F, const std::vector<int>& tris)
+{
+    double sum = 0.0;
+    long long cnt = 0;
+    for (int t : tris)
+        for (int j = 0; j < 3; ++j) {
+            const int a = F[3 * (size_t)t + j], b = F[3 * (size_t)t + (j + 1) % 3];
+            const double dx = Vrest[3 * (size_t)a] - Vrest[3 * (size_t)b];
+            const double dy = Vrest[3 * (size_t)a + 1] - Vrest[3 * (size_t)b + 1];
+            const double dz = Vrest[3 * (size_t)a + 2] - Vrest[3 * (size_t)b + 2];
+            sum += std::sqrt(dx * dx + dy * dy + dz * dz);
+            ++cnt;
+        }
+    const double eps = sum / static_cast<double>(cnt) * 0.5 * 0.1;
+    return std::sqrt(3.0) / 4.0 * eps * eps;
+}
+
+// attaches an air loop to the last emitted problem (nAir -1: the reference
+// abandons this problem, its energy decrease is -DBL_MAX)
+void emit_air(Batch& B, const std::vector<int>& local, const std::vector<double2>& pos, double thres, bool reject)
+{
+    LocalProblem& P = B.prob.back();
+    P.airOff = static_cast<int>(B.apLocal.size());
+    P.airThres = thres;
+    if (reject || local.size() > static_cast<size_t>(kLoopMaxPts) || local.size() < 3) {
+        P.nAir = -1;
+        return;
+    }
+    P.nAir = static_cast<int>(local.size());
+    B.apLocal.insert(B.apLocal.end(), local.begin(), local.end());
+    B.apPos.insert(B.apPos.end(), pos.begin(), pos.end());
 }
 
 // the split filter: vertices sorted by -divGrad in a std::map (equal keys
@@ -405,11 +746,15 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
     TopoWorkspace& W = in.ws ? *in.ws : tmp;
     // size classes, largest first so that the long poles start first, each
     // with the schedule its size and count call for
+    // (the bijective problems, those with an air loop, form a fifth class
+    // of their own kernel)
     constexpr int kClasses = 4;
-    auto classOf = [&](int nTri) { return nTri > 160 ? 0 : nTri > 40 ? 1 : nTri > 8 ? 2 : 3; };
-    int count[kClasses] = {}, maxTri[kClasses] = {};
+    auto classOfP = [&](const LocalProblem& P) {
+        return P.nAir != 0 ? kClasses : P.nTri > 160 ? 0 : P.nTri > 40 ? 1 : P.nTri > 8 ? 2 : 3;
+    };
+    int count[kClasses + 1] = {}, maxTri[kClasses + 1] = {};
     for (int k : which) {
-        const int c = classOf(B.prob[k].nTri);
+        const int c = classOfP(B.prob[k]);
         count[c]++;
         maxTri[c] = std::max(maxTri[c], B.prob[k].nTri);
     }
@@ -418,13 +763,13 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
     const int maxCluster = in.bigCluster > 0 ? in.bigCluster : local_max_cluster();
     LocalSchedule sched[kClasses];
     for (int c = 0; c < kClasses; ++c) sched[c] = local_schedule(maxTri[c], count[c], numSMs, maxCluster);
-    int start[kClasses + 1] = {};
-    for (int c = 0; c < kClasses; ++c) start[c + 1] = start[c] + count[c];
+    int start[kClasses + 2] = {};
+    for (int c = 0; c <= kClasses; ++c) start[c + 1] = start[c] + count[c];
     std::vector<int> order(which.size());   // position in the class-sorted batch -> index into which
     {
-        int fill[kClasses];
-        for (int c = 0; c < kClasses; ++c) fill[c] = start[c];
-        for (size_t i = 0; i < which.size(); ++i) order[fill[classOf(B.prob[which[i]].nTri)]++] = static_cast<int>(i);
+        int fill[kClasses + 1];
+        for (int c = 0; c <= kClasses; ++c) fill[c] = start[c];
+        for (size_t i = 0; i < which.size(); ++i) order[fill[classOfP(B.prob[which[i]])]++] = static_cast<int>(i);
     }
     std::vector<LocalProblem> prob(which.size());
     for (size_t p = 0; p < which.size(); ++p) {
@@ -433,18 +778,19 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
     }
     LocalBatch db;
     db.fp32Hessian = fp32;
-    const size_t sizes[7] = {sizeof(LocalProblem) * prob.size(), sizeof(int) * B.ltGlobal.size(),
+    const size_t sizes[9] = {sizeof(LocalProblem) * prob.size(), sizeof(int) * B.ltGlobal.size(),
                              sizeof(int) * B.ltCorner.size(), sizeof(double2) * B.lvPos.size(),
                              sizeof(int) * B.lvSlot.size(), sizeof(int) * B.initTri.size(),
-                             sizeof(LocalResult) * prob.size()};
-    const void* src[6] = {prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
-                          B.initTri.data()};
+                             sizeof(LocalResult) * prob.size(), sizeof(int) * B.apLocal.size(),
+                             sizeof(double2) * B.apPos.size()};
+    const void* src[9] = {prob.data(), B.ltGlobal.data(), B.ltCorner.data(), B.lvPos.data(), B.lvSlot.data(),
+                          B.initTri.data(), nullptr, B.apLocal.data(), B.apPos.data()};
     std::vector<LocalResult> out(prob.size());
     cudaError_t e = cudaSuccess;
     const bool reuse = batchId != 0 && W.uploaded == batchId;
-    for (int k = 0; k < 7 && e == cudaSuccess; ++k)
+    for (int k = 0; k < 9 && e == cudaSuccess; ++k)
         if (W.cap[k] < sizes[k] || !W.buf[k]) {
-            if (k >= 1 && k <= 5) W.uploaded = 0;
+            if ((k >= 1 && k <= 5) || k >= 7) W.uploaded = 0;
             cudaFree(W.buf[k]);
             W.buf[k] = nullptr;
             W.cap[k] = 0;
@@ -453,8 +799,9 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
             if (e == cudaSuccess) W.cap[k] = want;
         }
     const bool upload = !(reuse && W.uploaded == batchId);
-    for (int k = 0; k < 6 && e == cudaSuccess; ++k)
-        if (k == 0 || upload) e = cudaMemcpyAsync(W.buf[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
+    for (int k = 0; k < 9 && e == cudaSuccess; ++k)
+        if (k != 6 && sizes[k] > 0 && (k == 0 || upload))
+            e = cudaMemcpyAsync(W.buf[k], src[k], sizes[k], cudaMemcpyHostToDevice, in.st);
     if (e == cudaSuccess) W.uploaded = batchId;
     for (int c = 0; c <= kClasses && e == cudaSuccess; ++c)
         if (!W.ev[c]) e = cudaEventCreateWithFlags(&W.ev[c], cudaEventDisableTiming);
@@ -465,6 +812,23 @@ int solve_batch(const TopoQueryIn& in, const Batch& B, unsigned long long batchI
         db.lvPos = static_cast<const double2*>(W.buf[3]);
         db.lvSlot = static_cast<const int*>(W.buf[4]);
         db.initTri = static_cast<const int*>(W.buf[5]);
+        db.apLocal = static_cast<const int*>(W.buf[7]);
+        db.apPos = static_cast<const double2*>(W.buf[8]);
+        if (count[kClasses]) {
+            // the bijective problems: one launch of their own kernel on the
+            // fifth stream
+            if (!W.aux[kClasses]) e = cudaStreamCreateWithFlags(&W.aux[kClasses], cudaStreamNonBlocking);
+            if (e == cudaSuccess && !W.ev[kClasses + 1])
+                e = cudaEventCreateWithFlags(&W.ev[kClasses + 1], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(W.aux[kClasses], W.ev[kClasses], 0);
+            LocalBatch cb = db;
+            cb.prob = static_cast<const LocalProblem*>(W.buf[0]) + start[kClasses];
+            cb.out = static_cast<LocalResult*>(W.buf[6]) + start[kClasses];
+            cb.nProb = count[kClasses];
+            if (e == cudaSuccess) e = launch_local_newton_bij(*in.dm, in.surfaceArea, cb, W.aux[kClasses]);
+            if (e == cudaSuccess) e = cudaEventRecord(W.ev[kClasses + 1], W.aux[kClasses]);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(in.st, W.ev[kClasses + 1], 0);
+        }
         for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
             if (!count[c]) continue;
             if (!W.aux[c]) {
@@ -1124,12 +1488,16 @@ void append_batch(Batch& dst, const Batch& src)
 {
     const int triBase = static_cast<int>(dst.ltGlobal.size()), vertBase = static_cast<int>(dst.lvPos.size()),
               initBase = static_cast<int>(dst.initTri.size());
+    const int airBase = static_cast<int>(dst.apLocal.size());
     for (LocalProblem P : src.prob) {
         P.triOff += triBase;
         P.vertOff += vertBase;
         P.initOff += initBase;
+        P.airOff += airBase;
         dst.prob.push_back(P);
     }
+    dst.apLocal.insert(dst.apLocal.end(), src.apLocal.begin(), src.apLocal.end());
+    dst.apPos.insert(dst.apPos.end(), src.apPos.begin(), src.apPos.end());
     dst.ltGlobal.insert(dst.ltGlobal.end(), src.ltGlobal.begin(), src.ltGlobal.end());
     dst.ltCorner.insert(dst.ltCorner.end(), src.ltCorner.begin(), src.ltCorner.end());
     dst.lvPos.insert(dst.lvPos.end(), src.lvPos.begin(), src.lvPos.end());
@@ -1195,7 +1563,7 @@ namespace {
 // querySplit / queryMerge) appended to B; candidatePool as the reference
 // reports it.
 int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp, std::vector<TopoCandidate>& out,
-             int& candidatePool, Batch& B, std::string* err)
+             int& candidatePool, Batch& B, std::string* err, const AirSrc* air)
 {
     const double R = in.virtualRadius;
     std::vector<int> tris, tris1, tris2;
@@ -1331,6 +1699,72 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
                 tg.se = rest_dist(in.Vrest, vI, nbVI) / R * (1.0 + 1.0) / 2.0;   // seInc
                 tg.nRows = cutThrough ? 4 : 2;
                 emit(B, T, in.rest, in.UV, tris, L, extra, slot, nFree, nFixed, tg);
+                if (air) {
+                    // separate the copies, then the air loop: vb's air fan
+                    // opened at the split (TriMesh.cpp:2597-2756)
+                    const LocalProblem& P = B.prob.back();
+                    std::vector<double2> lp(B.lvPos.begin() + P.vertOff, B.lvPos.begin() + P.vertOff + P.nVert);
+                    Topo LT;
+                    LT.build(P.nVert, L.corner.data(), static_cast<int>(tris.size()));
+                    const double dx = in.UV[2 * (size_t)vi] - in.UV[2 * (size_t)vb];
+                    const double dy = in.UV[2 * (size_t)vi + 1] - in.UV[2 * (size_t)vb + 1];
+                    const double epsSep = (dx * dx + dy * dy) * 1.0e-4;
+                    separate_copies(LT, lp, L.corner, lb, nLoc, epsSep);
+                    if (cutThrough) separate_copies(LT, lp, L.corner, li, nLoc + 1, epsSep);
+                    for (int l = 0; l < P.nVert; ++l) B.lvPos[P.vertOff + l] = lp[l];
+                    std::vector<int> rb, ri, al;
+                    std::vector<double2> ap;
+                    bool reject = !ring_loop(*air, vb, rb);
+                    auto meshPt = [&](int airId) {
+                        const int l = L.find(air->mesh_of(airId));
+                        if (l < 0) reject = true;
+                        al.push_back(l);
+                        ap.push_back(l >= 0 ? lp[l] : d2(0.0, 0.0));
+                    };
+                    auto localPt = [&](int l) {
+                        al.push_back(l);
+                        ap.push_back(lp[l]);
+                    };
+                    auto airRing = [&](const std::vector<int>& rows) {
+                        for (size_t r = 3; r < rows.size(); ++r) {
+                            al.push_back(-1);
+                            ap.push_back(air->pos(rows[r]));
+                        }
+                    };
+                    if (!reject && !cutThrough) {
+                        meshPt(rb[0]);
+                        localPt(nLoc);
+                        localPt(li);
+                        localPt(lb);
+                        meshPt(rb[2]);
+                        airRing(rb);
+                    }
+                    else if (!reject) {
+                        reject = !ring_loop(*air, vi, ri);
+                        // loops sharing an air vertex are abandoned (TriMesh.cpp:2700-2706)
+                        if (!reject) {
+                            std::vector<int> x(rb), y(ri);
+                            std::sort(x.begin(), x.end());
+                            std::sort(y.begin(), y.end());
+                            std::vector<int> both;
+                            std::set_intersection(x.begin(), x.end(), y.begin(), y.end(), std::back_inserter(both));
+                            reject = !both.empty();
+                        }
+                        if (!reject) {
+                            meshPt(rb[0]);
+                            localPt(nLoc);
+                            localPt(li);
+                            meshPt(ri[2]);
+                            airRing(ri);
+                            meshPt(ri[0]);
+                            localPt(nLoc + 1);
+                            localPt(lb);
+                            meshPt(rb[2]);
+                            airRing(rb);
+                        }
+                    }
+                    emit_air(B, al, ap, local_air_thres(in.Vrest, in.F, tris), reject);
+                }
             });
         }
         else {
@@ -1397,6 +1831,23 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
                                 R / 2.0;   // seInc (TriMesh.cpp:2246-2247)
                         tg.nRows = 2;
                         emit(B, T, in.rest, in.UV, umbrella, Lc, extra, slot, 2, nLoc - 1, tg);
+                        if (air) {
+                            // separate the copies; the opened slit is the air
+                            // loop (p2, vI, p0, copy) (TriMesh.cpp:2322-2372)
+                            const LocalProblem& P = B.prob.back();
+                            std::vector<double2> lp(B.lvPos.begin() + P.vertOff,
+                                                    B.lvPos.begin() + P.vertOff + P.nVert);
+                            Topo LT;
+                            LT.build(P.nVert, Lc.corner.data(), n);
+                            const double dx = in.UV[2 * (size_t)vI] - in.UV[2 * (size_t)p0];
+                            const double dy = in.UV[2 * (size_t)vI + 1] - in.UV[2 * (size_t)p0 + 1];
+                            separate_copies(LT, lp, Lc.corner, lv, nLoc, (dx * dx + dy * dy) * 1.0e-4);
+                            for (int l = 0; l < P.nVert; ++l) B.lvPos[P.vertOff + l] = lp[l];
+                            const int l2 = L.find(p2), l0 = L.find(p0);
+                            const std::vector<int> al{l2, lv, l0, nLoc};
+                            const std::vector<double2> ap{lp[l2], lp[lv], lp[l0], lp[nLoc]};
+                            emit_air(B, al, ap, local_air_thres(in.Vrest, in.F, umbrella), l2 < 0 || l0 < 0);
+                        }
                     }
                 }
             });
@@ -1476,10 +1927,12 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
             const int p0 = fork ? ce[0] : ce[3], p1 = fork ? ce[1] : ce[2], p2 = fork ? ce[2] : ce[1];
             // seam decrease, closing a split diamond (TriMesh.cpp:2121-2135)
             double seDec = rest_dist(in.Vrest, p0, p1) / R * (1.0 + 1.0) / 2.0;
+            bool closeup = false;
             for (int p = T.nbPtr[p0]; p < T.nbPtr[p0 + 1]; ++p) {
                 const int nbv = T.nb[p];
                 if (nbv != p1 && T.bnd[nbv] && T.adjacent(p2, nbv)) {
                     seDec += rest_dist(in.Vrest, p0, nbv) / R * (1.0 + 1.0) / 2.0;
+                    closeup = true;
                     break;
                 }
             }
@@ -1507,6 +1960,26 @@ int build_op(const TopoQueryIn& in, const Topo& T, int opType, double filterExp,
             const size_t before = B.lvPos.size();
             emit(B, T, in.rest, in.UV, triangles, L, {}, slot, 1, static_cast<int>(L.gv.size()) - 1, tg);
             B.lvPos[before + lm] = make_double2(mp[0], mp[1]);   // initMergedPos
+            if (air && !closeup) {
+                // the corner loop with the merged vertex at initMergedPos
+                // (TriMesh.cpp:2406, 2480-2497); closing up a diamond needs none
+                std::vector<int> loop, al;
+                std::vector<double2> pts;
+                const int cm[3] = {p0, p1, p2};
+                bool reject = !corner_loop(*air, cm, make_double2(mp[0], mp[1]), loop, pts);
+                if (!reject)
+                    for (size_t i = 0; i < loop.size(); ++i) {
+                        int l = -1;
+                        if (i < 3) {
+                            const int g = air->mesh_of(loop[i]);
+                            l = g == p2 ? lm : L.find(g);
+                            if (l < 0) reject = true;
+                        }
+                        al.push_back(l);
+                        if (l >= 0) pts[i] = B.lvPos[before + l];
+                    }
+                emit_air(B, al, pts, local_air_thres(in.Vrest, in.F, triangles), reject);
+            }
         }
         candidatePool = in.nCohE;
     }
@@ -1547,6 +2020,12 @@ void finish_op(int opType, double lambda_t, const Batch& B, size_t p0, size_t p1
         const LocalResult& r = res[k];
         const Batch::Tag& tg = B.tag[k];
         TopoCandidate& C = out[tg.cand];
+        if (B.prob[k].nAir != 0) {
+            stats.airProblems++;
+            if (B.prob[k].nAir < 0) stats.airRejected++;
+            stats.airSteinerMax = std::max(stats.airSteinerMax, r.airSteiner);
+            if (r.airStatus & (kLoopSteinerCap | kLoopQueueCap)) stats.airCapped++;
+        }
         stats.maxIters = std::max(stats.maxIters, r.iters);
         stats.totalIters += r.iters;
         if (r.status != 1) stats.nonConverged++;
@@ -1604,6 +2083,20 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
         if (err) *err = "topology query: adjacency of another mesh";
         return OC_ERR_INVALID;
     }
+    // bijective form: the whole-mesh air mesh the local loops come from
+    std::unique_ptr<AirSrc> airSrc;
+    if (in.bijective) {
+        if (!in.airV || !in.airF || !in.airBnd || in.nAirF <= 0 || in.nAirBnd <= 0 || in.nAirV < in.nAirBnd) {
+            if (err) *err = "topology query: the bijective form needs the scaffold's air mesh";
+            return OC_ERR_INVALID;
+        }
+        if ((opts.flags & kTopoLearned) || (opts.flags & kTopoRecordFeatures)) {
+            if (err) *err = "topology query: the learned proposal's features are defined without air loops";
+            return OC_ERR_INVALID;
+        }
+        airSrc = std::make_unique<AirSrc>();
+        airSrc->build(in);
+    }
     // every operation's problems in one batch, op i owning [start[i], start[i + 1])
     Batch B;
     std::vector<size_t> start(nOps + 1, 0);
@@ -1611,7 +2104,8 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
     for (int i = 0; i < nOps; ++i) {
         const auto t0 = clk::now();
         Batch Bi;
-        const int rc = build_op(in, T, ops[i], filterExp, results[i].cands, results[i].pool, Bi, err);
+        const int rc = build_op(in, T, ops[i], filterExp, results[i].cands, results[i].pool, Bi, err,
+                                airSrc.get());
         if (rc) return rc;
         append_batch(B, Bi);
         start[i + 1] = B.prob.size();

@@ -30,10 +30,10 @@ std::shared_ptr<TopoAdjacency> topo_adjacency(int nV, const int* F, int nF);
 // device buffers, streams and events of the batched local solves, kept
 // across queries (one per mesh; not for concurrent queries)
 struct TopoWorkspace {
-    void* buf[7] = {};
-    size_t cap[7] = {};
-    cudaStream_t aux[4] = {};
-    cudaEvent_t ev[5] = {};
+    void* buf[9] = {};
+    size_t cap[9] = {};
+    cudaStream_t aux[5] = {};
+    cudaEvent_t ev[6] = {};
     unsigned long long uploaded = 0;    // batch whose problem arrays buf[1..5] hold
     unsigned long long nextBatch = 1;
     std::shared_ptr<void> host;         // per-thread scratch of the host problem assembly
@@ -70,17 +70,28 @@ struct TopoQueryIn {
     // and energyChanges (DBL_MAX, DBL_MAX) (the list itself is the same on
     // every shard)
     int shardRank = 0, shardCount = 1;
+    // bijective form (TriMesh::scaffold set): the whole-mesh air mesh the
+    // local air loops come from (Scaffold::get1RingAirLoop /
+    // getCornerAirLoop, Scaffold.cpp:339-520): nAirV x 2 positions (rows <
+    // nAirBnd are the mesh vertices airBnd[i]), nAirF x 3 triangles
+    // (counter-clockwise)
+    bool bijective = false;
+    const double* airV = nullptr;
+    const int* airF = nullptr;
+    const int* airBnd = nullptr;
+    int nAirV = 0, nAirF = 0, nAirBnd = 0;
 };
 
 struct TopoStats {
     int nCandidates = 0, nProblems = 0, maxIters = 0, totalIters = 0, nonConverged = 0, nSelected = 0;
     long long totalTrials = 0;
+    int airProblems = 0, airRejected = 0, airSteinerMax = 0, airCapped = 0;   // bijective form
     double buildMs = 0.0, solveMs = 0.0, probeMs = 0.0, exactMs = 0.0;
 };
 
 struct Mlp;
 constexpr int kTopoNumFeatures = 32;
-enum { kTopoFp32Hessian = 1, kTopoRecordFeatures = 2, kTopoLearned = 4, kTopoAutotune = 8 };
+enum { kTopoFp32Hessian = 1, kTopoRecordFeatures = 2, kTopoLearned = 4, kTopoAutotune = 8, kTopoBijective = 16 };
 // the autotuner's table: one row per (device, size class, count bucket,
 // triangle bucket): the schedule it measured fastest and its milliseconds,
 // next to the fixed rule's

@@ -28,6 +28,8 @@
 //        topo      after the Newton loop, run the topology queries the
 //                  outer loop makes (TriMesh::querySplit boundary and
 //                  interior, queryMerge) and dump their candidate lists
+//                  (with bijectivity on, also the scaffold's air mesh the
+//                  local air loops come from)
 //        scafdump  dump, per iteration, the air mesh the iteration used
 //                  (vertices, triangles, boundary map, fixed air vertices)
 //                  and the augmented gradient / direction of iteration 0
@@ -401,6 +403,13 @@ int main(int argc, char** argv)
         Eigen::VectorXd dg;
         SD.computeDivGradPerVert(R, dg);
         npy_vec(out + "topo_divGrad.npy", dg);
+        if (R.scaffold) {
+            // bijectivity on: the air mesh the local air loops come from
+            const OptCuts::Scaffold& sc = *R.scaffold;
+            npy_mat(out + "topo_airV.npy", sc.airMesh.V);
+            npy_mati(out + "topo_airF.npy", sc.airMesh.F);
+            npy_veci(out + "topo_airBnd.npy", std::vector<int>(sc.bnd.data(), sc.bnd.data() + sc.bnd.size()));
+        }
         const double lambda_t = 1.0 - energyParams[0];
         auto dump = [&](const std::string& tag, const std::vector<std::vector<int>>& paths,
                         const std::vector<Eigen::MatrixXd>& poses, const std::vector<std::pair<double, double>>& ec) {
@@ -465,6 +474,18 @@ int main(int argc, char** argv)
             Rb.updateFeatures();
             dumpState("afterB", Rb);
             Rb.computeFeatures();   // as the next outer iteration sees it
+            // with bijectivity on, the air mesh of the new state
+            // (Optimizer::createFracture rebuilds the scaffold after every
+            // operation, Optimizer.cpp:425-430)
+            OptCuts::Scaffold scB;
+            if (Rb.scaffold) {
+                scB = OptCuts::Scaffold(Rb);
+                Rb.scaffold = &scB;
+                npy_mat(out + "topo_afterB_airV.npy", scB.airMesh.V);
+                npy_mati(out + "topo_afterB_airF.npy", scB.airMesh.F);
+                npy_veci(out + "topo_afterB_airBnd.npy",
+                         std::vector<int>(scB.bnd.data(), scB.bnd.data() + scB.bnd.size()));
+            }
             double bm;
             std::vector<int> pathM;
             Eigen::MatrixXd posM;

@@ -23,9 +23,14 @@ packs its dumps into one compressed .npz per case:
     scaf_fixed, scaf_off               iteration used (concatenated; scaf_off
                                        rows = nAirV, nAirF, nBnd, nFixed)
     gradw0                             augmented gradient of iteration 0
+    topo_airV, topo_airF, topo_airBnd  bijective topology cases: the
+                                       scaffold's air mesh of the state
+
+and air_loops.npz: local air loops Triangle meshed during bijective topology
+queries (recorded by oracle/_ref/ref_driver_trilog) with Triangle's output.
 
 Usage (needs the reference source tree; not part of the test run):
-    make -C oracle/ref && python tests/golden/make_golden.py
+    make -C oracle/ref all trilog && python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -66,6 +71,12 @@ CASES = {
     "sheet_3k_topo": ("sheet_3k", 0.999, 60, 16, False, ["nobij", "topo"]),
     "torus_768_topo": ("torus_768", 0.999, 60, 16, False, ["nobij", "topo"]),
     "ellipsoid_2k_topo": ("ellipsoid_2k", 0.999, 300, 16, False, ["nobij", "topo"]),
+    # the same with bijectivity on: the scaffold's air mesh of that state is
+    # kept (the local air loops come from it); the sphere after its
+    # one-point cut with the scaffold forced on
+    "icosphere_320_bij_topo": ("icosphere_320", 0.999, 60, 16, False, ["scaf", "topo"]),
+    "sheet_3k_bij_topo": ("sheet_3k", 0.999, 60, 16, False, ["topo"]),
+    "torus_768_bij_topo": ("torus_768", 0.999, 60, 16, False, ["topo"]),
     # three components (sphere, torus, sheet): each cut by its own Euler
     # characteristic, their UV disks on a grid; the scaffold holds them apart
     "components": ("components", 0.999, 30, 16, False, ["scafdump"]),
@@ -160,6 +171,9 @@ def run_case(name, key, lam, iters, hmax, states, flags):
             for k in ("opB_path", "opB_pos", "opI_path", "opI_pos", "opM_path", "opM_pos", "mergeB_best"):
                 if os.path.exists(out + "topo_%s.npy" % k):
                     pack["topo_" + k] = ld("topo_" + k)
+            for k in ("airV", "airF", "airBnd", "afterB_airV", "afterB_airF", "afterB_airBnd"):
+                if os.path.exists(out + "topo_%s.npy" % k):
+                    pack["topo_" + k] = ld("topo_" + k)
             for st in ("afterB", "afterI", "afterM"):
                 for k in ("V", "F", "Vrest", "cohE"):
                     if os.path.exists(out + "topo_%s_%s.npy" % (st, k)):
@@ -171,10 +185,78 @@ def run_case(name, key, lam, iters, hmax, states, flags):
     return pack
 
 
+TRILOG = os.path.join(ROOT, "oracle", "_ref", "ref_driver_trilog")
+# local air loops Triangle meshed during bijective topology queries
+# (oracle/ref/trilog.c records them): mesh key, Newton iterations, flags
+AIR_LOOP_RUNS = [("sheet_3k", 60, ["topo"]), ("torus_768", 60, ["topo"]), ("icosphere_320", 60, ["scaf", "topo"])]
+
+
+def read_trilog(path):
+    """Records of oracle/ref/trilog.c: (points in, segments, points out, triangles)."""
+    b = open(path, "rb").read()
+    o, recs = 0, []
+    while o < len(b):
+        nIn, nSeg, nOut, nTri = np.frombuffer(b, "<i4", 4, o)
+        o += 16
+        pin = np.frombuffer(b, "<f8", 2 * nIn, o).reshape(-1, 2); o += 16 * nIn
+        seg = np.frombuffer(b, "<i4", 2 * nSeg, o).reshape(-1, 2); o += 8 * nSeg
+        pout = np.frombuffer(b, "<f8", 2 * nOut, o).reshape(-1, 2); o += 16 * nOut
+        tri = np.frombuffer(b, "<i4", 3 * nTri, o).reshape(-1, 3); o += 12 * nTri
+        recs.append((pin, seg, pout, tri))
+    return recs
+
+
+def air_loops(per_size=40, steiner_max=400):
+    """tests/golden/air_loops.npz: loops in ring order (the segments
+    followed from point 0), Triangle's triangles in ring numbering and its
+    Steiner points; every loop Triangle refined (up to steiner_max) and the
+    first per_size loops of each size it did not."""
+    keep, seen = [], {}
+    for key, iters, flags in AIR_LOOP_RUNS:
+        V, F = meshes.CONFIGS[key]()
+        with tempfile.TemporaryDirectory() as td:
+            obj = os.path.join(td, "mesh.obj")
+            meshes.write_obj(obj, V, F)
+            out = os.path.join(td, "out") + "/"
+            os.makedirs(out)
+            log = os.path.join(td, "tri.bin")
+            subprocess.run([TRILOG, obj, out, "0.999", str(iters), "nodump"] + flags, check=True,
+                           stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                           env=dict(os.environ, OC_REF_THREADS="1", TRI_LOG=log))
+            recs = read_trilog(log)
+        for pin, seg, pout, tri in recs:
+            L = len(pin)
+            steiner = len(pout) - L
+            if steiner > 0:
+                if sum(1 for k in keep if k[3] > 0) >= steiner_max:
+                    continue
+            else:
+                if seen.get(L, 0) >= per_size:
+                    continue
+                seen[L] = seen.get(L, 0) + 1
+            nxt = {int(a): int(b) for a, b in seg}
+            ring = [0]
+            while len(ring) < L:
+                ring.append(nxt[ring[-1]])
+            inv = {old: new for new, old in enumerate(ring)}
+            inv.update({L + i: L + i for i in range(steiner)})
+            keep.append((pin[ring], np.array([[inv[int(v)] for v in t] for t in tri], np.int32), pout[L:], steiner))
+    pack = dict(loop_off=np.cumsum([0] + [len(k[0]) for k in keep]), loop_pts=np.concatenate([k[0] for k in keep]),
+                tri_off=np.cumsum([0] + [len(k[1]) for k in keep]), tri=np.concatenate([k[1] for k in keep]),
+                steiner_off=np.cumsum([0] + [len(k[2]) for k in keep]),
+                steiner=np.concatenate([k[2] for k in keep]).reshape(-1, 2))
+    np.savez_compressed(os.path.join(HERE, "air_loops.npz"), **pack)
+    print("air_loops: %d loops, %d refined" % (len(keep), sum(1 for k in keep if k[3] > 0)))
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle/ref")
     only = set(sys.argv[1:])
+    if not only or "air_loops" in only:
+        if not os.path.exists(TRILOG):
+            sys.exit("build the recording driver first: make -C oracle/ref trilog")
+        air_loops()
     for name, (key, lam, iters, hmax, states, flags) in CASES.items():
         if only and name not in only:
             continue
