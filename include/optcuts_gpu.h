@@ -332,7 +332,7 @@ enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2, OC_TOPO_AUTOTUNE =
  * weights.  Problems the reference abandons (air loops that share a vertex
  * or self-intersect) report an energy decrease of -DBL_MAX.  The air loops
  * come from the scaffold of the Optimizer last given this mesh
- * (oc_optimizer_set_scaffold / _build_scaffold); OC_ERR_INVALID without
+ * (oc_optimizer_set_scaffold / _rebuild_scaffold); OC_ERR_INVALID without
  * one, and with the learned proposal or OC_TOPO_RECORD_FEATURES. */
 int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out);
 /* No counterpart in the reference: the learned proposal.  Every local
@@ -511,7 +511,13 @@ int oc_optimizer_set_state(oc_optimizer* opt, int nV, const double* Vrest, const
 typedef struct oc_optcuts oc_optcuts;
 typedef struct {
     double upperBound;   /* b_d (4.1; values <= 4 become 4.1, main.cpp:1266-1269) */
-    int bijective;       /* 0: bijectivity off (the only form built) */
+    int bijective;       /* 1: bijectivity on (main.cpp's bijectiveParam): the
+                            optimizer's scaffold (started after the first inner
+                            loop when the optimizer has none, main.cpp:991-994)
+                            rebuilt after every Newton step and operation, the
+                            topology queries in their bijective form
+                            (OC_TOPO_BIJECTIVE), no exact final solve; not with
+                            mlp or recordFeatures */
     int topoLineSearch;  /* 1: fracture propagation after each operation */
     double filterExp;    /* filterExp_in, the interior-split filter (0.6) */
     int topoOptions;     /* OC_TOPO_FP32_HESSIAN */

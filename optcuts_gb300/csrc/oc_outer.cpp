@@ -182,9 +182,21 @@ struct oc_optcuts {
     }
     // EwDec_max of a query and its best candidate (querySplit returns 0 when
     // no vertex passes its filter, TriMesh.cpp:601-604, 618-621)
+    // the Optimizer's scaffolding is on (Optimizer::isScaffolding); the
+    // reference's TriMesh then has a scaffold and its queries are bijective
+    bool scafOn() const { return oc_optimizer_get_scaffold(opt, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr) == OC_OK; }
     int queryOptions() const
     {
-        return cfg.topoOptions | (cfg.recordFeatures && !cfg.mlp ? OC_TOPO_RECORD_FEATURES : 0);
+        return cfg.topoOptions | (cfg.recordFeatures && !cfg.mlp ? OC_TOPO_RECORD_FEATURES : 0) |
+               (cfg.bijective && scafOn() ? OC_TOPO_BIJECTIVE : 0);
+    }
+    // `scaffold = Scaffold(result, ...)` after a step (Optimizer.cpp:241-257)
+    void rebuildScaffold()
+    {
+        if (!scafOn()) return;
+        const auto t0 = std::chrono::steady_clock::now();
+        keep(oc_optimizer_rebuild_scaffold(opt));
+        ms[0] += ms_since(t0);
     }
     void keepFeatures(const oc_topo_result* r)
     {
@@ -278,7 +290,10 @@ struct oc_optcuts {
             const int op = propType == 1 ? kBSplit : kMerge;
             isMerge = propType == 2;
             oc_topo_result* r = nullptr;
-            if (!keep(oc_topology_query_tail(mesh, op, lt, cfg.topoOptions, &r))) return false;
+            if (!keep(oc_topology_query_tail(mesh, op, lt,
+                                             cfg.topoOptions | (cfg.bijective && scafOn() ? OC_TOPO_BIJECTIVE : 0),
+                                             &r)))
+                return false;
             best = bestOf(r, false, &pick);
             pickOp = op;
             oc_topo_result_destroy(r);
@@ -318,6 +333,7 @@ struct oc_optcuts {
             double eDec = 0.0;
             keep(oc_optimizer_last_edec(opt, &eDec));
             if (!createFracture(eDec, propagate, true)) {
+                rebuildScaffold();   // (an applied operation rebuilt it already)
                 if (lastPropagate) {
                     lastPropagate = false;
                     return 2;
@@ -326,6 +342,9 @@ struct oc_optcuts {
             else {
                 lastPropagate = true;
             }
+        }
+        else {
+            rebuildScaffold();
         }
         return 0;
     }
@@ -506,6 +525,13 @@ struct oc_optcuts {
             converged = 0;
             return;
         }
+        // bijectivity on after a one-point initial cut: the scaffold starts
+        // now (main.cpp:991-994); its energy enters at the next solve
+        if (cfg.bijective && !scafOn()) {
+            const auto t0 = std::chrono::steady_clock::now();
+            keep(oc_optimizer_rebuild_scaffold(opt));
+            ms[0] += ms_since(t0);
+        }
         record(0);
         if (!stationary(false)) {
             finish();
@@ -572,9 +598,9 @@ int oc_optcuts_create(oc_optimizer* opt, oc_mesh* mesh, const oc_optcuts_config*
     if (cfg) c = *cfg;
     // b_d <= 4 is replaced by 4.1 (main.cpp:1266-1269)
     if (!(c.upperBound > 4.0)) c.upperBound = 4.1;
-    // the bijective form needs the local solves' air meshes, which these
-    // queries do not build
-    if (c.bijective) return OC_ERR_INVALID;
+    // the learned proposal's features are defined on the bijectivity-off
+    // local solves
+    if (c.bijective && (c.mlp || c.recordFeatures)) return OC_ERR_INVALID;
     if (!(c.filterExp > 0.0) || c.filterExp > 1.0 || c.maxNewtonIters <= 0) return OC_ERR_INVALID;
     oc_optcuts* o = new (std::nothrow) oc_optcuts;
     if (!o) return OC_ERR_NOMEM;

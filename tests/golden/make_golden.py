@@ -93,6 +93,11 @@ CASES = {
     "icosphere_320_outer": ("icosphere_320", 0.999, 5000, 16, False, ["outer", "nobij"]),
     "icosphere_1k_outer": ("icosphere_1k", 0.999, 5000, 16, False, ["outer", "nobij"]),
     "icosphere_5k_outer": ("icosphere_5k", 0.999, 5000, 16, False, ["outer", "nobij"]),
+    # the same with bijectivity on (the reference's default: the scaffold
+    # starts after the first inner loop, bijective topology queries)
+    "icosphere_320_bij_outer": ("icosphere_320", 0.999, 5000, 16, False, ["outer"]),
+    "icosphere_1k_bij_outer": ("icosphere_1k", 0.999, 5000, 16, False, ["outer"]),
+    "icosphere_5k_bij_outer": ("icosphere_5k", 0.999, 5000, 16, False, ["outer"]),
 }
 OUTER_KEYS = ("outer_events", "outer_final", "outer_V", "outer_F", "outer_Vrest", "outer_cohE")
 SLIM_KEYS = ("scalars", "trace_E", "trace_Etot", "trace_gsq", "trace_alpha", "trace_status", "scaf_V", "scaf_F",

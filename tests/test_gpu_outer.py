@@ -107,3 +107,54 @@ def test_outer_loop_writes_reference_outputs(golden, tmp_path):
     np.testing.assert_allclose(v, g["mesh_V"], rtol=1e-6, atol=1e-6)   # rest positions in the input numbering
     first = [int(x.split("/")[0]) - 1 for x in f[0].split()[1:]]
     assert first == g["mesh_F"][0].tolist()
+
+
+BIJ_CASES = ["icosphere_320_bij_outer", "icosphere_1k_bij_outer"]
+
+
+def boundary_self_intersections(UV, F):
+    """Pairs of non-adjacent boundary edges of the UV layout that cross (0
+    for a bijective map)."""
+    from collections import Counter
+    cnt = Counter()
+    for a, b, c in F:
+        for u, v in ((a, b), (b, c), (c, a)):
+            cnt[(int(u), int(v))] += 1
+    bnd = [(u, v) for (u, v) in cnt if (v, u) not in cnt]
+    P = np.asarray(UV)
+
+    def cross(o, a, b):
+        return (a[0] - o[0]) * (b[1] - o[1]) - (a[1] - o[1]) * (b[0] - o[0])
+
+    n = 0
+    for i in range(len(bnd)):
+        a, b = P[bnd[i][0]], P[bnd[i][1]]
+        for j in range(i + 1, len(bnd)):
+            if set(bnd[i]) & set(bnd[j]):
+                continue
+            c, d = P[bnd[j][0]], P[bnd[j][1]]
+            if cross(a, b, c) * cross(a, b, d) < 0 and cross(c, d, a) * cross(c, d, b) < 0:
+                n += 1
+    return n
+
+
+@pytest.mark.parametrize("case", BIJ_CASES)
+def test_outer_loop_bijective_matches_reference(golden, case):
+    """Bijectivity on (the reference's default): the scaffold starts after
+    the first inner loop, every topology query is bijective, no exact final
+    solve.  The whole-mesh air meshes come from this project's generator,
+    not Triangle, so the trajectories separate at rounding level over the
+    run; the end state must still agree within 1%, stay within the bound,
+    and the final UV layout must not overlap itself."""
+    g = golden(case)
+    m, opt, o, finished = run_outer(g, bijective=True)
+    ref = g["outer_final"]
+    st = o.state()
+    assert finished and ref[5] == 1
+    assert m.checkInversion()
+    assert st["E_SD"] <= 4.1 + 1e-12
+    for k, i in (("E_SD", 0), ("E_se", 1), ("lambda", 2)):
+        assert abs(st[k] - ref[i]) <= 1e-2 * abs(ref[i]), (k, st[k], ref[i])
+    assert boundary_self_intersections(m.V, m.F) == 0
+    ev, rev = o.events(), g["outer_events"]
+    assert abs(ev[0, 1] - rev[0, 1]) <= 1e-3 * rev[0, 1]
