@@ -419,6 +419,21 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
             secs += s_
         topo["cpu_baseline"] = {"value": secs, "unit": "s", "cores": threads, "kind": "port",
                                 "sample": "the same three queries on the same state"}
+    # the same step in its bijective form (the scaffold's air mesh of this
+    # state, every local solve with its air loop re-meshed each iteration)
+    opt.rebuildScaffold()
+    queries(bijective=True)   # warm-up
+    t_bij, qs_bij = timed_step(bijective=True)
+    opt.clearScaffold()
+    air = [q["air"] for q in qs_bij]
+    topo["bijective"] = {"metric": "topology-step s (exhaustive, bijectivity on)", "value": t_bij, "unit": "s",
+                         "higher_is_better": False, **summary(qs_bij),
+                         "air_loops": {"problems": sum(a["problems"] for a in air),
+                                       "abandoned": sum(a["rejected"] for a in air),
+                                       "steiner_max": max(a["steiner_max"] for a in air),
+                                       "refinement_capped": sum(a["capped"] for a in air)},
+                         "local_iterations": sum(q["local_iters_total"] for q in qs_bij),
+                         "max_local_iterations": max(q["max_local_iters"] for q in qs_bij)}
     # applying the chosen operation (Optimizer::createFracture: mesh edit,
     # device mesh, Newton pattern and analysis, energy), timed once
     cands = [(q["EwDec_max"], op, q) for op, q in ((oc.OP_BOUNDARY_SPLIT, qb), (oc.OP_MERGE, qm)) if q["best"] >= 0]
@@ -436,12 +451,15 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
     return topo
 
 
-def outer_config0(oc, ctx):
-    """The whole OptCuts run (outer loop, bijectivity off, b_d = 4.1) on the
-    5,120-triangle icosphere from its Tutte start, against the reference's
-    own run of the same input (tests/golden/icosphere_5k_outer.npz, made by
-    the reference's sources on one x86-64 host thread)."""
-    path = os.path.join(ROOT, "tests", "golden", "icosphere_5k_outer.npz")
+def outer_config0(oc, ctx, bijective=True):
+    """The whole OptCuts run (outer loop, b_d = 4.1) on the 5,120-triangle
+    icosphere from its Tutte start, with bijectivity on (the reference's
+    default, its command line's bijectiveParam 1: scaffold from the first
+    topology step on, bijective local solves) or off, against the
+    reference's own run of the same input (tests/golden/icosphere_5k_*outer.npz,
+    made by the reference's sources on one x86-64 host thread)."""
+    name = "icosphere_5k_bij_outer" if bijective else "icosphere_5k_outer"
+    path = os.path.join(ROOT, "tests", "golden", name + ".npz")
     if not os.path.exists(path):
         return None
     with np.load(path) as z:
@@ -452,13 +470,14 @@ def outer_config0(oc, ctx):
     ctx.synchronize()
     t0 = time.perf_counter()
     opt.precompute()
-    o = oc.OptCuts(opt, upperBound=4.1)
+    o = oc.OptCuts(opt, upperBound=4.1, bijective=bijective)
     finished = o.run()
     ctx.synchronize()
     secs = time.perf_counter() - t0
     st = o.state()
     ref = g["outer_final"]
-    out = {"metric": "time to converge s (whole OptCuts run, bijectivity off, b_d 4.1)", "value": secs, "unit": "s",
+    form = "bijectivity on" if bijective else "bijectivity off"
+    out = {"metric": "time to converge s (whole OptCuts run, %s, b_d 4.1)" % form, "value": secs, "unit": "s",
            "higher_is_better": False, "workload": "icosphere_5k (5,120 triangles)", "finished": bool(finished),
            "newton_iterations": int(st["newton_iterations"]), "topology_steps": int(st["topology_steps"]),
            "E_SD": st["E_SD"], "E_se": st["E_se"], "lambda": st["lambda"],
@@ -575,7 +594,8 @@ def run_ours(args, rank, world):
 
     if rank != 0:
         return
-    outer0 = None if args.no_topology else outer_config0(oc, ctx)
+    outer0 = None if args.no_topology else outer_config0(oc, ctx, bijective=True)
+    outer0_off = None if args.no_topology else outer_config0(oc, ctx, bijective=False)
     # dominant phase: the multifrontal factorisation, FP64-FMA bound; the
     # algorithmic flops are the dense partial-Cholesky counts of its fronts
     ph_mean = {k: statistics.mean(p[k] for p in phases) for k in phases[0]}
@@ -619,7 +639,7 @@ def run_ours(args, rank, world):
                    "precision": "fp64 throughout (energy, gradient, Hessian eigen-clamp, LDL^T)"},
         "roofline": roofline, "roofline_solve": roofline_solve, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clocks, "energy_after": energy_after, "first_step": first,
-        "topology": topo, "outer_loop": outer0,
+        "topology": topo, "outer_loop": outer0, "outer_loop_bijectivity_off": outer0_off,
     }
     print(json.dumps(out), flush=True)
 
