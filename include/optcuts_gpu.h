@@ -333,7 +333,10 @@ enum { OC_TOPO_FP32_HESSIAN = 1, OC_TOPO_RECORD_FEATURES = 2, OC_TOPO_AUTOTUNE =
  * or self-intersect) report an energy decrease of -DBL_MAX.  The air loops
  * come from the scaffold of the Optimizer last given this mesh
  * (oc_optimizer_set_scaffold / _rebuild_scaffold); OC_ERR_INVALID without
- * one, and with the learned proposal or OC_TOPO_RECORD_FEATURES. */
+ * one.  With the learned proposal, the probe is the bijective solve's own
+ * first iteration (features of the local mesh alone, as without air
+ * loops); a network for bijective queries is trained on pairs that
+ * bijective queries recorded. */
 int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_topo_result** out);
 /* No counterpart in the reference: the learned proposal.  Every local
  * problem first gets one Newton step (its features: energies, gradient
@@ -516,8 +519,7 @@ typedef struct {
                             loop when the optimizer has none, main.cpp:991-994)
                             rebuilt after every Newton step and operation, the
                             topology queries in their bijective form
-                            (OC_TOPO_BIJECTIVE), no exact final solve; not with
-                            mlp or recordFeatures */
+                            (OC_TOPO_BIJECTIVE), no exact final solve */
     int topoLineSearch;  /* 1: fracture propagation after each operation */
     double filterExp;    /* filterExp_in, the interior-split filter (0.6) */
     int topoOptions;     /* OC_TOPO_FP32_HESSIAN */

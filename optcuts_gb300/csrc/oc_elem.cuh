@@ -185,6 +185,95 @@ __device__ void jacobi_eig4(T A[4][4], T V[4][4], T tol)
     }
 }
 
+// Eigen-decomposition of a symmetric 4x4 to FP64 accuracy with few FP64
+// instructions (GB300's FP64 pipe charges a warp instruction in full
+// whatever its active lanes): cyclic Jacobi in FP32 for a starting basis,
+// that basis made orthonormal in FP64 (modified Gram-Schmidt), K rotated
+// into it, then FP64 cyclic Jacobi sweeps on the nearly diagonal result
+// (quadratic convergence: one or two sweeps), each rotation updating only
+// the entries it changes (the 2x2 pivot block in closed form and the two
+// affected rows).  On return A's diagonal holds the eigenvalues and V the
+// eigenvectors as columns.
+__device__ void eig4_mixed(double A[4][4], double V[4][4])
+{
+    float Af[4][4], Vf[4][4];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) Af[i][j] = static_cast<float>(A[i][j]);
+    jacobi_eig4<float>(Af, Vf, 1e-14f);
+    double Q[4][4];
+    for (int c = 0; c < 4; ++c) {
+        double v[4];
+        for (int r = 0; r < 4; ++r) v[r] = static_cast<double>(Vf[r][c]);
+        for (int p = 0; p < c; ++p) {
+            double d = 0.0;
+            for (int r = 0; r < 4; ++r) d = d + Q[r][p] * v[r];
+            for (int r = 0; r < 4; ++r) v[r] = v[r] - d * Q[r][p];
+        }
+        double n2 = 0.0;
+        for (int r = 0; r < 4; ++r) n2 = n2 + v[r] * v[r];
+        const double inv = recip_sqrt(n2);
+        for (int r = 0; r < 4; ++r) Q[r][c] = v[r] * inv;
+    }
+    // B = Q^T A Q (symmetrised), then Jacobi on B with V = Q
+    double T[4][4];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            double acc = 0.0;
+            for (int k = 0; k < 4; ++k) acc = acc + A[r][k] * Q[k][c];
+            T[r][c] = acc;
+        }
+    for (int r = 0; r < 4; ++r)
+        for (int c = r; c < 4; ++c) {
+            double acc = 0.0;
+            for (int k = 0; k < 4; ++k) acc = acc + Q[k][r] * T[k][c];
+            A[r][c] = acc;
+        }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < r; ++c) A[r][c] = A[c][r];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) V[i][j] = Q[i][j];
+    double fro = 0.0;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) fro = fro + A[i][j] * A[i][j];
+    double prevOff = 0.0;
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) off = off + A[p][q] * A[p][q];
+        // off-diagonal below 1e-15 of the matrix (eigenvalues then exact to
+        // the rounding of their own size), or no longer decreasing
+        if (off <= 1e-30 * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) {
+                const double apq = A[p][q];
+                if (apq == 0.0) continue;
+                const double delta = (A[q][q] - A[p][p]) * 0.5;
+                const double t = (delta >= 0.0 ? apq : -apq) / (fabs(delta) + sqrt(delta * delta + apq * apq));
+                const double c = recip_sqrt(t * t + 1.0), sn = t * c;
+                // the pivot block in closed form: a_pp - t a_pq, a_qq + t a_pq, 0
+                A[p][p] = A[p][p] - t * apq;
+                A[q][q] = A[q][q] + t * apq;
+                A[p][q] = 0.0;
+                A[q][p] = 0.0;
+                for (int k = 0; k < 4; ++k) {
+                    if (k == p || k == q) continue;
+                    const double akp = A[k][p], akq = A[k][q];
+                    const double np = c * akp - sn * akq, nq = sn * akp + c * akq;
+                    A[k][p] = np;
+                    A[p][k] = np;
+                    A[k][q] = nq;
+                    A[q][k] = nq;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+}
+
 // makePD of a triangle's 6x6 Hessian for the local topology solves, in the
 // 4-dimensional complement of the two rigid translations (H t = 0 for them,
 // so H = Q K Q^T with K = Q^T H Q): Q = B (x) I2, B the orthonormal 3x2 basis
@@ -244,7 +333,8 @@ __device__ void project_psd_reduced(double H[6][6])
     T A[4][4], V[4][4];
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) A[i][j] = static_cast<T>(K[i][j] / scale);
-    jacobi_eig4<T>(A, V, sizeof(T) == 8 ? T(1e-34) : T(1e-14));
+    if constexpr (sizeof(T) == 8) eig4_mixed(A, V);
+    else jacobi_eig4<T>(A, V, T(1e-14));
     double lam[4];
     for (int m = 0; m < 4; ++m) lam[m] = A[m][m] < T(0) ? 0.0 : static_cast<double>(A[m][m]) * scale;
     double W[6][4];   // Q V

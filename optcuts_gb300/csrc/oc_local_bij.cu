@@ -53,8 +53,13 @@ namespace {
 // line search run over the local triangles and the air triangles
 // (Optimizer.cpp:575-652, 764-843); lastEDec counts the local mesh's
 // energy change only (:630-633); the result is the local mesh's energy
-// alone (computeEnergyVal(..., excludeScaffold = true)).  One warp per
-// problem; lane 0 runs the loop mesher and the LDL^T.
+// alone (computeEnergyVal(..., excludeScaffold = true)).
+//
+// One warp per problem.  GB300's FP64 pipe takes a warp instruction whole
+// whatever its active lanes, so the local and air triangles go through
+// every per-triangle step together (one lane each: one pass of the element
+// Hessians instead of two), and the LDL^T spreads each elimination step
+// over the lanes; lane 0 runs the loop mesher and the fixed-order sums.
 constexpr int kBijFree = kLocalMaxFree + kLoopMaxSteiner;   // free vertices: local slots, then Steiner points
 constexpr int kBijDof = 2 * kBijFree;
 constexpr int kBijProbs = 2;                                // problems (warps) per block
@@ -66,9 +71,10 @@ struct BijShared {
     double2 apFix[kLoopMaxV];       // position of a fixed air vertex
     double2 pos[kBijFree], pos0[kBijFree];
     double dir[kBijDof], g[kBijDof];
+    int perm[kBijDof];
     double H[kBijDof][kBijDof];
-    double bc;
-    double triE[32];
+    double bc[2];
+    double triE[32], triA[32];
     double triG[32][6];
     double triH[32][21];
     int triSlot[32][3];
@@ -94,47 +100,109 @@ __device__ __forceinline__ int bsym21(int i, int j)
 
 __device__ __forceinline__ double warp_bcast(BijShared& S, double v)
 {
-    if ((threadIdx.x & 31) == 0) S.bc = v;
+    if ((threadIdx.x & 31) == 0) S.bc[0] = v;
     __syncwarp();
-    v = S.bc;
+    v = S.bc[0];
     __syncwarp();
     return v;
 }
 
-// corners of local triangle t at pos (or pos0 + alpha dir)
-__device__ __forceinline__ void mesh_corners(const LocalBatch& b, const LocalProblem& P, const BijShared& S, int t,
-                                             bool withDir, double alpha, double2 U[3], int slot[3])
+// triangle t of the combined list: the local triangles, then the air
+// triangles; corners at pos (or pos0 + alpha dir), free slots, rest
+// constants and weight (air: w_scaf / |F_air| for gradient and Hessian)
+struct TriView {
+    double2 U[3];
+    int slot[3];
+    double A2, e0, e1, e01, e0d, e1d, e01d, w;
+    bool air;
+};
+
+__device__ __forceinline__ double2 at_slot(const BijShared& S, int sl, bool withDir, double alpha)
 {
-    for (int k = 0; k < 3; ++k) {
-        const int lv = b.ltCorner[3 * (P.triOff + t) + k];
-        const int sl = b.lvSlot[P.vertOff + lv];
-        slot[k] = sl;
-        if (sl >= 0)
-            U[k] = withDir ? make_double2(S.pos0[sl].x + alpha * S.dir[2 * sl], S.pos0[sl].y + alpha * S.dir[2 * sl + 1])
-                           : S.pos[sl];
-        else
-            U[k] = b.lvPos[P.vertOff + lv];
+    return withDir ? make_double2(S.pos0[sl].x + alpha * S.dir[2 * sl], S.pos0[sl].y + alpha * S.dir[2 * sl + 1])
+                   : S.pos[sl];
+}
+
+__device__ __forceinline__ void tri_view(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P,
+                                         const BijShared& S, int t, bool withDir, double alpha, TriView& v)
+{
+    if (t < P.nTri) {
+        for (int k = 0; k < 3; ++k) {
+            const int lv = b.ltCorner[3 * (P.triOff + t) + k];
+            const int sl = b.lvSlot[P.vertOff + lv];
+            v.slot[k] = sl;
+            v.U[k] = sl >= 0 ? at_slot(S, sl, withDir, alpha) : b.lvPos[P.vertOff + lv];
+        }
+        const int g = b.ltGlobal[P.triOff + t];
+        v.A2 = m.A2[g];
+        v.e0 = m.e0[g];
+        v.e1 = m.e1[g];
+        v.e01 = m.e01[g];
+        v.e0d = m.e0d[g];
+        v.e1d = m.e1d[g];
+        v.e01d = m.e01d[g];
+        v.w = m.area[g] / P.localArea;
+        v.air = false;
+    }
+    else {
+        const int a = t - P.nTri;
+        for (int k = 0; k < 3; ++k) {
+            const int q = S.M.T[a][k];
+            const int sl = S.apSlot[q];
+            v.slot[k] = sl;
+            v.U[k] = sl >= 0 ? at_slot(S, sl, withDir, alpha) : S.apFix[q];
+        }
+        const double* r = S.air[a];
+        v.A2 = r[0];
+        v.e0 = r[1];
+        v.e1 = r[2];
+        v.e01 = r[3];
+        v.e0d = r[4];
+        v.e1d = r[5];
+        v.e01d = r[6];
+        v.w = S.wAir;
+        v.air = true;
     }
 }
 
-__device__ __forceinline__ void air_corners(const BijShared& S, int t, bool withDir, double alpha, double2 U[3],
-                                            int slot[3])
+// the local mesh's energy (weights triArea / localArea) and the air
+// energy (w_scaf / |F_air| times the uniform-weight sum, Optimizer.cpp:
+// 774-777), each summed in triangle order, in one pass
+__device__ void bij_energies(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P, BijShared& S,
+                             bool withDir, double alpha, double& eMesh, double& eAir)
 {
-    for (int k = 0; k < 3; ++k) {
-        const int a = S.M.T[t][k];
-        const int sl = S.apSlot[a];
-        slot[k] = sl;
-        if (sl >= 0)
-            U[k] = withDir ? make_double2(S.pos0[sl].x + alpha * S.dir[2 * sl], S.pos0[sl].y + alpha * S.dir[2 * sl + 1])
-                           : S.pos[sl];
-        else
-            U[k] = S.apFix[a];
+    const int lane = threadIdx.x & 31;
+    const int nAll = P.nTri + S.nAirT;
+    double am = 0.0, aa = 0.0;
+    for (int c0 = 0; c0 < nAll; c0 += 32) {
+        const int t = c0 + lane;
+        double e = 0.0;
+        if (t < nAll) {
+            TriView v;
+            tri_view(m, b, P, S, t, withDir, alpha, v);
+            e = sd_energy(v.U[0], v.U[1], v.U[2], v.A2, v.e0, v.e1, v.e01, v.air ? 1.0 : v.w);
+        }
+        S.triE[lane] = e;
+        __syncwarp();
+        if (lane == 0) {
+            const int n = min(32, nAll - c0);
+            for (int k = 0; k < n; ++k) {
+                if (c0 + k < P.nTri) am = am + S.triE[k];
+                else aa = aa + S.triE[k];
+            }
+            S.bc[0] = am;
+            S.bc[1] = aa * S.wAir;
+        }
+        __syncwarp();
     }
+    if (nAll == 0 && lane == 0) S.bc[0] = S.bc[1] = 0.0;
+    __syncwarp();
+    eMesh = S.bc[0];
+    eAir = S.bc[1];
+    __syncwarp();
 }
 
-// local mesh energy (weights triArea / localArea), triangle order
-__device__ double bij_mesh_energy(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P, BijShared& S,
-                                  bool withDir, double alpha)
+__device__ double bij_mesh_energy(const DeviceMesh& m, const LocalBatch& b, const LocalProblem& P, BijShared& S)
 {
     const int lane = threadIdx.x & 31;
     double acc = 0.0;
@@ -142,11 +210,9 @@ __device__ double bij_mesh_energy(const DeviceMesh& m, const LocalBatch& b, cons
         const int t = c0 + lane;
         double e = 0.0;
         if (t < P.nTri) {
-            double2 U[3];
-            int sl[3];
-            mesh_corners(b, P, S, t, withDir, alpha, U, sl);
-            const int g = b.ltGlobal[P.triOff + t];
-            e = elem_energy(m, g, m.area[g] / P.localArea, U[0], U[1], U[2]);
+            TriView v;
+            tri_view(m, b, P, S, t, false, 0.0, v);
+            e = sd_energy(v.U[0], v.U[1], v.U[2], v.A2, v.e0, v.e1, v.e01, v.w);
         }
         S.triE[lane] = e;
         __syncwarp();
@@ -157,31 +223,6 @@ __device__ double bij_mesh_energy(const DeviceMesh& m, const LocalBatch& b, cons
         __syncwarp();
     }
     return warp_bcast(S, acc);
-}
-
-// air energy: w_scaf / |F_air| times the uniform-weight sum (Optimizer.cpp:774-777)
-__device__ double bij_air_energy(BijShared& S, bool withDir, double alpha)
-{
-    const int lane = threadIdx.x & 31;
-    double acc = 0.0;
-    for (int c0 = 0; c0 < S.nAirT; c0 += 32) {
-        const int t = c0 + lane;
-        double e = 0.0;
-        if (t < S.nAirT) {
-            double2 U[3];
-            int sl[3];
-            air_corners(S, t, withDir, alpha, U, sl);
-            e = sd_energy(U[0], U[1], U[2], S.air[t][0], S.air[t][1], S.air[t][2], S.air[t][3], 1.0);
-        }
-        S.triE[lane] = e;
-        __syncwarp();
-        if (lane == 0) {
-            const int n = min(32, S.nAirT - c0);
-            for (int k = 0; k < n; ++k) acc = acc + S.triE[k];
-        }
-        __syncwarp();
-    }
-    return warp_bcast(S, acc * S.wAir);
 }
 
 __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh m, double surfaceArea, LocalBatch b)
@@ -212,6 +253,8 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
     if (lane == 0) {
         S.mstatus = 0;
         S.maxSteiner = 0;
+        S.nAirT = 0;
+        S.wAir = 0.0;
     }
     __syncwarp();
     // initial energy: the candidate's global triangles with global weights,
@@ -237,6 +280,68 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
     int status = 0, it = 0, trials = 0;
     bool failed = false;
     constexpr int kEntRounds = (kBijDof * (kBijDof + 1) / 2 + 31) / 32;
+    // raw quantities of the starting point for the learned proposal's
+    // features, the local mesh's alone and as the unconstrained solve
+    // records them: energy, per-triangle unweighted energies (max, min,
+    // mean log, mean log^2), gradients at free slots 0 and 1, triangles
+    // touching them and their energy; the first step fills the rest
+    double raw[kLocalRaw];
+    for (int k = 0; k < kLocalRaw; ++k) raw[k] = 0.0;
+    {
+        double acc[12] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, -1e300};
+        for (int c0 = 0; c0 < P.nTri; c0 += 32) {
+            const int t = c0 + lane;
+            if (t < P.nTri) {
+                TriView v;
+                tri_view(m, b, P, S, t, false, 0.0, v);
+                const double e = sd_energy(v.U[0], v.U[1], v.U[2], v.A2, v.e0, v.e1, v.e01, v.w);
+                const double eu = e / (4.0 * v.w);
+                double2 cg3[3];
+                tri_corner_grads(v.U[0], v.U[1], v.U[2], v.A2, v.e0, v.e1, v.e01, v.w, cg3);
+                double q[4] = {0.0, 0.0, 0.0, 0.0};
+                double touch0 = 0.0, touch1 = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    if (v.slot[k] == 0) { q[0] += cg3[k].x; q[1] += cg3[k].y; touch0 = 1.0; }
+                    if (v.slot[k] == 1) { q[2] += cg3[k].x; q[3] += cg3[k].y; touch1 = 1.0; }
+                }
+                for (int k = 0; k < 4; ++k) S.triG[lane][k] = q[k];
+                S.triH[lane][0] = e;
+                S.triH[lane][1] = eu;
+                S.triH[lane][2] = log(eu);
+                S.triH[lane][3] = touch0;
+                S.triH[lane][4] = touch1;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                const int n = min(32, P.nTri - c0);
+                for (int k = 0; k < n; ++k) {
+                    const double e = S.triH[k][0], eu = S.triH[k][1], l = S.triH[k][2];
+                    acc[0] += l;
+                    acc[1] += l * l;
+                    for (int c = 0; c < 4; ++c) acc[2 + c] += S.triG[k][c];
+                    if (S.triH[k][3] != 0.0) { acc[6] += 1.0; acc[8] += e; }
+                    if (S.triH[k][4] != 0.0) { acc[7] += 1.0; acc[9] += e; }
+                    acc[10] = fmax(acc[10], eu);
+                    acc[11] = fmax(acc[11], -eu);
+                }
+            }
+            __syncwarp();
+        }
+        const double E0 = bij_mesh_energy(m, b, P, S);
+        raw[0] = E0;
+        raw[4] = E0;
+        raw[5] = acc[10];
+        raw[6] = -acc[11];
+        raw[7] = acc[0] / P.nTri;
+        raw[8] = acc[1] / P.nTri;
+        raw[9] = acc[2] * acc[2] + acc[3] * acc[3];
+        raw[10] = acc[4] * acc[4] + acc[5] * acc[5];
+        raw[11] = acc[2] * acc[4] + acc[3] * acc[5];
+        raw[12] = acc[6];
+        raw[13] = acc[7];
+        raw[14] = acc[8];
+        raw[15] = acc[9];
+    }
     for (;;) {
         if (it >= P.maxIter) break;
         // ---- the local scaffold from the current positions
@@ -306,192 +411,172 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
         __syncwarp();
         const int nFree = nFreeMesh + S.nSteiner;
         const int nDof = 2 * nFree;
-        // ---- gradient: the local mesh's, plus w_air times the air mesh's
-        // on the loop vertices and the Steiner points (Scaffold::augmentGradient)
-        double gm = 0.0, ga = 0.0;
-        for (int c0 = 0; c0 < P.nTri; c0 += 32) {
+        const int nAll = P.nTri + S.nAirT;
+        // ---- gradient: the local mesh's plus w_air times the air mesh's
+        // (Scaffold::augmentGradient), one pass over both meshes
+        double gj = 0.0;
+        for (int c0 = 0; c0 < nAll; c0 += 32) {
             const int t = c0 + lane;
-            if (t < P.nTri) {
-                double2 U[3];
-                int sl[3];
-                mesh_corners(b, P, S, t, false, 0.0, U, sl);
-                const int g = b.ltGlobal[P.triOff + t];
+            if (t < nAll) {
+                TriView v;
+                tri_view(m, b, P, S, t, false, 0.0, v);
                 double2 cg3[3];
-                tri_corner_grads(U[0], U[1], U[2], m.A2[g], m.e0[g], m.e1[g], m.e01[g], m.area[g] / P.localArea, cg3);
+                tri_corner_grads(v.U[0], v.U[1], v.U[2], v.A2, v.e0, v.e1, v.e01, v.w, cg3);
                 for (int k = 0; k < 3; ++k) {
                     S.triG[lane][2 * k] = cg3[k].x;
                     S.triG[lane][2 * k + 1] = cg3[k].y;
-                    S.triSlot[lane][k] = sl[k];
+                    S.triSlot[lane][k] = v.slot[k];
                 }
             }
             __syncwarp();
             if (lane < nDof) {
-                const int n = min(32, P.nTri - c0);
+                const int n = min(32, nAll - c0);
                 for (int q = 0; q < n; ++q)
                     for (int k = 0; k < 3; ++k)
-                        if (S.triSlot[q][k] == (lane >> 1)) gm = gm + S.triG[q][2 * k + (lane & 1)];
+                        if (S.triSlot[q][k] == (lane >> 1)) gj = gj + S.triG[q][2 * k + (lane & 1)];
             }
             __syncwarp();
         }
-        for (int c0 = 0; c0 < S.nAirT; c0 += 32) {
-            const int t = c0 + lane;
-            if (t < S.nAirT) {
-                double2 U[3];
-                int sl[3];
-                air_corners(S, t, false, 0.0, U, sl);
-                double2 cg3[3];
-                tri_corner_grads(U[0], U[1], U[2], S.air[t][0], S.air[t][1], S.air[t][2], S.air[t][3], 1.0, cg3);
-                for (int k = 0; k < 3; ++k) {
-                    S.triG[lane][2 * k] = cg3[k].x;
-                    S.triG[lane][2 * k + 1] = cg3[k].y;
-                    S.triSlot[lane][k] = sl[k];
-                }
-            }
-            __syncwarp();
-            if (lane < nDof) {
-                const int n = min(32, S.nAirT - c0);
-                for (int q = 0; q < n; ++q)
-                    for (int k = 0; k < 3; ++k)
-                        if (S.triSlot[q][k] == (lane >> 1)) ga = ga + S.triG[q][2 * k + (lane & 1)];
-            }
-            __syncwarp();
-        }
-        if (lane < nDof) S.g[lane] = (lane >> 1) < nFreeMesh ? gm + S.wAir * ga : S.wAir * ga;
+        if (lane < nDof) S.g[lane] = gj;
         __syncwarp();
         double gsq = 0.0;
         for (int j = 0; j < nDof; ++j) gsq = gsq + S.g[j] * S.g[j];
+        if (it == 0) raw[1] = gsq;
         if (gsq < P.targetGRes) {   // Optimizer.cpp:215-221
             status = 1;
             break;
         }
-        // ---- dense Hessian: projected local blocks, plus w_air times the
-        // projected air blocks (Scaffold::augmentProxyMatrix, dense form)
+        // ---- dense Hessian: projected local and air blocks (the air ones
+        // weighted w_air, Scaffold::augmentProxyMatrix's dense form), one pass
         const int nEnt = nDof * (nDof + 1) / 2;
-        double hm[kEntRounds], ha[kEntRounds];
-        for (int r = 0; r < kEntRounds; ++r) hm[r] = ha[r] = 0.0;
-        for (int pass = 0; pass < 2; ++pass) {
-            const int nT = pass == 0 ? P.nTri : S.nAirT;
-            for (int c0 = 0; c0 < nT; c0 += 32) {
-                const int t = c0 + lane;
-                if (t < nT) {
-                    double2 U[3];
-                    int sl[3];
-                    double H6[6][6];
-                    if (pass == 0) {
-                        mesh_corners(b, P, S, t, false, 0.0, U, sl);
-                        const int g = b.ltGlobal[P.triOff + t];
-                        tri_hessian(U, m.A2[g], m.e0d[g], m.e1d[g], m.e01d[g], m.area[g] / P.localArea, H6,
-                                    b.fp32Hessian ? 2 : 1);
-                    }
-                    else {
-                        air_corners(S, t, false, 0.0, U, sl);
-                        tri_hessian(U, S.air[t][0], S.air[t][4], S.air[t][5], S.air[t][6], 1.0, H6,
-                                    b.fp32Hessian ? 2 : 1);
-                    }
-                    for (int i = 0; i < 6; ++i)
-                        for (int j = i; j < 6; ++j) S.triH[lane][bsym21(i, j)] = H6[i][j];
-                    for (int k = 0; k < 3; ++k) S.triSlot[lane][k] = sl[k];
-                }
-                __syncwarp();
-                const int n = min(32, nT - c0);
-                for (int r = 0; r < kEntRounds; ++r) {
-                    const int e = lane + 32 * r;
-                    if (e >= nEnt) continue;
-                    int i = 0, rem = e;
-                    while (rem >= nDof - i) { rem -= nDof - i; ++i; }
-                    const int j = i + rem;
-                    double acc = pass == 0 ? hm[r] : ha[r];
-                    for (int q = 0; q < n; ++q)
-                        for (int a = 0; a < 3; ++a) {
-                            if (S.triSlot[q][a] != (i >> 1)) continue;
-                            for (int c = 0; c < 3; ++c)
-                                if (S.triSlot[q][c] == (j >> 1))
-                                    acc = acc + S.triH[q][bsym21(2 * a + (i & 1), 2 * c + (j & 1))];
-                        }
-                    if (pass == 0) hm[r] = acc;
-                    else ha[r] = acc;
-                }
-                __syncwarp();
+        double hacc[kEntRounds];
+        for (int r = 0; r < kEntRounds; ++r) hacc[r] = 0.0;
+        for (int c0 = 0; c0 < nAll; c0 += 32) {
+            const int t = c0 + lane;
+            if (t < nAll) {
+                TriView v;
+                tri_view(m, b, P, S, t, false, 0.0, v);
+                double H6[6][6];
+                tri_hessian(v.U, v.A2, v.e0d, v.e1d, v.e01d, v.w, H6, b.fp32Hessian ? 2 : 1);
+                for (int i = 0; i < 6; ++i)
+                    for (int j = i; j < 6; ++j) S.triH[lane][bsym21(i, j)] = H6[i][j];
+                for (int k = 0; k < 3; ++k) S.triSlot[lane][k] = v.slot[k];
             }
+            __syncwarp();
+            const int n = min(32, nAll - c0);
+            for (int r = 0; r < kEntRounds; ++r) {
+                const int e = lane + 32 * r;
+                if (e >= nEnt) break;
+                int i = 0, rem = e;
+                while (rem >= nDof - i) { rem -= nDof - i; ++i; }
+                const int j = i + rem;
+                double acc = hacc[r];
+                for (int q = 0; q < n; ++q)
+                    for (int a = 0; a < 3; ++a) {
+                        if (S.triSlot[q][a] != (i >> 1)) continue;
+                        for (int c = 0; c < 3; ++c)
+                            if (S.triSlot[q][c] == (j >> 1))
+                                acc = acc + S.triH[q][bsym21(2 * a + (i & 1), 2 * c + (j & 1))];
+                    }
+                hacc[r] = acc;
+            }
+            __syncwarp();
         }
         for (int r = 0; r < kEntRounds; ++r) {
             const int e = lane + 32 * r;
-            if (e >= nEnt) continue;
+            if (e >= nEnt) break;
             int i = 0, rem = e;
             while (rem >= nDof - i) { rem -= nDof - i; ++i; }
             const int j = i + rem;
-            const double v = hm[r] + S.wAir * ha[r];
-            S.H[i][j] = v;
-            S.H[j][i] = v;
+            S.H[i][j] = hacc[r];
+            S.H[j][i] = hacc[r];
         }
+        if (lane < nDof) S.perm[lane] = lane;
         __syncwarp();
         // ---- H d = -g: LDL^T with symmetric pivoting on the largest
-        // remaining diagonal (Eigen::LDLT), in place in S.H
+        // remaining diagonal (Eigen::LDLT), each step over the lanes (the
+        // arithmetic of every entry as a single thread would do it)
+        double dmax = 0.0;
+        for (int i = 0; i < nDof; ++i) dmax = fmax(dmax, fabs(S.H[i][i]));
+        for (int k = 0; k < nDof; ++k) {
+            int piv = k;
+            for (int i = k + 1; i < nDof; ++i)
+                if (fabs(S.H[i][i]) > fabs(S.H[piv][piv])) piv = i;
+            if (piv != k) {
+                for (int j = lane; j < nDof; j += 32) {
+                    const double t = S.H[k][j];
+                    S.H[k][j] = S.H[piv][j];
+                    S.H[piv][j] = t;
+                }
+                __syncwarp();
+                for (int i = lane; i < nDof; i += 32) {
+                    const double t = S.H[i][k];
+                    S.H[i][k] = S.H[i][piv];
+                    S.H[i][piv] = t;
+                }
+                if (lane == 0) {
+                    const int tp = S.perm[k];
+                    S.perm[k] = S.perm[piv];
+                    S.perm[piv] = tp;
+                }
+                __syncwarp();
+            }
+            const double d = S.H[k][k];
+            if (!(fabs(d) > 1e-300 + 1e-15 * dmax)) {
+                __syncwarp();
+                if (lane == 0) S.H[k][k] = 0.0;
+                for (int i = k + 1 + lane; i < nDof; i += 32) S.H[i][k] = 0.0;
+                __syncwarp();
+                continue;
+            }
+            for (int i = k + 1 + lane; i < nDof; i += 32) S.H[i][k] = S.H[i][k] / d;
+            __syncwarp();
+            // the trailing update, pairs (i, j), k < j <= i, over the lanes
+            const int mRem = nDof - k - 1;
+            const int nPairs = mRem * (mRem + 1) / 2;
+            for (int p = lane; p < nPairs; p += 32) {
+                int ii = 0, rem = p;
+                while (rem > ii) { rem -= ii + 1; ++ii; }
+                const int i = k + 1 + ii, j = k + 1 + rem;
+                const double v = S.H[i][j] - S.H[i][k] * d * S.H[j][k];
+                S.H[i][j] = v;
+                S.H[j][i] = v;
+            }
+            __syncwarp();
+        }
         if (lane == 0) {
-            int perm[kBijDof];
-            double y[kBijDof];
-            for (int i = 0; i < nDof; ++i) {
-                perm[i] = i;
-                y[i] = -S.g[i];
-            }
-            double dmax = 0.0;
-            for (int i = 0; i < nDof; ++i) dmax = fmax(dmax, fabs(S.H[i][i]));
-            for (int k = 0; k < nDof; ++k) {
-                int piv = k;
-                for (int i = k + 1; i < nDof; ++i)
-                    if (fabs(S.H[i][i]) > fabs(S.H[piv][piv])) piv = i;
-                if (piv != k) {
-                    for (int j = 0; j < nDof; ++j) { const double t = S.H[k][j]; S.H[k][j] = S.H[piv][j]; S.H[piv][j] = t; }
-                    for (int i = 0; i < nDof; ++i) { const double t = S.H[i][k]; S.H[i][k] = S.H[i][piv]; S.H[i][piv] = t; }
-                    const int tp = perm[k]; perm[k] = perm[piv]; perm[piv] = tp;
-                }
-                const double d = S.H[k][k];
-                if (!(fabs(d) > 1e-300 + 1e-15 * dmax)) {
-                    S.H[k][k] = 0.0;
-                    for (int i = k + 1; i < nDof; ++i) S.H[i][k] = 0.0;
-                    continue;
-                }
-                for (int i = k + 1; i < nDof; ++i) S.H[i][k] = S.H[i][k] / d;
-                for (int i = k + 1; i < nDof; ++i)
-                    for (int j = k + 1; j <= i; ++j) {
-                        S.H[i][j] = S.H[i][j] - S.H[i][k] * d * S.H[j][k];
-                        S.H[j][i] = S.H[i][j];
-                    }
-            }
             double x[kBijDof];
-            for (int i = 0; i < nDof; ++i) x[i] = y[perm[i]];
+            for (int i = 0; i < nDof; ++i) x[i] = -S.g[S.perm[i]];
             for (int i = 0; i < nDof; ++i)
                 for (int k = 0; k < i; ++k) x[i] = x[i] - S.H[i][k] * x[k];
             for (int i = 0; i < nDof; ++i) x[i] = (S.H[i][i] != 0.0) ? x[i] / S.H[i][i] : 0.0;
             for (int i = nDof - 1; i >= 0; --i)
                 for (int k = i + 1; k < nDof; ++k) x[i] = x[i] - S.H[k][i] * x[k];
-            for (int i = 0; i < nDof; ++i) S.dir[perm[i]] = x[i];
+            for (int i = 0; i < nDof; ++i) S.dir[S.perm[i]] = x[i];
         }
         __syncwarp();
         // ---- line search (Optimizer.cpp:575-652) over both meshes
         double bound = 1.0;
-        for (int pass = 0; pass < 2; ++pass) {
-            const int nT = pass == 0 ? P.nTri : S.nAirT;
-            for (int t = lane; t < nT; t += 32) {
-                double2 U[3], D[3];
-                int sl[3];
-                if (pass == 0) mesh_corners(b, P, S, t, false, 0.0, U, sl);
-                else air_corners(S, t, false, 0.0, U, sl);
-                for (int k = 0; k < 3; ++k)
-                    D[k] = sl[k] >= 0 ? make_double2(S.dir[2 * sl[k]], S.dir[2 * sl[k] + 1]) : make_double2(0.0, 0.0);
-                bound = fmin(bound, tri_step_bound(U[0], U[1], U[2], D[0], D[1], D[2], 1.0));
-            }
+        for (int t = lane; t < nAll; t += 32) {
+            TriView v;
+            tri_view(m, b, P, S, t, false, 0.0, v);
+            double2 D[3];
+            for (int k = 0; k < 3; ++k)
+                D[k] = v.slot[k] >= 0 ? make_double2(S.dir[2 * v.slot[k]], S.dir[2 * v.slot[k] + 1])
+                                      : make_double2(0.0, 0.0);
+            bound = fmin(bound, tri_step_bound(v.U[0], v.U[1], v.U[2], D[0], D[1], D[2], 1.0));
         }
         for (int o = 16; o > 0; o >>= 1) bound = fmin(bound, __shfl_xor_sync(0xffffffffu, bound, o));
         double step = bound * 0.99;
         if (lane < nFree) S.pos0[lane] = S.pos[lane];
         __syncwarp();
         // energy with the new scaffold at the current layout
-        const double eAir0 = bij_air_energy(S, false, 0.0);
-        lastE = bij_mesh_energy(m, b, P, S, false, 0.0) + eAir0;
+        double eMesh0, eAir0, eMesh, eAir;
+        bij_energies(m, b, P, S, false, 0.0, eMesh0, eAir0);
+        lastE = eMesh0 + eAir0;
         bool stopped = false;
-        double eAir = bij_air_energy(S, true, step);
-        double testE = bij_mesh_energy(m, b, P, S, true, step) + eAir;
+        bij_energies(m, b, P, S, true, step, eMesh, eAir);
+        double testE = eMesh + eAir;
         ++trials;
         while (testE > lastE) {
             step = step / 2.0;
@@ -499,8 +584,8 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
                 stopped = true;
                 break;
             }
-            eAir = bij_air_energy(S, true, step);
-            testE = bij_mesh_energy(m, b, P, S, true, step) + eAir;
+            bij_energies(m, b, P, S, true, step, eMesh, eAir);
+            testE = eMesh + eAir;
             ++trials;
         }
         if (lane < nFree) {
@@ -510,6 +595,11 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
         __syncwarp();
         const double lastEDec = (lastE - testE) + (eAir - eAir0);
         if ((lastEDec / lastE < 1.0e-6 * step) && (step > 1.0e-3)) stopped = true;
+        if (it == 0) {
+            raw[2] = step;
+            raw[3] = trials;
+            raw[4] = eMesh;   // the local mesh's energy after the first step
+        }
         lastE = testE;
         ++it;
         if (!isfinite(lastE)) {
@@ -522,7 +612,7 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
         }
     }
     // the local mesh's energy at the final layout (excludeScaffold)
-    const double curE = bij_mesh_energy(m, b, P, S, false, 0.0);
+    const double curE = bij_mesh_energy(m, b, P, S);
     if (lane == 0) {
         LocalResult r;
         r.initE = initE;
@@ -532,7 +622,7 @@ __global__ void __launch_bounds__(32 * kBijProbs) k_local_newton_bij(DeviceMesh 
         r.iters = it;
         r.status = failed ? 3 : (isfinite(curE) ? status : 2);
         r.trials = trials;
-        for (int k = 0; k < kLocalRaw; ++k) r.raw[k] = 0.0;
+        for (int k = 0; k < kLocalRaw; ++k) r.raw[k] = raw[k];
         r.cycles = clock64() - clk0;
         r.airStatus = S.mstatus;
         r.airSteiner = S.maxSteiner;

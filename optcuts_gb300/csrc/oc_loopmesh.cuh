@@ -380,19 +380,24 @@ __host__ __device__ inline int loop_mesh(const double2* pts, int L, int maxStein
     for (int i = 1; i + 1 < L; ++i)
         area2 += (pts[i].x - pts[0].x) * (pts[i + 1].y - pts[0].y) - (pts[i].y - pts[0].y) * (pts[i + 1].x - pts[0].x);
     const bool ccw = area2 > 0.0;
-    // ear clipping over a counter-clockwise index ring
+    // ear clipping over a counter-clockwise index ring; only vertices that
+    // are not strictly convex can lie in an ear, so only they are tested
     short ring[kLoopMaxPts];
+    signed char convex[kLoopMaxPts];   // by ring position
     int n = L;
     for (int i = 0; i < L; ++i) ring[i] = static_cast<short>(ccw ? i : L - 1 - i);
+    for (int i = 0; i < n; ++i)
+        convex[i] = orient(M.P[ring[(i + n - 1) % n]], M.P[ring[i]], M.P[ring[(i + 1) % n]]) > 0 ? 1 : 0;
     int guard = 0;
     while (n > 3) {
         bool clipped = false;
         for (int i = 0; i < n && !clipped; ++i) {
+            if (!convex[i]) continue;   // reflex or flat
             const int ip = ring[(i + n - 1) % n], iv = ring[i], in = ring[(i + 1) % n];
             const double2 p = M.P[ip], v = M.P[iv], q = M.P[in];
-            if (orient(p, v, q) <= 0) continue;   // reflex or flat
             bool ear = true;
             for (int j = 0; j < n && ear; ++j) {
+                if (convex[j]) continue;
                 const int w = ring[j];
                 if (w == ip || w == iv || w == in) continue;
                 const double2 x = M.P[w];
@@ -403,8 +408,15 @@ __host__ __device__ inline int loop_mesh(const double2* pts, int L, int maxStein
             M.T[M.nT][1] = static_cast<short>(iv);
             M.T[M.nT][2] = static_cast<short>(in);
             ++M.nT;
-            for (int j = i; j + 1 < n; ++j) ring[j] = ring[j + 1];
+            for (int j = i; j + 1 < n; ++j) {
+                ring[j] = ring[j + 1];
+                convex[j] = convex[j + 1];
+            }
             --n;
+            // the two neighbours' corners changed
+            const int a = (i + n - 1) % n, b = i % n;
+            convex[a] = orient(M.P[ring[(a + n - 1) % n]], M.P[ring[a]], M.P[ring[(a + 1) % n]]) > 0 ? 1 : 0;
+            convex[b] = orient(M.P[ring[(b + n - 1) % n]], M.P[ring[b]], M.P[ring[(b + 1) % n]]) > 0 ? 1 : 0;
             clipped = true;
         }
         if (!clipped || ++guard > kLoopMaxPts) return kLoopNoEar;
@@ -416,19 +428,39 @@ __host__ __device__ inline int loop_mesh(const double2* pts, int L, int maxStein
     ++M.nT;
     link_all(M);
     // Lawson flips to the constrained Delaunay triangulation (the polygon's
-    // edges have no neighbour and are never flipped)
+    // edges have no neighbour and are never flipped): every interior edge
+    // once, then the outer edges of each flipped quad again
     {
-        bool any = true;
-        int rounds = 0;
-        while (any) {
-            any = false;
-            for (int t = 0; t < M.nT; ++t)
-                for (int k = 0; k < 3; ++k)
-                    if (illegal(M, t, k)) {
-                        flip(M, t, k);
-                        any = true;
-                    }
-            if (++rounds > 4 * kLoopMaxTri) return kLoopFlipCap;
+        short stk[6 * kLoopMaxTri][2];   // (triangle, its lower-numbered vertex of the edge)
+        int sp = 0;
+        for (int t = 0; t < M.nT; ++t)
+            for (int k = 0; k < 3; ++k)
+                if (M.N[t][k] > t) {
+                    stk[sp][0] = static_cast<short>(t);
+                    stk[sp][1] = M.T[t][k];
+                    ++sp;
+                }
+        int flips = 0;
+        while (sp > 0) {
+            --sp;
+            const int t = stk[sp][0], a = stk[sp][1];
+            int k = -1;
+            for (int q = 0; q < 3; ++q)
+                if (M.T[t][q] == a) k = q;
+            if (k < 0 || M.N[t][k] < 0 || !illegal(M, t, k)) continue;
+            const int s2 = M.N[t][k];
+            flip(M, t, k);
+            if (++flips > 4 * kLoopMaxTri * kLoopMaxTri) return kLoopFlipCap;
+            // t = (d c a), s2 = (c d b): their edges other than (d, c)
+            if (sp + 4 > 6 * kLoopMaxTri) return kLoopFlipCap;
+            for (int q = 1; q < 3; ++q) {
+                stk[sp][0] = static_cast<short>(t);
+                stk[sp][1] = M.T[t][q];
+                ++sp;
+                stk[sp][0] = static_cast<short>(s2);
+                stk[sp][1] = M.T[s2][q];
+                ++sp;
+            }
         }
     }
     if (maxSteiner <= 0) return kLoopOk;

@@ -598,9 +598,6 @@ int oc_optcuts_create(oc_optimizer* opt, oc_mesh* mesh, const oc_optcuts_config*
     if (cfg) c = *cfg;
     // b_d <= 4 is replaced by 4.1 (main.cpp:1266-1269)
     if (!(c.upperBound > 4.0)) c.upperBound = 4.1;
-    // the learned proposal's features are defined on the bijectivity-off
-    // local solves
-    if (c.bijective && (c.mlp || c.recordFeatures)) return OC_ERR_INVALID;
     if (!(c.filterExp > 0.0) || c.filterExp > 1.0 || c.maxNewtonIters <= 0) return OC_ERR_INVALID;
     oc_optcuts* o = new (std::nothrow) oc_optcuts;
     if (!o) return OC_ERR_NOMEM;

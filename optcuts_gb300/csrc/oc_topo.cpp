@@ -2090,10 +2090,6 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
             if (err) *err = "topology query: the bijective form needs the scaffold's air mesh";
             return OC_ERR_INVALID;
         }
-        if ((opts.flags & kTopoLearned) || (opts.flags & kTopoRecordFeatures)) {
-            if (err) *err = "topology query: the learned proposal's features are defined without air loops";
-            return OC_ERR_INVALID;
-        }
         airSrc = std::make_unique<AirSrc>();
         airSrc->build(in);
     }
