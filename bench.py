@@ -61,6 +61,8 @@ def parse():
                    help="Newton iterations the outer loop may spend reaching that state")
     p.add_argument("--top-frac", type=float, default=0.1, help="fraction of local problems solved exactly (learned)")
     p.add_argument("--train-epochs", type=int, default=30, help="MLP training epochs over the exhaustive pairs")
+    p.add_argument("--topo-bijective", default="on", choices=["on", "off"],
+                   help="outer loop and timed topology step with bijectivity on (the reference's default) or off")
     return p.parse_args()
 
 
@@ -301,14 +303,19 @@ def ranking(ex, le, top_frac):
 
 def topology_section(args, oc, ctx, opt, mesh, st, rank):
     """The topology step on the state the outer loop reaches after
-    args.outer_steps topology operations (the bijectivity-off outer loop of
-    the library: dual updates, propagation; its first inner loop converges
-    the Newton phase), timed exhaustive and with the learned proposal trained
-    on the (features, target) pairs the outer loop's own exhaustive queries
-    recorded on the way."""
-    opt.clearScaffold()            # bijectivity off: no air mesh
+    args.outer_steps topology operations (the library's outer loop: dual
+    updates, propagation; its first inner loop converges the Newton phase),
+    with bijectivity on by default (the reference's default: scaffold on,
+    every local solve with its air loop).  Timed: the exhaustive step, the
+    learned proposal trained on the (features, target) pairs the outer
+    loop's own exhaustive queries recorded on the way, and the
+    bijectivity-off step on the same state (with its FP32-projection and
+    autotuned variants and the CPU port beside it)."""
+    bij = args.topo_bijective == "on"
+    if not bij:
+        opt.clearScaffold()            # bijectivity off: no air mesh
     mesh.setCohesiveEdges(st.cohE)
-    outer = oc.OptCuts(opt, recordFeatures=True, maxNewtonIters=args.outer_newton_cap)
+    outer = oc.OptCuts(opt, bijective=bij, recordFeatures=True, maxNewtonIters=args.outer_newton_cap)
     ctx.synchronize()
     t0 = time.perf_counter()
     passes, finished = 0, False
@@ -320,6 +327,8 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
         if opt.solve(1) == 1:
             converged = True
             break
+        if bij:
+            opt.rebuildScaffold()          # Optimizer.cpp:251-257
     ctx.synchronize()
     outer_s = time.perf_counter() - t0
     so = outer.state()
@@ -342,37 +351,42 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
 
     def summary(qs):
         qb, qm, qi = qs
-        return {"query_ms": qb["query_ms"], "gpu_solve_ms": qb["solve_ms"], "probe_ms": qb["probe_ms"],
-                "exact_ms": qb["exact_ms"],
-                "host_build_ms": {name: q["build_ms"] for name, q in zip(("boundary_split", "merge", "interior_split"),
-                                                                        qs)},
-                "local_problems": sum(q["local_problems"] for q in qs),
-                "exact_solves": sum(q["selected"] for q in qs),
-                "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"], "interior_split": qi["EwDec_max"]}}
+        out = {"query_ms": qb["query_ms"], "gpu_solve_ms": qb["solve_ms"], "probe_ms": qb["probe_ms"],
+               "exact_ms": qb["exact_ms"],
+               "host_build_ms": {name: q["build_ms"] for name, q in
+                                 zip(("boundary_split", "merge", "interior_split"), qs)},
+               "local_problems": sum(q["local_problems"] for q in qs),
+               "exact_solves": sum(q["selected"] for q in qs),
+               "local_iterations": sum(q["local_iters_total"] for q in qs),
+               "max_local_iterations": max(q["max_local_iters"] for q in qs),
+               "best": {"boundary_split": qb["EwDec_max"], "merge": qm["EwDec_max"],
+                        "interior_split": qi["EwDec_max"]}}
+        air = [q["air"] for q in qs]
+        if any(a["problems"] for a in air):
+            out["air_loops"] = {"problems": sum(a["problems"] for a in air),
+                                "abandoned": sum(a["rejected"] for a in air),
+                                "steiner_max": max(a["steiner_max"] for a in air),
+                                "refinement_capped": sum(a["capped"] for a in air)}
+        return out
 
-    queries()   # warm-up
-    t_gpu, qs = timed_step(features=True)
-    t_fp32, qs32 = timed_step(fp32=True)
-    queries(autotune=True)   # the schedule autotuner measures its candidates on this state
-    t_tuned, qs_t = timed_step(autotune=True)
+    queries(bijective=bij)   # warm-up
+    t_gpu, qs = timed_step(features=True, bijective=bij)
+    t_fp32, qs32 = timed_step(fp32=True, bijective=bij)
     qb, qm, qi = qs
+    form = "on (scaffold on, every local solve with its air loop)" if bij else "off (no air meshes)"
     topo = {"metric": "topology-step s (exhaustive candidate evaluation: boundary split, merge and interior split "
                       "queries of one state, solved together)", "value": t_gpu, "unit": "s",
-            "higher_is_better": False, "bijectivity": "off (outer loop and local solves without air meshes)",
-            "state": {"what": "after %d topology operations of the outer loop, inner loop converged" %
-                              int(so["topology_steps"]),
+            "higher_is_better": False, "bijectivity": form,
+            "state": {"what": "after %d topology operations of the outer loop (bijectivity %s), inner loop converged" %
+                              (int(so["topology_steps"]), "on" if bij else "off"),
                       "newton_iterations": opt.getIterNum(), "topology_steps": int(so["topology_steps"]),
                       "converged": converged, "finished": bool(finished), "lambda": lam_t, "E_SD": so["E_SD"],
                       "E_se": so["E_se"], "vertices": int(so["vertices"]), "outer_loop_s": outer_s,
                       "outer_loop_ms": {k: so[k] for k in ("newton_ms", "query_ms", "apply_ms")}},
             "candidates": {"boundary_split": len(qb["candidates"]), "merge": len(qm["candidates"]),
                            "interior_split": len(qi["candidates"])},
-            "max_local_iterations": max(q["max_local_iters"] for q in qs),
-            "local_iterations": sum(q["local_iters_total"] for q in qs),
             "local_capped": sum(q["local_capped"] for q in qs),
-            **summary(qs), "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)},
-            "autotuned_schedules": {"value": t_tuned, "unit": "s", **summary(qs_t),
-                                    "table": oc.topology_schedules()}}
+            **summary(qs), "fp32_hessian_option": {"value": t_fp32, "unit": "s", **summary(qs32)}}
     e_w = opt.getLastEnergyVal(excludeScaffold=True) + lam_t * so["E_se"]
 
     def after(qs_):
@@ -384,9 +398,9 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
         loss = mlp.train(X, t, epochs=args.train_epochs, batch=512, lr=2e-3, seed=3)
         ctx.synchronize()
         train_s = time.perf_counter() - t1
-        queries(mlp=mlp, topFrac=args.top_frac)   # warm-up
-        t_l, ql = timed_step(mlp=mlp, topFrac=args.top_frac)
-        t_l32, ql32 = timed_step(mlp=mlp, topFrac=args.top_frac, fp32=True)
+        queries(mlp=mlp, topFrac=args.top_frac, bijective=bij)   # warm-up
+        t_l, ql = timed_step(mlp=mlp, topFrac=args.top_frac, bijective=bij)
+        t_l32, ql32 = timed_step(mlp=mlp, topFrac=args.top_frac, fp32=True, bijective=bij)
         ew_ex, ew_l, ew_ex32, ew_l32 = after(qs), after(ql), after(qs32), after(ql32)
         # the exhaustive pass's own pairs at this state: held out from training
         Xh = np.concatenate([q["features"] for q in qs])
@@ -409,6 +423,23 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
                     "epochs": args.train_epochs, "batch": 512, "seed": 3, "train_s": train_s, "final_mse": loss,
                     "target_var": float(np.var(t)), "train_r2": 1.0 - loss / float(np.var(t)) if np.var(t) else None,
                     "heldout_r2": r2}}
+    if bij:
+        # the same state's step without air loops, for comparison
+        queries()
+        t_off, qs_off = timed_step()
+        t_off32, qs_off32 = timed_step(fp32=True)
+        queries(autotune=True)   # the schedule autotuner measures its candidates on this state
+        t_tuned, qs_t = timed_step(autotune=True)
+        topo["bijectivity_off"] = {"metric": "topology-step s (exhaustive, bijectivity off, same state)",
+                                   "value": t_off, "unit": "s", **summary(qs_off),
+                                   "fp32_hessian_option": {"value": t_off32, "unit": "s", **summary(qs_off32)},
+                                   "autotuned_schedules": {"value": t_tuned, "unit": "s", **summary(qs_t),
+                                                           "table": oc.topology_schedules()}}
+    else:
+        queries(autotune=True)
+        t_tuned, qs_t = timed_step(autotune=True)
+        topo["autotuned_schedules"] = {"value": t_tuned, "unit": "s", **summary(qs_t),
+                                       "table": oc.topology_schedules()}
     if rank == 0 and not args.no_cpu_baseline:
         import oracle as O
         threads = os.cpu_count() or 1
@@ -418,24 +449,10 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
             _, s_ = O.topology_query(mesh.V_rest, uv, mesh.F, mesh.cohE, op, lam_t, threads=threads)
             secs += s_
         topo["cpu_baseline"] = {"value": secs, "unit": "s", "cores": threads, "kind": "port",
-                                "sample": "the same three queries on the same state"}
-    # the same step in its bijective form (the scaffold's air mesh of this
-    # state, every local solve with its air loop re-meshed each iteration)
-    opt.rebuildScaffold()
-    queries(bijective=True)   # warm-up
-    t_bij, qs_bij = timed_step(bijective=True)
-    opt.clearScaffold()
-    air = [q["air"] for q in qs_bij]
-    topo["bijective"] = {"metric": "topology-step s (exhaustive, bijectivity on)", "value": t_bij, "unit": "s",
-                         "higher_is_better": False, **summary(qs_bij),
-                         "air_loops": {"problems": sum(a["problems"] for a in air),
-                                       "abandoned": sum(a["rejected"] for a in air),
-                                       "steiner_max": max(a["steiner_max"] for a in air),
-                                       "refinement_capped": sum(a["capped"] for a in air)},
-                         "local_iterations": sum(q["local_iters_total"] for q in qs_bij),
-                         "max_local_iterations": max(q["max_local_iters"] for q in qs_bij)}
+                                "sample": "the same three queries on the same state, bijectivity off (the port "
+                                          "has no air loops)"}
     # applying the chosen operation (Optimizer::createFracture: mesh edit,
-    # device mesh, Newton pattern and analysis, energy), timed once
+    # device mesh, Newton pattern and analysis, scaffold, energy), timed once
     cands = [(q["EwDec_max"], op, q) for op, q in ((oc.OP_BOUNDARY_SPLIT, qb), (oc.OP_MERGE, qm)) if q["best"] >= 0]
     if cands:
         ew, op, q = max(cands, key=lambda x: x[0])
@@ -447,7 +464,8 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
         topo["apply"] = {"value": time.perf_counter() - t1, "unit": "s",
                          "op": {0: "boundary_split", 1: "interior_split", 2: "merge"}[op], "EwDec": ew,
                          "phases_ms": {k: round(v, 2) for k, v in opt.applyTiming().items()},
-                         "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and analysis, energy"}
+                         "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and analysis, "
+                                 "scaffold, energy"}
     return topo
 
 

@@ -343,8 +343,9 @@ int oc_topology_query(oc_mesh* mesh, int opType, double lambda_t, double filterE
  * split between the split copies, first-step decrease, ...; 32 values),
  * the MLP predicts the fraction of its excess energy the full solve would
  * remove, the predicted E_w decreases are ranked and only the top fraction
- * topFrac of the problems is solved exactly; the exact solves alone decide
- * the candidates' values (unsolved candidates report -DBL_MAX). */
+ * topFrac of the problems is solved exactly (at least 32 of them, or all of
+ * an operation that has fewer); the exact solves alone decide the
+ * candidates' values (unsolved candidates report -DBL_MAX). */
 typedef struct oc_mlp oc_mlp;
 int oc_topology_query_learned(oc_mesh* mesh, int opType, double lambda_t, double filterExp, int options, oc_mlp* mlp,
                               double topFrac, oc_topo_result** out);

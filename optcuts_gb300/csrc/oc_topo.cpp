@@ -2155,8 +2155,12 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
                 ex.ewPred.resize(ni);
                 for (int j = 0; j < ni; ++j) ex.ewPred[j] = -pred[j].first * (op == kOpInteriorSplit ? 0.5 : 1.0);
                 std::stable_sort(pred.begin(), pred.end());
+                // the top fraction, and never fewer than kMinExact problems
+                // (an operation with few candidates, a step's merges
+                // typically, is solved exhaustively)
+                constexpr int kMinExact = 32;
                 int kTop = static_cast<int>(std::ceil(opts.topFrac * ni));
-                kTop = std::max(1, std::min(ni, kTop));
+                kTop = std::max(std::min(ni, kMinExact), std::min(ni, kTop));
                 for (int q = 0; q < kTop; ++q) {
                     solved[start[i] + pred[q].second] = 1;
                     sel.push_back(static_cast<int>(start[i] + pred[q].second));

@@ -101,3 +101,24 @@ def test_bijective_needs_a_scaffold(golden):
     m.setCohesiveEdges(g["topo_cohE"])
     with pytest.raises(oc.OCError):
         m.querySplit(g["topo_best"][3], bijective=True)
+
+
+def test_learned_bijective_probe_features_and_full_fraction(golden):
+    """The learned proposal on bijective queries: its probe is the bijective
+    solve's own first iteration, so the one-step pass sees exactly the
+    features an exhaustive bijective query records; with the whole fraction
+    solved exactly it reproduces the exhaustive query."""
+    g = golden("sheet_3k_bij_topo")
+    m, opt = bij_state(g)
+    lam = g["topo_best"][3]
+    ex = m.querySplit(lam, splitInterior=True, features=True, bijective=True)
+    mlp = oc.MLP(32, 128, seed=3)
+    le = m.querySplit(lam, splitInterior=True, mlp=mlp, topFrac=0.1, bijective=True)
+    np.testing.assert_array_equal(le["features"], ex["features"])
+    assert le["selected"] == max(min(ex["local_problems"], 32), int(np.ceil(0.1 * ex["local_problems"])))
+    full = m.querySplit(lam, splitInterior=True, mlp=mlp, topFrac=1.0, bijective=True)
+    assert [c["EwDec"] for c in full["candidates"]] == [c["EwDec"] for c in ex["candidates"]]
+    # trained on the exhaustive pairs, the learned pass keeps the best candidate
+    mlp.train(ex["features"], ex["target"], epochs=40, batch=256, lr=2e-3, seed=3)
+    le = m.querySplit(lam, splitInterior=True, mlp=mlp, topFrac=0.2, bijective=True)
+    assert le["EwDec_max"] == pytest.approx(ex["EwDec_max"], rel=1e-12)
