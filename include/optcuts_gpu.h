@@ -212,6 +212,14 @@ typedef struct {
                              (default: at every node the smaller balanced
                              separator of a BFS level set and a bisection of
                              the current UV positions) or OC_ORDER_BFS */
+    int carryAnalysis;    /* 1 (default): after a topology operation the direct
+                             solver's dissection tree is carried over (a copy
+                             joins its source vertex's node, a merged vertex
+                             the nodes' common ancestor) and only the front
+                             structures are rebuilt; a full analysis when the
+                             tree no longer separates the pattern, after 64
+                             carried analyses or once the factor cost grew 30%;
+                             0: a full analysis after every operation */
 } oc_optimizer_config;
 
 int oc_optimizer_default_config(oc_optimizer_config* cfg);
@@ -445,6 +453,12 @@ int oc_optimizer_create_fracture(oc_optimizer* opt, int opType, const int* path,
  * edit, device mesh rebuild, scaffold rebuild, Newton pattern and symbolic
  * analysis (host), their device allocation and upload, energy evaluation */
 int oc_optimizer_apply_timing(oc_optimizer* opt, double* out6);
+/* The direct solver's last symbolic analysis: carried = the number of
+ * carried analyses since the last full one (0: that was a full analysis),
+ * host milliseconds of its dissection (0 when carried) and of its front
+ * structures, its factor flops and those of the last full analysis. */
+int oc_optimizer_analysis_info(oc_optimizer* opt, int* carried, double* ndMs, double* symMs, double* flops,
+                               double* fullFlops);
 /* the same operation on a mesh alone */
 int oc_mesh_apply_topology(oc_mesh* mesh, int opType, const int* path, int pathLen, const double* newVertPos,
                            int posRows);

@@ -49,7 +49,8 @@ _vp = ctypes.c_void_p
 class OptimizerConfig(ctypes.Structure):
     _fields_ = [("pcgTol", ctypes.c_double), ("pcgMaxIter", ctypes.c_int), ("relGL2Tol", ctypes.c_double),
                 ("lineSearchBatch", ctypes.c_int), ("timing", ctypes.c_int), ("linearSolver", ctypes.c_int),
-                ("scaffoldPattern", ctypes.c_int), ("hessianProjection", ctypes.c_int), ("ordering", ctypes.c_int)]
+                ("scaffoldPattern", ctypes.c_int), ("hessianProjection", ctypes.c_int), ("ordering", ctypes.c_int),
+                ("carryAnalysis", ctypes.c_int)]
 
 
 class OptCutsConfig(ctypes.Structure):
@@ -122,6 +123,7 @@ _SIGS = {
     "oc_topo_result_candidate": [_vp, ctypes.c_int, _d, _d, _i, _i, _d, _i],
     "oc_topo_result_destroy": [_vp],
     "oc_topo_result_air": [_vp, _i, _i, _i, _i],
+    "oc_optimizer_analysis_info": [_vp, _i, _d, _d, _d, _d],
     "oc_air_loop_mesh": [_vp, ctypes.c_int, ctypes.c_int, _i, _vp, _i, _vp, _i],
     "oc_topo_result_iterations": [_vp, _i, _i, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_create_fracture": [_vp, ctypes.c_int, _i, ctypes.c_int, _d, ctypes.c_int],
@@ -1023,6 +1025,17 @@ class Optimizer:
         self.ctx.check(lib().oc_optimizer_create_fracture(self.h, op, _pi(path), len(path), _pd(pos), len(pos)),
                        "createFracture")
         self.data._sync_topology()
+
+    def analysisInfo(self):
+        """The direct solver's last symbolic analysis: carried analyses since
+        the last full one (0: full), host ms of the dissection and of the
+        front structures, factor flops and those of the last full analysis."""
+        c = ctypes.c_int()
+        d = [ctypes.c_double() for _ in range(4)]
+        self.ctx.check(lib().oc_optimizer_analysis_info(self.h, ctypes.byref(c), *(ctypes.byref(x) for x in d)),
+                       "analysisInfo")
+        return {"carried": c.value, "nd_ms": d[0].value, "sym_ms": d[1].value, "flops": d[2].value,
+                "full_flops": d[3].value}
 
     def applyTiming(self):
         """Phase durations (ms) of the last createFracture: mesh edit, device

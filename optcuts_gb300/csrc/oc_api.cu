@@ -17,7 +17,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <array>
 #include <new>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -54,6 +56,11 @@ struct oc_mesh {
     // fracture tails (TriMesh::curFracTail, curInteriorFracTails), kept by
     // the applied operations for fracture propagation
     int tails[3] = {-1, -1, -1};
+    // the last topology operations' effect on the vertex ids, by the
+    // topoVersion each produced: {version, kind, x, y, nV before} (kind 0:
+    // copies of x (and y) appended; 1: y merged into x, the last vertex
+    // moved into y's slot) -- what an incremental symbolic analysis needs
+    std::vector<std::array<long long, 5>> editLog;
 };
 
 struct oc_linsys {
@@ -70,6 +77,11 @@ struct oc_linsys {
     oc::CholPlan chol;
     // last set_pattern: host pattern + symbolic analysis, device allocation + upload (ms)
     double patternHostMs = 0.0, patternDevMs = 0.0;
+    // the mesh state the plan was analysed for: its topoVersion, mesh
+    // vertex count (the system's first vertices) and whether the plan's
+    // root front is a scaffold clique
+    unsigned long long analyzedVersion = ~0ULL;
+    int analyzedMeshNV = 0;
 };
 
 struct oc_optimizer {
@@ -460,10 +472,132 @@ void free_bsr(oc::DeviceBsr& b)
 // mask: fixed rows for the pattern (diagonal only); rowFixed (optional):
 // the fixed rows for the values where they differ (rows kept in the pattern
 // but assembled as fixed, e.g. the padding slots of a scaffold clique)
+// The dissection tree of the plan last analysed, carried through the
+// topology operations applied since (edits: {version, kind, x, y, nV
+// before}, in order): a copy joins its source vertex's node, a merged
+// vertex the lowest common ancestor of the two nodes (a node above both
+// separates everything they did), the last vertex moved into a removed
+// slot keeps its node; system vertices past the mesh's (the scaffold's air
+// slots) and the clique (scaffold boundary and air) go to the root node,
+// which every other node descends from; nodes left empty are spliced out.
+// Every separator of the old tree still separates the new pattern, so the
+// front structures follow without a new dissection.  False when the tree
+// cannot be carried (no root where a clique now needs one, two merged
+// vertices in different trees).
+bool carry_dissection(const oc::CholPlan& P, int oldMeshNV, const std::vector<std::array<long long, 5>>& edits,
+                      int newMeshNV, int nSys, const std::vector<int>* clique, std::vector<oc::NdNode>& out,
+                      int& rootNode)
+{
+    const int nOld = static_cast<int>(P.nd.size());
+    if (nOld == 0 || (clique != nullptr) != (P.ndRoot >= 0)) return false;
+    std::vector<int> parent(nOld, -1);
+    for (int f = 0; f < nOld; ++f)
+        for (int c : P.nd[f].children) parent[c] = f;
+    std::vector<int> nodeOf(P.nV, -1);
+    std::vector<long long> key(P.nV, 0);
+    long long k = 0;
+    for (int f = 0; f < nOld; ++f)
+        for (int v : P.nd[f].S) {
+            if (v < 0 || v >= P.nV) return false;
+            nodeOf[v] = f;
+            key[v] = k++;
+        }
+    if (oldMeshNV > P.nV) return false;
+    std::vector<int> mn(nodeOf.begin(), nodeOf.begin() + oldMeshNV);
+    std::vector<long long> mk(key.begin(), key.begin() + oldMeshNV);
+    const int root = P.ndRoot;
+    auto lca = [&](int x, int y) {
+        for (int guard = 0; x != y && guard <= 2 * nOld; ++guard) {
+            if (x < 0 || y < 0) return -1;
+            if (x < y) x = parent[x];
+            else y = parent[y];
+        }
+        return x == y ? x : -1;
+    };
+    for (const auto& e : edits) {
+        const int n = static_cast<int>(mn.size());
+        if (e[4] != n) return false;
+        if (e[1] == 0) {
+            for (int j = 2; j <= 3; ++j) {
+                const long long src = e[j];
+                if (src < 0) continue;
+                if (src >= n) return false;
+                mn.push_back(mn[src]);
+                mk.push_back(k++);
+            }
+        }
+        else {
+            const long long a = e[2], b = e[3];
+            if (a < 0 || b < 0 || a >= n || b >= n) return false;
+            const int na = mn[a], nb = mn[b];
+            int m = (na == root || nb == root) ? root : lca(na, nb);
+            if (m < 0) return false;
+            mn[a] = m;
+            const int back = n - 1;
+            if (b < back) {
+                mn[b] = mn[back];
+                mk[b] = mk[back];
+            }
+            mn.pop_back();
+            mk.pop_back();
+        }
+    }
+    if (static_cast<int>(mn.size()) != newMeshNV || nSys < newMeshNV) return false;
+    std::vector<int> node(nSys, root);
+    std::vector<long long> vkey(nSys, 0);
+    for (int v = 0; v < newMeshNV; ++v) {
+        node[v] = mn[v];
+        vkey[v] = mk[v];
+    }
+    for (int v = newMeshNV; v < nSys; ++v) vkey[v] = k++;
+    std::vector<char> inClique(nSys, 0);
+    if (clique)
+        for (int v : *clique) {
+            if (v < 0 || v >= nSys) return false;
+            node[v] = root;
+            inClique[v] = 1;
+        }
+    for (int v = 0; v < nSys; ++v)
+        if (node[v] < 0) return false;
+    // vertices per node, in their old elimination order (the root: the
+    // clique's order, then the vertices that stayed there)
+    std::vector<std::vector<int>> S(nOld);
+    std::vector<int> ord(nSys);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return vkey[x] < vkey[y]; });
+    for (int v : ord)
+        if (!inClique[v]) S[node[v]].push_back(v);
+    if (clique) {
+        std::vector<int> rs(clique->begin(), clique->end());
+        rs.insert(rs.end(), S[root].begin(), S[root].end());
+        S[root].swap(rs);
+    }
+    // splice out empty nodes (not the root); renumber in postorder
+    std::vector<int> newIdx(nOld, -1);
+    int nNew = 0;
+    for (int f = 0; f < nOld; ++f)
+        if (!S[f].empty() || f == root) newIdx[f] = nNew++;
+    auto keptParent = [&](int f) {
+        int p = parent[f];
+        while (p >= 0 && newIdx[p] < 0) p = parent[p];
+        return p;
+    };
+    out.assign(nNew, oc::NdNode{});
+    for (int f = 0; f < nOld; ++f) {
+        if (newIdx[f] < 0) continue;
+        out[newIdx[f]].S.swap(S[f]);
+        const int p = keptParent(f);
+        if (p >= 0) out[newIdx[p]].children.push_back(newIdx[f]);
+    }
+    rootNode = root >= 0 ? newIdx[root] : -1;
+    return true;
+}
+
 int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::vector<unsigned char>& mask,
                        const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr,
                        const double* xy = nullptr, const std::vector<unsigned char>* rowFixed = nullptr,
-                       const int* nbPtr = nullptr, const int* nbIdx = nullptr)
+                       const int* nbPtr = nullptr, const int* nbIdx = nullptr,
+                       const std::vector<oc::NdNode>* carried = nullptr, int carriedRoot = -1)
 {
     oc_ctx* ctx = ls->ctx;
     auto t = std::chrono::steady_clock::now();
@@ -510,7 +644,22 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
         // analyze_pattern (EigenLibSolver.cpp:71-77): symbolic factorisation;
         // a clique (scaffold boundary + air vertices) is eliminated last
         ls->patternDevMs += ms_since(t);
-        oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique, xy);
+        bool done = false;
+        if (carried) {
+            // the carried dissection tree: front structures only; a full
+            // analysis when it does not separate the pattern, after 64
+            // carried analyses, or once the factor cost grew 30% over the
+            // last full analysis's
+            const double full = ls->chol.fullFlops;
+            if (ls->chol.incremental < 64 && full > 0.0) {
+                ++ls->chol.incremental;
+                ls->chol.ndMs = 0.0;
+                oc::chol_analyze_nodes(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), *carried, carriedRoot);
+                ls->chol.nd = *carried;
+                done = ls->chol.valid && ls->chol.flops <= 1.3 * full;
+            }
+        }
+        if (!done) oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique, xy);
         ls->patternHostMs += ms_since(t);
         std::string err;
         int rc = oc::chol_upload(ls->chol, &err);
@@ -842,7 +991,9 @@ static int apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, 
     std::vector<double> Vrest(m->Vrest);
     std::string err;
     int tails[3] = {m->tails[0], m->tails[1], m->tails[2]};
-    int rc = oc::topo_apply(opType, path, pathLen, newVertPos, posRows, F, Vrest, uv, cohE, &err, tails);
+    int edit[3] = {-1, -1, -1};
+    const int nV0 = m->d.nV;
+    int rc = oc::topo_apply(opType, path, pathLen, newVertPos, posRows, F, Vrest, uv, cohE, &err, tails, edit);
     if (rc) return fail(m->ctx, rc, err);
     std::copy(tails, tails + 3, m->tails);
     m->F.swap(F);
@@ -851,6 +1002,10 @@ static int apply_topology(oc_mesh* m, int opType, const int* path, int pathLen, 
     if (ms2) ms2[0] = ms_since(t);
     rc = mesh_rebuild(m, uv);
     if (ms2) ms2[1] = ms_since(t);
+    if (rc == OC_OK && edit[0] >= 0) {
+        if (m->editLog.size() >= 1024) m->editLog.erase(m->editLog.begin(), m->editLog.begin() + 512);
+        m->editLog.push_back({static_cast<long long>(m->topoVersion), edit[0], edit[1], edit[2], nV0});
+    }
     return rc;
 }
 
@@ -1600,6 +1755,7 @@ int oc_optimizer_default_config(oc_optimizer_config* c)
     c->scaffoldPattern = 0;
     c->hessianProjection = OC_HESSIAN_JACOBI6;
     c->ordering = OC_ORDER_AUTO;
+    c->carryAnalysis = 1;
     return OC_OK;
 }
 
@@ -1721,12 +1877,33 @@ static int compute_energy(oc_optimizer* o, const double2* uv, const double2* dir
 // reference re-analyses every iteration).
 static constexpr int kCliqueMax = 512;
 
+// The dissection tree of the solver's last analysis carried through the
+// topology operations applied since (false: analyse from scratch).
+static bool carried_tree(oc_optimizer* o, int nSys, const std::vector<int>* clique, std::vector<oc::NdNode>& out,
+                         int& root)
+{
+    oc_mesh* m = o->mesh;
+    oc_linsys* ls = o->ls;
+    if (!o->cfg.carryAnalysis || ls->kind != OC_SOLVER_DIRECT || ls->analyzedVersion == ~0ULL ||
+        ls->analyzedVersion > m->topoVersion || (o->scaf && !o->cliqueMode))
+        return false;
+    std::vector<std::array<long long, 5>> edits;
+    for (const auto& e : m->editLog)
+        if (static_cast<unsigned long long>(e[0]) > ls->analyzedVersion) edits.push_back(e);
+    if (edits.size() != m->topoVersion - ls->analyzedVersion) return false;
+    for (size_t i = 0; i < edits.size(); ++i)
+        if (static_cast<unsigned long long>(edits[i][0]) != ls->analyzedVersion + 1 + i) return false;
+    return carry_dissection(ls->chol, ls->analyzedMeshNV, edits, m->d.nV, nSys, clique, out, root);
+}
+
 static int ensure_pattern(oc_optimizer* o)
 {
     oc_mesh* m = o->mesh;
     const int nV = m->d.nV;
     if (o->patternStale) {
         int rc;
+        std::vector<oc::NdNode> carried;
+        int carriedRoot = -1;
         // current positions of the system's vertices: the ordering's
         // geometric bisection reads them
         const int nXY = o->cfg.ordering == OC_ORDER_BFS ? 0 : (o->scaf ? o->nWhole : nV);
@@ -1740,7 +1917,9 @@ static int ensure_pattern(oc_optimizer* o)
         if (!o->scaf) {
             std::vector<unsigned char> mask(nV, 0);
             for (int v : m->fixed) mask[v] = 1;
-            rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask, nullptr, 0, nullptr, xyp);
+            const bool carry = carried_tree(o, nV, nullptr, carried, carriedRoot);
+            rc = linsys_set_pattern(o->ls, nV, m->F.data(), m->d.nF, mask, nullptr, 0, nullptr, xyp, nullptr,
+                                    nullptr, nullptr, carry ? &carried : nullptr, carriedRoot);
         }
         else {
             // rowFixed: 1 = fixed mesh vertex or unused air slot, 2 = fixed in
@@ -1759,15 +1938,21 @@ static int ensure_pattern(oc_optimizer* o)
                 for (int v = nV; v < o->nWhole; ++v) clique.push_back(v);
                 std::vector<unsigned char> pmask(mask);
                 for (int v = o->nWholeReal; v < o->nWhole; ++v) pmask[v] = 0;
+                const bool carry = carried_tree(o, o->nWhole, &clique, carried, carriedRoot);
                 rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, pmask, nullptr, 0, &clique, xyp,
-                                        &mask);
+                                        &mask, nullptr, nullptr, carry ? &carried : nullptr, carriedRoot);
             }
             else {
                 rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, o->airFw.data(),
                                         static_cast<int>(o->airFw.size() / 3), nullptr, xyp);
             }
         }
-        if (rc) return rc;
+        if (rc) {
+            o->ls->analyzedVersion = ~0ULL;
+            return rc;
+        }
+        o->ls->analyzedVersion = m->topoVersion;
+        o->ls->analyzedMeshNV = nV;
         o->patternStale = false;
         o->airContribStale = o->scaf;
     }
@@ -2311,6 +2496,19 @@ int oc_optimizer_create_fracture(oc_optimizer* o, int opType, const int* path, i
     rc = compute_energy(o, current_uv(o), nullptr, nullptr, 1, &o->lastEnergyVal, &o->eScaf);
     o->applyMs[5] = ms_since(t);
     return rc;
+}
+
+int oc_optimizer_analysis_info(oc_optimizer* o, int* carried, double* ndMs, double* symMs, double* flops,
+                               double* fullFlops)
+{
+    if (!o || !o->ls) return OC_ERR_INVALID;
+    const oc::CholPlan& P = o->ls->chol;
+    if (carried) *carried = P.incremental;
+    if (ndMs) *ndMs = P.ndMs;
+    if (symMs) *symMs = P.symMs;
+    if (flops) *flops = P.flops;
+    if (fullFlops) *fullFlops = P.fullFlops;
+    return OC_OK;
 }
 
 int oc_optimizer_apply_timing(oc_optimizer* o, double* out6)

@@ -27,6 +27,8 @@
 
 #include "oc_chol.h"
 
+#include <chrono>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -41,11 +43,6 @@ namespace oc {
 
 // ------------------------------------------------------------------ symbolic
 namespace {
-
-struct NdNode {
-    std::vector<int> S;
-    std::vector<int> children;
-};
 
 // Nested dissection of `verts` by BFS level sets from a pseudo-peripheral
 // vertex, into `nodes` in postorder (children first, the separator last;
@@ -223,9 +220,8 @@ constexpr long long kUpdSplitBlocks = 8 * 152;
 void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize,
                   const std::vector<int>* rootVerts, const double* xy)
 {
+    const auto t0 = std::chrono::steady_clock::now();
     P = CholPlan{};
-    P.nV = nV;
-    P.nDof = 2 * nV;
     // the bisection needs an order on the coordinates: BFS alone unless all are finite
     if (xy)
         for (long long i = 0; i < 2LL * nV; ++i)
@@ -263,6 +259,30 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
         }
     }
     if (rootVerts && !rootVerts->empty()) nodes.push_back(NdNode{*rootVerts, roots});
+    const int rootNode = (rootVerts && !rootVerts->empty()) ? static_cast<int>(nodes.size()) - 1 : -1;
+    const double ndMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    chol_analyze_nodes(P, nV, rowPtr, col, nodes, rootNode);
+    P.nd.swap(nodes);
+    P.ndMs = ndMs;
+    P.fullFlops = P.flops;
+    P.incremental = 0;
+}
+
+void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, const std::vector<NdNode>& nodes,
+                        int rootNode)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    {
+        const double ndMs = P.ndMs, fullFlops = P.fullFlops;
+        const int inc = P.incremental;
+        P = CholPlan{};
+        P.ndMs = ndMs;
+        P.fullFlops = fullFlops;
+        P.incremental = inc;
+    }
+    P.nV = nV;
+    P.nDof = 2 * nV;
+    P.ndRoot = rootNode;
     // nodes are created children-first: creation order is a postorder
     const int nF = static_cast<int>(nodes.size());
     P.nFronts = nF;
@@ -509,6 +529,7 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
             }
     });
     if (bad) P.valid = false;
+    P.symMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 // ------------------------------------------------------------------ kernels

@@ -19,6 +19,14 @@ constexpr int kRectCols = 8;   // columns of L21 per CTA in the backward GEMV^T 
 constexpr int kNarrowK = 64;
 constexpr int kNarrowRows = 256;
 
+// One node of the nested-dissection tree: its vertices (a separator, a
+// leaf, or the forced root set) and its children (node indices; nodes are
+// kept in postorder, children first).
+struct NdNode {
+    std::vector<int> S;
+    std::vector<int> children;
+};
+
 struct TileTask {           // one CTA's work item in a tiled front kernel
     int front, i, j, p;
 };
@@ -26,6 +34,15 @@ struct TileTask {           // one CTA's work item in a tiled front kernel
 struct CholPlan {
     // ---- host symbolic data ----
     int nV = 0, nDof = 0, nFronts = 0, nLevels = 0;
+    // the dissection tree the fronts come from (postorder; ndRoot: the
+    // forced-root node, -1 without one), kept for incremental analyses;
+    // fullFlops: the factor flops of the last full analysis, incremental:
+    // incremental analyses since then
+    std::vector<NdNode> nd;
+    int ndRoot = -1;
+    double fullFlops = 0.0;
+    int incremental = 0;
+    double ndMs = 0.0, symMs = 0.0;   // host time of the last analysis: dissection, front structures
     bool valid = true;                   // every index map resolved (checked before upload)
     std::vector<int> vertOrder;          // elimination order of vertices
     std::vector<int> permDof;            // permuted DOF -> original DOF
@@ -94,6 +111,12 @@ struct CholPlan {
 // roots.
 void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize = 16,
                   const std::vector<int>* rootVerts = nullptr, const double* xy = nullptr);
+// The front structures of a given dissection tree (nodes in postorder,
+// rootNode the forced-root node or -1): everything chol_analyze does after
+// its dissection.  P.valid is false when the tree does not separate the
+// pattern (a child's update row missing from its parent front).
+void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, const std::vector<NdNode>& nodes,
+                        int rootNode);
 int chol_upload(CholPlan& P, std::string* err);
 void chol_free(CholPlan& P);
 // Numeric factorisation of the block-CSR values (FP32 storage, FP64 fronts).

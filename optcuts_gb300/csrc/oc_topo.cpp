@@ -1040,7 +1040,7 @@ void replace_in(std::vector<int>& F, const std::vector<int>& tris, int from, int
 
 int topo_apply(int opType, const int* path, int pathLen, const double* pos, int posRows, std::vector<int>& F,
                std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err,
-               int* tails)
+               int* tails, int* edit)
 {
     auto bad = [&](const char* m) {
         if (err) *err = m;
@@ -1079,6 +1079,11 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
         if (both) walk_edge(T, vi, vb, true, sepI, bEi);
         auto idx = coh_index(cohE);
         const int nb = push_vertex(vb, pos + 2);
+        if (edit) {
+            edit[0] = 0;
+            edit[1] = vb;
+            edit[2] = both ? vi : -1;
+        }
         UV[2 * (size_t)vb] = pos[0];
         UV[2 * (size_t)vb + 1] = pos[1];
         replace_in(F, sepB, vb, nb);
@@ -1128,6 +1133,11 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
             if (vNew == path[0]) return bad("interior split: not a valid path");
         }
         const int nn = push_vertex(vI, pos);
+        if (edit) {
+            edit[0] = 0;
+            edit[1] = vI;
+            edit[2] = -1;
+        }
         UV[2 * (size_t)vI] = pos[2];
         UV[2 * (size_t)vI + 1] = pos[3];
         replace_in(F, left, vI, nn);
@@ -1150,6 +1160,11 @@ int topo_apply(int opType, const int* path, int pathLen, const double* pos, int 
         int* ci = coh_find(idx, path[0], path[1]);
         if (!ci) return bad("merge: the edge is not a cohesive edge");
         const int cRow = *ci;
+        if (edit) {
+            edit[0] = 1;
+            edit[1] = a;
+            edit[2] = b;
+        }
         UV[2 * (size_t)a] = pos[0];
         UV[2 * (size_t)a + 1] = pos[1];
         const int back = nV - 1;

@@ -164,9 +164,12 @@ int mlp_predict_host(Mlp& m, const float* X, int n, float* y);
 // splitEdgeOnBoundary (TriMesh.cpp:2891-2899), an interior split through
 // createFracture / splitOrMerge (Optimizer.cpp:397-399, TriMesh.cpp:1039-1043)
 // and mergeBoundaryEdges (TriMesh.cpp:3046-3048, 3169-3171) do.
+// edit (optional, out): what happened to the vertex ids -- {0, src0, src1}:
+// vertices appended, copies of src0 (and src1, -1 if none); {1, a, b}: b
+// merged into a, then the last vertex moved into b's slot
 int topo_apply(int opType, const int* path, int pathLen, const double* newVertPos, int posRows, std::vector<int>& F,
                std::vector<double>& Vrest, std::vector<double>& UV, std::vector<int>& cohE, std::string* err,
-               int* tails = nullptr);
+               int* tails = nullptr, int* edit = nullptr);
 
 // igl::cut_to_disk as the reference vendors it (src/Utils/cut_to_disk.cpp):
 // the cut graph of a genus >= 1 surface as vertex lists (a closed loop
