@@ -133,6 +133,142 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
     }
 }
 
+// Eigen-decomposition of a symmetric 6x6 to FP64 accuracy with a fraction
+// of the FP64 instructions of jacobi_eig6: cyclic Jacobi in FP32 on the
+// matrix scaled by its largest entry (a starting basis; FP32 instructions
+// are 64x cheaper on GB300), that basis made orthonormal in FP64 (modified
+// Gram-Schmidt), A rotated into it, then FP64 cyclic Jacobi sweeps on the
+// nearly diagonal result until the off-diagonal mass reaches the rounding
+// floor, each rotation updating only the entries it changes.  Only IEEE
+// operations (division, square root) so that a host restatement compiled
+// without contraction rounds identically.  On return A's diagonal holds the
+// eigenvalues and V the eigenvectors as columns.
+__device__ void eig6_mixed(double A[6][6], double V[6][6])
+{
+    double s = 0.0;
+    bool finite = true;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            finite = finite && isfinite(A[i][j]);
+            s = fmax(s, fabs(A[i][j]));
+        }
+    if (!finite || !(s > 0.0)) {
+        jacobi_eig6(A, V);
+        return;
+    }
+    float Af[6][6], Vf[6][6];
+    const double inv = 1.0 / s;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            Af[i][j] = static_cast<float>(A[i][j] * inv);
+            Vf[i][j] = (i == j) ? 1.0f : 0.0f;
+        }
+    {
+        float fro = 0.0f;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) fro += Af[i][j] * Af[i][j];
+        float prevOff = 0.0f;
+        for (int sweep = 0; sweep < 30; ++sweep) {
+            float off = 0.0f;
+            for (int p = 0; p < 6; ++p)
+                for (int q = p + 1; q < 6; ++q) off += Af[p][q] * Af[p][q];
+            if (off <= 1e-14f * fro || (sweep > 0 && off >= prevOff)) break;
+            prevOff = off;
+            for (int p = 0; p < 6; ++p)
+                for (int q = p + 1; q < 6; ++q) {
+                    const float apq = Af[p][q];
+                    if (apq == 0.0f) continue;
+                    const float theta = (Af[q][q] - Af[p][p]) / (2.0f * apq);
+                    const float t = (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+                    const float c = 1.0f / sqrtf(t * t + 1.0f), sn = t * c;
+                    for (int k = 0; k < 6; ++k) {
+                        const float akp = Af[k][p], akq = Af[k][q];
+                        Af[k][p] = c * akp - sn * akq;
+                        Af[k][q] = sn * akp + c * akq;
+                    }
+                    for (int k = 0; k < 6; ++k) {
+                        const float apk = Af[p][k], aqk = Af[q][k];
+                        Af[p][k] = c * apk - sn * aqk;
+                        Af[q][k] = sn * apk + c * aqk;
+                    }
+                    for (int k = 0; k < 6; ++k) {
+                        const float vkp = Vf[k][p], vkq = Vf[k][q];
+                        Vf[k][p] = c * vkp - sn * vkq;
+                        Vf[k][q] = sn * vkp + c * vkq;
+                    }
+                }
+        }
+    }
+    double Q[6][6];
+    for (int c = 0; c < 6; ++c) {
+        double v[6];
+        for (int r = 0; r < 6; ++r) v[r] = static_cast<double>(Vf[r][c]);
+        for (int p = 0; p < c; ++p) {
+            double d = 0.0;
+            for (int r = 0; r < 6; ++r) d = d + Q[r][p] * v[r];
+            for (int r = 0; r < 6; ++r) v[r] = v[r] - d * Q[r][p];
+        }
+        double n2 = 0.0;
+        for (int r = 0; r < 6; ++r) n2 = n2 + v[r] * v[r];
+        const double in = 1.0 / sqrt(n2);
+        for (int r = 0; r < 6; ++r) Q[r][c] = v[r] * in;
+    }
+    double T[6][6];
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) {
+            double acc = 0.0;
+            for (int k = 0; k < 6; ++k) acc = acc + A[r][k] * Q[k][c];
+            T[r][c] = acc;
+        }
+    for (int r = 0; r < 6; ++r)
+        for (int c = r; c < 6; ++c) {
+            double acc = 0.0;
+            for (int k = 0; k < 6; ++k) acc = acc + Q[k][r] * T[k][c];
+            A[r][c] = acc;
+        }
+    for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < r; ++c) A[r][c] = A[c][r];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) V[i][j] = Q[i][j];
+    double fro = 0.0;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) fro = fro + A[i][j] * A[i][j];
+    double prevOff = 0.0;
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 6; ++p)
+            for (int q = p + 1; q < 6; ++q) off = off + A[p][q] * A[p][q];
+        if (off <= 1e-34 * fro || (sweep > 0 && off >= prevOff)) break;
+        prevOff = off;
+        for (int p = 0; p < 6; ++p)
+            for (int q = p + 1; q < 6; ++q) {
+                const double apq = A[p][q];
+                if (apq == 0.0) continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                A[p][p] = A[p][p] - t * apq;
+                A[q][q] = A[q][q] + t * apq;
+                A[p][q] = 0.0;
+                A[q][p] = 0.0;
+                for (int k = 0; k < 6; ++k) {
+                    if (k == p || k == q) continue;
+                    const double akp = A[k][p], akq = A[k][q];
+                    const double np = c * akp - sn * akq, nq = sn * akp + c * akq;
+                    A[k][p] = np;
+                    A[p][k] = np;
+                    A[k][q] = nq;
+                    A[q][k] = nq;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+}
+
 __device__ __forceinline__ double recip_sqrt(double x) { return rsqrt(x); }
 __device__ __forceinline__ float recip_sqrt(float x) { return rsqrtf(x); }
 
@@ -413,7 +549,7 @@ __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, do
     double A[6][6], V[6][6];
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) A[i][j] = H[i][j];
-    jacobi_eig6(A, V);
+    eig6_mixed(A, V);
     double lam[6], lmin = A[0][0];
     for (int i = 0; i < 6; ++i) {
         lam[i] = A[i][i];
