@@ -353,6 +353,7 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
         qb, qm, qi = qs
         out = {"query_ms": qb["query_ms"], "gpu_solve_ms": qb["solve_ms"], "probe_ms": qb["probe_ms"],
                "exact_ms": qb["exact_ms"],
+               "host_ms": {k: round(v, 3) for k, v in qb["host_ms"].items()},
                "host_build_ms": {name: q["build_ms"] for name, q in
                                  zip(("boundary_split", "merge", "interior_split"), qs)},
                "local_problems": sum(q["local_problems"] for q in qs),
@@ -464,6 +465,8 @@ def topology_section(args, oc, ctx, opt, mesh, st, rank):
         topo["apply"] = {"value": time.perf_counter() - t1, "unit": "s",
                          "op": {0: "boundary_split", 1: "interior_split", 2: "merge"}[op], "EwDec": ew,
                          "phases_ms": {k: round(v, 2) for k, v in opt.applyTiming().items()},
+                         "analysis": {k: (round(v, 2) if isinstance(v, float) and k.endswith("_ms") else v)
+                                      for k, v in opt.analysisInfo().items()},
                          "what": "Optimizer::createFracture: mesh edit, device mesh, Newton pattern and analysis, "
                                  "scaffold, energy"}
     return topo

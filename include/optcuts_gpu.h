@@ -146,6 +146,14 @@ int oc_linsys_set_type(oc_linsys* ls, int solverKind);
 /* analyze_pattern() (EigenLibSolver.cpp:71-77): symbolic factorisation
  * (nested dissection, front structure); set_pattern runs it implicitly. */
 int oc_linsys_analyze_pattern(oc_linsys* ls);
+/* No reference counterpart (a launch choice of the direct solver): the
+ * largest thread-block cluster (1..8 CTAs) per front that the substitutions
+ * of the top tree levels use; 1 keeps one CTA per front everywhere.  The
+ * solution is the same bits for every value.  Default 8. */
+int oc_linsys_set_solve_cluster(oc_linsys* ls, int maxCluster);
+/* Tree levels of the current plan whose substitutions run as clusters, and
+ * the largest cluster size among them (1 when none). */
+int oc_linsys_solve_clusters(oc_linsys* ls, int* levels, int* largest);
 /* Symbolic statistics of the direct solver: out[0..7] = fronts, tree levels,
  * largest front rows, front pool doubles, factor flops, tiled launches,
  * factor entries (sum of m*k), DOF. */
@@ -260,6 +268,10 @@ int oc_optimizer_phase_ms(oc_optimizer* opt, double* out7);
 int oc_optimizer_launch_count(oc_optimizer* opt, long long* launches);
 /* oc_linsys_stats of the optimizer's own solver (after precompute). */
 int oc_optimizer_solver_stats(oc_optimizer* opt, double* out8);
+/* oc_linsys_set_solve_cluster on the optimizer's own solver. */
+int oc_optimizer_set_solve_cluster(oc_optimizer* opt, int maxCluster);
+/* oc_linsys_solve_clusters on the optimizer's own solver. */
+int oc_optimizer_solve_clusters(oc_optimizer* opt, int* levels, int* largest);
 
 /* ---- Scaffold (Scaffold.hpp:18-70; Optimizer.cpp scaffolding branches) ---
  * Replaces `scaffold = Scaffold(result, UV_bnds, E, bnd)` (Optimizer.cpp:
@@ -373,6 +385,11 @@ int oc_topo_result_features(const oc_topo_result* r, int* nRows, float* X, float
 /* learned queries: problems solved exactly, ms of the one-step pass and of
  * the exact solves */
 int oc_topo_result_timing(const oc_topo_result* r, int* nSelected, double* probeMs, double* exactMs);
+/* host phases of the query's step (ms, shared by the operations queried
+ * together): out4 = inputs (positions, split filter, adjacency, air-mesh
+ * copies), air-loop sources, ranking (features, MLP, selection; learned
+ * queries), candidate lists */
+int oc_topo_result_host_phases(const oc_topo_result* r, double* out4);
 /* per local problem: its candidate, its exact E_w decrease (NaN where the
  * learned proposal did not solve it) and the predicted decrease (learned
  * queries; else NaN), on the candidates' scale (interior splits halved):

@@ -108,6 +108,11 @@ _SIGS = {
     "oc_optimizer_phase_ms": [_vp, _d],
     "oc_optimizer_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
     "oc_optimizer_solver_stats": [_vp, _d],
+    "oc_optimizer_set_solve_cluster": [_vp, ctypes.c_int],
+    "oc_linsys_set_solve_cluster": [_vp, ctypes.c_int],
+    "oc_topo_result_host_phases": [_vp, _d],
+    "oc_linsys_solve_clusters": [_vp, _i, _i],
+    "oc_optimizer_solve_clusters": [_vp, _i, _i],
     "oc_optimizer_set_scaffold": [_vp, _d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double],
     "oc_optimizer_clear_scaffold": [_vp],
     "oc_optimizer_rebuild_scaffold": [_vp],
@@ -415,6 +420,8 @@ class TriMesh:
             lib().oc_topo_result_iterations(h, ctypes.byref(tot), ctypes.byref(cap), ctypes.byref(tri))
             nsel, pms, ems = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
             lib().oc_topo_result_timing(h, ctypes.byref(nsel), ctypes.byref(pms), ctypes.byref(ems))
+            hph = np.zeros(4)
+            lib().oc_topo_result_host_phases(h, _pd(hph))
             X = tgt = prd = None
             if features or mlp is not None:
                 nrow = ctypes.c_int()
@@ -457,6 +464,7 @@ class TriMesh:
                 "solve_ms": sms.value, "local_iters_total": tot.value, "local_capped": cap.value,
                 "local_trials_total": tri.value, "selected": nsel.value, "probe_ms": pms.value,
                 "exact_ms": ems.value, "features": X, "target": tgt, "predicted": prd,
+                "host_ms": dict(zip(("prep", "air", "rank", "finish"), hph.tolist())),
                 "problems": dict(cand=pc, EwDec=pe, EwDec_pred=pp, **pstat), "query_ms": query_ms,
                 "air": {"problems": ap.value, "rejected": ar.value, "steiner_max": asx.value, "capped": acap.value}}
 
@@ -592,6 +600,17 @@ class LinSysSolver:
         out = np.zeros(8)
         self.ctx.check(lib().oc_linsys_stats(self.h, _pd(out)), "stats")
         return symbolic_stats_dict(out)
+
+    def set_solve_cluster(self, maxCluster):
+        """Largest thread-block cluster per front (1..8) in the direct
+        solver's substitutions; the solution is the same bits for every value."""
+        self.ctx.check(lib().oc_linsys_set_solve_cluster(self.h, int(maxCluster)), "set_solve_cluster")
+
+    def solve_clusters(self):
+        """(tree levels whose substitutions run as clusters, largest cluster)"""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().oc_linsys_solve_clusters(self.h, ctypes.byref(a), ctypes.byref(b)), "solve_clusters")
+        return a.value, b.value
 
     def factorize(self):
         return self.ctx.check(lib().oc_linsys_factorize(self.h), "factorize") == OC_OK
@@ -1138,6 +1157,16 @@ class Optimizer:
         out = np.zeros(8)
         self.ctx.check(lib().oc_optimizer_solver_stats(self.h, _pd(out)), "solver_stats")
         return symbolic_stats_dict(out)
+
+    def set_solve_cluster(self, maxCluster):
+        """LinSysSolver.set_solve_cluster on this optimizer's own solver."""
+        self.ctx.check(lib().oc_optimizer_set_solve_cluster(self.h, int(maxCluster)), "set_solve_cluster")
+
+    def solve_clusters(self):
+        """LinSysSolver.solve_clusters on this optimizer's own solver."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_solve_clusters(self.h, ctypes.byref(a), ctypes.byref(b)), "solve_clusters")
+        return a.value, b.value
 
     def launch_count(self):
         n = ctypes.c_longlong()

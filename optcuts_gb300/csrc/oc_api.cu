@@ -1088,6 +1088,7 @@ static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_
                             int nCandVerts = 0, int mergeFork = -2, int shardRank = 0, int shardCount = 1)
 {
     if (!m || !out || nOps <= 0) return OC_ERR_INVALID;
+    auto tPrep = std::chrono::steady_clock::now();
     bool split = false;
     for (int i = 0; i < nOps; ++i) {
         out[i] = nullptr;
@@ -1160,9 +1161,11 @@ static int topology_queries(oc_mesh* m, const int* ops, int nOps, double lambda_
     }
     std::vector<oc::TopoOpResult> res(nOps);
     std::string err;
+    const double prepMs = ms_since(tPrep);
     const int rc = oc::topo_query_ops(in, ops, nOps, lambda_t, filterExp > 0.0 ? filterExp : 0.6, opts, res.data(),
                                       &err);
     if (rc) return fail(m->ctx, rc, err);
+    for (int i = 0; i < nOps; ++i) res[i].stats.prepMs = prepMs;
     for (int i = 0; i < nOps; ++i) {
         oc_topo_result* r = new (std::nothrow) oc_topo_result;
         if (!r) {
@@ -1336,6 +1339,16 @@ int oc_topo_result_timing(const oc_topo_result* r, int* nSelected, double* probe
     if (nSelected) *nSelected = r->stats.nSelected;
     if (probeMs) *probeMs = r->stats.probeMs;
     if (exactMs) *exactMs = r->stats.exactMs;
+    return OC_OK;
+}
+
+int oc_topo_result_host_phases(const oc_topo_result* r, double* out4)
+{
+    if (!r || !out4) return OC_ERR_INVALID;
+    out4[0] = r->stats.prepMs;
+    out4[1] = r->stats.airMs;
+    out4[2] = r->stats.rankMs;
+    out4[3] = r->stats.finishMs;
     return OC_OK;
 }
 
@@ -1556,6 +1569,21 @@ int oc_linsys_analyze_pattern(oc_linsys* ls)
     std::string err;
     int rc = oc::chol_upload(ls->chol, &err);
     return rc ? fail(ls->ctx, rc, err) : OC_OK;
+}
+
+int oc_linsys_set_solve_cluster(oc_linsys* ls, int maxCluster)
+{
+    if (!ls || maxCluster < 1 || maxCluster > 8) return OC_ERR_INVALID;
+    oc::chol_set_solve_cluster(ls->chol, maxCluster);
+    return OC_OK;
+}
+
+int oc_linsys_solve_clusters(oc_linsys* ls, int* levels, int* largest)
+{
+    if (!ls || !levels || !largest) return OC_ERR_INVALID;
+    *levels = ls->kind == OC_SOLVER_DIRECT ? oc::chol_solve_cluster_levels(ls->chol, largest) : 0;
+    if (ls->kind != OC_SOLVER_DIRECT) *largest = 1;
+    return OC_OK;
 }
 
 static void chol_stats(const oc::CholPlan& P, double* out)
@@ -2347,6 +2375,18 @@ int oc_optimizer_solver_stats(oc_optimizer* o, double* out8)
 {
     if (!o) return OC_ERR_INVALID;
     return oc_linsys_stats(o->ls, out8);
+}
+
+int oc_optimizer_set_solve_cluster(oc_optimizer* o, int maxCluster)
+{
+    if (!o) return OC_ERR_INVALID;
+    return oc_linsys_set_solve_cluster(o->ls, maxCluster);
+}
+
+int oc_optimizer_solve_clusters(oc_optimizer* o, int* levels, int* largest)
+{
+    if (!o) return OC_ERR_INVALID;
+    return oc_linsys_solve_clusters(o->ls, levels, largest);
 }
 
 int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, const int* airF, int nAirF,

@@ -162,7 +162,8 @@ void nd_build(const int* rowPtr, const int* col, std::vector<int>& verts, std::v
         return make_leaf();
     if (sep.empty() || (left.empty() && right.empty())) return make_leaf();
     // the two halves: each into its own node list, the larger of them on a
-    // second thread when both are big
+    // second thread when both are big (a thread of its own: the recursion
+    // measured slower on the host pool's workers)
     std::vector<NdNode> ln, rn;
     const bool par = depth < 6 && left.size() > kNdParallel && right.size() > kNdParallel;
     if (par) {
@@ -221,7 +222,11 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
                   const std::vector<int>* rootVerts, const double* xy)
 {
     const auto t0 = std::chrono::steady_clock::now();
-    P = CholPlan{};
+    {
+        const int cl = P.solveCluster;
+        P = CholPlan{};
+        P.solveCluster = cl;
+    }
     // the bisection needs an order on the coordinates: BFS alone unless all are finite
     if (xy)
         for (long long i = 0; i < 2LL * nV; ++i)
@@ -274,11 +279,12 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
     const auto t0 = std::chrono::steady_clock::now();
     {
         const double ndMs = P.ndMs, fullFlops = P.fullFlops;
-        const int inc = P.incremental;
+        const int inc = P.incremental, cl = P.solveCluster;
         P = CholPlan{};
         P.ndMs = ndMs;
         P.fullFlops = fullFlops;
         P.incremental = inc;
+        P.solveCluster = cl;
     }
     P.nV = nV;
     P.nDof = 2 * nV;
@@ -339,11 +345,12 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
                 B[f].assign(cand.begin(), cand.end());   // elimination positions, ascending
             }
         });
-    // fronts
-    P.fk.resize(nF); P.fm.resize(nF); P.fparent = parent; P.flevel.assign(nF, 0); P.fdofStart.resize(nF);
+    // fronts: sizes and offsets in one pass, then the row lists in parallel
+    P.fk.resize(nF); P.fm.resize(nF); P.fparent = parent; P.flevel = flev; P.fdofStart.resize(nF);
     P.foff.resize(nF); P.fupd.resize(nF); P.frowOff.resize(nF); P.relOff.resize(nF);
     P.childOff.assign(nF + 1, 0);
     long long pool = 0, upd = 0;
+    size_t rows = 0, rels = 0;
     for (int f = 0; f < nF; ++f) {
         const int ns = static_cast<int>(nodes[f].S.size());
         const int k = 2 * ns, m = 2 * (ns + static_cast<int>(B[f].size()));
@@ -354,27 +361,38 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
         pool += (long long)m * m;
         P.fupd[f] = upd;
         upd += m - k;
-        P.frowOff[f] = static_cast<int>(P.rowIdx.size());
-        for (int i = 0; i < ns; ++i) { P.rowIdx.push_back(2 * (vstart[f] + i)); P.rowIdx.push_back(2 * (vstart[f] + i) + 1); }
-        for (int u : B[f]) { P.rowIdx.push_back(2 * u); P.rowIdx.push_back(2 * u + 1); }
+        P.frowOff[f] = static_cast<int>(rows);
+        rows += m;
+        P.relOff[f] = static_cast<int>(rels);
+        if (parent[f] >= 0) rels += m - k;
         P.maxM = std::max(P.maxM, m);
-        int lv = 0;
-        for (int c : nodes[f].children) lv = std::max(lv, P.flevel[c] + 1);
-        P.flevel[f] = lv;
         P.childOff[f + 1] = P.childOff[f] + static_cast<int>(nodes[f].children.size());
         const double kk = k, mm = m, r = mm - kk;
         P.flops += kk * kk * kk / 3.0 + kk * kk * r + kk * r * r;
     }
     P.poolSize = pool;
     P.updSize = upd;
+    P.rowIdx.resize(rows);
+    host_parallel_for(nF, 256, [&](size_t f0, size_t f1) {
+        for (size_t f = f0; f < f1; ++f) {
+            int* out = P.rowIdx.data() + P.frowOff[f];
+            const int ns = static_cast<int>(nodes[f].S.size());
+            for (int i = 0; i < ns; ++i) {
+                *out++ = 2 * (vstart[f] + i);
+                *out++ = 2 * (vstart[f] + i) + 1;
+            }
+            for (int u : B[f]) {
+                *out++ = 2 * u;
+                *out++ = 2 * u + 1;
+            }
+        }
+    });
+    P.childList.resize(P.childOff[nF]);
     for (int f = 0; f < nF; ++f)
-        for (int c : nodes[f].children) P.childList.push_back(c);
+        std::copy(nodes[f].children.begin(), nodes[f].children.end(), P.childList.begin() + P.childOff[f]);
     // child update row -> parent row (both row lists ascending)
     std::atomic<int> bad{0};
-    for (int f = 0; f < nF; ++f) {
-        P.relOff[f] = static_cast<int>(P.relIdx.size());
-        if (parent[f] >= 0) P.relIdx.resize(P.relIdx.size() + (P.fm[f] - P.fk[f]));
-    }
+    P.relIdx.resize(rels);
     host_parallel_for(nF, 256, [&](size_t f0, size_t f1) {
         for (size_t f = f0; f < f1; ++f) {
             const int pf = parent[f];
@@ -408,8 +426,18 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
     }
     // launch schedule: per level, extend-add per child slot, the first
     // panel's diagonal tiles, then per panel the panel solve and the trailing
-    // update (whose first block also factors the next panel's diagonal tile)
-    for (int l = 0; l < P.nLevels; ++l) {
+    // update (whose first block also factors the next panel's diagonal tile).
+    // Levels are independent: each is built on its own host task, then the
+    // lists are joined in level order.
+    struct LevelSched {
+        std::vector<TileTask> tasks;
+        std::vector<CholPlan::Launch> launches;
+    };
+    std::vector<LevelSched> sched(P.nLevels);
+    host_run_tasks(P.nLevels, [&](size_t li) {
+        const int l = static_cast<int>(li);
+        std::vector<TileTask>& T = sched[l].tasks;
+        std::vector<CholPlan::Launch>& Ls = sched[l].launches;
         const int* lf = P.levelFronts.data() + P.levelFrontOff[l];
         const int nl = P.levelFrontOff[l + 1] - P.levelFrontOff[l];
         int maxKids = 0, maxPanels = 0;
@@ -419,27 +447,27 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
             maxPanels = std::max(maxPanels, (P.fk[f] + kTile - 1) / kTile);
         }
         for (int c = 0; c < maxKids; ++c) {
-            const int off = static_cast<int>(P.tasks.size());
+            const int off = static_cast<int>(T.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if (P.childOff[f + 1] - P.childOff[f] <= c) continue;
                 const int ch = P.childList[P.childOff[f] + c];
                 const int u = P.fm[ch] - P.fk[ch];
-                for (int j0 = 0; j0 < u; j0 += 16) P.tasks.push_back(TileTask{ch, f, j0, std::min(j0 + 16, u)});
+                for (int j0 = 0; j0 < u; j0 += 16) T.push_back(TileTask{ch, f, j0, std::min(j0 + 16, u)});
             }
-            const int cnt = static_cast<int>(P.tasks.size()) - off;
-            if (cnt) P.launches.push_back({0, l, 0, off, cnt, c});
+            const int cnt = static_cast<int>(T.size()) - off;
+            if (cnt) Ls.push_back({0, l, 0, off, cnt, c});
         }
         {   // the first panel's diagonal tiles (the later ones are factored
             // at the end of the previous panel's trailing update)
-            const int off = static_cast<int>(P.tasks.size());
+            const int off = static_cast<int>(T.size());
             for (int i = 0; i < nl; ++i)
-                if (P.fk[lf[i]] > 0) P.tasks.push_back(TileTask{lf[i], 0, 0, 0});
-            if ((int)P.tasks.size() > off) P.launches.push_back({4, l, 0, off, (int)P.tasks.size() - off, 0});
+                if (P.fk[lf[i]] > 0) T.push_back(TileTask{lf[i], 0, 0, 0});
+            if ((int)T.size() > off) Ls.push_back({4, l, 0, off, (int)T.size() - off, 0});
         }
         for (int p = 0; p < maxPanels; ++p) {
             // panel: one CTA per tile row below the factored diagonal tile
-            int off = static_cast<int>(P.tasks.size());
+            int off = static_cast<int>(T.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
@@ -447,10 +475,10 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
                 for (int ti = p + 1; ti < nt; ++ti) {
                     int r0, h;
                     tile_bounds(P.fk[f], P.fm[f], ti, r0, h);
-                    for (int g = 0; g * kPanelRows < h; ++g) P.tasks.push_back(TileTask{f, ti, g, p});
+                    for (int g = 0; g * kPanelRows < h; ++g) T.push_back(TileTask{f, ti, g, p});
                 }
             }
-            if ((int)P.tasks.size() > off) P.launches.push_back({1, l, p, off, (int)P.tasks.size() - off, 0});
+            if ((int)T.size() > off) Ls.push_back({1, l, p, off, (int)T.size() - off, 0});
             // trailing region [s, m) x [s, m), s = end of panel p, in the
             // lower triangle of 64 x 64 blocks, or of 32 x 32 blocks when
             // there are fewer than kUpdSplitBlocks 64 x 64 ones
@@ -467,17 +495,30 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
                 n64 += nb * (nb + 1) / 2;
             }
             const int edge = n64 < kUpdSplitBlocks ? kUpdSmall : kUpd;
-            off = static_cast<int>(P.tasks.size());
+            off = static_cast<int>(T.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
                 const int nb = blocks_of(f, edge);
                 for (int bj = 0; bj < nb; ++bj)
-                    for (int bi = bj; bi < nb; ++bi) P.tasks.push_back(TileTask{f, bi, bj, p});
+                    for (int bi = bj; bi < nb; ++bi) T.push_back(TileTask{f, bi, bj, p});
             }
-            if ((int)P.tasks.size() > off)
-                P.launches.push_back({edge == kUpd ? 3 : 5, l, p, off, (int)P.tasks.size() - off, 0});
+            if ((int)T.size() > off)
+                Ls.push_back({edge == kUpd ? 3 : 5, l, p, off, (int)T.size() - off, 0});
         }
+    });
+    {
+        std::vector<size_t> base(P.nLevels + 1, 0);
+        for (int l = 0; l < P.nLevels; ++l) base[l + 1] = base[l] + sched[l].tasks.size();
+        P.tasks.resize(base[P.nLevels]);
+        host_run_tasks(P.nLevels, [&](size_t l) {
+            std::copy(sched[l].tasks.begin(), sched[l].tasks.end(), P.tasks.begin() + base[l]);
+        });
+        for (int l = 0; l < P.nLevels; ++l)
+            for (CholPlan::Launch L : sched[l].launches) {
+                L.taskOff += static_cast<int>(base[l]);
+                P.launches.push_back(L);
+            }
     }
     // substitution chunks of the rectangular part of each front, per level
     P.rectRowOff.assign(P.nLevels + 1, 0);
@@ -592,14 +633,16 @@ __device__ __forceinline__ int tri_col_start(int j, int w) { return j * w - (j *
 
 __device__ __forceinline__ void diag_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(kDiagThreads) : "memory"); }
 
-// pivot d (a zero or non-finite value replaced by 1e-300) and 1 / d
+// pivot d (a zero or non-finite value replaced by 1e-300) and 1 / d, the
+// correctly rounded reciprocal (the same bits as the division 1.0 / d, by
+// the reciprocal's shorter sequence: it is on the tile's dependent chain)
 __device__ __forceinline__ void diag_pivot(double dRaw, double* piv, int& nBad)
 {
     const bool bad = !(dRaw != 0.0) || !isfinite(dRaw);
     const double d = bad ? 1e-300 : dRaw;
     nBad += bad;
     piv[0] = d;
-    piv[1] = 1.0 / d;
+    piv[1] = __drcp_rn(d);
 }
 
 __device__ void ldl_diag_tile(double* __restrict__ F, int m, int s0, int w, double* scratch, int* flag)
@@ -1201,6 +1244,320 @@ __global__ void __launch_bounds__(NT) k_bwd(const int* __restrict__ fronts, cons
     if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
 }
 
+// ---- cluster substitutions for the top tree levels ----
+//
+// A level of few large fronts leaves one SM per front walking ~50 dependent
+// 32-column blocks, its updates limited by what one SM pulls from memory.
+// Here a front gets a thread-block cluster of C CTAs (C <= 8) and its 32-row
+// blocks are dealt out round-robin: block j belongs to rank j % C.  Every CTA
+// holds the front's whole right-hand side in shared memory.  The owner of a
+// block applies the previous block's columns to it (lookahead) and runs the
+// same shuffle chain as k_fwd / k_bwd, then writes the 32 solved values into
+// every other CTA's shared memory (st.shared::cluster) followed by a release
+// arrive on that CTA's per-block mbarrier; each CTA's updaters wait (acquire,
+// cluster scope) for the block and apply it to the rows (forward) or columns
+// (backward) of the blocks it owns.  No cluster-wide barrier per block: the
+// chain passes from rank to rank through point-to-point mbarriers, the
+// updates spread over C SMs.  Per row / column the contributions are taken in
+// the same order and with the same FMA chains as in k_fwd / k_bwd, so the
+// results are bit-identical to theirs.  Every wait is bounded; one that runs
+// out raises the abort flag of every CTA of the cluster, so all loops end,
+// and the kernel's flag reports it as in k_fwd.
+constexpr int kClMaxBlocks = 128;   // pivot blocks per front (k <= 4096)
+constexpr int kClThreads = 256;
+
+__device__ __forceinline__ uint32_t cl_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t cl_size()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ void cl_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// this CTA's shared address a, as seen in cluster rank r's window
+__device__ __forceinline__ uint32_t cl_map(uint32_t a, uint32_t r)
+{
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(a), "r"(r));
+    return out;
+}
+
+__device__ __forceinline__ void cl_store(uint32_t a, double v)
+{
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+
+__device__ __forceinline__ void cl_store_int(uint32_t a, int v)
+{
+    asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void cl_arrive_remote(uint32_t a)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(a) : "memory");
+}
+
+// bounded wait with cluster-scope acquire (sees the remote CTAs' stores)
+__device__ __forceinline__ bool cl_wait_bounded(unsigned long long* b, uint32_t parity, volatile int* abort)
+{
+    const uint32_t a = smem_addr(b);
+    for (int i = 0; i < kSolveWaitPolls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (*abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+
+// a wait ran out: raise the abort flag of every CTA of the cluster
+__device__ __forceinline__ void cl_abort(int* abortFlag, uint32_t C)
+{
+    const uint32_t a = smem_addr(abortFlag);
+    for (uint32_t r = 0; r < C; ++r) cl_store_int(cl_map(a, r), 1);
+}
+
+// Forward substitution, pivot part, one cluster per front (see above).
+__global__ void __launch_bounds__(kClThreads) k_fwd_cl(const int* __restrict__ fronts, const int* __restrict__ fk,
+                                                       const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                       const long long* __restrict__ fupd, const int* __restrict__ fdof,
+                                                       const int* __restrict__ childOff, const int* __restrict__ childList,
+                                                       const int* __restrict__ relOff, const int* __restrict__ relIdx,
+                                                       const double* __restrict__ pool, double* __restrict__ upd,
+                                                       double* __restrict__ y, int* __restrict__ flag)
+{
+    extern __shared__ double sh[];
+    __shared__ double tile[32 * 33];
+    __shared__ unsigned long long recv[kClMaxBlocks], updated[kClMaxBlocks];
+    __shared__ int abortFlag;
+    constexpr int NU = kClThreads - 32;   // updater threads
+    const uint32_t C = cl_size(), q = cl_rank();
+    const int f = fronts[blockIdx.x / C];
+    const int k = fk[f], m = fm[f], d0 = fdof[f];
+    const int nb = (k + 31) / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : 0.0;
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < nb; ++j) {
+            mbar_init(&recv[j], 32);
+            mbar_init(&updated[j], NU);
+        }
+        abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    for (int c = childOff[f]; c < childOff[f + 1]; ++c) {
+        const int ch = childList[c];
+        const int u = fm[ch] - fk[ch];
+        const int* rel = relIdx + relOff[ch];
+        const double* uc = upd + fupd[ch];
+        for (int i = threadIdx.x; i < u; i += blockDim.x) sh[rel[i]] += uc[i];
+        __syncthreads();
+    }
+    cl_sync();   // every CTA's barriers initialised before the first remote arrive
+    const double* L = pool + foff[f];
+    if (warp == 0) {
+        for (int j = (int)q; j < nb; j += (int)C) {
+            const int c0 = 32 * j, w = min(32, k - c0);
+            const int r = c0 + lane;
+            double dl[32], lv[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) dl[c] = (lane < w && c < w) ? L[r + (long long)(c0 + c) * m] : 0.0;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) lv[c] = (j >= 1 && lane < w) ? L[r + (long long)(c0 - 32 + c) * m] : 0.0;
+            // block j-1 solved (by its owner) and this CTA's updaters done
+            // with block j-2 on these rows
+            bool ok = j < 1 || cl_wait_bounded(&recv[j - 1], 0, &abortFlag);
+            ok = ok && (j < 2 || cl_wait_bounded(&updated[j - 2], 0, &abortFlag));
+            if (!__all_sync(0xffffffffu, ok)) break;
+            if (j >= 1 && lane < w) {
+                const int p0 = c0 - 32;
+                double acc = 0.0;
+#pragma unroll
+                for (int c = 0; c < 32; ++c) acc = fma(lv[c], sh[p0 + c], acc);
+                sh[r] -= acc;
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                if (lane < w) tile[lane * 33 + c] = dl[c];
+            __syncwarp();
+            double v = lane < w ? sh[r] : 0.0;
+            for (int c = 0; c < w; ++c) {
+                const double yc = __shfl_sync(0xffffffffu, v, c);
+                if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
+            }
+            if (lane < w) sh[r] = v;
+            __syncwarp();
+            // publish: the 32 values into every other CTA, then its barrier
+            const uint32_t av = smem_addr(&sh[c0 + (lane < w ? lane : 0)]), ab = smem_addr(&recv[j]);
+            for (uint32_t t = 1; t < C; ++t) {
+                const uint32_t dst = (q + t) % C;
+                if (lane < w) cl_store(cl_map(av, dst), v);
+                cl_arrive_remote(cl_map(ab, dst));
+            }
+            mbar_arrive(&recv[j]);
+        }
+        if (abortFlag) cl_abort(&abortFlag, C);
+    }
+    else {
+        const int t = threadIdx.x - 32;
+        for (int b = 0; b < nb; ++b) {
+            if (!cl_wait_bounded(&recv[b], 0, &abortFlag)) break;
+            const int c0 = 32 * b, w = min(32, k - c0);
+            // this CTA's blocks from b + 2 on: the first is the smallest
+            // i >= b + 2 with i % C == q
+            int i0 = b + 2 + (int)((q + C - (uint32_t)((b + 2) % C)) % C);
+            const int nOwn = i0 < nb ? (nb - 1 - i0) / (int)C + 1 : 0;
+            for (int idx = t; idx < 32 * nOwn; idx += NU) {
+                const int r = 32 * (i0 + (idx >> 5) * (int)C) + (idx & 31);
+                if (r >= k) continue;
+                double lv[32];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) lv[c] = c < w ? L[r + (long long)(c0 + c) * m] : 0.0;
+                double acc = 0.0;
+#pragma unroll
+                for (int c = 0; c < 32; ++c)
+                    if (c < w) acc = fma(lv[c], sh[c0 + c], acc);
+                sh[r] -= acc;
+            }
+            mbar_arrive(&updated[b]);
+        }
+        if (abortFlag) cl_abort(&abortFlag, C);
+    }
+    __syncthreads();
+    for (int j = (int)q; j < nb; j += (int)C)
+        for (int r = 32 * j + threadIdx.x; r < min(k, 32 * j + 32); r += blockDim.x) y[d0 + r] = sh[r];
+    if (q == 0)
+        for (int r = k + threadIdx.x; r < m; r += blockDim.x) upd[fupd[f] + (r - k)] = sh[r];
+    if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
+    cl_sync();   // no CTA leaves while another may still write into it
+}
+
+// Backward substitution, pivot part, one cluster per front: column block b
+// belongs to rank b % C; blocks go from the last down (see k_bwd).
+__global__ void __launch_bounds__(kClThreads) k_bwd_cl(const int* __restrict__ fronts, const int* __restrict__ fk,
+                                                       const int* __restrict__ fm, const long long* __restrict__ foff,
+                                                       const int* __restrict__ fdof, const double* __restrict__ pool,
+                                                       const double* __restrict__ y, const double* __restrict__ tdot,
+                                                       double* __restrict__ x, int* __restrict__ flag)
+{
+    extern __shared__ double sh[];
+    __shared__ double tile[32 * 33];
+    __shared__ unsigned long long recv[kClMaxBlocks], updated[kClMaxBlocks];
+    __shared__ int abortFlag;
+    constexpr int NU = kClThreads - 32;
+    const uint32_t C = cl_size(), q = cl_rank();
+    const int f = fronts[blockIdx.x / C];
+    const int k = fk[f], m = fm[f], d0 = fdof[f];
+    const int nb = (k + 31) / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double* L = pool + foff[f];
+    const bool rect = m > k;
+    for (int r = threadIdx.x; r < k; r += blockDim.x)
+        sh[r] = y[d0 + r] / L[r + (long long)r * m] - (rect ? tdot[d0 + r] : 0.0);
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < nb; ++j) {
+            mbar_init(&recv[j], 32);
+            mbar_init(&updated[j], NU);
+        }
+        abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    cl_sync();
+    if (warp == 0) {
+        // this CTA's blocks, from the last down
+        const int top = (nb - 1) - (int)((uint32_t)(nb - 1 + C - q) % C);
+        for (int b = top; b >= 0; b -= (int)C) {
+            const int c0 = 32 * b, w = min(32, k - c0);
+            const int c = c0 + lane;
+            const int r0 = c0 + 32, w1 = b + 1 <= nb - 1 ? min(32, k - r0) : 0;
+            double dl[32], lv[32];
+#pragma unroll
+            for (int r = 0; r < 32; ++r) dl[r] = (lane < w && r < w) ? L[(c0 + r) + (long long)c * m] : 0.0;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) lv[r] = (lane < w && r < w1) ? L[(r0 + r) + (long long)c * m] : 0.0;
+            bool ok = b + 1 > nb - 1 || cl_wait_bounded(&recv[b + 1], 0, &abortFlag);
+            ok = ok && (b + 2 > nb - 1 || cl_wait_bounded(&updated[b + 2], 0, &abortFlag));
+            if (!__all_sync(0xffffffffu, ok)) break;
+            if (b + 1 <= nb - 1 && lane < w) {
+                double acc = 0.0;
+#pragma unroll
+                for (int r = 0; r < 32; ++r)
+                    if (r < w1) acc = fma(lv[r], sh[r0 + r], acc);
+                sh[c] -= acc;
+            }
+#pragma unroll
+            for (int r = 0; r < 32; ++r)
+                if (lane < w) tile[r * 33 + lane] = dl[r];
+            __syncwarp();
+            double v = lane < w ? sh[c] : 0.0;
+            for (int r = w - 1; r >= 0; --r) {
+                const double xr = __shfl_sync(0xffffffffu, v, r);
+                if (lane < r) v -= tile[r * 33 + lane] * xr;
+            }
+            if (lane < w) sh[c] = v;
+            __syncwarp();
+            const uint32_t av = smem_addr(&sh[c0 + (lane < w ? lane : 0)]), ab = smem_addr(&recv[b]);
+            for (uint32_t t = 1; t < C; ++t) {
+                const uint32_t dst = (q + t) % C;
+                if (lane < w) cl_store(cl_map(av, dst), v);
+                cl_arrive_remote(cl_map(ab, dst));
+            }
+            mbar_arrive(&recv[b]);
+        }
+        if (abortFlag) cl_abort(&abortFlag, C);
+    }
+    else {
+        const int t = threadIdx.x - 32;
+        for (int s = nb - 1; s >= 1; --s) {
+            if (!cl_wait_bounded(&recv[s], 0, &abortFlag)) break;
+            const int r0 = 32 * s, w = min(32, k - r0);
+            // this CTA's column blocks up to s - 2: the last is the largest
+            // i <= s - 2 with i % C == q
+            const int hi = s - 2;
+            const int i1 = hi >= 0 ? hi - (int)((uint32_t)(hi + C - q) % C) : -1;
+            const int nOwn = i1 >= 0 ? i1 / (int)C + 1 : 0;
+            for (int idx = t; idx < 32 * nOwn; idx += NU) {
+                const int c = 32 * (i1 - (idx >> 5) * (int)C) + (idx & 31);
+                double lv[32];
+#pragma unroll
+                for (int r = 0; r < 32; ++r) lv[r] = r < w ? L[(r0 + r) + (long long)c * m] : 0.0;
+                double acc = 0.0;
+#pragma unroll
+                for (int r = 0; r < 32; ++r)
+                    if (r < w) acc = fma(lv[r], sh[r0 + r], acc);
+                sh[c] -= acc;
+            }
+            mbar_arrive(&updated[s]);
+        }
+        if (abortFlag) cl_abort(&abortFlag, C);
+    }
+    __syncthreads();
+    for (int j = (int)q; j < nb; j += (int)C)
+        for (int r = 32 * j + threadIdx.x; r < min(k, 32 * j + 32); r += blockDim.x) x[d0 + r] = sh[r];
+    if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
+    cl_sync();
+}
+
 template <typename T>
 cudaError_t up(T** d, const std::vector<T>& h)
 {
@@ -1326,6 +1683,37 @@ int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string
     return OC_OK;
 }
 
+// Cluster size for a level's pivot-part substitutions: levels of few fronts
+// with at least two 32-column blocks per rank get a cluster per front, sized
+// so that the level fills up to ~152 CTAs; 1 (one CTA per front) otherwise.
+static int solve_cluster_for(const CholPlan& P, int l)
+{
+    const int cnt = P.levelFrontOff[l + 1] - P.levelFrontOff[l];
+    const int nb = (P.levelMaxK[l] + 31) / 32;
+    if (P.solveCluster < 2 || nb > kClMaxBlocks) return 1;
+    for (int C = std::min(P.solveCluster, 8); C >= 2; C /= 2)
+        if (cnt * C <= 152 && nb >= 2 * C) return C;
+    return 1;
+}
+
+template <typename... A>
+static void launch_cluster(void (*kern)(A...), int grid, int C, size_t shm, cudaStream_t st, A... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kClThreads);
+    cfg.dynamicSmemBytes = shm;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, size_t shm,
                           size_t shmK)
 {
@@ -1334,6 +1722,14 @@ static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double si
     for (int l = 0; l < P.nLevels; ++l) {
         const int off = P.levelFrontOff[l], cnt = P.levelFrontOff[l + 1] - off;
         const size_t lshm = sizeof(double) * (size_t)std::max(P.levelMaxM[l], 1);
+        const int C = solve_cluster_for(P, l);
+        if (C > 1)
+            launch_cluster(k_fwd_cl, cnt * C, C, lshm, st, (const int*)(P.dLevelFronts + off), (const int*)P.dFk,
+                           (const int*)P.dFm, (const long long*)P.dFoff, (const long long*)P.dFupd,
+                           (const int*)P.dFdofStart, (const int*)P.dChildOff, (const int*)P.dChildList,
+                           (const int*)P.dRelOff, (const int*)P.dRelIdx, (const double*)P.pool, P.upd, P.yperm,
+                           P.dSolveFlag);
+        else
         switch (kSolveThreadsFor(P.levelMaxK[l])) {
 #define OC_FWD(NT)                                                                                                      \
     k_fwd<NT><<<cnt, NT, lshm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFupd, P.dFdofStart, P.dChildOff,     \
@@ -1362,6 +1758,13 @@ static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double si
                                                                 P.dFdofStart, P.dFrowOff, P.dRowIdx, P.pool, P.xperm,
                                                                 P.tmpDot);
         const size_t lshm = sizeof(double) * (size_t)std::max(P.levelMaxM[l], 1);
+        const int C = solve_cluster_for(P, l);
+        if (C > 1)
+            launch_cluster(k_bwd_cl, cnt * C, C, lshm, st, (const int*)(P.dLevelFronts + off), (const int*)P.dFk,
+                           (const int*)P.dFm, (const long long*)P.dFoff, (const int*)P.dFdofStart,
+                           (const double*)P.pool, (const double*)P.yperm, (const double*)P.tmpDot, P.xperm,
+                           P.dSolveFlag);
+        else
         switch (kSolveThreadsFor(P.levelMaxK[l])) {
 #define OC_BWD(NT)                                                                                                      \
     k_bwd<NT><<<cnt, NT, lshm, st>>>(P.dLevelFronts + off, P.dFk, P.dFm, P.dFoff, P.dFdofStart, P.pool, P.yperm,          \
@@ -1373,6 +1776,26 @@ static void enqueue_solve(CholPlan& P, const double2* rhs, double2* x, double si
         }
     }
     k_permute_out<<<(n + 255) / 256, 256, 0, st>>>(P.xperm, P.dPermDof, n, reinterpret_cast<double*>(x));
+}
+
+int chol_solve_cluster_levels(const CholPlan& P, int* largest)
+{
+    int n = 0, big = 1;
+    for (int l = 0; l < P.nLevels; ++l) {
+        const int C = solve_cluster_for(P, l);
+        if (C > 1) ++n;
+        big = std::max(big, C);
+    }
+    if (largest) *largest = big;
+    return n;
+}
+
+void chol_set_solve_cluster(CholPlan& P, int maxCluster)
+{
+    P.solveCluster = std::max(1, std::min(maxCluster, 8));
+    if (P.solveGraph) cudaGraphExecDestroy(P.solveGraph);
+    P.solveGraph = nullptr;
+    P.solveKey[0] = P.solveKey[1] = nullptr;
 }
 
 int chol_solve_status(CholPlan& P, cudaStream_t st, int* timedOut)
@@ -1398,6 +1821,8 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
         cudaFuncSetAttribute(k_bwd<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         cudaFuncSetAttribute(k_bwd<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
         cudaFuncSetAttribute(k_bwd<kFwdThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_fwd_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+        cudaFuncSetAttribute(k_bwd_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     }
     if (shmK > 48 * 1024) cudaFuncSetAttribute(k_fwd_rect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmK);
     if (P.useGraphs && (!P.solveGraph || P.solveKey[0] != rhs || P.solveKey[1] != x || P.solveSign != sign)) {

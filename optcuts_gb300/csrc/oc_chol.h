@@ -95,6 +95,9 @@ struct CholPlan {
     bool onDevice = false;
     // captured launch sequences (fixed per topology)
     bool useGraphs = true;
+    // largest thread-block cluster per front in the substitutions of the top
+    // levels (1: one CTA per front everywhere); results are the same bits
+    int solveCluster = 8;
     cudaGraphExec_t factGraph = nullptr, solveGraph = nullptr;
     const void* factKey = nullptr;
     const void* solveKey[2] = {nullptr, nullptr};
@@ -123,6 +126,12 @@ void chol_free(CholPlan& P);
 int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBadPivots);
 // Solves A x = sign * rhs.
 int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStream_t st, std::string* err);
+// largest cluster per front in the substitutions (1..8; drops the captured
+// solve graph so that the next solve records the new launches)
+void chol_set_solve_cluster(CholPlan& P, int maxCluster);
+// tree levels whose pivot-part substitutions run as clusters, and the
+// largest cluster size among them (1 when none)
+int chol_solve_cluster_levels(const CholPlan& P, int* largest);
 // whether a substitution kernel gave up a bounded wait since the upload
 // (synchronises the stream)
 int chol_solve_status(CholPlan& P, cudaStream_t st, int* timedOut);

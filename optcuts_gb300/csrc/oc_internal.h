@@ -6,27 +6,158 @@
 #include "optcuts_gpu.h"
 
 #include <algorithm>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
 #include <string>
+#include <atomic>
+#include <pthread.h>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace oc {
 
-// fn(begin, end) over contiguous chunks of [0, n) on up to 16 host threads
-// (the calling thread takes the first chunk); one chunk below 2 * minChunk
+// Persistent host worker pool: up to 15 workers (16 threads with the caller)
+// started on first use, so a parallel loop costs a wake-up instead of a
+// thread spawn and join per worker (~0.5 ms for 15 threads).  A job is a
+// count of tasks; workers and the calling thread claim tasks in index order
+// under the pool's lock, the caller runs tasks until none is left and then
+// waits only for tasks other threads already claimed, so a task may itself
+// run a nested job (a worker caller drives its own job to completion).
+// Tasks must not throw (as on a std::thread).  A forked child process gets
+// a new pool (a fork handler drops the parent's, whose workers do not exist
+// there).  A job of one task runs inline without touching the pool.
+class HostPool {
+public:
+    static HostPool& get()
+    {
+        HostPool* p = current().load(std::memory_order_acquire);
+        if (p) return *p;
+        std::lock_guard<std::mutex> g(create_mu());
+        p = current().load(std::memory_order_relaxed);
+        if (!p) {
+            static const bool hooked = [] {
+                // a forked child starts without the parent's workers
+                pthread_atfork(nullptr, nullptr, [] { current().store(nullptr, std::memory_order_relaxed); });
+                return true;
+            }();
+            (void)hooked;
+            p = new HostPool();   // never destroyed: its workers block forever
+            current().store(p, std::memory_order_release);
+        }
+        return *p;
+    }
+    static size_t threads()
+    {
+        static const size_t n = std::max<size_t>(1, std::min<size_t>(std::thread::hardware_concurrency(), 16));
+        return n;
+    }
+    void run(size_t nTasks, void (*call)(void*, size_t), void* ctx)
+    {
+        if (nTasks == 0) return;
+        if (nTasks == 1) {
+            call(ctx, 0);
+            return;
+        }
+        start_workers();
+        Job j{call, ctx, nTasks, 0, 0};
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            queue_.push_back(&j);
+        }
+        cv_.notify_all();
+        for (;;) {
+            size_t t;
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                if (j.next >= j.n) break;
+                t = j.next++;
+                if (j.next == j.n) queue_.erase(std::find(queue_.begin(), queue_.end(), &j));
+            }
+            call(ctx, t);
+            finish(j);
+        }
+        std::unique_lock<std::mutex> lk(mu_);
+        doneCv_.wait(lk, [&] { return j.done == j.n; });
+    }
+
+private:
+    struct Job {
+        void (*call)(void*, size_t);
+        void* ctx;
+        size_t n, next, done;
+    };
+    HostPool() = default;
+    static std::atomic<HostPool*>& current()
+    {
+        static std::atomic<HostPool*> p{nullptr};
+        return p;
+    }
+    static std::mutex& create_mu()
+    {
+        static std::mutex m;
+        return m;
+    }
+    void start_workers()
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        if (started_) return;
+        started_ = true;
+        for (size_t w = 1; w < threads(); ++w) std::thread([this] { loop(); }).detach();
+    }
+    void finish(Job& j)
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        if (++j.done == j.n) doneCv_.notify_all();
+    }
+    void loop()
+    {
+        for (;;) {
+            Job* j;
+            size_t t;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return !queue_.empty(); });
+                j = queue_.front();
+                t = j->next++;
+                if (j->next == j->n) queue_.pop_front();
+            }
+            j->call(j->ctx, t);
+            finish(*j);
+        }
+    }
+    bool started_ = false;
+    std::mutex mu_;
+    std::condition_variable cv_, doneCv_;
+    std::deque<Job*> queue_;
+};
+
+// fn(t) for every t in [0, nTasks) on the host worker pool
+template <class Fn>
+void host_run_tasks(size_t nTasks, Fn&& fn)
+{
+    if (nTasks <= 1) {
+        if (nTasks) fn(size_t(0));
+        return;
+    }
+    using F = std::remove_reference_t<Fn>;
+    HostPool::get().run(nTasks, [](void* c, size_t t) { (*static_cast<F*>(c))(t); },
+                        const_cast<void*>(static_cast<const void*>(&fn)));
+}
+
+// fn(begin, end) over contiguous chunks of [0, n), one per host thread (up
+// to 16); a single chunk below 2 * minChunk.  The chunk boundaries depend
+// only on n, minChunk and the host's thread count.
 template <class Fn>
 void host_parallel_for(size_t n, size_t minChunk, Fn&& fn)
 {
-    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t nt = std::max<size_t>(1, std::min<size_t>({hw, 16, n / std::max<size_t>(1, minChunk)}));
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(HostPool::threads(), n / std::max<size_t>(1, minChunk)));
     if (nt == 1) {
         if (n) fn(size_t(0), n);
         return;
     }
-    std::vector<std::thread> th;
-    for (size_t t = 1; t < nt; ++t) th.emplace_back([&fn, n, nt, t] { fn(n * t / nt, n * (t + 1) / nt); });
-    fn(size_t(0), n / nt);
-    for (auto& x : th) x.join();
+    host_run_tasks(nt, [&](size_t t) { fn(n * t / nt, n * (t + 1) / nt); });
 }
 
 // 2x2 FP64 matrix, row-major (block-Jacobi inverse of one vertex row).

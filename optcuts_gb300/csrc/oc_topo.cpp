@@ -6,9 +6,9 @@
 // paths, zipper-bottom cohesive pairs with the merged-position projection),
 // builds every local mesh (TriMesh::computeLocalEdDec_inSplit / _bSplit /
 // _merge, TriMesh.cpp:2262-2794, with the local cut or split applied) as a
-// packed problem, and one launch of k_local_newton solves them all (one warp
-// per problem).  This is the bijectivity-off form of the queries: the local
-// meshes carry no air mesh.
+// packed problem, and the device solves them all in batched launches
+// (k_local_newton per size class; with bijectivity on, k_local_newton_bij,
+// whose problems also carry the candidates' local air loops).
 
 #include "oc_topo.h"
 #include "oc_mlp.h"
@@ -41,75 +41,130 @@ struct Topo {
     std::vector<int> nbPtr, nb;            // sorted neighbours per vertex
     std::vector<char> bnd;
 
+    // Counting sorts in chunks on the host pool: chunk c of the items counts
+    // per key, the per-key offsets of the chunks follow in chunk order, and
+    // each chunk scatters its items in item order, so every list comes out
+    // in the order of the sequential counting sort.
     void build(int nV_, const int* F_, int nF_)
     {
         nV = nV_;
         nF = nF_;
         F = F_;
-        hoPtr.assign(nV + 1, 0);
-        for (long long i = 0; i < 3LL * nF; ++i) hoPtr[F[i] + 1]++;
-        for (int v = 0; v < nV; ++v) hoPtr[v + 1] += hoPtr[v];
+        const int nt = static_cast<int>(std::max<size_t>(1, std::min<size_t>(HostPool::threads(), nF / 8192)));
+        std::vector<int> off((size_t)nt * nV);   // per chunk and key: count, then offset within the key
+        auto chunk = [](int n, int c, int nt) { return std::make_pair((int)((long long)n * c / nt),
+                                                                     (int)((long long)n * (c + 1) / nt)); };
+        // key ranges of the per-key passes (offsets, sorts, merges)
+        const int nk = static_cast<int>(std::max<size_t>(1, std::min<size_t>(HostPool::threads(), nV / 4096)));
+        auto prefix_keys = [&](std::vector<int>& ptr) {
+            ptr.assign(nV + 1, 0);
+            host_run_tasks(nk, [&](size_t q) {
+                const auto r = chunk(nV, (int)q, nk);
+                for (int v = r.first; v < r.second; ++v) {
+                    int s = 0;
+                    for (int c = 0; c < nt; ++c) {
+                        const int x = off[(size_t)c * nV + v];
+                        off[(size_t)c * nV + v] = s;
+                        s += x;
+                    }
+                    ptr[v + 1] = s;
+                }
+            });
+            for (int v = 0; v < nV; ++v) ptr[v + 1] += ptr[v];
+        };
+        // out-half-edges per vertex, in triangle order
+        host_run_tasks(nt, [&](size_t c) {
+            int* o = off.data() + c * nV;
+            std::fill(o, o + nV, 0);
+            const auto r = chunk(nF, (int)c, nt);
+            for (long long i = 3LL * r.first; i < 3LL * r.second; ++i) o[F[i]]++;
+        });
+        prefix_keys(hoPtr);
         hoTo.resize(3 * (size_t)nF);
         hoTri.resize(3 * (size_t)nF);
-        std::vector<int> fill(hoPtr.begin(), hoPtr.end() - 1);
-        for (int t = 0; t < nF; ++t)
-            for (int k = 0; k < 3; ++k) {
-                const int a = F[3 * t + k], b = F[3 * t + (k + 1) % 3];
-                hoTo[fill[a]] = b;
-                hoTri[fill[a]++] = t;
-            }
-        // out-half-edges of each vertex sorted by target (edge_tri bisects)
-        for (int a = 0; a < nV; ++a) {
-            const int p0 = hoPtr[a], p1 = hoPtr[a + 1];
-            for (int p = p0 + 1; p < p1; ++p) {   // insertion sort: a handful per vertex
-                const int to = hoTo[p], tri = hoTri[p];
-                int q = p;
-                for (; q > p0 && hoTo[q - 1] > to; --q) {
-                    hoTo[q] = hoTo[q - 1];
-                    hoTri[q] = hoTri[q - 1];
+        host_run_tasks(nt, [&](size_t c) {
+            int* o = off.data() + c * nV;
+            const auto r = chunk(nF, (int)c, nt);
+            for (int t = r.first; t < r.second; ++t)
+                for (int k = 0; k < 3; ++k) {
+                    const int a = F[3 * t + k], b = F[3 * t + (k + 1) % 3];
+                    const int p = hoPtr[a] + o[a]++;
+                    hoTo[p] = b;
+                    hoTri[p] = t;
                 }
-                hoTo[q] = to;
-                hoTri[q] = tri;
+        });
+        // out-half-edges of each vertex sorted by target (edge_tri bisects)
+        host_run_tasks(nk, [&](size_t q) {
+            const auto r = chunk(nV, (int)q, nk);
+            for (int a = r.first; a < r.second; ++a) {
+                const int p0 = hoPtr[a], p1 = hoPtr[a + 1];
+                for (int p = p0 + 1; p < p1; ++p) {   // insertion sort: a handful per vertex
+                    const int to = hoTo[p], tri = hoTri[p];
+                    int q2 = p;
+                    for (; q2 > p0 && hoTo[q2 - 1] > to; --q2) {
+                        hoTo[q2] = hoTo[q2 - 1];
+                        hoTri[q2] = hoTri[q2 - 1];
+                    }
+                    hoTo[q2] = to;
+                    hoTri[q2] = tri;
+                }
             }
-        }
-        // in-half-edges of each vertex (sources ascending: counting sort
-        // over sources in order)
-        std::vector<int> hiPtr(nV + 1, 0), hiFrom(3 * (size_t)nF);
-        for (int a = 0; a < nV; ++a)
-            for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) hiPtr[hoTo[p] + 1]++;
-        for (int v = 0; v < nV; ++v) hiPtr[v + 1] += hiPtr[v];
-        {
-            std::vector<int> pos(hiPtr.begin(), hiPtr.end() - 1);
-            for (int a = 0; a < nV; ++a)
-                for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) hiFrom[pos[hoTo[p]]++] = a;
-        }
+        });
+        // in-half-edges of each vertex, sources ascending (chunks of sources)
+        std::vector<int> hiPtr, hiFrom(3 * (size_t)nF);
+        host_run_tasks(nt, [&](size_t c) {
+            int* o = off.data() + c * nV;
+            std::fill(o, o + nV, 0);
+            const auto r = chunk(nV, (int)c, nt);
+            for (int p = hoPtr[r.first]; p < hoPtr[r.second]; ++p) o[hoTo[p]]++;
+        });
+        prefix_keys(hiPtr);
+        host_run_tasks(nt, [&](size_t c) {
+            int* o = off.data() + c * nV;
+            const auto r = chunk(nV, (int)c, nt);
+            for (int a = r.first; a < r.second; ++a)
+                for (int p = hoPtr[a]; p < hoPtr[a + 1]; ++p) hiFrom[hiPtr[hoTo[p]] + o[hoTo[p]]++] = a;
+        });
         // neighbours = out-targets merged with in-sources; a neighbour in
         // only one of the two lists is across a boundary edge
-        // (TriMesh::isBoundaryVert, TriMesh.cpp:2069-2083)
-        nbPtr.assign(nV + 1, 0);
-        nb.clear();
-        nb.reserve(3 * (size_t)nF + nV);
-        bnd.assign(nV, 0);
-        for (int v = 0; v < nV; ++v) {
-            int i = hoPtr[v], j = hiPtr[v];
+        // (TriMesh::isBoundaryVert, TriMesh.cpp:2069-2083): sizes first,
+        // then the lists
+        auto merge = [&](int v, int* out, char* border) {
+            int i = hoPtr[v], j = hiPtr[v], n = 0;
             const int ie = hoPtr[v + 1], je = hiPtr[v + 1];
             while (i < ie || j < je) {
+                int x;
                 if (j >= je || (i < ie && hoTo[i] < hiFrom[j])) {
-                    nb.push_back(hoTo[i++]);
-                    bnd[v] = 1;
+                    x = hoTo[i++];
+                    *border = 1;
                 }
                 else if (i >= ie || hiFrom[j] < hoTo[i]) {
-                    nb.push_back(hiFrom[j++]);
-                    bnd[v] = 1;
+                    x = hiFrom[j++];
+                    *border = 1;
                 }
                 else {
-                    nb.push_back(hoTo[i]);
+                    x = hoTo[i];
                     ++i;
                     ++j;
                 }
+                if (out) out[n] = x;
+                ++n;
             }
-            nbPtr[v + 1] = static_cast<int>(nb.size());
-        }
+            return n;
+        };
+        nbPtr.assign(nV + 1, 0);
+        bnd.assign(nV, 0);
+        host_run_tasks(nk, [&](size_t q) {
+            const auto r = chunk(nV, (int)q, nk);
+            for (int v = r.first; v < r.second; ++v) nbPtr[v + 1] = merge(v, nullptr, &bnd[v]);
+        });
+        for (int v = 0; v < nV; ++v) nbPtr[v + 1] += nbPtr[v];
+        nb.resize(nbPtr[nV]);
+        host_run_tasks(nk, [&](size_t q) {
+            const auto r = chunk(nV, (int)q, nk);
+            char dummy = 0;
+            for (int v = r.first; v < r.second; ++v) merge(v, nb.data() + nbPtr[v], &dummy);
+        });
     }
 
     int edge_tri(int a, int b) const
@@ -624,35 +679,22 @@ std::vector<int> filter_candidates(const std::vector<std::pair<double, int>>& ke
     auto byKey = [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first < y.first; };
     const size_t n = keyed.size();
     std::vector<std::pair<double, int>> s(keyed), tmp(n);
-    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-    const size_t nt = std::max<size_t>(1, std::min<size_t>({hw, 16, n / 4096}));
+    const size_t nt = std::max<size_t>(1, std::min<size_t>(HostPool::threads(), n / 4096));
     std::vector<size_t> cut(nt + 1);
     for (size_t t = 0; t <= nt; ++t) cut[t] = n * t / nt;
-    {
-        std::vector<std::thread> th;
-        for (size_t t = 1; t < nt; ++t)
-            th.emplace_back([&, t] { std::stable_sort(s.begin() + cut[t], s.begin() + cut[t + 1], byKey); });
-        std::stable_sort(s.begin() + cut[0], s.begin() + cut[1], byKey);
-        for (auto& x : th) x.join();
-    }
+    host_run_tasks(nt, [&](size_t t) { std::stable_sort(s.begin() + cut[t], s.begin() + cut[t + 1], byKey); });
     while (cut.size() > 2) {
         std::vector<size_t> next;
-        std::vector<std::thread> th;
-        for (size_t k = 0; k + 1 < cut.size(); k += 2) {
-            next.push_back(cut[k]);
-            if (k + 2 < cut.size()) {
-                const size_t a0 = cut[k], a1 = cut[k + 1], a2 = cut[k + 2];
-                th.emplace_back([&, a0, a1, a2] {
-                    std::merge(s.begin() + a0, s.begin() + a1, s.begin() + a1, s.begin() + a2, tmp.begin() + a0, byKey);
-                });
-            }
-            else {
-                const size_t a0 = cut[k], a1 = cut[k + 1];
-                std::copy(s.begin() + a0, s.begin() + a1, tmp.begin() + a0);
-            }
-        }
-        for (auto& x : th) x.join();
+        for (size_t k = 0; k + 1 < cut.size(); k += 2) next.push_back(cut[k]);
         next.push_back(n);
+        host_run_tasks((cut.size()) / 2, [&](size_t i) {
+            const size_t k = 2 * i;
+            if (k + 2 < cut.size())
+                std::merge(s.begin() + cut[k], s.begin() + cut[k + 1], s.begin() + cut[k + 1], s.begin() + cut[k + 2],
+                           tmp.begin() + cut[k], byKey);
+            else
+                std::copy(s.begin() + cut[k], s.begin() + cut[k + 1], tmp.begin() + cut[k]);
+        });
         s.swap(tmp);
         cut.swap(next);
     }
@@ -1546,8 +1588,7 @@ void build_parallel(const TopoQueryIn& in, size_t n, Batch& B, const Body& body)
         cache->nV = in.nV;
         cache->nF = in.nF;
     }
-    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-    const int nt = static_cast<int>(std::max<size_t>(1, std::min<size_t>({hw, 16, n / 16 + 1})));
+    const int nt = static_cast<int>(std::max<size_t>(1, std::min<size_t>(HostPool::threads(), n / 16 + 1)));
     if (static_cast<int>(cache->ctx.size()) < nt) cache->ctx.resize(nt);
     auto work = [&](int t) {
         std::unique_ptr<BuildCtx>& X = cache->ctx[t];
@@ -1563,10 +1604,7 @@ void build_parallel(const TopoQueryIn& in, size_t n, Batch& B, const Body& body)
         const size_t a = n * t / nt, b = n * (t + 1) / nt;
         for (size_t i = a; i < b; ++i) body(*X, i);
     };
-    std::vector<std::thread> th;
-    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
-    work(0);
-    for (auto& x : th) x.join();
+    host_run_tasks(nt, [&](size_t t) { work(static_cast<int>(t)); });
     for (int t = 0; t < nt; ++t) append_batch(B, cache->ctx[t]->B);
 }
 
@@ -2100,6 +2138,7 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
     }
     // bijective form: the whole-mesh air mesh the local loops come from
     std::unique_ptr<AirSrc> airSrc;
+    const auto tAir = clk::now();
     if (in.bijective) {
         if (!in.airV || !in.airF || !in.airBnd || in.nAirF <= 0 || in.nAirBnd <= 0 || in.nAirV < in.nAirBnd) {
             if (err) *err = "topology query: the bijective form needs the scaffold's air mesh";
@@ -2108,6 +2147,7 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
         airSrc = std::make_unique<AirSrc>();
         airSrc->build(in);
     }
+    const double airMs = std::chrono::duration<double, std::milli>(clk::now() - tAir).count();
     // every operation's problems in one batch, op i owning [start[i], start[i + 1])
     Batch B;
     std::vector<size_t> start(nOps + 1, 0);
@@ -2137,7 +2177,7 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
     const bool learned = (opts.flags & kTopoLearned) && opts.mlp;
     const int fp32 = opts.flags & kTopoFp32Hessian;
     const bool tune = (opts.flags & kTopoAutotune) != 0;
-    double probeMs = 0.0, exactMs = 0.0;
+    double probeMs = 0.0, exactMs = 0.0, rankMs = 0.0;
     if (n) {
         std::string e2;
         std::vector<int> all(n);
@@ -2187,6 +2227,7 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
             std::sort(sel.begin(), sel.end());
             std::vector<LocalResult> full(n);
             const auto tB = clk::now();
+            rankMs = std::chrono::duration<double, std::milli>(tB - tA).count();
             rc = solve_batch(in, B, batchId, sel, -1, fp32, full, &e2, tune);
             if (rc) { if (err) *err = e2; return rc; }
             for (int k : sel) res[k] = full[k];
@@ -2212,14 +2253,19 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
             }
         }
     }
-    const double solveMs = std::chrono::duration<double, std::milli>(clk::now() - t1).count();
+    const auto t2 = clk::now();
+    const double solveMs = std::chrono::duration<double, std::milli>(t2 - t1).count();
     for (int i = 0; i < nOps; ++i) {
         TopoOpResult& R = results[i];
         R.stats.solveMs = solveMs;   // shared by the operations solved together
         R.stats.probeMs = probeMs;
         R.stats.exactMs = exactMs;
+        R.stats.rankMs = rankMs;
+        R.stats.airMs = airMs;
         finish_op(ops[i], lambda_t, B, start[i], start[i + 1], res, solved, R.cands, R.best, R.stats, &R.extras);
     }
+    const double finishMs = std::chrono::duration<double, std::milli>(clk::now() - t2).count();
+    for (int i = 0; i < nOps; ++i) results[i].stats.finishMs = finishMs;
     return OC_OK;
 }
 

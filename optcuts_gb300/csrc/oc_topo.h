@@ -87,6 +87,10 @@ struct TopoStats {
     long long totalTrials = 0;
     int airProblems = 0, airRejected = 0, airSteinerMax = 0, airCapped = 0;   // bijective form
     double buildMs = 0.0, solveMs = 0.0, probeMs = 0.0, exactMs = 0.0;
+    // host phases of the whole step (shared by its operations): inputs
+    // (positions, split filter, adjacency, air mesh copies), the air-loop
+    // sources, ranking (features, MLP, selection), candidate lists
+    double prepMs = 0.0, airMs = 0.0, rankMs = 0.0, finishMs = 0.0;
 };
 
 struct Mlp;
