@@ -903,9 +903,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, uint32_
     return false;
 }
 
+// Updaters of the pivot-part kernels: every warp but warp 0 and the warps
+// that share its SM sub-partition (warp % 4 == 0).  GB300's FP64 pipe takes
+// a warp instruction whole, so an updater's FMAs on warp 0's sub-partition
+// queue ahead of the chain's dependent steps (measured: ~9.5 us per 32-row
+// block on the top levels with them there).
+__host__ __device__ constexpr int upd_warps(int nt) { return nt / 32 - (nt / 32 + 3) / 4; }
+__device__ __forceinline__ int upd_rank(int warp) { return warp - 1 - warp / 4; }
+
 // Block sizes of the pivot-part kernels: warp 0 solves, the other NT - 32
 // threads update; a level's launch takes the size its largest front needs.
-constexpr int kFwdThreads = 512;
+constexpr int kFwdThreads = 384;   // 12 warps: up to 170 registers a thread
 constexpr int kSolveThreadsFor(int maxK) { return maxK <= 64 ? 64 : (maxK <= 384 ? 256 : kFwdThreads); }
 
 // Forward substitution, pivot part of one front (one CTA per front of the
@@ -942,8 +950,8 @@ __global__ void __launch_bounds__(NT) k_fwd(const int* __restrict__ fronts, cons
     if (threadIdx.x == 0) {
         mbar_init(&solved[0], 32);
         mbar_init(&solved[1], 32);
-        mbar_init(&updated[0], NT - 32);
-        mbar_init(&updated[1], NT - 32);
+        mbar_init(&updated[0], 32 * upd_warps(NT));
+        mbar_init(&updated[1], 32 * upd_warps(NT));
         abortFlag = 0;
     }
     __syncthreads();
@@ -958,47 +966,55 @@ __global__ void __launch_bounds__(NT) k_fwd(const int* __restrict__ fronts, cons
     const double* L = pool + foff[f];
     const int nb = (k + 31) / 32;
     if (warp == 0) {
+        double an = 0.0;   // this block's rows' sums over the previous block's columns
         for (int j = 0; j < nb; ++j) {
             const int c0 = 32 * j, w = min(32, k - c0);
             const int r = c0 + lane;
-            // the diagonal block's entries of this lane's row, loads first
-            double dl[32];
+            // the diagonal block's entries of this lane's row, and the next
+            // block's row entries of this block's columns, loads first
+            const int n0 = c0 + 32, wn = j + 1 < nb ? min(32, k - n0) : 0;
+            double dl[32], ln[32];
 #pragma unroll
             for (int c = 0; c < 32; ++c) dl[c] = (lane < w && c < w) ? L[r + (long long)(c0 + c) * m] : 0.0;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) ln[c] = lane < wn ? L[(n0 + lane) + (long long)(c0 + c) * m] : 0.0;
             // the updaters are done with block j-2 on this block's rows
             if (j >= 2 && !mbar_wait_bounded(&updated[j & 1], ((j - 2) >> 1) & 1, &abortFlag)) break;
-            if (j >= 1 && lane < w) {   // block j-1's columns on this block's rows
-                const int p0 = c0 - 32;
-                double lv[32];
-#pragma unroll
-                for (int c = 0; c < 32; ++c) lv[c] = L[r + (long long)(p0 + c) * m];
-                double acc = 0.0;
-#pragma unroll
-                for (int c = 0; c < 32; ++c) acc = fma(lv[c], sh[p0 + c], acc);
-                sh[r] -= acc;
-            }
+            // block j-1's columns on this block's rows, summed along the
+            // previous block's chain (one column per step, in column order)
+            if (j >= 1 && lane < w) sh[r] -= an;
 #pragma unroll
             for (int c = 0; c < 32; ++c)
                 if (lane < w) tile[lane * 33 + c] = dl[c];
             __syncwarp();
-            double v = lane < w ? sh[r] : 0.0;
-            for (int c = 0; c < w; ++c) {
-                const double yc = __shfl_sync(0xffffffffu, v, c);
-                if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
+            double v = lane < w ? sh[r] : 0.0, anNext = 0.0;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < w) {   // warp-uniform
+                    const double yc = __shfl_sync(0xffffffffu, v, c);
+                    if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
+                    anNext = fma(ln[c], yc, anNext);
+                }
             }
+            an = anNext;
             if (lane < w) sh[r] = v;
             __syncwarp();
             mbar_arrive(&solved[j & 1]);
         }
     }
-    else {
-        const int t = threadIdx.x - 32;
+    else if (warp & 3) {
+        constexpr int NU = 32 * upd_warps(NT);
+        const int t = 32 * upd_rank(warp) + lane;
         for (int b = 0; b < nb; ++b) {
             if (!mbar_wait_bounded(&solved[b & 1], (b >> 1) & 1, &abortFlag)) break;
             const int c0 = 32 * b, w = min(32, k - c0);
             // one row per thread and pass, the block's columns loaded at once;
-            // each row summed in column order
-            for (int r = c0 + 64 + t; r < k; r += NT - 32) {
+            // each row summed in column order.  Row r always belongs to
+            // updater r % NU: a thread finishes block b on its rows before
+            // it takes block b + 1, so every row takes the blocks in order
+            // whatever the other threads' progress
+            const int r0 = c0 + 64;
+            for (int r = r0 + ((t - r0) % NU + NU) % NU; r < k; r += NU) {
                 double lv[32];
 #pragma unroll
                 for (int c = 0; c < 32; ++c) lv[c] = c < w ? L[r + (long long)(c0 + c) * m] : 0.0;
@@ -1176,8 +1192,8 @@ __global__ void __launch_bounds__(NT) k_bwd(const int* __restrict__ fronts, cons
     if (threadIdx.x == 0) {
         mbar_init(&solved[0], 32);
         mbar_init(&solved[1], 32);
-        mbar_init(&updated[0], NT - 32);
-        mbar_init(&updated[1], NT - 32);
+        mbar_init(&updated[0], 32 * upd_warps(NT));
+        mbar_init(&updated[1], 32 * upd_warps(NT));
         abortFlag = 0;
     }
     __syncthreads();
@@ -1189,16 +1205,19 @@ __global__ void __launch_bounds__(NT) k_bwd(const int* __restrict__ fronts, cons
         for (int b = nb - 1; b >= 0; --b) {
             const int c0 = 32 * b, w = min(32, k - c0);
             const int c = c0 + lane;
-            double dl[32];   // the diagonal block's column of this lane, loads first
+            // the diagonal block's column of this lane and block b + 1's rows
+            // of it, loads first (the lookahead sums those rows in row order,
+            // so it cannot ride along the block below's chain, which yields
+            // its values from the last row down)
+            const int r0 = c0 + 32, w1 = b + 1 <= nb - 1 ? min(32, k - r0) : 0;
+            double dl[32], lv[32];
 #pragma unroll
             for (int r = 0; r < 32; ++r) dl[r] = (lane < w && r < w) ? L[(c0 + r) + (long long)c * m] : 0.0;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) lv[r] = (lane < w && r < w1) ? L[(r0 + r) + (long long)c * m] : 0.0;
             // the other warps are done with blocks b + 2 and above on these columns
             if (b + 2 <= nb - 1 && !mbar_wait_bounded(&updated[b & 1], parity(b + 2), &abortFlag)) break;
             if (b + 1 <= nb - 1 && lane < w) {   // block b + 1's rows on this block's columns
-                const int r0 = c0 + 32, w1 = min(32, k - r0);
-                double lv[32];
-#pragma unroll
-                for (int r = 0; r < 32; ++r) lv[r] = r < w1 ? L[(r0 + r) + (long long)c * m] : 0.0;
                 double acc = 0.0;
 #pragma unroll
                 for (int r = 0; r < 32; ++r)
@@ -1220,13 +1239,14 @@ __global__ void __launch_bounds__(NT) k_bwd(const int* __restrict__ fronts, cons
             mbar_arrive(&solved[b & 1]);
         }
     }
-    else {
-        const int t = threadIdx.x - 32;
+    else if (warp & 3) {
+        constexpr int NU = 32 * upd_warps(NT);
+        const int t = 32 * upd_rank(warp) + lane;
         for (int s = nb - 1; s >= 1; --s) {
             if (!mbar_wait_bounded(&solved[s & 1], parity(s), &abortFlag)) break;
             const int r0 = 32 * s, w = min(32, k - r0);
             // block s's rows on the columns before block s - 1
-            for (int c = t; c < 32 * (s - 1); c += NT - 32) {
+            for (int c = t; c < 32 * (s - 1); c += NU) {
                 double lv[32];
 #pragma unroll
                 for (int r = 0; r < 32; ++r) lv[r] = r < w ? L[(r0 + r) + (long long)c * m] : 0.0;
@@ -1252,9 +1272,11 @@ __global__ void __launch_bounds__(NT) k_bwd(const int* __restrict__ fronts, cons
 // blocks are dealt out round-robin: block j belongs to rank j % C.  Every CTA
 // holds the front's whole right-hand side in shared memory.  The owner of a
 // block applies the previous block's columns to it (lookahead) and runs the
-// same shuffle chain as k_fwd / k_bwd, then writes the 32 solved values into
-// every other CTA's shared memory (st.shared::cluster) followed by a release
-// arrive on that CTA's per-block mbarrier; each CTA's updaters wait (acquire,
+// same shuffle chain as k_fwd / k_bwd, then pushes the 32 solved values
+// into every other CTA's shared memory with asynchronous stores that count
+// their bytes off that CTA's per-block mbarrier (st.async ... complete_tx:
+// the sender waits for nothing; each receiving CTA posted the bytes it
+// expects per block at the start); each CTA's updaters wait (acquire,
 // cluster scope) for the block and apply it to the rows (forward) or columns
 // (backward) of the blocks it owns.  No cluster-wide barrier per block: the
 // chain passes from rank to rank through point-to-point mbarriers, the
@@ -1293,19 +1315,48 @@ __device__ __forceinline__ uint32_t cl_map(uint32_t a, uint32_t r)
     return out;
 }
 
-__device__ __forceinline__ void cl_store(uint32_t a, double v)
-{
-    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
-}
-
 __device__ __forceinline__ void cl_store_int(uint32_t a, int v)
 {
     asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void cl_arrive_remote(uint32_t a)
+// an asynchronous store of v into another CTA's shared memory that counts
+// its 8 bytes off that CTA's mbarrier (remBar, the same CTA's window): the
+// sender does not wait for the store, the receiver's barrier completes when
+// the bytes it expects have landed
+__device__ __forceinline__ void cl_store_async(uint32_t remAddr, double v, uint32_t remBar)
 {
-    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(a) : "memory");
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(remAddr),
+                 "l"(__double_as_longlong(v)), "r"(remBar)
+                 : "memory");
+}
+
+// this CTA's barrier b expects `bytes` of asynchronous stores (and takes
+// its one arrival)
+__device__ __forceinline__ void mbar_expect_bytes(unsigned long long* b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+
+// before leaving: every block pushed into this CTA has landed (waits that
+// find nothing coming end after a short bound; only after an abort)
+__device__ __forceinline__ void cl_drain(unsigned long long* recv, int nb, uint32_t C, uint32_t q)
+{
+    for (int j = 0; j < nb; ++j) {
+        if ((uint32_t)j % C == q) continue;
+        const uint32_t a = smem_addr(&recv[j]);
+        for (int i = 0; i < (1 << 16); ++i) {
+            uint32_t done;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}\n"
+                : "=r"(done)
+                : "r"(a), "r"(0u)
+                : "memory");
+            if (done) break;
+        }
+    }
 }
 
 // bounded wait with cluster-scope acquire (sees the remote CTAs' stores)
@@ -1347,8 +1398,9 @@ __global__ void __launch_bounds__(kClThreads) k_fwd_cl(const int* __restrict__ f
     extern __shared__ double sh[];
     __shared__ double tile[32 * 33];
     __shared__ unsigned long long recv[kClMaxBlocks], updated[kClMaxBlocks];
+    __shared__ double accIn[32];   // this CTA's next block: the previous block's columns on its rows
     __shared__ int abortFlag;
-    constexpr int NU = kClThreads - 32;   // updater threads
+    constexpr int NU = 32 * upd_warps(kClThreads);   // updater threads
     const uint32_t C = cl_size(), q = cl_rank();
     const int f = fronts[blockIdx.x / C];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
@@ -1356,12 +1408,22 @@ __global__ void __launch_bounds__(kClThreads) k_fwd_cl(const int* __restrict__ f
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = threadIdx.x; r < m; r += blockDim.x) sh[r] = r < k ? y[d0 + r] : 0.0;
     if (threadIdx.x == 0) {
+        // a block's values: this CTA's warp 0 (32 local arrivals) or
+        // another rank's asynchronous stores (one arrival here, the bytes)
         for (int j = 0; j < nb; ++j) {
-            mbar_init(&recv[j], 32);
+            mbar_init(&recv[j], (uint32_t)j % C == q ? 32 : 1);
             mbar_init(&updated[j], NU);
         }
         abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // block j's values, and with them, when block j + 1 is this CTA's,
+        // its rows' sums over block j's columns
+        for (int j = 0; j < nb; ++j)
+            if ((uint32_t)j % C != q) {
+                uint32_t bytes = 8u * (uint32_t)min(32, k - 32 * j);
+                if (j + 1 < nb && (uint32_t)(j + 1) % C == q) bytes += 8u * (uint32_t)min(32, k - 32 * (j + 1));
+                mbar_expect_bytes(&recv[j], bytes);
+            }
     }
     __syncthreads();
     for (int c = childOff[f]; c < childOff[f + 1]; ++c) {
@@ -1378,60 +1440,80 @@ __global__ void __launch_bounds__(kClThreads) k_fwd_cl(const int* __restrict__ f
         for (int j = (int)q; j < nb; j += (int)C) {
             const int c0 = 32 * j, w = min(32, k - c0);
             const int r = c0 + lane;
-            double dl[32], lv[32];
+            // the next block's rows (another rank's): their sums over this
+            // block's columns are accumulated along the chain, one column per
+            // step in column order -- the lookahead k_fwd runs after the chain
+            const int n0 = c0 + 32, wn = j + 1 < nb ? min(32, k - n0) : 0;
+            double dl[32], ln[32];
 #pragma unroll
             for (int c = 0; c < 32; ++c) dl[c] = (lane < w && c < w) ? L[r + (long long)(c0 + c) * m] : 0.0;
 #pragma unroll
-            for (int c = 0; c < 32; ++c) lv[c] = (j >= 1 && lane < w) ? L[r + (long long)(c0 - 32 + c) * m] : 0.0;
-            // block j-1 solved (by its owner) and this CTA's updaters done
-            // with block j-2 on these rows
+            for (int c = 0; c < 32; ++c) ln[c] = lane < wn ? L[(n0 + lane) + (long long)(c0 + c) * m] : 0.0;
+            // block j-1's values and its columns' sums on these rows (from
+            // its owner), and this CTA's updaters done with block j-2 here
             bool ok = j < 1 || cl_wait_bounded(&recv[j - 1], 0, &abortFlag);
             ok = ok && (j < 2 || cl_wait_bounded(&updated[j - 2], 0, &abortFlag));
             if (!__all_sync(0xffffffffu, ok)) break;
-            if (j >= 1 && lane < w) {
-                const int p0 = c0 - 32;
-                double acc = 0.0;
-#pragma unroll
-                for (int c = 0; c < 32; ++c) acc = fma(lv[c], sh[p0 + c], acc);
-                sh[r] -= acc;
-            }
+            if (j >= 1 && lane < w) sh[r] -= accIn[lane];
 #pragma unroll
             for (int c = 0; c < 32; ++c)
                 if (lane < w) tile[lane * 33 + c] = dl[c];
             __syncwarp();
-            double v = lane < w ? sh[r] : 0.0;
-            for (int c = 0; c < w; ++c) {
-                const double yc = __shfl_sync(0xffffffffu, v, c);
-                if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
+            double v = lane < w ? sh[r] : 0.0, an = 0.0;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < w) {   // warp-uniform
+                    const double yc = __shfl_sync(0xffffffffu, v, c);
+                    if (lane > c && lane < w) v -= tile[lane * 33 + c] * yc;
+                    an = fma(ln[c], yc, an);
+                }
             }
             if (lane < w) sh[r] = v;
             __syncwarp();
-            // publish: the 32 values into every other CTA, then its barrier
+            // publish: the w values into every other CTA, counted off its
+            // barrier for block j, and the next block's sums to its owner
+            // (on the same barrier there); then this CTA's own barrier
             const uint32_t av = smem_addr(&sh[c0 + (lane < w ? lane : 0)]), ab = smem_addr(&recv[j]);
-            for (uint32_t t = 1; t < C; ++t) {
-                const uint32_t dst = (q + t) % C;
-                if (lane < w) cl_store(cl_map(av, dst), v);
-                cl_arrive_remote(cl_map(ab, dst));
+            if (lane < w)
+                for (uint32_t t = 1; t < C; ++t) {
+                    const uint32_t dst = (q + t) % C;
+                    cl_store_async(cl_map(av, dst), v, cl_map(ab, dst));
+                }
+            if (lane < wn) {
+                const uint32_t nxt = (q + 1) % C;
+                cl_store_async(cl_map(smem_addr(&accIn[lane]), nxt), an, cl_map(ab, nxt));
             }
             mbar_arrive(&recv[j]);
         }
         if (abortFlag) cl_abort(&abortFlag, C);
     }
-    else {
-        const int t = threadIdx.x - 32;
+    else if (warp & 3) {
+        const int t = 32 * upd_rank(warp) + lane;
+        // this CTA's rows numbered 32 u + (r % 32) over its blocks q + u C;
+        // row number rho always belongs to updater rho % NU (a row takes the
+        // blocks in order, as in k_fwd)
+        const int nOwnAll = (int)q < nb ? (nb - 1 - (int)q) / (int)C + 1 : 0;
         for (int b = 0; b < nb; ++b) {
-            if (!cl_wait_bounded(&recv[b], 0, &abortFlag)) break;
             const int c0 = 32 * b, w = min(32, k - c0);
             // this CTA's blocks from b + 2 on: the first is the smallest
             // i >= b + 2 with i % C == q
-            int i0 = b + 2 + (int)((q + C - (uint32_t)((b + 2) % C)) % C);
-            const int nOwn = i0 < nb ? (nb - 1 - i0) / (int)C + 1 : 0;
-            for (int idx = t; idx < 32 * nOwn; idx += NU) {
-                const int r = 32 * (i0 + (idx >> 5) * (int)C) + (idx & 31);
-                if (r >= k) continue;
-                double lv[32];
+            const int i0 = b + 2 + (int)((q + C - (uint32_t)((b + 2) % C)) % C);
+            const int rho0 = 32 * ((i0 - (int)q) / (int)C);
+            const int rhoF = rho0 + ((t - rho0) % NU + NU) % NU;
+            // the first row's entries of block b's columns, loaded before the
+            // block's values arrive (the factor is final)
+            const int rF = rhoF < 32 * nOwnAll ? 32 * ((int)q + (rhoF >> 5) * (int)C) + (rhoF & 31) : k;
+            double lv[32];
 #pragma unroll
-                for (int c = 0; c < 32; ++c) lv[c] = c < w ? L[r + (long long)(c0 + c) * m] : 0.0;
+            for (int c = 0; c < 32; ++c) lv[c] = (rF < k && c < w) ? L[rF + (long long)(c0 + c) * m] : 0.0;
+            if (!cl_wait_bounded(&recv[b], 0, &abortFlag)) break;
+            for (int rho = rhoF; rho < 32 * nOwnAll; rho += NU) {
+                const int r = 32 * ((int)q + (rho >> 5) * (int)C) + (rho & 31);
+                if (r >= k) continue;
+                if (rho != rhoF) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) lv[c] = c < w ? L[r + (long long)(c0 + c) * m] : 0.0;
+                }
                 double acc = 0.0;
 #pragma unroll
                 for (int c = 0; c < 32; ++c)
@@ -1447,7 +1529,10 @@ __global__ void __launch_bounds__(kClThreads) k_fwd_cl(const int* __restrict__ f
         for (int r = 32 * j + threadIdx.x; r < min(k, 32 * j + 32); r += blockDim.x) y[d0 + r] = sh[r];
     if (q == 0)
         for (int r = k + threadIdx.x; r < m; r += blockDim.x) upd[fupd[f] + (r - k)] = sh[r];
-    if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
+    if (threadIdx.x == 0) {
+        cl_drain(recv, nb, C, q);
+        if (abortFlag) atomicExch(flag, 1);
+    }
     cl_sync();   // no CTA leaves while another may still write into it
 }
 
@@ -1463,7 +1548,7 @@ __global__ void __launch_bounds__(kClThreads) k_bwd_cl(const int* __restrict__ f
     __shared__ double tile[32 * 33];
     __shared__ unsigned long long recv[kClMaxBlocks], updated[kClMaxBlocks];
     __shared__ int abortFlag;
-    constexpr int NU = kClThreads - 32;
+    constexpr int NU = 32 * upd_warps(kClThreads);
     const uint32_t C = cl_size(), q = cl_rank();
     const int f = fronts[blockIdx.x / C];
     const int k = fk[f], m = fm[f], d0 = fdof[f];
@@ -1474,12 +1559,16 @@ __global__ void __launch_bounds__(kClThreads) k_bwd_cl(const int* __restrict__ f
     for (int r = threadIdx.x; r < k; r += blockDim.x)
         sh[r] = y[d0 + r] / L[r + (long long)r * m] - (rect ? tdot[d0 + r] : 0.0);
     if (threadIdx.x == 0) {
+        // a block's values: this CTA's warp 0 (32 local arrivals) or
+        // another rank's asynchronous stores (one arrival here, the bytes)
         for (int j = 0; j < nb; ++j) {
-            mbar_init(&recv[j], 32);
+            mbar_init(&recv[j], (uint32_t)j % C == q ? 32 : 1);
             mbar_init(&updated[j], NU);
         }
         abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int j = 0; j < nb; ++j)
+            if ((uint32_t)j % C != q) mbar_expect_bytes(&recv[j], 8u * (uint32_t)min(32, k - 32 * j));
     }
     __syncthreads();
     cl_sync();
@@ -1517,30 +1606,39 @@ __global__ void __launch_bounds__(kClThreads) k_bwd_cl(const int* __restrict__ f
             if (lane < w) sh[c] = v;
             __syncwarp();
             const uint32_t av = smem_addr(&sh[c0 + (lane < w ? lane : 0)]), ab = smem_addr(&recv[b]);
-            for (uint32_t t = 1; t < C; ++t) {
-                const uint32_t dst = (q + t) % C;
-                if (lane < w) cl_store(cl_map(av, dst), v);
-                cl_arrive_remote(cl_map(ab, dst));
-            }
+            if (lane < w)
+                for (uint32_t t = 1; t < C; ++t) {
+                    const uint32_t dst = (q + t) % C;
+                    cl_store_async(cl_map(av, dst), v, cl_map(ab, dst));
+                }
             mbar_arrive(&recv[b]);
         }
         if (abortFlag) cl_abort(&abortFlag, C);
     }
-    else {
-        const int t = threadIdx.x - 32;
+    else if (warp & 3) {
+        const int t = 32 * upd_rank(warp) + lane;
         for (int s = nb - 1; s >= 1; --s) {
-            if (!cl_wait_bounded(&recv[s], 0, &abortFlag)) break;
             const int r0 = 32 * s, w = min(32, k - r0);
             // this CTA's column blocks up to s - 2: the last is the largest
             // i <= s - 2 with i % C == q
             const int hi = s - 2;
             const int i1 = hi >= 0 ? hi - (int)((uint32_t)(hi + C - q) % C) : -1;
             const int nOwn = i1 >= 0 ? i1 / (int)C + 1 : 0;
-            for (int idx = t; idx < 32 * nOwn; idx += NU) {
-                const int c = 32 * (i1 - (idx >> 5) * (int)C) + (idx & 31);
-                double lv[32];
+            // this CTA's columns numbered 32 u + (c % 32) over its blocks
+            // q + u C; column number gam always belongs to updater gam % NU.
+            // The first column's entries of block s's rows are loaded before
+            // the block's values arrive (the factor is final)
+            const int cF = t < 32 * nOwn ? 32 * ((int)q + (t >> 5) * (int)C) + (t & 31) : -1;
+            double lv[32];
 #pragma unroll
-                for (int r = 0; r < 32; ++r) lv[r] = r < w ? L[(r0 + r) + (long long)c * m] : 0.0;
+            for (int r = 0; r < 32; ++r) lv[r] = (cF >= 0 && r < w) ? L[(r0 + r) + (long long)cF * m] : 0.0;
+            if (!cl_wait_bounded(&recv[s], 0, &abortFlag)) break;
+            for (int gam = t; gam < 32 * nOwn; gam += NU) {
+                const int c = 32 * ((int)q + (gam >> 5) * (int)C) + (gam & 31);
+                if (gam != t) {
+#pragma unroll
+                    for (int r = 0; r < 32; ++r) lv[r] = r < w ? L[(r0 + r) + (long long)c * m] : 0.0;
+                }
                 double acc = 0.0;
 #pragma unroll
                 for (int r = 0; r < 32; ++r)
@@ -1554,7 +1652,10 @@ __global__ void __launch_bounds__(kClThreads) k_bwd_cl(const int* __restrict__ f
     __syncthreads();
     for (int j = (int)q; j < nb; j += (int)C)
         for (int r = 32 * j + threadIdx.x; r < min(k, 32 * j + 32); r += blockDim.x) x[d0 + r] = sh[r];
-    if (threadIdx.x == 0 && abortFlag) atomicExch(flag, 1);
+    if (threadIdx.x == 0) {
+        cl_drain(recv, nb, C, q);   // block 0's values, which no updater waits for
+        if (abortFlag) atomicExch(flag, 1);
+    }
     cl_sync();
 }
 
