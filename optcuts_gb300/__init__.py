@@ -452,9 +452,12 @@ class TriMesh:
                 lib().oc_topo_result_candidates(h, ew.ctypes.data_as(_vp), ec.ctypes.data_as(_vp),
                                                 paths.ctypes.data_as(_vp), pos.ctypes.data_as(_vp),
                                                 rows.ctypes.data_as(_vp))
-            cands = [{"EwDec": float(ew[c]), "energyChanges": (float(ec[c, 0]), float(ec[c, 1])),
-                      "path": [int(x) for x in paths[c] if x >= 0],
-                      "newVertPos": pos[c, :2 * rows[c]].reshape(-1, 2)} for c in range(nc)]
+            # (plain lists first: per-element numpy indexing costs more than
+            # the query's own bookkeeping at ten thousand candidates)
+            ewl, ecl, pl, rl = ew.tolist(), ec.tolist(), paths.tolist(), rows.tolist()
+            p3 = pos.reshape(nc, 4, 2)
+            cands = [{"EwDec": ewl[c], "energyChanges": (ecl[c][0], ecl[c][1]),
+                      "path": [x for x in pl[c] if x >= 0], "newVertPos": p3[c, :rl[c]]} for c in range(nc)]
         finally:
             lib().oc_topo_result_destroy(h)
         b = best.value
