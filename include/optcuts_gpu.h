@@ -425,6 +425,12 @@ int oc_mlp_set_tensor_cores(oc_mlp* mlp, int on);
  * on the tensor cores (tensorCores 1) or the CUDA cores (0) */
 int oc_bf16_gemm(oc_ctx* ctx, int M, int N, int K, const float* A, long long sam, long long sak, const float* B,
                  long long sbk, long long sbn, float* C, int tensorCores);
+/* The bound of the tensor-core kernels' mbarrier waits for later launches,
+ * in polls (0: give up at once; -1: the default, 2^20; process-wide).  A
+ * wait that runs out ends that product with OC_ERR_TIMEOUT after its MMAs
+ * in flight have drained; the context stays usable.  A bound of 0
+ * exercises that path. */
+int oc_tc_set_wait_polls(int polls);
 /* candidate count, index of the largest E_w decrease (-1: none), size of
  * the filtered pool (inSplitTotalAmt for interior splits), local problems
  * solved, their largest iteration count, host build and device solve ms */

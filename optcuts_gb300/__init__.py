@@ -32,6 +32,7 @@ OC_OK = 0
 OC_ERR_INVALID = 1
 OC_ERR_INVERTED = 2
 OC_ERR_NOT_CONVERGED = 3
+OC_ERR_TIMEOUT = 4
 OC_ERR_NOT_SPD = 8
 
 
@@ -111,6 +112,7 @@ _SIGS = {
     "oc_optimizer_set_solve_cluster": [_vp, ctypes.c_int],
     "oc_linsys_set_solve_cluster": [_vp, ctypes.c_int],
     "oc_topo_result_host_phases": [_vp, _d],
+    "oc_tc_set_wait_polls": [ctypes.c_int],
     "oc_linsys_solve_clusters": [_vp, _i, _i],
     "oc_optimizer_solve_clusters": [_vp, _i, _i],
     "oc_optimizer_set_scaffold": [_vp, _d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double],

@@ -420,6 +420,13 @@ OC_EXPORT int oc_mlp_set_tensor_cores(oc_mlp* p, int on)
     return OC_OK;
 }
 
+OC_EXPORT int oc_tc_set_wait_polls(int polls)
+{
+    if (polls < -1) return OC_ERR_INVALID;
+    oc::tc_set_wait_polls(polls);
+    return OC_OK;
+}
+
 // C (M x N, row-major, host) = A(m, k) B(k, n) with host operands and
 // strides in elements, BF16 operands and FP32 accumulation, on the tensor
 // cores (tensorCores 1) or the CUDA cores (0)

@@ -16,6 +16,7 @@
 
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cstdint>
 
 namespace oc {
@@ -52,9 +53,9 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
            (static_cast<uint32_t>(M >> 4) << 24);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int polls = kWaitPolls)
 {
-    for (int i = 0; i < kWaitPolls; ++i) {
+    for (int i = 0; i < polls; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -95,7 +96,8 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(int M, int N, int K, con
                                                         long long sam, long long sak, const float* __restrict__ B,
                                                         long long sbk, long long sbn, float* __restrict__ C,
                                                         long long ldc, float alpha, float beta,
-                                                        const float* __restrict__ bias, int nInst, int* err)
+                                                        const float* __restrict__ bias, int nInst, int waitPolls,
+                                                        int* err)
 {
     __shared__ __align__(1024) uint8_t sA[kTcM * kTcK * 2];
     __shared__ __align__(1024) uint8_t sB[kTcN * kTcK * 2];
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(int M, int N, int K, con
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                          : "memory");
         }
-        ok = mbar_wait(bar, parity);
+        ok = mbar_wait(bar, parity, waitPolls);
         parity ^= 1u;
         // a block whose wait ran out stops here; every thread sees the same
         // mbarrier, but make the decision uniform anyway
@@ -245,6 +247,12 @@ __global__ void __launch_bounds__(256) k_gemm_bf16(int M, int N, int K, const fl
 
 } // namespace
 
+namespace {
+std::atomic<int> g_waitPolls{-1};   // -1: kWaitPolls
+}
+
+void tc_set_wait_polls(int polls) { g_waitPolls.store(polls < 0 ? -1 : polls); }
+
 cudaError_t gemm_tc(cudaStream_t st, int M, int N, int K, const float* A, long long sam, long long sak, const float* B,
                     long long sbk, long long sbn, float* C, long long ldc, float alpha, float beta, const float* bias,
                     int* err)
@@ -253,7 +261,9 @@ cudaError_t gemm_tc(cudaStream_t st, int M, int N, int K, const float* A, long l
     if (K <= 0 || !err) return cudaErrorInvalidValue;
     const int nInst = N >= kTcN ? kTcN : ((N + 15) / 16) * 16;
     dim3 grid((N + kTcN - 1) / kTcN, (M + kTcM - 1) / kTcM);
-    k_gemm_tc<<<grid, kTcThreads, 0, st>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, alpha, beta, bias, nInst, err);
+    const int polls = g_waitPolls.load();
+    k_gemm_tc<<<grid, kTcThreads, 0, st>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, alpha, beta, bias, nInst,
+                                           polls >= 0 ? polls : kWaitPolls, err);
     return cudaGetLastError();
 }
 

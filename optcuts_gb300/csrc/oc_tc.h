@@ -15,6 +15,13 @@ cudaError_t gemm_tc(cudaStream_t st, int M, int N, int K, const float* A, long l
                     long long sbk, long long sbn, float* C, long long ldc, float alpha, float beta, const float* bias,
                     int* err);
 
+// The bound of the in-loop mbarrier waits of later gemm_tc launches, in
+// polls (0: give up at once; -1: the default, 2^20; process-wide).  A wait
+// that runs out raises *err, waits for the MMAs in flight with the default
+// bound, releases the tensor memory and returns: a bound of 0 is how the
+// timeout path is tested without a fault.
+void tc_set_wait_polls(int polls);
+
 // The same product on the CUDA cores (BF16 operands, FP32 accumulation):
 // the reference the tensor-core kernel is tested against, and the form for
 // the one-column products (K or N of 1) of the network.

@@ -106,6 +106,28 @@ def test_tensor_core_gemm_matches_cuda_cores(M, N, K, ta, tb):
     np.testing.assert_allclose(tc, cc, rtol=0, atol=2e-5 * scale)
 
 
+def test_tensor_core_wait_timeout_is_reported():
+    """The bounded mbarrier wait of the tensor-core GEMM, made to run out
+    (a bound of 0 polls: the first stage's MMAs are in flight): the product
+    ends with OC_ERR_TIMEOUT after the kernel drained its MMAs and released
+    its tensor memory, and the next product on the same context, with the
+    default bound, is correct."""
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(1000, 128)).astype(np.float32)
+    B = rng.normal(size=(128, 128)).astype(np.float32)
+    assert oc.lib().oc_tc_set_wait_polls(0) == oc.OC_OK
+    try:
+        with pytest.raises(oc.OCError) as e:
+            oc.bf16_gemm(A, B, True)
+        assert e.value.status == oc.OC_ERR_TIMEOUT
+    finally:
+        assert oc.lib().oc_tc_set_wait_polls(-1) == oc.OC_OK
+    assert oc.lib().oc_tc_set_wait_polls(-2) == oc.OC_ERR_INVALID
+    tc = oc.bf16_gemm(A, B, True)
+    exact = ref.bf16(A).astype(np.float64) @ ref.bf16(B).astype(np.float64)
+    assert np.abs(tc - exact).max() <= 1e-5 * np.sqrt(128) * 4.0
+
+
 def test_network_on_tensor_cores_matches_cuda_cores():
     """The two product kernels accumulate in a different order, so a hidden
     activation can round to the neighbouring BF16 value (2^-8 relative) on
