@@ -2189,7 +2189,10 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
             probeMs = std::chrono::duration<double, std::milli>(tA - t1).count();
             // features -> predicted fraction of excess energy removed -> E_w decrease
             std::vector<float> X(n * kTopoNumFeatures), r(n);
-            for (size_t k = 0; k < n; ++k) topo_features(B.prob[k], res[k], opOf[k], in, &X[k * kTopoNumFeatures]);
+            host_parallel_for(n, 1024, [&](size_t k0, size_t k1) {
+                for (size_t k = k0; k < k1; ++k)
+                    topo_features(B.prob[k], res[k], opOf[k], in, &X[k * kTopoNumFeatures]);
+            });
             rc = mlp_predict_host(*opts.mlp, X.data(), static_cast<int>(n), r.data());
             if (rc) { if (err) *err = "topology query: MLP inference failed"; return rc; }
             std::fill(solved.begin(), solved.end(), 0);
@@ -2209,13 +2212,15 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
                 TopoExtras& ex = results[i].extras;
                 ex.ewPred.resize(ni);
                 for (int j = 0; j < ni; ++j) ex.ewPred[j] = -pred[j].first * (op == kOpInteriorSplit ? 0.5 : 1.0);
-                std::stable_sort(pred.begin(), pred.end());
                 // the top fraction, and never fewer than kMinExact problems
                 // (an operation with few candidates, a step's merges
-                // typically, is solved exhaustively)
+                // typically, is solved exhaustively): the kTop smallest
+                // (-decrease, index) pairs, a total order, so the set is the
+                // first kTop of the sorted list
                 constexpr int kMinExact = 32;
                 int kTop = static_cast<int>(std::ceil(opts.topFrac * ni));
                 kTop = std::max(std::min(ni, kMinExact), std::min(ni, kTop));
+                if (kTop < ni) std::nth_element(pred.begin(), pred.begin() + kTop, pred.end());
                 for (int q = 0; q < kTop; ++q) {
                     solved[start[i] + pred[q].second] = 1;
                     sel.push_back(static_cast<int>(start[i] + pred[q].second));
@@ -2243,13 +2248,15 @@ int topo_query_ops(const TopoQueryIn& in, const int* ops, int nOps, double lambd
                 const size_t ni = start[i + 1] - start[i];
                 ex.X.assign(ni * kTopoNumFeatures, 0.0f);
                 ex.target.assign(ni, 0.0f);
-                for (size_t j = 0; j < ni; ++j) {
-                    const size_t k = start[i] + j;
-                    topo_features(B.prob[k], res[k], ops[i], in, &ex.X[j * kTopoNumFeatures]);
-                    const double xs = excess_global(B.prob[k], res[k], in.surfaceArea);
-                    const double t = xs > 0.0 ? res[k].eDec / xs : 0.0;
-                    ex.target[j] = static_cast<float>(std::max(-1.0, std::min(1.0, t)));
-                }
+                host_parallel_for(ni, 1024, [&](size_t j0, size_t j1) {
+                    for (size_t j = j0; j < j1; ++j) {
+                        const size_t k = start[i] + j;
+                        topo_features(B.prob[k], res[k], ops[i], in, &ex.X[j * kTopoNumFeatures]);
+                        const double xs = excess_global(B.prob[k], res[k], in.surfaceArea);
+                        const double t = xs > 0.0 ? res[k].eDec / xs : 0.0;
+                        ex.target[j] = static_cast<float>(std::max(-1.0, std::min(1.0, t)));
+                    }
+                });
             }
         }
     }
