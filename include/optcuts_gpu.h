@@ -226,8 +226,12 @@ typedef struct {
                              the nodes' common ancestor) and only the front
                              structures are rebuilt; a full analysis when the
                              tree no longer separates the pattern, after 64
-                             carried analyses or once the factor cost grew 30%;
-                             0: a full analysis after every operation */
+                             carried analyses or once the factor cost grew 30%.
+                             A scaffold past the dense-clique size then keeps
+                             its air-only vertices in the root front (its air
+                             meshes' patterns change the front structures
+                             only); 0: a full analysis after every operation
+                             and every new air pattern */
 } oc_optimizer_config;
 
 int oc_optimizer_default_config(oc_optimizer_config* cfg);

@@ -597,7 +597,8 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
                        const int* extraF = nullptr, int nExtraF = 0, const std::vector<int>* clique = nullptr,
                        const double* xy = nullptr, const std::vector<unsigned char>* rowFixed = nullptr,
                        const int* nbPtr = nullptr, const int* nbIdx = nullptr,
-                       const std::vector<oc::NdNode>* carried = nullptr, int carriedRoot = -1)
+                       const std::vector<oc::NdNode>* carried = nullptr, int carriedRoot = -1,
+                       const std::vector<int>* rootVerts = nullptr)
 {
     oc_ctx* ctx = ls->ctx;
     auto t = std::chrono::steady_clock::now();
@@ -659,7 +660,8 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
                 done = ls->chol.valid && ls->chol.flops <= 1.3 * full;
             }
         }
-        if (!done) oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, clique, xy);
+        // a clique, or the given root set, is eliminated last as one front
+        if (!done) oc::chol_analyze(ls->chol, nV, ls->rowPtr.data(), ls->col.data(), 16, rootVerts ? rootVerts : clique, xy);
         ls->patternHostMs += ms_since(t);
         std::string err;
         int rc = oc::chol_upload(ls->chol, &err);
@@ -1913,7 +1915,7 @@ static bool carried_tree(oc_optimizer* o, int nSys, const std::vector<int>* cliq
     oc_mesh* m = o->mesh;
     oc_linsys* ls = o->ls;
     if (!o->cfg.carryAnalysis || ls->kind != OC_SOLVER_DIRECT || ls->analyzedVersion == ~0ULL ||
-        ls->analyzedVersion > m->topoVersion || (o->scaf && !o->cliqueMode))
+        ls->analyzedVersion > m->topoVersion)
         return false;
     std::vector<std::array<long long, 5>> edits;
     for (const auto& e : m->editLog)
@@ -1971,8 +1973,20 @@ static int ensure_pattern(oc_optimizer* o)
                                         &mask, nullptr, nullptr, carry ? &carried : nullptr, carriedRoot);
             }
             else {
+                // the exact air pattern (a scaffold too large for the clique):
+                // with carried analyses the air-only vertices form the root
+                // front above the mesh's dissection, a valid elimination tree
+                // for every air mesh of the same boundary (each path through
+                // the air crosses the root), so a rebuilt air mesh or a
+                // topology operation re-derives only the front structures
+                std::vector<int> airRoot;
+                if (o->cfg.carryAnalysis)
+                    for (int v = nV; v < o->nWhole; ++v) airRoot.push_back(v);
+                const std::vector<int>* root = airRoot.empty() ? nullptr : &airRoot;
+                const bool carry = root && carried_tree(o, o->nWhole, root, carried, carriedRoot);
                 rc = linsys_set_pattern(o->ls, o->nWhole, m->F.data(), m->d.nF, mask, o->airFw.data(),
-                                        static_cast<int>(o->airFw.size() / 3), nullptr, xyp);
+                                        static_cast<int>(o->airFw.size() / 3), nullptr, xyp, nullptr, nullptr,
+                                        nullptr, carry ? &carried : nullptr, carriedRoot, root);
             }
         }
         if (rc) {
