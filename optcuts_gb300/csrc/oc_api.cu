@@ -75,8 +75,9 @@ struct oc_linsys {
     bool patternSet = false;
     int kind = OC_SOLVER_DIRECT;
     oc::CholPlan chol;
-    // last set_pattern: host pattern + symbolic analysis, device allocation + upload (ms)
-    double patternHostMs = 0.0, patternDevMs = 0.0;
+    // last set_pattern: host pattern + symbolic analysis, device allocation + upload (ms);
+    // carryMs: the carried dissection tree it took (counted with the host part)
+    double patternHostMs = 0.0, patternDevMs = 0.0, carryMs = 0.0;
     // the mesh state the plan was analysed for: its topoVersion, mesh
     // vertex count (the system's first vertices) and whether the plan's
     // root front is a scaffold clique
@@ -201,38 +202,41 @@ bool rest_constants(const double* V_rest, const int* F, int nF, double areaThres
                     double& surfaceArea)
 {
     rest.resize(8 * (size_t)nF);
+    // per triangle on the host pool; the area is then summed in triangle
+    // order, as the reference's loop does
+    std::atomic<bool> invalid{false};
+    oc::host_parallel_for(nF, 4096, [&](size_t t0, size_t t1) {
+        for (size_t t = t0; t < t1; ++t) {
+            const double* P1 = V_rest + 3 * (size_t)F[3 * t];
+            const double* P2 = V_rest + 3 * (size_t)F[3 * t + 1];
+            const double* P3 = V_rest + 3 * (size_t)F[3 * t + 2];
+            const double a[3] = {P2[0] - P1[0], P2[1] - P1[1], P2[2] - P1[2]};
+            const double b[3] = {P3[0] - P1[0], P3[1] - P1[1], P3[2] - P1[2]};
+            const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            double* r = &rest[8 * t];
+            r[0] = 0.5 * std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            if (r[0] == 0.0) invalid = true;
+            if (r[0] < areaThres) {
+                r[0] = areaThres;
+                r[1] = areaThres * areaThres;
+                r[2] = r[3] = 4.0 / std::sqrt(3.0) * areaThres;
+                r[4] = r[2] / 2.0;
+                r[5] = r[6] = 2.0 / std::sqrt(3.0) / areaThres;
+                r[7] = r[5] / 2.0;
+            }
+            else {
+                r[1] = r[0] * r[0];
+                r[2] = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+                r[3] = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+                r[4] = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+                r[5] = r[2] / 2. / r[1];
+                r[6] = r[3] / 2. / r[1];
+                r[7] = r[4] / 2. / r[1];
+            }
+        }
+    });
     surfaceArea = 0.0;
-    bool invalid = false;
-    for (int t = 0; t < nF; ++t) {
-        const double* P1 = V_rest + 3 * (size_t)F[3 * t];
-        const double* P2 = V_rest + 3 * (size_t)F[3 * t + 1];
-        const double* P3 = V_rest + 3 * (size_t)F[3 * t + 2];
-        const double a[3] = {P2[0] - P1[0], P2[1] - P1[1], P2[2] - P1[2]};
-        const double b[3] = {P3[0] - P1[0], P3[1] - P1[1], P3[2] - P1[2]};
-        const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
-        double* r = &rest[8 * (size_t)t];
-        r[0] = 0.5 * std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-        if (r[0] == 0.0) invalid = true;
-        if (r[0] < areaThres) {
-            r[0] = areaThres;
-            surfaceArea += areaThres;
-            r[1] = areaThres * areaThres;
-            r[2] = r[3] = 4.0 / std::sqrt(3.0) * areaThres;
-            r[4] = r[2] / 2.0;
-            r[5] = r[6] = 2.0 / std::sqrt(3.0) / areaThres;
-            r[7] = r[5] / 2.0;
-        }
-        else {
-            surfaceArea += r[0];
-            r[1] = r[0] * r[0];
-            r[2] = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
-            r[3] = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
-            r[4] = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
-            r[5] = r[2] / 2. / r[1];
-            r[6] = r[3] / 2. / r[1];
-            r[7] = r[4] / 2. / r[1];
-        }
-    }
+    for (int t = 0; t < nF; ++t) surfaceArea += rest[8 * (size_t)t];   // the clamped area where clamped
     return !invalid;
 }
 
@@ -263,15 +267,17 @@ int device_mesh_upload(oc_ctx* ctx, oc::DeviceMesh& d, int nV, const int* F, int
     std::vector<int> f0(nF), f1(nF), f2(nF);
     std::vector<double> col[9];
     for (auto& c : col) c.resize(nF);
-    for (int t = 0; t < nF; ++t) {
-        f0[t] = F[3 * t]; f1[t] = F[3 * t + 1]; f2[t] = F[3 * t + 2];
-        const double* r = &rest[8 * (size_t)t];
-        col[0][t] = r[1];                    // triAreaSq
-        col[1][t] = r[0] / surfaceArea;      // w (SymDirichletEnergy.cpp:41)
-        col[2][t] = r[2]; col[3][t] = r[3]; col[4][t] = r[4];
-        col[5][t] = r[5]; col[6][t] = r[6]; col[7][t] = r[7];
-        col[8][t] = r[0];                    // triArea
-    }
+    oc::host_parallel_for(nF, 8192, [&](size_t t0, size_t t1) {
+        for (size_t t = t0; t < t1; ++t) {
+            f0[t] = F[3 * t]; f1[t] = F[3 * t + 1]; f2[t] = F[3 * t + 2];
+            const double* r = &rest[8 * t];
+            col[0][t] = r[1];                    // triAreaSq
+            col[1][t] = r[0] / surfaceArea;      // w (SymDirichletEnergy.cpp:41)
+            col[2][t] = r[2]; col[3][t] = r[3]; col[4][t] = r[4];
+            col[5][t] = r[5]; col[6][t] = r[6]; col[7][t] = r[7];
+            col[8][t] = r[0];                    // triArea
+        }
+    });
     // vertex -> corners, sorted by triangle id
     std::vector<int> vcPtr(nV + 1, 0), vcIdx(3 * (size_t)nF);
     for (int t = 0; t < nF; ++t)
@@ -562,11 +568,14 @@ bool carry_dissection(const oc::CholPlan& P, int oldMeshNV, const std::vector<st
     // vertices per node, in their old elimination order (the root: the
     // clique's order, then the vertices that stayed there)
     std::vector<std::vector<int>> S(nOld);
-    std::vector<int> ord(nSys);
-    std::iota(ord.begin(), ord.end(), 0);
-    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return vkey[x] < vkey[y]; });
-    for (int v : ord)
-        if (!inClique[v]) S[node[v]].push_back(v);
+    // the keys are distinct and below k: the order by key is a bucket fill
+    std::vector<int> byKey(static_cast<size_t>(k), -1);
+    for (int v = 0; v < nSys; ++v) {
+        if (vkey[v] < 0 || vkey[v] >= k || byKey[vkey[v]] >= 0) return false;
+        byKey[vkey[v]] = v;
+    }
+    for (int v : byKey)
+        if (v >= 0 && !inClique[v]) S[node[v]].push_back(v);
     if (clique) {
         std::vector<int> rs(clique->begin(), clique->end());
         rs.insert(rs.end(), S[root].begin(), S[root].end());
@@ -605,7 +614,8 @@ int linsys_set_pattern(oc_linsys* ls, int nV, const int* F, int nF, const std::v
     std::vector<int> cPtr, cIdx;
     build_pattern(nV, F, nF, mask, ls->rowPtr, ls->col, ls->diagSlot, cPtr, cIdx, extraF, nExtraF, clique, nbPtr,
                   nbIdx);
-    ls->patternHostMs = ms_since(t);
+    ls->patternHostMs = ms_since(t) + ls->carryMs;
+    ls->carryMs = 0.0;
     ls->patternDevMs = 0.0;
     ls->rowFixed = rowFixed ? *rowFixed : mask;
     free_bsr(ls->b);
@@ -953,12 +963,19 @@ static int mesh_rebuild(oc_mesh* m, const std::vector<double>& uvHost)
     double avg = 0.0;
     const double* Vr = m->Vrest.data();
     const int* F = m->F.data();
-    for (int t = 0; t < nF; ++t)
-        for (int j = 0; j < 3; ++j) {
-            const double* p = Vr + 3 * (size_t)F[3 * t + j];
-            const double* q = Vr + 3 * (size_t)F[3 * t + (j + 1) % 3];
-            avg += std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]));
-        }
+    {   // edge lengths on the host pool, summed in triangle order
+        std::vector<double> el(3 * (size_t)nF);
+        oc::host_parallel_for(nF, 4096, [&](size_t t0, size_t t1) {
+            for (size_t t = t0; t < t1; ++t)
+                for (int j = 0; j < 3; ++j) {
+                    const double* p = Vr + 3 * (size_t)F[3 * t + j];
+                    const double* q = Vr + 3 * (size_t)F[3 * t + (j + 1) % 3];
+                    el[3 * t + j] = std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
+                                              (p[2] - q[2]) * (p[2] - q[2]));
+                }
+        });
+        for (double x : el) avg += x;
+    }
     m->scalars[0] = surfaceArea;
     m->scalars[1] = avg / (3.0 * nF);
     m->scalars[2] = std::sqrt(surfaceArea / M_PI);
@@ -1550,7 +1567,7 @@ int oc_linsys_destroy(oc_linsys* ls)
     if (!ls) return OC_ERR_INVALID;
     free_bsr(ls->b);
     oc::pcg_free(ls->wk);
-    oc::chol_free(ls->chol);
+    oc::chol_destroy(ls->chol);
     cudaFree(ls->dFlag); cudaFree(ls->tmpIn); cudaFree(ls->tmpOut);
     delete ls;
     return OC_OK;
@@ -1923,7 +1940,10 @@ static bool carried_tree(oc_optimizer* o, int nSys, const std::vector<int>* cliq
     if (edits.size() != m->topoVersion - ls->analyzedVersion) return false;
     for (size_t i = 0; i < edits.size(); ++i)
         if (static_cast<unsigned long long>(edits[i][0]) != ls->analyzedVersion + 1 + i) return false;
-    return carry_dissection(ls->chol, ls->analyzedMeshNV, edits, m->d.nV, nSys, clique, out, root);
+    auto t = std::chrono::steady_clock::now();
+    const bool ok = carry_dissection(ls->chol, ls->analyzedMeshNV, edits, m->d.nV, nSys, clique, out, root);
+    ls->carryMs = ms_since(t);
+    return ok;
 }
 
 static int ensure_pattern(oc_optimizer* o)

@@ -224,8 +224,10 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
     const auto t0 = std::chrono::steady_clock::now();
     {
         const int cl = P.solveCluster;
+        const CholPlan::Keep keep = P.keep;
         P = CholPlan{};
         P.solveCluster = cl;
+        P.keep = keep;
     }
     // the bisection needs an order on the coordinates: BFS alone unless all are finite
     if (xy)
@@ -280,11 +282,13 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
     {
         const double ndMs = P.ndMs, fullFlops = P.fullFlops;
         const int inc = P.incremental, cl = P.solveCluster;
+        const CholPlan::Keep keep = P.keep;
         P = CholPlan{};
         P.ndMs = ndMs;
         P.fullFlops = fullFlops;
         P.incremental = inc;
         P.solveCluster = cl;
+        P.keep = keep;
     }
     P.nV = nV;
     P.nDof = 2 * nV;
@@ -1659,14 +1663,6 @@ __global__ void __launch_bounds__(kClThreads) k_bwd_cl(const int* __restrict__ f
     cl_sync();
 }
 
-template <typename T>
-cudaError_t up(T** d, const std::vector<T>& h)
-{
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(d), sizeof(T) * (h.empty() ? 1 : h.size()));
-    if (e != cudaSuccess) return e;
-    if (!h.empty()) e = cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
-    return e;
-}
 
 } // namespace
 
@@ -1678,21 +1674,65 @@ int chol_upload(CholPlan& P, std::string* err)
     }
     cudaError_t e = cudaSuccess;
     auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-    chk(cudaMalloc(&P.pool, sizeof(double) * (size_t)std::max<long long>(P.poolSize, 1)));
-    chk(cudaMalloc(&P.upd, sizeof(double) * (size_t)std::max<long long>(P.updSize, 1)));
-    chk(cudaMalloc(&P.yperm, sizeof(double) * (size_t)std::max(P.nDof, 1)));
-    chk(cudaMalloc(&P.xperm, sizeof(double) * (size_t)std::max(P.nDof, 1)));
-    chk(up(&P.dPermDof, P.permDof)); chk(up(&P.dFk, P.fk)); chk(up(&P.dFm, P.fm));
-    chk(up(&P.dFdofStart, P.fdofStart)); chk(up(&P.dFrowOff, P.frowOff)); chk(up(&P.dFoff, P.foff));
-    chk(up(&P.dFupd, P.fupd)); chk(up(&P.dRowIdx, P.rowIdx)); chk(up(&P.dChildOff, P.childOff));
-    chk(up(&P.dChildList, P.childList)); chk(up(&P.dRelOff, P.relOff)); chk(up(&P.dRelIdx, P.relIdx));
-    chk(up(&P.dLevelFronts, P.levelFronts)); chk(up(&P.dTasks, P.tasks)); chk(up(&P.dAsmDest, P.asmDest));
-    chk(up(&P.dAsmLd, P.asmLd)); chk(up(&P.dAsmDiag, P.asmDiag));
-    chk(up(&P.dRectRowTasks, P.rectRowTasks)); chk(up(&P.dRectColTasks, P.rectColTasks));
-    chk(cudaMalloc(&P.tmpDot, sizeof(double) * (size_t)std::max(P.nDof, 1)));
-    chk(cudaMalloc(&P.dFlag, sizeof(int)));
-    chk(cudaMalloc(&P.dSolveFlag, sizeof(int)));
-    chk(cudaMemset(P.dSolveFlag, 0, sizeof(int)));
+    // a buffer of at least `need` elements, grown by a quarter when too small
+    auto grow = [&](auto*& ptr, size_t& cap, size_t need) {
+        if (e != cudaSuccess || (ptr && cap >= need)) return;
+        cudaFree(ptr);
+        ptr = nullptr;
+        cap = 0;
+        const size_t want = need + need / 4 + 64;
+        chk(cudaMalloc(reinterpret_cast<void**>(&ptr), sizeof(*ptr) * want));
+        if (e == cudaSuccess) cap = want;
+    };
+    CholPlan::Keep& K = P.keep;
+    grow(K.pool, K.poolCap, (size_t)std::max<long long>(P.poolSize, 1));
+    grow(K.upd, K.updCap, (size_t)std::max<long long>(P.updSize, 1));
+    grow(K.vec, K.vecCap, 3 * (size_t)std::max(P.nDof, 1));
+    if (!K.flags) chk(cudaMalloc(reinterpret_cast<void**>(&K.flags), 2 * sizeof(int)));
+    // the index arrays, each at a 256-byte-aligned offset of one buffer
+    struct Part { void** dst; const void* src; size_t bytes; };
+    const Part parts[] = {
+        {reinterpret_cast<void**>(&P.dPermDof), P.permDof.data(), sizeof(int) * P.permDof.size()},
+        {reinterpret_cast<void**>(&P.dFk), P.fk.data(), sizeof(int) * P.fk.size()},
+        {reinterpret_cast<void**>(&P.dFm), P.fm.data(), sizeof(int) * P.fm.size()},
+        {reinterpret_cast<void**>(&P.dFdofStart), P.fdofStart.data(), sizeof(int) * P.fdofStart.size()},
+        {reinterpret_cast<void**>(&P.dFrowOff), P.frowOff.data(), sizeof(int) * P.frowOff.size()},
+        {reinterpret_cast<void**>(&P.dFoff), P.foff.data(), sizeof(long long) * P.foff.size()},
+        {reinterpret_cast<void**>(&P.dFupd), P.fupd.data(), sizeof(long long) * P.fupd.size()},
+        {reinterpret_cast<void**>(&P.dRowIdx), P.rowIdx.data(), sizeof(int) * P.rowIdx.size()},
+        {reinterpret_cast<void**>(&P.dChildOff), P.childOff.data(), sizeof(int) * P.childOff.size()},
+        {reinterpret_cast<void**>(&P.dChildList), P.childList.data(), sizeof(int) * P.childList.size()},
+        {reinterpret_cast<void**>(&P.dRelOff), P.relOff.data(), sizeof(int) * P.relOff.size()},
+        {reinterpret_cast<void**>(&P.dRelIdx), P.relIdx.data(), sizeof(int) * P.relIdx.size()},
+        {reinterpret_cast<void**>(&P.dLevelFronts), P.levelFronts.data(), sizeof(int) * P.levelFronts.size()},
+        {reinterpret_cast<void**>(&P.dTasks), P.tasks.data(), sizeof(TileTask) * P.tasks.size()},
+        {reinterpret_cast<void**>(&P.dAsmDest), P.asmDest.data(), sizeof(long long) * P.asmDest.size()},
+        {reinterpret_cast<void**>(&P.dAsmLd), P.asmLd.data(), sizeof(int) * P.asmLd.size()},
+        {reinterpret_cast<void**>(&P.dAsmDiag), P.asmDiag.data(), sizeof(unsigned char) * P.asmDiag.size()},
+        {reinterpret_cast<void**>(&P.dRectRowTasks), P.rectRowTasks.data(), sizeof(int2) * P.rectRowTasks.size()},
+        {reinterpret_cast<void**>(&P.dRectColTasks), P.rectColTasks.data(), sizeof(int2) * P.rectColTasks.size()},
+    };
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    size_t total = 0;
+    for (const Part& q : parts) total += al(std::max<size_t>(q.bytes, 1));
+    grow(K.idx, K.idxCap, total);
+    if (e == cudaSuccess) {
+        size_t off = 0;
+        for (const Part& q : parts) {
+            *q.dst = K.idx + off;
+            if (q.bytes) chk(cudaMemcpyAsync(K.idx + off, q.src, q.bytes, cudaMemcpyHostToDevice, 0));
+            off += al(std::max<size_t>(q.bytes, 1));
+        }
+        P.pool = K.pool;
+        P.upd = K.upd;
+        P.yperm = K.vec;
+        P.xperm = K.vec + std::max(P.nDof, 1);
+        P.tmpDot = K.vec + 2 * (size_t)std::max(P.nDof, 1);
+        P.dFlag = K.flags;
+        P.dSolveFlag = K.flags + 1;
+        chk(cudaMemsetAsync(P.dSolveFlag, 0, sizeof(int), 0));
+        chk(cudaStreamSynchronize(0));
+    }
     if (e != cudaSuccess) {
         if (err) *err = std::string("chol upload: ") + cudaGetErrorString(e);
         chol_free(P);
@@ -1709,12 +1749,6 @@ void chol_free(CholPlan& P)
     P.factGraph = P.solveGraph = nullptr;
     P.factKey = nullptr;
     P.solveKey[0] = P.solveKey[1] = nullptr;
-    cudaFree(P.pool); cudaFree(P.upd); cudaFree(P.yperm); cudaFree(P.xperm);
-    cudaFree(P.dPermDof); cudaFree(P.dFk); cudaFree(P.dFm); cudaFree(P.dFdofStart); cudaFree(P.dFrowOff);
-    cudaFree(P.dFoff); cudaFree(P.dFupd); cudaFree(P.dRowIdx); cudaFree(P.dChildOff); cudaFree(P.dChildList);
-    cudaFree(P.dRelOff); cudaFree(P.dRelIdx); cudaFree(P.dLevelFronts); cudaFree(P.dTasks);
-    cudaFree(P.dAsmDest); cudaFree(P.dAsmLd); cudaFree(P.dAsmDiag); cudaFree(P.dFlag); cudaFree(P.dSolveFlag);
-    cudaFree(P.dRectRowTasks); cudaFree(P.dRectColTasks); cudaFree(P.tmpDot);
     P.dRectRowTasks = P.dRectColTasks = nullptr;
     P.tmpDot = nullptr;
     P.pool = P.upd = P.yperm = P.xperm = nullptr;
@@ -1728,6 +1762,17 @@ void chol_free(CholPlan& P)
     P.dFlag = nullptr;
     P.dSolveFlag = nullptr;
     P.onDevice = false;
+}
+
+void chol_destroy(CholPlan& P)
+{
+    chol_free(P);
+    cudaFree(P.keep.idx);
+    cudaFree(P.keep.pool);
+    cudaFree(P.keep.upd);
+    cudaFree(P.keep.vec);
+    cudaFree(P.keep.flags);
+    P.keep = CholPlan::Keep{};
 }
 
 static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)

@@ -77,7 +77,22 @@ struct CholPlan {
     std::vector<int> asmLd;              // per slot: leading dimension (front m)
     std::vector<unsigned char> asmDiag;  // per slot: diagonal block (lower half only)
 
-    // ---- device copies ----
+    // ---- device memory kept across analyses (grown with headroom, freed by
+    // chol_destroy): the index arrays at 256-byte-aligned offsets of one
+    // buffer, the front pool, the update vectors, the three DOF vectors and
+    // the two flags
+    struct Keep {
+        char* idx = nullptr;
+        size_t idxCap = 0;
+        double* pool = nullptr;
+        size_t poolCap = 0;
+        double* upd = nullptr;
+        size_t updCap = 0;
+        double* vec = nullptr;
+        size_t vecCap = 0;
+        int* flags = nullptr;
+    } keep;
+    // ---- device copies (views into keep) ----
     double* pool = nullptr;
     double* upd = nullptr;
     double* yperm = nullptr;     // nDof
@@ -121,7 +136,11 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
 void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, const std::vector<NdNode>& nodes,
                         int rootNode);
 int chol_upload(CholPlan& P, std::string* err);
+// drops the plan's device views and captured graphs (the kept device memory
+// stays for the next upload)
 void chol_free(CholPlan& P);
+// chol_free, and the kept device memory released
+void chol_destroy(CholPlan& P);
 // Numeric factorisation of the block-CSR values (FP32 storage, FP64 fronts).
 int chol_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st, std::string* err, int* nBadPivots);
 // Solves A x = sign * rhs.
