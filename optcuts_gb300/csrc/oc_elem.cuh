@@ -140,9 +140,11 @@ __device__ void jacobi_eig6(double A[6][6], double V[6][6])
 // Gram-Schmidt), A rotated into it, then FP64 cyclic Jacobi sweeps on the
 // nearly diagonal result until the off-diagonal mass reaches the rounding
 // floor, each rotation updating only the entries it changes.  Only IEEE
-// operations (division, square root) so that a host restatement compiled
-// without contraction rounds identically.  On return A's diagonal holds the
-// eigenvalues and V the eigenvectors as columns.
+// operations (division, square root, and explicit fused multiply-adds where
+// a product meets a sum: one rounding, half the FP64 instructions of a
+// product and a sum in this file's no-contraction build), so that a host
+// restatement with std::fma rounds identically.  On return A's diagonal
+// holds the eigenvalues and V the eigenvectors as columns.
 __device__ void eig6_mixed(double A[6][6], double V[6][6])
 {
     double s = 0.0;
@@ -205,11 +207,11 @@ __device__ void eig6_mixed(double A[6][6], double V[6][6])
         for (int r = 0; r < 6; ++r) v[r] = static_cast<double>(Vf[r][c]);
         for (int p = 0; p < c; ++p) {
             double d = 0.0;
-            for (int r = 0; r < 6; ++r) d = d + Q[r][p] * v[r];
-            for (int r = 0; r < 6; ++r) v[r] = v[r] - d * Q[r][p];
+            for (int r = 0; r < 6; ++r) d = fma(Q[r][p], v[r], d);
+            for (int r = 0; r < 6; ++r) v[r] = fma(-d, Q[r][p], v[r]);
         }
         double n2 = 0.0;
-        for (int r = 0; r < 6; ++r) n2 = n2 + v[r] * v[r];
+        for (int r = 0; r < 6; ++r) n2 = fma(v[r], v[r], n2);
         const double in = 1.0 / sqrt(n2);
         for (int r = 0; r < 6; ++r) Q[r][c] = v[r] * in;
     }
@@ -217,13 +219,13 @@ __device__ void eig6_mixed(double A[6][6], double V[6][6])
     for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 6; ++c) {
             double acc = 0.0;
-            for (int k = 0; k < 6; ++k) acc = acc + A[r][k] * Q[k][c];
+            for (int k = 0; k < 6; ++k) acc = fma(A[r][k], Q[k][c], acc);
             T[r][c] = acc;
         }
     for (int r = 0; r < 6; ++r)
         for (int c = r; c < 6; ++c) {
             double acc = 0.0;
-            for (int k = 0; k < 6; ++k) acc = acc + Q[k][r] * T[k][c];
+            for (int k = 0; k < 6; ++k) acc = fma(Q[k][r], T[k][c], acc);
             A[r][c] = acc;
         }
     for (int r = 0; r < 6; ++r)
@@ -232,12 +234,12 @@ __device__ void eig6_mixed(double A[6][6], double V[6][6])
         for (int j = 0; j < 6; ++j) V[i][j] = Q[i][j];
     double fro = 0.0;
     for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) fro = fro + A[i][j] * A[i][j];
+        for (int j = 0; j < 6; ++j) fro = fma(A[i][j], A[i][j], fro);
     double prevOff = 0.0;
     for (int sweep = 0; sweep < 40; ++sweep) {
         double off = 0.0;
         for (int p = 0; p < 6; ++p)
-            for (int q = p + 1; q < 6; ++q) off = off + A[p][q] * A[p][q];
+            for (int q = p + 1; q < 6; ++q) off = fma(A[p][q], A[p][q], off);
         if (off <= 1e-34 * fro || (sweep > 0 && off >= prevOff)) break;
         prevOff = off;
         for (int p = 0; p < 6; ++p)
@@ -245,16 +247,16 @@ __device__ void eig6_mixed(double A[6][6], double V[6][6])
                 const double apq = A[p][q];
                 if (apq == 0.0) continue;
                 const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-                A[p][p] = A[p][p] - t * apq;
-                A[q][q] = A[q][q] + t * apq;
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+                const double c = 1.0 / sqrt(fma(t, t, 1.0)), sn = t * c;
+                A[p][p] = fma(-t, apq, A[p][p]);
+                A[q][q] = fma(t, apq, A[q][q]);
                 A[p][q] = 0.0;
                 A[q][p] = 0.0;
                 for (int k = 0; k < 6; ++k) {
                     if (k == p || k == q) continue;
                     const double akp = A[k][p], akq = A[k][q];
-                    const double np = c * akp - sn * akq, nq = sn * akp + c * akq;
+                    const double np = fma(c, akp, -(sn * akq)), nq = fma(sn, akp, c * akq);
                     A[k][p] = np;
                     A[p][k] = np;
                     A[k][q] = nq;
@@ -262,8 +264,8 @@ __device__ void eig6_mixed(double A[6][6], double V[6][6])
                 }
                 for (int k = 0; k < 6; ++k) {
                     const double vkp = V[k][p], vkq = V[k][q];
-                    V[k][p] = c * vkp - sn * vkq;
-                    V[k][q] = sn * vkp + c * vkq;
+                    V[k][p] = fma(c, vkp, -(sn * vkq));
+                    V[k][q] = fma(sn, vkp, c * vkq);
                 }
             }
     }
@@ -561,7 +563,7 @@ __device__ void tri_hessian(const double2 U[3], double triAreaSq, double e0d, do
         for (int i = 0; i < 6; ++i)
             for (int j = 0; j < 6; ++j) {
                 double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += V[i][k] * lam[k] * V[j][k];
+                for (int k = 0; k < 6; ++k) s = fma(V[i][k] * lam[k], V[j][k], s);
                 H[i][j] = s;
             }
     }

@@ -109,9 +109,10 @@ void jacobi_eig(double A[6][6], double V[6][6], int n)
 // basis), that basis made orthonormal in double precision (modified
 // Gram-Schmidt), A rotated into it (B = Q^T A Q, upper triangle mirrored),
 // then double-precision cyclic Jacobi sweeps that update only the entries a
-// rotation changes (diagonal by a_pp - t a_pq, a_qq + t a_pq).  Compiled
-// without contraction, every operation rounds as on the device.  Non-finite
-// or all-zero input falls back to jacobi_eig.
+// rotation changes (diagonal by a_pp - t a_pq, a_qq + t a_pq), the products
+// meeting sums as explicit std::fma.  Compiled without contraction, every
+// operation rounds as on the device.  Non-finite or all-zero input falls
+// back to jacobi_eig.
 void eig6_mixed(double A[6][6], double V[6][6])
 {
     double s = 0.0;
@@ -175,11 +176,11 @@ void eig6_mixed(double A[6][6], double V[6][6])
         for (int r = 0; r < 6; ++r) v[r] = static_cast<double>(Vf[r][c]);
         for (int p = 0; p < c; ++p) {
             double d = 0.0;
-            for (int r = 0; r < 6; ++r) d = d + Q[r][p] * v[r];
-            for (int r = 0; r < 6; ++r) v[r] = v[r] - d * Q[r][p];
+            for (int r = 0; r < 6; ++r) d = std::fma(Q[r][p], v[r], d);
+            for (int r = 0; r < 6; ++r) v[r] = std::fma(-d, Q[r][p], v[r]);
         }
         double n2 = 0.0;
-        for (int r = 0; r < 6; ++r) n2 = n2 + v[r] * v[r];
+        for (int r = 0; r < 6; ++r) n2 = std::fma(v[r], v[r], n2);
         const double in = 1.0 / std::sqrt(n2);
         for (int r = 0; r < 6; ++r) Q[r][c] = v[r] * in;
     }
@@ -187,13 +188,13 @@ void eig6_mixed(double A[6][6], double V[6][6])
     for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 6; ++c) {
             double acc = 0.0;
-            for (int k = 0; k < 6; ++k) acc = acc + A[r][k] * Q[k][c];
+            for (int k = 0; k < 6; ++k) acc = std::fma(A[r][k], Q[k][c], acc);
             T[r][c] = acc;
         }
     for (int r = 0; r < 6; ++r)
         for (int c = r; c < 6; ++c) {
             double acc = 0.0;
-            for (int k = 0; k < 6; ++k) acc = acc + Q[k][r] * T[k][c];
+            for (int k = 0; k < 6; ++k) acc = std::fma(Q[k][r], T[k][c], acc);
             A[r][c] = acc;
         }
     for (int r = 0; r < 6; ++r)
@@ -201,12 +202,12 @@ void eig6_mixed(double A[6][6], double V[6][6])
     std::memcpy(V, Q, sizeof(Q));
     double fro = 0.0;
     for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) fro = fro + A[i][j] * A[i][j];
+        for (int j = 0; j < 6; ++j) fro = std::fma(A[i][j], A[i][j], fro);
     double prevOff = 0.0;
     for (int sweep = 0; sweep < 40; ++sweep) {
         double off = 0.0;
         for (int p = 0; p < 6; ++p)
-            for (int q = p + 1; q < 6; ++q) off = off + A[p][q] * A[p][q];
+            for (int q = p + 1; q < 6; ++q) off = std::fma(A[p][q], A[p][q], off);
         if (off <= 1e-34 * fro || (sweep > 0 && off >= prevOff)) break;
         prevOff = off;
         for (int p = 0; p < 6; ++p)
@@ -214,16 +215,16 @@ void eig6_mixed(double A[6][6], double V[6][6])
                 const double apq = A[p][q];
                 if (apq == 0.0) continue;
                 const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
-                A[p][p] = A[p][p] - t * apq;
-                A[q][q] = A[q][q] + t * apq;
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(std::fma(theta, theta, 1.0)));
+                const double c = 1.0 / std::sqrt(std::fma(t, t, 1.0)), sn = t * c;
+                A[p][p] = std::fma(-t, apq, A[p][p]);
+                A[q][q] = std::fma(t, apq, A[q][q]);
                 A[p][q] = 0.0;
                 A[q][p] = 0.0;
                 for (int k = 0; k < 6; ++k) {
                     if (k == p || k == q) continue;
                     const double akp = A[k][p], akq = A[k][q];
-                    const double np = c * akp - sn * akq, nq = sn * akp + c * akq;
+                    const double np = std::fma(c, akp, -(sn * akq)), nq = std::fma(sn, akp, c * akq);
                     A[k][p] = np;
                     A[p][k] = np;
                     A[k][q] = nq;
@@ -231,8 +232,8 @@ void eig6_mixed(double A[6][6], double V[6][6])
                 }
                 for (int k = 0; k < 6; ++k) {
                     const double vkp = V[k][p], vkq = V[k][q];
-                    V[k][p] = c * vkp - sn * vkq;
-                    V[k][q] = sn * vkp + c * vkq;
+                    V[k][p] = std::fma(c, vkp, -(sn * vkq));
+                    V[k][q] = std::fma(sn, vkp, c * vkq);
                 }
             }
     }
@@ -259,7 +260,7 @@ void make_pd(double H[6][6])
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) {
             double s = 0.0;
-            for (int k = 0; k < 6; ++k) s += V[i][k] * lam[k] * V[j][k];
+            for (int k = 0; k < 6; ++k) s = std::fma(V[i][k] * lam[k], V[j][k], s);
             H[i][j] = s;
         }
 }
