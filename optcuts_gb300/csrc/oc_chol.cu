@@ -210,11 +210,13 @@ __host__ __device__ __forceinline__ void tile_bounds(int k, int m, int t, int& s
 
 // rows of a tile row per panel-solve block (one warp per row)
 constexpr int kPanelRows = 8;
-// trailing updates: 32 x 32 blocks when a launch has fewer 64 x 64 blocks
-// than eight per SM on 152 SMs (measured at 199k: 15.5 ms per factorisation
-// with a threshold of two per SM, 15.3 with four, 14.7 with eight)
+// trailing updates in 32 x 32 blocks (2 x 2 per thread): finer than 64 x 64
+// blocks, so the launches' last waves leave less of the GPU idle.  Measured
+// per factorisation: 199k 14.68 ms with 64 x 64 blocks wherever a launch had
+// at least eight per SM, 13.99 ms with 32 x 32 everywhere; 2M triangles 212
+// against 203 ms; the same bits either way (each entry takes the same FMA
+// chain over the panel's columns)
 constexpr int kUpdSmall = 32;
-constexpr long long kUpdSplitBlocks = 8 * 152;
 
 } // namespace
 
@@ -484,31 +486,17 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
             }
             if ((int)T.size() > off) Ls.push_back({1, l, p, off, (int)T.size() - off, 0});
             // trailing region [s, m) x [s, m), s = end of panel p, in the
-            // lower triangle of 64 x 64 blocks, or of 32 x 32 blocks when
-            // there are fewer than kUpdSplitBlocks 64 x 64 ones
-            auto blocks_of = [&](int f, int edge) {
-                const int s = std::min((p + 1) * kTile, P.fk[f]);
-                const int nb = (P.fm[f] - s + edge - 1) / edge;
-                return nb;
-            };
-            long long n64 = 0;
-            for (int i = 0; i < nl; ++i) {
-                const int f = lf[i];
-                if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
-                const long long nb = blocks_of(f, kUpd);
-                n64 += nb * (nb + 1) / 2;
-            }
-            const int edge = n64 < kUpdSplitBlocks ? kUpdSmall : kUpd;
+            // lower triangle of kUpdSmall x kUpdSmall blocks
             off = static_cast<int>(T.size());
             for (int i = 0; i < nl; ++i) {
                 const int f = lf[i];
                 if ((P.fk[f] + kTile - 1) / kTile <= p) continue;
-                const int nb = blocks_of(f, edge);
+                const int s0 = std::min((p + 1) * kTile, P.fk[f]);
+                const int nb = (P.fm[f] - s0 + kUpdSmall - 1) / kUpdSmall;
                 for (int bj = 0; bj < nb; ++bj)
                     for (int bi = bj; bi < nb; ++bi) T.push_back(TileTask{f, bi, bj, p});
             }
-            if ((int)T.size() > off)
-                Ls.push_back({edge == kUpd ? 3 : 5, l, p, off, (int)T.size() - off, 0});
+            if ((int)T.size() > off) Ls.push_back({5, l, p, off, (int)T.size() - off, 0});
         }
     });
     {
@@ -778,9 +766,9 @@ __global__ void __launch_bounds__(32 * kPanelRows) k_ldl_panel(const TileTask* _
 // of panel p, in B x B blocks (task: block row bi, block column bj <= bi,
 // lower triangle only).  256 threads, P x P accumulators each (B = 16 P);
 // the panel columns of both block rows are staged column-major in shared
-// memory so a thread's rows (or columns) are 16-byte reads.  B = 64 in
-// general; B = 32 for launches too small to fill the GPU with 64 x 64
-// blocks (four times the blocks, a quarter of the work each).
+// memory so a thread's rows (or columns) are 16-byte reads.  Launched with
+// B = 32 (kUpdSmall): four times the blocks of B = 64, a quarter of the work
+// each, and less of the GPU idle in a launch's last wave.
 template <int B, int P>
 __global__ void __launch_bounds__(256) k_ldl_update(const TileTask* __restrict__ tasks, const int* __restrict__ fk,
                                                     const int* __restrict__ fm, const long long* __restrict__ foff,
@@ -1786,8 +1774,9 @@ static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)
         case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
         case 1: k_ldl_panel<<<L.taskCount, 32 * kPanelRows, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
         case 4: k_ldl_diag<<<L.taskCount, kDiagThreads, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        case 5: k_ldl_update<32, 2><<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        default: k_ldl_update<kUpd, 4><<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+        default:   // 5
+            k_ldl_update<kUpdSmall, 2><<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag);
+            break;
         }
     }
 }

@@ -11,7 +11,6 @@
 namespace oc {
 
 constexpr int kTile = 32;      // dense tile edge (FP64) of the front kernels
-constexpr int kUpd = 64;       // edge of the trailing-update blocks (FP64, 4x4 per thread)
 constexpr int kRectRows = 32;  // rows of L21 per CTA in the forward GEMV (a warp's lanes)
 constexpr int kRectCols = 8;   // columns of L21 per CTA in the backward GEMV^T (a warp each)
 // levels whose fronts all have at most kNarrowK pivots use the narrow
@@ -58,9 +57,9 @@ struct CholPlan {
     int maxM = 0;
     // per-level front lists and tiled task lists
     std::vector<int> levelFrontOff, levelFronts;
-    // kind: 0 extend-add of child slot `child`, 1 panel solve, 3 trailing
-    // update in 64 x 64 blocks, 5 in 32 x 32 blocks (both also factor the
-    // next panel's diagonal tile), 4 the first panel's diagonal tiles
+    // kind: 0 extend-add of child slot `child`, 1 panel solve, 5 trailing
+    // update in 32 x 32 blocks (which also factors the next panel's diagonal
+    // tile), 4 the first panel's diagonal tiles
     struct Launch { int kind; int level; int p; int taskOff; int taskCount; int child; };
     std::vector<Launch> launches;        // in execution order
     std::vector<TileTask> tasks;
