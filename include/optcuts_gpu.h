@@ -154,6 +154,13 @@ int oc_linsys_set_solve_cluster(oc_linsys* ls, int maxCluster);
 /* Tree levels of the current plan whose substitutions run as clusters, and
  * the largest cluster size among them (1 when none). */
 int oc_linsys_solve_clusters(oc_linsys* ls, int* levels, int* largest);
+/* No reference counterpart (a launch choice of the direct solver): the most
+ * CUDA streams (1..4) the factorization's independent subtrees may run on,
+ * from the next analysis (set_pattern) on.  The factor is the same bits for
+ * every value.  Default 4. */
+int oc_linsys_set_factor_streams(oc_linsys* ls, int streams);
+/* Streams and subtree groups the current plan's factorization uses. */
+int oc_linsys_factor_streams(oc_linsys* ls, int* streams, int* groups);
 /* Symbolic statistics of the direct solver: out[0..7] = fronts, tree levels,
  * largest front rows, front pool doubles, factor flops, tiled launches,
  * factor entries (sum of m*k), DOF. */
@@ -276,6 +283,11 @@ int oc_optimizer_solver_stats(oc_optimizer* opt, double* out8);
 int oc_optimizer_set_solve_cluster(oc_optimizer* opt, int maxCluster);
 /* oc_linsys_solve_clusters on the optimizer's own solver. */
 int oc_optimizer_solve_clusters(oc_optimizer* opt, int* levels, int* largest);
+/* oc_linsys_set_factor_streams on the optimizer's own solver (call before
+ * precompute to cover every analysis). */
+int oc_optimizer_set_factor_streams(oc_optimizer* opt, int streams);
+/* oc_linsys_factor_streams on the optimizer's own solver. */
+int oc_optimizer_factor_streams(oc_optimizer* opt, int* streams, int* groups);
 
 /* ---- Scaffold (Scaffold.hpp:18-70; Optimizer.cpp scaffolding branches) ---
  * Replaces `scaffold = Scaffold(result, UV_bnds, E, bnd)` (Optimizer.cpp:

@@ -111,10 +111,14 @@ _SIGS = {
     "oc_optimizer_solver_stats": [_vp, _d],
     "oc_optimizer_set_solve_cluster": [_vp, ctypes.c_int],
     "oc_linsys_set_solve_cluster": [_vp, ctypes.c_int],
+    "oc_linsys_set_factor_streams": [_vp, ctypes.c_int],
+    "oc_linsys_factor_streams": [_vp, _i, _i],
     "oc_topo_result_host_phases": [_vp, _d],
     "oc_tc_set_wait_polls": [ctypes.c_int],
     "oc_linsys_solve_clusters": [_vp, _i, _i],
     "oc_optimizer_solve_clusters": [_vp, _i, _i],
+    "oc_optimizer_set_factor_streams": [_vp, ctypes.c_int],
+    "oc_optimizer_factor_streams": [_vp, _i, _i],
     "oc_optimizer_set_scaffold": [_vp, _d, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_double],
     "oc_optimizer_clear_scaffold": [_vp],
     "oc_optimizer_rebuild_scaffold": [_vp],
@@ -615,6 +619,18 @@ class LinSysSolver:
         """(tree levels whose substitutions run as clusters, largest cluster)"""
         a, b = ctypes.c_int(), ctypes.c_int()
         self.ctx.check(lib().oc_linsys_solve_clusters(self.h, ctypes.byref(a), ctypes.byref(b)), "solve_clusters")
+        return a.value, b.value
+
+    def set_factor_streams(self, streams):
+        """Most CUDA streams (1..4) for the factorization's independent
+        subtrees, from the next set_pattern on; the factor is the same bits
+        for every value."""
+        self.ctx.check(lib().oc_linsys_set_factor_streams(self.h, int(streams)), "set_factor_streams")
+
+    def factor_streams(self):
+        """(streams, subtree groups) of the current plan's factorization"""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().oc_linsys_factor_streams(self.h, ctypes.byref(a), ctypes.byref(b)), "factor_streams")
         return a.value, b.value
 
     def factorize(self):
@@ -1171,6 +1187,17 @@ class Optimizer:
         """LinSysSolver.solve_clusters on this optimizer's own solver."""
         a, b = ctypes.c_int(), ctypes.c_int()
         self.ctx.check(lib().oc_optimizer_solve_clusters(self.h, ctypes.byref(a), ctypes.byref(b)), "solve_clusters")
+        return a.value, b.value
+
+    def set_factor_streams(self, streams):
+        """LinSysSolver.set_factor_streams on this optimizer's own solver
+        (before precompute, to cover every analysis)."""
+        self.ctx.check(lib().oc_optimizer_set_factor_streams(self.h, int(streams)), "set_factor_streams")
+
+    def factor_streams(self):
+        """LinSysSolver.factor_streams on this optimizer's own solver."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        self.ctx.check(lib().oc_optimizer_factor_streams(self.h, ctypes.byref(a), ctypes.byref(b)), "factor_streams")
         return a.value, b.value
 
     def launch_count(self):

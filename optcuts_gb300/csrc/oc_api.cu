@@ -1597,6 +1597,22 @@ int oc_linsys_set_solve_cluster(oc_linsys* ls, int maxCluster)
     return OC_OK;
 }
 
+int oc_linsys_set_factor_streams(oc_linsys* ls, int streams)
+{
+    if (!ls || streams < 1 || streams > oc::CholPlan::kMaxFactStreams) return OC_ERR_INVALID;
+    oc::chol_set_factor_streams(ls->chol, streams);
+    return OC_OK;
+}
+
+int oc_linsys_factor_streams(oc_linsys* ls, int* streams, int* groups)
+{
+    if (!ls || !streams || !groups) return OC_ERR_INVALID;
+    const bool direct = ls->kind == OC_SOLVER_DIRECT && ls->patternSet;
+    *streams = direct ? ls->chol.nFactStreams : 1;
+    *groups = direct ? static_cast<int>(ls->chol.grpStream.size()) : 0;
+    return OC_OK;
+}
+
 int oc_linsys_solve_clusters(oc_linsys* ls, int* levels, int* largest)
 {
     if (!ls || !levels || !largest) return OC_ERR_INVALID;
@@ -2421,6 +2437,18 @@ int oc_optimizer_solve_clusters(oc_optimizer* o, int* levels, int* largest)
 {
     if (!o) return OC_ERR_INVALID;
     return oc_linsys_solve_clusters(o->ls, levels, largest);
+}
+
+int oc_optimizer_set_factor_streams(oc_optimizer* o, int streams)
+{
+    if (!o) return OC_ERR_INVALID;
+    return oc_linsys_set_factor_streams(o->ls, streams);
+}
+
+int oc_optimizer_factor_streams(oc_optimizer* o, int* streams, int* groups)
+{
+    if (!o) return OC_ERR_INVALID;
+    return oc_linsys_factor_streams(o->ls, streams, groups);
 }
 
 int oc_optimizer_set_scaffold(oc_optimizer* o, const double* airV, int nAirV, const int* airF, int nAirF,

@@ -225,10 +225,11 @@ void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int le
 {
     const auto t0 = std::chrono::steady_clock::now();
     {
-        const int cl = P.solveCluster;
+        const int cl = P.solveCluster, fs = P.factStreams;
         const CholPlan::Keep keep = P.keep;
         P = CholPlan{};
         P.solveCluster = cl;
+        P.factStreams = fs;
         P.keep = keep;
     }
     // the bisection needs an order on the coordinates: BFS alone unless all are finite
@@ -283,13 +284,14 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
     const auto t0 = std::chrono::steady_clock::now();
     {
         const double ndMs = P.ndMs, fullFlops = P.fullFlops;
-        const int inc = P.incremental, cl = P.solveCluster;
+        const int inc = P.incremental, cl = P.solveCluster, fs = P.factStreams;
         const CholPlan::Keep keep = P.keep;
         P = CholPlan{};
         P.ndMs = ndMs;
         P.fullFlops = fullFlops;
         P.incremental = inc;
         P.solveCluster = cl;
+        P.factStreams = fs;
         P.keep = keep;
     }
     P.nV = nV;
@@ -430,22 +432,133 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
         std::vector<int> fill(P.levelFrontOff.begin(), P.levelFrontOff.end() - 1);
         for (int f = 0; f < nF; ++f) P.levelFronts[fill[P.flevel[f]]++] = f;
     }
-    // launch schedule: per level, extend-add per child slot, the first
-    // panel's diagonal tiles, then per panel the panel solve and the trailing
-    // update (whose first block also factors the next panel's diagonal tile).
-    // Levels are independent: each is built on its own host task, then the
-    // lists are joined in level order.
+    // factorization groups, for launches on up to factStreams streams.  A
+    // subtree is cut below its top chain, at the first node with two to four
+    // big children (big: at least 5% of the factor flops; a chain node's small
+    // children stay with the chain): the big subtrees run concurrently, the
+    // first on the subtree's stream, the others on streams of their own, and
+    // the chain, with every small subtree hanging off it, joins them.  Cuts
+    // are made largest subtree first while streams are left; uncut subtrees
+    // are leaf groups.  Groups are numbered in postorder, so every group
+    // comes after those it waits for.
+    std::vector<int> grp(nF, 0);
+    {
+        std::vector<double> fl(nF, 0.0);   // subtree flops (children come first)
+        for (int f = 0; f < nF; ++f) {
+            const double kk = P.fk[f], r = (double)P.fm[f] - P.fk[f];
+            fl[f] += kk * kk * kk / 3.0 + kk * kk * r + kk * r * r;
+            for (int c : nodes[f].children) fl[f] += fl[c];
+        }
+        std::vector<int> roots;
+        double total = 0.0;
+        for (int f = 0; f < nF; ++f)
+            if (parent[f] < 0) {
+                roots.push_back(f);
+                total += fl[f];
+            }
+        const auto big = [&](int c) { return fl[c] >= 0.05 * total; };
+        // subtree r (-1: the forest of all roots) -> its big children below
+        // the chain of nodes with one big child
+        auto split_of = [&](int r) {
+            std::vector<int> bigK;
+            for (;;) {
+                bigK.clear();
+                for (int c : r < 0 ? roots : nodes[r].children)
+                    if (big(c)) bigK.push_back(c);
+                if (bigK.size() != 1) return bigK;
+                r = bigK[0];
+            }
+        };
+        const int top = roots.size() == 1 ? roots[0] : -1;
+        std::vector<char> cut(nF + 1, 0);   // indexed by subtree root + 1
+        {
+            std::vector<int> leaves{top};
+            int streams = 1;
+            for (;;) {
+                int best = -2;
+                double bestFl = -1.0;
+                for (int r : leaves) {
+                    const size_t k = split_of(r).size();
+                    const double rf = r < 0 ? total : fl[r];
+                    if (k >= 2 && k <= 4 && streams + (int)k - 1 <= P.factStreams && rf > bestFl) {
+                        best = r;
+                        bestFl = rf;
+                    }
+                }
+                if (best == -2) break;
+                cut[best + 1] = 1;
+                const std::vector<int> kids = split_of(best);
+                streams += static_cast<int>(kids.size()) - 1;
+                leaves.erase(std::find(leaves.begin(), leaves.end(), best));
+                leaves.insert(leaves.end(), kids.begin(), kids.end());
+            }
+        }
+        // r's subtree into group g, except the subtrees of `stop`
+        auto mark = [&](int r, const std::vector<int>& stop, int g) {
+            std::vector<int> stack{r};
+            while (!stack.empty()) {
+                const int f = stack.back();
+                stack.pop_back();
+                grp[f] = g;
+                for (int c : nodes[f].children)
+                    if (std::find(stop.begin(), stop.end(), c) == stop.end()) stack.push_back(c);
+            }
+        };
+        int streamsUsed = 1;
+        // returns the group that finishes subtree r
+        std::function<int(int, int)> build = [&](int r, int stream) -> int {
+            std::vector<int> kids, kidGroups;
+            if (cut[r + 1]) {
+                kids = split_of(r);
+                for (size_t i = 0; i < kids.size(); ++i)
+                    kidGroups.push_back(build(kids[i], i == 0 ? stream : streamsUsed++));
+            }
+            const int g = static_cast<int>(P.grpStream.size());
+            P.grpStream.push_back(stream);
+            for (int d : kidGroups)   // waits between streams only
+                if (P.grpStream[d] != stream) P.grpWait.push_back(d);
+            P.grpWaitOff.push_back(static_cast<int>(P.grpWait.size()));
+            if (r < 0) {   // the forest: every tree that is not one of the big subtrees
+                for (int c : roots)
+                    if (std::find(kids.begin(), kids.end(), c) == kids.end()) mark(c, kids, g);
+            }
+            else mark(r, kids, g);   // a leaf group, or the chain with its small subtrees
+            return g;
+        };
+        P.grpWaitOff.assign(1, 0);
+        build(top, 0);
+        P.nFactStreams = streamsUsed;
+        if ((int)P.grpStream.size() > CholPlan::kMaxFactGroups) {   // cannot happen: <= 2 x streams - 1
+            std::fill(grp.begin(), grp.end(), 0);
+            P.grpStream.assign(1, 0);
+            P.grpWaitOff.assign(2, 0);
+            P.grpWait.clear();
+            P.nFactStreams = 1;
+        }
+    }
+    const int nGrp = static_cast<int>(P.grpStream.size());
+    std::vector<std::vector<int>> glf(static_cast<size_t>(nGrp) * P.nLevels);
+    for (int l = 0; l < P.nLevels; ++l)
+        for (int i = P.levelFrontOff[l]; i < P.levelFrontOff[l + 1]; ++i) {
+            const int f = P.levelFronts[i];
+            glf[static_cast<size_t>(grp[f]) * P.nLevels + l].push_back(f);
+        }
+    // launch schedule: per group and level, extend-add per child slot, the
+    // first panel's diagonal tiles, then per panel the panel solve and the
+    // trailing update (whose first block also factors the next panel's
+    // diagonal tile).  Each (group, level) is built on its own host task,
+    // then the lists are joined group by group in level order.
     struct LevelSched {
         std::vector<TileTask> tasks;
         std::vector<CholPlan::Launch> launches;
     };
-    std::vector<LevelSched> sched(P.nLevels);
-    host_run_tasks(P.nLevels, [&](size_t li) {
-        const int l = static_cast<int>(li);
-        std::vector<TileTask>& T = sched[l].tasks;
-        std::vector<CholPlan::Launch>& Ls = sched[l].launches;
-        const int* lf = P.levelFronts.data() + P.levelFrontOff[l];
-        const int nl = P.levelFrontOff[l + 1] - P.levelFrontOff[l];
+    std::vector<LevelSched> sched(static_cast<size_t>(nGrp) * P.nLevels);
+    host_run_tasks(sched.size(), [&](size_t item) {
+        const int l = static_cast<int>(item % P.nLevels);
+        std::vector<TileTask>& T = sched[item].tasks;
+        std::vector<CholPlan::Launch>& Ls = sched[item].launches;
+        const int* lf = glf[item].data();
+        const int nl = static_cast<int>(glf[item].size());
         int maxKids = 0, maxPanels = 0;
         for (int i = 0; i < nl; ++i) {
             const int f = lf[i];
@@ -500,17 +613,20 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
         }
     });
     {
-        std::vector<size_t> base(P.nLevels + 1, 0);
-        for (int l = 0; l < P.nLevels; ++l) base[l + 1] = base[l] + sched[l].tasks.size();
-        P.tasks.resize(base[P.nLevels]);
-        host_run_tasks(P.nLevels, [&](size_t l) {
-            std::copy(sched[l].tasks.begin(), sched[l].tasks.end(), P.tasks.begin() + base[l]);
+        std::vector<size_t> base(sched.size() + 1, 0);
+        for (size_t i = 0; i < sched.size(); ++i) base[i + 1] = base[i] + sched[i].tasks.size();
+        P.tasks.resize(base[sched.size()]);
+        host_run_tasks(sched.size(), [&](size_t i) {
+            std::copy(sched[i].tasks.begin(), sched[i].tasks.end(), P.tasks.begin() + base[i]);
         });
-        for (int l = 0; l < P.nLevels; ++l)
-            for (CholPlan::Launch L : sched[l].launches) {
-                L.taskOff += static_cast<int>(base[l]);
+        P.grpLaunchOff.assign(1, 0);
+        for (size_t i = 0; i < sched.size(); ++i) {
+            for (CholPlan::Launch L : sched[i].launches) {
+                L.taskOff += static_cast<int>(base[i]);
                 P.launches.push_back(L);
             }
+            if ((i + 1) % P.nLevels == 0) P.grpLaunchOff.push_back(static_cast<int>(P.launches.size()));
+        }
     }
     // substitution chunks of the rectangular part of each front, per level
     P.rectRowOff.assign(P.nLevels + 1, 0);
@@ -1718,6 +1834,15 @@ int chol_upload(CholPlan& P, std::string* err)
         P.tmpDot = K.vec + 2 * (size_t)std::max(P.nDof, 1);
         P.dFlag = K.flags;
         P.dSolveFlag = K.flags + 1;
+        if (P.nFactStreams > 1 && !K.fork) {   // the factorization's streams and events
+            chk(cudaEventCreateWithFlags(&K.fork, cudaEventDisableTiming));
+            for (int a = 0; a < CholPlan::kMaxFactStreams - 1 && e == cudaSuccess; ++a) {
+                chk(cudaStreamCreateWithFlags(&K.aux[a], cudaStreamNonBlocking));
+                chk(cudaEventCreateWithFlags(&K.join[a], cudaEventDisableTiming));
+            }
+            for (int g = 0; g < CholPlan::kMaxFactGroups && e == cudaSuccess; ++g)
+                chk(cudaEventCreateWithFlags(&K.grpEnd[g], cudaEventDisableTiming));
+        }
         chk(cudaMemsetAsync(P.dSolveFlag, 0, sizeof(int), 0));
         chk(cudaStreamSynchronize(0));
     }
@@ -1760,6 +1885,13 @@ void chol_destroy(CholPlan& P)
     cudaFree(P.keep.upd);
     cudaFree(P.keep.vec);
     cudaFree(P.keep.flags);
+    for (int a = 0; a < CholPlan::kMaxFactStreams - 1; ++a) {
+        if (P.keep.aux[a]) cudaStreamDestroy(P.keep.aux[a]);
+        if (P.keep.join[a]) cudaEventDestroy(P.keep.join[a]);
+    }
+    for (int g = 0; g < CholPlan::kMaxFactGroups; ++g)
+        if (P.keep.grpEnd[g]) cudaEventDestroy(P.keep.grpEnd[g]);
+    if (P.keep.fork) cudaEventDestroy(P.keep.fork);
     P.keep = CholPlan::Keep{};
 }
 
@@ -1768,16 +1900,37 @@ static void enqueue_factorize(CholPlan& P, const DeviceBsr& b, cudaStream_t st)
     cudaMemsetAsync(P.pool, 0, sizeof(double) * (size_t)P.poolSize, st);
     cudaMemsetAsync(P.dFlag, 0, sizeof(int), st);
     k_asm_fronts<<<(b.nnzb + 255) / 256, 256, 0, st>>>(b.val, P.dAsmDest, P.dAsmLd, P.dAsmDiag, b.nnzb, P.pool);
-    for (const auto& L : P.launches) {
-        const TileTask* t = P.dTasks + L.taskOff;
-        switch (L.kind) {
-        case 0: k_extend<<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
-        case 1: k_ldl_panel<<<L.taskCount, 32 * kPanelRows, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
-        case 4: k_ldl_diag<<<L.taskCount, kDiagThreads, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
-        default:   // 5
-            k_ldl_update<kUpdSmall, 2><<<L.taskCount, 256, 0, st>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag);
-            break;
+    // the groups' streams fork off after the assembly; each group waits for
+    // the ends of the groups it joins, runs its launches and records its own
+    // end; every stream joins st at the end
+    const int nS = P.keep.fork ? P.nFactStreams : 1;
+    const int nG = static_cast<int>(P.grpStream.size());
+    if (nS > 1) {
+        cudaEventRecord(P.keep.fork, st);
+        for (int a = 1; a < nS; ++a) cudaStreamWaitEvent(P.keep.aux[a - 1], P.keep.fork, 0);
+    }
+    for (int g = 0; g < nG; ++g) {
+        const cudaStream_t ls = (nS > 1 && P.grpStream[g] > 0) ? P.keep.aux[P.grpStream[g] - 1] : st;
+        if (nS > 1)
+            for (int i = P.grpWaitOff[g]; i < P.grpWaitOff[g + 1]; ++i)
+                cudaStreamWaitEvent(ls, P.keep.grpEnd[P.grpWait[i]], 0);
+        for (int li = P.grpLaunchOff[g]; li < P.grpLaunchOff[g + 1]; ++li) {
+            const CholPlan::Launch& L = P.launches[li];
+            const TileTask* t = P.dTasks + L.taskOff;
+            switch (L.kind) {
+            case 0: k_extend<<<L.taskCount, 256, 0, ls>>>(t, P.dFk, P.dFm, P.dFoff, P.dRelOff, P.dRelIdx, P.pool); break;
+            case 1: k_ldl_panel<<<L.taskCount, 32 * kPanelRows, 0, ls>>>(t, P.dFk, P.dFm, P.dFoff, P.pool); break;
+            case 4: k_ldl_diag<<<L.taskCount, kDiagThreads, 0, ls>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag); break;
+            default:   // 5
+                k_ldl_update<kUpdSmall, 2><<<L.taskCount, 256, 0, ls>>>(t, P.dFk, P.dFm, P.dFoff, P.pool, P.dFlag);
+                break;
+            }
         }
+        if (nS > 1) cudaEventRecord(P.keep.grpEnd[g], ls);
+    }
+    for (int a = 1; a < nS; ++a) {
+        cudaEventRecord(P.keep.join[a - 1], P.keep.aux[a - 1]);
+        cudaStreamWaitEvent(st, P.keep.join[a - 1], 0);
     }
 }
 
@@ -1923,6 +2076,11 @@ int chol_solve_cluster_levels(const CholPlan& P, int* largest)
     }
     if (largest) *largest = big;
     return n;
+}
+
+void chol_set_factor_streams(CholPlan& P, int streams)
+{
+    P.factStreams = std::max(1, std::min(streams, (int)CholPlan::kMaxFactStreams));
 }
 
 void chol_set_solve_cluster(CholPlan& P, int maxCluster)

@@ -61,6 +61,14 @@ struct CholPlan {
     // update in 32 x 32 blocks (which also factors the next panel's diagonal
     // tile), 4 the first panel's diagonal tiles
     struct Launch { int kind; int level; int p; int taskOff; int taskCount; int child; };
+    // factorization groups (subtrees and the chains that join them): group
+    // g's launches launches[grpLaunchOff[g] .. grpLaunchOff[g+1]) run on
+    // stream grpStream[g] (0 = the caller's stream), after the ends of groups
+    // grpWait[grpWaitOff[g] .. grpWaitOff[g+1])
+    static constexpr int kMaxFactStreams = 4, kMaxFactGroups = 2 * kMaxFactStreams;
+    int factStreams = kMaxFactStreams;   // the most streams an analysis may use
+    int nFactStreams = 1;                // streams the current plan uses
+    std::vector<int> grpStream, grpWaitOff, grpWait, grpLaunchOff;
     std::vector<Launch> launches;        // in execution order
     std::vector<TileTask> tasks;
     // substitution work split: per level, (front, first row/column) chunks of
@@ -90,6 +98,8 @@ struct CholPlan {
         double* vec = nullptr;
         size_t vecCap = 0;
         int* flags = nullptr;
+        cudaStream_t aux[kMaxFactStreams - 1] = {};   // factorization streams 1, 2, ..
+        cudaEvent_t fork = nullptr, join[kMaxFactStreams - 1] = {}, grpEnd[kMaxFactGroups] = {};
     } keep;
     // ---- device copies (views into keep) ----
     double* pool = nullptr;
@@ -147,6 +157,8 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
 // largest cluster per front in the substitutions (1..8; drops the captured
 // solve graph so that the next solve records the new launches)
 void chol_set_solve_cluster(CholPlan& P, int maxCluster);
+// the most streams the factorization of the next analysis may use (1..4)
+void chol_set_factor_streams(CholPlan& P, int streams);
 // tree levels whose pivot-part substitutions run as clusters, and the
 // largest cluster size among them (1 when none)
 int chol_solve_cluster_levels(const CholPlan& P, int* largest);
