@@ -155,9 +155,9 @@ int oc_linsys_set_solve_cluster(oc_linsys* ls, int maxCluster);
  * the largest cluster size among them (1 when none). */
 int oc_linsys_solve_clusters(oc_linsys* ls, int* levels, int* largest);
 /* No reference counterpart (a launch choice of the direct solver): the most
- * CUDA streams (1..4) the factorization's independent subtrees may run on,
+ * CUDA streams (1..8) the factorization's independent subtrees may run on,
  * from the next analysis (set_pattern) on.  The factor is the same bits for
- * every value.  Default 4. */
+ * every value.  Default 8. */
 int oc_linsys_set_factor_streams(oc_linsys* ls, int streams);
 /* Streams and subtree groups the current plan's factorization uses. */
 int oc_linsys_factor_streams(oc_linsys* ls, int* streams, int* groups);

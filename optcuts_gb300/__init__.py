@@ -622,7 +622,7 @@ class LinSysSolver:
         return a.value, b.value
 
     def set_factor_streams(self, streams):
-        """Most CUDA streams (1..4) for the factorization's independent
+        """Most CUDA streams (1..8) for the factorization's independent
         subtrees, from the next set_pattern on; the factor is the same bits
         for every value."""
         self.ctx.check(lib().oc_linsys_set_factor_streams(self.h, int(streams)), "set_factor_streams")

@@ -218,6 +218,17 @@ constexpr int kPanelRows = 8;
 // chain over the panel's columns)
 constexpr int kUpdSmall = 32;
 
+// The smallest factorization (flops) whose independent subtrees get streams
+// of their own.  The split saves time on every graph replay but doubles the
+// graph's launches, so capturing and instantiating it after a pattern change
+// costs more (~1 ms more at 199k triangles).  Measured per Newton step (eight
+// streams against one): 5k triangles, 3.8e7 flops, factorization 0.90 -> 0.83
+// ms, but a whole 5k outer loop with its 38 pattern changes 0.83 -> 0.89 s;
+// 41k torus, 1.2e9 flops, re-analysed every step, factorization 3.96 -> 3.80
+// ms and the step 16.0 -> 16.3 ms; 199k, 8.9e9 flops, pattern kept, 14.0 ->
+// 12.5 ms.
+constexpr double kStreamMinFlops = 4e9;
+
 } // namespace
 
 void chol_analyze(CholPlan& P, int nV, const int* rowPtr, const int* col, int leafSize,
@@ -440,7 +451,8 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
     // the chain, with every small subtree hanging off it, joins them.  Cuts
     // are made largest subtree first while streams are left; uncut subtrees
     // are leaf groups.  Groups are numbered in postorder, so every group
-    // comes after those it waits for.
+    // comes after those it waits for.  Factorizations below kStreamMinFlops
+    // stay on one stream (see there).
     std::vector<int> grp(nF, 0);
     {
         std::vector<double> fl(nF, 0.0);   // subtree flops (children come first)
@@ -480,7 +492,8 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
                 for (int r : leaves) {
                     const size_t k = split_of(r).size();
                     const double rf = r < 0 ? total : fl[r];
-                    if (k >= 2 && k <= 4 && streams + (int)k - 1 <= P.factStreams && rf > bestFl) {
+                    if (k >= 2 && k <= 4 && streams + (int)k - 1 <= P.factStreams && total >= kStreamMinFlops &&
+                        rf > bestFl) {
                         best = r;
                         bestFl = rf;
                     }

@@ -65,7 +65,7 @@ struct CholPlan {
     // g's launches launches[grpLaunchOff[g] .. grpLaunchOff[g+1]) run on
     // stream grpStream[g] (0 = the caller's stream), after the ends of groups
     // grpWait[grpWaitOff[g] .. grpWaitOff[g+1])
-    static constexpr int kMaxFactStreams = 4, kMaxFactGroups = 2 * kMaxFactStreams;
+    static constexpr int kMaxFactStreams = 8, kMaxFactGroups = 2 * kMaxFactStreams;
     int factStreams = kMaxFactStreams;   // the most streams an analysis may use
     int nFactStreams = 1;                // streams the current plan uses
     std::vector<int> grpStream, grpWaitOff, grpWait, grpLaunchOff;
@@ -157,7 +157,7 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
 // largest cluster per front in the substitutions (1..8; drops the captured
 // solve graph so that the next solve records the new launches)
 void chol_set_solve_cluster(CholPlan& P, int maxCluster);
-// the most streams the factorization of the next analysis may use (1..4)
+// the most streams the factorization of the next analysis may use (1..8)
 void chol_set_factor_streams(CholPlan& P, int streams);
 // tree levels whose pivot-part substitutions run as clusters, and the
 // largest cluster size among them (1 when none)

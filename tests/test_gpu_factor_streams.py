@@ -1,6 +1,7 @@
 """The direct solver's factorization with its independent subtrees on
 several CUDA streams (joined by events inside the captured graph) against
-one stream: the same factor bits, so the same solutions."""
+one stream: the same factor bits, so the same solutions.  Streams are used
+from 4 GFLOP per factorization on, so both cases are large enough."""
 import numpy as np
 import pytest
 
@@ -37,30 +38,35 @@ def _solve(state, streams, fixed, rhs_seed=4):
 
 
 def test_factor_streams_bit_identical(state):
-    runs = {s: _solve(state, s, [0]) for s in (1, 2, 4)}
+    runs = {s: _solve(state, s, [0]) for s in (1, 2, 4, 8)}
     assert runs[1][0].factor_streams() == (1, 1)
     s2, g2 = runs[2][0].factor_streams()
     s4, g4 = runs[4][0].factor_streams()
     assert s2 == 2 and g2 == 3, (s2, g2)
     assert 3 <= s4 <= 4 and s4 < g4 <= 2 * s4 - 1, (s4, g4)
-    for s in (2, 4):
+    s8, g8 = runs[8][0].factor_streams()
+    assert s4 <= s8 <= 8 and s8 < g8 <= 2 * s8 - 1, (s8, g8)
+    for s in (2, 4, 8):
         np.testing.assert_array_equal(runs[s][1], runs[1][1])
         np.testing.assert_array_equal(runs[s][2], runs[1][2])
-    ls, x, x2, b = runs[4]   # the solver holds the second (doubled) matrix
+    ls, x, x2, b = runs[8]   # the solver holds the second (doubled) matrix
     assert np.linalg.norm(ls.multiply(x2) - b) <= 1e-10 * np.linalg.norm(b)
     np.testing.assert_allclose(x2, 0.5 * x, rtol=1e-9, atol=1e-12)
     with pytest.raises(oc.OCError):
         ls.set_factor_streams(0)
     with pytest.raises(oc.OCError):
-        ls.set_factor_streams(5)
+        ls.set_factor_streams(9)
 
 
-def test_factor_streams_bit_identical_newton(state):
-    """Newton steps with the scaffold (the air mesh's vertices as the root
-    front above the dissected mesh, re-analysed as the air mesh is rebuilt)
-    take the same path on four streams as on one."""
+def test_factor_streams_bit_identical_newton():
+    """Newton steps with the scaffold (the air mesh as the root front above
+    the dissected mesh) at 199k triangles take the same path on eight streams
+    as on one."""
+    from optcuts_gb300 import init as I
+    from optcuts_gb300 import meshes as M
+    state = I.init_uv(*M.CONFIGS["ellipsoid_199k"]())
     runs = []
-    for s in (1, 4):
+    for s in (1, 8):
         m = oc.TriMesh(state.V_rest, state.UV, state.F, state.fixedVert)
         opt = oc.Optimizer(m, [0.001])
         opt.set_factor_streams(s)
@@ -72,7 +78,7 @@ def test_factor_streams_bit_identical_newton(state):
             opt.rebuildScaffold()
             E.append(opt.getLastEnergyVal())
         used = opt.factor_streams()[0]
-        assert (used == 1) if s == 1 else (used >= 2), (s, used)
+        assert (used == 1) if s == 1 else (used >= 2), (s, used, opt.solver_stats()["flops"])
         runs.append((np.array(E), m.V.copy()))
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
     np.testing.assert_array_equal(runs[0][1], runs[1][1])
