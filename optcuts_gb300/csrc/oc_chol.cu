@@ -722,15 +722,37 @@ __global__ void __launch_bounds__(256) k_extend(const TileTask* __restrict__ tas
     const TileTask t = tasks[blockIdx.x];
     const int ch = t.front, par = t.i;
     const int kc = fk[ch], mc = fm[ch], mp = fm[par];
-    const int u = mc - kc;
-    const double* C = pool + foff[ch];
-    double* Pm = pool + foff[par];
+    const int u = mc - kc, j1 = t.p;
+    const double* __restrict__ C = pool + foff[ch];   // the child's and the parent's
+    double* __restrict__ Pm = pool + foff[par];       // fronts do not overlap
     const int* rel = relIdx + relOff[ch];
-    for (int j = t.j; j < t.p; ++j) {
-        const int pj = rel[j];
-        const double* cc = C + (long long)(kc + j) * mc + kc;
-        double* pc = Pm + (long long)pj * mp;
-        for (int i = j + threadIdx.x; i < u; i += blockDim.x) pc[rel[i]] += cc[i];
+    // the block's columns j0 <= j < j1, rows j <= i < u, numbered column by
+    // column; each thread takes every 256th entry, four per round with all
+    // loads first (each parent entry is added to once: same sums in any order)
+    int j = t.j, off = threadIdx.x;
+    while (j < j1 && off >= u - j) off -= u - j, ++j;
+    while (j < j1) {
+        long long src[4], dst[4];
+        int n = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (j < j1) {
+                src[q] = (long long)(kc + j) * mc + kc + j + off;
+                dst[q] = (long long)rel[j] * mp + rel[j + off];
+                n = q + 1;
+                off += blockDim.x;
+                while (j < j1 && off >= u - j) off -= u - j, ++j;
+            }
+        double v[4], w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < n) {
+                v[q] = C[src[q]];
+                w[q] = Pm[dst[q]];
+            }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < n) Pm[dst[q]] = w[q] + v[q];
     }
 }
 
