@@ -173,6 +173,12 @@ int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, in
  * optimizer uses for a scaffold's full pattern) */
 int oc_chol_analyze_stats_xy(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
                              const double* xy, double* out8);
+/* No reference counterpart (a check of the direct solver's launch plan),
+ * host only: the same analysis with at most maxStreams (1..8) factorization
+ * streams; out3 = streams used, subtree groups, and 1 when every front's
+ * children finish before it under the plan's streams and event waits. */
+int oc_chol_analyze_groups(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
+                           int maxStreams, int* out3);
 /* Its vertex elimination order (nV entries), host only. */
 int oc_chol_analyze_order(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
                           int* vertexOrder);

@@ -91,6 +91,7 @@ _SIGS = {
     "oc_linsys_stats": [_vp, _d],
     "oc_chol_analyze_stats": [ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_int, _d],
     "oc_chol_analyze_stats_xy": [ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_int, _d, _d],
+    "oc_chol_analyze_groups": [ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i],
     "oc_linsys_set_pattern": [_vp, ctypes.c_int, _i, ctypes.c_int, _i, ctypes.c_int],
     "oc_linsys_update_a": [_vp, _i, _i, _d, ctypes.c_int],
     "oc_linsys_factorize": [_vp],
@@ -766,6 +767,20 @@ def chol_analyze_stats(nV, F, fixedVert=(0,), leafSize=16, xy=None):
     if rc != OC_OK:
         raise OCError(rc, "oc_chol_analyze_stats")
     return symbolic_stats_dict(out)
+
+
+def chol_analyze_groups(nV, F, fixedVert=(0,), leafSize=16, maxStreams=8):
+    """The direct solver's factorization streams for this pattern, host only:
+    (streams used, subtree groups, whether every front's children finish
+    before it under the plan's streams and waits)."""
+    F = _i4(F)
+    fx = _i4(np.asarray(fixedVert).reshape(-1))
+    out = np.zeros(3, np.int32)
+    rc = lib().oc_chol_analyze_groups(int(nV), _pi(F), len(F), _pi(fx), len(fx), int(leafSize), int(maxStreams),
+                                      _pi(out))
+    if rc != OC_OK:
+        raise OCError(rc, "oc_chol_analyze_groups")
+    return int(out[0]), int(out[1]), bool(out[2])
 
 
 def air_loop_mesh(pts, maxSteiner=12):

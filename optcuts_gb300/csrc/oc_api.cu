@@ -1642,6 +1642,30 @@ int oc_linsys_stats(oc_linsys* ls, double* out8)
     return OC_OK;
 }
 
+int oc_chol_analyze_groups(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize,
+                           int maxStreams, int* out3)
+{
+    if (nV <= 0 || nF < 0 || (nF && !F) || nFixed < 0 || (nFixed && !fixedVert) || !out3 || maxStreams < 1 ||
+        maxStreams > oc::CholPlan::kMaxFactStreams)
+        return OC_ERR_INVALID;
+    for (long long i = 0; i < 3LL * nF; ++i)
+        if (F[i] < 0 || F[i] >= nV) return OC_ERR_INVALID;
+    std::vector<unsigned char> mask(nV, 0);
+    for (int i = 0; i < nFixed; ++i) {
+        if (fixedVert[i] < 0 || fixedVert[i] >= nV) return OC_ERR_INVALID;
+        mask[fixedVert[i]] = 1;
+    }
+    std::vector<int> rowPtr, col, diagSlot, cPtr, cIdx;
+    build_pattern(nV, F, nF, mask, rowPtr, col, diagSlot, cPtr, cIdx);
+    oc::CholPlan P;
+    oc::chol_set_factor_streams(P, maxStreams);
+    oc::chol_analyze(P, nV, rowPtr.data(), col.data(), leafSize > 0 ? leafSize : 16);
+    out3[0] = P.nFactStreams;
+    out3[1] = static_cast<int>(P.grpStream.size());
+    out3[2] = oc::chol_groups_ordered(P) ? 1 : 0;
+    return P.valid ? OC_OK : OC_ERR_INVALID;
+}
+
 int oc_chol_analyze_stats(int nV, const int* F, int nF, const int* fixedVert, int nFixed, int leafSize, double* out8)
 {
     return oc_chol_analyze_stats_xy(nV, F, nF, fixedVert, nFixed, leafSize, nullptr, out8);

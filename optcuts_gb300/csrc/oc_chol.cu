@@ -549,6 +549,7 @@ void chol_analyze_nodes(CholPlan& P, int nV, const int* rowPtr, const int* col, 
             P.nFactStreams = 1;
         }
     }
+    P.frontGroup = grp;
     const int nGrp = static_cast<int>(P.grpStream.size());
     std::vector<std::vector<int>> glf(static_cast<size_t>(nGrp) * P.nLevels);
     for (int l = 0; l < P.nLevels; ++l)
@@ -2116,6 +2117,41 @@ int chol_solve_cluster_levels(const CholPlan& P, int* largest)
 void chol_set_factor_streams(CholPlan& P, int streams)
 {
     P.factStreams = std::max(1, std::min(streams, (int)CholPlan::kMaxFactStreams));
+}
+
+bool chol_groups_ordered(const CholPlan& P)
+{
+    const int nG = static_cast<int>(P.grpStream.size());
+    if (nG < 1 || nG > CholPlan::kMaxFactGroups || (int)P.grpWaitOff.size() != nG + 1 ||
+        (int)P.grpLaunchOff.size() != nG + 1 || P.grpLaunchOff[nG] != (int)P.launches.size() ||
+        (int)P.frontGroup.size() != P.nFronts)
+        return false;
+    // hb[a][b]: group a's launches finish before group b's start
+    std::vector<std::vector<char>> hb(nG, std::vector<char>(nG, 0));
+    for (int g = 0; g < nG; ++g) {
+        if (P.grpStream[g] < 0 || P.grpStream[g] >= P.nFactStreams) return false;
+        if (P.grpLaunchOff[g] > P.grpLaunchOff[g + 1]) return false;
+        for (int h = 0; h < g; ++h)
+            if (P.grpStream[h] == P.grpStream[g]) hb[h][g] = 1;
+        for (int i = P.grpWaitOff[g]; i < P.grpWaitOff[g + 1]; ++i) {
+            if (P.grpWait[i] < 0 || P.grpWait[i] >= g) return false;   // waits only on earlier groups
+            hb[P.grpWait[i]][g] = 1;
+        }
+    }
+    for (int k = 0; k < nG; ++k)
+        for (int a = 0; a < nG; ++a)
+            if (hb[a][k])
+                for (int b = 0; b < nG; ++b)
+                    if (hb[k][b]) hb[a][b] = 1;
+    for (int f = 0; f < P.nFronts; ++f) {
+        const int gf = P.frontGroup[f];
+        if (gf < 0 || gf >= nG) return false;
+        for (int i = P.childOff[f]; i < P.childOff[f + 1]; ++i) {
+            const int c = P.childList[i], gc = P.frontGroup[c];
+            if (gc == gf ? P.flevel[c] >= P.flevel[f] : !hb[gc][gf]) return false;
+        }
+    }
+    return true;
 }
 
 void chol_set_solve_cluster(CholPlan& P, int maxCluster)

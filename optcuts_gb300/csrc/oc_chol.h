@@ -69,6 +69,7 @@ struct CholPlan {
     int factStreams = kMaxFactStreams;   // the most streams an analysis may use
     int nFactStreams = 1;                // streams the current plan uses
     std::vector<int> grpStream, grpWaitOff, grpWait, grpLaunchOff;
+    std::vector<int> frontGroup;         // per front, its group
     std::vector<Launch> launches;        // in execution order
     std::vector<TileTask> tasks;
     // substitution work split: per level, (front, first row/column) chunks of
@@ -159,6 +160,10 @@ int chol_solve(CholPlan& P, const double2* rhs, double2* x, double sign, cudaStr
 void chol_set_solve_cluster(CholPlan& P, int maxCluster);
 // the most streams the factorization of the next analysis may use (1..8)
 void chol_set_factor_streams(CholPlan& P, int streams);
+// true when every front's children finish before it under the plan's
+// streams and waits (same group at a lower level, an earlier group on the
+// same stream, or a chain of waits), and the group tables are consistent
+bool chol_groups_ordered(const CholPlan& P);
 // tree levels whose pivot-part substitutions run as clusters, and the
 // largest cluster size among them (1 when none)
 int chol_solve_cluster_levels(const CholPlan& P, int* largest);
