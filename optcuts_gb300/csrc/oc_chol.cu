@@ -15,7 +15,9 @@
 //    tree level at a time; within a level every front is factorised by the
 //    same batched tile kernels (32 x 32 FP64 tiles: LDL^T of the diagonal
 //    tile, triangular solve of the panel, trailing update), so one launch
-//    serves all fronts of a level;
+//    serves all fronts of a level; in large factorizations the independent
+//    subtrees below the tree's top chain run this on streams of their own
+//    (events join them, all inside one captured graph);
 //  * solve: forward and backward substitution front by front, level by
 //    level, with the children's update vectors extend-added in a fixed
 //    order (deterministic, no atomics).
